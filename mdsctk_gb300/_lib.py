@@ -1,0 +1,87 @@
+"""ctypes binding of libmdsgpu (the C ABI declared in include/mdsgpu.h).
+
+The library is loaded from ``mdsctk_gb300/lib/libmdsgpu.so`` (built in-tree by
+``mdsctk_gb300/build.py``). There is no fallback: if the library is missing
+or fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmdsgpu.so")
+
+MDS_OK = 0
+MDS_ERR_ARG = -1
+MDS_ERR_CUDA = -2
+MDS_ERR_NOMEM = -3
+MDS_ERR_UNSUPPORTED = -4
+MDS_ERR_TIMEOUT = -5
+MDS_ERR_INTERNAL = -6
+
+MDS_NOFIT = 0x1
+MDS_FULL = 0x2
+MDS_DEVICE_IO = 0x4
+MDS_CORRELATION = 0x8
+MDS_PREC_FP32 = 0x00
+MDS_PREC_BF16X3 = 0x10
+MDS_PREC_FP16X3 = 0x20
+
+PRECISIONS = {"fp32": MDS_PREC_FP32, "bf16x3": MDS_PREC_BF16X3, "fp16x3": MDS_PREC_FP16X3}
+
+
+class MdsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"mdsgpu error {code}: {msg}")
+        self.code = code
+
+
+class KnnStats(ctypes.Structure):
+    _fields_ = [("prep_ms", ctypes.c_double), ("screen_ms", ctypes.c_double),
+                ("recheck_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("pairs", ctypes.c_longlong), ("kprime", ctypes.c_int),
+                ("rows_flagged", ctypes.c_int), ("passes", ctypes.c_int),
+                ("screen_launches", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+# Exported symbols and their signatures (kept in step with include/mdsgpu.h).
+_vp, _i, _u, _sz, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint, ctypes.c_size_t, ctypes.c_double
+_ip = ctypes.POINTER(ctypes.c_int)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+SIGNATURES = {
+    "mds_version": ([], ctypes.c_char_p),
+    "mds_create": ([_i, _sz, ctypes.POINTER(_vp)], _i),
+    "mds_destroy": ([_vp], _i),
+    "mds_last_error": ([_vp], ctypes.c_char_p),
+    "mds_get_knn_stats": ([_vp, ctypes.POINTER(KnnStats)], _i),
+    "mds_knn_rms": ([_vp, _vp, _i, _vp, _i, _i, _vp, _i, _u, _vp, _vp, _ip], _i),
+    "mds_knn_data": ([_vp, _vp, _i, _vp, _i, _i, _i, _u, _vp, _vp, _ip], _i),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libmdsgpu (raises if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libmdsgpu is not built ({LIB_PATH} missing); run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def check(ctx, code: int):
+    if code != MDS_OK:
+        msg = lib().mds_last_error(ctx)
+        raise MdsError(code, msg.decode() if msg else "")

@@ -1,0 +1,55 @@
+// ctx.cu -- context lifecycle, error reporting and version of libmdsgpu.
+#include "mds_common.cuh"
+
+int mds_fail(mds_ctx* ctx, int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->last_error = buf;
+  return code;
+}
+
+extern "C" const char* mds_version(void) { return "mdsgpu 0.1 (sm_103a)"; }
+
+extern "C" int mds_create(int device, size_t hbm_budget, mds_ctx** out) {
+  if (!out) return MDS_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MDS_ERR_CUDA;
+  if (device < 0 || device >= ndev) return MDS_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MDS_ERR_CUDA;
+  mds_ctx* c = new mds_ctx();
+  c->device = device;
+  c->hbm_budget = hbm_budget;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return MDS_ERR_CUDA;
+  }
+  for (auto& e : c->ev) cudaEventCreate(&e);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return MDS_OK;
+}
+
+extern "C" int mds_destroy(mds_ctx* ctx) {
+  if (!ctx) return MDS_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MDS_OK;
+}
+
+extern "C" const char* mds_last_error(const mds_ctx* ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+extern "C" int mds_get_knn_stats(const mds_ctx* ctx, mds_knn_stats* out) {
+  if (!ctx || !out) return MDS_ERR_ARG;
+  *out = ctx->stats;
+  return MDS_OK;
+}

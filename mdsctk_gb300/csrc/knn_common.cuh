@@ -1,0 +1,79 @@
+// knn_common.cuh -- plan, sorting helpers and cross-file declarations of the
+// kNN pipelines (knn_rms.cu, knn_rms_tc.cu, knn_data.cu, knn_api.cu).
+#pragma once
+
+#include "mds_common.cuh"
+
+struct KnnRmsPlan {
+  int nref = 0, nfit = 0, natoms = 0;
+  int Ap = 0;      // natoms rounded up to 64 (zero-padded atoms)
+  int k = 0;       // clamped k
+  int kprime = 0;  // candidates kept per row by the screen
+  int nofit = 0, full = 0;
+  unsigned prec = MDS_PREC_FP32;
+  float guard_fp32 = 0.f;  // lower-bound margin per unit of |a_i|^2+|a_j|^2
+  float guard_tc = 0.f;
+};
+
+// Split hi/lo tensor-core operands of one frame set (knn_rms_tc.cu).
+struct TcOperands {
+  DevBuf buf;      // [ntiles][K][rows] packed tiles
+  int n = 0;       // frames
+  int rows = 0;    // padded operand rows
+  int K = 0;       // padded reduction length per split part
+};
+
+__device__ __forceinline__ void warp_bitonic_sort(uint64_t* a, int n, int P2, int lane) {
+  for (int x = n + lane; x < P2; x += 32) a[x] = MDS_KEY_INF;
+  __syncwarp();
+  for (int k = 2; k <= P2; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < P2; i += 32) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          uint64_t x = a[i], y = a[ixj];
+          bool up = (i & k) == 0;
+          if ((x > y) == up) {
+            a[i] = y;
+            a[ixj] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+}
+
+// All threads of the block; P2 a power of two; a[] fully initialised.
+__device__ __forceinline__ void block_bitonic_sort(uint64_t* a, int P2) {
+  for (int k = 2; k <= P2; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          uint64_t x = a[i], y = a[ixj];
+          bool up = (i & k) == 0;
+          if ((x > y) == up) {
+            a[i] = y;
+            a[ixj] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+}
+
+__host__ __device__ static inline int next_pow2(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float* draw_fit,
+                const float* hmass, double* dout_d, int* dout_i);
+
+// tensor-core screen (knn_rms_tc.cu)
+int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op);
+int tc_choose_nseg(mds_ctx* ctx, const KnnRmsPlan& pl, int nfit);
+int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
+                     const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
+                     int* cand_n);

@@ -1,0 +1,809 @@
+// knn_rms.cu -- all-pairs minimum-RMSD k-nearest neighbours on sm_103a.
+//
+// Replaces the compute core of knn_rms.cpp (distance() :38-41, the centring
+// :186-206 and the OpenMP row loop with permutation::sort(k+1) :213-293).
+//
+// Pipeline (all on ctx->stream):
+//  1. k_center      reset_x centring (knn_rms.cpp:189,199) of every frame,
+//                   scaled by sqrt(w/M) so that every sum below is per unit
+//                   mass; layout [frame][xyz][Ap] float (atom-major, Ap =
+//                   natoms rounded up to 64, zero padded).
+//  2. k_prealign    superpose every frame once onto a template mu (first
+//                   reference frame in its principal axes), store deviations
+//                   a = R y - mu and the per-frame screen record.
+//  3. screen        all pairs: deviation Gram + shifted QCP lower bound of
+//                   RMSD^2, fused per-row top-K' (never an N x N matrix).
+//                   FP32 CUDA cores (k_screen_fp32) or tcgen05 split BF16
+//                   (knn_rms_tc.cu).
+//  4. k_recheck     merge the per-segment candidate lists, recompute every
+//                   candidate exactly the way the reference does (optimal
+//                   rotation, then the RMSD of the rotated coordinates),
+//                   select k+1, drop position 0, verify the guard.
+//  5. rows whose guard failed are screened again with 4x the candidates.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "knn_common.cuh"
+#include "qcp.cuh"
+
+// ---------------------------------------------------------------------------
+// 1. centring
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum_d(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0;
+  int nw = blockDim.x >> 5;
+  for (int i = 0; i < nw; ++i) s += red[i];
+  return s;
+}
+
+// One block per frame. raw: [n][natoms][3]; out: [n][3][Ap]; E: |y|^2 per
+// unit mass (double). tm: float sum of masses in file order (reset_x's tm).
+__global__ void k_center(const float* __restrict__ raw, int n, int natoms, int Ap,
+                         const float* __restrict__ mass, const float* __restrict__ swn, float tm,
+                         float* __restrict__ out, double* __restrict__ E) {
+  __shared__ double red[32];
+  int f = blockIdx.x;
+  if (f >= n) return;
+  const float* x = raw + (int64_t)f * natoms * 3;
+  double s[3] = {0, 0, 0};
+  for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
+    float mm = mass[a];
+    for (int c = 0; c < 3; ++c) s[c] += (double)(mm * x[3 * a + c]);
+  }
+  double com[3];
+  for (int c = 0; c < 3; ++c) com[c] = block_sum_d(s[c], red) / (double)tm;
+  double e = 0;
+  float* o = out + (int64_t)f * 3 * Ap;
+  for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      float v = 0.0f;
+      if (a < natoms) {
+        float y = (float)((double)x[3 * a + c] - com[c]);  // reset_x: double shift, float store
+        v = y * swn[a];
+        e += (double)v * (double)v;
+      }
+      o[c * Ap + a] = v;
+    }
+  }
+  e = block_sum_d(e, red);
+  if (threadIdx.x == 0) E[f] = e;
+}
+
+// ---------------------------------------------------------------------------
+// 2. superposition onto the template
+// ---------------------------------------------------------------------------
+// mu: [3][Ap] double (template, principal axes). M0: sum mu mu^T (9 doubles).
+// dev: [n][3][Ap] float deviations a = R y - mu (FP32 screen operand).
+// rec: [n][MDS_REC] screen record.
+__global__ void k_prealign(const float* __restrict__ Y, const double* __restrict__ E, int n,
+                           int natoms, int Ap, const double* __restrict__ mu,
+                           const double* __restrict__ M0, int nofit, float* __restrict__ dev,
+                           float* __restrict__ rec) {
+  __shared__ double red[32];
+  __shared__ double Rsh[9];
+  int f = blockIdx.x;
+  if (f >= n) return;
+  const float* y = Y + (int64_t)f * 3 * Ap;
+  if (!nofit) {
+    double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
+      double yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
+      double mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) s[3 * c + d] += yc[c] * mc[d];
+    }
+    double S[9];
+    for (int i = 0; i < 9; ++i) S[i] = block_sum_d(s[i], red);
+    if (threadIdx.x == 0) {
+      double emu = M0[0] + M0[4] + M0[8];
+      double R[9];
+      qcp_rotation_fp64(S, 0.5 * (E[f] + emu), R);
+      for (int i = 0; i < 9; ++i) Rsh[i] = R[i];
+    }
+  } else if (threadIdx.x == 0) {
+    for (int i = 0; i < 9; ++i) Rsh[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  double R[9];
+  for (int i = 0; i < 9; ++i) R[i] = Rsh[i];
+  double ea = 0, u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float* o = dev + (int64_t)f * 3 * Ap;
+  for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
+    if (a < natoms) {
+      double yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
+      double mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
+      float av[3];
+      for (int c = 0; c < 3; ++c) {
+        double ry = R[3 * c] * yc[0] + R[3 * c + 1] * yc[1] + R[3 * c + 2] * yc[2];
+        av[c] = (float)(ry - mc[c]);
+        o[c * Ap + a] = av[c];
+      }
+      for (int c = 0; c < 3; ++c) {
+        ea += (double)av[c] * av[c];
+        for (int d = 0; d < 3; ++d) u[3 * c + d] += (double)av[c] * mc[d];
+      }
+    } else {
+      for (int c = 0; c < 3; ++c) o[c * Ap + a] = 0.0f;
+    }
+  }
+  ea = block_sum_d(ea, red);
+  double U[9];
+  for (int i = 0; i < 9; ++i) U[i] = block_sum_d(u[i], red);
+  if (threadIdx.x == 0) {
+    float* r = rec + (int64_t)f * MDS_REC;
+    double sxx = U[0], syy = U[4], szz = U[8];
+    double sxy = 0.5 * (U[1] + U[3]), sxz = 0.5 * (U[2] + U[6]), syz = 0.5 * (U[5] + U[7]);
+    r[0] = (float)(M0[0] + sxx);
+    r[1] = (float)(M0[4] + syy);
+    r[2] = (float)(M0[8] + szz);
+    r[3] = (float)(0.5 * (M0[1] + M0[3]) + sxy);
+    r[4] = (float)(0.5 * (M0[2] + M0[6]) + sxz);
+    r[5] = (float)(0.5 * (M0[5] + M0[7]) + syz);
+    r[6] = (float)sxx; r[7] = (float)syy; r[8] = (float)szz;
+    r[9] = (float)sxy; r[10] = (float)sxz; r[11] = (float)syz;
+    r[12] = (float)(U[5] - U[7]);
+    r[13] = (float)(U[6] - U[2]);
+    r[14] = (float)(U[1] - U[3]);
+    r[15] = (float)ea;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3. FP32 CUDA-core screen: tile of 32 fit x 64 ref frames per step, each
+//    thread owns 2 x 4 pairs (72 accumulators), atoms staged through shared
+//    memory in chunks of 32 with cp.async double buffering.
+// ---------------------------------------------------------------------------
+#define SC_TM 32
+#define SC_TN 64
+#define SC_KC 32
+#define SC_FS 98  // floats per frame per stage: 3*32 + 2 (bank spread)
+#define SC_THREADS 256
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool valid) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  int sz = valid ? 8 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+__global__ void __launch_bounds__(SC_THREADS, 1)
+k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
+              const float* __restrict__ recf, const float* __restrict__ recr, int nrows,
+              const int* __restrict__ rowlist, int Nr, int Ap, int nofit, float guard, int Kp,
+              int nseg, uint64_t* __restrict__ cand, int* __restrict__ cand_n) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* sfit = reinterpret_cast<float*>(smem_raw);                 // [2][32*98]
+  float* sref = sfit + 2 * SC_TM * SC_FS;                           // [2][64*98]
+  float* scol = sref + 2 * SC_TN * SC_FS;                           // [64][16]
+  int* scnt = reinterpret_cast<int*>(scol + SC_TN * MDS_REC);       // [32]
+  float* sthr = reinterpret_cast<float*>(scnt + SC_TM);             // [32]
+  uint64_t* pool = reinterpret_cast<uint64_t*>(sthr + SC_TM);       // [32][P2]
+  // a row's pool holds its K' best plus one tile of new entries; its stride
+  // is the power of two the sort works on
+  const int P2 = next_pow2(Kp + SC_TN);
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int rt = blockIdx.x / nseg, seg = blockIdx.x % nseg;
+  const int row0 = rt * SC_TM;
+  // column segment [c0, c1) in whole tiles
+  const int ntiles = (Nr + SC_TN - 1) / SC_TN;
+  const int t0 = (int)((int64_t)ntiles * seg / nseg), t1 = (int)((int64_t)ntiles * (seg + 1) / nseg);
+
+  int grow[2];
+  float rrec[2][MDS_REC];
+  for (int p = 0; p < 2; ++p) {
+    int lr = row0 + ty + 16 * p;
+    grow[p] = (lr < nrows) ? (rowlist ? rowlist[lr] : lr) : -1;
+    for (int i = 0; i < MDS_REC; ++i) rrec[p][i] = (grow[p] >= 0) ? recf[(int64_t)grow[p] * MDS_REC + i] : 0.f;
+  }
+  if (tid < SC_TM) {
+    scnt[tid] = 0;
+    sthr[tid] = __int_as_float(0x7f800000);
+  }
+  const int nchunks = Ap / SC_KC;
+
+  auto load_chunk = [&](int stage, int tile, int kc) {
+    float* df = sfit + stage * SC_TM * SC_FS;
+    float* dr = sref + stage * SC_TN * SC_FS;
+    // fit: 32 frames x 3 coords x 16 pairs of floats
+    for (int e = tid; e < SC_TM * 3 * 16; e += SC_THREADS) {
+      int fr = e / 48, rem = e % 48, c = rem / 16, h = rem % 16;
+      int lr = row0 + fr;
+      int g = (lr < nrows) ? (rowlist ? rowlist[lr] : lr) : -1;
+      const float* src = Af + ((int64_t)(g < 0 ? 0 : g) * 3 + c) * Ap + kc * SC_KC + 2 * h;
+      cp_async8(df + fr * SC_FS + c * SC_KC + 2 * h, src, g >= 0);
+    }
+    for (int e = tid; e < SC_TN * 3 * 16; e += SC_THREADS) {
+      int fr = e / 48, rem = e % 48, c = rem / 16, h = rem % 16;
+      int j = tile * SC_TN + fr;
+      const float* src = Ar + ((int64_t)(j < Nr ? j : 0) * 3 + c) * Ap + kc * SC_KC + 2 * h;
+      cp_async8(dr + fr * SC_FS + c * SC_KC + 2 * h, src, j < Nr);
+    }
+  };
+
+  for (int tile = t0; tile < t1; ++tile) {
+    // column records of this tile
+    __syncthreads();
+    for (int e = tid; e < SC_TN * MDS_REC; e += SC_THREADS) {
+      int fr = e / MDS_REC, i = e % MDS_REC;
+      int j = tile * SC_TN + fr;
+      scol[e] = (j < Nr) ? recr[(int64_t)j * MDS_REC + i] : 0.f;
+    }
+    float acc[2][4][9];
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int i = 0; i < 9; ++i) acc[p][q][i] = 0.f;
+
+    load_chunk(0, tile, 0);
+    cp_async_commit();
+    for (int kc = 0; kc < nchunks; ++kc) {
+      if (kc + 1 < nchunks) {
+        load_chunk((kc + 1) & 1, tile, kc + 1);
+        cp_async_commit();
+        cp_async_wait1();
+      } else {
+        cp_async_wait0();
+      }
+      __syncthreads();
+      const float* df = sfit + (kc & 1) * SC_TM * SC_FS;
+      const float* dr = sref + (kc & 1) * SC_TN * SC_FS;
+#pragma unroll 2
+      for (int a = 0; a < SC_KC; a += 2) {
+        float2 fv[2][3], rv[4][3];
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            fv[p][c] = *reinterpret_cast<const float2*>(df + (ty + 16 * p) * SC_FS + c * SC_KC + a);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            rv[q][c] = *reinterpret_cast<const float2*>(dr + (tx + 16 * q) * SC_FS + c * SC_KC + a);
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+                acc[p][q][3 * c + d] = fmaf(fv[p][c].x, rv[q][d].x, acc[p][q][3 * c + d]);
+                acc[p][q][3 * c + d] = fmaf(fv[p][c].y, rv[q][d].y, acc[p][q][3 * c + d]);
+              }
+      }
+      __syncthreads();
+    }
+    // epilogue: lower bounds and top-K' insertion
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      if (grow[p] < 0) continue;
+      int lr = ty + 16 * p;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        int j = tile * SC_TN + tx + 16 * q;
+        if (j >= Nr) continue;
+        const float* cr = scol + (tx + 16 * q) * MDS_REC;
+        float s = screen_shifted_f32(acc[p][q], rrec[p], cr, nofit != 0);
+        s = fmaxf(s - guard * (rrec[p][15] + cr[15]), 0.0f);
+        if (s < sthr[lr]) {
+          int pos = atomicAdd(&scnt[lr], 1);
+          pool[lr * P2 + pos] = mds_pack_key(s, j);
+        }
+      }
+    }
+    __syncthreads();
+    // compaction of rows whose pool exceeds K'
+    for (int r = warp; r < SC_TM; r += SC_THREADS / 32) {
+      int n = scnt[r];
+      if (n <= Kp) continue;
+      warp_bitonic_sort(pool + r * P2, n, P2, lane);
+      if (lane == 0) {
+        scnt[r] = Kp;
+        sthr[r] = mds_key_value(pool[r * P2 + Kp - 1]);
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // final: sort each row's pool and write it out
+  for (int r = warp; r < SC_TM; r += SC_THREADS / 32) {
+    int lr = row0 + r;
+    if (lr >= nrows) continue;
+    int n = min(scnt[r], Kp);
+    warp_bitonic_sort(pool + r * P2, scnt[r], P2, lane);
+    uint64_t* dst = cand + ((int64_t)lr * nseg + seg) * Kp;
+    for (int x = lane; x < n; x += 32) dst[x] = pool[r * P2 + x];
+    if (lane == 0) cand_n[(int64_t)lr * nseg + seg] = n;
+  }
+}
+
+size_t screen_fp32_smem(int Kp) {
+  return sizeof(float) * (2 * SC_TM * SC_FS + 2 * SC_TN * SC_FS + SC_TN * MDS_REC) +
+         sizeof(int) * SC_TM + sizeof(float) * SC_TM + sizeof(uint64_t) * SC_TM * next_pow2(Kp + SC_TN);
+}
+
+int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar,
+                       const float* recf, const float* recr, int nrows, const int* rowlist, int Kp,
+                       int nseg, uint64_t* cand, int* cand_n) {
+  size_t smem = screen_fp32_smem(Kp);
+  MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int nrt = (nrows + SC_TM - 1) / SC_TM;
+  k_screen_fp32<<<nrt * nseg, SC_THREADS, smem, ctx->stream>>>(
+      Af, Ar, recf, recr, nrows, rowlist, pl.nref, pl.Ap, pl.nofit, pl.guard_fp32, Kp, nseg, cand, cand_n);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// 4. merge + exact recheck + selection + output
+// ---------------------------------------------------------------------------
+#define RC_THREADS 256
+#define RC_CHUNK 128
+
+// Exact RMSD (nm) of fit frame (in shared memory) vs reference frame j for a
+// chunk of candidates: covariance per warp, FP64 rotation per thread, then
+// the RMSD of the rotated fit frame against the reference frame.
+__device__ void recheck_chunk(const float* __restrict__ sfit, double Ef, const float* __restrict__ Yr,
+                              const double* __restrict__ Er, int Ap, int natoms, const int* cj, int nc,
+                              bool nofit, float* sS, float* sR, float* sd) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (!nofit) {
+    for (int c = warp; c < nc; c += nw) {
+      const float* y = Yr + (int64_t)cj[c] * 3 * Ap;
+      float s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int a = lane; a < natoms; a += 32) {
+        float x0 = sfit[a], x1 = sfit[Ap + a], x2 = sfit[2 * Ap + a];
+        float y0 = __ldg(y + a), y1 = __ldg(y + Ap + a), y2 = __ldg(y + 2 * Ap + a);
+        s[0] = fmaf(x0, y0, s[0]); s[1] = fmaf(x0, y1, s[1]); s[2] = fmaf(x0, y2, s[2]);
+        s[3] = fmaf(x1, y0, s[3]); s[4] = fmaf(x1, y1, s[4]); s[5] = fmaf(x1, y2, s[5]);
+        s[6] = fmaf(x2, y0, s[6]); s[7] = fmaf(x2, y1, s[7]); s[8] = fmaf(x2, y2, s[8]);
+      }
+      for (int i = 0; i < 9; ++i) {
+        float v = s[i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sS[c * 9 + i] = v;
+      }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+      double S[9], R[9];
+      for (int i = 0; i < 9; ++i) S[i] = sS[c * 9 + i];
+      qcp_rotation_fp64(S, 0.5 * (Ef + Er[cj[c]]), R);
+      for (int i = 0; i < 9; ++i) sR[c * 9 + i] = (float)R[i];
+    }
+    __syncthreads();
+  }
+  for (int c = warp; c < nc; c += nw) {
+    const float* y = Yr + (int64_t)cj[c] * 3 * Ap;
+    float R[9];
+    for (int i = 0; i < 9; ++i) R[i] = nofit ? ((i % 4 == 0) ? 1.f : 0.f) : sR[c * 9 + i];
+    float acc = 0.f;
+    for (int a = lane; a < natoms; a += 32) {
+      float x0 = sfit[a], x1 = sfit[Ap + a], x2 = sfit[2 * Ap + a];
+      float y0 = __ldg(y + a), y1 = __ldg(y + Ap + a), y2 = __ldg(y + 2 * Ap + a);
+      float d0 = fmaf(R[0], x0, fmaf(R[1], x1, fmaf(R[2], x2, -y0)));
+      float d1 = fmaf(R[3], x0, fmaf(R[4], x1, fmaf(R[5], x2, -y1)));
+      float d2 = fmaf(R[6], x0, fmaf(R[7], x1, fmaf(R[8], x2, -y2)));
+      acc = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, acc)));
+    }
+    double v = acc;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sd[c] = (float)sqrt(v);
+  }
+  __syncthreads();
+}
+
+// One block per fit row (rows[b] or b). mode 0: merge nseg candidate lists of
+// K' keys, recheck, select k+1. mode 1: every reference is a candidate
+// (exact row). mode 2 (full matrix): write every exact distance in reference
+// order. Output: out_d/out_i rows of width `width` at row index grow.
+__global__ void __launch_bounds__(RC_THREADS)
+k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const float* __restrict__ Yr,
+          const double* __restrict__ Er, int nrows, const int* __restrict__ rowlist, int Nr, int Ap,
+          int natoms, int nofit, int mode, const uint64_t* __restrict__ cand,
+          const int* __restrict__ cand_n, int nseg, int Kp, int k, double* __restrict__ out_d,
+          int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* sfit = reinterpret_cast<float*>(smem_raw);               // [3*Ap]
+  float* sS = sfit + 3 * Ap;                                      // [CHUNK*9]
+  float* sR = sS + RC_CHUNK * 9;                                  // [CHUNK*9]
+  float* sd = sR + RC_CHUNK * 9;                                  // [CHUNK]
+  int* cj = reinterpret_cast<int*>(sd + RC_CHUNK);                // [CHUNK]
+  uint64_t* keys = reinterpret_cast<uint64_t*>(cj + RC_CHUNK);    // merge buffer / top list
+  __shared__ int s_total;
+
+  int lr = blockIdx.x;
+  if (lr >= nrows) return;
+  int grow = rowlist ? rowlist[lr] : lr;
+  const float* yf = Yf + (int64_t)grow * 3 * Ap;
+  for (int e = threadIdx.x; e < 3 * Ap; e += blockDim.x) sfit[e] = yf[e];
+  const double ef = Ef[grow];
+  const int k1 = k + 1;
+
+  if (mode == 2) {
+    __syncthreads();
+    for (int base = 0; base < Nr; base += RC_CHUNK) {
+      int nc = min(RC_CHUNK, Nr - base);
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) cj[c] = base + c;
+      __syncthreads();
+      recheck_chunk(sfit, ef, Yr, Er, Ap, natoms, cj, nc, nofit, sS, sR, sd);
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        out_d[(int64_t)grow * Nr + base + c] = (double)sd[c] * 10.0;
+        out_i[(int64_t)grow * Nr + base + c] = base + c;
+      }
+      __syncthreads();
+    }
+    return;
+  }
+
+  // Candidate list in keys[0..total): merged and trimmed to K' (mode 0) or
+  // implicit 0..Nr-1 (mode 1).
+  int total;
+  float tau;
+  if (mode == 0) {
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int s = 0; s < nseg; ++s) t += cand_n[(int64_t)lr * nseg + s];
+      s_total = t;
+    }
+    __syncthreads();
+    int t = s_total;
+    int P2 = 1;
+    while (P2 < t) P2 <<= 1;
+    // gather
+    int off = 0;
+    for (int s = 0; s < nseg; ++s) {
+      int ns = cand_n[(int64_t)lr * nseg + s];
+      const uint64_t* src = cand + ((int64_t)lr * nseg + s) * Kp;
+      for (int x = threadIdx.x; x < ns; x += blockDim.x) keys[off + x] = src[x];
+      off += ns;
+    }
+    for (int x = t + threadIdx.x; x < P2; x += blockDim.x) keys[x] = MDS_KEY_INF;
+    __syncthreads();
+    block_bitonic_sort(keys, P2);
+    total = min(t, Kp);
+    tau = (t >= Kp) ? mds_key_value(keys[Kp - 1]) : __int_as_float(0x7f800000);
+  } else {
+    total = Nr;
+    tau = __int_as_float(0x7f800000);
+  }
+  // top list of the k+1 best exact (value, index) keys, after the candidate
+  // list region: candidate list needs Kp (mode 0) entries, top list 2*CHUNK+k1.
+  uint64_t* top = keys + (mode == 0 ? max(Kp, 1) : 0);
+  int TP2 = 1;
+  while (TP2 < k1 + RC_CHUNK) TP2 <<= 1;
+  for (int x = threadIdx.x; x < TP2; x += blockDim.x) top[x] = MDS_KEY_INF;
+  __syncthreads();
+  for (int base = 0; base < total; base += RC_CHUNK) {
+    int nc = min(RC_CHUNK, total - base);
+    for (int c = threadIdx.x; c < nc; c += blockDim.x)
+      cj[c] = (mode == 0) ? mds_key_index(keys[base + c]) : base + c;
+    __syncthreads();
+    recheck_chunk(sfit, ef, Yr, Er, Ap, natoms, cj, nc, nofit, sS, sR, sd);
+    // place the chunk after the current k1 best and re-sort
+    for (int c = threadIdx.x; c < RC_CHUNK; c += blockDim.x)
+      top[k1 + c] = (c < nc) ? mds_pack_key(sd[c], cj[c]) : MDS_KEY_INF;
+    for (int x = k1 + RC_CHUNK + threadIdx.x; x < TP2; x += blockDim.x) top[x] = MDS_KEY_INF;
+    __syncthreads();
+    block_bitonic_sort(top, TP2);
+  }
+  // guard: the (k+1)-th exact RMSD^2 must not exceed the smallest lower bound
+  // of every excluded pair.
+  if (threadIdx.x == 0) {
+    double dk = (double)mds_key_value(top[k1 - 1]);
+    if (mode == 0 && !(dk * dk <= (double)tau)) {
+      int pos = atomicAdd(nflag, 1);
+      flagged[pos] = grow;
+    }
+  }
+  for (int x = threadIdx.x; x < k; x += blockDim.x) {
+    uint64_t key = top[x + 1];
+    out_d[(int64_t)grow * k + x] = (double)mds_key_value(key) * 10.0;
+    out_i[(int64_t)grow * k + x] = mds_key_index(key);
+  }
+}
+
+size_t recheck_smem(int Ap, int Kp, int k, int mode) {
+  int k1 = k + 1;
+  int TP2 = 1;
+  while (TP2 < k1 + RC_CHUNK) TP2 <<= 1;
+  size_t merge = 0;
+  if (mode == 0) {
+    merge = (size_t)std::max(Kp, 1);
+  }
+  size_t keys = std::max(merge + TP2, (size_t)0);
+  return sizeof(float) * (3 * Ap + 2 * RC_CHUNK * 9 + RC_CHUNK) + sizeof(int) * RC_CHUNK +
+         sizeof(uint64_t) * keys;
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+namespace {
+
+void jacobi3(double a[9], double d[3], double v[9]) {
+  for (int i = 0; i < 9; ++i) v[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = a[1] * a[1] + a[2] * a[2] + a[5] * a[5];
+    if (off < 1e-300) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        double apq = a[3 * p + q];
+        if (apq == 0.0) continue;
+        double theta = (a[3 * q + q] - a[3 * p + p]) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; ++k) {
+          double akp = a[3 * k + p], akq = a[3 * k + q];
+          a[3 * k + p] = c * akp - s * akq;
+          a[3 * k + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double apk = a[3 * p + k], aqk = a[3 * q + k];
+          a[3 * p + k] = c * apk - s * aqk;
+          a[3 * q + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double vkp = v[3 * k + p], vkq = v[3 * k + q];
+          v[3 * k + p] = c * vkp - s * vkq;
+          v[3 * k + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < 3; ++i) d[i] = a[4 * i];
+}
+
+}  // namespace
+
+// Template mu = first reference frame rotated into its principal axes (so
+// that sum mu mu^T is diagonal and the antisymmetric parts the screen needs
+// stay small).
+int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit,
+                   std::vector<double>& mu, double M0[9]) {
+  std::vector<float> y(3 * Ap);
+  MDS_CUDA(ctx, cudaMemcpyAsync(y.data(), dY0, sizeof(float) * 3 * Ap, cudaMemcpyDeviceToHost, ctx->stream));
+  MDS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double C[9] = {0};
+  for (int a = 0; a < natoms; ++a)
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 3; ++d) C[3 * c + d] += (double)y[c * Ap + a] * y[d * Ap + a];
+  double P[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, ev[3];
+  if (!nofit) {
+    double Cc[9];
+    std::copy(C, C + 9, Cc);
+    jacobi3(Cc, ev, P);
+    double det = P[0] * (P[4] * P[8] - P[5] * P[7]) - P[1] * (P[3] * P[8] - P[5] * P[6]) +
+                 P[2] * (P[3] * P[7] - P[4] * P[6]);
+    if (det < 0)
+      for (int i = 0; i < 3; ++i) P[3 * i] = -P[3 * i];
+  }
+  mu.assign(3 * Ap, 0.0);
+  for (int a = 0; a < natoms; ++a)
+    for (int d = 0; d < 3; ++d) {
+      double s = 0;
+      for (int c = 0; c < 3; ++c) s += (double)y[c * Ap + a] * P[3 * c + d];
+      mu[d * Ap + a] = s;
+    }
+  for (int i = 0; i < 9; ++i) M0[i] = 0;
+  for (int a = 0; a < natoms; ++a)
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 3; ++d) M0[3 * c + d] += mu[c * Ap + a] * mu[d * Ap + a];
+  return MDS_OK;
+}
+
+int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const double* Ef,
+                   const float* Yr, const double* Er, int nrows, const int* rowlist, int mode,
+                   const uint64_t* cand, const int* cand_n, int nseg, int Kp, int k, double* out_d,
+                   int* out_i, int* flagged, int* nflag) {
+  size_t smem = recheck_smem(pl.Ap, Kp, k, mode);
+  if (mode == 0) {
+    // the merge buffer holds nseg*Kp keys before trimming
+    int t = nseg * Kp, P2 = 1;
+    while (P2 < t) P2 <<= 1;
+    int TP2 = 1;
+    while (TP2 < k + 1 + RC_CHUNK) TP2 <<= 1;
+    size_t keys = std::max((size_t)P2, (size_t)Kp + TP2);
+    smem = sizeof(float) * (3 * pl.Ap + 2 * RC_CHUNK * 9 + RC_CHUNK) + sizeof(int) * RC_CHUNK +
+           sizeof(uint64_t) * keys;
+  }
+  if (smem > 227 * 1024)
+    return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck needs %zu bytes of shared memory (natoms/k too large)", smem);
+  MDS_CUDA(ctx, cudaFuncSetAttribute(k_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nrows > 0)
+    k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Yf, Ef, Yr, Er, nrows, rowlist, pl.nref, pl.Ap,
+                                                        pl.natoms, pl.nofit, mode, cand, cand_n, nseg,
+                                                        Kp, k, out_d, out_i, flagged, nflag);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+static int choose_nseg(int nrowtiles, int num_sms, int ncoltiles) {
+  int best = 1;
+  double besteff = 0;
+  for (int s = 1; s <= 8 && s <= ncoltiles; ++s) {
+    double waves = (double)nrowtiles * s / num_sms;
+    double eff = waves / std::ceil(waves);
+    if (eff > besteff + 0.02) {
+      besteff = eff;
+      best = s;
+    }
+    if (eff >= 0.95) break;
+  }
+  return best;
+}
+
+int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float* draw_fit,
+                const float* hmass, double* dout_d, int* dout_i) {
+  const int Ap = pl.Ap, natoms = pl.natoms;
+  mds_knn_stats& st = ctx->stats;
+  cudaStream_t s = ctx->stream;
+  // masses: sqrt(w/M) per atom, tm = float sum in file order (reset_x)
+  std::vector<float> swn(Ap, 0.f);
+  float tm = 0.f;
+  double M = 0;
+  for (int a = 0; a < natoms; ++a) {
+    tm += hmass[a];
+    M += hmass[a];
+  }
+  if (!(M > 0)) return mds_fail(ctx, MDS_ERR_ARG, "total mass must be positive");
+  for (int a = 0; a < natoms; ++a) swn[a] = (float)std::sqrt((double)hmass[a] / M);
+  DevBuf dmass, dswn;
+  MDS_TRY(dmass.alloc(ctx, sizeof(float) * natoms));
+  MDS_TRY(dswn.alloc(ctx, sizeof(float) * Ap));
+  MDS_CUDA(ctx, cudaMemcpyAsync(dmass.p, hmass, sizeof(float) * natoms, cudaMemcpyHostToDevice, s));
+  MDS_CUDA(ctx, cudaMemcpyAsync(dswn.p, swn.data(), sizeof(float) * Ap, cudaMemcpyHostToDevice, s));
+
+  const bool same = (draw_fit == nullptr);
+  const int nref = pl.nref, nfit = same ? nref : pl.nfit;
+  DevBuf Yr(ctx), Er(ctx), Yf(ctx), Ef(ctx);
+  MDS_TRY(Yr.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
+  MDS_TRY(Er.alloc(ctx, sizeof(double) * nref));
+  k_center<<<nref, 128, 0, s>>>(draw_ref, nref, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
+                                 Yr.as<float>(), Er.as<double>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  const float* Yfp = Yr.as<float>();
+  const double* Efp = Er.as<double>();
+  if (!same) {
+    MDS_TRY(Yf.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
+    MDS_TRY(Ef.alloc(ctx, sizeof(double) * nfit));
+    k_center<<<nfit, 128, 0, s>>>(draw_fit, nfit, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
+                                   Yf.as<float>(), Ef.as<double>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    Yfp = Yf.as<float>();
+    Efp = Ef.as<double>();
+  }
+
+  const int k = pl.k;
+  DevBuf flagged(ctx), nflag(ctx);
+  MDS_TRY(flagged.alloc(ctx, sizeof(int) * (size_t)std::max(nfit, 1)));
+  MDS_TRY(nflag.alloc(ctx, sizeof(int)));
+
+  if (pl.full) {
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+    MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), nfit, nullptr, 2,
+                           nullptr, nullptr, 1, 1, 0, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    MDS_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    st.recheck_ms = ms;
+    st.passes = 0;
+    return MDS_OK;
+  }
+
+  // template and superposition
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  std::vector<double> mu;
+  double M0[9];
+  MDS_TRY(build_template(ctx, Yr.as<float>(), Ap, natoms, pl.nofit != 0, mu, M0));
+  DevBuf dmu(ctx), dM0(ctx), Ar(ctx), Rr(ctx), Af(ctx), Rf(ctx);
+  MDS_TRY(dmu.alloc(ctx, sizeof(double) * 3 * Ap));
+  MDS_TRY(dM0.alloc(ctx, sizeof(double) * 9));
+  MDS_CUDA(ctx, cudaMemcpyAsync(dmu.p, mu.data(), sizeof(double) * 3 * Ap, cudaMemcpyHostToDevice, s));
+  MDS_CUDA(ctx, cudaMemcpyAsync(dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
+  MDS_TRY(Ar.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
+  MDS_TRY(Rr.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nref));
+  k_prealign<<<nref, 128, 0, s>>>(Yr.as<float>(), Er.as<double>(), nref, natoms, Ap, dmu.as<double>(),
+                                   dM0.as<double>(), pl.nofit, Ar.as<float>(), Rr.as<float>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  const float* Afp = Ar.as<float>();
+  const float* Rfp = Rr.as<float>();
+  if (!same) {
+    MDS_TRY(Af.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
+    MDS_TRY(Rf.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nfit));
+    k_prealign<<<nfit, 128, 0, s>>>(Yfp, Efp, nfit, natoms, Ap, dmu.as<double>(), dM0.as<double>(),
+                                     pl.nofit, Af.as<float>(), Rf.as<float>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    Afp = Af.as<float>();
+    Rfp = Rf.as<float>();
+  }
+  // tensor-core operands (split hi/lo), when that screen is selected
+  TcOperands tcr, tcf;
+  if (pl.prec != MDS_PREC_FP32) {
+    MDS_TRY(tc_prepare(ctx, pl, Ar.as<float>(), nref, tcr));
+    if (!same) MDS_TRY(tc_prepare(ctx, pl, Afp, nfit, tcf));
+  }
+
+  // first pass
+  int Kp = pl.kprime;
+  int ncoltiles = (nref + 63) / 64;
+  int nseg = choose_nseg((nfit + 31) / 32, ctx->num_sms, ncoltiles);
+  if (pl.prec != MDS_PREC_FP32) nseg = tc_choose_nseg(ctx, pl, nfit);
+  DevBuf cand(ctx), cand_n(ctx), rows(ctx);
+  MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)nfit * nseg * Kp));
+  MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)nfit * nseg));
+  MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  if (pl.prec == MDS_PREC_FP32) {
+    MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), nfit, nullptr, Kp, nseg,
+                               cand.as<uint64_t>(), cand_n.as<int>()));
+    st.screen_launches = 1;
+  } else {
+    MDS_TRY(launch_screen_tc(ctx, pl, same ? tcr : tcf, tcr, Rfp, Rr.as<float>(), nfit, Kp, nseg,
+                             cand.as<uint64_t>(), cand_n.as<int>()));
+    st.screen_launches = 1;
+  }
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), nfit, nullptr, 0,
+                         cand.as<uint64_t>(), cand_n.as<int>(), nseg, Kp, k, dout_d, dout_i,
+                         flagged.as<int>(), nflag.as<int>()));
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+  int hflag = 0;
+  MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  float t01 = 0, t12 = 0, t23 = 0;
+  cudaEventElapsedTime(&t01, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
+  cudaEventElapsedTime(&t23, ctx->ev[2], ctx->ev[3]);
+  st.prep_ms = t01;
+  st.screen_ms = t12;
+  st.recheck_ms = t23;
+  st.kprime = Kp;
+  st.rows_flagged = hflag;
+  st.passes = 1;
+
+  // re-screen flagged rows with more candidates (FP32 screen), then exact rows
+  while (hflag > 0) {
+    std::vector<int> hrows(hflag);
+    MDS_CUDA(ctx, cudaMemcpyAsync(hrows.data(), flagged.p, sizeof(int) * hflag, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    std::sort(hrows.begin(), hrows.end());
+    MDS_TRY(rows.alloc(ctx, sizeof(int) * hflag));
+    MDS_CUDA(ctx, cudaMemcpyAsync(rows.p, hrows.data(), sizeof(int) * hflag, cudaMemcpyHostToDevice, s));
+    MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
+    Kp = std::min(Kp * 4, 448);
+    st.passes++;
+    if (Kp >= nref || st.passes > 3) {
+      // exact rows: every reference is a candidate
+      MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), hflag, rows.as<int>(), 1,
+                             nullptr, nullptr, 1, 1, k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
+      MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      break;
+    }
+    int nseg2 = 1;
+    MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)hflag * nseg2 * Kp));
+    MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)hflag * nseg2));
+    MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), hflag, rows.as<int>(), Kp,
+                               nseg2, cand.as<uint64_t>(), cand_n.as<int>()));
+    MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), hflag, rows.as<int>(), 0,
+                           cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, k, dout_d, dout_i,
+                           flagged.as<int>(), nflag.as<int>()));
+    MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  }
+  return MDS_OK;
+}

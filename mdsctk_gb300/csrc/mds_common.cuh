@@ -1,0 +1,111 @@
+// mds_common.cuh -- shared definitions of libmdsgpu (context, errors,
+// device workspace, small device helpers).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mdsgpu.h"
+
+struct mds_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  size_t hbm_budget = 0;  // 0 = no limit beyond what cudaMalloc gives
+  size_t hbm_in_use = 0;
+  std::string last_error;
+  int num_sms = 0;
+  // statistics of the last kNN call (exposed through mds_knn_stats)
+  mds_knn_stats stats{};
+  // timing of the last call's dominant kernel (CUDA events on ctx->stream)
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+// Record an error message on the context and return `code`.
+int mds_fail(mds_ctx* ctx, int code, const char* fmt, ...);
+
+#define MDS_CUDA(ctx, call)                                                        \
+  do {                                                                             \
+    cudaError_t _e = (call);                                                       \
+    if (_e != cudaSuccess)                                                         \
+      return mds_fail((ctx), MDS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, \
+                      cudaGetErrorString(_e));                                     \
+  } while (0)
+
+// Device buffer owned by a context; freed on scope exit. Accounts against the
+// context's HBM budget.
+struct DevBuf {
+  mds_ctx* ctx = nullptr;
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  explicit DevBuf(mds_ctx* c) : ctx(c) {}
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) {
+      cudaFree(p);
+      if (ctx) ctx->hbm_in_use -= bytes;
+    }
+    p = nullptr;
+    bytes = 0;
+  }
+  // Returns MDS_OK or an error code (recorded on ctx).
+  int alloc(mds_ctx* c, size_t n) {
+    release();
+    ctx = c;
+    if (n == 0) n = 16;
+    if (ctx->hbm_budget && ctx->hbm_in_use + n > ctx->hbm_budget)
+      return mds_fail(ctx, MDS_ERR_NOMEM, "HBM budget exceeded: need %zu more bytes (in use %zu, budget %zu)",
+                      n, ctx->hbm_in_use, ctx->hbm_budget);
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return mds_fail(ctx, MDS_ERR_NOMEM, "cudaMalloc(%zu): %s", n, cudaGetErrorString(e));
+    }
+    bytes = n;
+    ctx->hbm_in_use += n;
+    return MDS_OK;
+  }
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+#define MDS_TRY(expr)              \
+  do {                             \
+    int _r = (expr);               \
+    if (_r != MDS_OK) return _r;   \
+  } while (0)
+
+static inline int mds_round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// Pack a non-negative float key and an index into one ordered 64-bit word:
+// ascending order = ascending (value, index).
+__host__ __device__ __forceinline__ uint64_t mds_pack_key(float s, int j) {
+#ifdef __CUDA_ARCH__
+  uint32_t u = __float_as_uint(s);
+#else
+  uint32_t u;
+  std::memcpy(&u, &s, 4);
+#endif
+  return ((uint64_t)u << 32) | (uint32_t)j;
+}
+__host__ __device__ __forceinline__ float mds_key_value(uint64_t k) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float((uint32_t)(k >> 32));
+#else
+  uint32_t u = (uint32_t)(k >> 32);
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+__host__ __device__ __forceinline__ int mds_key_index(uint64_t k) { return (int)(uint32_t)(k & 0xffffffffu); }
+
+#define MDS_KEY_INF 0xffffffffffffffffull

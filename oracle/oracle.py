@@ -1,0 +1,259 @@
+"""CPU oracle for the MDSCTK hot path -- TEST INFRASTRUCTURE ONLY.
+
+Loads ``oracle/_build/libmds_oracle.so`` (built from ``mds_oracle.cpp`` by
+``oracle/Makefile``) and adds the eigensolve step in Python. Only the tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import
+this module; the product library never does.
+
+Parity status: **parity unpinned** for the RMSD values (GROMACS do_fit /
+rmsdev / reset_x are third-party and absent; the reference cannot be built
+here and ships no golden outputs). The eigensolve is anchored on ARPACK, the
+reference's own solver dependency, through scipy's ``eigsh`` wrapper with the
+reference's parameters (decomp_sparse.cpp:185-237): which='LA',
+ncv=min(10*nev+1, n), tol=0, maxiter=100*nev.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libmds_oracle.so")
+_lib = None
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+
+def build() -> str:
+    """Compile the oracle library with the committed Makefile."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        c_int, c_dbl = ctypes.c_int, ctypes.c_double
+        L.orc_center.argtypes = [_f32p, c_int, c_int, _f32p]
+        L.orc_center.restype = None
+        L.orc_rmsd.argtypes = [_f32p, _f32p, c_int, _f32p, c_int]
+        L.orc_rmsd.restype = c_dbl
+        L.orc_rmsd_port.argtypes = [_f32p, _f32p, c_int, _f32p, c_int]
+        L.orc_rmsd_port.restype = c_dbl
+        L.orc_knn_rms.argtypes = [_f32p, c_int, _f32p, c_int, c_int, _f32p, c_int, c_int,
+                                  c_int, c_int, _f64p, _i32p]
+        L.orc_knn_rms.restype = c_int
+        L.orc_knn_rms_port.argtypes = [_f32p, c_int, _f32p, c_int, c_int, _f32p, c_int, c_int,
+                                       c_int, c_int, _f64p, _i32p]
+        L.orc_knn_rms_port.restype = c_int
+        L.orc_knn_data.argtypes = [_f64p, c_int, _f64p, c_int, c_int, c_int, c_int, c_int,
+                                   c_int, _f64p, _i32p]
+        L.orc_knn_data.restype = c_int
+        L.orc_sysparse.argtypes = [_f64p, _i32p, c_int, c_int, c_int, _i32p, _i32p, _f64p]
+        L.orc_sysparse.restype = ctypes.c_int64
+        L.orc_gesparse.argtypes = [_f64p, _i32p, c_int, c_int, c_int, c_int, _i32p, _i32p, _f64p]
+        L.orc_gesparse.restype = ctypes.c_int64
+        L.orc_affinity.argtypes = [c_int, _i32p, _i32p, _f64p, c_dbl, _f64p]
+        L.orc_affinity.restype = None
+        L.orc_affinity_nystrom.argtypes = [c_int, _i32p, _i32p, _f64p, c_dbl, _f64p]
+        L.orc_affinity_nystrom.restype = None
+        L.orc_sp_dsymv.argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+        L.orc_sp_dsymv.restype = None
+        L.orc_sp_dgemv.argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+        L.orc_sp_dgemv.restype = None
+        L.orc_num_threads.argtypes = []
+        L.orc_num_threads.restype = c_int
+        _lib = L
+    return _lib
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def center(xyz, mass):
+    """reset_x on every frame; returns a centred copy [n, natoms, 3] f32."""
+    x = _c(xyz, np.float32).copy()
+    n, na = x.shape[0], x.shape[1]
+    lib().orc_center(x.reshape(-1), n, na, _c(mass, np.float32))
+    return x
+
+
+def rmsd(x, y, mass, nofit=False):
+    """FP64 minimum RMSD (nm) between two centred frames."""
+    return lib().orc_rmsd(_c(x, np.float32).reshape(-1), _c(y, np.float32).reshape(-1),
+                          int(np.asarray(x).shape[0]), _c(mass, np.float32), int(nofit))
+
+
+def rmsd_port(ref, fit, mass, nofit=False):
+    """RMSD (nm) by the reference's do_fit + rmsdev procedure."""
+    return lib().orc_rmsd_port(_c(ref, np.float32).reshape(-1), _c(fit, np.float32).reshape(-1),
+                               int(np.asarray(ref).shape[0]), _c(mass, np.float32), int(nofit))
+
+
+def knn_rms(ref, fit, mass, k, nofit=False, sort=True, threads=0):
+    """knn_rms oracle (FP64). Returns (distances [nfit,k] in Angstrom, indices)."""
+    ref = _c(ref, np.float32)
+    fit = ref if fit is None else _c(fit, np.float32)
+    nref, na = ref.shape[0], ref.shape[1]
+    nfit = fit.shape[0]
+    kk = min(k, nref - 1)
+    width = kk if sort else nref
+    d = np.zeros(nfit * width, np.float64)
+    i = np.zeros(nfit * width, np.int32)
+    lib().orc_knn_rms(ref.reshape(-1), nref, fit.reshape(-1), nfit, na, _c(mass, np.float32),
+                      int(k), int(nofit), int(sort), int(threads), d, i)
+    return d.reshape(nfit, width), i.reshape(nfit, width)
+
+
+def knn_rms_port(ref, fit, mass, k, nofit=False, blksize=128, threads=0):
+    """The reference's CPU loop restated (the timed CPU baseline)."""
+    ref = _c(ref, np.float32)
+    fit = ref if fit is None else _c(fit, np.float32)
+    nref, na = ref.shape[0], ref.shape[1]
+    nfit = fit.shape[0]
+    kk = min(k, nref - 1)
+    d = np.zeros(nfit * kk, np.float64)
+    i = np.zeros(nfit * kk, np.int32)
+    lib().orc_knn_rms_port(ref.reshape(-1), nref, fit.reshape(-1), nfit, na,
+                           _c(mass, np.float32), int(k), int(nofit), int(blksize), int(threads),
+                           d, i)
+    return d.reshape(nfit, kk), i.reshape(nfit, kk)
+
+
+def knn_data(ref, fit, k, correlation=False, sort=True, threads=0):
+    """knn_data oracle (bit-exact FP64 restatement)."""
+    ref = _c(ref, np.float64)
+    fit = ref if fit is None else _c(fit, np.float64)
+    nref, dim = ref.shape
+    nfit = fit.shape[0]
+    kk = min(k, nref - 1)
+    width = kk if sort else nref
+    d = np.zeros(nfit * width, np.float64)
+    i = np.zeros(nfit * width, np.int32)
+    lib().orc_knn_data(ref.reshape(-1), nref, fit.reshape(-1), nfit, dim, int(k),
+                       int(correlation), int(sort), int(threads), d, i)
+    return d.reshape(nfit, width), i.reshape(nfit, width)
+
+
+def sysparse(dist, idx, k=None):
+    """make_sysparse oracle. dist/idx: [nrows, maxk]. Returns (n, pcol, irow, val)."""
+    dist = _c(dist, np.float64)
+    idx = _c(idx, np.int32)
+    nrows, maxk = dist.shape
+    k = maxk if k is None else k
+    pcol = np.zeros(nrows + 1, np.int32)
+    cap = max(1, nrows * k)
+    irow = np.zeros(cap, np.int32)
+    val = np.zeros(cap, np.float64)
+    nnz = lib().orc_sysparse(dist.reshape(-1), idx.reshape(-1), nrows, maxk, k, pcol, irow, val)
+    return nrows, pcol, irow[:nnz].copy(), val[:nnz].copy()
+
+
+def gesparse(dist, idx, k=None, symmetric=False):
+    """make_gesparse oracle. Returns (m, pcol, irow, val)."""
+    dist = _c(dist, np.float64)
+    idx = _c(idx, np.int32)
+    nrows, maxk = dist.shape
+    k = maxk if k is None else k
+    pcol = np.zeros(nrows + 1, np.int32)
+    cap = max(1, nrows * k * (2 if symmetric else 1))
+    irow = np.zeros(cap, np.int32)
+    val = np.zeros(cap, np.float64)
+    nnz = lib().orc_gesparse(dist.reshape(-1), idx.reshape(-1), nrows, maxk, k, int(symmetric),
+                             pcol, irow, val)
+    return nrows, pcol, irow[:nnz].copy(), val[:nnz].copy()
+
+
+def affinity(n, pcol, irow, val, sigma):
+    """Normalised Gaussian affinity (decomp_sparse.cpp:158-178). Returns (val, d^-1/2)."""
+    v = _c(val, np.float64).copy()
+    d = np.zeros(n, np.float64)
+    lib().orc_affinity(n, _c(pcol, np.int32), _c(irow, np.int32), v, float(sigma), d)
+    return v, d
+
+
+def affinity_nystrom(m, pcolB, irowB, valB, sigma, d_a):
+    v = _c(valB, np.float64).copy()
+    lib().orc_affinity_nystrom(m, _c(pcolB, np.int32), _c(irowB, np.int32), v, float(sigma),
+                               _c(d_a, np.float64))
+    return v
+
+
+def sp_dsymv(n, pcol, irow, A, v):
+    w = np.zeros(n, np.float64)
+    lib().orc_sp_dsymv(n, _c(irow, np.int32), _c(pcol, np.int32), _c(A, np.float64),
+                       _c(v, np.float64), w)
+    return w
+
+
+def sp_dgemv(n, pcol, irow, A, v):
+    w = np.zeros(n, np.float64)
+    lib().orc_sp_dgemv(n, _c(irow, np.int32), _c(pcol, np.int32), _c(A, np.float64),
+                       _c(v, np.float64), w)
+    return w
+
+
+def sym_operator(n, pcol, irow, A):
+    """scipy LinearOperator applying sp_dsymv semantics."""
+    from scipy.sparse.linalg import LinearOperator
+
+    pcol = _c(pcol, np.int32)
+    irow = _c(irow, np.int32)
+    A = _c(A, np.float64)
+    return LinearOperator((n, n), matvec=lambda v: sp_dsymv(n, pcol, irow, A, np.ravel(v)),
+                          dtype=np.float64)
+
+
+def decomp_sparse(n, pcol, irow, dist, sigma, nev, ncv=None, tol=0.0, maxiter=None, v0=None):
+    """decomp_sparse oracle: affinity, normalisation, ARPACK 'LA' eigenpairs.
+
+    Returns (evals descending [nev], evecs [nev, n], residuals [nev]) in the
+    reference's output order (decomp_sparse.cpp:242-270).
+    """
+    from scipy.sparse.linalg import eigsh
+
+    A, _ = affinity(n, pcol, irow, dist, sigma)
+    op = sym_operator(n, pcol, irow, A)
+    if ncv is None:
+        ncv = min(10 * nev + 1, n)
+    if maxiter is None:
+        maxiter = 100 * nev
+    w, V = eigsh(op, k=nev, which="LA", ncv=ncv, tol=tol, maxiter=maxiter, v0=v0)
+    order = np.argsort(w)[::-1]
+    w = w[order]
+    V = V[:, order].T.copy()
+    res = np.array([np.linalg.norm(sp_dsymv(n, pcol, irow, A, V[x]) - w[x] * V[x]) / abs(w[x])
+                    for x in range(nev)])
+    return w, V, res
+
+
+def dense_affinity(n, pcol, irow, dist, sigma):
+    """Dense normalised affinity matrix (exact cross-check for small n)."""
+    A, _ = affinity(n, pcol, irow, dist, sigma)
+    M = np.zeros((n, n))
+    for c in range(n):
+        for p in range(pcol[c], pcol[c + 1]):
+            r = irow[p]
+            if r == c and p == pcol[c]:
+                M[r, c] += A[p]
+            else:
+                M[r, c] += A[p]
+                M[c, r] += A[p]
+    return M
+
+
+def nystrom_extend(evals, evecs, m, pcolB, irowB, B):
+    """ext[x] = B^T (z_x / lambda_x) (decomp_sparse_nystrom.cpp:301-312)."""
+    out = np.zeros((len(evals), m))
+    for x in range(len(evals)):
+        out[x] = sp_dgemv(m, pcolB, irowB, B, evecs[x] / evals[x])
+    return out

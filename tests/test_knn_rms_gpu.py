@@ -1,0 +1,68 @@
+"""GPU parity of knn_rms against the FP64 oracle (tests marked gpu)."""
+import numpy as np
+import pytest
+
+from mdsctk_gb300 import synth
+
+TOL_A = 1e-4  # 1e-5 nm in the file's Angstrom units
+
+
+def _check_knn(d, i, od, oi, tol=TOL_A):
+    """Distances within tol; indices equal except where the oracle's
+    neighbouring distances are within tol of each other (near ties)."""
+    assert d.shape == od.shape
+    assert np.max(np.abs(d - od)) <= tol, np.max(np.abs(d - od))
+    bad = np.argwhere(i != oi)
+    for r, c in bad:
+        # a swap is legitimate only inside a tie band
+        v = od[r, c]
+        assert abs(d[r, c] - v) <= tol
+        near = np.abs(od[r] - v) <= 2 * tol
+        assert near.sum() >= 2, (r, c, i[r, c], oi[r, c], v)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32"])
+@pytest.mark.parametrize("n,natoms,k,basins", [(300, 304, 20, 1), (257, 97, 10, 4), (200, 1000, 30, 2)])
+def test_knn_rms_self(ctx, oracle, precision, n, natoms, k, basins):
+    x = synth.trajectory(n, natoms, seed=n + natoms, basins=basins, dwell=60)
+    m = synth.uniform_masses(natoms)
+    d, i = ctx.knn_rms(x, None, m, k, precision=precision)
+    od, oi = oracle.knn_rms(x, None, m, k)
+    _check_knn(d, i, od, oi)
+
+
+@pytest.mark.gpu
+def test_knn_rms_fit_vs_ref_masses(ctx, oracle):
+    rng = np.random.default_rng(1)
+    ref = synth.trajectory(220, 60, seed=11, basins=3, dwell=40)
+    fit = synth.trajectory(75, 60, seed=12, basins=3, dwell=40)
+    m = rng.uniform(1.0, 16.0, size=60).astype(np.float32)
+    d, i = ctx.knn_rms(ref, fit, m, 15)
+    od, oi = oracle.knn_rms(ref, fit, m, 15)
+    _check_knn(d, i, od, oi)
+
+
+@pytest.mark.gpu
+def test_knn_rms_nofit_and_full(ctx, oracle):
+    x = synth.trajectory(150, 45, seed=5)
+    m = synth.uniform_masses(45)
+    d, i = ctx.knn_rms(x, None, m, 12, nofit=True)
+    od, oi = oracle.knn_rms(x, None, m, 12, nofit=True)
+    _check_knn(d, i, od, oi)
+    d, i = ctx.knn_rms(x[:40], x[40:90], m, 0, sort=False)
+    od, oi = oracle.knn_rms(x[:40], x[40:90], m, 0, sort=False)
+    assert np.max(np.abs(d - od)) <= TOL_A
+    assert (i == np.arange(40)[None, :]).all()
+
+
+@pytest.mark.gpu
+def test_knn_rms_k_clamp_and_tiny(ctx, oracle):
+    x = synth.trajectory(5, 10, seed=2)
+    m = synth.uniform_masses(10)
+    d, i = ctx.knn_rms(x, None, m, 50)  # k clamped to 4
+    od, oi = oracle.knn_rms(x, None, m, 50)
+    assert d.shape == (5, 4)
+    _check_knn(d, i, od, oi)
+    d, i = ctx.knn_rms(x[:1], None, m, 3)  # one frame: k = 0
+    assert d.shape == (1, 0)
