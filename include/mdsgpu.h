@@ -63,6 +63,7 @@ typedef struct mds_knn_stats {
   int rows_flagged;    /* rows whose guard failed in the first pass */
   int passes;          /* screen passes (1 + re-screens of flagged rows) */
   int screen_launches; /* kernel launches of the screen */
+  int launches;        /* all kernel launches of the call */
 } mds_knn_stats;
 
 /* Library version string. */
@@ -97,6 +98,29 @@ int mds_knn_rms(mds_ctx* ctx, const float* ref_xyz, int n_ref, const float* fit_
                 int32_t* out_i, int* k_used);
 
 /*
+ * Diagnostic of the knn_rms candidate screen (no reference counterpart: the
+ * reference computes every pair exactly). Runs centring, superposition onto
+ * the template and the screen selected by the precision flag, and returns,
+ * per fit frame, the `kprime` smallest screen keys in ascending order:
+ * (float lower bound of RMSD^2 in nm^2, as its bit pattern) << 32 | index.
+ *   keys [n_fit][kprime] uint64, counts [n_fit] (entries valid per row).
+ */
+int mds_knn_rms_screen(mds_ctx* ctx, const float* ref_xyz, int n_ref, const float* fit_xyz, int n_fit,
+                       int natoms, const float* mass, int kprime, unsigned flags, uint64_t* keys,
+                       int32_t* counts);
+
+/*
+ * Diagnostic of the superposition step of knn_rms (no reference
+ * counterpart): every frame centred (reset_x), scaled by sqrt(mass/M) and
+ * superposed onto the template (the first frame in its principal axes).
+ *   dev [n_ref][3][Ap] float deviations a = R y - mu, Ap = natoms rounded
+ *       up to 64 (padding zero); rec [n_ref][16] float screen records:
+ *       M0+sym(U) (6), sym(U) (6), antisym(U) (3), |a|^2, with U = sum a mu^T.
+ */
+int mds_knn_rms_superpose(mds_ctx* ctx, const float* ref_xyz, int n_ref, int natoms, const float* mass,
+                          unsigned flags, float* dev, float* rec);
+
+/*
  * knn_data: k nearest reference vectors by Euclidean distance
  * (euclidean_distance, mdsctk.cpp:330-335) or, with MDS_CORRELATION, by
  * correlation distance (mdsctk.cpp:337-360). Replaces knn_data.cpp:176-250.
@@ -106,6 +130,58 @@ int mds_knn_rms(mds_ctx* ctx, const float* ref_xyz, int n_ref, const float* fit_
  */
 int mds_knn_data(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, int n_fit,
                  int dim, int k, unsigned flags, double* out_d, int32_t* out_i, int* k_used);
+
+/*
+ * make_sysparse: kNN lists -> symmetric sparse matrix holding one strict
+ * triangle of distances, CSC (column c holds rows r > c, ascending).
+ * Replaces make_sysparse.cpp:225-329 (Berkeley-DB B-tree insertion with
+ * compare_edge, mdsctk.cpp:567-577, put-overwrite, cursor walk split_edges,
+ * mdsctk.cpp:580-604). Rows r = 0..n_rows-1 of dist/idx ([n_rows][maxk]),
+ * first k entries of each row (-n, k <= maxk). For an edge listed by both
+ * ends, the later row's value wins, as the later put does.
+ *   pcol [n_rows+1], irow [cap], val [cap]; *nnz receives the count
+ *   (cap >= n_rows * k always suffices).
+ */
+int mds_sysparse(mds_ctx* ctx, const double* dist, const int32_t* idx, int n_rows, int maxk, int k,
+                 unsigned flags, int32_t* pcol, int32_t* irow, double* val, int64_t cap, int64_t* nnz);
+
+/*
+ * make_gesparse: kNN lists of queries against landmarks -> general CSC,
+ * column = query row, rows = landmark indices ascending; with `symmetric`
+ * (-s) also the transposed entry where it is absent at insertion time.
+ * Replaces make_gesparse.cpp:246-335. cap >= n_rows * k * (symmetric ? 2 : 1).
+ */
+int mds_gesparse(mds_ctx* ctx, const double* dist, const int32_t* idx, int n_rows, int maxk, int k,
+                 int symmetric, unsigned flags, int32_t* pcol, int32_t* irow, double* val, int64_t cap,
+                 int64_t* nnz);
+
+/*
+ * decomp_sparse: Gaussian affinity exp(-d^2 / 2 sigma^2) of the stored
+ * triangle, symmetric normalisation D^-1/2 W D^-1/2, and the nev largest
+ * eigenpairs ('LA'). Replaces decomp_sparse.cpp:138-277 and its ARPACK
+ * driver (dsaupd/dseupd, :185-237).
+ *   n, pcol [n+1], irow [nnz], dist [nnz]: the .ssm matrix (CSC).
+ *   ncv <= 0: min(10 nev + 1, n) as the reference; tol <= 0: machine
+ *   epsilon (tol = 0 in the reference); maxiter <= 0: 100 nev.
+ *   evals [nev] descending; evecs [nev][n] in the same order (unit norm,
+ *   sign arbitrary as ARPACK's); resid [nev] = ||A z - lambda z|| / |lambda|
+ *   (may be NULL); nconv receives the converged count (may be NULL).
+ */
+int mds_decomp_sparse(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow, const double* dist,
+                      double sigma, int nev, int ncv, double tol, int maxiter, unsigned flags, double* evals,
+                      double* evecs, double* resid, int* nconv);
+
+/*
+ * decomp_sparse_nystrom: decomp_sparse plus the Nystrom extension of the
+ * eigenvectors to m out-of-sample queries: B = the .gsm matrix (CSC, column =
+ * query, rows = landmarks) kernelised with the landmark degrees and its own
+ * column sums, ext[x] = B^T (z_x / lambda_x). Replaces
+ * decomp_sparse_nystrom.cpp:173-312. ext [nev][m].
+ */
+int mds_decomp_sparse_nystrom(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow, const double* dist,
+                              int m, const int32_t* pcolB, const int32_t* irowB, const double* distB,
+                              double sigma, int nev, int ncv, double tol, int maxiter, unsigned flags,
+                              double* evals, double* evecs, double* ext, double* resid, int* nconv);
 
 #ifdef __cplusplus
 }

@@ -42,7 +42,7 @@ class KnnStats(ctypes.Structure):
                 ("recheck_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("pairs", ctypes.c_longlong), ("kprime", ctypes.c_int),
                 ("rows_flagged", ctypes.c_int), ("passes", ctypes.c_int),
-                ("screen_launches", ctypes.c_int)]
+                ("screen_launches", ctypes.c_int), ("launches", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -59,7 +59,14 @@ SIGNATURES = {
     "mds_last_error": ([_vp], ctypes.c_char_p),
     "mds_get_knn_stats": ([_vp, ctypes.POINTER(KnnStats)], _i),
     "mds_knn_rms": ([_vp, _vp, _i, _vp, _i, _i, _vp, _i, _u, _vp, _vp, _ip], _i),
+    "mds_knn_rms_screen": ([_vp, _vp, _i, _vp, _i, _i, _vp, _i, _u, _vp, _vp], _i),
+    "mds_knn_rms_superpose": ([_vp, _vp, _i, _i, _vp, _u, _vp, _vp], _i),
     "mds_knn_data": ([_vp, _vp, _i, _vp, _i, _i, _i, _u, _vp, _vp, _ip], _i),
+    "mds_sysparse": ([_vp, _vp, _vp, _i, _i, _i, _u, _vp, _vp, _vp, ctypes.c_int64, _i64p], _i),
+    "mds_gesparse": ([_vp, _vp, _vp, _i, _i, _i, _i, _u, _vp, _vp, _vp, ctypes.c_int64, _i64p], _i),
+    "mds_decomp_sparse": ([_vp, _i, _vp, _vp, _vp, _d, _i, _i, _d, _i, _u, _vp, _vp, _vp, _ip], _i),
+    "mds_decomp_sparse_nystrom": ([_vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _d, _i, _i, _d, _i, _u, _vp, _vp,
+                                   _vp, _vp, _ip], _i),
 }
 
 _lib = None

@@ -101,6 +101,41 @@ class Context:
         L.check(self.h, rc)
         return d, i
 
+    def knn_rms_screen(self, ref, fit=None, mass=None, kprime: int = 32, nofit: bool = False,
+                       precision: str = "fp32"):
+        """Candidate screen diagnostic: per fit frame, the kprime smallest
+        lower bounds of RMSD^2 (nm^2) and their reference indices, ascending.
+        Returns (bounds [n_fit, kprime] f32, indices [n_fit, kprime] i32,
+        counts [n_fit])."""
+        ref = np.ascontiguousarray(ref, dtype=np.float32)
+        fit = None if fit is None else np.ascontiguousarray(fit, dtype=np.float32)
+        n_ref, natoms = ref.shape[0], ref.shape[1]
+        n_fit = n_ref if fit is None else fit.shape[0]
+        mass = np.ones(natoms, np.float32) if mass is None else np.ascontiguousarray(mass, np.float32)
+        flags = L.PRECISIONS[precision] | (L.MDS_NOFIT if nofit else 0)
+        keys = np.zeros((n_fit, kprime), np.uint64)
+        counts = np.zeros(n_fit, np.int32)
+        rc = self._lib.mds_knn_rms_screen(self.h, _ptr(ref), n_ref, _ptr(fit),
+                                          n_fit if fit is not None else 0, natoms, _ptr(mass), int(kprime),
+                                          flags, _ptr(keys), _ptr(counts))
+        L.check(self.h, rc)
+        bounds = (keys >> np.uint64(32)).astype(np.uint32).view(np.float32)
+        idx = (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32).view(np.int32)
+        return bounds, idx, counts
+
+    def knn_rms_superpose(self, ref, mass=None, nofit: bool = False):
+        """Superposition diagnostic: (deviations [n, 3, Ap] f32, records [n, 16] f32)."""
+        ref = np.ascontiguousarray(ref, dtype=np.float32)
+        n, natoms = ref.shape[0], ref.shape[1]
+        ap = (natoms + 63) // 64 * 64
+        mass = np.ones(natoms, np.float32) if mass is None else np.ascontiguousarray(mass, np.float32)
+        dev = np.zeros((n, 3, ap), np.float32)
+        rec = np.zeros((n, 16), np.float32)
+        rc = self._lib.mds_knn_rms_superpose(self.h, _ptr(ref), n, natoms, _ptr(mass),
+                                             L.MDS_NOFIT if nofit else 0, _ptr(dev), _ptr(rec))
+        L.check(self.h, rc)
+        return dev, rec
+
     def knn_data(self, ref, fit=None, k: int = 1, correlation: bool = False, sort: bool = True,
                  precision: str = "fp32", out=None):
         """knn_data: k nearest reference vectors (Euclidean, or correlation
@@ -132,3 +167,65 @@ class Context:
                                     dim, int(k), flags, _ptr(d), _ptr(i), ctypes.byref(ku))
         L.check(self.h, rc)
         return d, i
+
+    # ------------------------------------------------------------ sparse
+    def sysparse(self, dist, idx, k=None):
+        """make_sysparse: returns (n, pcol, irow, val) of the strict lower
+        triangle of distances (CSC)."""
+        dist = np.ascontiguousarray(dist, np.float64)
+        idx = np.ascontiguousarray(idx, np.int32)
+        n, maxk = dist.shape
+        k = maxk if k is None else int(k)
+        cap = max(1, n * k)
+        pcol = np.zeros(n + 1, np.int32)
+        irow = np.zeros(cap, np.int32)
+        val = np.zeros(cap, np.float64)
+        nnz = ctypes.c_int64(0)
+        L.check(self.h, self._lib.mds_sysparse(self.h, _ptr(dist), _ptr(idx), n, maxk, k, 0, _ptr(pcol),
+                                               _ptr(irow), _ptr(val), cap, ctypes.byref(nnz)))
+        return n, pcol, irow[:nnz.value].copy(), val[:nnz.value].copy()
+
+    def gesparse(self, dist, idx, k=None, symmetric=False):
+        """make_gesparse: returns (m, pcol, irow, val) (CSC, column = query)."""
+        dist = np.ascontiguousarray(dist, np.float64)
+        idx = np.ascontiguousarray(idx, np.int32)
+        n, maxk = dist.shape
+        k = maxk if k is None else int(k)
+        cap = max(1, n * k * (2 if symmetric else 1))
+        pcol = np.zeros(n + 1, np.int32)
+        irow = np.zeros(cap, np.int32)
+        val = np.zeros(cap, np.float64)
+        nnz = ctypes.c_int64(0)
+        L.check(self.h, self._lib.mds_gesparse(self.h, _ptr(dist), _ptr(idx), n, maxk, k, int(bool(symmetric)), 0,
+                                               _ptr(pcol), _ptr(irow), _ptr(val), cap, ctypes.byref(nnz)))
+        return n, pcol, irow[:nnz.value].copy(), val[:nnz.value].copy()
+
+    def decomp_sparse(self, n, pcol, irow, dist, sigma, nev, ncv=0, tol=0.0, maxiter=0):
+        """decomp_sparse: (evals descending [nev], evecs [nev, n], residuals [nev], nconv)."""
+        pcol = np.ascontiguousarray(pcol, np.int32)
+        irow = np.ascontiguousarray(irow, np.int32)
+        dist = np.ascontiguousarray(dist, np.float64)
+        ev = np.zeros(nev)
+        V = np.zeros((nev, n))
+        res = np.zeros(nev)
+        nc = ctypes.c_int(0)
+        L.check(self.h, self._lib.mds_decomp_sparse(self.h, int(n), _ptr(pcol), _ptr(irow), _ptr(dist), float(sigma),
+                                                    int(nev), int(ncv), float(tol), int(maxiter), 0, _ptr(ev),
+                                                    _ptr(V), _ptr(res), ctypes.byref(nc)))
+        return ev, V, res, nc.value
+
+    def decomp_sparse_nystrom(self, n, pcol, irow, dist, m, pcolB, irowB, distB, sigma, nev, ncv=0, tol=0.0,
+                              maxiter=0):
+        """decomp_sparse_nystrom: (evals, evecs [nev, n], ext [nev, m], residuals, nconv)."""
+        a = [np.ascontiguousarray(v, t) for v, t in ((pcol, np.int32), (irow, np.int32), (dist, np.float64),
+                                                      (pcolB, np.int32), (irowB, np.int32), (distB, np.float64))]
+        ev = np.zeros(nev)
+        V = np.zeros((nev, n))
+        E = np.zeros((nev, m))
+        res = np.zeros(nev)
+        nc = ctypes.c_int(0)
+        L.check(self.h, self._lib.mds_decomp_sparse_nystrom(
+            self.h, int(n), _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), int(m), _ptr(a[3]), _ptr(a[4]), _ptr(a[5]),
+            float(sigma), int(nev), int(ncv), float(tol), int(maxiter), 0, _ptr(ev), _ptr(V), _ptr(E), _ptr(res),
+            ctypes.byref(nc)))
+        return ev, V, E, res, nc.value

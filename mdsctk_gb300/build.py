@@ -59,9 +59,37 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_tools()
     if verbose:
         print("built", LIB)
     return LIB
+
+
+TOOLS = ("knn_rms", "knn_data", "make_sysparse", "make_gesparse", "decomp_sparse", "decomp_sparse_nystrom")
+BINDIR = os.path.join(HERE, "bin")
+
+
+def build_tools() -> None:
+    """The drop-in command-line tools: C++ mains linked against libmdsgpu."""
+    os.makedirs(BINDIR, exist_ok=True)
+    tdir = os.path.join(CSRC, "tools")
+    headers = [os.path.join(tdir, f) for f in os.listdir(tdir) if f.endswith(".h")]
+    cxx = shutil.which("g++") or "g++"
+
+    def one(name):
+        src = os.path.join(tdir, name + ".cpp")
+        out = os.path.join(BINDIR, name)
+        deps = [src, LIB] + headers
+        if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+            return
+        cmd = [cxx, "-O2", "-std=c++17", "-Wall", src, "-o", out, "-L" + LIBDIR, "-lmdsgpu",
+               "-Wl,-rpath,$ORIGIN/../lib"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"tool build failed for {name}:\n{r.stdout}\n{r.stderr}")
+
+    with cf.ThreadPoolExecutor(max_workers=len(TOOLS)) as ex:
+        list(ex.map(one, TOOLS))
 
 
 if __name__ == "__main__":

@@ -1,0 +1,807 @@
+// decomp.cu -- spectral decomposition of the normalised Gaussian affinity
+// (decomp_sparse, decomp_sparse_nystrom) on sm_103a, FP64.
+//
+// Replaces decomp_sparse.cpp:138-277 and decomp_sparse_nystrom.cpp:173-312:
+//  1. symmetrise + kernelise: the stored triangle (CSC, one entry per
+//     undirected edge, values are distances) is expanded into a symmetric CSR
+//     holding both triangles: each stored off-diagonal entry gives (r,c) and
+//     (c,r); a diagonal entry keeps the weight sp_dsymv gives it (once when it
+//     is its column's first entry, twice otherwise, mdsctk.cpp:293-313). A
+//     stable radix sort by (row, col) makes every row's order deterministic.
+//     w = exp(-d^2 / 2 sigma^2); degrees as decomp_sparse.cpp:162-169 (each
+//     stored entry adds w to both its row and its column, a diagonal entry
+//     twice); entries scaled by d_r^-1/2 d_c^-1/2.
+//  2. SpMV: FP64, one warp per row of the expanded CSR.
+//  3. Thick-restart Lanczos (Wu & Simon 2000; equivalent to ARPACK's
+//     implicitly restarted Lanczos for symmetric matrices) keeping ARPACK's
+//     contract: which='LA', nev, ncv, tol (0 = machine epsilon, converged
+//     when the Ritz estimate <= tol * max(eps^(2/3), |theta|)), maxiter
+//     restarts, start vector from a fixed seed. Full reorthogonalisation
+//     (classical Gram-Schmidt applied twice) by FP64 GEMV kernels; the
+//     projected matrix (ncv x ncv, arrowhead + tridiagonal) is solved on the
+//     host by Householder reduction and the implicit QL algorithm.
+//  4. Eigenvalues descending, eigenvectors in the same order, residuals
+//     ||A z - lambda z||_2 / |lambda| (decomp_sparse.cpp:242-270).
+//  5. Nystrom: B (general CSC, columns = queries) kernelised with the
+//     landmark degrees d_a and its own column sums (decomp_sparse_nystrom.cpp:
+//     181-219); extension ext[x] = B^T (z_x / lambda_x) for all nev vectors
+//     in one pass (:301-312).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mds_common.cuh"
+
+// ---------------------------------------------------------------------------
+// 1. symmetrise + kernelise
+// ---------------------------------------------------------------------------
+// half-entries: key = (row << 32 | col) (both non-negative), value = stored
+// position p << 2 | kind; kind 0 off-diagonal, 1 diagonal first-in-column
+// (matvec weight 1), 2 diagonal elsewhere (matvec weight 2).
+__global__ void k_sym_expand(const int* __restrict__ pcol, const int* __restrict__ irow, int n,
+                             unsigned long long* __restrict__ keys, int64_t* __restrict__ vals,
+                             const int64_t* __restrict__ pos, int* __restrict__ bad) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  int64_t o = pos[c];
+  for (int p = pcol[c]; p < pcol[c + 1]; ++p) {
+    int r = irow[p];
+    if (r < 0 || r >= n) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    if (r == c) {
+      keys[o] = ((unsigned long long)r << 32) | (unsigned)c;
+      vals[o++] = ((int64_t)p << 2) | (p == pcol[c] ? 1 : 2);
+    } else {
+      keys[o] = ((unsigned long long)r << 32) | (unsigned)c;
+      vals[o++] = ((int64_t)p << 2);
+      keys[o] = ((unsigned long long)c << 32) | (unsigned)r;
+      vals[o++] = ((int64_t)p << 2);
+    }
+  }
+}
+
+__global__ void k_sym_count(const int* __restrict__ pcol, const int* __restrict__ irow, int n,
+                            int* __restrict__ cnt) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  int m = 0;
+  for (int p = pcol[c]; p < pcol[c + 1]; ++p) m += (irow[p] == c) ? 1 : 2;
+  cnt[c] = m;
+}
+
+__global__ void k_scan_i64(const int* __restrict__ in, int n, int64_t* __restrict__ out) {
+  __shared__ long long part[1024];
+  int per = (n + blockDim.x - 1) / blockDim.x;
+  int b = threadIdx.x * per, e = min(n, b + per);
+  long long s = 0;
+  for (int i = b; i < e; ++i) s += in[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long acc = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      long long v = part[i];
+      part[i] = acc;
+      acc += v;
+    }
+  }
+  __syncthreads();
+  long long acc = part[threadIdx.x];
+  for (int i = b; i < e; ++i) {
+    out[i] = acc;
+    acc += in[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) out[n] = acc;
+}
+
+// sorted half-entries -> CSR row pointers (lower_bound per row)
+__global__ void k_rowptr(const unsigned long long* __restrict__ keys, int64_t m, int n, int64_t* __restrict__ rp) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > n) return;
+  unsigned long long t = (unsigned long long)r << 32;
+  int64_t lo = 0, hi = m;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) / 2;
+    if (keys[mid] < t) lo = mid + 1; else hi = mid;
+  }
+  rp[r] = lo;
+}
+
+// affinity weight of every half-entry, degree of every row (column order:
+// deterministic), then d^-1/2. One warp per row.
+__global__ void k_sym_degree(const unsigned long long* __restrict__ keys, const int64_t* __restrict__ vals,
+                             const int64_t* __restrict__ rp, const double* __restrict__ dist, int n,
+                             double inv2s2, int* __restrict__ col, double* __restrict__ w,
+                             double* __restrict__ dinv) {
+  int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0.0;
+  for (int64_t e = rp[row] + lane; e < rp[row + 1]; e += 32) {
+    int64_t v = vals[e];
+    int kind = (int)(v & 3);
+    double d = dist[v >> 2];
+    double a = exp(-(d * d) * inv2s2);
+    col[e] = (int)(keys[e] & 0xffffffffu);
+    w[e] = a * (kind == 2 ? 2.0 : 1.0);  // the weight sp_dsymv gives it
+    s += (kind == 0) ? a : 2.0 * a;      // the reference's degree sum
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) dinv[row] = 1.0 / sqrt(s);
+}
+
+__global__ void k_sym_normalise(const int64_t* __restrict__ rp, const int* __restrict__ col,
+                                const double* __restrict__ dinv, int n, double* __restrict__ w) {
+  int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double dr = dinv[row];
+  for (int64_t e = rp[row] + lane; e < rp[row + 1]; e += 32) w[e] *= dr * dinv[col[e]];
+}
+
+// ---------------------------------------------------------------------------
+// 2. SpMV and dense vector kernels
+// ---------------------------------------------------------------------------
+__global__ void k_spmv(const int64_t* __restrict__ rp, const int* __restrict__ col, const double* __restrict__ w,
+                       const double* __restrict__ x, int n, double* __restrict__ y) {
+  int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0.0;
+  for (int64_t e = rp[row] + lane; e < rp[row + 1]; e += 32) s += w[e] * __ldg(x + col[e]);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[row] = s;
+}
+
+// h[j] = sum_i V[i + j*ld] * w[i], j < ncols; partial sums per block then a
+// second kernel reduces them (deterministic order).
+#define GV_ROWS 2048
+__global__ void k_gemv_t_part(const double* __restrict__ V, int64_t ld, int n, int ncols,
+                              const double* __restrict__ w, double* __restrict__ part) {
+  extern __shared__ double sh[];  // [blockDim/32][ncols]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int r0 = blockIdx.x * GV_ROWS, r1 = min(n, r0 + GV_ROWS);
+  for (int j = warp; j < ncols; j += nw) {
+    double s = 0.0;
+    for (int i = r0 + lane; i < r1; i += 32) s += V[i + j * ld] * w[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = s;
+  }
+  (void)sh;
+}
+__global__ void k_reduce_part(const double* __restrict__ part, int nparts, int ncols, double* __restrict__ h) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ncols) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += part[(int64_t)b * ncols + j];
+  h[j] = s;
+}
+// w -= V[:, 0:ncols] h
+__global__ void k_gemv_sub(const double* __restrict__ V, int64_t ld, int n, int ncols,
+                           const double* __restrict__ h, double* __restrict__ w) {
+  extern __shared__ double hs[];
+  for (int j = threadIdx.x; j < ncols; j += blockDim.x) hs[j] = h[j];
+  __syncthreads();
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int j = 0; j < ncols; ++j) s += V[i + j * ld] * hs[j];
+  w[i] -= s;
+}
+__global__ void k_scale_copy(const double* __restrict__ w, double a, int n, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = w[i] * a;
+}
+// X[:, 0:ncols_out] = V[:, 0:m] * Y (m x ncols_out, column-major on device)
+__global__ void k_gemm_vy(const double* __restrict__ V, int64_t ld, int n, int m, const double* __restrict__ Y,
+                          int nout, double* __restrict__ X, int64_t ldx) {
+  extern __shared__ double ys[];  // [m][nout] chunk: we read Y directly
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int c = 0; c < nout; ++c) {
+    double s = 0.0;
+    for (int j = 0; j < m; ++j) s += V[i + j * ld] * Y[j + (int64_t)c * m];
+    X[i + c * ldx] = s;
+  }
+  (void)ys;
+}
+
+// ---------------------------------------------------------------------------
+// small dense symmetric eigensolver (host, FP64): Householder reduction to
+// tridiagonal form followed by the implicit QL algorithm with Wilkinson
+// shifts (the classical tred2 / tql2 procedures, written from the
+// published method).
+// ---------------------------------------------------------------------------
+namespace {
+
+void householder_tridiag(std::vector<double>& a, int n, std::vector<double>& d, std::vector<double>& e) {
+  // a: row-major n x n, on exit holds the orthogonal transform Q (a = Q)
+  d.assign(n, 0.0);
+  e.assign(n, 0.0);
+  for (int i = n - 1; i > 0; --i) {
+    int l = i - 1;
+    double h = 0.0, scale = 0.0;
+    if (l > 0) {
+      for (int k = 0; k <= l; ++k) scale += std::fabs(a[i * n + k]);
+      if (scale == 0.0) {
+        e[i] = a[i * n + l];
+      } else {
+        for (int k = 0; k <= l; ++k) {
+          a[i * n + k] /= scale;
+          h += a[i * n + k] * a[i * n + k];
+        }
+        double f = a[i * n + l];
+        double g = (f >= 0.0) ? -std::sqrt(h) : std::sqrt(h);
+        e[i] = scale * g;
+        h -= f * g;
+        a[i * n + l] = f - g;
+        f = 0.0;
+        for (int j = 0; j <= l; ++j) {
+          a[j * n + i] = a[i * n + j] / h;
+          g = 0.0;
+          for (int k = 0; k <= j; ++k) g += a[j * n + k] * a[i * n + k];
+          for (int k = j + 1; k <= l; ++k) g += a[k * n + j] * a[i * n + k];
+          e[j] = g / h;
+          f += e[j] * a[i * n + j];
+        }
+        double hh = f / (h + h);
+        for (int j = 0; j <= l; ++j) {
+          f = a[i * n + j];
+          e[j] = g = e[j] - hh * f;
+          for (int k = 0; k <= j; ++k) a[j * n + k] -= (f * e[k] + g * a[i * n + k]);
+        }
+      }
+    } else {
+      e[i] = a[i * n + l];
+    }
+    d[i] = h;
+  }
+  d[0] = 0.0;
+  e[0] = 0.0;
+  for (int i = 0; i < n; ++i) {
+    int l = i - 1;
+    if (d[i] != 0.0) {
+      for (int j = 0; j <= l; ++j) {
+        double g = 0.0;
+        for (int k = 0; k <= l; ++k) g += a[i * n + k] * a[k * n + j];
+        for (int k = 0; k <= l; ++k) a[k * n + j] -= g * a[k * n + i];
+      }
+    }
+    d[i] = a[i * n + i];
+    a[i * n + i] = 1.0;
+    for (int j = 0; j <= l; ++j) a[j * n + i] = a[i * n + j] = 0.0;
+  }
+}
+
+bool implicit_ql(std::vector<double>& d, std::vector<double>& e, int n, std::vector<double>& z) {
+  for (int i = 1; i < n; ++i) e[i - 1] = e[i];
+  e[n - 1] = 0.0;
+  for (int l = 0; l < n; ++l) {
+    int iter = 0, m;
+    do {
+      for (m = l; m < n - 1; ++m) {
+        double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(e[m]) <= 1e-300 + std::numeric_limits<double>::epsilon() * dd) break;
+      }
+      if (m != l) {
+        if (iter++ == 60) return false;
+        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+        double r = std::hypot(g, 1.0);
+        g = d[m] - d[l] + e[l] / (g + (g >= 0 ? std::fabs(r) : -std::fabs(r)));
+        double s = 1.0, c = 1.0, p = 0.0;
+        int i;
+        for (i = m - 1; i >= l; --i) {
+          double f = s * e[i], b = c * e[i];
+          e[i + 1] = (r = std::hypot(f, g));
+          if (r == 0.0) {
+            d[i + 1] -= p;
+            e[m] = 0.0;
+            break;
+          }
+          s = f / r;
+          c = g / r;
+          g = d[i + 1] - p;
+          r = (d[i] - g) * s + 2.0 * c * b;
+          d[i + 1] = g + (p = s * r);
+          g = c * r - b;
+          for (int k = 0; k < n; ++k) {
+            f = z[k * n + i + 1];
+            z[k * n + i + 1] = s * z[k * n + i] + c * f;
+            z[k * n + i] = c * z[k * n + i] - s * f;
+          }
+        }
+        if (r == 0.0 && i >= l) continue;
+        d[l] -= p;
+        e[l] = g;
+        e[m] = 0.0;
+      }
+    } while (m != l);
+  }
+  return true;
+}
+
+// eigen-decomposition of symmetric T (row-major m x m): ascending values,
+// vectors as columns of Z (row-major).
+bool sym_eig(const std::vector<double>& T, int m, std::vector<double>& w, std::vector<double>& Z) {
+  Z = T;
+  std::vector<double> e;
+  householder_tridiag(Z, m, w, e);
+  if (!implicit_ql(w, e, m, Z)) return false;
+  // sort ascending
+  std::vector<int> ord(m);
+  for (int i = 0; i < m; ++i) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](int a, int b) { return w[a] < w[b]; });
+  std::vector<double> w2(m), Z2((size_t)m * m);
+  for (int c = 0; c < m; ++c) {
+    w2[c] = w[ord[c]];
+    for (int r = 0; r < m; ++r) Z2[r * m + c] = Z[r * m + ord[c]];
+  }
+  w.swap(w2);
+  Z.swap(Z2);
+  return true;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// device-resident symmetric operator
+// ---------------------------------------------------------------------------
+struct SymOp {
+  int n = 0;
+  int64_t nnz = 0;
+  DevBuf rp, col, w, dinv;
+};
+
+static int build_symop(mds_ctx* ctx, int n, const int* dpcol, const int* dirow, const double* ddist, double sigma,
+                       SymOp& op) {
+  cudaStream_t s = ctx->stream;
+  op.n = n;
+  DevBuf cnt(ctx), pos(ctx), bad(ctx), k0(ctx), v0(ctx), k1(ctx), v1(ctx);
+  MDS_TRY(cnt.alloc(ctx, sizeof(int) * std::max(n, 1)));
+  MDS_TRY(pos.alloc(ctx, sizeof(int64_t) * (n + 1)));
+  MDS_TRY(bad.alloc(ctx, sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+  ctx->stats.launches += 2;
+  k_sym_count<<<(n + 255) / 256, 256, 0, s>>>(dpcol, dirow, n, cnt.as<int>());
+  k_scan_i64<<<1, 1024, 0, s>>>(cnt.as<int>(), n, pos.as<int64_t>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  int64_t m = 0;
+  MDS_CUDA(ctx, cudaMemcpyAsync(&m, pos.as<int64_t>() + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  op.nnz = m;
+  MDS_TRY(k0.alloc(ctx, sizeof(unsigned long long) * std::max<int64_t>(m, 1)));
+  MDS_TRY(v0.alloc(ctx, sizeof(int64_t) * std::max<int64_t>(m, 1)));
+  MDS_TRY(k1.alloc(ctx, sizeof(unsigned long long) * std::max<int64_t>(m, 1)));
+  MDS_TRY(v1.alloc(ctx, sizeof(int64_t) * std::max<int64_t>(m, 1)));
+  ctx->stats.launches++;
+  k_sym_expand<<<(n + 255) / 256, 256, 0, s>>>(dpcol, dirow, n, k0.as<unsigned long long>(), v0.as<int64_t>(),
+                                               pos.as<int64_t>(), bad.as<int>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  int hbad = 0;
+  MDS_CUDA(ctx, cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  if (hbad) return mds_fail(ctx, MDS_ERR_ARG, "row index outside [0, n) in the sparse matrix");
+  int bits = 0;
+  while ((1ll << bits) < (int64_t)n) ++bits;
+  unsigned long long mask = ((1ull << bits) - 1ull) | (((1ull << bits) - 1ull) << 32);
+  int which = 0;
+  MDS_TRY(radix_sort(ctx, k0.as<unsigned long long>(), v0.as<int64_t>(), k1.as<unsigned long long>(),
+                     v1.as<int64_t>(), m, mask, &which));
+  unsigned long long* keys = which ? k1.as<unsigned long long>() : k0.as<unsigned long long>();
+  int64_t* vals = which ? v1.as<int64_t>() : v0.as<int64_t>();
+  MDS_TRY(op.rp.alloc(ctx, sizeof(int64_t) * (n + 1)));
+  MDS_TRY(op.col.alloc(ctx, sizeof(int) * std::max<int64_t>(m, 1)));
+  MDS_TRY(op.w.alloc(ctx, sizeof(double) * std::max<int64_t>(m, 1)));
+  MDS_TRY(op.dinv.alloc(ctx, sizeof(double) * std::max(n, 1)));
+  const int wb = (int)(((int64_t)n * 32 + 255) / 256);
+  ctx->stats.launches += 3;
+  k_rowptr<<<(n + 1 + 255) / 256, 256, 0, s>>>(keys, m, n, op.rp.as<int64_t>());
+  k_sym_degree<<<wb, 256, 0, s>>>(keys, vals, op.rp.as<int64_t>(), ddist, n, 1.0 / (2.0 * sigma * sigma),
+                                  op.col.as<int>(), op.w.as<double>(), op.dinv.as<double>());
+  k_sym_normalise<<<wb, 256, 0, s>>>(op.rp.as<int64_t>(), op.col.as<int>(), op.dinv.as<double>(), n,
+                                     op.w.as<double>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+static void spmv(mds_ctx* ctx, const SymOp& op, const double* x, double* y) {
+  ctx->stats.launches++;
+  k_spmv<<<(int)(((int64_t)op.n * 32 + 255) / 256), 256, 0, ctx->stream>>>(op.rp.as<int64_t>(), op.col.as<int>(),
+                                                                           op.w.as<double>(), x, op.n, y);
+}
+
+// ---------------------------------------------------------------------------
+// 3. thick-restart Lanczos
+// ---------------------------------------------------------------------------
+struct LanczosOut {
+  std::vector<double> evals;  // descending
+  int nconv = 0;
+  int restarts = 0;
+  int matvecs = 0;
+};
+
+static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, int maxiter, double* dX /*n*nev*/,
+                   LanczosOut& out) {
+  cudaStream_t s = ctx->stream;
+  const int n = op.n;
+  const int m = ncv;
+  const int64_t ld = n;
+  DevBuf V(ctx), wv(ctx), h(ctx), part(ctx), Yd(ctx), tmp(ctx);
+  MDS_TRY(V.alloc(ctx, sizeof(double) * (size_t)n * (m + 1)));
+  MDS_TRY(wv.alloc(ctx, sizeof(double) * n));
+  MDS_TRY(h.alloc(ctx, sizeof(double) * (m + 1)));
+  const int nparts = (n + GV_ROWS - 1) / GV_ROWS;
+  MDS_TRY(part.alloc(ctx, sizeof(double) * (size_t)nparts * (m + 1)));
+  MDS_TRY(Yd.alloc(ctx, sizeof(double) * (size_t)m * m));
+  MDS_TRY(tmp.alloc(ctx, sizeof(double) * (size_t)n * m));
+  double* Vp = V.as<double>();
+  double* w = wv.as<double>();
+  const double eps = std::numeric_limits<double>::epsilon();
+  const double eps23 = std::pow(eps, 2.0 / 3.0);
+  if (tol <= 0.0) tol = eps;
+
+  auto dots = [&](int ncols, std::vector<double>& hh) -> int {
+    ctx->stats.launches += 2;
+    k_gemv_t_part<<<nparts, 256, 0, s>>>(Vp, ld, n, ncols, w, part.as<double>());
+    k_reduce_part<<<(ncols + 127) / 128, 128, 0, s>>>(part.as<double>(), nparts, ncols, h.as<double>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    hh.resize(ncols);
+    MDS_CUDA(ctx, cudaMemcpyAsync(hh.data(), h.p, sizeof(double) * ncols, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    return MDS_OK;
+  };
+  auto subtract = [&](int ncols, const std::vector<double>& hh) -> int {
+    MDS_CUDA(ctx, cudaMemcpyAsync(h.p, hh.data(), sizeof(double) * ncols, cudaMemcpyHostToDevice, s));
+    ctx->stats.launches++;
+    k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * ncols, s>>>(Vp, ld, n, ncols, h.as<double>(), w);
+    MDS_CUDA(ctx, cudaGetLastError());
+    return MDS_OK;
+  };
+  auto norm_w = [&](double* nr) -> int {
+    // ||w|| through the same partial-sum kernels (V column = w itself)
+    ctx->stats.launches += 2;
+    k_gemv_t_part<<<nparts, 256, 0, s>>>(w, ld, n, 1, w, part.as<double>());
+    k_reduce_part<<<1, 128, 0, s>>>(part.as<double>(), nparts, 1, h.as<double>());
+    double v = 0;
+    MDS_CUDA(ctx, cudaMemcpyAsync(&v, h.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    *nr = std::sqrt(std::max(v, 0.0));
+    return MDS_OK;
+  };
+  // start vector: fixed-seed pseudo-random, orthogonalised and normalised
+  {
+    std::vector<double> v0(n);
+    uint64_t st = 0x9E3779B97F4A7C15ull;
+    for (int i = 0; i < n; ++i) {
+      st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+      v0[i] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    }
+    MDS_CUDA(ctx, cudaMemcpyAsync(w, v0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    double nr = 0;
+    MDS_TRY(norm_w(&nr));
+    ctx->stats.launches++;
+    k_scale_copy<<<(n + 255) / 256, 256, 0, s>>>(w, 1.0 / nr, n, Vp);
+  }
+  int k = 0;
+  std::vector<double> theta_k, s_k;  // kept Ritz values and couplings
+  std::vector<double> alpha(m, 0.0), beta(m, 0.0);
+  std::vector<double> hh, hh2, T, Z, th;
+  int restart = 0;
+  for (;; ++restart) {
+    for (int j = k; j < m; ++j) {
+      spmv(ctx, op, Vp + (int64_t)j * ld, w);
+      out.matvecs++;
+      // full reorthogonalisation against v_0..v_j (twice); alpha_j = v_j . Av_j
+      MDS_TRY(dots(j + 1, hh));
+      alpha[j] = hh[j];
+      MDS_TRY(subtract(j + 1, hh));
+      MDS_TRY(dots(j + 1, hh2));
+      MDS_TRY(subtract(j + 1, hh2));
+      alpha[j] += hh2[j];
+      double b = 0;
+      MDS_TRY(norm_w(&b));
+      beta[j] = b;
+      double scale = std::max(std::fabs(alpha[j]), 1.0);
+      if (b <= eps * scale * 10.0) {
+        // invariant subspace: continue with a fresh direction orthogonal to V
+        std::vector<double> v0(n);
+        uint64_t st = 0xD1B54A32D192ED03ull + 7919ull * (uint64_t)(j + 1 + restart * m);
+        for (int i = 0; i < n; ++i) {
+          st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+          v0[i] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+        }
+        MDS_CUDA(ctx, cudaMemcpyAsync(w, v0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        for (int rep = 0; rep < 2; ++rep) {
+          MDS_TRY(dots(j + 1, hh));
+          MDS_TRY(subtract(j + 1, hh));
+        }
+        double nr = 0;
+        MDS_TRY(norm_w(&nr));
+        beta[j] = 0.0;
+        ctx->stats.launches++;
+        k_scale_copy<<<(n + 255) / 256, 256, 0, s>>>(w, 1.0 / nr, n, Vp + (int64_t)(j + 1) * ld);
+      } else {
+        ctx->stats.launches++;
+        k_scale_copy<<<(n + 255) / 256, 256, 0, s>>>(w, 1.0 / b, n, Vp + (int64_t)(j + 1) * ld);
+      }
+    }
+    // projected matrix: arrowhead (kept Ritz pairs) + tridiagonal
+    T.assign((size_t)m * m, 0.0);
+    for (int i = 0; i < k; ++i) {
+      T[i * m + i] = theta_k[i];
+      T[i * m + k] = T[k * m + i] = s_k[i];
+    }
+    for (int j = k; j < m; ++j) {
+      T[j * m + j] = alpha[j];
+      if (j + 1 < m) T[j * m + j + 1] = T[(j + 1) * m + j] = beta[j];
+    }
+    if (!sym_eig(T, m, th, Z)) return mds_fail(ctx, MDS_ERR_INTERNAL, "projected eigenproblem did not converge");
+    const double bm = beta[m - 1];
+    // wanted: the nev largest (ascending order -> last nev)
+    int nconv = 0;
+    for (int c = m - nev; c < m; ++c) {
+      double est = std::fabs(bm * Z[(m - 1) * m + c]);
+      if (est <= tol * std::max(eps23, std::fabs(th[c]))) ++nconv;
+    }
+    out.nconv = nconv;
+    if (nconv >= nev || restart >= maxiter) {
+      // Ritz vectors of the wanted values, descending
+      std::vector<double> Y((size_t)m * nev);
+      out.evals.resize(nev);
+      for (int x = 0; x < nev; ++x) {
+        int c = m - 1 - x;
+        out.evals[x] = th[c];
+        for (int r = 0; r < m; ++r) Y[r + (size_t)x * m] = Z[r * m + c];
+      }
+      MDS_CUDA(ctx, cudaMemcpyAsync(Yd.p, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice, s));
+      ctx->stats.launches++;
+      k_gemm_vy<<<(n + 127) / 128, 128, 0, s>>>(Vp, ld, n, m, Yd.as<double>(), nev, dX, n);
+      MDS_CUDA(ctx, cudaGetLastError());
+      out.restarts = restart;
+      return MDS_OK;
+    }
+    // thick restart with the kk largest Ritz pairs
+    int kk = std::min(m - 2, nev + std::max(nconv, (m - nev) / 2));
+    kk = std::max(kk, nev);
+    std::vector<double> Y((size_t)m * kk);
+    theta_k.assign(kk, 0.0);
+    s_k.assign(kk, 0.0);
+    for (int x = 0; x < kk; ++x) {
+      int c = m - kk + x;
+      theta_k[x] = th[c];
+      s_k[x] = bm * Z[(m - 1) * m + c];
+      for (int r = 0; r < m; ++r) Y[r + (size_t)x * m] = Z[r * m + c];
+    }
+    MDS_CUDA(ctx, cudaMemcpyAsync(Yd.p, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice, s));
+    ctx->stats.launches++;
+    k_gemm_vy<<<(n + 127) / 128, 128, 0, s>>>(Vp, ld, n, m, Yd.as<double>(), kk, tmp.as<double>(), n);
+    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_CUDA(ctx, cudaMemcpyAsync(Vp, tmp.p, sizeof(double) * (size_t)n * kk, cudaMemcpyDeviceToDevice, s));
+    MDS_CUDA(ctx, cudaMemcpyAsync(Vp + (int64_t)kk * ld, Vp + (int64_t)m * ld, sizeof(double) * n,
+                                  cudaMemcpyDeviceToDevice, s));
+    k = kk;
+  }
+}
+
+// residual ||A z - lambda z|| / |lambda| for each vector
+__global__ void k_resid_part(const double* __restrict__ Az, const double* __restrict__ z, double lam, int n,
+                             double* __restrict__ part) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double r = Az[i] - lam * z[i];
+    s += r * r;
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// ---------------------------------------------------------------------------
+// 5. Nystrom
+// ---------------------------------------------------------------------------
+// B affinity: w = exp(-d^2/2s^2); d_b[q] = (sum of column q)^-1/2;
+// B[l,q] = w * d_a[l] * d_b[q]   (one warp per column q)
+__global__ void k_nystrom_b(const int* __restrict__ pcol, const int* __restrict__ irow, const double* __restrict__ dist,
+                            int m, int n, double inv2s2, const double* __restrict__ dinv_a, double* __restrict__ B,
+                            int* __restrict__ bad) {
+  int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (q >= m) return;
+  double s = 0.0;
+  for (int p = pcol[q] + lane; p < pcol[q + 1]; p += 32) {
+    double d = dist[p];
+    double a = exp(-(d * d) * inv2s2);
+    B[p] = a;
+    s += a;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  double db = 1.0 / sqrt(s);
+  for (int p = pcol[q] + lane; p < pcol[q + 1]; p += 32) {
+    int l = irow[p];
+    if (l < 0 || l >= n) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    B[p] *= dinv_a[l] * db;
+  }
+}
+// ext[x][q] = sum_{p in col q} B[p] z_x[irow[p]] / lambda_x, all x at once
+__global__ void k_nystrom_ext(const int* __restrict__ pcol, const int* __restrict__ irow, const double* __restrict__ B,
+                              int m, int n, const double* __restrict__ Z, const double* __restrict__ inv_lam, int nev,
+                              double* __restrict__ ext) {
+  int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (q >= m) return;
+  for (int x = 0; x < nev; ++x) {
+    double s = 0.0;
+    for (int p = pcol[q] + lane; p < pcol[q + 1]; p += 32) s += B[p] * Z[(int64_t)x * n + irow[p]];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) ext[(int64_t)x * m + q] = s * inv_lam[x];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+static int decomp_impl(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow, const double* dist, double sigma,
+                       int nev, int ncv, double tol, int maxiter, unsigned flags, double* evals, double* evecs,
+                       double* resid, int* nconv, int m, const int32_t* pcolB, const int32_t* irowB,
+                       const double* distB, double* ext) {
+  if (!ctx) return MDS_ERR_ARG;
+  ctx->stats = mds_knn_stats{};
+  if (!pcol || !irow || !dist || !evals || !evecs) return mds_fail(ctx, MDS_ERR_ARG, "null argument");
+  if (n < 1 || nev < 1) return mds_fail(ctx, MDS_ERR_ARG, "invalid sizes n=%d nev=%d", n, nev);
+  if (!(sigma > 0.0)) return mds_fail(ctx, MDS_ERR_ARG, "sigma must be positive");
+  // decomp_sparse.cpp:199-205: ncv = min(10 nev + 1, n), maxiter = 100 nev
+  if (ncv <= 0) ncv = std::min(10 * nev + 1, n);
+  ncv = std::min(ncv, n);
+  if (maxiter <= 0) maxiter = 100 * nev;
+  if (nev >= ncv) return mds_fail(ctx, MDS_ERR_ARG, "need nev < ncv <= n (nev=%d ncv=%d n=%d)", nev, ncv, n);
+  if (ncv > 4096) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "ncv=%d too large", ncv);
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const bool dev = (flags & MDS_DEVICE_IO) != 0;
+  std::vector<int> hp;
+  const int* hpcol = pcol;
+  if (dev) {
+    hp.resize(n + 1);
+    MDS_CUDA(ctx, cudaMemcpyAsync(hp.data(), pcol, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    hpcol = hp.data();
+  }
+  const int64_t nnz = hpcol[n];
+  if (nnz < 0 || hpcol[0] != 0) return mds_fail(ctx, MDS_ERR_ARG, "malformed column pointers");
+  for (int c = 0; c < n; ++c)
+    if (hpcol[c + 1] < hpcol[c]) return mds_fail(ctx, MDS_ERR_ARG, "column pointers not ascending at %d", c);
+  DevBuf dp(ctx), dr(ctx), dd(ctx), dX(ctx);
+  const int* ppcol = pcol;
+  const int* pirow = irow;
+  const double* pdist = dist;
+  if (!dev) {
+    MDS_TRY(dp.alloc(ctx, sizeof(int) * (n + 1)));
+    MDS_TRY(dr.alloc(ctx, sizeof(int) * std::max<int64_t>(nnz, 1)));
+    MDS_TRY(dd.alloc(ctx, sizeof(double) * std::max<int64_t>(nnz, 1)));
+    MDS_CUDA(ctx, cudaMemcpyAsync(dp.p, pcol, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+    if (nnz) {
+      MDS_CUDA(ctx, cudaMemcpyAsync(dr.p, irow, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+      MDS_CUDA(ctx, cudaMemcpyAsync(dd.p, dist, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
+    }
+    ppcol = dp.as<int>();
+    pirow = dr.as<int>();
+    pdist = dd.as<double>();
+  }
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  SymOp op;
+  MDS_TRY(build_symop(ctx, n, ppcol, pirow, pdist, sigma, op));
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  double* pX = evecs;
+  if (!dev) {
+    MDS_TRY(dX.alloc(ctx, sizeof(double) * (size_t)n * nev));
+    pX = dX.as<double>();
+  }
+  LanczosOut lo;
+  MDS_TRY(lanczos(ctx, op, nev, ncv, tol, maxiter, pX, lo));
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  for (int x = 0; x < nev; ++x) evals[x] = lo.evals[x];
+  if (nconv) *nconv = lo.nconv;
+  // residuals
+  if (resid) {
+    DevBuf Az(ctx), part(ctx);
+    MDS_TRY(Az.alloc(ctx, sizeof(double) * n));
+    MDS_TRY(part.alloc(ctx, sizeof(double) * 256));
+    for (int x = 0; x < nev; ++x) {
+      spmv(ctx, op, pX + (int64_t)x * n, Az.as<double>());
+      ctx->stats.launches++;
+      k_resid_part<<<256, 256, 0, s>>>(Az.as<double>(), pX + (int64_t)x * n, lo.evals[x], n, part.as<double>());
+      std::vector<double> hpart(256);
+      MDS_CUDA(ctx, cudaMemcpyAsync(hpart.data(), part.p, sizeof(double) * 256, cudaMemcpyDeviceToHost, s));
+      MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      double ss = 0;
+      for (double v : hpart) ss += v;
+      resid[x] = std::sqrt(ss) / std::fabs(lo.evals[x]);
+    }
+  }
+  // Nystrom extension
+  if (m > 0 && ext) {
+    if (!pcolB || !irowB || !distB) return mds_fail(ctx, MDS_ERR_ARG, "null Nystrom argument");
+    std::vector<int> hpB;
+    const int* hpcolB = pcolB;
+    if (dev) {
+      hpB.resize(m + 1);
+      MDS_CUDA(ctx, cudaMemcpyAsync(hpB.data(), pcolB, sizeof(int) * (m + 1), cudaMemcpyDeviceToHost, s));
+      MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      hpcolB = hpB.data();
+    }
+    const int64_t nnzB = hpcolB[m];
+    DevBuf bp(ctx), br(ctx), bd(ctx), B(ctx), il(ctx), de(ctx), bad(ctx);
+    const int* qp = pcolB;
+    const int* qr = irowB;
+    const double* qd = distB;
+    if (!dev) {
+      MDS_TRY(bp.alloc(ctx, sizeof(int) * (m + 1)));
+      MDS_TRY(br.alloc(ctx, sizeof(int) * std::max<int64_t>(nnzB, 1)));
+      MDS_TRY(bd.alloc(ctx, sizeof(double) * std::max<int64_t>(nnzB, 1)));
+      MDS_CUDA(ctx, cudaMemcpyAsync(bp.p, pcolB, sizeof(int) * (m + 1), cudaMemcpyHostToDevice, s));
+      if (nnzB) {
+        MDS_CUDA(ctx, cudaMemcpyAsync(br.p, irowB, sizeof(int) * nnzB, cudaMemcpyHostToDevice, s));
+        MDS_CUDA(ctx, cudaMemcpyAsync(bd.p, distB, sizeof(double) * nnzB, cudaMemcpyHostToDevice, s));
+      }
+      qp = bp.as<int>();
+      qr = br.as<int>();
+      qd = bd.as<double>();
+    }
+    MDS_TRY(B.alloc(ctx, sizeof(double) * std::max<int64_t>(nnzB, 1)));
+    MDS_TRY(il.alloc(ctx, sizeof(double) * nev));
+    MDS_TRY(bad.alloc(ctx, sizeof(int)));
+    MDS_CUDA(ctx, cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+    std::vector<double> inv(nev);
+    for (int x = 0; x < nev; ++x) inv[x] = 1.0 / lo.evals[x];
+    MDS_CUDA(ctx, cudaMemcpyAsync(il.p, inv.data(), sizeof(double) * nev, cudaMemcpyHostToDevice, s));
+    double* pext = ext;
+    if (!dev) {
+      MDS_TRY(de.alloc(ctx, sizeof(double) * (size_t)m * nev));
+      pext = de.as<double>();
+    }
+    const int wb = (int)(((int64_t)m * 32 + 255) / 256);
+    ctx->stats.launches += 2;
+    k_nystrom_b<<<wb, 256, 0, s>>>(qp, qr, qd, m, n, 1.0 / (2.0 * sigma * sigma), op.dinv.as<double>(),
+                                   B.as<double>(), bad.as<int>());
+    k_nystrom_ext<<<wb, 256, 0, s>>>(qp, qr, B.as<double>(), m, n, pX, il.as<double>(), nev, pext);
+    MDS_CUDA(ctx, cudaGetLastError());
+    int hbad = 0;
+    MDS_CUDA(ctx, cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (!dev) MDS_CUDA(ctx, cudaMemcpyAsync(ext, pext, sizeof(double) * (size_t)m * nev, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    if (hbad) return mds_fail(ctx, MDS_ERR_ARG, "landmark index outside [0, n) in the general sparse matrix");
+  }
+  if (!dev) MDS_CUDA(ctx, cudaMemcpyAsync(evecs, pX, sizeof(double) * (size_t)n * nev, cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  float a = 0, b = 0;
+  cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+  ctx->stats.prep_ms = a;
+  ctx->stats.screen_ms = b;  // eigensolve time
+  ctx->stats.passes = lo.restarts;
+  ctx->stats.pairs = lo.matvecs;
+  return MDS_OK;
+}
+
+extern "C" int mds_decomp_sparse(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow, const double* dist,
+                                 double sigma, int nev, int ncv, double tol, int maxiter, unsigned flags,
+                                 double* evals, double* evecs, double* resid, int* nconv) {
+  return decomp_impl(ctx, n, pcol, irow, dist, sigma, nev, ncv, tol, maxiter, flags, evals, evecs, resid, nconv, 0,
+                     nullptr, nullptr, nullptr, nullptr);
+}
+
+extern "C" int mds_decomp_sparse_nystrom(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow,
+                                         const double* dist, int m, const int32_t* pcolB, const int32_t* irowB,
+                                         const double* distB, double sigma, int nev, int ncv, double tol, int maxiter,
+                                         unsigned flags, double* evals, double* evecs, double* ext, double* resid,
+                                         int* nconv) {
+  if (m < 0) return mds_fail(ctx, MDS_ERR_ARG, "m must be >= 0");
+  return decomp_impl(ctx, n, pcol, irow, dist, sigma, nev, ncv, tol, maxiter, flags, evals, evecs, resid, nconv, m,
+                     pcolB, irowB, distB, ext);
+}

@@ -13,14 +13,22 @@ struct KnnRmsPlan {
   unsigned prec = MDS_PREC_FP32;
   float guard_fp32 = 0.f;  // lower-bound margin per unit of |a_i|^2+|a_j|^2
   float guard_tc = 0.f;
+  // diagnostic mode (mds_knn_rms_screen): stop after the screen, one column
+  // segment, and copy the candidate lists to these host buffers
+  uint64_t* screen_keys = nullptr;  // [nfit][kprime]
+  int* screen_counts = nullptr;     // [nfit]
+  // diagnostic mode (mds_knn_rms_superpose): stop after the superposition
+  // onto the template and copy the reference set's deviations and records
+  float* prep_dev = nullptr;  // [nref][3][Ap]
+  float* prep_rec = nullptr;  // [nref][16]
 };
 
 // Split hi/lo tensor-core operands of one frame set (knn_rms_tc.cu).
 struct TcOperands {
-  DevBuf buf;      // [ntiles][K][rows] packed tiles
+  DevBuf A, B;     // row-tile (fit role) and column-tile (reference role) layouts
   int n = 0;       // frames
-  int rows = 0;    // padded operand rows
-  int K = 0;       // padded reduction length per split part
+  int rowsA = 0, rowsB = 0;
+  int K = 0;       // padded atoms per split part (row length is 2K: hi | lo)
 };
 
 __device__ __forceinline__ void warp_bitonic_sort(uint64_t* a, int n, int P2, int lane) {
@@ -72,7 +80,8 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
                 const float* hmass, double* dout_d, int* dout_i);
 
 // tensor-core screen (knn_rms_tc.cu)
-int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op);
+int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout);
+int tc_seg_stride();
 int tc_choose_nseg(mds_ctx* ctx, const KnnRmsPlan& pl, int nfit);
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,

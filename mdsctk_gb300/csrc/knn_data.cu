@@ -1,0 +1,503 @@
+// knn_data.cu -- k nearest vectors (knn_data) on sm_103a.
+//
+// Replaces the compute core of knn_data.cpp:176-250 with
+// euclidean_distance (mdsctk.cpp:330-335) or correlation_distance
+// (mdsctk.cpp:337-360).
+//
+//  1. k_vec_prep   per vector: FP32 copy (screen operand), squared norm, and
+//                  for the correlation metric the reference's own sums in its
+//                  order (sum, sum of squares -> mean and scale) and the
+//                  standardized FP32 vector.
+//  2. k_screen_dot all pairs: FP32 dot products on CUDA cores (64 x 64 tile,
+//                  4 x 4 pairs per thread), screen value = lower bound of the
+//                  squared distance (Euclidean: |x|^2 + |y|^2 - 2 x.y, minus a
+//                  rounding guard; correlation: (1 - r)/2 minus a guard),
+//                  fused per-row top-K' in shared memory.
+//  3. k_data_recheck merge the column segments, recompute every candidate in
+//                  FP64 with the reference's exact operation order (no fused
+//                  multiply-add, sequential sum), select k+1 by (value, index),
+//                  drop position 0, verify the guard.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "knn_common.cuh"
+
+#define DT_TM 64
+#define DT_TN 64
+#define DT_KC 32
+#define DT_THREADS 256
+#define DT_FS 36  // floats per vector per stage (32 + 4: bank spread, 16-byte rows)
+
+// ---------------------------------------------------------------------------
+// 1. per-vector preparation
+// ---------------------------------------------------------------------------
+// X [n][dim] double -> Xf [n][Dp] float (plain or standardized), nrm[n]
+// (float squared norm of the screen operand), mean/scale (double, for the
+// correlation recheck).
+__global__ void k_vec_prep(const double* __restrict__ X, int n, int dim, int Dp, int corr,
+                           float* __restrict__ Xf, float* __restrict__ nrm, double* __restrict__ mean,
+                           double* __restrict__ scale) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const double* x = X + (int64_t)v * dim;
+  float* o = Xf + (int64_t)v * Dp;
+  if (!corr) {
+    float s = 0.f;
+    for (int i = 0; i < dim; ++i) {
+      float f = (float)x[i];
+      o[i] = f;
+      s = fmaf(f, f, s);
+    }
+    for (int i = dim; i < Dp; ++i) o[i] = 0.f;
+    nrm[v] = s;
+    return;
+  }
+  // the reference's single-pass sums (correlation_distance, mdsctk.cpp:339-351)
+  double sum = 0.0, sq = 0.0, dsize = (double)dim;
+  for (int i = 0; i < dim; ++i) {
+    sum = __dadd_rn(sum, x[i]);
+    sq = __dadd_rn(sq, __dmul_rn(x[i], x[i]));
+  }
+  double sd = sqrt(__ddiv_rn(__dsub_rn(__dmul_rn(dsize, sq), __dmul_rn(sum, sum)),
+                             __dmul_rn(dsize, __dsub_rn(dsize, 1.0))));
+  double mu = __ddiv_rn(sum, dsize);
+  mean[v] = mu;
+  scale[v] = sd;
+  // standardized screen operand: z = (x - mean) / (sd * sqrt(dim - 1)), so r = z_a . z_b
+  double inv = (sd > 0.0) ? 1.0 / (sd * sqrt(dsize - 1.0)) : 0.0;
+  float s = 0.f;
+  for (int i = 0; i < dim; ++i) {
+    float f = (float)((x[i] - mu) * inv);
+    o[i] = f;
+    s = fmaf(f, f, s);
+  }
+  for (int i = dim; i < Dp; ++i) o[i] = 0.f;
+  nrm[v] = s;
+}
+
+// ---------------------------------------------------------------------------
+// 2. screen
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cpa16(void* smem, const void* gmem, bool valid) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  int sz = valid ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
+
+__global__ void __launch_bounds__(DT_THREADS, 1)
+k_screen_dot(const float* __restrict__ Xf, const float* __restrict__ Xr, const float* __restrict__ nf,
+             const float* __restrict__ nr, int nrows, const int* __restrict__ rowlist, int Nr, int Dp,
+             int corr, float guard, int Kp, int nseg, uint64_t* __restrict__ cand, int* __restrict__ cand_n) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* sf = reinterpret_cast<float*>(smem_raw);        // [2][64*36]
+  float* sr = sf + 2 * DT_TM * DT_FS;                     // [2][64*36]
+  float* snr = sr + 2 * DT_TN * DT_FS;                    // [64]
+  int* scnt = reinterpret_cast<int*>(snr + DT_TN);        // [64]
+  float* sthr = reinterpret_cast<float*>(scnt + DT_TM);   // [64]
+  uint64_t* pool = reinterpret_cast<uint64_t*>(sthr + DT_TM);
+  const int P2 = next_pow2(Kp + DT_TN);
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4, lane = tid & 31, warp = tid >> 5;
+  const int rt = blockIdx.x / nseg, seg = blockIdx.x % nseg;
+  const int row0 = rt * DT_TM;
+  const int ntiles = (Nr + DT_TN - 1) / DT_TN;
+  const int t0 = (int)((int64_t)ntiles * seg / nseg), t1 = (int)((int64_t)ntiles * (seg + 1) / nseg);
+  int grow[4];
+  float rn[4];
+  for (int p = 0; p < 4; ++p) {
+    int lr = row0 + ty + 16 * p;
+    grow[p] = (lr < nrows) ? (rowlist ? rowlist[lr] : lr) : -1;
+    rn[p] = grow[p] >= 0 ? nf[grow[p]] : 0.f;
+  }
+  if (tid < DT_TM) {
+    scnt[tid] = 0;
+    sthr[tid] = __int_as_float(0x7f800000);
+  }
+  const int nch = Dp / DT_KC;
+  auto load = [&](int stage, int tile, int kc) {
+    float* df = sf + stage * DT_TM * DT_FS;
+    float* dr = sr + stage * DT_TN * DT_FS;
+    for (int e = tid; e < DT_TM * 8; e += DT_THREADS) {
+      int v = e >> 3, h = e & 7;
+      int lr = row0 + v;
+      int g = (lr < nrows) ? (rowlist ? rowlist[lr] : lr) : -1;
+      cpa16(df + v * DT_FS + 4 * h, Xf + (int64_t)(g < 0 ? 0 : g) * Dp + kc * DT_KC + 4 * h, g >= 0);
+    }
+    for (int e = tid; e < DT_TN * 8; e += DT_THREADS) {
+      int v = e >> 3, h = e & 7;
+      int j = tile * DT_TN + v;
+      cpa16(dr + v * DT_FS + 4 * h, Xr + (int64_t)(j < Nr ? j : 0) * Dp + kc * DT_KC + 4 * h, j < Nr);
+    }
+  };
+  for (int tile = t0; tile < t1; ++tile) {
+    __syncthreads();
+    if (tid < DT_TN) {
+      int j = tile * DT_TN + tid;
+      snr[tid] = (j < Nr) ? nr[j] : 0.f;
+    }
+    float acc[4][4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = 0.f;
+    load(0, tile, 0);
+    asm volatile("cp.async.commit_group;\n" ::);
+    for (int kc = 0; kc < nch; ++kc) {
+      if (kc + 1 < nch) {
+        load((kc + 1) & 1, tile, kc + 1);
+        asm volatile("cp.async.commit_group;\n" ::);
+        asm volatile("cp.async.wait_group 1;\n" ::);
+      } else {
+        asm volatile("cp.async.wait_group 0;\n" ::);
+      }
+      __syncthreads();
+      const float* df = sf + (kc & 1) * DT_TM * DT_FS;
+      const float* dr = sr + (kc & 1) * DT_TN * DT_FS;
+#pragma unroll
+      for (int a = 0; a < DT_KC; a += 4) {
+        float4 fv[4], rv[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) fv[p] = *reinterpret_cast<const float4*>(df + (ty + 16 * p) * DT_FS + a);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) rv[q] = *reinterpret_cast<const float4*>(dr + (tx + 16 * q) * DT_FS + a);
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            acc[p][q] = fmaf(fv[p].x, rv[q].x, acc[p][q]);
+            acc[p][q] = fmaf(fv[p].y, rv[q].y, acc[p][q]);
+            acc[p][q] = fmaf(fv[p].z, rv[q].z, acc[p][q]);
+            acc[p][q] = fmaf(fv[p].w, rv[q].w, acc[p][q]);
+          }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      if (grow[p] < 0) continue;
+      int lr = ty + 16 * p;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        int j = tile * DT_TN + tx + 16 * q;
+        if (j >= Nr) continue;
+        float cn = snr[tx + 16 * q];
+        float s = corr ? 0.5f * (1.0f - acc[p][q]) : rn[p] + cn - 2.0f * acc[p][q];
+        s = fmaxf(s - guard * (rn[p] + cn), 0.0f);
+        if (s < sthr[lr]) {
+          int pos = atomicAdd(&scnt[lr], 1);
+          pool[lr * P2 + pos] = mds_pack_key(s, j);
+        }
+      }
+    }
+    __syncthreads();
+    for (int r = warp; r < DT_TM; r += DT_THREADS / 32) {
+      int n = scnt[r];
+      if (n <= Kp) continue;
+      warp_bitonic_sort(pool + r * P2, n, P2, lane);
+      if (lane == 0) {
+        scnt[r] = Kp;
+        sthr[r] = mds_key_value(pool[r * P2 + Kp - 1]);
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int r = warp; r < DT_TM; r += DT_THREADS / 32) {
+    int lr = row0 + r;
+    if (lr >= nrows) continue;
+    int n = min(scnt[r], Kp);
+    warp_bitonic_sort(pool + r * P2, scnt[r], P2, lane);
+    uint64_t* dst = cand + ((int64_t)lr * nseg + seg) * Kp;
+    for (int x = lane; x < n; x += 32) dst[x] = pool[r * P2 + x];
+    if (lane == 0) cand_n[(int64_t)lr * nseg + seg] = n;
+  }
+}
+
+static size_t screen_dot_smem(int Kp) {
+  return sizeof(float) * (2 * DT_TM * DT_FS + 2 * DT_TN * DT_FS + DT_TN) + sizeof(int) * DT_TM +
+         sizeof(float) * DT_TM + sizeof(uint64_t) * DT_TM * next_pow2(Kp + DT_TN);
+}
+
+// ---------------------------------------------------------------------------
+// 3. exact recheck in the reference's arithmetic
+// ---------------------------------------------------------------------------
+// euclidean_distance(size, reference=fit row a, fitting=ref row b)
+__device__ __forceinline__ double exact_euclid(const double* a, const double* b, int dim) {
+  double value = 0.0;
+  for (int x = 0; x < dim; ++x) {
+    double t = __dsub_rn(a[x], b[x]);
+    value = __dadd_rn(value, __dmul_rn(t, t));
+  }
+  return value;  // squared; sqrt taken by the caller
+}
+// correlation_distance with per-vector means/scales precomputed by k_vec_prep
+__device__ __forceinline__ double exact_corr(const double* a, double ma, double sa, const double* b, double mb,
+                                             double sb, int dim) {
+  double dsize = (double)dim, value = 0.0;
+  for (int x = 0; x < dim; ++x) value = __dadd_rn(value, __dmul_rn(__dsub_rn(a[x], ma), __dsub_rn(b[x], mb)));
+  value = __ddiv_rn(__dsub_rn(1.0, __ddiv_rn(value, __dmul_rn(__dmul_rn(__dsub_rn(dsize, 1.0), sa), sb))), 2.0);
+  if (value < 0.0) value = 0.0;
+  return value;  // squared distance; sqrt taken by the caller
+}
+
+#define DR_THREADS 256
+
+// One block per fit row. mode 0: candidates from the screen; mode 1: every
+// reference (exact row); mode 2: full row output in reference order.
+__global__ void __launch_bounds__(DR_THREADS)
+k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref, const double* __restrict__ mf,
+               const double* __restrict__ sfv, const double* __restrict__ mr, const double* __restrict__ srv,
+               const float* __restrict__ nf, int nrows, const int* __restrict__ rowlist, int Nr, int dim, int corr,
+               int mode, const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int Kp, int k,
+               double* __restrict__ out_d, int* __restrict__ out_i, int* __restrict__ flagged,
+               int* __restrict__ nflag) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sa = reinterpret_cast<double*>(smem_raw);              // [dim]
+  uint64_t* keys = reinterpret_cast<uint64_t*>(sa + dim);        // merge buffer, then candidates
+  __shared__ int s_total;
+  const int lr = blockIdx.x;
+  if (lr >= nrows) return;
+  const int grow = rowlist ? rowlist[lr] : lr;
+  for (int e = threadIdx.x; e < dim; e += blockDim.x) sa[e] = Xfit[(int64_t)grow * dim + e];
+  const double ma = corr ? mf[grow] : 0.0, sda = corr ? sfv[grow] : 0.0;
+  const int k1 = k + 1;
+  __syncthreads();
+  if (mode == 2) {
+    for (int j = threadIdx.x; j < Nr; j += blockDim.x) {
+      const double* b = Xref + (int64_t)j * dim;
+      double v = corr ? exact_corr(sa, ma, sda, b, mr[j], srv[j], dim) : exact_euclid(sa, b, dim);
+      out_d[(int64_t)grow * Nr + j] = sqrt(v);
+      out_i[(int64_t)grow * Nr + j] = j;
+    }
+    return;
+  }
+  int total;
+  float tau = __int_as_float(0x7f800000);
+  if (mode == 0) {
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int s = 0; s < nseg; ++s) t += cand_n[(int64_t)lr * nseg + s];
+      s_total = t;
+    }
+    __syncthreads();
+    const int t = s_total;
+    const int P2 = next_pow2(max(t, 1));
+    int off = 0;
+    for (int s = 0; s < nseg; ++s) {
+      int ns = cand_n[(int64_t)lr * nseg + s];
+      const uint64_t* src = cand + ((int64_t)lr * nseg + s) * Kp;
+      for (int x = threadIdx.x; x < ns; x += blockDim.x) keys[off + x] = src[x];
+      off += ns;
+    }
+    for (int x = t + threadIdx.x; x < P2; x += blockDim.x) keys[x] = MDS_KEY_INF;
+    __syncthreads();
+    block_bitonic_sort(keys, P2);
+    total = min(t, Kp);
+    if (t >= Kp) tau = mds_key_value(keys[Kp - 1]);
+  } else {
+    total = Nr;
+  }
+  // Exact (value, index) pairs: the k+1 best so far in slots [0, k1), the
+  // chunk being rechecked after them; the candidate keys stay in keys[0, Kp).
+  const int CH = (mode == 0) ? next_pow2(max(Kp, 1)) : 1024;
+  const int BP2 = next_pow2(k1 + CH);
+  double* bval = reinterpret_cast<double*>(keys + (mode == 0 ? Kp : 0));
+  int* bidx = reinterpret_cast<int*>(bval + BP2);
+  const int step = (mode == 0) ? max(total, 1) : CH;
+  for (int x = threadIdx.x; x < BP2; x += blockDim.x) {
+    bval[x] = __longlong_as_double(0x7ff0000000000000ll);
+    bidx[x] = 0x7fffffff;
+  }
+  __syncthreads();
+  for (int base = 0; base < total; base += step) {
+    int nc = min(step, total - base);
+    for (int c = threadIdx.x; c < BP2 - k1; c += blockDim.x) {
+      double v = __longlong_as_double(0x7ff0000000000000ll);
+      int j = 0x7fffffff;
+      if (c < nc) {
+        j = (mode == 0) ? mds_key_index(keys[base + c]) : base + c;
+        const double* b = Xref + (int64_t)j * dim;
+        v = corr ? exact_corr(sa, ma, sda, b, mr[j], srv[j], dim) : exact_euclid(sa, b, dim);
+      }
+      bval[k1 + c] = v;
+      bidx[k1 + c] = j;
+    }
+    __syncthreads();
+    // bitonic sort of (value, index) pairs
+    for (int kk = 2; kk <= BP2; kk <<= 1)
+      for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+        for (int i = threadIdx.x; i < BP2; i += blockDim.x) {
+          int ixj = i ^ jj;
+          if (ixj > i) {
+            double va = bval[i], vb = bval[ixj];
+            int ia = bidx[i], ib = bidx[ixj];
+            bool gt = (va > vb) || (va == vb && ia > ib);
+            bool up = (i & kk) == 0;
+            if (gt == up) {
+              bval[i] = vb; bval[ixj] = va;
+              bidx[i] = ib; bidx[ixj] = ia;
+            }
+          }
+        }
+        __syncthreads();
+      }
+  }
+  if (threadIdx.x == 0 && mode == 0) {
+    double dk = bval[k1 - 1];
+    if (!(dk <= (double)tau)) {
+      int pos = atomicAdd(nflag, 1);
+      flagged[pos] = grow;
+    }
+  }
+  for (int x = threadIdx.x; x < k; x += blockDim.x) {
+    out_d[(int64_t)grow * k + x] = sqrt(bval[x + 1]);
+    out_i[(int64_t)grow * k + x] = bidx[x + 1];
+  }
+}
+
+static size_t data_recheck_smem(int dim, int Kp, int nseg, int k, int mode) {
+  int k1 = k + 1;
+  size_t merge = (mode == 0) ? (size_t)next_pow2(std::max(nseg * Kp, 1)) : 0;
+  int CH = (mode == 0) ? next_pow2(std::max(Kp, 1)) : 1024;
+  int BP2 = next_pow2(k1 + CH);
+  size_t tail = (size_t)(mode == 0 ? Kp : 0) * 8 + (size_t)BP2 * (8 + 4);
+  return sizeof(double) * dim + std::max(merge * 8, tail) + 64;
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit, int nfit, int dim, int k,
+                 bool corr, bool full, unsigned prec, double* dout_d, int* dout_i) {
+  cudaStream_t s = ctx->stream;
+  mds_knn_stats& st = ctx->stats;
+  const bool same = (dfit == nullptr);
+  if (same) {
+    dfit = dref;
+    nfit = nref;
+  }
+  const int Dp = mds_round_up(dim, DT_KC);
+  DevBuf Xr(ctx), Nrm(ctx), Mr(ctx), Sr(ctx), Xf(ctx), Nf(ctx), Mf(ctx), Sf(ctx), flagged(ctx), nflag(ctx);
+  MDS_TRY(Xr.alloc(ctx, sizeof(float) * (size_t)nref * Dp));
+  MDS_TRY(Nrm.alloc(ctx, sizeof(float) * nref));
+  MDS_TRY(Mr.alloc(ctx, sizeof(double) * nref));
+  MDS_TRY(Sr.alloc(ctx, sizeof(double) * nref));
+  st.launches = 0;
+  st.launches++;
+  k_vec_prep<<<(nref + 127) / 128, 128, 0, s>>>(dref, nref, dim, Dp, corr, Xr.as<float>(), Nrm.as<float>(),
+                                                Mr.as<double>(), Sr.as<double>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  const float* xf = Xr.as<float>();
+  const float* nfp = Nrm.as<float>();
+  const double* mf = Mr.as<double>();
+  const double* sf = Sr.as<double>();
+  if (!same) {
+    MDS_TRY(Xf.alloc(ctx, sizeof(float) * (size_t)nfit * Dp));
+    MDS_TRY(Nf.alloc(ctx, sizeof(float) * nfit));
+    MDS_TRY(Mf.alloc(ctx, sizeof(double) * nfit));
+    MDS_TRY(Sf.alloc(ctx, sizeof(double) * nfit));
+    st.launches++;
+    k_vec_prep<<<(nfit + 127) / 128, 128, 0, s>>>(dfit, nfit, dim, Dp, corr, Xf.as<float>(), Nf.as<float>(),
+                                                  Mf.as<double>(), Sf.as<double>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    xf = Xf.as<float>();
+    nfp = Nf.as<float>();
+    mf = Mf.as<double>();
+    sf = Sf.as<double>();
+  }
+  MDS_TRY(flagged.alloc(ctx, sizeof(int) * (size_t)std::max(nfit, 1)));
+  MDS_TRY(nflag.alloc(ctx, sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
+  auto recheck = [&](int nrows, const int* rowlist, int mode, const uint64_t* cand, const int* cand_n, int nseg,
+                     int Kp) -> int {
+    size_t smem = data_recheck_smem(dim, Kp, nseg, k, mode);
+    if (smem > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "knn_data recheck: dim/k too large");
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    st.launches++;
+    if (nrows > 0)
+      k_data_recheck<<<nrows, DR_THREADS, smem, s>>>(dfit, dref, mf, sf, Mr.as<double>(), Sr.as<double>(), nfp,
+                                                     nrows, rowlist, nref, dim, corr, mode, cand, cand_n, nseg, Kp,
+                                                     k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    return MDS_OK;
+  };
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  if (full) {
+    MDS_TRY(recheck(nfit, nullptr, 2, nullptr, nullptr, 1, 1));
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    st.recheck_ms = ms;
+    return MDS_OK;
+  }
+  int Kp = std::min(mds_round_up(std::max(k + 1 + 32, (k + 1) * 3 / 2), 32), 448);
+  const int nrt = (nfit + DT_TM - 1) / DT_TM, nct = (nref + DT_TN - 1) / DT_TN;
+  int nseg = 1;
+  {
+    double besteff = 0;
+    for (int sg = 1; sg <= 8 && sg <= nct; ++sg) {
+      double w = (double)nrt * sg / ctx->num_sms, eff = w / std::ceil(w);
+      if (eff > besteff + 0.02) {
+        besteff = eff;
+        nseg = sg;
+      }
+      if (eff >= 0.95) break;
+    }
+  }
+  const float guard = corr ? 1.0f / 65536.0f : 1.0f / 65536.0f;
+  DevBuf cand(ctx), cand_n(ctx), rows(ctx);
+  MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)nfit * nseg * Kp));
+  MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)nfit * nseg));
+  size_t smem = screen_dot_smem(Kp);
+  MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  st.launches++;
+  st.screen_launches = 1;
+  k_screen_dot<<<nrt * nseg, DT_THREADS, smem, s>>>(xf, Xr.as<float>(), nfp, Nrm.as<float>(), nfit, nullptr, nref,
+                                                     Dp, corr, guard, Kp, nseg, cand.as<uint64_t>(),
+                                                     cand_n.as<int>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  MDS_TRY(recheck(nfit, nullptr, 0, cand.as<uint64_t>(), cand_n.as<int>(), nseg, Kp));
+  MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+  int hflag = 0;
+  MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  float a = 0, b = 0;
+  cudaEventElapsedTime(&a, ctx->ev[1], ctx->ev[2]);
+  cudaEventElapsedTime(&b, ctx->ev[2], ctx->ev[3]);
+  st.screen_ms = a;
+  st.recheck_ms = b;
+  st.kprime = Kp;
+  st.rows_flagged = hflag;
+  st.passes = 1;
+  while (hflag > 0) {
+    std::vector<int> hrows(hflag);
+    MDS_CUDA(ctx, cudaMemcpyAsync(hrows.data(), flagged.p, sizeof(int) * hflag, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    std::sort(hrows.begin(), hrows.end());
+    MDS_TRY(rows.alloc(ctx, sizeof(int) * hflag));
+    MDS_CUDA(ctx, cudaMemcpyAsync(rows.p, hrows.data(), sizeof(int) * hflag, cudaMemcpyHostToDevice, s));
+    MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
+    st.passes++;
+    Kp = std::min(Kp * 4, 448);
+    if (Kp >= nref || st.passes > 3) {
+      MDS_TRY(recheck(hflag, rows.as<int>(), 1, nullptr, nullptr, 1, 1));
+      MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      break;
+    }
+    MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)hflag * Kp));
+    MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)hflag));
+    smem = screen_dot_smem(Kp);
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    st.launches++;
+    k_screen_dot<<<(hflag + DT_TM - 1) / DT_TM, DT_THREADS, smem, s>>>(xf, Xr.as<float>(), nfp, Nrm.as<float>(),
+                                                                       hflag, rows.as<int>(), nref, Dp, corr, guard,
+                                                                       Kp, 1, cand.as<uint64_t>(), cand_n.as<int>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_TRY(recheck(hflag, rows.as<int>(), 0, cand.as<uint64_t>(), cand_n.as<int>(), 1, Kp));
+    MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  }
+  return MDS_OK;
+}

@@ -30,16 +30,27 @@
 // ---------------------------------------------------------------------------
 // 1. centring
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double block_sum_d(double v, double* red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+// Block sum of N values at once: every warp reduces its N partial sums with
+// shuffles, lane 0 stores them in red[warp * N + i], one barrier, then every
+// thread adds the warps' rows in order. red holds (blockDim/32) * N doubles.
+template <int N>
+__device__ __forceinline__ void block_sum_vec(double (&v)[N], double* red) {
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
   __syncthreads();
-  if (l == 0) red[w] = v;
+  if (l == 0)
+#pragma unroll
+    for (int i = 0; i < N; ++i) red[w * N + i] = v[i];
   __syncthreads();
-  double s = 0;
-  int nw = blockDim.x >> 5;
-  for (int i = 0; i < nw; ++i) s += red[i];
-  return s;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    double s = 0;
+    for (int j = 0; j < nw; ++j) s += red[j * N + i];
+    v[i] = s;
+  }
+  __syncthreads();
 }
 
 // One block per frame. raw: [n][natoms][3]; out: [n][3][Ap]; E: |y|^2 per
@@ -47,7 +58,7 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
 __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int Ap,
                          const float* __restrict__ mass, const float* __restrict__ swn, float tm,
                          float* __restrict__ out, double* __restrict__ E) {
-  __shared__ double red[32];
+  __shared__ double red[32 * 3];
   int f = blockIdx.x;
   if (f >= n) return;
   const float* x = raw + (int64_t)f * natoms * 3;
@@ -56,8 +67,9 @@ __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int A
     float mm = mass[a];
     for (int c = 0; c < 3; ++c) s[c] += (double)(mm * x[3 * a + c]);
   }
+  block_sum_vec<3>(s, red);
   double com[3];
-  for (int c = 0; c < 3; ++c) com[c] = block_sum_d(s[c], red) / (double)tm;
+  for (int c = 0; c < 3; ++c) com[c] = s[c] / (double)tm;
   double e = 0;
   float* o = out + (int64_t)f * 3 * Ap;
   for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
@@ -71,8 +83,9 @@ __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int A
       o[c * Ap + a] = v;
     }
   }
-  e = block_sum_d(e, red);
-  if (threadIdx.x == 0) E[f] = e;
+  double ev[1] = {e};
+  block_sum_vec<1>(ev, red);
+  if (threadIdx.x == 0) E[f] = ev[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -85,7 +98,7 @@ __global__ void k_prealign(const float* __restrict__ Y, const double* __restrict
                            int natoms, int Ap, const double* __restrict__ mu,
                            const double* __restrict__ M0, int nofit, float* __restrict__ dev,
                            float* __restrict__ rec) {
-  __shared__ double red[32];
+  __shared__ double red[32 * 10];
   __shared__ double Rsh[9];
   int f = blockIdx.x;
   if (f >= n) return;
@@ -98,8 +111,9 @@ __global__ void k_prealign(const float* __restrict__ Y, const double* __restrict
       for (int c = 0; c < 3; ++c)
         for (int d = 0; d < 3; ++d) s[3 * c + d] += yc[c] * mc[d];
     }
+    block_sum_vec<9>(s, red);
     double S[9];
-    for (int i = 0; i < 9; ++i) S[i] = block_sum_d(s[i], red);
+    for (int i = 0; i < 9; ++i) S[i] = s[i];
     if (threadIdx.x == 0) {
       double emu = M0[0] + M0[4] + M0[8];
       double R[9];
@@ -132,9 +146,11 @@ __global__ void k_prealign(const float* __restrict__ Y, const double* __restrict
       for (int c = 0; c < 3; ++c) o[c * Ap + a] = 0.0f;
     }
   }
-  ea = block_sum_d(ea, red);
+  double eu[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
+  block_sum_vec<10>(eu, red);
+  ea = eu[0];
   double U[9];
-  for (int i = 0; i < 9; ++i) U[i] = block_sum_d(u[i], red);
+  for (int i = 0; i < 9; ++i) U[i] = eu[1 + i];
   if (threadIdx.x == 0) {
     float* r = rec + (int64_t)f * MDS_REC;
     double sxx = U[0], syy = U[4], szz = U[8];
@@ -342,6 +358,7 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
   size_t smem = screen_fp32_smem(Kp);
   MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int nrt = (nrows + SC_TM - 1) / SC_TM;
+  ctx->stats.launches++;
   k_screen_fp32<<<nrt * nseg, SC_THREADS, smem, ctx->stream>>>(
       Af, Ar, recf, recr, nrows, rowlist, pl.nref, pl.Ap, pl.nofit, pl.guard_fp32, Kp, nseg, cand, cand_n);
   MDS_CUDA(ctx, cudaGetLastError());
@@ -415,7 +432,7 @@ __global__ void __launch_bounds__(RC_THREADS)
 k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const float* __restrict__ Yr,
           const double* __restrict__ Er, int nrows, const int* __restrict__ rowlist, int Nr, int Ap,
           int natoms, int nofit, int mode, const uint64_t* __restrict__ cand,
-          const int* __restrict__ cand_n, int nseg, int Kp, int k, double* __restrict__ out_d,
+          const int* __restrict__ cand_n, int nseg, int segstride, int Kp, int k, double* __restrict__ out_d,
           int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* sfit = reinterpret_cast<float*>(smem_raw);               // [3*Ap]
@@ -468,7 +485,7 @@ k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const flo
     int off = 0;
     for (int s = 0; s < nseg; ++s) {
       int ns = cand_n[(int64_t)lr * nseg + s];
-      const uint64_t* src = cand + ((int64_t)lr * nseg + s) * Kp;
+      const uint64_t* src = cand + ((int64_t)lr * nseg + s) * segstride;
       for (int x = threadIdx.x; x < ns; x += blockDim.x) keys[off + x] = src[x];
       off += ns;
     }
@@ -607,8 +624,8 @@ int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofi
 
 int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const double* Ef,
                    const float* Yr, const double* Er, int nrows, const int* rowlist, int mode,
-                   const uint64_t* cand, const int* cand_n, int nseg, int Kp, int k, double* out_d,
-                   int* out_i, int* flagged, int* nflag) {
+                   const uint64_t* cand, const int* cand_n, int nseg, int segstride, int Kp, int k,
+                   double* out_d, int* out_i, int* flagged, int* nflag) {
   size_t smem = recheck_smem(pl.Ap, Kp, k, mode);
   if (mode == 0) {
     // the merge buffer holds nseg*Kp keys before trimming
@@ -623,10 +640,11 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const do
   if (smem > 227 * 1024)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck needs %zu bytes of shared memory (natoms/k too large)", smem);
   MDS_CUDA(ctx, cudaFuncSetAttribute(k_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nrows > 0) ctx->stats.launches++;
   if (nrows > 0)
     k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Yf, Ef, Yr, Er, nrows, rowlist, pl.nref, pl.Ap,
                                                         pl.natoms, pl.nofit, mode, cand, cand_n, nseg,
-                                                        Kp, k, out_d, out_i, flagged, nflag);
+                                                        segstride, Kp, k, out_d, out_i, flagged, nflag);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
@@ -672,6 +690,8 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   DevBuf Yr(ctx), Er(ctx), Yf(ctx), Ef(ctx);
   MDS_TRY(Yr.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
   MDS_TRY(Er.alloc(ctx, sizeof(double) * nref));
+  st.launches = 0;
+  st.launches++;
   k_center<<<nref, 128, 0, s>>>(draw_ref, nref, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
                                  Yr.as<float>(), Er.as<double>());
   MDS_CUDA(ctx, cudaGetLastError());
@@ -680,6 +700,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   if (!same) {
     MDS_TRY(Yf.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
     MDS_TRY(Ef.alloc(ctx, sizeof(double) * nfit));
+    st.launches++;
     k_center<<<nfit, 128, 0, s>>>(draw_fit, nfit, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
                                    Yf.as<float>(), Ef.as<double>());
     MDS_CUDA(ctx, cudaGetLastError());
@@ -695,7 +716,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   if (pl.full) {
     MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
     MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), nfit, nullptr, 2,
-                           nullptr, nullptr, 1, 1, 0, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
+                           nullptr, nullptr, 1, 1, 1, 0, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
     MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
     MDS_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
     float ms = 0;
@@ -717,6 +738,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_CUDA(ctx, cudaMemcpyAsync(dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(Ar.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
   MDS_TRY(Rr.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nref));
+  st.launches++;
   k_prealign<<<nref, 128, 0, s>>>(Yr.as<float>(), Er.as<double>(), nref, natoms, Ap, dmu.as<double>(),
                                    dM0.as<double>(), pl.nofit, Ar.as<float>(), Rr.as<float>());
   MDS_CUDA(ctx, cudaGetLastError());
@@ -725,17 +747,26 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   if (!same) {
     MDS_TRY(Af.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
     MDS_TRY(Rf.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nfit));
+    st.launches++;
     k_prealign<<<nfit, 128, 0, s>>>(Yfp, Efp, nfit, natoms, Ap, dmu.as<double>(), dM0.as<double>(),
                                      pl.nofit, Af.as<float>(), Rf.as<float>());
     MDS_CUDA(ctx, cudaGetLastError());
     Afp = Af.as<float>();
     Rfp = Rf.as<float>();
   }
+  if (pl.prep_dev) {
+    MDS_CUDA(ctx, cudaMemcpyAsync(pl.prep_dev, Ar.p, sizeof(float) * 3 * Ap * (size_t)nref,
+                                  cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaMemcpyAsync(pl.prep_rec, Rr.p, sizeof(float) * MDS_REC * (size_t)nref,
+                                  cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    return MDS_OK;
+  }
   // tensor-core operands (split hi/lo), when that screen is selected
   TcOperands tcr, tcf;
   if (pl.prec != MDS_PREC_FP32) {
-    MDS_TRY(tc_prepare(ctx, pl, Ar.as<float>(), nref, tcr));
-    if (!same) MDS_TRY(tc_prepare(ctx, pl, Afp, nfit, tcf));
+    MDS_TRY(tc_prepare(ctx, pl, Ar.as<float>(), nref, tcr, 1));
+    MDS_TRY(tc_prepare(ctx, pl, Afp, nfit, same ? tcr : tcf, 0));
   }
 
   // first pass
@@ -743,8 +774,10 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   int ncoltiles = (nref + 63) / 64;
   int nseg = choose_nseg((nfit + 31) / 32, ctx->num_sms, ncoltiles);
   if (pl.prec != MDS_PREC_FP32) nseg = tc_choose_nseg(ctx, pl, nfit);
+  if (pl.screen_keys) nseg = 1;
   DevBuf cand(ctx), cand_n(ctx), rows(ctx);
-  MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)nfit * nseg * Kp));
+  const int segstride = (pl.prec == MDS_PREC_FP32) ? Kp : tc_seg_stride();
+  MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)nfit * nseg * segstride));
   MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)nfit * nseg));
   MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
@@ -758,8 +791,19 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.screen_launches = 1;
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  if (pl.screen_keys) {
+    MDS_CUDA(ctx, cudaMemcpy2DAsync(pl.screen_keys, sizeof(uint64_t) * Kp, cand.p, sizeof(uint64_t) * segstride,
+                                    sizeof(uint64_t) * Kp, nfit, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaMemcpyAsync(pl.screen_counts, cand_n.p, sizeof(int) * nfit, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    float t12 = 0;
+    cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
+    st.screen_ms = t12;
+    st.kprime = Kp;
+    return MDS_OK;
+  }
   MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), nfit, nullptr, 0,
-                         cand.as<uint64_t>(), cand_n.as<int>(), nseg, Kp, k, dout_d, dout_i,
+                         cand.as<uint64_t>(), cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i,
                          flagged.as<int>(), nflag.as<int>()));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0;
@@ -790,7 +834,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     if (Kp >= nref || st.passes > 3) {
       // exact rows: every reference is a candidate
       MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), hflag, rows.as<int>(), 1,
-                             nullptr, nullptr, 1, 1, k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
+                             nullptr, nullptr, 1, 1, 1, k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
       break;
     }
@@ -800,7 +844,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), hflag, rows.as<int>(), Kp,
                                nseg2, cand.as<uint64_t>(), cand_n.as<int>()));
     MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), hflag, rows.as<int>(), 0,
-                           cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, k, dout_d, dout_i,
+                           cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, Kp, k, dout_d, dout_i,
                            flagged.as<int>(), nflag.as<int>()));
     MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MDS_CUDA(ctx, cudaStreamSynchronize(s));

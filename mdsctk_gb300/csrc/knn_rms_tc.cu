@@ -1,11 +1,512 @@
-// knn_rms_tc.cu -- tcgen05 split-precision candidate screen (in progress).
-#include "knn_common.cuh"
+// knn_rms_tc.cu -- the all-pairs candidate screen of knn_rms on the 5th
+// generation tensor cores (tcgen05 + TMEM + TMA), split precision.
+//
+// The nine A-long contractions of every frame pair (the 3x3 deviation Gram
+// G_ij = sum_a a_i(a) a_j(a)^T) are one GEMM: rows (frame, xyz) of the fit
+// set times rows (frame, xyz) of the reference set, reduced over atoms.
+// Each operand is split x = hi + lo in BF16 (or FP16) and the product is
+// hi*hi + hi*lo + lo*hi, accumulated in FP32 in TMEM.
+//
+// CTA tile: M = 128 TMEM lanes = 40 fit frames (each 32-lane quarter holds
+// 10 frames x 3 coordinates, two padding lanes), N = 240 columns = 80
+// reference frames stored coordinate-major (x of 80 frames, then y, then z).
+// Reduction in K-blocks of 32 atoms through a 4-stage TMA pipeline
+// (64-byte swizzle). Two TMEM accumulators (2 x 240 of 512 columns) let the
+// MMA of one column tile run under the epilogue of the previous one.
+//
+// Warp roles (320 threads, one CTA per SM, persistent over work items =
+// (row tile, column segment)):
+//   warp 0      TMA producer (one thread)
+//   warp 1      TMEM allocator + MMA issuer (one thread)
+//   warps 2..9  epilogue: two warps per TMEM lane quarter, each taking half
+//               of the column chunks. A 3-lane shuffle transpose gives each
+//               lane the full 3x3 Gram of one pair; the shifted QCP bound
+//               (qcp.cuh) and the guard give the lower bound of RMSD^2;
+//               passing pairs are appended to a per-(row, segment) buffer of
+//               512 keys in global memory, compacted to the best K' in
+//               shared-memory scratch when it fills.
+// Every wait is bounded; on a timeout the kernel records an error, drains,
+// frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
-int tc_prepare(mds_ctx* ctx, const KnnRmsPlan&, const float*, int, TcOperands&) {
-  return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen not built yet");
+#include <algorithm>
+#include <cmath>
+
+#include "knn_common.cuh"
+#include "qcp.cuh"
+#include "tc_ptx.cuh"
+
+#define TC_FR_M 40
+#define TC_FR_N 80
+#define TC_M 128
+#define TC_N 240
+#define TC_KB 32
+#define TC_STAGES 4
+#define TC_THREADS 320
+#define TC_EPI_WARPS 8
+#define TC_CAPG 512
+#define TC_A_BYTES (TC_M * TC_KB * 2)
+#define TC_B_BYTES (TC_N * TC_KB * 2)
+#define TC_STAGE_BYTES (2 * TC_A_BYTES + 2 * TC_B_BYTES)
+#define TC_TMEM_COLS 512
+
+// ---------------------------------------------------------------------------
+// operand preparation: FP32 deviations [n][3][Ap] -> split hi|lo rows
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T to_lp(float x);
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_lp<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
+template <>
+__device__ __forceinline__ __half to_lp<__half>(float x) { return __float2half_rn(x); }
+template <class T>
+__device__ __forceinline__ float from_lp(T x);
+template <>
+__device__ __forceinline__ float from_lp<__nv_bfloat16>(__nv_bfloat16 x) { return __bfloat162float(x); }
+template <>
+__device__ __forceinline__ float from_lp<__half>(__half x) { return __half2float(x); }
+
+// layout 0 (fit side, A): row t*128 + q*32 + 3f + c  <- frame t*40 + q*10 + f
+// layout 1 (ref side, B): row t*240 + c*80 + g        <- frame t*80 + g
+template <class T>
+__global__ void k_tc_split(const float* __restrict__ dev, int n, int Ap, int layout, int rows, float scale,
+                           T* __restrict__ out) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t total = (int64_t)rows * Ap;
+  if (idx >= total) return;
+  int r = (int)(idx / Ap), k = (int)(idx % Ap);
+  int frame, c;
+  bool valid;
+  if (layout == 0) {
+    int t = r / TC_M, w = r % TC_M, q = w / 32, l = w % 32;
+    frame = t * TC_FR_M + q * 10 + l / 3;
+    c = l % 3;
+    valid = (l < 30) && frame < n;
+  } else {
+    int t = r / TC_N, w = r % TC_N;
+    c = w / TC_FR_N;
+    frame = t * TC_FR_N + w % TC_FR_N;
+    valid = frame < n;
+  }
+  float x = valid ? dev[((int64_t)frame * 3 + c) * Ap + k] * scale : 0.0f;
+  T hi = to_lp<T>(x);
+  T lo = to_lp<T>(x - from_lp<T>(hi));
+  out[(int64_t)r * 2 * Ap + k] = hi;
+  out[(int64_t)r * 2 * Ap + Ap + k] = lo;
 }
-int tc_choose_nseg(mds_ctx*, const KnnRmsPlan&, int) { return 1; }
-int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan&, const TcOperands&, const TcOperands&,
-                     const float*, const float*, int, int, int, uint64_t*, int*) {
-  return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen not built yet");
+
+static float tc_scale(unsigned prec) { return prec == MDS_PREC_FP16X3 ? 64.0f : 1.0f; }
+
+int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout) {
+  int rows = (layout == 0) ? (n + TC_FR_M - 1) / TC_FR_M * TC_M : (n + TC_FR_N - 1) / TC_FR_N * TC_N;
+  DevBuf& buf = (layout == 0) ? op.A : op.B;
+  MDS_TRY(buf.alloc(ctx, (size_t)rows * 2 * pl.Ap * 2));
+  if (layout == 0) op.rowsA = rows; else op.rowsB = rows;
+  op.n = n;
+  op.K = pl.Ap;
+  int64_t total = (int64_t)rows * pl.Ap;
+  int blocks = (int)((total + 255) / 256);
+  ctx->stats.launches++;
+  if (pl.prec == MDS_PREC_FP16X3)
+    k_tc_split<__half><<<blocks, 256, 0, ctx->stream>>>(dev, n, pl.Ap, layout, rows, tc_scale(pl.prec),
+                                                        buf.as<__half>());
+  else
+    k_tc_split<__nv_bfloat16><<<blocks, 256, 0, ctx->stream>>>(dev, n, pl.Ap, layout, rows, tc_scale(pl.prec),
+                                                               buf.as<__nv_bfloat16>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the screen kernel
+// ---------------------------------------------------------------------------
+struct TcShared {
+  uint64_t full[TC_STAGES], empty[TC_STAGES], tfull[2], tempty[2], done;
+  uint32_t tmem_base;
+  int abortf;
+  int bar_count, bar_gen;
+  int cnt[TC_FR_M];
+  float thr[TC_FR_M];
+  float colrec[TC_FR_N * MDS_REC];
+};
+
+#define TC_SMEM_BYTES (TC_STAGES * TC_STAGE_BYTES + sizeof(TcShared) + TC_EPI_WARPS * TC_CAPG * 8 + 1024)
+
+__device__ __forceinline__ float sel3(int i, float a0, float a1, float a2) {
+  return i == 0 ? a0 : (i == 1 ? a1 : a2);
+}
+
+// Barrier of the eight epilogue warps (spin on a generation counter,
+// bounded). Returns false if it timed out or the kernel aborts.
+__device__ __forceinline__ bool ep_sync(TcShared* S, int lane) {
+  __threadfence_block();
+  __syncwarp();
+  int ok = 1;
+  if (lane == 0) {
+    volatile int* gen = &S->bar_gen;
+    int g = *gen;
+    __threadfence_block();
+    if (atomicAdd(&S->bar_count, 1) == TC_EPI_WARPS - 1) {
+      S->bar_count = 0;
+      __threadfence_block();
+      atomicAdd(&S->bar_gen, 1);
+    } else {
+      uint64_t t0 = gtimer_ns();
+      while (*gen == g) {
+        if (*(volatile int*)&S->abortf) { ok = 0; break; }
+        if (gtimer_ns() - t0 > 1000000000ull) {
+          *(volatile int*)&S->abortf = 1;
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence_block();
+  }
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+            const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
+            int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems,
+            uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  unsigned char* stages = base;
+  TcShared* S = reinterpret_cast<TcShared*>(base + TC_STAGES * TC_STAGE_BYTES);
+  uint64_t* scratch_all = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(S) + sizeof(TcShared));
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nkb = Ap / TC_KB;
+  const int ncoltiles = (Nr + TC_FR_N - 1) / TC_FR_N;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&S->full[s], 1);
+      mbar_init(&S->empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&S->tfull[b], 1);
+      mbar_init(&S->tempty[b], TC_EPI_WARPS);
+    }
+    mbar_init(&S->done, 1);
+    S->abortf = 0;
+    S->bar_count = 0;
+    S->bar_gen = 0;
+    mbar_fence_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(&S->tmem_base, TC_TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S->tmem_base;
+  volatile int* abortf = &S->abortf;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      uint32_t stage = 0, phase = 0;
+      bool ok = true;
+      for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+        const int rt = item / nseg, seg = item % nseg;
+        const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+        for (int tile = t0; tile < t1 && ok; ++tile)
+          for (int kb = 0; kb < nkb; ++kb) {
+            if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf)) { ok = false; break; }
+            unsigned char* st = stages + stage * TC_STAGE_BYTES;
+            mbar_expect_tx(&S->full[stage], TC_STAGE_BYTES);
+            tma_load_2d(st, &tmA, &S->full[stage], kb * TC_KB, rt * TC_M);
+            tma_load_2d(st + TC_A_BYTES, &tmA, &S->full[stage], Ap + kb * TC_KB, rt * TC_M);
+            tma_load_2d(st + 2 * TC_A_BYTES, &tmB, &S->full[stage], kb * TC_KB, tile * TC_N);
+            tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, &S->full[stage], Ap + kb * TC_KB, tile * TC_N);
+            if (++stage == TC_STAGES) { stage = 0; phase ^= 1; }
+          }
+      }
+      if (!ok) {
+        atomicMax(err, 1);
+        // drain: every issued stage completes or times out
+        for (int s = 0; s < TC_STAGES; ++s) {
+          volatile int dummy = 0;
+          mbar_wait(&S->full[s], 0, &dummy, 50000000ull);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      uint32_t stage = 0, phase = 0, acc = 0;
+      bool ok = true;
+      const uint32_t sbase = smem_u32(stages);
+      for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+        const int seg = item % nseg;
+        const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+        for (int tile = t0; tile < t1 && ok; ++tile, ++acc) {
+          const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
+          if (!mbar_wait(&S->tempty[b], aph ^ 1, abortf)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t d = tbase + b * 256;
+          for (int kb = 0; kb < nkb; ++kb) {
+            if (!mbar_wait(&S->full[stage], phase, abortf)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t st = sbase + stage * TC_STAGE_BYTES;
+#pragma unroll
+            for (int ks = 0; ks < TC_KB / 16; ++ks) {
+              const uint64_t ahi = umma_desc_sw64(st + ks * 32);
+              const uint64_t alo = umma_desc_sw64(st + TC_A_BYTES + ks * 32);
+              const uint64_t bhi = umma_desc_sw64(st + 2 * TC_A_BYTES + ks * 32);
+              const uint64_t blo = umma_desc_sw64(st + 2 * TC_A_BYTES + TC_B_BYTES + ks * 32);
+              umma_f16(d, ahi, bhi, idesc, (kb | ks) != 0);
+              umma_f16(d, ahi, blo, idesc, 1);
+              umma_f16(d, alo, bhi, idesc, 1);
+            }
+            umma_commit(&S->empty[stage]);
+            if (++stage == TC_STAGES) { stage = 0; phase ^= 1; }
+          }
+          if (ok) umma_commit(&S->tfull[b]);
+        }
+      }
+      if (!ok) atomicMax(err, 2);
+      // all MMAs of this thread retire before TMEM is freed
+      umma_commit(&S->done);
+      volatile int dummy = 0;
+      mbar_wait(&S->done, 0, &dummy, 200000000ull);
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int ew = warp - 2;
+    const int q = warp & 3;          // TMEM lane quarter of this warp
+    const int h = ew >> 2;           // column half
+    const int f = lane / 3, c = lane % 3;
+    const int rloc = q * 10 + f;     // row within the 40-frame tile (f < 10)
+    uint64_t* scratch = scratch_all + ew * TC_CAPG;
+    const float INF = __int_as_float(0x7f800000);
+    uint32_t acc = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      const int rt = item / nseg, seg = item % nseg;
+      const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+      const int grow = rt * TC_FR_M + rloc;
+      const bool rowok = (f < 10) && grow < nfit;
+      float rrec[MDS_REC];
+#pragma unroll
+      for (int i = 0; i < MDS_REC; ++i) rrec[i] = rowok ? __ldg(recf + (int64_t)grow * MDS_REC + i) : 0.f;
+      // rows owned by this warp for resets and compaction: f = h, h+2, ...
+      if (lane < 5) {
+        int fr = h + 2 * lane;
+        S->cnt[q * 10 + fr] = 0;
+        S->thr[q * 10 + fr] = INF;
+      }
+      for (int tile = t0; tile < t1; ++tile, ++acc) {
+        const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
+        // column records of this tile
+        for (int e = ew * 32 + lane; e < TC_FR_N * MDS_REC; e += TC_EPI_WARPS * 32) {
+          int j = tile * TC_FR_N + e / MDS_REC;
+          S->colrec[e] = (j < Nr) ? __ldg(recr + (int64_t)j * MDS_REC + e % MDS_REC) : 0.f;
+        }
+        if (!mbar_wait(&S->tfull[b], aph, abortf)) { ok = false; break; }
+        tc_fence_after();
+        if (!ep_sync(S, lane)) { ok = false; break; }
+        const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256;
+        uint64_t* rowbuf = candbuf + ((int64_t)grow * nseg + seg) * TC_CAPG;
+#pragma unroll 1
+        for (int ci = h * 5; ci < h * 5 + 5; ++ci) {
+          float vx[8], vy[8], vz[8];
+          tmem_ld8(tq + 8 * ci, vx);
+          tmem_ld8(tq + TC_FR_N + 8 * ci, vy);
+          tmem_ld8(tq + 2 * TC_FR_N + 8 * ci, vz);
+          tmem_wait_ld();
+#pragma unroll
+          for (int g0 = 0; g0 < 8; g0 += 3) {
+            // v[g][d]: row (f, c) of the Gram of pair (f, column frame g0+g)
+            float v[3][3];
+#pragma unroll
+            for (int g = 0; g < 3; ++g) {
+              v[g][0] = (g0 + g < 8) ? vx[(g0 + g) & 7] : 0.f;
+              v[g][1] = (g0 + g < 8) ? vy[(g0 + g) & 7] : 0.f;
+              v[g][2] = (g0 + g < 8) ? vz[(g0 + g) & 7] : 0.f;
+            }
+            // 3-lane transpose: lane (f, m=c) gathers rows 0..2 of block m
+            float R[3][3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) R[0][d] = sel3(c, v[0][d], v[1][d], v[2][d]);
+#pragma unroll
+            for (int s = 1; s < 3; ++s) {
+              const int src = 3 * f + (c + s) % 3;
+              const int gi = (c + 3 - s) % 3;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+                float send = sel3(gi, v[0][d], v[1][d], v[2][d]);
+                R[s][d] = __shfl_sync(0xffffffffu, send, src & 31);
+              }
+            }
+            // row (c + s) % 3 of block m is R[s]
+            float G[9];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              G[0 + d] = sel3(c, R[0][d], R[2][d], R[1][d]) * ginv;
+              G[3 + d] = sel3(c, R[1][d], R[0][d], R[2][d]) * ginv;
+              G[6 + d] = sel3(c, R[2][d], R[1][d], R[0][d]) * ginv;
+            }
+            const int gl = 8 * ci + g0 + c;
+            const int j = tile * TC_FR_N + gl;
+            if (rowok && (g0 + c < 8) && j < Nr) {
+              const float* cr = S->colrec + gl * MDS_REC;
+              float sv = screen_shifted_f32(G, rrec, cr, nofit != 0);
+              sv = fmaxf(sv - guard * (rrec[15] + cr[15]), 0.0f);
+              if (sv < *(volatile float*)&S->thr[rloc]) {
+                int pos = atomicAdd(&S->cnt[rloc], 1);
+                if (pos < TC_CAPG)
+                  rowbuf[pos] = mds_pack_key(sv, j);
+                else
+                  atomicMax(err, 4);  // cannot happen with K' + 160 <= capacity
+              }
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S->tempty[b]);
+        if (!ep_sync(S, lane)) { ok = false; break; }
+        // compaction of this warp's rows
+        for (int fr = h; fr < 10; fr += 2) {
+          const int r = q * 10 + fr;
+          const int gr = rt * TC_FR_M + r;
+          if (gr >= nfit) continue;
+          int n = S->cnt[r];
+          bool need = (n > Kp) && (n > TC_CAPG - TC_FR_N || S->thr[r] == INF);
+          if (!need) continue;
+          uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
+          n = min(n, TC_CAPG);
+          for (int x = lane; x < n; x += 32) scratch[x] = src[x];
+          warp_bitonic_sort(scratch, n, TC_CAPG, lane);
+          for (int x = lane; x < Kp; x += 32) src[x] = scratch[x];
+          __syncwarp();
+          if (lane == 0) {
+            S->cnt[r] = Kp;
+            S->thr[r] = mds_key_value(scratch[Kp - 1]);
+          }
+          __syncwarp();
+        }
+      }
+      if (!ok) break;
+      if (!ep_sync(S, lane)) { ok = false; break; }
+      // final: sort and publish this warp's rows of the item
+      for (int fr = h; fr < 10; fr += 2) {
+        const int r = q * 10 + fr;
+        const int gr = rt * TC_FR_M + r;
+        if (gr >= nfit) continue;
+        int n = min(S->cnt[r], TC_CAPG);
+        uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
+        for (int x = lane; x < n; x += 32) scratch[x] = src[x];
+        warp_bitonic_sort(scratch, n, TC_CAPG, lane);
+        int keep = min(n, Kp);
+        for (int x = lane; x < keep; x += 32) src[x] = scratch[x];
+        if (lane == 0) cand_n[(int64_t)gr * nseg + seg] = keep;
+        __syncwarp();
+      }
+      if (!ep_sync(S, lane)) { ok = false; break; }
+    }
+    if (!ok && lane == 0) atomicMax(err, 3);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tbase, TC_TMEM_COLS);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*PFN_encodeTiled_t)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                      const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                      CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                      CUtensorMapFloatOOBfill);
+
+static int encode_map(mds_ctx* ctx, CUtensorMap* map, const void* ptr, int rows, int Ap, int boxrows,
+                      unsigned prec) {
+  static PFN_encodeTiled_t fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+      return mds_fail(ctx, MDS_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    fn = reinterpret_cast<PFN_encodeTiled_t>(p);
+  }
+  cuuint64_t gdim[2] = {(cuuint64_t)(2 * Ap), (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)(2 * Ap) * 2};
+  cuuint32_t box[2] = {TC_KB, (cuuint32_t)boxrows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, prec == MDS_PREC_FP16X3 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                  2, const_cast<void*>(ptr), gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return mds_fail(ctx, MDS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return MDS_OK;
+}
+
+int tc_choose_nseg(mds_ctx* ctx, const KnnRmsPlan& pl, int nfit) {
+  int nrt = (nfit + TC_FR_M - 1) / TC_FR_M;
+  int nct = (pl.nref + TC_FR_N - 1) / TC_FR_N;
+  int best = 1;
+  double besteff = 0;
+  for (int s = 1; s <= 8 && s <= nct; ++s) {
+    double w = (double)nrt * s / ctx->num_sms;
+    double eff = w / std::ceil(w);
+    if (eff > besteff + 0.02) {
+      besteff = eff;
+      best = s;
+    }
+    if (eff >= 0.97) break;
+  }
+  return best;
+}
+
+int tc_seg_stride() { return TC_CAPG; }
+
+int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
+                     const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
+                     int* cand_n) {
+  if (Kp + 2 * TC_FR_N > TC_CAPG)
+    return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen supports K' <= %d (k too large)",
+                    TC_CAPG - 2 * TC_FR_N);
+  if (pl.Ap % TC_KB) return mds_fail(ctx, MDS_ERR_INTERNAL, "padded atom count not a multiple of %d", TC_KB);
+  CUtensorMap mA, mB;
+  MDS_TRY(encode_map(ctx, &mA, fit.A.p, fit.rowsA, pl.Ap, TC_M, pl.prec));
+  MDS_TRY(encode_map(ctx, &mB, ref.B.p, ref.rowsB, pl.Ap, TC_N, pl.prec));
+  const int nrt = (nfit + TC_FR_M - 1) / TC_FR_M;
+  const int nitems = nrt * nseg;
+  const int grid = std::min(nitems, ctx->num_sms);
+  const size_t smem = TC_SMEM_BYTES;
+  MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DevBuf err(ctx);
+  MDS_TRY(err.alloc(ctx, sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, sizeof(int), ctx->stream));
+  const float s = tc_scale(pl.prec);
+  const uint32_t idesc = umma_idesc_f16(TC_M, TC_N, pl.prec == MDS_PREC_FP16X3 ? 0 : 1);
+  ctx->stats.launches++;
+  k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
+                                                       pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
+                                                       cand, cand_n, err.as<int>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  int herr = 0;
+  MDS_CUDA(ctx, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MDS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (herr) return mds_fail(ctx, MDS_ERR_TIMEOUT, "tensor-core screen: a bounded wait timed out (role %d)", herr);
+  return MDS_OK;
 }

@@ -85,6 +85,12 @@ struct DevBuf {
 
 static inline int mds_round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+// Stable LSD radix sort (8-bit digits over the bits set in `mask`) of n
+// (uint64 key, int64 value) pairs, ping-ponging between (k0,v0) and (k1,v1);
+// *which = 1 if the result ended in (k1,v1) (sparse.cu).
+int radix_sort(mds_ctx* ctx, unsigned long long* k0, int64_t* v0, unsigned long long* k1, int64_t* v1,
+               int64_t n, unsigned long long mask, int* which);
+
 // Pack a non-negative float key and an index into one ordered 64-bit word:
 // ascending order = ascending (value, index).
 __host__ __device__ __forceinline__ uint64_t mds_pack_key(float s, int j) {
