@@ -276,7 +276,7 @@ def main():
                    "d2h_bytes_per_step": int(n * kk * 12)}}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rows = args.cpu_rows or 4 * threads
+        rows = args.cpu_rows or 16 * threads
         v, dt = cpu_sample(x, rows, k, threads)
         res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": f"{rows} fit rows x {n} reference frames ({dt:.1f} s)"}

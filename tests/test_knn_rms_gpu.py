@@ -22,7 +22,7 @@ def _check_knn(d, i, od, oi, tol=TOL_A):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x3"])
 @pytest.mark.parametrize("n,natoms,k,basins", [(300, 304, 20, 1), (257, 97, 10, 4), (200, 1000, 30, 2)])
 def test_knn_rms_self(ctx, oracle, precision, n, natoms, k, basins):
     x = synth.trajectory(n, natoms, seed=n + natoms, basins=basins, dwell=60)
@@ -33,12 +33,13 @@ def test_knn_rms_self(ctx, oracle, precision, n, natoms, k, basins):
 
 
 @pytest.mark.gpu
-def test_knn_rms_fit_vs_ref_masses(ctx, oracle):
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_knn_rms_fit_vs_ref_masses(ctx, oracle, precision):
     rng = np.random.default_rng(1)
     ref = synth.trajectory(220, 60, seed=11, basins=3, dwell=40)
     fit = synth.trajectory(75, 60, seed=12, basins=3, dwell=40)
     m = rng.uniform(1.0, 16.0, size=60).astype(np.float32)
-    d, i = ctx.knn_rms(ref, fit, m, 15)
+    d, i = ctx.knn_rms(ref, fit, m, 15, precision=precision)
     od, oi = oracle.knn_rms(ref, fit, m, 15)
     _check_knn(d, i, od, oi)
 

@@ -13,8 +13,8 @@ def _exact_d2(oracle, x, m):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32"])
-@pytest.mark.parametrize("n,natoms,basins", [(320, 304, 4), (240, 1000, 8)])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x3"])
+@pytest.mark.parametrize("n,natoms,basins", [(320, 304, 4), (240, 1000, 8), (100, 37, 2)])
 def test_screen_lower_bound_and_completeness(ctx, oracle, precision, n, natoms, basins):
     x = synth.trajectory(n, natoms, seed=7 * n + natoms, basins=basins, dwell=60, drift_sigma=0.08)
     m = synth.uniform_masses(natoms)
@@ -37,7 +37,7 @@ def test_screen_lower_bound_and_completeness(ctx, oracle, precision, n, natoms, 
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
 def test_knn_rms_no_flagged_rows(ctx, oracle, precision):
     """On well-conditioned multi-basin data the guard holds on the first pass."""
     x = synth.trajectory(600, 1000, seed=99, basins=8, dwell=100, drift_sigma=0.08)
