@@ -220,12 +220,14 @@ def main():
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
-    screen_ms, recheck_ms, launches, flagged = [], [], 0, 0
+    screen_ms, recheck_ms, prep_ms, total_ms, launches, flagged = [], [], [], [], 0, 0
     for _ in range(args.steps):
         step_dev()
         st = ctx.stats()
         screen_ms.append(st["screen_ms"])
         recheck_ms.append(st["recheck_ms"])
+        prep_ms.append(st["prep_ms"])
+        total_ms.append(st["total_ms"])
         launches += st["launches"]
         flagged = max(flagged, st["rows_flagged"])
     ev1.record()
@@ -267,7 +269,9 @@ def main():
                         "frac": achieved / peak, "traffic": None,
                         "kernel": "screen", "kernel_ms": scr, "flops_per_launch": flops,
                         "peak_kind": f"{pk_kind} bf16 burst"},
-           "stages_ms": {"screen": scr, "recheck": sorted(recheck_ms)[len(recheck_ms) // 2]},
+           "stages_ms": {"prep": sorted(prep_ms)[len(prep_ms) // 2], "screen": scr,
+                         "recheck": sorted(recheck_ms)[len(recheck_ms) // 2],
+                         "call": sorted(total_ms)[len(total_ms) // 2]},
            "rows_flagged": flagged,
            "clocks": clocks,
            "gpu_launches": launches,

@@ -183,6 +183,65 @@ int mds_decomp_sparse_nystrom(mds_ctx* ctx, int n, const int32_t* pcol, const in
                               double sigma, int nev, int ncv, double tol, int maxiter, unsigned flags,
                               double* evals, double* evecs, double* ext, double* resid, int* nconv);
 
+/*
+ * Resident Nystrom serving (no single reference counterpart: it keeps on the
+ * device what the file pipeline examples/cluster_rms_nystrom.bash:54-66
+ * recomputes per run -- knn_rms on the landmarks, make_sysparse,
+ * decomp_sparse_nystrom's eigenpairs and degrees -- and serves query frames:
+ * knn_rms -f queries (nearest landmark dropped), make_gesparse and the
+ * extension ext = B^T z / lambda, decomp_sparse_nystrom.cpp:181-219,301-312).
+ * Requests are admitted continuously into batches (slots sized by the HBM
+ * budget), each batch runs as a captured CUDA graph on its slot's stream.
+ */
+typedef struct mds_server mds_server;
+
+typedef struct mds_server_config {
+  int device;
+  int k;                /* neighbours per frame (landmark graph and queries) */
+  double sigma;         /* Gaussian kernel width, in the distance file's units (Angstrom) */
+  int nev, ncv;         /* eigenpairs; ncv <= 0: min(10 nev + 1, n) */
+  double tol;           /* <= 0: machine epsilon */
+  int maxiter;          /* <= 0: 100 nev */
+  unsigned flags;       /* MDS_PREC_*, MDS_NOFIT */
+  int max_batch_frames; /* frames per batch (and per request); <= 0: 4096 */
+  int slots;            /* concurrent batches (<= 0: 3), bounded by the HBM budget */
+  size_t hbm_budget;    /* bytes for the slots; 0: half the free device memory */
+  int use_graphs;       /* capture each batch size bucket in a CUDA graph */
+} mds_server_config;
+
+typedef struct mds_request_info {
+  double queue_ms; /* submit -> admitted into a batch */
+  double total_ms; /* submit -> results published */
+  int batch;       /* batch id */
+  int batch_frames;
+} mds_request_info;
+
+typedef struct mds_server_stats {
+  int slots;
+  long long slot_bytes;
+  long long requests_submitted, requests_done, batches, frames;
+  long long graph_launches, graphs_captured, rows_flagged;
+  double model_knn_ms, model_decomp_ms;
+  int model_nconv;
+} mds_server_stats;
+
+/* Build the landmark model from land_xyz [n][natoms][3] (nm) and start the
+ * serving thread. */
+int mds_server_create(const mds_server_config* cfg, const float* land_xyz, int n, int natoms, const float* mass,
+                      mds_server** out);
+int mds_server_destroy(mds_server* s);
+const char* mds_server_last_error(const mds_server* s);
+/* evals [nev] descending, evecs [nev][n] (may be NULL) of the landmark model */
+int mds_server_model(mds_server* s, double* evals, double* evecs);
+/* Queue m query frames [m][natoms][3] (copied); returns a ticket. */
+int mds_server_submit(mds_server* s, const float* query_xyz, int m, int64_t* ticket);
+/* Wait up to timeout_ms for a ticket: ext [nev][m] (eigenvector x, query q),
+ * knn_d [m][k] (Angstrom), knn_i [m][k] (landmark ids); any may be NULL.
+ * MDS_ERR_TIMEOUT if it is not done yet (the ticket stays valid). */
+int mds_server_wait(mds_server* s, int64_t ticket, int timeout_ms, double* ext, double* knn_d, int32_t* knn_i,
+                    mds_request_info* info);
+int mds_server_get_stats(mds_server* s, mds_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,30 @@ class KnnStats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("k", ctypes.c_int), ("sigma", ctypes.c_double),
+                ("nev", ctypes.c_int), ("ncv", ctypes.c_int), ("tol", ctypes.c_double),
+                ("maxiter", ctypes.c_int), ("flags", ctypes.c_uint), ("max_batch_frames", ctypes.c_int),
+                ("slots", ctypes.c_int), ("hbm_budget", ctypes.c_size_t), ("use_graphs", ctypes.c_int)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("queue_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("batch", ctypes.c_int),
+                ("batch_frames", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int), ("slot_bytes", ctypes.c_longlong),
+                ("requests_submitted", ctypes.c_longlong), ("requests_done", ctypes.c_longlong),
+                ("batches", ctypes.c_longlong), ("frames", ctypes.c_longlong),
+                ("graph_launches", ctypes.c_longlong), ("graphs_captured", ctypes.c_longlong),
+                ("rows_flagged", ctypes.c_longlong), ("model_knn_ms", ctypes.c_double),
+                ("model_decomp_ms", ctypes.c_double), ("model_nconv", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 # Exported symbols and their signatures (kept in step with include/mdsgpu.h).
 _vp, _i, _u, _sz, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint, ctypes.c_size_t, ctypes.c_double
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -65,6 +89,13 @@ SIGNATURES = {
     "mds_sysparse": ([_vp, _vp, _vp, _i, _i, _i, _u, _vp, _vp, _vp, ctypes.c_int64, _i64p], _i),
     "mds_gesparse": ([_vp, _vp, _vp, _i, _i, _i, _i, _u, _vp, _vp, _vp, ctypes.c_int64, _i64p], _i),
     "mds_decomp_sparse": ([_vp, _i, _vp, _vp, _vp, _d, _i, _i, _d, _i, _u, _vp, _vp, _vp, _ip], _i),
+    "mds_server_create": ([ctypes.POINTER(ServerConfig), _vp, _i, _i, _vp, ctypes.POINTER(_vp)], _i),
+    "mds_server_destroy": ([_vp], _i),
+    "mds_server_last_error": ([_vp], ctypes.c_char_p),
+    "mds_server_model": ([_vp, _vp, _vp], _i),
+    "mds_server_submit": ([_vp, _vp, _i, _i64p], _i),
+    "mds_server_wait": ([_vp, ctypes.c_int64, _i, _vp, _vp, _vp, ctypes.POINTER(RequestInfo)], _i),
+    "mds_server_get_stats": ([_vp, ctypes.POINTER(ServerStats)], _i),
     "mds_decomp_sparse_nystrom": ([_vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _d, _i, _i, _d, _i, _u, _vp, _vp,
                                    _vp, _vp, _ip], _i),
 }

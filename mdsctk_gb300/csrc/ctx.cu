@@ -11,6 +11,20 @@ int mds_fail(mds_ctx* ctx, int code, const char* fmt, ...) {
   return code;
 }
 
+void mds_trim_cache(mds_ctx* ctx, size_t keep) {
+  if (!ctx || ctx->cache.empty()) return;
+  cudaStreamSynchronize(ctx->stream);
+  size_t cached = 0;
+  for (auto& kv : ctx->cache) cached += kv.first;
+  while (!ctx->cache.empty() && cached > keep) {
+    auto it = std::prev(ctx->cache.end());  // largest first
+    cudaFree(it->second);
+    cached -= it->first;
+    ctx->hbm_in_use -= it->first;
+    ctx->cache.erase(it);
+  }
+}
+
 extern "C" const char* mds_version(void) { return "mdsgpu 0.1 (sm_103a)"; }
 
 extern "C" int mds_create(int device, size_t hbm_budget, mds_ctx** out) {
@@ -37,6 +51,7 @@ extern "C" int mds_destroy(mds_ctx* ctx) {
   if (!ctx) return MDS_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  mds_trim_cache(ctx, 0);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);

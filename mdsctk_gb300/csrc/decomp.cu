@@ -789,6 +789,27 @@ static int decomp_impl(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* 
   return MDS_OK;
 }
 
+// Device-resident eigensolve for the serving model: the .ssm arrays on the
+// device in, eigenvalues (host, descending), eigenvectors Z [nev][n] and the
+// landmark inverse-square-root degrees d_a [n] (device) out.
+int decomp_resident(mds_ctx* ctx, int n, const int* dpcol, const int* dirow, const double* ddist, double sigma,
+                    int nev, int ncv, double tol, int maxiter, std::vector<double>& evals, double* dZ, double* ddinv,
+                    int* nconv) {
+  if (ncv <= 0) ncv = std::min(10 * nev + 1, n);
+  ncv = std::min(ncv, n);
+  if (maxiter <= 0) maxiter = 100 * nev;
+  if (nev < 1 || nev >= ncv) return mds_fail(ctx, MDS_ERR_ARG, "need 0 < nev < ncv <= n");
+  SymOp op;
+  MDS_TRY(build_symop(ctx, n, dpcol, dirow, ddist, sigma, op));
+  LanczosOut lo;
+  MDS_TRY(lanczos(ctx, op, nev, ncv, tol, maxiter, dZ, lo));
+  MDS_CUDA(ctx, cudaMemcpyAsync(ddinv, op.dinv.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  MDS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  evals = lo.evals;
+  if (nconv) *nconv = lo.nconv;
+  return MDS_OK;
+}
+
 extern "C" int mds_decomp_sparse(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow, const double* dist,
                                  double sigma, int nev, int ncv, double tol, int maxiter, unsigned flags,
                                  double* evals, double* evecs, double* resid, int* nconv) {

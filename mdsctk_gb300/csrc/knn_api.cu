@@ -103,7 +103,13 @@ static int knn_rms_impl(mds_ctx* ctx, const float* ref_xyz, int n_ref, const flo
   pl.nofit = (flags & MDS_NOFIT) ? 1 : 0;
   pl.full = full ? 1 : 0;
   pl.prec = prec;
-  pl.kprime = std::min(mds_round_up(std::max(k + 1 + 32, (k + 1) * 3 / 2), 32), 448);
+  // K' = 2(k+1) (at least k+33): the recheck stops early once the k+1 best
+  // are settled, so a wide K' mainly makes the guard hold on the first pass.
+  const int kpmax = (prec == MDS_PREC_FP32) ? 448 : 352;
+  pl.kprime = std::min(mds_round_up(std::max(k + 1 + 32, 2 * (k + 1)), 32), kpmax);
+  if (!full && pl.kprime < k + 1 + 16)
+    return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k=%d is too large for the %s screen (use fp32 precision)", k,
+                    prec == MDS_PREC_FP32 ? "fp32" : "tensor-core");
   if (hooks.screen_keys) {
     if (hooks.screen_kprime > 448) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "kprime > 448");
     pl.kprime = hooks.screen_kprime;

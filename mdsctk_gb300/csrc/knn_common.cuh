@@ -79,10 +79,26 @@ __host__ __device__ static inline int next_pow2(int x) {
 int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float* draw_fit,
                 const float* hmass, double* dout_d, int* dout_i);
 
+// pieces of the knn_rms pipeline (knn_rms.cu), reused by the serving loop
+int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass,
+                  const float* dswn, float tm, float* Y, double* E);
+int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const double* dmu,
+                    const double* dM0, int nofit, float* A, float* R);
+int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit, std::vector<double>& mu,
+                   double M0[9]);
+int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* recf,
+                       const float* recr, int nrows, const int* rowlist, int Kp, int nseg, uint64_t* cand,
+                       int* cand_n);
+int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const double* Ef, const float* Yr,
+                   const double* Er, int nrows, const int* rowlist, int mode, const uint64_t* cand,
+                   const int* cand_n, int nseg, int segstride, int Kp, int k, double* out_d, int* out_i,
+                   int* flagged, int* nflag);
+int choose_nseg_fp32(int nfit, int num_sms, int nref);
+
 // tensor-core screen (knn_rms_tc.cu)
 int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout);
 int tc_seg_stride();
 int tc_choose_nseg(mds_ctx* ctx, const KnnRmsPlan& pl, int nfit);
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
-                     int* cand_n);
+                     int* cand_n, int* derr = nullptr);

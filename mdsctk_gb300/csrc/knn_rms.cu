@@ -313,9 +313,10 @@ k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
         int j = tile * SC_TN + tx + 16 * q;
         if (j >= Nr) continue;
         const float* cr = scol + (tx + 16 * q) * MDS_REC;
-        float s = screen_shifted_f32(acc[p][q], rrec[p], cr, nofit != 0);
-        s = fmaxf(s - guard * (rrec[p][15] + cr[15]), 0.0f);
-        if (s < sthr[lr]) {
+        const float thr = sthr[lr];
+        float s = screen_shifted_f32(acc[p][q], rrec[p], cr, nofit != 0, guard * (rrec[p][15] + cr[15]), thr);
+        s = fmaxf(s, 0.0f);
+        if (s < thr) {
           int pos = atomicAdd(&scnt[lr], 1);
           pool[lr * P2 + pos] = mds_pack_key(s, j);
         }
@@ -356,7 +357,12 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
                        const float* recf, const float* recr, int nrows, const int* rowlist, int Kp,
                        int nseg, uint64_t* cand, int* cand_n) {
   size_t smem = screen_fp32_smem(Kp);
-  MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static bool attr_set = false;  // once: launches may also happen while a stream is captured
+  if (!attr_set) {
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr_set = true;
+  }
+  if (smem > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "screen shared memory %zu", smem);
   int nrt = (nrows + SC_TM - 1) / SC_TM;
   ctx->stats.launches++;
   k_screen_fp32<<<nrt * nseg, SC_THREADS, smem, ctx->stream>>>(
@@ -478,20 +484,20 @@ k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const flo
       s_total = t;
     }
     __syncthreads();
-    int t = s_total;
-    int P2 = 1;
-    while (P2 < t) P2 <<= 1;
-    // gather
-    int off = 0;
-    for (int s = 0; s < nseg; ++s) {
-      int ns = cand_n[(int64_t)lr * nseg + s];
-      const uint64_t* src = cand + ((int64_t)lr * nseg + s) * segstride;
-      for (int x = threadIdx.x; x < ns; x += blockDim.x) keys[off + x] = src[x];
-      off += ns;
-    }
-    for (int x = t + threadIdx.x; x < P2; x += blockDim.x) keys[x] = MDS_KEY_INF;
+    const int t = s_total;
+    // streaming merge: keys[0, Kp) holds the best K' so far (sorted), each
+    // segment's list (at most K' keys) is placed after it and the whole
+    // buffer re-sorted; shared memory stays O(K') for any segment count.
+    const int P2 = next_pow2(2 * Kp);
+    for (int x = threadIdx.x; x < P2; x += blockDim.x) keys[x] = MDS_KEY_INF;
     __syncthreads();
-    block_bitonic_sort(keys, P2);
+    for (int s = 0; s < nseg; ++s) {
+      const int ns = min(cand_n[(int64_t)lr * nseg + s], Kp);
+      const uint64_t* src = cand + ((int64_t)lr * nseg + s) * segstride;
+      for (int x = threadIdx.x; x < P2 - Kp; x += blockDim.x) keys[Kp + x] = (x < ns) ? src[x] : MDS_KEY_INF;
+      __syncthreads();
+      block_bitonic_sort(keys, P2);
+    }
     total = min(t, Kp);
     tau = (t >= Kp) ? mds_key_value(keys[Kp - 1]) : __int_as_float(0x7f800000);
   } else {
@@ -505,8 +511,15 @@ k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const flo
   while (TP2 < k1 + RC_CHUNK) TP2 <<= 1;
   for (int x = threadIdx.x; x < TP2; x += blockDim.x) top[x] = MDS_KEY_INF;
   __syncthreads();
-  for (int base = 0; base < total; base += RC_CHUNK) {
-    int nc = min(RC_CHUNK, total - base);
+  // Candidates come in ascending order of their lower bound; once the (k+1)-th
+  // exact RMSD^2 is below the next candidate's bound, no later candidate (nor
+  // any excluded pair, whose bound is at least tau) can enter the k+1 best.
+  __shared__ int s_stop;
+  bool stopped = false;
+  int base = 0;
+  const int first = min(RC_CHUNK, (k1 + 8 + 31) / 32 * 32);
+  while (base < total) {
+    int nc = min((mode == 0 && base == 0) ? first : RC_CHUNK, total - base);
     for (int c = threadIdx.x; c < nc; c += blockDim.x)
       cj[c] = (mode == 0) ? mds_key_index(keys[base + c]) : base + c;
     __syncthreads();
@@ -517,12 +530,25 @@ k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const flo
     for (int x = k1 + RC_CHUNK + threadIdx.x; x < TP2; x += blockDim.x) top[x] = MDS_KEY_INF;
     __syncthreads();
     block_bitonic_sort(top, TP2);
+    base += nc;
+    if (mode == 0 && base < total) {
+      if (threadIdx.x == 0) {
+        double dk = (double)mds_key_value(top[k1 - 1]);
+        double next = (double)mds_key_value(keys[base]);
+        s_stop = (dk * dk * (1.0 + 1e-6) < next) ? 1 : 0;
+      }
+      __syncthreads();
+      if (s_stop) {
+        stopped = true;
+        break;
+      }
+    }
   }
   // guard: the (k+1)-th exact RMSD^2 must not exceed the smallest lower bound
   // of every excluded pair.
   if (threadIdx.x == 0) {
     double dk = (double)mds_key_value(top[k1 - 1]);
-    if (mode == 0 && !(dk * dk <= (double)tau)) {
+    if (mode == 0 && !stopped && !(dk * dk * (1.0 + 1e-6) <= (double)tau)) {
       int pos = atomicAdd(nflag, 1);
       flagged[pos] = grow;
     }
@@ -628,9 +654,8 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const do
                    double* out_d, int* out_i, int* flagged, int* nflag) {
   size_t smem = recheck_smem(pl.Ap, Kp, k, mode);
   if (mode == 0) {
-    // the merge buffer holds nseg*Kp keys before trimming
-    int t = nseg * Kp, P2 = 1;
-    while (P2 < t) P2 <<= 1;
+    // the streaming merge works on the best K' plus one segment's K'
+    int P2 = next_pow2(2 * Kp);
     int TP2 = 1;
     while (TP2 < k + 1 + RC_CHUNK) TP2 <<= 1;
     size_t keys = std::max((size_t)P2, (size_t)Kp + TP2);
@@ -639,7 +664,11 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const do
   }
   if (smem > 227 * 1024)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck needs %zu bytes of shared memory (natoms/k too large)", smem);
-  MDS_CUDA(ctx, cudaFuncSetAttribute(k_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static bool attr_set = false;  // once: launches may also happen while a stream is captured
+  if (!attr_set) {
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr_set = true;
+  }
   if (nrows > 0) ctx->stats.launches++;
   if (nrows > 0)
     k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Yf, Ef, Yr, Er, nrows, rowlist, pl.nref, pl.Ap,
@@ -647,6 +676,41 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const do
                                                         segstride, Kp, k, out_d, out_i, flagged, nflag);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
+}
+
+// Launch wrappers used by the resident serving path (serve.cu).
+int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass,
+                  const float* dswn, float tm, float* Y, double* E) {
+  if (n <= 0) return MDS_OK;
+  ctx->stats.launches++;
+  k_center<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dmass, dswn, tm, Y, E);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const double* dmu,
+                    const double* dM0, int nofit, float* A, float* R) {
+  if (n <= 0) return MDS_OK;
+  ctx->stats.launches++;
+  k_prealign<<<n, 128, 0, ctx->stream>>>(Y, E, n, natoms, Ap, dmu, dM0, nofit, A, R);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+int choose_nseg_fp32(int nfit, int num_sms, int nref) {
+  int nrt = (nfit + SC_TM - 1) / SC_TM, nct = (nref + SC_TN - 1) / SC_TN;
+  int best = 1;
+  double besteff = 0;
+  for (int s = 1; s <= 8 && s <= nct; ++s) {
+    double waves = (double)nrt * s / num_sms;
+    double eff = waves / std::ceil(waves);
+    if (eff > besteff + 0.02) {
+      besteff = eff;
+      best = s;
+    }
+    if (eff >= 0.95) break;
+  }
+  return best;
 }
 
 static int choose_nseg(int nrowtiles, int num_sms, int ncoltiles) {
@@ -838,7 +902,9 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
       break;
     }
-    int nseg2 = 1;
+    // few rows: spread each over many column segments so the whole GPU works
+    const int nrt2 = (hflag + SC_TM - 1) / SC_TM;
+    const int nseg2 = std::max(1, std::min((2 * ctx->num_sms + nrt2 - 1) / nrt2, (nref + SC_TN - 1) / SC_TN));
     MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)hflag * nseg2 * Kp));
     MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)hflag * nseg2));
     MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), hflag, rows.as<int>(), Kp,

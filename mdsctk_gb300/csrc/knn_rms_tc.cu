@@ -155,6 +155,7 @@ __device__ __forceinline__ bool ep_sync(TcShared* S, int lane) {
     } else {
       uint64_t t0 = gtimer_ns();
       while (*gen == g) {
+        __nanosleep(64);
         if (*(volatile int*)&S->abortf) { ok = 0; break; }
         if (gtimer_ns() - t0 > 1000000000ull) {
           *(volatile int*)&S->abortf = 1;
@@ -223,7 +224,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
         for (int tile = t0; tile < t1 && ok; ++tile)
           for (int kb = 0; kb < nkb; ++kb) {
-            if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf)) { ok = false; break; }
+            if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
             unsigned char* st = stages + stage * TC_STAGE_BYTES;
             mbar_expect_tx(&S->full[stage], TC_STAGE_BYTES);
             tma_load_2d(st, &tmA, &S->full[stage], kb * TC_KB, rt * TC_M);
@@ -253,11 +254,11 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
         for (int tile = t0; tile < t1 && ok; ++tile, ++acc) {
           const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
-          if (!mbar_wait(&S->tempty[b], aph ^ 1, abortf)) { ok = false; break; }
+          if (!mbar_wait(&S->tempty[b], aph ^ 1, abortf, 1000000000ull, 64)) { ok = false; break; }
           tc_fence_after();
           const uint32_t d = tbase + b * 256;
           for (int kb = 0; kb < nkb; ++kb) {
-            if (!mbar_wait(&S->full[stage], phase, abortf)) { ok = false; break; }
+            if (!mbar_wait(&S->full[stage], phase, abortf, 1000000000ull, 64)) { ok = false; break; }
             tc_fence_after();
             const uint32_t st = sbase + stage * TC_STAGE_BYTES;
 #pragma unroll
@@ -363,9 +364,10 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             const int j = tile * TC_FR_N + gl;
             if (rowok && (g0 + c < 8) && j < Nr) {
               const float* cr = S->colrec + gl * MDS_REC;
-              float sv = screen_shifted_f32(G, rrec, cr, nofit != 0);
-              sv = fmaxf(sv - guard * (rrec[15] + cr[15]), 0.0f);
-              if (sv < *(volatile float*)&S->thr[rloc]) {
+              const float thr = *(volatile float*)&S->thr[rloc];
+              float sv = screen_shifted_f32(G, rrec, cr, nofit != 0, guard * (rrec[15] + cr[15]), thr);
+              sv = fmaxf(sv, 0.0f);
+              if (sv < thr) {
                 int pos = atomicAdd(&S->cnt[rloc], 1);
                 if (pos < TC_CAPG)
                   rowbuf[pos] = mds_pack_key(sv, j);
@@ -481,7 +483,7 @@ int tc_seg_stride() { return TC_CAPG; }
 
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
-                     int* cand_n) {
+                     int* cand_n, int* derr) {
   if (Kp + 2 * TC_FR_N > TC_CAPG)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen supports K' <= %d (k too large)",
                     TC_CAPG - 2 * TC_FR_N);
@@ -493,17 +495,28 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
   const int nitems = nrt * nseg;
   const int grid = std::min(nitems, ctx->num_sms);
   const size_t smem = TC_SMEM_BYTES;
-  MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static bool attr_set = false;  // set once: the call is also made while a stream is being captured
+  if (!attr_set) {
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  // With an external error flag the caller checks it after the stream is
+  // synchronised (the launch can then be captured in a CUDA graph).
   DevBuf err(ctx);
-  MDS_TRY(err.alloc(ctx, sizeof(int)));
-  MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, sizeof(int), ctx->stream));
+  int* e = derr;
+  if (!e) {
+    MDS_TRY(err.alloc(ctx, sizeof(int)));
+    e = err.as<int>();
+  }
+  MDS_CUDA(ctx, cudaMemsetAsync(e, 0, sizeof(int), ctx->stream));
   const float s = tc_scale(pl.prec);
   const uint32_t idesc = umma_idesc_f16(TC_M, TC_N, pl.prec == MDS_PREC_FP16X3 ? 0 : 1);
   ctx->stats.launches++;
   k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
-                                                       cand, cand_n, err.as<int>());
+                                                       cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
+  if (derr) return MDS_OK;
   int herr = 0;
   MDS_CUDA(ctx, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   MDS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

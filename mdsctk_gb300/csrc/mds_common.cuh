@@ -8,6 +8,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -17,7 +19,11 @@ struct mds_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   size_t hbm_budget = 0;  // 0 = no limit beyond what cudaMalloc gives
-  size_t hbm_in_use = 0;
+  size_t hbm_in_use = 0;  // bytes held by live buffers and by the cache
+  // Freed device blocks kept for reuse by later calls (size -> pointer).
+  // Every use of a block is ordered on `stream`, so a block returned here can
+  // be handed out again without synchronising.
+  std::multimap<size_t, void*> cache;
   std::string last_error;
   int num_sms = 0;
   // statistics of the last kNN call (exposed through mds_knn_stats)
@@ -28,6 +34,10 @@ struct mds_ctx {
 
 // Record an error message on the context and return `code`.
 int mds_fail(mds_ctx* ctx, int code, const char* fmt, ...);
+
+// Free cached device blocks until at most `keep` bytes remain cached
+// (synchronises the context's stream first).
+void mds_trim_cache(mds_ctx* ctx, size_t keep);
 
 #define MDS_CUDA(ctx, call)                                                        \
   do {                                                                             \
@@ -49,24 +59,36 @@ struct DevBuf {
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) {
-      cudaFree(p);
-      if (ctx) ctx->hbm_in_use -= bytes;
-    }
+    if (p && ctx) ctx->cache.emplace(bytes, p);  // stays counted in hbm_in_use
     p = nullptr;
     bytes = 0;
   }
-  // Returns MDS_OK or an error code (recorded on ctx).
+  // Returns MDS_OK or an error code (recorded on ctx). Sizes are rounded up
+  // to 4 KiB; a cached block of up to twice the size is reused.
   int alloc(mds_ctx* c, size_t n) {
     release();
     ctx = c;
-    if (n == 0) n = 16;
+    n = (std::max<size_t>(n, 16) + 4095) & ~(size_t)4095;
+    auto it = ctx->cache.lower_bound(n);
+    if (it != ctx->cache.end() && it->first <= 2 * n) {
+      bytes = it->first;
+      p = it->second;
+      ctx->cache.erase(it);
+      return MDS_OK;
+    }
+    if (ctx->hbm_budget && ctx->hbm_in_use + n > ctx->hbm_budget) mds_trim_cache(ctx, 0);
     if (ctx->hbm_budget && ctx->hbm_in_use + n > ctx->hbm_budget)
       return mds_fail(ctx, MDS_ERR_NOMEM, "HBM budget exceeded: need %zu more bytes (in use %zu, budget %zu)",
                       n, ctx->hbm_in_use, ctx->hbm_budget);
     cudaError_t e = cudaMalloc(&p, n);
     if (e != cudaSuccess) {
+      cudaGetLastError();
+      mds_trim_cache(ctx, 0);
+      e = cudaMalloc(&p, n);
+    }
+    if (e != cudaSuccess) {
       p = nullptr;
+      cudaGetLastError();
       return mds_fail(ctx, MDS_ERR_NOMEM, "cudaMalloc(%zu): %s", n, cudaGetErrorString(e));
     }
     bytes = n;

@@ -159,10 +159,17 @@ __device__ inline double qcp_rotation_fp64(const double* S, double e0half, doubl
 // Screen value (lower bound of RMSD^2, nm^2) from the deviation Gram
 // G[3*c+d] = sum a_i^c a_j^d of fit frame i (row record r) and reference
 // frame j (column record q). nofit: plain |a_i - a_j|^2.
+//
+// `guard` is subtracted from the result (the rounding margin of the caller's
+// Gram). When a cheap lower bound already reaches `thr`, that bound is
+// returned without the quartic solve (the caller rejects such pairs anyway):
+// with g >= lambda_max(D') (Gershgorin), nu <= (g + sqrt(g^2 + 4|b|^2)) / 2,
+// the largest eigenvalue of [[0, |b|], [|b|, g]], which dominates K'.
 __device__ __forceinline__ float screen_shifted_f32(const float* G, const float* r, const float* q,
-                                                    bool nofit) {
+                                                    bool nofit, float guard = 0.0f,
+                                                    float thr = __builtin_huge_valf()) {
   float D = r[15] + q[15] - 2.0f * (G[0] + G[4] + G[8]);
-  if (nofit) return fmaxf(D, 0.0f);
+  if (nofit) return fmaxf(D - guard, 0.0f);
   // symmetric part of S
   float sxx = r[0] + q[6] + G[0];
   float syy = r[1] + q[7] + G[4];
@@ -177,13 +184,20 @@ __device__ __forceinline__ float screen_shifted_f32(const float* G, const float*
   // D' = lower-right block of K - tr(S) I
   float d00 = -2.0f * (syy + szz), d11 = -2.0f * (sxx + szz), d22 = -2.0f * (sxx + syy);
   float d01 = 2.0f * sxy, d02 = 2.0f * sxz, d12 = 2.0f * syz;
+  float beta0 = b0 * b0 + b1 * b1 + b2 * b2;
+  {
+    float g = fmaxf(fmaxf(d00 + fabsf(d01) + fabsf(d02), d11 + fabsf(d01) + fabsf(d12)),
+                    d22 + fabsf(d02) + fabsf(d12));
+    float nu_up = 0.5f * (g + sqrtf(fmaf(g, g, 4.0f * beta0)));
+    float lb = D - 2.0f * fmaxf(nu_up, 0.0f) - guard;
+    if (lb >= thr) return lb;
+  }
   // adjugate of D' (symmetric)
   float a00 = d11 * d22 - d12 * d12, a11 = d00 * d22 - d02 * d02, a22 = d00 * d11 - d01 * d01;
   float a01 = d02 * d12 - d01 * d22, a02 = d01 * d12 - d02 * d11, a12 = d01 * d02 - d00 * d12;
   float t = d00 + d11 + d22;
   float m2 = a00 + a11 + a22;
   float det = d00 * a00 + d01 * a01 + d02 * a02;
-  float beta0 = b0 * b0 + b1 * b1 + b2 * b2;
   float Db0 = d00 * b0 + d01 * b1 + d02 * b2;
   float Db1 = d01 * b0 + d11 * b1 + d12 * b2;
   float Db2 = d02 * b0 + d12 * b1 + d22 * b2;
@@ -200,5 +214,5 @@ __device__ __forceinline__ float screen_shifted_f32(const float* G, const float*
     float step = (qd > 0.0f) ? qv / qd : 0.0f;
     nu = fmaxf(nu - fmaxf(step, 0.0f), 0.0f);
   }
-  return fmaxf(D - 2.0f * nu, 0.0f);
+  return fmaxf(D - 2.0f * nu - guard, 0.0f);
 }

@@ -43,9 +43,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Wait for the phase of parity `parity`; gives up after `limit_ns` or when
 // *abortf is set, setting *abortf itself on a timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abortf,
-                                          uint64_t limit_ns = 1000000000ull) {
+                                          uint64_t limit_ns = 1000000000ull, unsigned max_backoff_ns = 256) {
   if (mbar_try_wait(bar, parity)) return true;
   uint64_t t0 = gtimer_ns();
+  unsigned backoff = 8;
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abortf) return false;
@@ -53,6 +54,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
       *abortf = 1;
       return false;
     }
+    // back off so that a waiting warp does not take issue slots from the
+    // warps of its SM sub-partition that have work
+    __nanosleep(backoff);
+    if (backoff < max_backoff_ns) backoff <<= 1;
   }
 }
 
