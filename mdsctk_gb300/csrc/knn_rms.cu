@@ -358,11 +358,9 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
                        int nseg, uint64_t* cand, int* cand_n) {
   size_t smem = screen_fp32_smem(Kp);
   static bool attr_set = false;  // once: launches may also happen while a stream is captured
-  if (!attr_set) {
-    MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr_set = true;
-  }
-  if (smem > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "screen shared memory %zu", smem);
+  static size_t limit = 0;
+  MDS_TRY(mds_allow_dyn_smem(ctx, k_screen_fp32, &attr_set, &limit));
+  if (smem > limit) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "screen shared memory %zu > %zu", smem, limit);
   int nrt = (nrows + SC_TM - 1) / SC_TM;
   ctx->stats.launches++;
   k_screen_fp32<<<nrt * nseg, SC_THREADS, smem, ctx->stream>>>(
@@ -665,10 +663,9 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const do
   if (smem > 227 * 1024)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck needs %zu bytes of shared memory (natoms/k too large)", smem);
   static bool attr_set = false;  // once: launches may also happen while a stream is captured
-  if (!attr_set) {
-    MDS_CUDA(ctx, cudaFuncSetAttribute(k_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr_set = true;
-  }
+  static size_t limit = 0;
+  MDS_TRY(mds_allow_dyn_smem(ctx, k_recheck, &attr_set, &limit));
+  if (smem > limit) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck shared memory %zu > %zu", smem, limit);
   if (nrows > 0) ctx->stats.launches++;
   if (nrows > 0)
     k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Yf, Ef, Yr, Er, nrows, rowlist, pl.nref, pl.Ap,

@@ -105,6 +105,26 @@ struct DevBuf {
     if (_r != MDS_OK) return _r;   \
   } while (0)
 
+// Let `kernel` use all the dynamic shared memory the device allows next to its
+// static shared memory. Done once per kernel (*done), so that later launches
+// (also those made while a stream is captured) need no attribute call.
+template <class Kernel>
+int mds_allow_dyn_smem(mds_ctx* ctx, Kernel kernel, bool* done, size_t* limit) {
+  if (!*done) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return mds_fail(ctx, MDS_ERR_CUDA, "cudaFuncGetAttributes");
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    int dyn = optin - (int)fa.sharedSizeBytes;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    if (e != cudaSuccess)
+      return mds_fail(ctx, MDS_ERR_CUDA, "cudaFuncSetAttribute(%d): %s", dyn, cudaGetErrorString(e));
+    *limit = (size_t)dyn;
+    *done = true;
+  }
+  return MDS_OK;
+}
+
 static inline int mds_round_up(int x, int m) { return (x + m - 1) / m * m; }
 
 // Stable LSD radix sort (8-bit digits over the bits set in `mask`) of n

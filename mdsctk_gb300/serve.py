@@ -37,6 +37,7 @@ class Server:
         self.h = h
         self.k = min(k, self.n - 1)
         self.nev = nev
+        self._sizes = {}  # ticket -> frames (dict operations are atomic under the GIL)
 
     def _check(self, rc):
         if rc != L.MDS_OK:
@@ -55,11 +56,10 @@ class Server:
         t = ctypes.c_int64(0)
         self._check(self._lib.mds_server_submit(self.h, q.ctypes.data_as(ctypes.c_void_p), q.shape[0],
                                                 ctypes.byref(t)))
-        self._sizes = getattr(self, "_sizes", {})
         self._sizes[t.value] = q.shape[0]
         return t.value
 
-    def wait(self, ticket: int, timeout_ms: int = 600000):
+    def wait(self, ticket: int, timeout_ms: int = 120000):
         m = self._sizes.pop(ticket)
         ext = np.zeros((self.nev, m))
         d = np.zeros((m, self.k))
