@@ -132,6 +132,27 @@ int mds_knn_data(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, 
                  int dim, int k, unsigned flags, double* out_d, int32_t* out_i, int* k_used);
 
 /*
+ * knn_data without device allocation. This entry point has no counterpart in
+ * the reference. It is for callers that cannot allocate device memory where
+ * they call: a thread that is capturing a CUDA stream into a graph (cudaMalloc
+ * is not allowed during a global-mode capture), or a process whose device
+ * memory is held entirely by another allocator. It computes what mds_knn_data
+ * computes (same outputs), takes DEVICE pointers for every array, and keeps
+ * all of its scratch in one fixed 32 MiB array inside the library, so it
+ * calls no cudaMalloc/cudaFree. Problems whose scratch would exceed 32 MiB
+ * (about n_fit * (2(k+1) rounded up to 32) * 8 bytes of candidates plus n *
+ * dim * 4 bytes of vectors) are rejected with MDS_ERR_UNSUPPORTED.
+ *   flags: 0 or MDS_CORRELATION (sorted output only).
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture. Calls share the array: calls that
+ * may overlap on the GPU (other contexts or threads) race and must be
+ * serialised by the caller. Every GPU that loads the library holds the 32 MiB
+ * until the process exits.
+ */
+int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, int n_fit, int dim, int k,
+                         unsigned flags, double* out_d, int32_t* out_i, int* k_used);
+
+/*
  * make_sysparse: kNN lists -> symmetric sparse matrix holding one strict
  * triangle of distances, CSC (column c holds rows r > c, ascending).
  * Replaces make_sysparse.cpp:225-329 (Berkeley-DB B-tree insertion with

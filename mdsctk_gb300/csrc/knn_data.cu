@@ -501,3 +501,135 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   }
   return MDS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant (mds_knn_data_noalloc). Some callers cannot obtain
+// device memory at the point of the call: a host thread capturing a stream
+// into a CUDA graph (cudaMalloc is not allowed during a global-mode capture),
+// or a process whose device memory is reserved in full by another allocator.
+// This entry point takes device inputs and outputs and keeps every scratch
+// buffer in one file-scope device array of fixed size, so it never calls
+// cudaMalloc or cudaFree. Every GPU that loads this library holds the array
+// until the process exits.
+// ---------------------------------------------------------------------------
+#define MDS_NOALLOC_SCRATCH_BYTES (32u << 20)  // 32 MiB
+
+static __device__ __align__(256) unsigned char g_knn_data_scratch[MDS_NOALLOC_SCRATCH_BYTES];
+
+// Device address of the array, taken once per device with that device
+// current (the host symbol g_knn_data_scratch is only a stand-in for it).
+static void* noalloc_scratch(mds_ctx* ctx) {
+  static void* addr[256] = {nullptr};
+  int dev = ctx->device;
+  if (dev < 0 || dev >= 256) return nullptr;
+  if (!addr[dev]) {
+    cudaSetDevice(dev);
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_knn_data_scratch) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    addr[dev] = p;
+  }
+  return addr[dev];
+}
+
+extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, int n_fit,
+                                    int dim, int k, unsigned flags, double* out_d, int32_t* out_i, int* k_used) {
+  if (!ctx) return MDS_ERR_ARG;
+  ctx->stats = mds_knn_stats{};
+  if (!ref || !out_d || !out_i) return mds_fail(ctx, MDS_ERR_ARG, "null array argument");
+  if (n_ref < 1 || dim < 1 || n_fit < 0)
+    return mds_fail(ctx, MDS_ERR_ARG, "invalid sizes: n_ref=%d n_fit=%d dim=%d", n_ref, n_fit, dim);
+  if (flags & ~(MDS_CORRELATION | MDS_DEVICE_IO))
+    return mds_fail(ctx, MDS_ERR_ARG, "mds_knn_data_noalloc accepts only MDS_CORRELATION (inputs are device pointers)");
+  const bool corr = (flags & MDS_CORRELATION) != 0;
+  const bool same = (fit == nullptr);
+  if (same) n_fit = n_ref;
+  if (k < 0) return mds_fail(ctx, MDS_ERR_ARG, "k must be >= 0");
+  if (n_ref - 1 < k) k = n_ref - 1;  // knn_data.cpp:186-188
+  if (k_used) *k_used = k;
+  if (n_fit == 0 || k == 0) return MDS_OK;
+  const int Dp = mds_round_up(dim, DT_KC);
+  const int Kp = std::min(mds_round_up(std::max(k + 1 + 32, 2 * (k + 1)), 32), 448);
+  if (Kp < k + 1 + 16) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k=%d too large", k);
+  // scratch layout, 256-byte aligned pieces
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t need = 0;
+  const size_t o_xr = need;  need += up(sizeof(float) * (size_t)n_ref * Dp);
+  const size_t o_nr = need;  need += up(sizeof(float) * (size_t)n_ref);
+  const size_t o_mr = need;  need += up(sizeof(double) * (size_t)n_ref);
+  const size_t o_sr = need;  need += up(sizeof(double) * (size_t)n_ref);
+  size_t o_xf = 0, o_nf = 0, o_mf = 0, o_sf = 0;
+  if (!same) {
+    o_xf = need;  need += up(sizeof(float) * (size_t)n_fit * Dp);
+    o_nf = need;  need += up(sizeof(float) * (size_t)n_fit);
+    o_mf = need;  need += up(sizeof(double) * (size_t)n_fit);
+    o_sf = need;  need += up(sizeof(double) * (size_t)n_fit);
+  }
+  const size_t o_cand = need;  need += up(sizeof(uint64_t) * (size_t)n_fit * Kp);
+  const size_t o_cn = need;    need += up(sizeof(int) * (size_t)n_fit);
+  const size_t o_fl = need;    need += up(sizeof(int) * (size_t)n_fit);
+  const size_t o_nfl = need;   need += up(sizeof(int));
+  if (need > MDS_NOALLOC_SCRATCH_BYTES)
+    return mds_fail(ctx, MDS_ERR_UNSUPPORTED,
+                    "mds_knn_data_noalloc: this problem needs %zu bytes of scratch, more than the fixed %u bytes "
+                    "(use mds_knn_data)", need, (unsigned)MDS_NOALLOC_SCRATCH_BYTES);
+  unsigned char* base = static_cast<unsigned char*>(noalloc_scratch(ctx));
+  if (!base) return mds_fail(ctx, MDS_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  float* xr = reinterpret_cast<float*>(base + o_xr);
+  float* nr = reinterpret_cast<float*>(base + o_nr);
+  double* mr = reinterpret_cast<double*>(base + o_mr);
+  double* sr = reinterpret_cast<double*>(base + o_sr);
+  const float* xf = xr;
+  const float* nf = nr;
+  const double* mf = mr;
+  const double* sf = sr;
+  k_vec_prep<<<(n_ref + 127) / 128, 128, 0, s>>>(ref, n_ref, dim, Dp, corr, xr, nr, mr, sr);
+  if (!same) {
+    float* xf2 = reinterpret_cast<float*>(base + o_xf);
+    float* nf2 = reinterpret_cast<float*>(base + o_nf);
+    double* mf2 = reinterpret_cast<double*>(base + o_mf);
+    double* sf2 = reinterpret_cast<double*>(base + o_sf);
+    k_vec_prep<<<(n_fit + 127) / 128, 128, 0, s>>>(fit, n_fit, dim, Dp, corr, xf2, nf2, mf2, sf2);
+    xf = xf2; nf = nf2; mf = mf2; sf = sf2;
+  }
+  MDS_CUDA(ctx, cudaGetLastError());
+  uint64_t* cand = reinterpret_cast<uint64_t*>(base + o_cand);
+  int* cand_n = reinterpret_cast<int*>(base + o_cn);
+  int* flagged = reinterpret_cast<int*>(base + o_fl);
+  int* nflag = reinterpret_cast<int*>(base + o_nfl);
+  // the array keeps the previous call's contents: the flag counter restarts at zero
+  MDS_CUDA(ctx, cudaMemsetAsync(nflag, 0, sizeof(int), s));
+  const size_t ssm = screen_dot_smem(Kp);
+  if (ssm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k too large");
+  MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+  const int nrt = (n_fit + DT_TM - 1) / DT_TM;
+  k_screen_dot<<<nrt, DT_THREADS, ssm, s>>>(xf, xr, nf, nr, n_fit, nullptr, n_ref, Dp, corr, 1.0f / 65536.0f, Kp, 1,
+                                            cand, cand_n);
+  MDS_CUDA(ctx, cudaGetLastError());
+  const double* dfit = same ? ref : fit;
+  size_t rsm = data_recheck_smem(dim, Kp, 1, k, 0);
+  if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
+  MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
+  k_data_recheck<<<n_fit, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, n_fit, nullptr, n_ref, dim, corr, 0,
+                                                cand, cand_n, 1, Kp, k, out_d, out_i, flagged, nflag);
+  MDS_CUDA(ctx, cudaGetLastError());
+  int hflag = 0;
+  MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  ctx->stats.rows_flagged = hflag;
+  if (hflag > 0) {
+    // rows whose guard failed: every reference vector is rechecked exactly
+    rsm = data_recheck_smem(dim, 1, 1, k, 1);
+    if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
+    k_data_recheck<<<hflag, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, hflag, flagged, n_ref, dim, corr, 1,
+                                                  nullptr, nullptr, 1, 1, k, out_d, out_i, flagged, nflag);
+    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  }
+  return MDS_OK;
+}
