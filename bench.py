@@ -53,7 +53,245 @@ def parse():
     p.add_argument("--k", type=int, default=K)
     p.add_argument("--cpu-rows", type=int, default=0, help="fit rows of the CPU sample (0 = auto)")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--serve", action="store_true",
+                   help="Nystrom serving benchmark (50,000 landmarks x 304 atoms, k=50, nev=10)")
+    p.add_argument("--serve-seconds", type=float, default=8.0)
+    p.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate, requests/s")
+    p.add_argument("--pipeline", choices=["small", "scale", "euclid"],
+                   help="per-stage wall time of a whole pipeline: small = 2,000 x 304 frames (parity vs the oracle), "
+                        "scale = 100,000 x 304 (kNN k=64, sysparse, Lanczos nev=20 ncv=60 tol=1e-8), "
+                        "euclid = knn_data 200,000 x 64, k=32")
+    p.add_argument("--pipeline-cpu", action="store_true", help="also time the CPU oracle's sysparse and eigsh")
+    p.add_argument("--precision-report", action="store_true",
+                   help="per-pair screen RMSD error vs FP64 and output agreement on sampled rows")
     return p.parse_args()
+
+
+def run_serve(args):
+    """Serving: landmarks stay resident; requests of 1-4096 frames (log-uniform
+    sizes, 90% from the basin generator, 10% off-manifold) arrive as a Poisson
+    stream; latency = submit -> results. The plain path serves one request at a
+    time (one slot, no batching, no CUDA graphs) on the same arrival stream."""
+    import numpy as np
+    import threading
+
+    from mdsctk_gb300 import Context, synth
+    from mdsctk_gb300.serve import Server
+
+    natoms, n_land, k, nev = 304, 50_000, 50, 10
+    land = synth.trajectory(n_land, natoms, seed=SEED + 5, basins=16, dwell=500.0)
+    m = np.ones(natoms, np.float32)
+    with Context(0) as c:
+        d, _ = c.knn_rms(land, None, m, k, precision=args.precision)
+    sigma = float(np.median(d))
+    rng = np.random.default_rng(SEED + 6)
+    nreq = max(8, int(args.serve_rate * args.serve_seconds))
+    sizes = np.exp(rng.uniform(0, np.log(4096), nreq)).astype(int).clip(1, 4096)
+    gaps = rng.exponential(1.0 / args.serve_rate, nreq)
+    pool = synth.trajectory(8192, natoms, seed=SEED + 7, basins=16, dwell=500.0, off_manifold=0.1, off_sigma=0.3)
+    starts = rng.integers(0, 8192 - 4096, nreq)
+
+    def run(batched):
+        srv = Server(land, m, k=k, sigma=sigma, nev=nev, precision=args.precision, max_batch_frames=4096)
+        # warm every size bucket of every slot (graph capture happens on first use)
+        for b in (1, 2, 4, 8, 16, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096):
+            for t in [srv.submit(pool[:b]) for _ in range(srv.stats()["slots"])]:
+                srv.wait(t)
+        lat, done = [None] * nreq, threading.Event()
+        tickets = [None] * nreq
+
+        def waiter():
+            for j in range(nreq):
+                while tickets[j] is None:
+                    time.sleep(1e-4)
+                _, _, _, info = srv.wait(tickets[j])
+                lat[j] = info["total_ms"]
+            done.set()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        tnext = t0
+        for j in range(nreq):
+            tnext += gaps[j]
+            while time.perf_counter() < tnext:
+                time.sleep(2e-5)
+            tickets[j] = srv.submit(pool[starts[j]:starts[j] + sizes[j]])
+        done.wait()
+        wall = time.perf_counter() - t0
+        th.join()
+        st = srv.stats()
+        srv.close()
+        lat = np.array(lat)
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "queries_per_s": float(sizes.sum() / wall),
+                "requests_per_s": float(nreq / wall), "batches": st["batches"],
+                "graph_launches": st["graph_launches"], "slots": st["slots"], "rows_flagged": st["rows_flagged"],
+                "model_knn_ms": st["model_knn_ms"], "model_decomp_ms": st["model_decomp_ms"]}
+
+    def run_plain():
+        # one request at a time, no batching and no graphs: measure each
+        # request's service time alone, then queue them FIFO on the same
+        # Poisson arrival times (latency = finish - arrival)
+        srv = Server(land, m, k=k, sigma=sigma, nev=nev, precision=args.precision, max_batch_frames=4096,
+                     slots=1, use_graphs=False)
+        srv.wait(srv.submit(pool[:4096]))
+        svc = np.zeros(nreq)
+        for j in range(nreq):
+            t0 = time.perf_counter()
+            srv.wait(srv.submit(pool[starts[j]:starts[j] + sizes[j]]))
+            svc[j] = time.perf_counter() - t0
+        srv.close()
+        arr = np.cumsum(gaps)
+        fin, lat = 0.0, np.zeros(nreq)
+        for j in range(nreq):
+            fin = max(arr[j], fin) + svc[j]
+            lat[j] = (fin - arr[j]) * 1e3
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "queries_per_s": float(sizes.sum() / max(fin, arr[-1])),
+                "service_ms_mean": float(svc.mean() * 1e3)}
+
+    res_b = run(True)
+    res_p = run_plain()
+    out = {"metric": "Nystrom serving latency", "unit": "ms", "higher_is_better": False, "value": res_b["p99_ms"],
+           "data": "synthetic", "dtype": args.precision,
+           "config": {"workload": f"Nystrom serving: {n_land} landmarks x {natoms} atoms, k={k}, nev={nev}, "
+                                  f"requests of 1-4096 frames (log-uniform), Poisson {args.serve_rate}/s, "
+                                  f"10% off-manifold", "requests": nreq, "sigma_A": sigma},
+           "batched": res_b, "plain_per_request": res_p}
+    print(json.dumps(out))
+    return 0
+
+
+def run_precision_report(args):
+    """Screen precision vs FP64 on two workloads: the benchmark trajectory
+    (all pairs, sampled rows) and the serving case (off-trajectory queries
+    against 50,000 landmarks, where neighbour distances are concentrated).
+    Per candidate pair of the screen (the 256 smallest bounds of a row):
+    coef = (screen value before the guard - exact RMSD^2) / (|a_i|^2 + |a_j|^2),
+    the quantity the guard c * (|a_i|^2 + |a_j|^2) must cover (positive =
+    over-estimate); the guard in use per precision; how many bounds exceed
+    the exact value (must be 0); and knn_rms output agreement with the oracle."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from mdsctk_gb300 import Context, synth
+
+    O.build()
+    guards = {"fp32": 2.0 ** -16, "bf16x3": 2.0 ** -14, "fp16x3": 2.0 ** -14}  # MDS_GUARD_FP32 / _TC
+    rep = {"metric": "kNN-RMSD screen error vs FP64"}
+    x = workload(args.frames, args.atoms)
+    land = synth.trajectory(50_000, 304, seed=SEED + 5, basins=16, dwell=500.0)
+    qry = synth.trajectory(64, 304, seed=SEED + 7, basins=16, dwell=500.0, off_manifold=0.1, off_sigma=0.3)
+    cases = {"trajectory": (x, x[np.linspace(0, x.shape[0] - 1, 64).astype(int)], args.k),
+             "serving_queries": (land, qry, 50)}
+    with Context(0) as c:
+        for name, (ref, fit, k) in cases.items():
+            m = np.ones(ref.shape[1], np.float32)
+            _, rec = c.knn_rms_superpose(np.concatenate([ref, fit]), m)  # one template: ref[0]
+            Ea_r, Ea_f = rec[:ref.shape[0], 15].astype(np.float64), rec[ref.shape[0]:, 15].astype(np.float64)
+            exact = [dict() for _ in range(len(fit))]
+            out = {"config": {"ref_frames": ref.shape[0], "atoms": ref.shape[1], "fit_rows": len(fit), "k": k}}
+            for prec, guard in guards.items():
+                lb, idx, cnt = c.knn_rms_screen(ref, fit, m, 256, precision=prec)
+                coefs, viol = [], 0
+                for r in range(len(fit)):
+                    need = [j for j in idx[r] if j not in exact[r]]
+                    if need:
+                        ed, _ = O.knn_rms(ref[need], fit[r:r + 1], m, 0, sort=False)
+                        for jj, j in enumerate(need):
+                            exact[r][j] = (ed[0, jj] / 10.0) ** 2
+                    ex2 = np.array([exact[r][j] for j in idx[r]])
+                    E = Ea_f[r] + Ea_r[idx[r]]
+                    viol += int(np.sum(lb[r] > ex2 * (1 + 1e-6) + 1e-12))
+                    ok = lb[r] > 0  # unclamped values only
+                    coefs.append(((lb[r] + guard * E) - ex2)[ok] / E[ok])
+                cf = np.concatenate(coefs)
+                d, i = c.knn_rms(ref, fit, m, k, precision=prec)
+                st = c.stats()
+                od, oi = O.knn_rms(ref, fit, m, k)
+                out[prec] = {"guard_c": guard, "coef_max": float(cf.max()), "coef_p99_abs": float(np.percentile(
+                    np.abs(cf), 99)), "coef_p50_abs": float(np.percentile(np.abs(cf), 50)), "pairs": int(cf.size),
+                    "bounds_above_exact": viol, "mean_Ea_nm2": float(np.mean(Ea_f)),
+                    "rows_flagged": st["rows_flagged"], "output_max_abs_err_A": float(np.max(np.abs(d - od))),
+                    "index_agreement": float(np.mean(i == oi))}
+            rep[name] = out
+    print(json.dumps(rep))
+    return 0
+
+
+def run_pipeline(args):
+    """Per-stage wall time (host arrays in and out, as the tools run) of one
+    pipeline; each stage is timed once after one untimed run of the same
+    stage. 'small' also checks every stage against the oracle."""
+    import numpy as np
+
+    from mdsctk_gb300 import Context, synth
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    out = {"metric": "pipeline stage wall time", "unit": "s", "pipeline": args.pipeline, "data": "synthetic"}
+    st = {}
+
+    def timed(name, fn, ctx=None):
+        fn()
+        t0 = time.perf_counter()
+        r = fn()
+        st[name] = time.perf_counter() - t0
+        if ctx is not None:
+            st[name + "_stats"] = ctx.stats()
+        return r
+
+    with Context(0) as c:
+        if args.pipeline in ("small", "scale"):
+            n, k, nev = (2000, 50, 10) if args.pipeline == "small" else (100_000, 64, 20)
+            ncv, tol = (0, 0.0) if args.pipeline == "small" else (60, 1e-8)
+            x = synth.trajectory(n, 304, seed=SEED + 11, basins=1 if args.pipeline == "small" else 16,
+                                 drift_sigma=0.05, dwell=500.0)
+            m = np.ones(304, np.float32)
+            out["config"] = {"workload": f"knn_rms {n} x 304, k={k}; make_sysparse; decomp_sparse nev={nev} "
+                                         f"ncv={ncv or 'min(10 nev + 1, n)'} tol={tol}", "precision": args.precision}
+            d, i = timed("knn_rms", lambda: c.knn_rms(x, None, m, k, precision=args.precision), c)
+            sigma = float(np.median(d))
+            nn, pcol, irow, val = timed("make_sysparse", lambda: c.sysparse(d, i))
+            w, V, res, nconv = timed("decomp_sparse",
+                                     lambda: c.decomp_sparse(nn, pcol, irow, val, sigma, nev, ncv=ncv, tol=tol), c)
+            st["nconv"] = nconv
+            st["max_residual"] = float(np.max(res))
+            st["pairs_per_s"] = n * n / st["knn_rms"]
+            if args.pipeline == "small":
+                od, oi = O.knn_rms(x, None, m, k)
+                st["parity_knn_max_abs_err_A"] = float(np.max(np.abs(d - od)))
+                st["parity_knn_index_agreement"] = float(np.mean(i == oi))
+                on, op, oir, ov = O.sysparse(d, i)
+                st["parity_sysparse_bit_exact"] = bool(np.array_equal(pcol, op) and np.array_equal(irow, oir)
+                                                       and np.array_equal(val, ov))
+                M = O.dense_affinity(nn, pcol, irow, val, sigma)
+                ex = np.linalg.eigvalsh(M)[::-1][:nev]
+                st["parity_evals_max_rel_err"] = float(np.max(np.abs(w - ex) / np.abs(ex)))
+            if args.pipeline_cpu:
+                t0 = time.perf_counter()
+                O.sysparse(d, i)
+                st["cpu_make_sysparse"] = time.perf_counter() - t0
+                t0 = time.perf_counter()
+                O.decomp_sparse(nn, pcol, irow, val, sigma, nev, ncv=ncv or None, tol=tol)
+                st["cpu_decomp_sparse_eigsh"] = time.perf_counter() - t0
+        else:
+            n, dim, k = 200_000, 64, 32
+            x = synth.dihedral_vectors(n, dim, seed=SEED + 13).astype(np.float64)
+            out["config"] = {"workload": f"knn_data {n} x {dim} (f64), k={k}"}
+            d, i = timed("knn_data", lambda: c.knn_data(x, None, k), c)
+            st["pairs_per_s"] = n * n / st["knn_data"]
+            rows = np.linspace(0, n - 1, 256).astype(int)
+            od, oi = O.knn_data(x, x[rows], k)
+            st["parity_rows_checked"] = len(rows)
+            st["parity_bit_exact_distances"] = bool(np.array_equal(d[rows], od))
+    out["stages"] = st
+    print(json.dumps(out))
+    return 0
 
 
 def workload(frames, atoms):
@@ -176,6 +414,12 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve:
+        return run_serve(args)
+    if args.precision_report:
+        return run_precision_report(args)
+    if args.pipeline:
+        return run_pipeline(args)
     import numpy as np
     import torch
 

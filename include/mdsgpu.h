@@ -153,6 +153,34 @@ int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, const doubl
                          unsigned flags, double* out_d, int32_t* out_i, int* k_used);
 
 /*
+ * GROMACS .xtc trajectories, the input format of knn_rms (read through
+ * GROMACS in the reference: read_first_xtc / read_next_xtc,
+ * knn_rms.cpp:155-203; XTC_file, mdsctk.cpp:217-267).
+ *
+ * mds_xtc_index walks the frame headers of an in-memory .xtc file (host
+ * code, no context). With offsets == NULL it only counts: *nframes frames of
+ * *natoms atoms. Otherwise offsets [max_frames] receives the byte offset of
+ * every frame and, if room is left, the end offset after the last one
+ * (pass max_frames >= nframes + 1). A truncated last frame is not counted
+ * (read_next_xtc stops there). Returns MDS_ERR_ARG on a bad magic number or
+ * a change of atom count.
+ */
+int mds_xtc_index(const unsigned char* buf, size_t len, int64_t* offsets, int max_frames, int* nframes,
+                  int* natoms);
+
+/*
+ * mds_xtc_decode decodes nframes frames (offsets [nframes + 1] from
+ * mds_xtc_index) on the GPU, one thread per frame, into xyz
+ * [nframes][natoms][3] float nm, exactly as GROMACS decodes them
+ * (int * (float)(1/precision)). buf is host memory; with MDS_DEVICE_IO, xyz
+ * is a device pointer and the frames stay in HBM for mds_knn_rms. steps,
+ * times [nframes] and boxes [nframes][9] are optional host outputs (NULL to
+ * skip). A malformed frame returns MDS_ERR_ARG naming the frame.
+ */
+int mds_xtc_decode(mds_ctx* ctx, const unsigned char* buf, size_t len, const int64_t* offsets, int nframes,
+                   int natoms, unsigned flags, float* xyz, int* steps, float* times, float* boxes);
+
+/*
  * make_sysparse: kNN lists -> symmetric sparse matrix holding one strict
  * triangle of distances, CSC (column c holds rows r > c, ascending).
  * Replaces make_sysparse.cpp:225-329 (Berkeley-DB B-tree insertion with
@@ -203,6 +231,39 @@ int mds_decomp_sparse_nystrom(mds_ctx* ctx, int n, const int32_t* pcol, const in
                               int m, const int32_t* pcolB, const int32_t* irowB, const double* distB,
                               double sigma, int nev, int ncv, double tol, int maxiter, unsigned flags,
                               double* evals, double* evecs, double* ext, double* resid, int* nconv);
+
+/*
+ * auto_decomp_sparse: decomp_sparse with a sigma per landmark instead of one
+ * sigma. Landmark x's list is its stored distances in neighbour-index order,
+ * cut to the first k_sigma entries, then sorted; sigma_x = sum / k_sigma
+ * (auto_decomp_sparse.cpp:153-168). perplexity > 0 (-K) replaces them by
+ * entropic-affinity sigmas, the distribution over the k_sigma sorted
+ * distances having perplexity K (mdsctk.cpp:388-565; agrees with the
+ * reference to the root-finding tolerance, as the reference warm-starts each
+ * landmark from the previous one). Affinity exp(-d^2 / (2 s_c s_r)) of the
+ * stored entry's column c and row r (:180-182); the rest as decomp_sparse.
+ * Replaces auto_decomp_sparse.cpp:135-258. sigmas [n] receives the sigmas
+ * (may be NULL). k_sigma <= 4096; with perplexity, every landmark must hold
+ * at least k_sigma >= ceil(K) distances (the reference reads past shorter
+ * lists), else MDS_ERR_ARG.
+ */
+int mds_auto_decomp_sparse(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow, const double* dist,
+                           int k_sigma, double perplexity, int nev, int ncv, double tol, int maxiter, unsigned flags,
+                           double* evals, double* evecs, double* resid, int* nconv, double* sigmas);
+
+/*
+ * auto_decomp_sparse_nystrom: auto_decomp_sparse plus the Nystrom extension;
+ * B's affinity uses the landmark's sigma twice, exp(-d^2 / (2 s_l s_l))
+ * (auto_decomp_sparse_nystrom.cpp:171-173). The reference tool accepts -K
+ * but never applies it (its perplexity switch is not set); its CLI here
+ * passes perplexity 0 the same way. Replaces
+ * auto_decomp_sparse_nystrom.cpp:140-285.
+ */
+int mds_auto_decomp_sparse_nystrom(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow,
+                                   const double* dist, int m, const int32_t* pcolB, const int32_t* irowB,
+                                   const double* distB, int k_sigma, double perplexity, int nev, int ncv, double tol,
+                                   int maxiter, unsigned flags, double* evals, double* evecs, double* ext,
+                                   double* resid, int* nconv, double* sigmas);
 
 /*
  * Resident Nystrom serving (no single reference counterpart: it keeps on the

@@ -99,6 +99,11 @@ SIGNATURES = {
     "mds_server_get_stats": ([_vp, ctypes.POINTER(ServerStats)], _i),
     "mds_decomp_sparse_nystrom": ([_vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _d, _i, _i, _d, _i, _u, _vp, _vp,
                                    _vp, _vp, _ip], _i),
+    "mds_xtc_index": ([_vp, _sz, _vp, _i, _ip, _ip], _i),
+    "mds_xtc_decode": ([_vp, _vp, _sz, _vp, _i, _i, _u, _vp, _vp, _vp, _vp], _i),
+    "mds_auto_decomp_sparse": ([_vp, _i, _vp, _vp, _vp, _i, _d, _i, _i, _d, _i, _u, _vp, _vp, _vp, _ip, _vp], _i),
+    "mds_auto_decomp_sparse_nystrom": ([_vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _i, _i, _d, _i, _u,
+                                        _vp, _vp, _vp, _vp, _ip, _vp], _i),
 }
 
 _lib = None

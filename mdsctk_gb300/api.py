@@ -56,6 +56,32 @@ class Context:
     def __exit__(self, *a):
         self.close()
 
+    def xtc_read(self, path_or_bytes, device_out: bool = False):
+        """Read a GROMACS .xtc trajectory (decoded on the GPU): returns
+        (xyz [frames, atoms, 3] float32 nm, steps, times). With device_out the
+        frames come back as a torch CUDA tensor, ready for knn_rms."""
+        b = path_or_bytes if isinstance(path_or_bytes, (bytes, bytearray)) else open(path_or_bytes, "rb").read()
+        buf = ctypes.create_string_buffer(bytes(b), len(b))
+        nf, na = ctypes.c_int(0), ctypes.c_int(0)
+        rc = self._lib.mds_xtc_index(buf, len(b), None, 0, ctypes.byref(nf), ctypes.byref(na))
+        if rc != L.MDS_OK:
+            raise L.MdsError(rc, "not an xtc trajectory (bad magic number or changing atom count)")
+        off = np.zeros(nf.value + 1, np.int64)
+        self._lib.mds_xtc_index(buf, len(b), _ptr(off), nf.value + 1, ctypes.byref(nf), ctypes.byref(na))
+        steps = np.zeros(nf.value, np.int32)
+        times = np.zeros(nf.value, np.float32)
+        if device_out:
+            import torch
+
+            xyz = torch.empty((nf.value, na.value, 3), dtype=torch.float32, device=f"cuda:{self.device}")
+            flags = L.MDS_DEVICE_IO
+        else:
+            xyz = np.zeros((nf.value, na.value, 3), np.float32)
+            flags = 0
+        L.check(self.h, self._lib.mds_xtc_decode(self.h, buf, len(b), _ptr(off), nf.value, na.value, flags,
+                                                 _ptr(xyz), _ptr(steps), _ptr(times), None))
+        return xyz, steps, times
+
     def stats(self) -> dict:
         s = L.KnnStats()
         L.check(self.h, self._lib.mds_get_knn_stats(self.h, ctypes.byref(s)))
@@ -229,3 +255,34 @@ class Context:
             float(sigma), int(nev), int(ncv), float(tol), int(maxiter), 0, _ptr(ev), _ptr(V), _ptr(E), _ptr(res),
             ctypes.byref(nc)))
         return ev, V, E, res, nc.value
+
+    def auto_decomp_sparse(self, n, pcol, irow, dist, k_sigma, nev, perplexity=None, ncv=0, tol=0.0, maxiter=0):
+        """auto_decomp_sparse: (evals, evecs [nev, n], residuals, nconv, sigmas [n])."""
+        a = [np.ascontiguousarray(v, t) for v, t in ((pcol, np.int32), (irow, np.int32), (dist, np.float64))]
+        ev = np.zeros(nev)
+        V = np.zeros((nev, n))
+        res = np.zeros(nev)
+        sig = np.zeros(n)
+        nc = ctypes.c_int(0)
+        L.check(self.h, self._lib.mds_auto_decomp_sparse(
+            self.h, int(n), _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), int(k_sigma), float(perplexity or 0.0), int(nev),
+            int(ncv), float(tol), int(maxiter), 0, _ptr(ev), _ptr(V), _ptr(res), ctypes.byref(nc), _ptr(sig)))
+        return ev, V, res, nc.value, sig
+
+    def auto_decomp_sparse_nystrom(self, n, pcol, irow, dist, m, pcolB, irowB, distB, k_sigma, nev, perplexity=None,
+                                   ncv=0, tol=0.0, maxiter=0):
+        """auto_decomp_sparse_nystrom: (evals, evecs [nev, n], ext [nev, m], residuals, nconv, sigmas [n])."""
+        a = [np.ascontiguousarray(v, t) for v, t in ((pcol, np.int32), (irow, np.int32), (dist, np.float64),
+                                                      (pcolB, np.int32), (irowB, np.int32), (distB, np.float64))]
+        ev = np.zeros(nev)
+        V = np.zeros((nev, n))
+        E = np.zeros((nev, m))
+        res = np.zeros(nev)
+        sig = np.zeros(n)
+        nc = ctypes.c_int(0)
+        L.check(self.h, self._lib.mds_auto_decomp_sparse_nystrom(
+            self.h, int(n), _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), int(m), _ptr(a[3]), _ptr(a[4]), _ptr(a[5]),
+            int(k_sigma), float(perplexity or 0.0), int(nev), int(ncv), float(tol), int(maxiter), 0, _ptr(ev),
+            _ptr(V), _ptr(E),
+            _ptr(res), ctypes.byref(nc), _ptr(sig)))
+        return ev, V, E, res, nc.value, sig

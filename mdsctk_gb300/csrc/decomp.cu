@@ -112,10 +112,13 @@ __global__ void k_rowptr(const unsigned long long* __restrict__ keys, int64_t m,
 
 // affinity weight of every half-entry, degree of every row (column order:
 // deterministic), then d^-1/2. One warp per row.
+// den = 2 sigma^2 (decomp_sparse.cpp:159), or with per-landmark sigmas
+// (auto_decomp_sparse.cpp:182) 2 s_c s_r of the stored entry's column c and
+// row r (the smaller and the larger index of a strictly lower-triangle entry).
 __global__ void k_sym_degree(const unsigned long long* __restrict__ keys, const int64_t* __restrict__ vals,
                              const int64_t* __restrict__ rp, const double* __restrict__ dist, int n,
-                             double inv2s2, int* __restrict__ col, double* __restrict__ w,
-                             double* __restrict__ dinv) {
+                             double den, const double* __restrict__ sig, int* __restrict__ col,
+                             double* __restrict__ w, double* __restrict__ dinv) {
   int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (row >= n) return;
   double s = 0.0;
@@ -123,8 +126,11 @@ __global__ void k_sym_degree(const unsigned long long* __restrict__ keys, const 
     int64_t v = vals[e];
     int kind = (int)(v & 3);
     double d = dist[v >> 2];
-    double a = exp(-(d * d) * inv2s2);
-    col[e] = (int)(keys[e] & 0xffffffffu);
+    int c = (int)(keys[e] & 0xffffffffu);
+    double dn = den;
+    if (sig) dn = 2.0 * sig[min(row, c)] * sig[max(row, c)];
+    double a = exp(-(d * d) / dn);
+    col[e] = c;
     w[e] = a * (kind == 2 ? 2.0 : 1.0);  // the weight sp_dsymv gives it
     s += (kind == 0) ? a : 2.0 * a;      // the reference's degree sum
   }
@@ -138,6 +144,146 @@ __global__ void k_sym_normalise(const int64_t* __restrict__ rp, const int* __res
   if (row >= n) return;
   double dr = dinv[row];
   for (int64_t e = rp[row] + lane; e < rp[row + 1]; e += 32) w[e] *= dr * dinv[col[e]];
+}
+
+// ---------------------------------------------------------------------------
+// 1b. per-landmark sigmas (auto_decomp_sparse.cpp:153-178, mdsctk.cpp:388-565)
+// ---------------------------------------------------------------------------
+// The landmark's list is its stored distances in neighbour-index order (the
+// sorted symmetric rows give exactly that order; a diagonal entry counts
+// twice), cut to the first ka entries, then sorted ascending:
+// sigma = (sum in ascending order) / ka. One warp per landmark; the list is
+// sorted in shared memory (P2 = next power of two >= ka doubles per warp).
+// `lists` (n x ka, +inf past the list's end) keeps the sorted lists for the
+// entropic step; *short_list is set if a list has fewer than ka entries.
+__global__ void k_auto_sigma_mean(const int64_t* __restrict__ vals, const int64_t* __restrict__ rp,
+                                  const double* __restrict__ dist, int n, int ka, int P2, double* __restrict__ sig,
+                                  double* __restrict__ lists, int* __restrict__ short_list) {
+  extern __shared__ double sl[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (row >= n) return;
+  double* L = sl + (size_t)warp * P2;
+  int base = 0;
+  for (int64_t e0 = rp[row]; e0 < rp[row + 1] && base < ka; e0 += 32) {
+    int64_t e = e0 + lane;
+    int mult = 0;
+    double dv = 0.0;
+    if (e < rp[row + 1]) {
+      int64_t v = vals[e];
+      mult = ((v & 3) == 0) ? 1 : 2;
+      dv = dist[v >> 2];
+    }
+    int inc = mult;
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    int pos = base + inc - mult;
+    for (int r = 0; r < mult; ++r)
+      if (pos + r < ka) L[pos + r] = dv;
+    base += __shfl_sync(0xffffffffu, inc, 31);
+  }
+  const int cnt = min(base, ka);
+  for (int t = cnt + lane; t < P2; t += 32) L[t] = __longlong_as_double(0x7ff0000000000000ll);
+  __syncwarp();
+  for (int size = 2; size <= P2; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = lane; t < P2 / 2; t += 32) {
+        int i = 2 * t - (t & (stride - 1)), j = i + stride;
+        double a = L[i], b = L[j];
+        if ((a > b) == ((i & size) == 0)) {
+          L[i] = b;
+          L[j] = a;
+        }
+      }
+      __syncwarp();
+    }
+  if (lane == 0) {
+    double acc = 0.0;
+    for (int t = 0; t < cnt; ++t) acc += L[t];
+    sig[row] = acc / (double)ka;
+    if (cnt < ka) atomicExch(short_list, 1);
+  }
+  if (lists)
+    for (int t = lane; t < ka; t += 32) lists[(int64_t)row * ka + t] = L[t];
+}
+
+// Entropic sigma of one landmark: the log-precision b at which the entropy of
+// p_x ~ exp(-d_x^2 e^b) over the ka sorted distances equals log K, by Newton
+// steps kept inside a shrinking bracket [lo, hi] and bisection whenever the
+// value or the slope is unusable (mdsctk.cpp:388-486); sigma = 1/sqrt(2 e^b).
+// The bracket comes from mdsctk.cpp:517-530. The reference solves landmarks
+// one after another, each started from its predecessor's b; here each starts
+// at its own bracket's midpoint and all run in parallel, so sigmas agree to
+// the root-finding tolerance (|entropy - log K| < 1e-10), not bit for bit.
+// At most `cap` iterations (*capped set if reached).
+__global__ void k_auto_sigma_entropic(const double* __restrict__ lists, int n, int ka, double K, double p1, int cap,
+                                      double* __restrict__ sig, int* __restrict__ capped) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  const double* d = lists + (int64_t)x * ka;
+  const double N = (double)ka, logK = log(K), logN = log(N), logNK = logN - logK;
+  const double realmin = 2.225074e-308, tol = 1e-10, sq_eps = 1.4901161193847656e-08;  // 2^-26
+  const double a0 = d[0] * d[0], a1 = d[1] * d[1], ak = d[ka - 1] * d[ka - 1];
+  double hi = log((2.0 * log(p1 * (N - 1.0) / (1.0 - p1))) / (a1 - a0));
+  double l1 = log((2.0 * logNK / (1.0 - (1.0 / N))) / (ak - a0));
+  double l2 = log((2.0 * sqrt(logNK)) / sqrt((ak * ak) - (a0 * a0)));
+  double lo = (l1 > l2) ? l1 : l2;
+  double b = (lo + hi) / 2.0;
+  int it = 1, total = 0;
+  for (;;) {
+    if (++total > cap) {
+      atomicExch(capped, 1);
+      break;
+    }
+    const double eb = exp(b);
+    bool trouble = false;
+    double z = 0.0, e, mean = 0.0, m2 = 0.0;
+    for (int t = 0; t < ka; ++t) z += exp(-(d[t] * d[t]) * eb);
+    if (z < realmin) {
+      e = -logK;
+      trouble = true;
+    } else {
+      for (int t = 0; t < ka; ++t) {
+        double q = exp(-(d[t] * d[t]) * eb) * ((d[t] * d[t]) / z);
+        mean += q;
+        m2 += q * (d[t] * d[t]);
+      }
+      e = eb * mean + log(z) - logK;
+    }
+    if (fabs(e) < tol) break;
+    if (hi - lo < 10.0 * sq_eps) break;
+    if (e < 0.0 && b <= hi) hi = b;
+    else if (e > 0.0 && b >= lo) lo = b;
+    trouble = trouble || e < -logK || e > logN - logK;
+    double g = 0.0;
+    if (!trouble) {
+      if (it == 20) {
+        b = (lo + hi) / 2.0;
+        it = 1;
+        continue;
+      }
+      g = (eb * eb) * ((mean * mean) - m2);
+      if (g == 0) trouble = true;
+    }
+    if (trouble) {
+      double t2 = 0.0;
+      const double elo = exp(lo), ehi = exp(hi);
+      for (int t = 0; t < ka; ++t) t2 += exp(-(d[t] * d[t]) * elo) + exp(-(d[t] * d[t]) * ehi);
+      if (t2 < 2.0 * sqrt(realmin)) break;
+      b = (lo + hi) / 2.0;
+      it = 1;
+      continue;
+    }
+    b += -e / g;
+    if (b < lo || b > hi) {
+      b = (lo + hi) / 2.0;
+      it = 0;
+    }
+    ++it;
+  }
+  sig[x] = 1.0 / sqrt(2.0 * exp(b));
 }
 
 // ---------------------------------------------------------------------------
@@ -155,7 +301,7 @@ __global__ void k_spmv(const int64_t* __restrict__ rp, const int* __restrict__ c
 
 // h[j] = sum_i V[i + j*ld] * w[i], j < ncols; partial sums per block then a
 // second kernel reduces them (deterministic order).
-#define GV_ROWS 2048
+#define GV_ROWS 256
 __global__ void k_gemv_t_part(const double* __restrict__ V, int64_t ld, int n, int ncols,
                               const double* __restrict__ w, double* __restrict__ part) {
   extern __shared__ double sh[];  // [blockDim/32][ncols]
@@ -169,12 +315,15 @@ __global__ void k_gemv_t_part(const double* __restrict__ V, int64_t ld, int n, i
   }
   (void)sh;
 }
+// h[j] = sum over blocks of part[b][j]: one warp per column (lanes take
+// blocks b = lane, lane + 32, ...; fixed shuffle tree, deterministic)
 __global__ void k_reduce_part(const double* __restrict__ part, int nparts, int ncols, double* __restrict__ h) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (j >= ncols) return;
   double s = 0.0;
-  for (int b = 0; b < nparts; ++b) s += part[(int64_t)b * ncols + j];
-  h[j] = s;
+  for (int b = lane; b < nparts; b += 32) s += part[(int64_t)b * ncols + j];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) h[j] = s;
 }
 // w -= V[:, 0:ncols] h
 __global__ void k_gemv_sub(const double* __restrict__ V, int64_t ld, int n, int ncols,
@@ -187,6 +336,25 @@ __global__ void k_gemv_sub(const double* __restrict__ V, int64_t ld, int n, int 
   double s = 0.0;
   for (int j = 0; j < ncols; ++j) s += V[i + j * ld] * hs[j];
   w[i] -= s;
+}
+// alpha_j = both projections onto v_j; beta_j = ||w||; breakdown when beta_j
+// <= tol * max(|alpha_j|, 1)
+__global__ void k_lz_finish(const double* __restrict__ h1, const double* __restrict__ h2,
+                            const double* __restrict__ nrm, int idx, int j, double tol, double* __restrict__ alpha,
+                            double* __restrict__ beta, int* __restrict__ brk) {
+  if (threadIdx.x != 0) return;
+  double a = h1[idx] + h2[idx];
+  double b = sqrt(fmax(nrm[0], 0.0));
+  alpha[j] = a;
+  beta[j] = b;
+  brk[j] = (b <= tol * fmax(fabs(a), 1.0)) ? 1 : 0;
+}
+// v_{j+1} = w / beta_j (zeros after a breakdown; those steps are redone)
+__global__ void k_lz_scale(const double* __restrict__ w, const double* __restrict__ beta, const int* __restrict__ brk,
+                           int j, int n, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = brk[j] ? 0.0 : w[i] * (1.0 / beta[j]);
 }
 __global__ void k_scale_copy(const double* __restrict__ w, double a, int n, double* __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -346,14 +514,70 @@ bool sym_eig(const std::vector<double>& T, int m, std::vector<double>& w, std::v
 // ---------------------------------------------------------------------------
 // device-resident symmetric operator
 // ---------------------------------------------------------------------------
+// Largest k-sigma the per-landmark sigma kernel takes (its sorted list lives
+// in 32 KB of shared memory).
+#define MDS_MAX_KSIGMA 4096
+
+// Per-landmark sigmas into `sig` (n doubles), from the sorted symmetric rows.
+static int auto_sigmas(mds_ctx* ctx, int n, const int64_t* vals, const int64_t* rp, const double* ddist, int ka,
+                       double K, DevBuf& sig) {
+  cudaStream_t s = ctx->stream;
+  if (ka < 1 || ka > MDS_MAX_KSIGMA) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k-sigma %d outside [1, %d]", ka,
+                                                     MDS_MAX_KSIGMA);
+  const bool entropic = K > 0.0;
+  if (entropic && (ka < 2 || (int)std::ceil(K) > ka))
+    return mds_fail(ctx, MDS_ERR_ARG, "perplexity %g needs 2 <= ceil(K) <= k-sigma (%d)", K, ka);
+  int P2 = 1;
+  while (P2 < ka) P2 <<= 1;
+  const int wpb = std::max(1, std::min(8, 1024 / P2));  // warps per block, <= 32 KB of lists
+  DevBuf lists(ctx), flags(ctx);
+  MDS_TRY(sig.alloc(ctx, sizeof(double) * std::max(n, 1)));
+  MDS_TRY(flags.alloc(ctx, 2 * sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(flags.p, 0, 2 * sizeof(int), s));
+  if (entropic) MDS_TRY(lists.alloc(ctx, sizeof(double) * (size_t)n * ka));
+  ctx->stats.launches++;
+  k_auto_sigma_mean<<<(n + wpb - 1) / wpb, 32 * wpb, sizeof(double) * P2 * wpb, s>>>(
+      vals, rp, ddist, n, ka, P2, sig.as<double>(), entropic ? lists.as<double>() : nullptr, flags.as<int>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  int hf[2] = {0, 0};
+  if (entropic) {
+    MDS_CUDA(ctx, cudaMemcpyAsync(hf, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    if (hf[0])
+      return mds_fail(ctx, MDS_ERR_ARG, "a landmark has fewer than k-sigma=%d stored distances (the entropic "
+                      "sigmas read past its list)", ka);
+    // p1 (mdsctk.cpp:505-514): scalar, on the host
+    const double N = (double)ka, logK = std::log(K);
+    double p1;
+    if (logK > std::log(std::sqrt(2.0 * N))) {
+      p1 = 3.0 / 4.0;
+    } else {
+      p1 = 1.0 / 4.0;
+      for (int it = 0; it < 100; ++it) p1 -= (-p1 * std::log(p1 / N) - logK) / (-std::log(p1 / N) + 1.0);
+      p1 = 1.0 - (p1 / 2.0);
+    }
+    ctx->stats.launches++;
+    k_auto_sigma_entropic<<<(n + 127) / 128, 128, 0, s>>>(lists.as<double>(), n, ka, K, p1, 10000,
+                                                          sig.as<double>(), flags.as<int>() + 1);
+    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_CUDA(ctx, cudaMemcpyAsync(hf + 1, flags.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    if (hf[1]) return mds_fail(ctx, MDS_ERR_INTERNAL, "entropic sigma did not settle within 10000 iterations");
+  }
+  return MDS_OK;
+}
+
 struct SymOp {
   int n = 0;
   int64_t nnz = 0;
   DevBuf rp, col, w, dinv;
+  DevBuf sig;  // per-landmark sigmas (auto mode only)
 };
 
+// ka > 0 selects per-landmark sigmas (mean of the ka-entry lists; entropic
+// with perplexity K when K > 0) in place of the single sigma.
 static int build_symop(mds_ctx* ctx, int n, const int* dpcol, const int* dirow, const double* ddist, double sigma,
-                       SymOp& op) {
+                       SymOp& op, int ka = 0, double K = 0.0) {
   cudaStream_t s = ctx->stream;
   op.n = n;
   DevBuf cnt(ctx), pos(ctx), bad(ctx), k0(ctx), v0(ctx), k1(ctx), v1(ctx);
@@ -394,10 +618,13 @@ static int build_symop(mds_ctx* ctx, int n, const int* dpcol, const int* dirow, 
   MDS_TRY(op.w.alloc(ctx, sizeof(double) * std::max<int64_t>(m, 1)));
   MDS_TRY(op.dinv.alloc(ctx, sizeof(double) * std::max(n, 1)));
   const int wb = (int)(((int64_t)n * 32 + 255) / 256);
-  ctx->stats.launches += 3;
+  ctx->stats.launches++;
   k_rowptr<<<(n + 1 + 255) / 256, 256, 0, s>>>(keys, m, n, op.rp.as<int64_t>());
-  k_sym_degree<<<wb, 256, 0, s>>>(keys, vals, op.rp.as<int64_t>(), ddist, n, 1.0 / (2.0 * sigma * sigma),
-                                  op.col.as<int>(), op.w.as<double>(), op.dinv.as<double>());
+  if (ka > 0) MDS_TRY(auto_sigmas(ctx, n, vals, op.rp.as<int64_t>(), ddist, ka, K, op.sig));
+  ctx->stats.launches += 2;
+  k_sym_degree<<<wb, 256, 0, s>>>(keys, vals, op.rp.as<int64_t>(), ddist, n, 2.0 * sigma * sigma,
+                                  ka > 0 ? op.sig.as<double>() : nullptr, op.col.as<int>(), op.w.as<double>(),
+                                  op.dinv.as<double>());
   k_sym_normalise<<<wb, 256, 0, s>>>(op.rp.as<int64_t>(), op.col.as<int>(), op.dinv.as<double>(), n,
                                      op.w.as<double>());
   MDS_CUDA(ctx, cudaGetLastError());
@@ -420,30 +647,43 @@ struct LanczosOut {
   int matvecs = 0;
 };
 
+// With nlock > 0 the sequence runs on the operator deflated by the nlock
+// orthonormal columns dLock [nlock][n]: every new basis vector is
+// orthogonalised against them as well as against the Lanczos basis.
 static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, int maxiter, double* dX /*n*nev*/,
-                   LanczosOut& out) {
+                   LanczosOut& out, const double* dLock = nullptr, int nlock = 0,
+                   uint64_t seed = 0x9E3779B97F4A7C15ull) {
   cudaStream_t s = ctx->stream;
   const int n = op.n;
   const int m = ncv;
   const int64_t ld = n;
   DevBuf V(ctx), wv(ctx), h(ctx), part(ctx), Yd(ctx), tmp(ctx);
-  MDS_TRY(V.alloc(ctx, sizeof(double) * (size_t)n * (m + 1)));
+  MDS_TRY(V.alloc(ctx, sizeof(double) * (size_t)n * (nlock + m + 1)));
   MDS_TRY(wv.alloc(ctx, sizeof(double) * n));
-  MDS_TRY(h.alloc(ctx, sizeof(double) * (m + 1)));
+  MDS_TRY(h.alloc(ctx, sizeof(double) * (nlock + m + 1)));
   const int nparts = (n + GV_ROWS - 1) / GV_ROWS;
-  MDS_TRY(part.alloc(ctx, sizeof(double) * (size_t)nparts * (m + 1)));
+  MDS_TRY(part.alloc(ctx, sizeof(double) * (size_t)nparts * (nlock + m + 1)));
   MDS_TRY(Yd.alloc(ctx, sizeof(double) * (size_t)m * m));
   MDS_TRY(tmp.alloc(ctx, sizeof(double) * (size_t)n * m));
-  double* Vp = V.as<double>();
+  DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx);
+  MDS_TRY(h1.alloc(ctx, sizeof(double) * (nlock + m + 1)));
+  MDS_TRY(h2.alloc(ctx, sizeof(double) * (nlock + m + 1)));
+  MDS_TRY(ab.alloc(ctx, sizeof(double) * 2 * m));
+  MDS_TRY(brk.alloc(ctx, sizeof(int) * m));
+  double* Vl = V.as<double>();           // locked columns, then the Lanczos basis
+  double* Vp = Vl + (int64_t)nlock * ld;  // Lanczos basis v_0..v_m
+  if (nlock)
+    MDS_CUDA(ctx, cudaMemcpyAsync(Vl, dLock, sizeof(double) * (size_t)n * nlock, cudaMemcpyDeviceToDevice, s));
   double* w = wv.as<double>();
   const double eps = std::numeric_limits<double>::epsilon();
   const double eps23 = std::pow(eps, 2.0 / 3.0);
   if (tol <= 0.0) tol = eps;
 
+  // dots/subtract act on the first ncols columns of [locked | basis]
   auto dots = [&](int ncols, std::vector<double>& hh) -> int {
     ctx->stats.launches += 2;
-    k_gemv_t_part<<<nparts, 256, 0, s>>>(Vp, ld, n, ncols, w, part.as<double>());
-    k_reduce_part<<<(ncols + 127) / 128, 128, 0, s>>>(part.as<double>(), nparts, ncols, h.as<double>());
+    k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, ncols, w, part.as<double>());
+    k_reduce_part<<<(ncols + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, ncols, h.as<double>());
     MDS_CUDA(ctx, cudaGetLastError());
     hh.resize(ncols);
     MDS_CUDA(ctx, cudaMemcpyAsync(hh.data(), h.p, sizeof(double) * ncols, cudaMemcpyDeviceToHost, s));
@@ -453,10 +693,11 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   auto subtract = [&](int ncols, const std::vector<double>& hh) -> int {
     MDS_CUDA(ctx, cudaMemcpyAsync(h.p, hh.data(), sizeof(double) * ncols, cudaMemcpyHostToDevice, s));
     ctx->stats.launches++;
-    k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * ncols, s>>>(Vp, ld, n, ncols, h.as<double>(), w);
+    k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * ncols, s>>>(Vl, ld, n, ncols, h.as<double>(), w);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
+  std::vector<double> hh0;
   auto norm_w = [&](double* nr) -> int {
     // ||w|| through the same partial-sum kernels (V column = w itself)
     ctx->stats.launches += 2;
@@ -471,12 +712,16 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   // start vector: fixed-seed pseudo-random, orthogonalised and normalised
   {
     std::vector<double> v0(n);
-    uint64_t st = 0x9E3779B97F4A7C15ull;
+    uint64_t st = seed;
     for (int i = 0; i < n; ++i) {
       st ^= st << 13; st ^= st >> 7; st ^= st << 17;
       v0[i] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
     }
     MDS_CUDA(ctx, cudaMemcpyAsync(w, v0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    for (int rep = 0; rep < 2 && nlock; ++rep) {
+      MDS_TRY(dots(nlock, hh0));
+      MDS_TRY(subtract(nlock, hh0));
+    }
     double nr = 0;
     MDS_TRY(norm_w(&nr));
     ctx->stats.launches++;
@@ -488,42 +733,64 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   std::vector<double> hh, hh2, T, Z, th;
   int restart = 0;
   for (;; ++restart) {
-    for (int j = k; j < m; ++j) {
-      spmv(ctx, op, Vp + (int64_t)j * ld, w);
-      out.matvecs++;
-      // full reorthogonalisation against v_0..v_j (twice); alpha_j = v_j . Av_j
-      MDS_TRY(dots(j + 1, hh));
-      alpha[j] = hh[j];
-      MDS_TRY(subtract(j + 1, hh));
-      MDS_TRY(dots(j + 1, hh2));
-      MDS_TRY(subtract(j + 1, hh2));
-      alpha[j] += hh2[j];
-      double b = 0;
-      MDS_TRY(norm_w(&b));
-      beta[j] = b;
-      double scale = std::max(std::fabs(alpha[j]), 1.0);
-      if (b <= eps * scale * 10.0) {
-        // invariant subspace: continue with a fresh direction orthogonal to V
-        std::vector<double> v0(n);
-        uint64_t st = 0xD1B54A32D192ED03ull + 7919ull * (uint64_t)(j + 1 + restart * m);
-        for (int i = 0; i < n; ++i) {
-          st ^= st << 13; st ^= st >> 7; st ^= st << 17;
-          v0[i] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
-        }
-        MDS_CUDA(ctx, cudaMemcpyAsync(w, v0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-        for (int rep = 0; rep < 2; ++rep) {
-          MDS_TRY(dots(j + 1, hh));
-          MDS_TRY(subtract(j + 1, hh));
-        }
-        double nr = 0;
-        MDS_TRY(norm_w(&nr));
-        beta[j] = 0.0;
-        ctx->stats.launches++;
-        k_scale_copy<<<(n + 255) / 256, 256, 0, s>>>(w, 1.0 / nr, n, Vp + (int64_t)(j + 1) * ld);
-      } else {
-        ctx->stats.launches++;
-        k_scale_copy<<<(n + 255) / 256, 256, 0, s>>>(w, 1.0 / b, n, Vp + (int64_t)(j + 1) * ld);
+    // Lanczos steps k..m-1 run with no host round trip: the projections,
+    // alpha_j, beta_j and the next basis vector are computed on the device;
+    // alpha/beta/breakdown flags are read once afterwards. A breakdown
+    // (invariant subspace, beta_j ~ 0) found then restarts the steps after
+    // it from a fresh direction orthogonal to the basis.
+    for (int j0 = k; j0 < m;) {
+      for (int j = j0; j < m; ++j) {
+        spmv(ctx, op, Vp + (int64_t)j * ld, w);
+        out.matvecs++;
+        const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
+        ctx->stats.launches += 10;
+        k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
+        k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h1.as<double>());
+        k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h1.as<double>(), w);
+        k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
+        k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h2.as<double>());
+        k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h2.as<double>(), w);
+        k_gemv_t_part<<<nparts, 256, 0, s>>>(w, ld, n, 1, w, part.as<double>());
+        k_reduce_part<<<1, 128, 0, s>>>(part.as<double>(), nparts, 1, h.as<double>());
+        k_lz_finish<<<1, 32, 0, s>>>(h1.as<double>(), h2.as<double>(), h.as<double>(), nlock + j, j, eps * 10.0,
+                                     ab.as<double>(), ab.as<double>() + m, brk.as<int>());
+        k_lz_scale<<<(n + 255) / 256, 256, 0, s>>>(w, ab.as<double>() + m, brk.as<int>(), j, n,
+                                                   Vp + (int64_t)(j + 1) * ld);
       }
+      MDS_CUDA(ctx, cudaGetLastError());
+      std::vector<double> hab(2 * m);
+      std::vector<int> hbrk(m);
+      MDS_CUDA(ctx, cudaMemcpyAsync(hab.data(), ab.p, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, s));
+      MDS_CUDA(ctx, cudaMemcpyAsync(hbrk.data(), brk.p, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+      MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      int jb = -1;
+      for (int j = j0; j < m; ++j) {
+        alpha[j] = hab[j];
+        beta[j] = hab[m + j];
+        if (hbrk[j]) {
+          jb = j;
+          break;
+        }
+      }
+      if (jb < 0) break;
+      // invariant subspace at step jb: continue with a fresh direction orthogonal to V
+      std::vector<double> v0(n);
+      uint64_t st = 0xD1B54A32D192ED03ull + (seed - 0x9E3779B97F4A7C15ull) + 7919ull * (uint64_t)(jb + 1 + restart * m);
+      for (int i = 0; i < n; ++i) {
+        st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+        v0[i] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+      }
+      MDS_CUDA(ctx, cudaMemcpyAsync(w, v0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      for (int rep = 0; rep < 2; ++rep) {
+        MDS_TRY(dots(nlock + jb + 1, hh));
+        MDS_TRY(subtract(nlock + jb + 1, hh));
+      }
+      double nr = 0;
+      MDS_TRY(norm_w(&nr));
+      beta[jb] = 0.0;
+      ctx->stats.launches++;
+      k_scale_copy<<<(n + 255) / 256, 256, 0, s>>>(w, 1.0 / nr, n, Vp + (int64_t)(jb + 1) * ld);
+      j0 = jb + 1;
     }
     // projected matrix: arrowhead (kept Ritz pairs) + tridiagonal
     T.assign((size_t)m * m, 0.0);
@@ -583,6 +850,49 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   }
 }
 
+// Lanczos from one start vector sees one direction of each eigenspace, so a
+// wanted eigenvalue of multiplicity > 1 (e.g. 1.0 once per connected
+// component of the kNN graph) can be missed. After convergence, run a short
+// sequence (three restarts of 20 vectors) on the operator deflated by the nev
+// converged vectors: its top Ritz value is a lower bound of the deflated
+// spectrum's top, so a value more than 1e-10 (relative) above the nev-th
+// eigenvalue proves a missed eigenpair; it is then converged to the requested
+// tolerance, inserted in order (dropping the smallest) and the check repeats.
+// Eigenvalues within 1e-10 of the nev-th are interchangeable with it.
+static int lanczos_complete(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, int maxiter, double* dX,
+                            LanczosOut& out) {
+  MDS_TRY(lanczos(ctx, op, nev, ncv, tol, maxiter, dX, out));
+  const int n = op.n;
+  const int ncv2 = std::min(20, n - nev);
+  if (ncv2 < 3) return MDS_OK;
+  cudaStream_t s = ctx->stream;
+  DevBuf y(ctx);
+  MDS_TRY(y.alloc(ctx, sizeof(double) * n));
+  const double eps = std::numeric_limits<double>::epsilon();
+  (void)eps;
+  for (int pass = 0; pass < nev; ++pass) {
+    const uint64_t seed = 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull * (uint64_t)(pass + 1);
+    LanczosOut o2;
+    MDS_TRY(lanczos(ctx, op, 1, ncv2, 1e-6, 3, y.as<double>(), o2, dX, nev, seed));
+    out.matvecs += o2.matvecs;
+    const double th = o2.evals[0], lo = out.evals[nev - 1];
+    if (!(th > lo + 1e-10 * std::max(1.0, std::fabs(lo)))) break;
+    o2 = LanczosOut();  // converge the missed pair to the requested tolerance
+    MDS_TRY(lanczos(ctx, op, 1, ncv2, tol, maxiter, y.as<double>(), o2, dX, nev, seed));
+    out.matvecs += o2.matvecs;
+    int p = nev - 1;
+    while (p > 0 && out.evals[p - 1] < o2.evals[0]) --p;
+    for (int c = nev - 1; c > p; --c) {
+      out.evals[c] = out.evals[c - 1];
+      MDS_CUDA(ctx, cudaMemcpyAsync(dX + (int64_t)c * n, dX + (int64_t)(c - 1) * n, sizeof(double) * n,
+                                    cudaMemcpyDeviceToDevice, s));
+    }
+    out.evals[p] = o2.evals[0];
+    MDS_CUDA(ctx, cudaMemcpyAsync(dX + (int64_t)p * n, y.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  return MDS_OK;
+}
+
 // residual ||A z - lambda z|| / |lambda| for each vector
 __global__ void k_resid_part(const double* __restrict__ Az, const double* __restrict__ z, double lam, int n,
                              double* __restrict__ part) {
@@ -606,15 +916,22 @@ __global__ void k_resid_part(const double* __restrict__ Az, const double* __rest
 // ---------------------------------------------------------------------------
 // B affinity: w = exp(-d^2/2s^2); d_b[q] = (sum of column q)^-1/2;
 // B[l,q] = w * d_a[l] * d_b[q]   (one warp per column q)
+// den = 2 sigma^2, or with per-landmark sigmas 2 s_l s_l of the entry's
+// landmark l (auto_decomp_sparse_nystrom.cpp:171-173).
 __global__ void k_nystrom_b(const int* __restrict__ pcol, const int* __restrict__ irow, const double* __restrict__ dist,
-                            int m, int n, double inv2s2, const double* __restrict__ dinv_a, double* __restrict__ B,
-                            int* __restrict__ bad) {
+                            int m, int n, double den, const double* __restrict__ sig,
+                            const double* __restrict__ dinv_a, double* __restrict__ B, int* __restrict__ bad) {
   int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (q >= m) return;
   double s = 0.0;
   for (int p = pcol[q] + lane; p < pcol[q + 1]; p += 32) {
     double d = dist[p];
-    double a = exp(-(d * d) * inv2s2);
+    double dn = den;
+    if (sig) {
+      int l = irow[p];
+      dn = (l >= 0 && l < n) ? 2.0 * sig[l] * sig[l] : 1.0;
+    }
+    double a = exp(-(d * d) / dn);
     B[p] = a;
     s += a;
   }
@@ -646,14 +963,19 @@ __global__ void k_nystrom_ext(const int* __restrict__ pcol, const int* __restric
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+// k_sigma > 0: per-landmark sigmas (auto_decomp_sparse), entropic when
+// perplexity > 0; `sigma` is then unused and sig_out (n, may be null) gets
+// the sigmas.
 static int decomp_impl(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow, const double* dist, double sigma,
                        int nev, int ncv, double tol, int maxiter, unsigned flags, double* evals, double* evecs,
                        double* resid, int* nconv, int m, const int32_t* pcolB, const int32_t* irowB,
-                       const double* distB, double* ext) {
+                       const double* distB, double* ext, int k_sigma = 0, double perplexity = 0.0,
+                       double* sig_out = nullptr) {
   if (!ctx) return MDS_ERR_ARG;
   ctx->stats = mds_knn_stats{};
   if (!pcol || !irow || !dist || !evals || !evecs) return mds_fail(ctx, MDS_ERR_ARG, "null argument");
   if (n < 1 || nev < 1) return mds_fail(ctx, MDS_ERR_ARG, "invalid sizes n=%d nev=%d", n, nev);
+  if (k_sigma > 0) sigma = 1.0;
   if (!(sigma > 0.0)) return mds_fail(ctx, MDS_ERR_ARG, "sigma must be positive");
   // decomp_sparse.cpp:199-205: ncv = min(10 nev + 1, n), maxiter = 100 nev
   if (ncv <= 0) ncv = std::min(10 * nev + 1, n);
@@ -695,7 +1017,10 @@ static int decomp_impl(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* 
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   SymOp op;
-  MDS_TRY(build_symop(ctx, n, ppcol, pirow, pdist, sigma, op));
+  MDS_TRY(build_symop(ctx, n, ppcol, pirow, pdist, sigma, op, k_sigma, perplexity));
+  if (k_sigma > 0 && sig_out)
+    MDS_CUDA(ctx, cudaMemcpyAsync(sig_out, op.sig.p, sizeof(double) * n,
+                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
   double* pX = evecs;
   if (!dev) {
@@ -703,7 +1028,7 @@ static int decomp_impl(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* 
     pX = dX.as<double>();
   }
   LanczosOut lo;
-  MDS_TRY(lanczos(ctx, op, nev, ncv, tol, maxiter, pX, lo));
+  MDS_TRY(lanczos_complete(ctx, op, nev, ncv, tol, maxiter, pX, lo));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
   for (int x = 0; x < nev; ++x) evals[x] = lo.evals[x];
   if (nconv) *nconv = lo.nconv;
@@ -767,7 +1092,8 @@ static int decomp_impl(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* 
     }
     const int wb = (int)(((int64_t)m * 32 + 255) / 256);
     ctx->stats.launches += 2;
-    k_nystrom_b<<<wb, 256, 0, s>>>(qp, qr, qd, m, n, 1.0 / (2.0 * sigma * sigma), op.dinv.as<double>(),
+    k_nystrom_b<<<wb, 256, 0, s>>>(qp, qr, qd, m, n, 2.0 * sigma * sigma,
+                                   k_sigma > 0 ? op.sig.as<double>() : nullptr, op.dinv.as<double>(),
                                    B.as<double>(), bad.as<int>());
     k_nystrom_ext<<<wb, 256, 0, s>>>(qp, qr, B.as<double>(), m, n, pX, il.as<double>(), nev, pext);
     MDS_CUDA(ctx, cudaGetLastError());
@@ -802,7 +1128,7 @@ int decomp_resident(mds_ctx* ctx, int n, const int* dpcol, const int* dirow, con
   SymOp op;
   MDS_TRY(build_symop(ctx, n, dpcol, dirow, ddist, sigma, op));
   LanczosOut lo;
-  MDS_TRY(lanczos(ctx, op, nev, ncv, tol, maxiter, dZ, lo));
+  MDS_TRY(lanczos_complete(ctx, op, nev, ncv, tol, maxiter, dZ, lo));
   MDS_CUDA(ctx, cudaMemcpyAsync(ddinv, op.dinv.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
   MDS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   evals = lo.evals;
@@ -825,4 +1151,26 @@ extern "C" int mds_decomp_sparse_nystrom(mds_ctx* ctx, int n, const int32_t* pco
   if (m < 0) return mds_fail(ctx, MDS_ERR_ARG, "m must be >= 0");
   return decomp_impl(ctx, n, pcol, irow, dist, sigma, nev, ncv, tol, maxiter, flags, evals, evecs, resid, nconv, m,
                      pcolB, irowB, distB, ext);
+}
+
+extern "C" int mds_auto_decomp_sparse(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow,
+                                      const double* dist, int k_sigma, double perplexity, int nev, int ncv, double tol,
+                                      int maxiter, unsigned flags, double* evals, double* evecs, double* resid,
+                                      int* nconv, double* sigmas) {
+  if (!ctx) return MDS_ERR_ARG;
+  if (k_sigma < 1) return mds_fail(ctx, MDS_ERR_ARG, "k-sigma must be >= 1");
+  return decomp_impl(ctx, n, pcol, irow, dist, 1.0, nev, ncv, tol, maxiter, flags, evals, evecs, resid, nconv, 0,
+                     nullptr, nullptr, nullptr, nullptr, k_sigma, perplexity, sigmas);
+}
+
+extern "C" int mds_auto_decomp_sparse_nystrom(mds_ctx* ctx, int n, const int32_t* pcol, const int32_t* irow,
+                                              const double* dist, int m, const int32_t* pcolB, const int32_t* irowB,
+                                              const double* distB, int k_sigma, double perplexity, int nev, int ncv,
+                                              double tol, int maxiter, unsigned flags, double* evals, double* evecs,
+                                              double* ext, double* resid, int* nconv, double* sigmas) {
+  if (!ctx) return MDS_ERR_ARG;
+  if (k_sigma < 1) return mds_fail(ctx, MDS_ERR_ARG, "k-sigma must be >= 1");
+  if (m < 0) return mds_fail(ctx, MDS_ERR_ARG, "m must be >= 0");
+  return decomp_impl(ctx, n, pcol, irow, dist, 1.0, nev, ncv, tol, maxiter, flags, evals, evecs, resid, nconv, m,
+                     pcolB, irowB, distB, ext, k_sigma, perplexity, sigmas);
 }

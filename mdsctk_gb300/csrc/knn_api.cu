@@ -118,8 +118,8 @@ static int knn_rms_impl(mds_ctx* ctx, const float* ref_xyz, int n_ref, const flo
   }
   pl.prep_dev = hooks.prep_dev;
   pl.prep_rec = hooks.prep_rec;
-  pl.guard_fp32 = 1.0f / 65536.0f;
-  pl.guard_tc = 1.0f / 8192.0f;
+  pl.guard_fp32 = MDS_GUARD_FP32;
+  pl.guard_tc = MDS_GUARD_TC;
   ctx->stats.pairs = (long long)n_ref * n_fit;
   ctx->stats.kprime = pl.kprime;
   if (n_fit == 0 || (!full && k == 0)) return MDS_OK;

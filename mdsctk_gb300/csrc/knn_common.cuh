@@ -4,6 +4,17 @@
 
 #include "mds_common.cuh"
 
+// Screen guards: the lower bound of RMSD^2 is the screen value minus
+// c * (|a_i|^2 + |a_j|^2), a = deviation from the template. c covers the
+// rounding of the screen's Gram (FP32 FMA chains, or split BF16/FP16
+// products accumulated in FP32 by the tensor cores). Measured over the
+// 256 nearest candidates of sampled rows (20,000 x 1,000-atom trajectory and
+// 50,000 x 304-atom landmarks against off-trajectory queries), the largest
+// over-estimate per unit of |a_i|^2 + |a_j|^2 was 1.3e-6 (FP32), 6.1e-6
+// (BF16x3) and 9.6e-6 (FP16x3): the guards below are 12x and 6x above them.
+#define MDS_GUARD_FP32 (1.0f / 65536.0f)
+#define MDS_GUARD_TC (1.0f / 16384.0f)
+
 struct KnnRmsPlan {
   int nref = 0, nfit = 0, natoms = 0;
   int Ap = 0;      // natoms rounded up to 64 (zero-padded atoms)

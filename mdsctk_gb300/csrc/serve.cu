@@ -149,8 +149,8 @@ struct mds_server {
     p.kprime = Kp;
     p.nofit = (cfg.flags & MDS_NOFIT) ? 1 : 0;
     p.prec = prec;
-    p.guard_fp32 = 1.0f / 65536.0f;
-    p.guard_tc = 1.0f / 8192.0f;
+    p.guard_fp32 = MDS_GUARD_FP32;
+    p.guard_tc = MDS_GUARD_TC;
     return p;
   }
 };

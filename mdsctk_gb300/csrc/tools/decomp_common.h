@@ -18,8 +18,14 @@ inline double sqrt_eps() {
   return std::sqrt(eps);
 }
 
-inline void add_decomp_options(Parser& p) {
-  p.add("sigma", 'q', DOUBLE, "Input:  Standard deviation of gaussian kernel (real)");
+// auto_decomp_sparse[_nystrom] take -k/-K (per-landmark sigmas) in place of -q.
+inline void add_decomp_options(Parser& p, bool auto_sigma = false) {
+  if (auto_sigma) {
+    p.add("k-sigma", 'k', INT, "Input:  K-nn to average for sigmas (int)");
+    p.add("k-perplexity", 'K', DOUBLE, "Input:  Desired perplexity within knn (real)");
+  } else {
+    p.add("sigma", 'q', DOUBLE, "Input:  Standard deviation of gaussian kernel (real)");
+  }
   p.add("nevals", 'n', INT, "Input:  Number of eigenvalues/vectors (int)");
   p.add("ssm-file", 's', STRING, "Input:  Symmetric sparse matrix file (string:filename)", "distances.ssm");
   p.add("evals-file", 'v', STRING, "Output:  Eigenvalues file (string:filename)", "eigenvalues.dat");
@@ -34,8 +40,11 @@ inline void add_decomp_options(Parser& p) {
 
 // ext may be null (decomp_sparse); otherwise the m extension values follow
 // the n eigenvector values on the same line / in the same record.
+// max_style: auto_decomp_sparse's wording of the residual report
+// (auto_decomp_sparse.cpp:244-248).
 inline int write_decomp(const Parser& p, int n, int nev, const std::vector<double>& ev, const std::vector<double>& V,
-                        const std::vector<double>* ext, int m, const std::vector<double>& res, int nconv) {
+                        const std::vector<double>* ext, int m, const std::vector<double>& res, int nconv,
+                        bool max_style = false) {
   std::cout << "Number of converged eigenvalues/vectors found: " << nconv << std::endl;
   const bool bin = p.b("binary-out");
   std::ofstream fv(p.str("evals-file").c_str(), bin ? std::ios::binary : std::ios::out);
@@ -59,12 +68,34 @@ inline int write_decomp(const Parser& p, int n, int nev, const std::vector<doubl
     maxr = std::max(maxr, res[x]);
   }
   const double eps = sqrt_eps();
-  std::cout << "Max residual: " << maxr << " (eps: " << eps << ")" << std::endl;
+  std::cout << (max_style ? "Maximum residual: " : "Max residual: ") << maxr << " (eps: " << eps << ")"
+            << std::endl;
   if (maxr > eps) {
-    std::cout << "*** Sum of residuals too high (max_r > eps)!" << std::endl;
+    std::cout << (max_style ? "*** Max residual too high (max_r > eps)!" : "*** Sum of residuals too high (max_r > eps)!")
+              << std::endl;
     std::cout << "*** Please, check results manually..." << std::endl;
   }
   return 0;
+}
+
+// average sigma as the reference prints it (sequential sum / n)
+inline void print_average_sigma(const std::vector<double>& sig) {
+  double s = sig.empty() ? 0.0 : sig[0];
+  for (size_t x = 1; x < sig.size(); ++x) s += sig[x];
+  std::cout << "Average sigma: " << (s / (double)sig.size()) << std::endl << std::endl;
+}
+
+inline bool check_auto_args(const Parser& p) {
+  bool ok = true;
+  if (!p.is_set("k-sigma")) {
+    std::cout << "ERROR: --k-sigma not supplied." << std::endl << std::endl;
+    ok = false;
+  }
+  if (!p.is_set("nevals")) {
+    std::cout << "ERROR: --nevals not supplied." << std::endl << std::endl;
+    ok = false;
+  }
+  return ok;
 }
 
 inline bool check_decomp_args(const Parser& p) {

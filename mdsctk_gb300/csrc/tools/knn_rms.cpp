@@ -4,9 +4,10 @@
 // Angstrom; indices.dat: int[n_fit][k]).
 //
 // Inputs: -p topology (.pdb or .gro: atom count and masses by element, the
-// masses GROMACS assigns to the common elements), -r/-f coordinates: raw
-// float32 frames [natoms][3] in nm (the layout flatten_xtc writes). XTC
-// trajectories are recognised and rejected with a message.
+// masses GROMACS assigns to the common elements), -r/-f coordinates: GROMACS
+// .xtc trajectories (decoded on the GPU by mds_xtc_decode; an atom count
+// that differs from the topology's exits with status 4, knn_rms.cpp:157-178)
+// or raw float32 frames [natoms][3] in nm (the layout flatten_xtc writes).
 #include <algorithm>
 #include <cctype>
 #include <sstream>
@@ -65,13 +66,30 @@ static bool read_topology(const std::string& path, std::vector<float>& mass) {
   return true;
 }
 
-static int read_frames(const std::string& path, int natoms, std::vector<float>& x, int& n) {
+// Returns 0, -1 (cannot open), -3 (malformed .xtc), or -4 (the .xtc holds
+// `*xtc_atoms` atoms, not natoms).
+static int read_frames(mds_ctx* ctx, const std::string& path, int natoms, std::vector<float>& x, int& n,
+                       int* xtc_atoms) {
   std::vector<char> b;
   if (!cli::read_file(path, b)) return -1;
-  if (b.size() >= 4) {
-    unsigned char* u = reinterpret_cast<unsigned char*>(b.data());
-    int magic = (u[0] << 24) | (u[1] << 16) | (u[2] << 8) | u[3];
-    if (magic == 1995) return -2;  // XTC
+  const unsigned char* u = reinterpret_cast<const unsigned char*>(b.data());
+  if (b.size() >= 4 && ((u[0] << 24) | (u[1] << 16) | (u[2] << 8) | u[3]) == 1995) {
+    int nfr = 0, na = 0;
+    if (mds_xtc_index(u, b.size(), nullptr, 0, &nfr, &na) != MDS_OK) return -3;
+    if (na != natoms) {
+      *xtc_atoms = na;
+      return -4;
+    }
+    std::vector<int64_t> off(nfr + 1);
+    if (mds_xtc_index(u, b.size(), off.data(), nfr + 1, &nfr, &na) != MDS_OK) return -3;
+    x.resize((size_t)nfr * 3 * natoms);
+    if (nfr && mds_xtc_decode(ctx, u, b.size(), off.data(), nfr, natoms, 0, x.data(), nullptr, nullptr,
+                              nullptr) != MDS_OK) {
+      std::cout << "*** ERROR *** " << mds_last_error(ctx) << std::endl;
+      return -3;
+    }
+    n = nfr;
+    return 0;
   }
   size_t fr = sizeof(float) * 3 * (size_t)natoms;
   n = (int)(b.size() / fr);
@@ -135,20 +153,30 @@ int main(int argc, char** argv) {
   }
   std::cout << "done." << std::endl;
   const int natoms = (int)mass.size();
+  mds_ctx* ctx = nullptr;
+  int rc = mds_create(p.i("device"), 0, &ctx);
+  if (rc) return cli::fail(ctx, rc);
   std::vector<float> xr, xf;
   int nr = 0, nf = 0;
   for (int pass = 0; pass < 2; ++pass) {
     const std::string& fn = pass ? fit : ref;
     if (pass && fit == ref) break;
-    int rr = read_frames(fn, natoms, pass ? xf : xr, pass ? nf : nr);
+    int xa = 0;
+    int rr = read_frames(ctx, fn, natoms, pass ? xf : xr, pass ? nf : nr, &xa);
     if (rr == -1) {
       std::cout << "*** ERROR *** could not open " << fn << std::endl;
       return -1;
     }
-    if (rr == -2) {
-      std::cout << "*** ERROR *** " << fn << " is an XTC trajectory; convert it to raw float frames "
-                << "(flatten_xtc layout) first" << std::endl;
+    if (rr == -3) {
+      std::cout << "*** ERROR *** " << fn << " is not a readable XTC trajectory" << std::endl;
       return -1;
+    }
+    if (rr == -4) {
+      std::cout << "*** ERROR ***" << std::endl
+                << "Number of atoms in topology file (" << natoms << ") "
+                << "does not match the number of atoms in the XTC file (" << fn << " : " << xa << ")."
+                << std::endl;
+      return 4;
     }
   }
   if (fit == ref) nf = nr;
@@ -156,9 +184,6 @@ int main(int argc, char** argv) {
     std::cout << "*** ERROR *** no reference frames" << std::endl;
     return -1;
   }
-  mds_ctx* ctx = nullptr;
-  int rc = mds_create(p.i("device"), 0, &ctx);
-  if (rc) return cli::fail(ctx, rc);
   unsigned flags = prec | (p.b("nofit") ? MDS_NOFIT : 0u) | (sort ? 0u : MDS_FULL);
   int kk = sort ? std::max(0, std::min(k, nr - 1)) : nr;
   std::vector<double> d((size_t)nf * kk);

@@ -500,6 +500,167 @@ void orc_affinity_nystrom(int m, const int* pcolB, const int* irowB, double* val
     for (int y = pcolB[x]; y < pcolB[x + 1]; ++y) valB[y] *= d_a[irowB[y]] * db[x];
 }
 
+// ---------------------------------------------------------------------------
+// auto_decomp_sparse per-landmark sigmas (auto_decomp_sparse.cpp:153-178,
+// auto_decomp_sparse_nystrom.cpp:144-163, mdsctk.cpp:388-565).
+// ---------------------------------------------------------------------------
+// Entropic-affinity root finding for one landmark (mdsctk.cpp:388-486): find
+// the log-precision b with entropy of exp(-d^2 e^b) (normalised) = log K, by
+// Newton steps inside a shrinking bracket [lo, hi], bisecting on trouble;
+// sigma = 1/sqrt(2 e^b). `d` holds the k smallest distances ascending.
+static double entropic_sigma(const double* d, int k, double b0, double logK, double logN, double lo, double hi) {
+  const int maxit = 20;
+  const double tol = 1e-10, realmin = 2.225074e-308;
+  const double sq_eps = std::ldexp(1.0, -26);  // sqrt of the machine epsilon loop's 2^-52
+  double b = (b0 < lo || b0 > hi) ? (lo + hi) / 2.0 : b0;
+  std::vector<double> p(k), q(k);
+  int it = 1;
+  for (;;) {
+    const double eb = std::exp(b);
+    bool trouble = false;
+    double z = 0.0, e, mean = 0.0;
+    for (int x = 0; x < k; ++x) p[x] = std::exp(-(d[x] * d[x]) * eb);
+    for (int x = 0; x < k; ++x) z += p[x];
+    if (z < realmin) {
+      e = -logK;
+      trouble = true;
+    } else {
+      for (int x = 0; x < k; ++x) q[x] = p[x] * ((d[x] * d[x]) / z);
+      for (int x = 0; x < k; ++x) mean += q[x];
+      e = eb * mean + std::log(z) - logK;
+    }
+    if (std::fabs(e) < tol) break;
+    if (hi - lo < 10.0 * sq_eps) break;
+    if (e < 0.0 && b <= hi) hi = b;
+    else if (e > 0.0 && b >= lo) lo = b;
+    trouble = trouble || e < -logK || e > logN - logK;
+    double g = 0.0;
+    if (!trouble) {
+      if (it == maxit) {
+        b = (lo + hi) / 2.0;
+        it = 1;
+        continue;
+      }
+      double m2 = 0.0;
+      for (int x = 0; x < k; ++x) m2 += q[x] * (d[x] * d[x]);
+      g = (eb * eb) * ((mean * mean) - m2);
+      if (g == 0) trouble = true;
+    }
+    if (trouble) {
+      double t = 0.0;
+      for (int x = 0; x < k; ++x)
+        t += std::exp(-(d[x] * d[x]) * std::exp(lo)) + std::exp(-(d[x] * d[x]) * std::exp(hi));
+      if (t < 2.0 * std::sqrt(realmin)) break;
+      b = (lo + hi) / 2.0;
+      it = 1;
+      continue;
+    }
+    b += -e / g;
+    if (b < lo || b > hi) {
+      b = (lo + hi) / 2.0;
+      it = 0;
+    }
+    ++it;
+  }
+  return 1.0 / std::sqrt(2.0 * std::exp(b));
+}
+
+// Per-landmark sigmas. List of landmark x = its stored distances in
+// neighbour-index order (entries of the columns before x that name x, then
+// column x's own entries; a diagonal entry twice), cut to the first ka
+// entries BEFORE sorting, then sorted ascending; sigma = sum / ka.
+// With use_perplexity, sigmas are replaced by the entropic ones
+// (mdsctk.cpp:488-565), solved landmark by landmark in ascending order of the
+// ceil(K)-th list entry, each warm-started from the previous solution.
+// Returns -1 if the entropic step would read past a list (fewer than ka
+// entries, or ceil(K) > ka), which the reference leaves undefined.
+int orc_auto_sigmas(int n, const int* pcol, const int* irow, const double* val, int ka, double K,
+                    int use_perplexity, double* sig) {
+  std::vector<std::vector<double>> L(n);
+  for (int x = 0; x < n; ++x)
+    for (int y = pcol[x]; y < pcol[x + 1]; ++y) {
+      L[x].push_back(val[y]);
+      L[irow[y]].push_back(val[y]);
+    }
+  for (int x = 0; x < n; ++x) {
+    if ((int)L[x].size() > ka) L[x].resize(ka);
+    std::sort(L[x].begin(), L[x].end());
+    double s = 0.0;
+    for (double v : L[x]) s += v;
+    sig[x] = s / (double)ka;
+  }
+  if (!use_perplexity) return 0;
+  const int Ki = (int)std::ceil(K);
+  if (ka < 2 || Ki < 1 || Ki > ka) return -1;
+  for (int x = 0; x < n; ++x)
+    if ((int)L[x].size() < ka) return -1;
+  const double N = (double)ka, logK = std::log(K), logN = std::log(N), logNK = logN - logK;
+  double p1;
+  if (logK > std::log(std::sqrt(2.0 * N))) {
+    p1 = 3.0 / 4.0;
+  } else {
+    p1 = 1.0 / 4.0;
+    for (int it = 0; it < 100; ++it) p1 -= (-p1 * std::log(p1 / N) - logK) / (-std::log(p1 / N) + 1.0);
+    p1 = 1.0 - (p1 / 2.0);
+  }
+  std::vector<double> lo(n), hi(n), kth(n);
+  for (int x = 0; x < n; ++x) {
+    const double* a = L[x].data();
+    hi[x] = std::log((2.0 * std::log(p1 * (N - 1.0) / (1.0 - p1))) / ((a[1] * a[1]) - (a[0] * a[0])));
+    double l1 = std::log((2.0 * logNK / (1.0 - (1.0 / N))) / ((a[ka - 1] * a[ka - 1]) - (a[0] * a[0])));
+    double l2 = std::log((2.0 * std::sqrt(logNK)) /
+                         std::sqrt(((a[ka - 1] * a[ka - 1]) * (a[ka - 1] * a[ka - 1])) -
+                                   ((a[0] * a[0]) * (a[0] * a[0]))));
+    lo[x] = (l1 > l2) ? l1 : l2;
+    kth[x] = a[Ki - 1];
+  }
+  // processing order: indices sorted by kth with std::sort (as permutation::sort)
+  std::vector<int> order(n);
+  for (int x = 0; x < n; ++x) order[x] = x;
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return kth[a] < kth[b]; });
+  double b0 = (lo[order[0]] + hi[order[0]]) / 2.0;
+  for (int j : order) {
+    sig[j] = entropic_sigma(L[j].data(), ka, b0, logK, logN, lo[j], hi[j]);
+    b0 = std::log((1.0 / sig[j]) * (1.0 / sig[j]) / 2.0);
+  }
+  return 0;
+}
+
+// auto_decomp_sparse affinity (auto_decomp_sparse.cpp:180-203): as
+// orc_affinity with w = exp(-d^2 / (2 s_col s_row)).
+void orc_affinity_auto(int n, const int* pcol, const int* irow, double* val, const double* sig, double* d_out) {
+  for (int x = 0; x < n; ++x)
+    for (int y = pcol[x]; y < pcol[x + 1]; ++y)
+      val[y] = std::exp(-(val[y] * val[y]) / (2.0 * sig[x] * sig[irow[y]]));
+  std::vector<double> d(n, 0.0);
+  for (int x = 0; x < n; ++x)
+    for (int y = pcol[x]; y < pcol[x + 1]; ++y) {
+      d[x] += val[y];
+      d[irow[y]] += val[y];
+    }
+  for (int x = 0; x < n; ++x) d[x] = 1.0 / std::sqrt(d[x]);
+  for (int x = 0; x < n; ++x)
+    for (int y = pcol[x]; y < pcol[x + 1]; ++y) val[y] *= d[irow[y]] * d[x];
+  if (d_out)
+    for (int x = 0; x < n; ++x) d_out[x] = d[x];
+}
+
+// auto_decomp_sparse_nystrom B (auto_decomp_sparse_nystrom.cpp:171-209):
+// w = exp(-d^2 / (2 s_l s_l)) with the landmark's sigma, then as
+// orc_affinity_nystrom.
+void orc_affinity_nystrom_auto(int m, const int* pcolB, const int* irowB, double* valB, const double* sig,
+                               const double* d_a) {
+  for (int x = 0; x < m; ++x)
+    for (int y = pcolB[x]; y < pcolB[x + 1]; ++y)
+      valB[y] = std::exp(-(valB[y] * valB[y]) / (2.0 * sig[irowB[y]] * sig[irowB[y]]));
+  std::vector<double> db(m, 0.0);
+  for (int x = 0; x < m; ++x)
+    for (int y = pcolB[x]; y < pcolB[x + 1]; ++y) db[x] += valB[y];
+  for (int x = 0; x < m; ++x) db[x] = 1.0 / std::sqrt(db[x]);
+  for (int x = 0; x < m; ++x)
+    for (int y = pcolB[x]; y < pcolB[x + 1]; ++y) valB[y] *= d_a[irowB[y]] * db[x];
+}
+
 // sp_dsymv (mdsctk.cpp:293-313): y = A x, A symmetric stored as one triangle
 // per column, a diagonal entry counted once only when it is the column's
 // first stored entry.
@@ -528,6 +689,184 @@ void orc_sp_dgemv(int n, const int* irow, const int* pcol, const double* A, cons
     w[i] = 0.0;
     for (int j = pcol[i]; j < pcol[i + 1]; ++j) w[i] += v[irow[j]] * A[j];
   }
+}
+
+// ---------------------------------------------------------------------------
+// .xtc decoding (GROMACS compressed coordinates; read through GROMACS by the
+// reference, mdsctk.cpp:217-267). Restated from the published format with a
+// plain bit-position reader and 128-bit mixed-radix arithmetic. Returns the
+// number of frames decoded into xyz [frame][atom][3] (at most max_frames), or
+// -1 on a malformed frame. *natoms receives the atom count.
+// ---------------------------------------------------------------------------
+static const int kXtcMagic[73] = {
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 8, 10, 12, 16, 20, 25, 32, 40, 50, 64, 80, 101, 128, 161, 203, 256, 322, 406,
+    512, 645, 812, 1024, 1290, 1625, 2048, 2580, 3250, 4096, 5060, 6501, 8192, 10321, 13003, 16384, 20642,
+    26007, 32768, 41285, 52015, 65536, 82570, 104031, 131072, 165140, 208063, 262144, 330280, 416127, 524287,
+    660561, 832255, 1048576, 1321122, 1664510, 2097152, 2642245, 3329021, 4194304, 5284491, 6658042, 8388607,
+    10568983, 13316085, 16777216};
+
+static uint32_t xdr_u32(const unsigned char* p) {
+  return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+}
+static float xdr_f32(const unsigned char* p) {
+  uint32_t u = xdr_u32(p);
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+struct BitPos {
+  const unsigned char* d;
+  uint64_t nbits, at = 0;
+  bool bad = false;
+  uint64_t take(int n) {  // n <= 64 bits, most significant first
+    uint64_t v = 0;
+    for (int i = 0; i < n; ++i) {
+      if (at >= nbits) {
+        bad = true;
+        return 0;
+      }
+      v = (v << 1) | ((d[at >> 3] >> (7 - (at & 7))) & 1u);
+      ++at;
+    }
+    return v;
+  }
+  // nbits-bit number sent as little-endian 8-bit groups (the last one short)
+  unsigned __int128 packed(int n) {
+    unsigned __int128 v = 0;
+    int shift = 0;
+    while (n > 8) {
+      v |= (unsigned __int128)take(8) << shift;
+      shift += 8;
+      n -= 8;
+    }
+    if (n > 0) v |= (unsigned __int128)take(n) << shift;
+    return v;
+  }
+};
+
+static int bits_needed(uint64_t size) {  // smallest b with 2^b > size
+  int b = 0;
+  while (b < 32 && (1ull << b) <= size) ++b;
+  return b;
+}
+
+int orc_xtc_decode(const unsigned char* buf, size_t len, int max_frames, int* natoms_out, float* xyz, int* steps,
+                   float* times) {
+  size_t o = 0;
+  int nf = 0, na = -1;
+  while (o + 56 <= len && nf < max_frames) {
+    const unsigned char* h = buf + o;
+    if (xdr_u32(h) != 1995) return -1;
+    int a = (int)xdr_u32(h + 4);
+    if (na >= 0 && a != na) return -1;
+    na = a;
+    if (steps) steps[nf] = (int)xdr_u32(h + 8);
+    if (times) times[nf] = xdr_f32(h + 12);
+    float* out = xyz ? xyz + (size_t)nf * a * 3 : nullptr;
+    if (a <= 9) {
+      if (o + 56 + 12 * (size_t)a > len) break;
+      if (out)
+        for (int i = 0; i < 3 * a; ++i) out[i] = xdr_f32(h + 56 + 4 * i);
+      o += 56 + 12 * (size_t)a;
+      ++nf;
+      continue;
+    }
+    if (o + 92 > len) break;
+    float prec = xdr_f32(h + 56);
+    long long mn[3], mx[3];
+    for (int c = 0; c < 3; ++c) {
+      mn[c] = (int)xdr_u32(h + 60 + 4 * c);
+      mx[c] = (int)xdr_u32(h + 72 + 4 * c);
+    }
+    int sidx = (int)xdr_u32(h + 84);
+    if (sidx < 9 || sidx > 72) return -1;
+    size_t nbytes = xdr_u32(h + 88);
+    if (o + 92 + nbytes > len) break;
+    uint64_t sz[3];
+    bool large = false;
+    for (int c = 0; c < 3; ++c) {
+      sz[c] = (uint64_t)(mx[c] - mn[c] + 1);
+      if (sz[c] > 0xffffff) large = true;
+    }
+    // bits of sz0*sz1*sz2 (exact)
+    unsigned __int128 prod = (unsigned __int128)sz[0] * sz[1] * sz[2];
+    int pbits = 0;  // bit length of the product itself (not of product - 1)
+    while (pbits < 128 && (prod >> pbits) != 0) ++pbits;
+    BitPos br{h + 92, (uint64_t)nbytes * 8};
+    const float inv = (float)(1.0 / (double)prec);
+    int smaller = kXtcMagic[std::max(9, sidx - 1)] / 2, smallnum = kXtcMagic[sidx] / 2;
+    long long prev[3] = {0, 0, 0};
+    int run = 0, i = 0, w = 0;
+    auto emit = [&](const long long* v) {
+      if (out)
+        for (int c = 0; c < 3; ++c) out[3 * w + c] = (float)(int)v[c] * inv;
+      ++w;
+    };
+    while (i < a) {
+      long long cur[3];
+      if (large) {
+        for (int c = 0; c < 3; ++c) cur[c] = (long long)(uint32_t)br.take(bits_needed(sz[c]));
+      } else {
+        unsigned __int128 v = br.packed(pbits);
+        cur[2] = (long long)(v % sz[2]);
+        v /= sz[2];
+        cur[1] = (long long)(v % sz[1]);
+        v /= sz[1];
+        cur[0] = (long long)(int32_t)(uint32_t)v;
+      }
+      ++i;
+      for (int c = 0; c < 3; ++c) {
+        cur[c] = (long long)(int32_t)(uint32_t)(cur[c] + mn[c]);
+        prev[c] = cur[c];
+      }
+      int dsmall = 0;
+      if (br.take(1)) {
+        int r = (int)br.take(5);
+        dsmall = r % 3 - 1;
+        run = r - r % 3;
+      }
+      if (run > 0) {
+        if (i + run / 3 > a) return -1;
+        const uint64_t m = (uint64_t)kXtcMagic[sidx];
+        for (int k = 0; k < run; k += 3) {
+          unsigned __int128 v = br.packed(sidx);
+          long long t[3];
+          t[2] = (long long)(v % m);
+          v /= m;
+          t[1] = (long long)(v % m);
+          v /= m;
+          t[0] = (long long)(int32_t)(uint32_t)v;
+          ++i;
+          for (int c = 0; c < 3; ++c) t[c] += prev[c] - smallnum;
+          if (k == 0) {
+            emit(t);      // the first atom of a run comes before the large one
+            emit(prev);
+            for (int c = 0; c < 3; ++c) prev[c] = t[c];
+          } else {
+            for (int c = 0; c < 3; ++c) prev[c] = t[c];
+            emit(t);
+          }
+        }
+      } else {
+        emit(cur);
+      }
+      if (br.bad) return -1;
+      sidx += dsmall;
+      if (sidx < 9 || sidx > 72) return -1;
+      if (dsmall < 0) {
+        smallnum = smaller;
+        smaller = sidx > 9 ? kXtcMagic[sidx - 1] / 2 : 0;
+      } else if (dsmall > 0) {
+        smaller = smallnum;
+        smallnum = kXtcMagic[sidx] / 2;
+      }
+    }
+    o += 92 + ((nbytes + 3) / 4) * 4;
+    ++nf;
+  }
+  if (natoms_out) *natoms_out = na < 0 ? 0 : na;
+  return nf;
 }
 
 int orc_num_threads(void) {

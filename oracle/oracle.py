@@ -65,6 +65,15 @@ def lib():
         L.orc_affinity.restype = None
         L.orc_affinity_nystrom.argtypes = [c_int, _i32p, _i32p, _f64p, c_dbl, _f64p]
         L.orc_affinity_nystrom.restype = None
+        L.orc_auto_sigmas.argtypes = [c_int, _i32p, _i32p, _f64p, c_int, c_dbl, c_int, _f64p]
+        L.orc_auto_sigmas.restype = c_int
+        L.orc_affinity_auto.argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+        L.orc_affinity_auto.restype = None
+        L.orc_affinity_nystrom_auto.argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+        L.orc_affinity_nystrom_auto.restype = None
+        L.orc_xtc_decode.argtypes = [ctypes.c_void_p, ctypes.c_size_t, c_int, _i32p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_xtc_decode.restype = c_int
         L.orc_sp_dsymv.argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
         L.orc_sp_dsymv.restype = None
         L.orc_sp_dgemv.argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
@@ -234,6 +243,70 @@ def decomp_sparse(n, pcol, irow, dist, sigma, nev, ncv=None, tol=0.0, maxiter=No
     res = np.array([np.linalg.norm(sp_dsymv(n, pcol, irow, A, V[x]) - w[x] * V[x]) / abs(w[x])
                     for x in range(nev)])
     return w, V, res
+
+
+def auto_sigmas(n, pcol, irow, dist, k_sigma, perplexity=None):
+    """Per-landmark sigmas of auto_decomp_sparse (auto_decomp_sparse.cpp:153-178,
+    mdsctk.cpp:388-565); perplexity None = the k-sigma means only."""
+    sig = np.zeros(n, np.float64)
+    rc = lib().orc_auto_sigmas(n, _c(pcol, np.int32), _c(irow, np.int32), _c(dist, np.float64), int(k_sigma),
+                               float(perplexity or 0.0), int(perplexity is not None), sig)
+    if rc != 0:
+        raise ValueError("entropic sigmas need every landmark list to hold k-sigma >= ceil(K) entries")
+    return sig
+
+
+def affinity_auto(n, pcol, irow, val, sig):
+    v = _c(val, np.float64).copy()
+    d = np.zeros(n, np.float64)
+    lib().orc_affinity_auto(n, _c(pcol, np.int32), _c(irow, np.int32), v, _c(sig, np.float64), d)
+    return v, d
+
+
+def affinity_nystrom_auto(m, pcolB, irowB, valB, sig, d_a):
+    v = _c(valB, np.float64).copy()
+    lib().orc_affinity_nystrom_auto(m, _c(pcolB, np.int32), _c(irowB, np.int32), v, _c(sig, np.float64),
+                                    _c(d_a, np.float64))
+    return v
+
+
+def auto_decomp_sparse(n, pcol, irow, dist, k_sigma, nev, perplexity=None, ncv=None, tol=0.0, maxiter=None):
+    """auto_decomp_sparse oracle: per-landmark sigmas, affinity with
+    exp(-d^2 / 2 s_c s_r), normalisation, ARPACK 'LA' eigenpairs.
+    Returns (evals descending, evecs [nev, n], residuals, sigmas)."""
+    from scipy.sparse.linalg import eigsh
+
+    sig = auto_sigmas(n, pcol, irow, dist, k_sigma, perplexity)
+    A, _ = affinity_auto(n, pcol, irow, dist, sig)
+    op = sym_operator(n, pcol, irow, A)
+    ncv = min(10 * nev + 1, n) if ncv is None else ncv
+    maxiter = 100 * nev if maxiter is None else maxiter
+    w, V = eigsh(op, k=nev, which="LA", ncv=ncv, tol=tol, maxiter=maxiter)
+    order = np.argsort(w)[::-1]
+    w = w[order]
+    V = V[:, order].T.copy()
+    res = np.array([np.linalg.norm(sp_dsymv(n, pcol, irow, A, V[x]) - w[x] * V[x]) / abs(w[x])
+                    for x in range(nev)])
+    return w, V, res, sig
+
+
+def xtc_read(path_or_bytes, max_frames=None):
+    """Decode an .xtc file: (xyz [frames, atoms, 3] float32 nm, steps, times)."""
+    b = path_or_bytes if isinstance(path_or_bytes, (bytes, bytearray)) else open(path_or_bytes, "rb").read()
+    buf = ctypes.create_string_buffer(bytes(b), len(b))
+    na = np.zeros(1, np.int32)
+    n = lib().orc_xtc_decode(buf, len(b), 1 << 30, na, None, None, None)
+    if n < 0:
+        raise ValueError("malformed xtc")
+    if max_frames is not None:
+        n = min(n, max_frames)
+    xyz = np.zeros((n, int(na[0]), 3), np.float32)
+    steps = np.zeros(n, np.int32)
+    times = np.zeros(n, np.float32)
+    vp = ctypes.c_void_p
+    lib().orc_xtc_decode(buf, len(b), n, na, xyz.ctypes.data_as(vp), steps.ctypes.data_as(vp),
+                         times.ctypes.data_as(vp))
+    return xyz, steps, times
 
 
 def dense_affinity(n, pcol, irow, dist, sigma):

@@ -3,8 +3,12 @@
 * rings.pts, swissroll.pts: the reference's own example inputs
   (examples/rings.pts: 400 x 2 f64; examples/swissroll.pts: 1000 x 3 f64),
   copied verbatim so the tests can run where the reference is absent.
+* trp-cage.xtc, trp-cage.pdb: the reference's example trajectory (1000
+  frames of the 60 backbone atoms of Trp-cage, GROMACS compressed
+  coordinates) and its topology, copied verbatim.
 * knn_data_*.npz: oracle outputs on those inputs (regression vectors of the
-  oracle; the reference itself cannot be built here).
+  oracle; the reference itself cannot be built without GROMACS, Boost,
+  Berkeley DB and ARPACK).
 
 Run from the repository root: python tests/golden/make_golden.py
 """
@@ -20,7 +24,7 @@ REFERENCE_EXAMPLES = "/root/reference/examples"
 
 
 def main():
-    for name in ("rings.pts", "swissroll.pts"):
+    for name in ("rings.pts", "swissroll.pts", "trp-cage.xtc", "trp-cage.pdb"):
         src = os.path.join(REFERENCE_EXAMPLES, name)
         if os.path.exists(src):
             shutil.copyfile(src, os.path.join(HERE, name))

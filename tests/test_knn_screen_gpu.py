@@ -37,6 +37,25 @@ def test_screen_lower_bound_and_completeness(ctx, oracle, precision, n, natoms, 
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x3"])
+def test_screen_lower_bound_off_trajectory_queries(ctx, oracle, precision):
+    """Queries off the landmarks' trajectory (distances concentrated, frames
+    far from the template): the guarded values stay lower bounds and the
+    kept set is complete."""
+    land = synth.trajectory(3000, 304, seed=5, basins=16, dwell=100.0)
+    qry = synth.trajectory(48, 304, seed=6, basins=16, dwell=100.0, off_manifold=0.2, off_sigma=0.3)
+    m = synth.uniform_masses(304)
+    lb, idx, cnt = ctx.knn_rms_screen(land, qry, m, 128, precision=precision)
+    d, _ = oracle.knn_rms(land, qry, m, 0, sort=False)
+    ex = (d / 10.0) ** 2
+    rows = np.arange(len(qry))[:, None]
+    assert np.all(lb <= ex[rows, idx] * (1 + 1e-6) + 1e-9), np.max(lb - ex[rows, idx])
+    tau = lb[:, -1]
+    for r in range(len(qry)):
+        assert set(np.nonzero(ex[r] < tau[r])[0].tolist()) <= set(idx[r].tolist()), r
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
 def test_knn_rms_no_flagged_rows(ctx, oracle, precision):
     """On well-conditioned multi-basin data the guard holds on the first pass."""

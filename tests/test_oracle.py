@@ -168,3 +168,83 @@ def test_decomp_oracle_vs_dense(oracle):
     we, Ve = np.linalg.eigh(M)
     assert np.allclose(w, we[::-1][:4], rtol=1e-10, atol=1e-10)
     assert np.all(res < 1e-8)
+
+
+def test_oracle_entropic_sigmas_reach_perplexity(oracle):
+    """Entropic sigmas: the normalised exp(-d^2/2s^2) over each landmark's
+    k-sigma sorted distances has perplexity K (to the 1e-10 root tolerance)."""
+    rng = np.random.default_rng(1)
+    x = np.concatenate([rng.normal(size=(300, 2)), rng.normal(size=(300, 2)) + 4])
+    d, i = oracle.knn_data(x, None, 12)
+    n, pc, ir, v = oracle.sysparse(d, i)
+    K, ka = 5.0, 10
+    sig = oracle.auto_sigmas(n, pc, ir, v, ka, perplexity=K)
+    lists = [[] for _ in range(n)]
+    for c in range(n):
+        for p in range(pc[c], pc[c + 1]):
+            lists[c].append(v[p])
+            lists[ir[p]].append(v[p])
+    for j in range(n):
+        a = np.sort(np.array(lists[j][:ka]))
+        p = np.exp(-a ** 2 / (2 * sig[j] ** 2))
+        p /= p.sum()
+        assert abs(-(p * np.log(p)).sum() - np.log(K)) < 1e-8
+    # the k-sigma mean is the plain mean of the first ka (by neighbour index), trimmed before sorting
+    mean = oracle.auto_sigmas(n, pc, ir, v, ka)
+    assert np.allclose(mean, [np.sum(np.sort(lists[j][:ka])) / ka for j in range(n)], rtol=0, atol=1e-15)
+
+
+def _xtc_frames_end(b):
+    """Byte offset where a header walk of an .xtc file ends."""
+    import struct
+
+    o = 0
+    while o + 56 <= len(b):
+        na = struct.unpack(">i", b[o + 4:o + 8])[0]
+        if na <= 9:
+            o += 56 + 12 * na
+        else:
+            nb = struct.unpack(">i", b[o + 88:o + 92])[0]
+            o += 92 + (nb + 3) // 4 * 4
+    return o
+
+
+def test_oracle_xtc_trp_cage(oracle):
+    """The example trajectory decodes to 1000 frames of 60 backbone atoms
+    (the topology's count); every N-CA, CA-C and C-N bond of every frame is
+    a physical length, and the frames use up the whole file."""
+    path = os.path.join(os.path.dirname(__file__), "golden", "trp-cage.xtc")
+    b = open(path, "rb").read()
+    xyz, steps, times = oracle.xtc_read(b)
+    assert xyz.shape == (1000, 60, 3)
+    pdb = open(os.path.join(os.path.dirname(__file__), "golden", "trp-cage.pdb")).read().splitlines()
+    names = [ln[12:16].strip() for ln in pdb if ln.startswith("ATOM")]
+    assert len(names) == 60 and names[:3] == ["N", "CA", "C"]
+    assert np.all(np.diff(steps) > 0) and np.all(np.diff(times) > 0)
+    bond = np.linalg.norm(xyz[:, 1:] - xyz[:, :-1], axis=2)
+    for t, (lo, hi) in enumerate(((0.13, 0.165), (0.135, 0.175), (0.12, 0.15))):  # N-CA, CA-C, C-N
+        assert lo < bond[:, t::3].min() and bond[:, t::3].max() < hi
+    assert _xtc_frames_end(b) == len(b)
+
+
+def test_oracle_xtc_synthetic_paths(oracle):
+    import xtc_synth as X
+
+    # raw frames (<= 9 atoms)
+    q = X.walk(7, 1)
+    f = X.encode_frame(q, prec=1000.0, step=5)
+    xyz, steps, _ = oracle.xtc_read(f + f)
+    assert xyz.shape == (2, 7, 3) and np.array_equal(xyz[0], (q / 1000.0).astype(np.float32))
+    # no runs, ranges above 2^24 (fixed-width fields)
+    q = X.walk(40, 2, step=3)
+    q[5] += 30_000_000
+    xyz, _, _ = oracle.xtc_read(X.encode_frame(q, prec=1e6))
+    inv = np.float32(1.0 / 1e6)
+    assert np.array_equal(xyz[0], q.astype(np.int32).astype(np.float32) * inv)
+    # runs, small-index changes, a run reused through a clear flag
+    q = X.walk(60, 3)
+    groups = [(2, 0, True), (2, 0, False), (0, 0, True), (3, 1, True), (1, -1, True), (5, 0, True),
+              (5, 0, False), (0, -1, True), (4, 0, True)]
+    groups += [(0, 0, True)] * (60 - sum(g[0] + 1 for g in groups))
+    xyz, _, _ = oracle.xtc_read(X.encode_frame(q, prec=1000.0, groups=groups, smallidx=12))
+    assert np.array_equal(xyz[0], q.astype(np.int32).astype(np.float32) * np.float32(1.0 / 1000.0))

@@ -28,9 +28,12 @@ def served(ctx, oracle):
 def test_model_matches_pipeline(served, oracle):
     srv, land, m, k, nev, sigma, (d, i) = served
     n, pcol, irow, val = oracle.sysparse(d, i)
-    wo, Vo, _ = oracle.decomp_sparse(n, pcol, irow, val, sigma, nev)
+    # this graph has three connected components, so 1.0 is a triple
+    # eigenvalue; ARPACK (one start vector) may return fewer copies, the
+    # exact spectrum (dense, n = 900) has all three
+    exact = np.linalg.eigvalsh(oracle.dense_affinity(n, pcol, irow, val, sigma))[::-1][:nev]
     w, V = srv.model()
-    assert np.allclose(w, wo, rtol=1e-6)
+    assert np.allclose(w, exact, rtol=1e-6)
 
 
 @pytest.mark.gpu
@@ -73,7 +76,7 @@ def test_alone_equals_in_the_mix(served):
         t.start()
     for t in th:
         t.join()
-    batched = sum(1 for o in out if o[3]["batch_frames"] > reqs[out.index(o)].shape[0])
+    batched = sum(1 for j, o in enumerate(out) if o[3]["batch_frames"] > reqs[j].shape[0])
     for a, o in zip(alone, out):
         for u, v in zip(a, o[:3]):
             assert np.array_equal(u, v)

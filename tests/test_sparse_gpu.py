@@ -113,3 +113,85 @@ def test_nystrom_extension(ctx, oracle):
     for x in range(5):
         ext_o = oracle.sp_dgemv(m, pb, ib, Bo, V[x] / w[x])  # the extension of this run's vector
         assert np.max(np.abs(E[x] - ext_o)) < 1e-10
+
+
+def _rings_graph(oracle, k=20, keep=12):
+    import os
+
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    x = np.fromfile(os.path.join(gold, "rings.pts"), np.float64).reshape(-1, 2)
+    d, i = oracle.knn_data(x, None, k)
+    return oracle.sysparse(d, i, keep)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ka", [1, 7, 12, 40])
+def test_auto_sigmas_mean_bit_exact(ctx, oracle, ka):
+    """k-sigma means: the first ka entries in neighbour-index order, sorted,
+    summed in ascending order (bit-exact), lists shorter than ka included."""
+    n, pcol, irow, val = _rings_graph(oracle)
+    w, V, res, nconv, sig = ctx.auto_decomp_sparse(n, pcol, irow, val, ka, 4)
+    osig = oracle.auto_sigmas(n, pcol, irow, val, ka)
+    assert np.array_equal(sig, osig)
+    wo, Vo, _, _ = oracle.auto_decomp_sparse(n, pcol, irow, val, ka, 4)
+    assert np.allclose(w, wo, rtol=1e-6, atol=1e-9)
+    assert np.max(res) < 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("K", [3.0, 7.5, 12.0])
+def test_auto_sigmas_entropic(ctx, oracle, K):
+    n, pcol, irow, val = _rings_graph(oracle)
+    w, V, res, nconv, sig = ctx.auto_decomp_sparse(n, pcol, irow, val, 12, 5, perplexity=K)
+    wo, Vo, _, osig = oracle.auto_decomp_sparse(n, pcol, irow, val, 12, 5, perplexity=K)
+    # same roots, different warm starts: agreement to the root-finding tolerance
+    assert np.allclose(sig, osig, rtol=1e-8)
+    assert np.allclose(w, wo, rtol=1e-6, atol=1e-9)
+    _same_subspaces(wo, V, Vo)
+
+
+def _same_subspaces(w, V, Vo, gap=1e-5):
+    """Eigenvectors agree up to rotation within groups of eigenvalues closer
+    than `gap` (sigmas that differ at 1e-10 rotate nearly degenerate pairs);
+    the group holding the last eigenvalue is skipped (its partners beyond nev
+    are unknown)."""
+    groups, cur = [], [0]
+    for x in range(1, len(w)):
+        if abs(w[x] - w[x - 1]) < gap * max(1.0, abs(w[x])):
+            cur.append(x)
+        else:
+            groups.append(cur)
+            cur = [x]
+    for g in groups:  # `cur` (the last group) is not compared
+        Q1, _ = np.linalg.qr(V[g].T)
+        Q2, _ = np.linalg.qr(Vo[g].T)
+        assert np.min(np.linalg.svd(Q1.T @ Q2, compute_uv=False)) > 1 - 1e-6
+
+
+@pytest.mark.gpu
+def test_auto_sigmas_rejects_short_lists(ctx, oracle):
+    from mdsctk_gb300 import MdsError
+
+    n, pcol, irow, val = _rings_graph(oracle, keep=3)
+    with pytest.raises(MdsError):  # every list holds >= 3, some < 30: the reference reads past them
+        ctx.auto_decomp_sparse(n, pcol, irow, val, 30, 3, perplexity=5.0)
+    with pytest.raises(MdsError):  # ceil(K) > k-sigma
+        ctx.auto_decomp_sparse(n, pcol, irow, val, 3, 3, perplexity=5.0)
+
+
+@pytest.mark.gpu
+def test_auto_nystrom(ctx, oracle):
+    rng = np.random.default_rng(8)
+    land = np.concatenate([rng.normal(size=(250, 2)), rng.normal(size=(250, 2)) + 5])
+    qry = np.concatenate([rng.normal(size=(60, 2)), rng.normal(size=(60, 2)) + 5])
+    d, i = oracle.knn_data(land, None, 12)
+    n, pcol, irow, val = oracle.sysparse(d, i)
+    dq, iq = oracle.knn_data(land, qry, 12)
+    m, pb, ib, vb = oracle.gesparse(dq, iq)
+    w, V, E, res, nconv, sig = ctx.auto_decomp_sparse_nystrom(n, pcol, irow, val, m, pb, ib, vb, 8, 5)
+    osig = oracle.auto_sigmas(n, pcol, irow, val, 8)
+    assert np.array_equal(sig, osig)
+    _, d_a = oracle.affinity_auto(n, pcol, irow, val, osig)
+    Bo = oracle.affinity_nystrom_auto(m, pb, ib, vb, osig, d_a)
+    Eo = oracle.nystrom_extend(w, V, m, pb, ib, Bo)
+    assert np.max(np.abs(E - Eo)) < 1e-10

@@ -103,3 +103,25 @@ def test_nystrom_tools(ctx, oracle, tmp_path):
     _run(build, tmp_path, "decomp_sparse_nystrom", "-q", "1.0", "-n", "3", "--binary-out")
     V = np.fromfile(tmp_path / "eigenvectors.dat", np.float64).reshape(3, 300 + 80)
     assert np.all(np.isfinite(V))
+
+
+@pytest.mark.gpu
+def test_auto_decomp_tools(ctx, oracle, tmp_path):
+    from mdsctk_gb300 import build
+
+    build.build()
+    x = np.fromfile(os.path.join(GOLD, "rings.pts"), np.float64).reshape(-1, 2)
+    x.tofile(tmp_path / "reference.pts")
+    _run(build, tmp_path, "knn_data", "-k", "20", "-v", "2", "-r", "reference.pts")
+    _run(build, tmp_path, "make_sysparse", "-k", "20", "-n", "12")
+    n, pcol, irow, val = _read_csc(tmp_path / "distances.ssm")
+    out = _run(build, tmp_path, "auto_decomp_sparse", "-k", "10", "-K", "6", "-n", "4", "--binary-out")
+    assert "Average sigma:" in out and "Maximum residual:" in out
+    w = np.fromfile(tmp_path / "eigenvalues.dat", np.float64)
+    wo, _, _, osig = oracle.auto_decomp_sparse(n, pcol, irow, val, 10, 4, perplexity=6.0)
+    assert np.allclose(w, wo, rtol=1e-6, atol=1e-9)
+    avg = float(out.split("Average sigma:")[1].split()[0])
+    assert abs(avg - osig.mean()) <= 1e-5 * osig.mean()
+    r = subprocess.run([os.path.join(build.BINDIR, "auto_decomp_sparse"), "-k", "3", "-K", "6", "-n", "4"],
+                       cwd=tmp_path, capture_output=True, text=True)
+    assert "WARNING: --k-perplexity (6) is higher than --k-sigma (3)" in r.stdout
