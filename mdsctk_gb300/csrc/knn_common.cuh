@@ -93,7 +93,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
 // pieces of the knn_rms pipeline (knn_rms.cu), reused by the serving loop
 int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass,
                   const float* dswn, float tm, float* Y, double* E);
-int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const double* dmu,
+int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const float* dmu,
                     const double* dM0, int nofit, float* A, float* R);
 int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit, std::vector<double>& mu,
                    double M0[9]);

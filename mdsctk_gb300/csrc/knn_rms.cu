@@ -55,6 +55,11 @@ __device__ __forceinline__ void block_sum_vec(double (&v)[N], double* red) {
 
 // One block per frame. raw: [n][natoms][3]; out: [n][3][Ap]; E: |y|^2 per
 // unit mass (double). tm: float sum of masses in file order (reset_x's tm).
+// Per-atom arithmetic is FP32 (FP64 issues at a small fraction of the FP32
+// rate on this GPU); only the block reductions of the per-thread partial sums
+// are FP64. The centre of mass therefore differs from reset_x's FP64 sum by
+// ~1e-7 relative, which moves an optimal-superposition RMSD only at second
+// order (the cross term vanishes for centred frames).
 __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int Ap,
                          const float* __restrict__ mass, const float* __restrict__ swn, float tm,
                          float* __restrict__ out, double* __restrict__ E) {
@@ -62,23 +67,23 @@ __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int A
   int f = blockIdx.x;
   if (f >= n) return;
   const float* x = raw + (int64_t)f * natoms * 3;
-  double s[3] = {0, 0, 0};
+  float p[3] = {0.f, 0.f, 0.f};
   for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
     float mm = mass[a];
-    for (int c = 0; c < 3; ++c) s[c] += (double)(mm * x[3 * a + c]);
+    for (int c = 0; c < 3; ++c) p[c] = fmaf(mm, x[3 * a + c], p[c]);
   }
+  double s[3] = {p[0], p[1], p[2]};
   block_sum_vec<3>(s, red);
-  double com[3];
-  for (int c = 0; c < 3; ++c) com[c] = s[c] / (double)tm;
-  double e = 0;
+  float com[3];
+  for (int c = 0; c < 3; ++c) com[c] = (float)(s[c] / (double)tm);
+  float e = 0.f;
   float* o = out + (int64_t)f * 3 * Ap;
   for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
     for (int c = 0; c < 3; ++c) {
       float v = 0.0f;
       if (a < natoms) {
-        float y = (float)((double)x[3 * a + c] - com[c]);  // reset_x: double shift, float store
-        v = y * swn[a];
-        e += (double)v * (double)v;
+        v = (x[3 * a + c] - com[c]) * swn[a];
+        e = fmaf(v, v, e);
       }
       o[c * Ap + a] = v;
     }
@@ -91,56 +96,59 @@ __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int A
 // ---------------------------------------------------------------------------
 // 2. superposition onto the template
 // ---------------------------------------------------------------------------
-// mu: [3][Ap] double (template, principal axes). M0: sum mu mu^T (9 doubles).
+// mu: [3][Ap] float (template, principal axes). M0: sum mu mu^T (9 doubles).
 // dev: [n][3][Ap] float deviations a = R y - mu (FP32 screen operand).
-// rec: [n][MDS_REC] screen record.
+// rec: [n][MDS_REC] screen record. The rotation only has to be a proper
+// rotation (x~ = mu + a is an exact rigid copy of the frame for any R; a
+// better fit only makes |a| smaller), so per-atom work is FP32; the 3x3 sums
+// are reduced in FP64 and the quaternion is solved in FP64 by one thread.
 __global__ void k_prealign(const float* __restrict__ Y, const double* __restrict__ E, int n,
-                           int natoms, int Ap, const double* __restrict__ mu,
+                           int natoms, int Ap, const float* __restrict__ mu,
                            const double* __restrict__ M0, int nofit, float* __restrict__ dev,
                            float* __restrict__ rec) {
   __shared__ double red[32 * 10];
-  __shared__ double Rsh[9];
+  __shared__ float Rsh[9];
   int f = blockIdx.x;
   if (f >= n) return;
   const float* y = Y + (int64_t)f * 3 * Ap;
   if (!nofit) {
-    double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float p[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
-      double yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
-      double mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
+      float yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
+      float mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
       for (int c = 0; c < 3; ++c)
-        for (int d = 0; d < 3; ++d) s[3 * c + d] += yc[c] * mc[d];
+        for (int d = 0; d < 3; ++d) p[3 * c + d] = fmaf(yc[c], mc[d], p[3 * c + d]);
     }
+    double s[9];
+    for (int i = 0; i < 9; ++i) s[i] = p[i];
     block_sum_vec<9>(s, red);
-    double S[9];
-    for (int i = 0; i < 9; ++i) S[i] = s[i];
     if (threadIdx.x == 0) {
       double emu = M0[0] + M0[4] + M0[8];
       double R[9];
-      qcp_rotation_fp64(S, 0.5 * (E[f] + emu), R);
-      for (int i = 0; i < 9; ++i) Rsh[i] = R[i];
+      qcp_rotation_fp64(s, 0.5 * (E[f] + emu), R);
+      for (int i = 0; i < 9; ++i) Rsh[i] = (float)R[i];
     }
   } else if (threadIdx.x == 0) {
-    for (int i = 0; i < 9; ++i) Rsh[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    for (int i = 0; i < 9; ++i) Rsh[i] = (i % 4 == 0) ? 1.0f : 0.0f;
   }
   __syncthreads();
-  double R[9];
+  float R[9];
   for (int i = 0; i < 9; ++i) R[i] = Rsh[i];
-  double ea = 0, u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float ea = 0.f, u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float* o = dev + (int64_t)f * 3 * Ap;
   for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
     if (a < natoms) {
-      double yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
-      double mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
+      float yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
+      float mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
       float av[3];
       for (int c = 0; c < 3; ++c) {
-        double ry = R[3 * c] * yc[0] + R[3 * c + 1] * yc[1] + R[3 * c + 2] * yc[2];
-        av[c] = (float)(ry - mc[c]);
+        float ry = fmaf(R[3 * c], yc[0], fmaf(R[3 * c + 1], yc[1], R[3 * c + 2] * yc[2]));
+        av[c] = ry - mc[c];
         o[c * Ap + a] = av[c];
       }
       for (int c = 0; c < 3; ++c) {
-        ea += (double)av[c] * av[c];
-        for (int d = 0; d < 3; ++d) u[3 * c + d] += (double)av[c] * mc[d];
+        ea = fmaf(av[c], av[c], ea);
+        for (int d = 0; d < 3; ++d) u[3 * c + d] = fmaf(av[c], mc[d], u[3 * c + d]);
       }
     } else {
       for (int c = 0; c < 3; ++c) o[c * Ap + a] = 0.0f;
@@ -148,10 +156,9 @@ __global__ void k_prealign(const float* __restrict__ Y, const double* __restrict
   }
   double eu[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
   block_sum_vec<10>(eu, red);
-  ea = eu[0];
-  double U[9];
-  for (int i = 0; i < 9; ++i) U[i] = eu[1 + i];
+  ea = (float)eu[0];
   if (threadIdx.x == 0) {
+    const double* U = eu + 1;
     float* r = rec + (int64_t)f * MDS_REC;
     double sxx = U[0], syy = U[4], szz = U[8];
     double sxy = 0.5 * (U[1] + U[3]), sxz = 0.5 * (U[2] + U[6]), syz = 0.5 * (U[5] + U[7]);
@@ -166,7 +173,7 @@ __global__ void k_prealign(const float* __restrict__ Y, const double* __restrict
     r[12] = (float)(U[5] - U[7]);
     r[13] = (float)(U[6] - U[2]);
     r[14] = (float)(U[1] - U[3]);
-    r[15] = (float)ea;
+    r[15] = (float)eu[0];
   }
 }
 
@@ -421,9 +428,11 @@ __device__ void recheck_chunk(const float* __restrict__ sfit, double Ef, const f
       float d2 = fmaf(R[6], x0, fmaf(R[7], x1, fmaf(R[8], x2, -y2)));
       acc = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, acc)));
     }
-    double v = acc;
+    // FP32 tree over the lanes (rmsdev accumulates in float as well; FP64
+    // issues at a small fraction of the FP32 rate here)
+    float v = acc;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sd[c] = (float)sqrt(v);
+    if (lane == 0) sd[c] = sqrtf(v);
   }
   __syncthreads();
 }
@@ -685,7 +694,7 @@ int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, co
   return MDS_OK;
 }
 
-int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const double* dmu,
+int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const float* dmu,
                     const double* dM0, int nofit, float* A, float* R) {
   if (n <= 0) return MDS_OK;
   ctx->stats.launches++;
@@ -793,14 +802,15 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   double M0[9];
   MDS_TRY(build_template(ctx, Yr.as<float>(), Ap, natoms, pl.nofit != 0, mu, M0));
   DevBuf dmu(ctx), dM0(ctx), Ar(ctx), Rr(ctx), Af(ctx), Rf(ctx);
-  MDS_TRY(dmu.alloc(ctx, sizeof(double) * 3 * Ap));
+  std::vector<float> muf(mu.begin(), mu.end());
+  MDS_TRY(dmu.alloc(ctx, sizeof(float) * 3 * Ap));
   MDS_TRY(dM0.alloc(ctx, sizeof(double) * 9));
-  MDS_CUDA(ctx, cudaMemcpyAsync(dmu.p, mu.data(), sizeof(double) * 3 * Ap, cudaMemcpyHostToDevice, s));
+  MDS_CUDA(ctx, cudaMemcpyAsync(dmu.p, muf.data(), sizeof(float) * 3 * Ap, cudaMemcpyHostToDevice, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(Ar.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
   MDS_TRY(Rr.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nref));
   st.launches++;
-  k_prealign<<<nref, 128, 0, s>>>(Yr.as<float>(), Er.as<double>(), nref, natoms, Ap, dmu.as<double>(),
+  k_prealign<<<nref, 128, 0, s>>>(Yr.as<float>(), Er.as<double>(), nref, natoms, Ap, dmu.as<float>(),
                                    dM0.as<double>(), pl.nofit, Ar.as<float>(), Rr.as<float>());
   MDS_CUDA(ctx, cudaGetLastError());
   const float* Afp = Ar.as<float>();
@@ -809,7 +819,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(Af.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
     MDS_TRY(Rf.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nfit));
     st.launches++;
-    k_prealign<<<nfit, 128, 0, s>>>(Yfp, Efp, nfit, natoms, Ap, dmu.as<double>(), dM0.as<double>(),
+    k_prealign<<<nfit, 128, 0, s>>>(Yfp, Efp, nfit, natoms, Ap, dmu.as<float>(), dM0.as<double>(),
                                      pl.nofit, Af.as<float>(), Rf.as<float>());
     MDS_CUDA(ctx, cudaGetLastError());
     Afp = Af.as<float>();

@@ -10,21 +10,23 @@
 // CTA tile: M = 128 TMEM lanes = 40 fit frames (each 32-lane quarter holds
 // 10 frames x 3 coordinates, two padding lanes), N = 240 columns = 80
 // reference frames stored coordinate-major (x of 80 frames, then y, then z).
-// Reduction in K-blocks of 32 atoms through a 4-stage TMA pipeline
+// Reduction in K-blocks of 32 atoms through a 3-stage TMA pipeline
 // (64-byte swizzle). Two TMEM accumulators (2 x 240 of 512 columns) let the
 // MMA of one column tile run under the epilogue of the previous one.
 //
-// Warp roles (320 threads, one CTA per SM, persistent over work items =
+// Warp roles (576 threads, one CTA per SM, persistent over work items =
 // (row tile, column segment)):
-//   warp 0      TMA producer (one thread)
-//   warp 1      TMEM allocator + MMA issuer (one thread)
-//   warps 2..9  epilogue: two warps per TMEM lane quarter, each taking half
-//               of the column chunks. A 3-lane shuffle transpose gives each
-//               lane the full 3x3 Gram of one pair; the shifted QCP bound
-//               (qcp.cuh) and the guard give the lower bound of RMSD^2;
-//               passing pairs are appended to a per-(row, segment) buffer of
-//               512 keys in global memory, compacted to the best K' in
-//               shared-memory scratch when it fills.
+//   warp 0       TMA producer (one thread)
+//   warp 1       TMEM allocator + MMA issuer (one thread)
+//   warps 2..17  epilogue: four warps per TMEM lane quarter, each taking a
+//                quarter of the column chunks. A 3-lane shuffle transpose
+//                gives each lane the full 3x3 Gram of one pair; the shifted
+//                QCP bound (qcp.cuh) and the guard give the lower bound of
+//                RMSD^2; passing pairs are appended to a per-(row, segment)
+//                buffer of 512 keys in global memory, cut back to the best K'
+//                by a warp radix select when it fills.
+// Column tiles are visited outward from the row tile's own frames when a set
+// is screened against itself, so thresholds tighten early.
 // Every wait is bounded; on a timeout the kernel records an error, drains,
 // frees its TMEM and returns.
 #include <cuda.h>
@@ -43,9 +45,9 @@
 #define TC_M 128
 #define TC_N 240
 #define TC_KB 32
-#define TC_STAGES 4
-#define TC_THREADS 320
-#define TC_EPI_WARPS 8
+#define TC_STAGES 3
+#define TC_THREADS 576
+#define TC_EPI_WARPS 16
 #define TC_CAPG 512
 #define TC_A_BYTES (TC_M * TC_KB * 2)
 #define TC_B_BYTES (TC_N * TC_KB * 2)
@@ -171,10 +173,100 @@ __device__ __forceinline__ bool ep_sync(TcShared* S, int lane) {
   return ok != 0;
 }
 
+// Column tiles of a segment [t0, t1) in the order the screen visits them:
+// outward from tile td (td, td+1, td-1, td+2, ...). For a frame set screened
+// against itself td is the tile holding the row tile's own frames, so a
+// row's threshold becomes tight early (trajectory neighbours are close in
+// time) and few later pairs pass it; otherwise td = t0 (plain order).
+__device__ __forceinline__ int tile_order(int i, int t0, int t1, int td) {
+  const int L = td - t0, Rn = t1 - 1 - td, m = min(L, Rn);
+  if (i == 0) return td;
+  if (i <= 2 * m) return (i & 1) ? td + (i + 1) / 2 : td - i / 2;
+  const int j = i - 2 * m;
+  return (Rn > L) ? td + m + j : td - m - j;
+}
+
+// Keep the Kp smallest of the n (<= TC_CAPG) keys in src (unsorted, in
+// src[0..Kp)) and return the largest kept value: a most-significant-digit
+// radix select over the 64-bit keys (8-bit digits, stopping as soon as the
+// digit bucket holding the Kp-th key is kept whole), then a ballot
+// compaction. hist: 256 ints of this warp's shared scratch.
+__device__ float warp_select_keep(uint64_t* src, int n, int Kp, int* hist, int lane) {
+  constexpr int PER = TC_CAPG / 32;
+  uint64_t kv[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int x = lane + 32 * i;
+    kv[i] = (x < n) ? src[x] : MDS_KEY_INF;
+  }
+  uint64_t prefix = 0, mask = 0;
+  int need = Kp;
+  for (int pass = 7; pass >= 0; --pass) {
+    const int sh = pass * 8;
+    for (int b = lane; b < 256; b += 32) hist[b] = 0;
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+      if ((kv[i] & mask) == prefix) atomicAdd(&hist[(int)((kv[i] >> sh) & 255u)], 1);
+    __syncwarp();
+    int c[8], loc = 0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      c[b] = hist[8 * lane + b];
+      loc += c[b];
+    }
+    int inc = loc;
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    const int exc = inc - loc;
+    int digit = -1, before = 0, cnt = 0;
+    if (exc < need && need <= inc) {
+      int acc = exc;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        if (digit < 0 && acc + c[b] >= need) {
+          digit = 8 * lane + b;
+          before = acc;
+          cnt = c[b];
+        }
+        acc += c[b];
+      }
+    }
+    const unsigned own = __ballot_sync(0xffffffffu, digit >= 0);
+    const int src_lane = __ffs(own) - 1;
+    digit = __shfl_sync(0xffffffffu, digit, src_lane);
+    before = __shfl_sync(0xffffffffu, before, src_lane);
+    cnt = __shfl_sync(0xffffffffu, cnt, src_lane);
+    __syncwarp();
+    need -= before;
+    prefix |= (uint64_t)digit << sh;
+    mask |= (uint64_t)255 << sh;
+    if (cnt == need) break;  // the whole bucket is kept
+  }
+  // keep every key whose processed digits are <= prefix's
+  int base = 0;
+  float vmax = 0.0f;
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const bool keep = kv[i] != MDS_KEY_INF && (kv[i] & mask) <= prefix;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (keep) {
+      src[base + __popc(bal & ((1u << lane) - 1u))] = kv[i];
+      vmax = fmaxf(vmax, mds_key_value(kv[i]));
+    }
+    base += __popc(bal);
+  }
+  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  __syncwarp();
+  return vmax;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
-            int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems,
+            int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
             uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
@@ -222,7 +314,9 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
         const int rt = item / nseg, seg = item % nseg;
         const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
-        for (int tile = t0; tile < t1 && ok; ++tile)
+        const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
+        for (int ti = 0; ti < t1 - t0 && ok; ++ti) {
+          const int tile = tile_order(ti, t0, t1, td);
           for (int kb = 0; kb < nkb; ++kb) {
             if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
             unsigned char* st = stages + stage * TC_STAGE_BYTES;
@@ -233,6 +327,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, &S->full[stage], Ap + kb * TC_KB, tile * TC_N);
             if (++stage == TC_STAGES) { stage = 0; phase ^= 1; }
           }
+        }
       }
       if (!ok) {
         atomicMax(err, 1);
@@ -288,7 +383,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     // ------------------------------------------------------------ epilogue
     const int ew = warp - 2;
     const int q = warp & 3;          // TMEM lane quarter of this warp
-    const int h = ew >> 2;           // column half
+    const int h = ew >> 2;           // column quarter: chunks [ci0, ci1) of the 10
+    const int ci0 = (h * 10) / 4, ci1 = ((h + 1) * 10) / 4;
     const int f = lane / 3, c = lane % 3;
     const int rloc = q * 10 + f;     // row within the 40-frame tile (f < 10)
     uint64_t* scratch = scratch_all + ew * TC_CAPG;
@@ -304,12 +400,14 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
       for (int i = 0; i < MDS_REC; ++i) rrec[i] = rowok ? __ldg(recf + (int64_t)grow * MDS_REC + i) : 0.f;
       // rows owned by this warp for resets and compaction: f = h, h+2, ...
-      if (lane < 5) {
-        int fr = h + 2 * lane;
+      if (lane < 3 && h + 4 * lane < 10) {
+        int fr = h + 4 * lane;
         S->cnt[q * 10 + fr] = 0;
         S->thr[q * 10 + fr] = INF;
       }
-      for (int tile = t0; tile < t1; ++tile, ++acc) {
+      const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
+      for (int ti = 0; ti < t1 - t0; ++ti, ++acc) {
+        const int tile = tile_order(ti, t0, t1, td);
         const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
         // column records of this tile
         for (int e = ew * 32 + lane; e < TC_FR_N * MDS_REC; e += TC_EPI_WARPS * 32) {
@@ -322,7 +420,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256;
         uint64_t* rowbuf = candbuf + ((int64_t)grow * nseg + seg) * TC_CAPG;
 #pragma unroll 1
-        for (int ci = h * 5; ci < h * 5 + 5; ++ci) {
+        for (int ci = ci0; ci < ci1; ++ci) {
           float vx[8], vy[8], vz[8];
           tmem_ld8(tq + 8 * ci, vx);
           tmem_ld8(tq + TC_FR_N + 8 * ci, vy);
@@ -382,7 +480,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         if (lane == 0) mbar_arrive(&S->tempty[b]);
         if (!ep_sync(S, lane)) { ok = false; break; }
         // compaction of this warp's rows
-        for (int fr = h; fr < 10; fr += 2) {
+        for (int fr = h; fr < 10; fr += 4) {
           const int r = q * 10 + fr;
           const int gr = rt * TC_FR_M + r;
           if (gr >= nfit) continue;
@@ -391,13 +489,10 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
           if (!need) continue;
           uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
           n = min(n, TC_CAPG);
-          for (int x = lane; x < n; x += 32) scratch[x] = src[x];
-          warp_bitonic_sort(scratch, n, TC_CAPG, lane);
-          for (int x = lane; x < Kp; x += 32) src[x] = scratch[x];
-          __syncwarp();
+          const float t = warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
           if (lane == 0) {
             S->cnt[r] = Kp;
-            S->thr[r] = mds_key_value(scratch[Kp - 1]);
+            S->thr[r] = t;
           }
           __syncwarp();
         }
@@ -405,7 +500,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       if (!ok) break;
       if (!ep_sync(S, lane)) { ok = false; break; }
       // final: sort and publish this warp's rows of the item
-      for (int fr = h; fr < 10; fr += 2) {
+      for (int fr = h; fr < 10; fr += 4) {
         const int r = q * 10 + fr;
         const int gr = rt * TC_FR_M + r;
         if (gr >= nfit) continue;
@@ -514,7 +609,7 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
   ctx->stats.launches++;
   k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
-                                                       cand, cand_n, e);
+                                                       &fit == &ref ? 1 : 0, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
   int herr = 0;

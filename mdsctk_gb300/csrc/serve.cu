@@ -174,7 +174,7 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
   MDS_CUDA(c, cudaMemsetAsync(sl.nflag.p, 0, sizeof(int), c->stream));
   MDS_TRY(launch_center(c, sl.raw.as<float>(), bucket, S->natoms, S->Ap, S->dmass.as<float>(), S->dswn.as<float>(),
                         S->tm, sl.Y.as<float>(), sl.E.as<double>()));
-  MDS_TRY(launch_prealign(c, sl.Y.as<float>(), sl.E.as<double>(), bucket, S->natoms, S->Ap, S->dmu.as<double>(),
+  MDS_TRY(launch_prealign(c, sl.Y.as<float>(), sl.E.as<double>(), bucket, S->natoms, S->Ap, S->dmu.as<float>(),
                           S->dM0.as<double>(), pl.nofit, sl.A.as<float>(), sl.R.as<float>()));
   int nseg;
   if (S->prec != MDS_PREC_FP32) {
@@ -465,13 +465,14 @@ static int build_model(mds_server* S, const float* hxyz, const float* hmass) {
   std::vector<double> mu;
   double M0[9];
   MDS_TRY(build_template(c, S->Y.as<float>(), Ap, natoms, (S->cfg.flags & MDS_NOFIT) != 0, mu, M0));
-  MDS_TRY(S->dmu.alloc(c, sizeof(double) * 3 * Ap));
+  MDS_TRY(S->dmu.alloc(c, sizeof(float) * 3 * Ap));
   MDS_TRY(S->dM0.alloc(c, sizeof(double) * 9));
-  MDS_CUDA(c, cudaMemcpyAsync(S->dmu.p, mu.data(), sizeof(double) * 3 * Ap, cudaMemcpyHostToDevice, s));
+  std::vector<float> muf(mu.begin(), mu.end());
+  MDS_CUDA(c, cudaMemcpyAsync(S->dmu.p, muf.data(), sizeof(float) * 3 * Ap, cudaMemcpyHostToDevice, s));
   MDS_CUDA(c, cudaMemcpyAsync(S->dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(S->A.alloc(c, sizeof(float) * 3 * (size_t)Ap * n));
   MDS_TRY(S->R.alloc(c, sizeof(float) * MDS_REC * (size_t)n));
-  MDS_TRY(launch_prealign(c, S->Y.as<float>(), S->E.as<double>(), n, natoms, Ap, S->dmu.as<double>(),
+  MDS_TRY(launch_prealign(c, S->Y.as<float>(), S->E.as<double>(), n, natoms, Ap, S->dmu.as<float>(),
                           S->dM0.as<double>(), (S->cfg.flags & MDS_NOFIT) ? 1 : 0, S->A.as<float>(),
                           S->R.as<float>()));
   if (S->prec != MDS_PREC_FP32) MDS_TRY(tc_prepare(c, S->plan(n), S->A.as<float>(), n, S->tc, 1));
