@@ -93,6 +93,10 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
 // pieces of the knn_rms pipeline (knn_rms.cu), reused by the serving loop
 int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass,
                   const float* dswn, float tm, float* Y, double* E);
+// Centring + superposition of n raw frames in one kernel: deviations and
+// records only (knn_rms.cu).
+int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
+                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R);
 int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const float* dmu,
                     const double* dM0, int nofit, float* A, float* R);
 int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit, std::vector<double>& mu,
@@ -100,8 +104,10 @@ int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofi
 int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* recf,
                        const float* recr, int nrows, const int* rowlist, int Kp, int nseg, uint64_t* cand,
                        int* cand_n);
-int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const double* Ef, const float* Yr,
-                   const double* Er, int nrows, const int* rowlist, int mode, const uint64_t* cand,
+// Exact recheck from the superposed deviations (Af/Ar [n][3][Ap]) and the
+// template mu [3][Ap] (knn_rms.cu).
+int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
+                   int nrows, const int* rowlist, int mode, const uint64_t* cand,
                    const int* cand_n, int nseg, int segstride, int Kp, int k, double* out_d, int* out_i,
                    int* flagged, int* nflag);
 int choose_nseg_fp32(int nfit, int num_sms, int nref);

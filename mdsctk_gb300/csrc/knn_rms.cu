@@ -177,6 +177,98 @@ __global__ void k_prealign(const float* __restrict__ Y, const double* __restrict
   }
 }
 
+// Centring and superposition in one kernel (one block per frame): the
+// centred, mass-scaled coordinates y = (x - com) sqrt(w/M) are recomputed from
+// the raw frame (L1-resident) in each of three passes -- centre of mass;
+// covariance with the template and |y|^2; deviations a = R y - mu with the
+// record sums -- so only the deviations and records are written. Arithmetic
+// as k_center and k_prealign.
+__global__ void k_prep(const float* __restrict__ raw, int n, int natoms, int Ap, const float* __restrict__ mass,
+                       const float* __restrict__ swn, float tm, const float* __restrict__ mu,
+                       const double* __restrict__ M0, int nofit, float* __restrict__ dev,
+                       float* __restrict__ rec) {
+  __shared__ double red[32 * 10];
+  __shared__ float Rsh[9];
+  const int f = blockIdx.x;
+  if (f >= n) return;
+  const float* x = raw + (int64_t)f * natoms * 3;
+  float com[3];
+  {
+    float p[3] = {0.f, 0.f, 0.f};
+    for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
+      const float mm = mass[a];
+      for (int c = 0; c < 3; ++c) p[c] = fmaf(mm, x[3 * a + c], p[c]);
+    }
+    double sc[3] = {p[0], p[1], p[2]};
+    block_sum_vec<3>(sc, red);
+    for (int c = 0; c < 3; ++c) com[c] = (float)(sc[c] / (double)tm);
+  }
+  if (!nofit) {
+    float p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // |y|^2, sum y mu^T
+    for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
+      const float w = swn[a];
+      float yc[3], mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
+      for (int c = 0; c < 3; ++c) yc[c] = (x[3 * a + c] - com[c]) * w;
+      p[0] = fmaf(yc[0], yc[0], fmaf(yc[1], yc[1], fmaf(yc[2], yc[2], p[0])));
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) p[1 + 3 * c + d] = fmaf(yc[c], mc[d], p[1 + 3 * c + d]);
+    }
+    double sv[10];
+    for (int i = 0; i < 10; ++i) sv[i] = p[i];
+    block_sum_vec<10>(sv, red);
+    if (threadIdx.x == 0) {
+      double R[9];
+      qcp_rotation_fp64(sv + 1, 0.5 * (sv[0] + M0[0] + M0[4] + M0[8]), R);
+      for (int i = 0; i < 9; ++i) Rsh[i] = (float)R[i];
+    }
+  } else if (threadIdx.x == 0) {
+    for (int i = 0; i < 9; ++i) Rsh[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+  }
+  __syncthreads();
+  float R[9];
+  for (int i = 0; i < 9; ++i) R[i] = Rsh[i];
+  float ea = 0.f, u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float* o = dev + (int64_t)f * 3 * Ap;
+  for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
+    if (a < natoms) {
+      const float w = swn[a];
+      float yc[3], mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]}, av[3];
+      for (int c = 0; c < 3; ++c) yc[c] = (x[3 * a + c] - com[c]) * w;
+      for (int c = 0; c < 3; ++c) {
+        const float ry = fmaf(R[3 * c], yc[0], fmaf(R[3 * c + 1], yc[1], R[3 * c + 2] * yc[2]));
+        av[c] = ry - mc[c];
+        o[c * Ap + a] = av[c];
+      }
+      for (int c = 0; c < 3; ++c) {
+        ea = fmaf(av[c], av[c], ea);
+        for (int d = 0; d < 3; ++d) u[3 * c + d] = fmaf(av[c], mc[d], u[3 * c + d]);
+      }
+    } else {
+      for (int c = 0; c < 3; ++c) o[c * Ap + a] = 0.0f;
+    }
+  }
+  double eu[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
+  block_sum_vec<10>(eu, red);
+  if (threadIdx.x == 0) {
+    const double* U = eu + 1;
+    float* r = rec + (int64_t)f * MDS_REC;
+    double sxx = U[0], syy = U[4], szz = U[8];
+    double sxy = 0.5 * (U[1] + U[3]), sxz = 0.5 * (U[2] + U[6]), syz = 0.5 * (U[5] + U[7]);
+    r[0] = (float)(M0[0] + sxx);
+    r[1] = (float)(M0[4] + syy);
+    r[2] = (float)(M0[8] + szz);
+    r[3] = (float)(0.5 * (M0[1] + M0[3]) + sxy);
+    r[4] = (float)(0.5 * (M0[2] + M0[6]) + sxz);
+    r[5] = (float)(0.5 * (M0[5] + M0[7]) + syz);
+    r[6] = (float)sxx; r[7] = (float)syy; r[8] = (float)szz;
+    r[9] = (float)sxy; r[10] = (float)sxz; r[11] = (float)syz;
+    r[12] = (float)(U[5] - U[7]);
+    r[13] = (float)(U[6] - U[2]);
+    r[14] = (float)(U[1] - U[3]);
+    r[15] = (float)eu[0];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // 3. FP32 CUDA-core screen: tile of 32 fit x 64 ref frames per step, each
 //    thread owns 2 x 4 pairs (72 accumulators), atoms staged through shared
@@ -385,54 +477,47 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
 // Exact RMSD (nm) of fit frame (in shared memory) vs reference frame j for a
 // chunk of candidates: covariance per warp, FP64 rotation per thread, then
 // the RMSD of the rotated fit frame against the reference frame.
-__device__ void recheck_chunk(const float* __restrict__ sfit, double Ef, const float* __restrict__ Yr,
-                              const double* __restrict__ Er, int Ap, int natoms, const int* cj, int nc,
-                              bool nofit, float* sS, float* sR, float* sd) {
+// Exact RMSD of the fit frame against nc reference frames cj[], one warp per
+// pair, in one pass over the atoms. With x~ = mu + a the superposed copies
+// (rigid copies of the frames) and d = a_i - a_j = x~_i - x~_j:
+//   D = sum |d|^2,  S = sum x~_i x~_j^T = C_i - P,  P = sum x~_i d^T,
+// C_i = sum x~_i x~_i^T (per row, precomputed). D is a sum of positive
+// terms, and P's antisymmetric part (the small vector b of the key matrix)
+// is formed from the small d, so FP32 keeps them accurate; RMSD^2 = D - 2 nu
+// (qcp.cuh: shifted_rmsd2_f32). sa = a_i, sx = x~_i (shared memory), C6 =
+// (Cxx, Cyy, Czz, Cxy, Cxz, Cyz).
+__device__ void recheck_chunk(const float* __restrict__ sa, const float* __restrict__ sx, const float* C6,
+                              const float* __restrict__ Ar, int Ap, int natoms, const int* cj, int nc, bool nofit,
+                              float* sd) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (!nofit) {
-    for (int c = warp; c < nc; c += nw) {
-      const float* y = Yr + (int64_t)cj[c] * 3 * Ap;
-      float s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-      for (int a = lane; a < natoms; a += 32) {
-        float x0 = sfit[a], x1 = sfit[Ap + a], x2 = sfit[2 * Ap + a];
-        float y0 = __ldg(y + a), y1 = __ldg(y + Ap + a), y2 = __ldg(y + 2 * Ap + a);
-        s[0] = fmaf(x0, y0, s[0]); s[1] = fmaf(x0, y1, s[1]); s[2] = fmaf(x0, y2, s[2]);
-        s[3] = fmaf(x1, y0, s[3]); s[4] = fmaf(x1, y1, s[4]); s[5] = fmaf(x1, y2, s[5]);
-        s[6] = fmaf(x2, y0, s[6]); s[7] = fmaf(x2, y1, s[7]); s[8] = fmaf(x2, y2, s[8]);
-      }
-      for (int i = 0; i < 9; ++i) {
-        float v = s[i];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) sS[c * 9 + i] = v;
-      }
-    }
-    __syncthreads();
-    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-      double S[9], R[9];
-      for (int i = 0; i < 9; ++i) S[i] = sS[c * 9 + i];
-      qcp_rotation_fp64(S, 0.5 * (Ef + Er[cj[c]]), R);
-      for (int i = 0; i < 9; ++i) sR[c * 9 + i] = (float)R[i];
-    }
-    __syncthreads();
-  }
   for (int c = warp; c < nc; c += nw) {
-    const float* y = Yr + (int64_t)cj[c] * 3 * Ap;
-    float R[9];
-    for (int i = 0; i < 9; ++i) R[i] = nofit ? ((i % 4 == 0) ? 1.f : 0.f) : sR[c * 9 + i];
-    float acc = 0.f;
+    const float* aj = Ar + (int64_t)cj[c] * 3 * Ap;
+    float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // D, P[9]
     for (int a = lane; a < natoms; a += 32) {
-      float x0 = sfit[a], x1 = sfit[Ap + a], x2 = sfit[2 * Ap + a];
-      float y0 = __ldg(y + a), y1 = __ldg(y + Ap + a), y2 = __ldg(y + 2 * Ap + a);
-      float d0 = fmaf(R[0], x0, fmaf(R[1], x1, fmaf(R[2], x2, -y0)));
-      float d1 = fmaf(R[3], x0, fmaf(R[4], x1, fmaf(R[5], x2, -y1)));
-      float d2 = fmaf(R[6], x0, fmaf(R[7], x1, fmaf(R[8], x2, -y2)));
-      acc = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, acc)));
+      const float d0 = sa[a] - __ldg(aj + a);
+      const float d1 = sa[Ap + a] - __ldg(aj + Ap + a);
+      const float d2 = sa[2 * Ap + a] - __ldg(aj + 2 * Ap + a);
+      v[0] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, v[0])));
+      if (!nofit) {
+        const float x0 = sx[a], x1 = sx[Ap + a], x2 = sx[2 * Ap + a];
+        v[1] = fmaf(x0, d0, v[1]); v[2] = fmaf(x0, d1, v[2]); v[3] = fmaf(x0, d2, v[3]);
+        v[4] = fmaf(x1, d0, v[4]); v[5] = fmaf(x1, d1, v[5]); v[6] = fmaf(x1, d2, v[6]);
+        v[7] = fmaf(x2, d0, v[7]); v[8] = fmaf(x2, d1, v[8]); v[9] = fmaf(x2, d2, v[9]);
+      }
     }
-    // FP32 tree over the lanes (rmsdev accumulates in float as well; FP64
-    // issues at a small fraction of the FP32 rate here)
-    float v = acc;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sd[c] = sqrtf(v);
+#pragma unroll
+    for (int i = 0; i < 10; ++i)
+      for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    if (lane == 0) {
+      float r2 = v[0];
+      if (!nofit) {
+        const float* P = v + 1;  // P[3r+s] = sum x~_r d_s
+        r2 = shifted_rmsd2_f32(v[0], C6[0] - P[0], C6[1] - P[4], C6[2] - P[8], 2.0f * C6[3] - (P[1] + P[3]),
+                               2.0f * C6[4] - (P[2] + P[6]), 2.0f * C6[5] - (P[5] + P[7]), P[7] - P[5],
+                               P[2] - P[6], P[3] - P[1]);
+      }
+      sd[c] = sqrtf(fmaxf(r2, 0.0f));
+    }
   }
   __syncthreads();
 }
@@ -442,26 +527,41 @@ __device__ void recheck_chunk(const float* __restrict__ sfit, double Ef, const f
 // (exact row). mode 2 (full matrix): write every exact distance in reference
 // order. Output: out_d/out_i rows of width `width` at row index grow.
 __global__ void __launch_bounds__(RC_THREADS)
-k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const float* __restrict__ Yr,
-          const double* __restrict__ Er, int nrows, const int* __restrict__ rowlist, int Nr, int Ap,
-          int natoms, int nofit, int mode, const uint64_t* __restrict__ cand,
-          const int* __restrict__ cand_n, int nseg, int segstride, int Kp, int k, double* __restrict__ out_d,
-          int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag) {
+k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const float* __restrict__ mu, int nrows,
+          const int* __restrict__ rowlist, int Nr, int Ap, int natoms, int nofit, int mode,
+          const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int segstride, int Kp, int k,
+          double* __restrict__ out_d, int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* sfit = reinterpret_cast<float*>(smem_raw);               // [3*Ap]
-  float* sS = sfit + 3 * Ap;                                      // [CHUNK*9]
-  float* sR = sS + RC_CHUNK * 9;                                  // [CHUNK*9]
-  float* sd = sR + RC_CHUNK * 9;                                  // [CHUNK]
+  float* sa = reinterpret_cast<float*>(smem_raw);                 // [3*Ap] a_i
+  float* sx = sa + 3 * Ap;                                        // [3*Ap] mu + a_i
+  float* sd = sx + 3 * Ap;                                        // [CHUNK]
   int* cj = reinterpret_cast<int*>(sd + RC_CHUNK);                // [CHUNK]
   uint64_t* keys = reinterpret_cast<uint64_t*>(cj + RC_CHUNK);    // merge buffer / top list
   __shared__ int s_total;
+  __shared__ double s_red[32 * 6];
+  __shared__ float C6[6];
 
   int lr = blockIdx.x;
   if (lr >= nrows) return;
   int grow = rowlist ? rowlist[lr] : lr;
-  const float* yf = Yf + (int64_t)grow * 3 * Ap;
-  for (int e = threadIdx.x; e < 3 * Ap; e += blockDim.x) sfit[e] = yf[e];
-  const double ef = Ef[grow];
+  const float* af = Af + (int64_t)grow * 3 * Ap;
+  for (int e = threadIdx.x; e < 3 * Ap; e += blockDim.x) {
+    const float av = af[e];
+    sa[e] = av;
+    sx[e] = mu[e] + av;
+  }
+  {
+    float p[6] = {0, 0, 0, 0, 0, 0};
+    for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
+      const float x0 = mu[a] + af[a], x1 = mu[Ap + a] + af[Ap + a], x2 = mu[2 * Ap + a] + af[2 * Ap + a];
+      p[0] = fmaf(x0, x0, p[0]); p[1] = fmaf(x1, x1, p[1]); p[2] = fmaf(x2, x2, p[2]);
+      p[3] = fmaf(x0, x1, p[3]); p[4] = fmaf(x0, x2, p[4]); p[5] = fmaf(x1, x2, p[5]);
+    }
+    double c[6] = {p[0], p[1], p[2], p[3], p[4], p[5]};
+    block_sum_vec<6>(c, s_red);
+    if (threadIdx.x < 6) C6[threadIdx.x] = (float)c[threadIdx.x];
+    __syncthreads();
+  }
   const int k1 = k + 1;
 
   if (mode == 2) {
@@ -470,7 +570,7 @@ k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const flo
       int nc = min(RC_CHUNK, Nr - base);
       for (int c = threadIdx.x; c < nc; c += blockDim.x) cj[c] = base + c;
       __syncthreads();
-      recheck_chunk(sfit, ef, Yr, Er, Ap, natoms, cj, nc, nofit, sS, sR, sd);
+      recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd);
       for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         out_d[(int64_t)grow * Nr + base + c] = (double)sd[c] * 10.0;
         out_i[(int64_t)grow * Nr + base + c] = base + c;
@@ -530,7 +630,7 @@ k_recheck(const float* __restrict__ Yf, const double* __restrict__ Ef, const flo
     for (int c = threadIdx.x; c < nc; c += blockDim.x)
       cj[c] = (mode == 0) ? mds_key_index(keys[base + c]) : base + c;
     __syncthreads();
-    recheck_chunk(sfit, ef, Yr, Er, Ap, natoms, cj, nc, nofit, sS, sR, sd);
+    recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd);
     // place the chunk after the current k1 best and re-sort
     for (int c = threadIdx.x; c < RC_CHUNK; c += blockDim.x)
       top[k1 + c] = (c < nc) ? mds_pack_key(sd[c], cj[c]) : MDS_KEY_INF;
@@ -576,8 +676,7 @@ size_t recheck_smem(int Ap, int Kp, int k, int mode) {
     merge = (size_t)std::max(Kp, 1);
   }
   size_t keys = std::max(merge + TP2, (size_t)0);
-  return sizeof(float) * (3 * Ap + 2 * RC_CHUNK * 9 + RC_CHUNK) + sizeof(int) * RC_CHUNK +
-         sizeof(uint64_t) * keys;
+  return sizeof(float) * (6 * Ap + RC_CHUNK) + sizeof(int) * RC_CHUNK + sizeof(uint64_t) * keys;
 }
 
 // ---------------------------------------------------------------------------
@@ -655,8 +754,8 @@ int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofi
   return MDS_OK;
 }
 
-int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const double* Ef,
-                   const float* Yr, const double* Er, int nrows, const int* rowlist, int mode,
+int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
+                   int nrows, const int* rowlist, int mode,
                    const uint64_t* cand, const int* cand_n, int nseg, int segstride, int Kp, int k,
                    double* out_d, int* out_i, int* flagged, int* nflag) {
   size_t smem = recheck_smem(pl.Ap, Kp, k, mode);
@@ -666,8 +765,7 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const do
     int TP2 = 1;
     while (TP2 < k + 1 + RC_CHUNK) TP2 <<= 1;
     size_t keys = std::max((size_t)P2, (size_t)Kp + TP2);
-    smem = sizeof(float) * (3 * pl.Ap + 2 * RC_CHUNK * 9 + RC_CHUNK) + sizeof(int) * RC_CHUNK +
-           sizeof(uint64_t) * keys;
+    smem = sizeof(float) * (6 * pl.Ap + RC_CHUNK) + sizeof(int) * RC_CHUNK + sizeof(uint64_t) * keys;
   }
   if (smem > 227 * 1024)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck needs %zu bytes of shared memory (natoms/k too large)", smem);
@@ -677,9 +775,9 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Yf, const do
   if (smem > limit) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck shared memory %zu > %zu", smem, limit);
   if (nrows > 0) ctx->stats.launches++;
   if (nrows > 0)
-    k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Yf, Ef, Yr, Er, nrows, rowlist, pl.nref, pl.Ap,
-                                                        pl.natoms, pl.nofit, mode, cand, cand_n, nseg,
-                                                        segstride, Kp, k, out_d, out_i, flagged, nflag);
+    k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Af, Ar, mu, nrows, rowlist, pl.nref, pl.Ap, pl.natoms,
+                                                        pl.nofit, mode, cand, cand_n, nseg, segstride, Kp, k,
+                                                        out_d, out_i, flagged, nflag);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
@@ -699,6 +797,15 @@ int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int na
   if (n <= 0) return MDS_OK;
   ctx->stats.launches++;
   k_prealign<<<n, 128, 0, ctx->stream>>>(Y, E, n, natoms, Ap, dmu, dM0, nofit, A, R);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
+                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R) {
+  if (n <= 0) return MDS_OK;
+  ctx->stats.launches++;
+  k_prep<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dmass, dswn, tm, dmu, dM0, nofit, A, R);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
@@ -757,50 +864,26 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
 
   const bool same = (draw_fit == nullptr);
   const int nref = pl.nref, nfit = same ? nref : pl.nfit;
-  DevBuf Yr(ctx), Er(ctx), Yf(ctx), Ef(ctx);
-  MDS_TRY(Yr.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
-  MDS_TRY(Er.alloc(ctx, sizeof(double) * nref));
+  // the first reference frame, centred, defines the template
+  DevBuf Y0(ctx), E0(ctx);
+  MDS_TRY(Y0.alloc(ctx, sizeof(float) * 3 * Ap));
+  MDS_TRY(E0.alloc(ctx, sizeof(double)));
   st.launches = 0;
   st.launches++;
-  k_center<<<nref, 128, 0, s>>>(draw_ref, nref, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
-                                 Yr.as<float>(), Er.as<double>());
+  k_center<<<1, 128, 0, s>>>(draw_ref, 1, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm, Y0.as<float>(),
+                             E0.as<double>());
   MDS_CUDA(ctx, cudaGetLastError());
-  const float* Yfp = Yr.as<float>();
-  const double* Efp = Er.as<double>();
-  if (!same) {
-    MDS_TRY(Yf.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
-    MDS_TRY(Ef.alloc(ctx, sizeof(double) * nfit));
-    st.launches++;
-    k_center<<<nfit, 128, 0, s>>>(draw_fit, nfit, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
-                                   Yf.as<float>(), Ef.as<double>());
-    MDS_CUDA(ctx, cudaGetLastError());
-    Yfp = Yf.as<float>();
-    Efp = Ef.as<double>();
-  }
 
   const int k = pl.k;
   DevBuf flagged(ctx), nflag(ctx);
   MDS_TRY(flagged.alloc(ctx, sizeof(int) * (size_t)std::max(nfit, 1)));
   MDS_TRY(nflag.alloc(ctx, sizeof(int)));
 
-  if (pl.full) {
-    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
-    MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), nfit, nullptr, 2,
-                           nullptr, nullptr, 1, 1, 1, 0, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
-    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
-    MDS_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
-    st.recheck_ms = ms;
-    st.passes = 0;
-    return MDS_OK;
-  }
-
   // template and superposition
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   std::vector<double> mu;
   double M0[9];
-  MDS_TRY(build_template(ctx, Yr.as<float>(), Ap, natoms, pl.nofit != 0, mu, M0));
+  MDS_TRY(build_template(ctx, Y0.as<float>(), Ap, natoms, pl.nofit != 0, mu, M0));
   DevBuf dmu(ctx), dM0(ctx), Ar(ctx), Rr(ctx), Af(ctx), Rf(ctx);
   std::vector<float> muf(mu.begin(), mu.end());
   MDS_TRY(dmu.alloc(ctx, sizeof(float) * 3 * Ap));
@@ -809,19 +892,15 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_CUDA(ctx, cudaMemcpyAsync(dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(Ar.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
   MDS_TRY(Rr.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nref));
-  st.launches++;
-  k_prealign<<<nref, 128, 0, s>>>(Yr.as<float>(), Er.as<double>(), nref, natoms, Ap, dmu.as<float>(),
-                                   dM0.as<double>(), pl.nofit, Ar.as<float>(), Rr.as<float>());
-  MDS_CUDA(ctx, cudaGetLastError());
+  MDS_TRY(launch_prep(ctx, draw_ref, nref, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm, dmu.as<float>(),
+                      dM0.as<double>(), pl.nofit, Ar.as<float>(), Rr.as<float>()));
   const float* Afp = Ar.as<float>();
   const float* Rfp = Rr.as<float>();
   if (!same) {
     MDS_TRY(Af.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
     MDS_TRY(Rf.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nfit));
-    st.launches++;
-    k_prealign<<<nfit, 128, 0, s>>>(Yfp, Efp, nfit, natoms, Ap, dmu.as<float>(), dM0.as<double>(),
-                                     pl.nofit, Af.as<float>(), Rf.as<float>());
-    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_TRY(launch_prep(ctx, draw_fit, nfit, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
+                        dmu.as<float>(), dM0.as<double>(), pl.nofit, Af.as<float>(), Rf.as<float>()));
     Afp = Af.as<float>();
     Rfp = Rf.as<float>();
   }
@@ -831,6 +910,18 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_CUDA(ctx, cudaMemcpyAsync(pl.prep_rec, Rr.p, sizeof(float) * MDS_REC * (size_t)nref,
                                   cudaMemcpyDeviceToHost, s));
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    return MDS_OK;
+  }
+  if (pl.full) {
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+    MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), nfit, nullptr, 2, nullptr, nullptr, 1, 1,
+                           1, 0, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    MDS_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    st.recheck_ms = ms;
+    st.passes = 0;
     return MDS_OK;
   }
   // tensor-core operands (split hi/lo), when that screen is selected
@@ -873,9 +964,9 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.kprime = Kp;
     return MDS_OK;
   }
-  MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), nfit, nullptr, 0,
-                         cand.as<uint64_t>(), cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i,
-                         flagged.as<int>(), nflag.as<int>()));
+  MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), nfit, nullptr, 0, cand.as<uint64_t>(),
+                         cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i, flagged.as<int>(),
+                         nflag.as<int>()));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0;
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -904,8 +995,8 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.passes++;
     if (Kp >= nref || st.passes > 3) {
       // exact rows: every reference is a candidate
-      MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), hflag, rows.as<int>(), 1,
-                             nullptr, nullptr, 1, 1, 1, k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
+      MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), hflag, rows.as<int>(), 1, nullptr,
+                             nullptr, 1, 1, 1, k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
       break;
     }
@@ -916,7 +1007,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)hflag * nseg2));
     MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), hflag, rows.as<int>(), Kp,
                                nseg2, cand.as<uint64_t>(), cand_n.as<int>()));
-    MDS_TRY(launch_recheck(ctx, pl, Yfp, Efp, Yr.as<float>(), Er.as<double>(), hflag, rows.as<int>(), 0,
+    MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), hflag, rows.as<int>(), 0,
                            cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, Kp, k, dout_d, dout_i,
                            flagged.as<int>(), nflag.as<int>()));
     MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -216,3 +216,39 @@ __device__ __forceinline__ float screen_shifted_f32(const float* G, const float*
   }
   return fmaxf(D - 2.0f * nu - guard, 0.0f);
 }
+
+// Exact RMSD^2 (per unit mass) of a frame pair from the shifted key matrix:
+// RMSD^2 = D - 2 nu, nu the largest eigenvalue of K - tr(S) I, whose lower
+// right block is D' = [[-2(Syy+Szz), Sxy2, Sxz2], [Sxy2, -2(Sxx+Szz), Syz2],
+// [Sxz2, Syz2, -2(Sxx+Syy)]] (Sab2 = Sab + Sba) and whose first row is
+// (0, b). nu is found by Newton from D/2 (an upper bound) to convergence.
+// Every input is well scaled (D = |x_i - x_j|^2 directly, b and D' at the
+// scale of S), so FP32 gives nu, and hence RMSD^2, to ~1e-6 relative.
+__device__ __forceinline__ float shifted_rmsd2_f32(float D, float Sxx, float Syy, float Szz, float Sxy2, float Sxz2,
+                                                   float Syz2, float b0, float b1, float b2) {
+  const float d00 = -2.0f * (Syy + Szz), d11 = -2.0f * (Sxx + Szz), d22 = -2.0f * (Sxx + Syy);
+  const float d01 = Sxy2, d02 = Sxz2, d12 = Syz2;
+  const float beta0 = b0 * b0 + b1 * b1 + b2 * b2;
+  const float a00 = d11 * d22 - d12 * d12, a11 = d00 * d22 - d02 * d02, a22 = d00 * d11 - d01 * d01;
+  const float a01 = d02 * d12 - d01 * d22, a02 = d01 * d12 - d02 * d11, a12 = d01 * d02 - d00 * d12;
+  const float t = d00 + d11 + d22;
+  const float m2 = a00 + a11 + a22;
+  const float det = d00 * a00 + d01 * a01 + d02 * a02;
+  const float Db0 = d00 * b0 + d01 * b1 + d02 * b2;
+  const float Db1 = d01 * b0 + d11 * b1 + d12 * b2;
+  const float Db2 = d02 * b0 + d12 * b1 + d22 * b2;
+  const float beta1 = b0 * Db0 + b1 * Db1 + b2 * Db2;
+  const float badjb = b0 * (a00 * b0 + a01 * b1 + a02 * b2) + b1 * (a01 * b0 + a11 * b1 + a12 * b2) +
+                      b2 * (a02 * b0 + a12 * b1 + a22 * b2);
+  const float k3 = -t, k2 = m2 - beta0, k1 = -(det + beta1 - t * beta0), k0 = -badjb;
+  float nu = 0.5f * fmaxf(D, 0.0f);
+  for (int it = 0; it < 40; ++it) {
+    const float qv = (((nu + k3) * nu + k2) * nu + k1) * nu + k0;
+    const float qd = ((4.0f * nu + 3.0f * k3) * nu + 2.0f * k2) * nu + k1;
+    const float step = (qd > 0.0f) ? qv / qd : 0.0f;
+    if (!(step > 1e-8f * nu)) break;  // converged (or at the rounding floor)
+    nu = fmaxf(nu - step, 0.0f);
+  }
+  return D - 2.0f * nu;
+}
+

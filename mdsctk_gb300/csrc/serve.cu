@@ -99,7 +99,7 @@ struct Request {
 struct Slot {
   mds_ctx* ctx = nullptr;
   int cap = 0;
-  DevBuf raw, Y, E, A, R, cand, cand_n, out_d, out_i, flagged, nflag, derr, ext;
+  DevBuf raw, A, R, cand, cand_n, out_d, out_i, flagged, nflag, derr, ext;
   TcOperands tcq;
   float* h_raw = nullptr;
   double* h_d = nullptr;
@@ -172,10 +172,8 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
   mds_ctx* c = sl.ctx;
   KnnRmsPlan pl = S->plan(bucket);
   MDS_CUDA(c, cudaMemsetAsync(sl.nflag.p, 0, sizeof(int), c->stream));
-  MDS_TRY(launch_center(c, sl.raw.as<float>(), bucket, S->natoms, S->Ap, S->dmass.as<float>(), S->dswn.as<float>(),
-                        S->tm, sl.Y.as<float>(), sl.E.as<double>()));
-  MDS_TRY(launch_prealign(c, sl.Y.as<float>(), sl.E.as<double>(), bucket, S->natoms, S->Ap, S->dmu.as<float>(),
-                          S->dM0.as<double>(), pl.nofit, sl.A.as<float>(), sl.R.as<float>()));
+  MDS_TRY(launch_prep(c, sl.raw.as<float>(), bucket, S->natoms, S->Ap, S->dmass.as<float>(), S->dswn.as<float>(),
+                      S->tm, S->dmu.as<float>(), S->dM0.as<double>(), pl.nofit, sl.A.as<float>(), sl.R.as<float>()));
   int nseg;
   if (S->prec != MDS_PREC_FP32) {
     nseg = std::min(tc_choose_nseg(c, pl, bucket), S->nseg_max);
@@ -189,7 +187,7 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
                                nullptr, S->Kp, nseg, sl.cand.as<uint64_t>(), sl.cand_n.as<int>()));
   }
   const int segstride = (S->prec == MDS_PREC_FP32) ? S->Kp : tc_seg_stride();
-  MDS_TRY(launch_recheck(c, pl, sl.Y.as<float>(), sl.E.as<double>(), S->Y.as<float>(), S->E.as<double>(), bucket,
+  MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), bucket,
                          nullptr, 0, sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), nseg, segstride, S->Kp, S->k,
                          sl.out_d.as<double>(), sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>()));
   c->stats.launches++;
@@ -240,7 +238,7 @@ static int finish_batch(mds_server* S, Slot& sl) {
     MDS_CUDA(c, cudaMemsetAsync(sl.nflag.p, 0, sizeof(int), c->stream));
     MDS_TRY(launch_screen_fp32(c, pl, sl.A.as<float>(), S->A.as<float>(), sl.R.as<float>(), S->R.as<float>(), h,
                                drows.as<int>(), Kp, nseg2, cand.as<uint64_t>(), cand_n.as<int>()));
-    MDS_TRY(launch_recheck(c, pl, sl.Y.as<float>(), sl.E.as<double>(), S->Y.as<float>(), S->E.as<double>(), h,
+    MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), h,
                            drows.as<int>(), 0, cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, Kp, S->k,
                            sl.out_d.as<double>(), sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>()));
     MDS_CUDA(c, cudaMemcpyAsync(&nflag, sl.nflag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -253,7 +251,7 @@ static int finish_batch(mds_server* S, Slot& sl) {
     }
   }
   if (nflag > 0)
-    MDS_TRY(launch_recheck(c, pl, sl.Y.as<float>(), sl.E.as<double>(), S->Y.as<float>(), S->E.as<double>(), nflag,
+    MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), nflag,
                            drows.as<int>(), 1, nullptr, nullptr, 1, 1, 1, S->k, sl.out_d.as<double>(),
                            sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>()));
   k_serve_ext<<<(sl.bucket + 127) / 128, 128, 0, c->stream>>>(
@@ -402,7 +400,7 @@ static size_t slot_bytes(const mds_server* S, int cap) {
   size_t ap = S->Ap;
   size_t b = 0;
   b += (size_t)cap * S->natoms * 3 * 4;                     // raw
-  b += 2 * (size_t)cap * 3 * ap * 4 + (size_t)cap * (8 + 64);  // Y, A, E, R
+  b += (size_t)cap * 3 * ap * 4 + (size_t)cap * 64;            // A, R
   b += ((size_t)cap / 40 + 1) * 128 * 2 * ap * 2;            // split operands
   b += (size_t)cap * S->nseg_max * S->segstride * 8 + (size_t)cap * S->nseg_max * 4;
   b += (size_t)cap * S->k * 12 + (size_t)cap * S->nev * 8 + (size_t)cap * 4;
@@ -458,9 +456,9 @@ static int build_model(mds_server* S, const float* hxyz, const float* hmass) {
   MDS_TRY(S->dlam.alloc(c, sizeof(double) * S->nev));
   MDS_CUDA(c, cudaMemcpyAsync(S->dlam.p, S->evals.data(), sizeof(double) * S->nev, cudaMemcpyHostToDevice, s));
   // resident prepared landmarks for the query screen and recheck
-  MDS_TRY(S->Y.alloc(c, sizeof(float) * 3 * (size_t)Ap * n));
-  MDS_TRY(S->E.alloc(c, sizeof(double) * n));
-  MDS_TRY(launch_center(c, raw.as<float>(), n, natoms, Ap, S->dmass.as<float>(), S->dswn.as<float>(), tm,
+  MDS_TRY(S->Y.alloc(c, sizeof(float) * 3 * (size_t)Ap));  // the first landmark, centred: the template
+  MDS_TRY(S->E.alloc(c, sizeof(double)));
+  MDS_TRY(launch_center(c, raw.as<float>(), 1, natoms, Ap, S->dmass.as<float>(), S->dswn.as<float>(), tm,
                         S->Y.as<float>(), S->E.as<double>()));
   std::vector<double> mu;
   double M0[9];
@@ -472,9 +470,9 @@ static int build_model(mds_server* S, const float* hxyz, const float* hmass) {
   MDS_CUDA(c, cudaMemcpyAsync(S->dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(S->A.alloc(c, sizeof(float) * 3 * (size_t)Ap * n));
   MDS_TRY(S->R.alloc(c, sizeof(float) * MDS_REC * (size_t)n));
-  MDS_TRY(launch_prealign(c, S->Y.as<float>(), S->E.as<double>(), n, natoms, Ap, S->dmu.as<float>(),
-                          S->dM0.as<double>(), (S->cfg.flags & MDS_NOFIT) ? 1 : 0, S->A.as<float>(),
-                          S->R.as<float>()));
+  MDS_TRY(launch_prep(c, raw.as<float>(), n, natoms, Ap, S->dmass.as<float>(), S->dswn.as<float>(), tm,
+                      S->dmu.as<float>(), S->dM0.as<double>(), (S->cfg.flags & MDS_NOFIT) ? 1 : 0, S->A.as<float>(),
+                      S->R.as<float>()));
   if (S->prec != MDS_PREC_FP32) MDS_TRY(tc_prepare(c, S->plan(n), S->A.as<float>(), n, S->tc, 1));
   MDS_CUDA(c, cudaStreamSynchronize(s));
   return MDS_OK;
@@ -519,8 +517,8 @@ extern "C" int mds_server_create(const mds_server_config* cfg, const float* land
     sl.cap = cap;
     mds_ctx* c = sl.ctx;
     const size_t fr = (size_t)natoms * 3;
-    bool ok = sl.raw.alloc(c, sizeof(float) * fr * cap) == MDS_OK && sl.Y.alloc(c, sizeof(float) * 3 * S->Ap * cap) == MDS_OK &&
-              sl.E.alloc(c, sizeof(double) * cap) == MDS_OK && sl.A.alloc(c, sizeof(float) * 3 * S->Ap * cap) == MDS_OK &&
+    bool ok = sl.raw.alloc(c, sizeof(float) * fr * cap) == MDS_OK &&
+              sl.A.alloc(c, sizeof(float) * 3 * S->Ap * cap) == MDS_OK &&
               sl.R.alloc(c, sizeof(float) * MDS_REC * cap) == MDS_OK &&
               sl.cand.alloc(c, sizeof(uint64_t) * (size_t)cap * S->nseg_max * S->segstride) == MDS_OK &&
               sl.cand_n.alloc(c, sizeof(int) * (size_t)cap * S->nseg_max) == MDS_OK &&
@@ -565,7 +563,7 @@ extern "C" int mds_server_destroy(mds_server* S) {
     cudaFreeHost(sl.h_ext);
     cudaFreeHost(sl.h_small);
     // buffers return to the slot context's cache, then the context frees them
-    sl.raw.release(); sl.Y.release(); sl.E.release(); sl.A.release(); sl.R.release(); sl.cand.release();
+    sl.raw.release(); sl.A.release(); sl.R.release(); sl.cand.release();
     sl.cand_n.release(); sl.out_d.release(); sl.out_i.release(); sl.flagged.release(); sl.nflag.release();
     sl.derr.release(); sl.ext.release(); sl.tcq.A.release(); sl.tcq.B.release();
     mds_destroy(sl.ctx);
