@@ -294,6 +294,21 @@ def run_pipeline(args):
     return 0
 
 
+# DRAM bytes (read + write) of one k_screen_tc launch on the default workload
+# (20,000 x 1,000 atoms, k = 100, bf16x3), from one ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum (a 1-pass metric pair) with
+# the command `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
+# --clock-control none -k regex:k_screen_tc -s 3 -c 1 python bench.py --steps 2
+# --warmup 3 --no-cpu`. Other workloads report null.
+SCREEN_TRAFFIC_BYTES = 3.94e9 + 0.52e9
+
+
+def screen_traffic(args):
+    if (args.frames, args.atoms, args.k, args.precision) == (N_FRAMES, N_ATOMS, K, "bf16x3"):
+        return SCREEN_TRAFFIC_BYTES
+    return None
+
+
 def workload(frames, atoms):
     from mdsctk_gb300 import synth
 
@@ -333,6 +348,13 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def wait_first(self, timeout=10.0):
+        """Block until nvidia-smi has produced its first sample, so that its
+        start-up (NVML initialisation) falls before the timed region."""
+        t0 = time.time()
+        while self.proc is not None and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.05)
 
     def stop(self):
         if self.proc is None:
@@ -459,6 +481,7 @@ def main():
     torch.cuda.synchronize()
     sampler = ClockSampler(local)
     sampler.start()
+    sampler.wait_first()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -510,7 +533,7 @@ def main():
                       "l2": "inputs (240 MB of frames) larger than L2 every step",
                       "parallelism": f"replicas x{world}"},
            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                        "frac": achieved / peak, "traffic": None,
+                        "frac": achieved / peak, "traffic": screen_traffic(args),
                         "kernel": "screen", "kernel_ms": scr, "flops_per_launch": flops,
                         "peak_kind": f"{pk_kind} bf16 burst"},
            "stages_ms": {"prep": sorted(prep_ms)[len(prep_ms) // 2], "screen": scr,

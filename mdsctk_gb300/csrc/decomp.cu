@@ -27,6 +27,7 @@
 //     181-219); extension ext[x] = B^T (z_x / lambda_x) for all nev vectors
 //     in one pass (:301-312).
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -360,18 +361,39 @@ __global__ void k_scale_copy(const double* __restrict__ w, double a, int n, doub
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = w[i] * a;
 }
-// X[:, 0:ncols_out] = V[:, 0:m] * Y (m x ncols_out, column-major on device)
+// X[:, 0:nout] = V[:, 0:m] * Y (Y: m x nout, column-major on device). One
+// thread per row and GV_CB output columns per block (grid.y); Y is staged in
+// shared memory GV_JT rows at a time, so every V element is read once per
+// GV_CB outputs. Each output is a sequential sum over j (deterministic).
+#define GV_CB 8
+#define GV_JT 64
 __global__ void k_gemm_vy(const double* __restrict__ V, int64_t ld, int n, int m, const double* __restrict__ Y,
                           int nout, double* __restrict__ X, int64_t ldx) {
-  extern __shared__ double ys[];  // [m][nout] chunk: we read Y directly
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int c = 0; c < nout; ++c) {
-    double s = 0.0;
-    for (int j = 0; j < m; ++j) s += V[i + j * ld] * Y[j + (int64_t)c * m];
-    X[i + c * ldx] = s;
+  __shared__ double ys[GV_JT][GV_CB];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c0 = blockIdx.y * GV_CB;
+  double acc[GV_CB];
+#pragma unroll
+  for (int c = 0; c < GV_CB; ++c) acc[c] = 0.0;
+  for (int j0 = 0; j0 < m; j0 += GV_JT) {
+    const int jn = min(GV_JT, m - j0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < GV_JT * GV_CB; e += blockDim.x) {
+      const int jj = e / GV_CB, cc = e % GV_CB;
+      ys[jj][cc] = (jj < jn && c0 + cc < nout) ? Y[(j0 + jj) + (int64_t)(c0 + cc) * m] : 0.0;
+    }
+    __syncthreads();
+    if (i < n)
+      for (int jj = 0; jj < jn; ++jj) {
+        const double v = V[i + (int64_t)(j0 + jj) * ld];
+#pragma unroll
+        for (int c = 0; c < GV_CB; ++c) acc[c] += v * ys[jj][c];
+      }
   }
-  (void)ys;
+  if (i < n)
+#pragma unroll
+    for (int c = 0; c < GV_CB; ++c)
+      if (c0 + c < nout) X[i + (int64_t)(c0 + c) * ldx] = acc[c];
 }
 
 // ---------------------------------------------------------------------------
@@ -666,6 +688,12 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   MDS_TRY(Yd.alloc(ctx, sizeof(double) * (size_t)m * m));
   MDS_TRY(tmp.alloc(ctx, sizeof(double) * (size_t)n * m));
   DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx);
+  // step graphs by first step of the cycle; destroyed on every return path
+  struct Graphs : std::map<int, cudaGraphExec_t> {
+    ~Graphs() {
+      for (auto& g : *this) cudaGraphExecDestroy(g.second);
+    }
+  } graphs;
   MDS_TRY(h1.alloc(ctx, sizeof(double) * (nlock + m + 1)));
   MDS_TRY(h2.alloc(ctx, sizeof(double) * (nlock + m + 1)));
   MDS_TRY(ab.alloc(ctx, sizeof(double) * 2 * m));
@@ -739,24 +767,42 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
     // (invariant subspace, beta_j ~ 0) found then restarts the steps after
     // it from a fresh direction orthogonal to the basis.
     for (int j0 = k; j0 < m;) {
-      for (int j = j0; j < m; ++j) {
-        spmv(ctx, op, Vp + (int64_t)j * ld, w);
-        out.matvecs++;
-        const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
-        ctx->stats.launches += 10;
-        k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
-        k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h1.as<double>());
-        k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h1.as<double>(), w);
-        k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
-        k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h2.as<double>());
-        k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h2.as<double>(), w);
-        k_gemv_t_part<<<nparts, 256, 0, s>>>(w, ld, n, 1, w, part.as<double>());
-        k_reduce_part<<<1, 128, 0, s>>>(part.as<double>(), nparts, 1, h.as<double>());
-        k_lz_finish<<<1, 32, 0, s>>>(h1.as<double>(), h2.as<double>(), h.as<double>(), nlock + j, j, eps * 10.0,
-                                     ab.as<double>(), ab.as<double>() + m, brk.as<int>());
-        k_lz_scale<<<(n + 255) / 256, 256, 0, s>>>(w, ab.as<double>() + m, brk.as<int>(), j, n,
-                                                   Vp + (int64_t)(j + 1) * ld);
+      // The steps j0..m-1 are one CUDA graph, captured the first time a cycle
+      // starts at j0 (every pointer and size is fixed within this call) and
+      // replayed afterwards: one launch instead of ~11 per step.
+      auto git = graphs.find(j0);
+      if (git == graphs.end()) {
+        MDS_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int j = j0; j < m; ++j) {
+          const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
+          k_spmv<<<(int)(((int64_t)op.n * 32 + 255) / 256), 256, 0, s>>>(op.rp.as<int64_t>(), op.col.as<int>(),
+                                                                         op.w.as<double>(), Vp + (int64_t)j * ld,
+                                                                         op.n, w);
+          k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
+          k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h1.as<double>());
+          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h1.as<double>(), w);
+          k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
+          k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h2.as<double>());
+          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h2.as<double>(), w);
+          k_gemv_t_part<<<nparts, 256, 0, s>>>(w, ld, n, 1, w, part.as<double>());
+          k_reduce_part<<<1, 128, 0, s>>>(part.as<double>(), nparts, 1, h.as<double>());
+          k_lz_finish<<<1, 32, 0, s>>>(h1.as<double>(), h2.as<double>(), h.as<double>(), nlock + j, j,
+                                       eps * 10.0, ab.as<double>(), ab.as<double>() + m, brk.as<int>());
+          k_lz_scale<<<(n + 255) / 256, 256, 0, s>>>(w, ab.as<double>() + m, brk.as<int>(), j, n,
+                                                     Vp + (int64_t)(j + 1) * ld);
+        }
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (ce != cudaSuccess) return mds_fail(ctx, MDS_ERR_CUDA, "Lanczos step capture: %s", cudaGetErrorString(ce));
+        cudaGraphExec_t ge = nullptr;
+        ce = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return mds_fail(ctx, MDS_ERR_CUDA, "Lanczos step graph: %s", cudaGetErrorString(ce));
+        git = graphs.emplace(j0, ge).first;
       }
+      MDS_CUDA(ctx, cudaGraphLaunch(git->second, s));
+      out.matvecs += m - j0;
+      ctx->stats.launches += 12 * (m - j0);
       MDS_CUDA(ctx, cudaGetLastError());
       std::vector<double> hab(2 * m);
       std::vector<int> hbrk(m);
@@ -822,14 +868,18 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
       }
       MDS_CUDA(ctx, cudaMemcpyAsync(Yd.p, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice, s));
       ctx->stats.launches++;
-      k_gemm_vy<<<(n + 127) / 128, 128, 0, s>>>(Vp, ld, n, m, Yd.as<double>(), nev, dX, n);
+      k_gemm_vy<<<dim3((n + 127) / 128, (nev + GV_CB - 1) / GV_CB), 128, 0, s>>>(Vp, ld, n, m, Yd.as<double>(), nev,
+                                                                               dX, n);
       MDS_CUDA(ctx, cudaGetLastError());
       out.restarts = restart;
       return MDS_OK;
     }
     // thick restart with the kk largest Ritz pairs
-    int kk = std::min(m - 2, nev + std::max(nconv, (m - nev) / 2));
-    kk = std::max(kk, nev);
+    // ARPACK's rule (dsaup2): keep nev + min(nconv, np/2) Ritz pairs, np =
+    // ncv - nev; with nev = 1 keep ncv/2 (ncv >= 6) or 2
+    int kk = nev + std::min(nconv, (m - nev) / 2);
+    if (kk == 1) kk = (m >= 6) ? m / 2 : (m > 2 ? 2 : 1);
+    kk = std::max(nev, std::min(kk, m - 2));
     std::vector<double> Y((size_t)m * kk);
     theta_k.assign(kk, 0.0);
     s_k.assign(kk, 0.0);
@@ -841,7 +891,8 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
     }
     MDS_CUDA(ctx, cudaMemcpyAsync(Yd.p, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice, s));
     ctx->stats.launches++;
-    k_gemm_vy<<<(n + 127) / 128, 128, 0, s>>>(Vp, ld, n, m, Yd.as<double>(), kk, tmp.as<double>(), n);
+    k_gemm_vy<<<dim3((n + 127) / 128, (kk + GV_CB - 1) / GV_CB), 128, 0, s>>>(Vp, ld, n, m, Yd.as<double>(), kk,
+                                                                              tmp.as<double>(), n);
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaMemcpyAsync(Vp, tmp.p, sizeof(double) * (size_t)n * kk, cudaMemcpyDeviceToDevice, s));
     MDS_CUDA(ctx, cudaMemcpyAsync(Vp + (int64_t)kk * ld, Vp + (int64_t)m * ld, sizeof(double) * n,

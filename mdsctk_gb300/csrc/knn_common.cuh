@@ -116,6 +116,24 @@ int choose_nseg_fp32(int nfit, int num_sms, int nref);
 int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout);
 int tc_seg_stride();
 int tc_choose_nseg(mds_ctx* ctx, const KnnRmsPlan& pl, int nfit);
+// Tile skipping data of the tensor-core screen (knn_rms_tc.cu): lower
+// bounds of RMSD from every fit frame to the pivot of every column tile
+// (pivlb [ncoltiles][nfit]) and the tiles' radii (prad [ncoltiles]).
+struct TcSkip {
+  const float* pivlb = nullptr;
+  const float* prad = nullptr;
+};
+// The pivots of a reference set: the middle frame of every column tile
+// (their deviations, records and split operands) and the tiles' radii.
+struct TcPivots {
+  DevBuf A, R, rad;
+  TcOperands tc;
+  int nC = 0;
+};
+int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv);
+int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
+                   const TcPivots& pv, float* lb, int* derr = nullptr);
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
-                     int* cand_n, int* derr = nullptr);
+                     int* cand_n, int* derr = nullptr, const TcSkip* skip = nullptr,
+                     float* dense = nullptr);

@@ -30,6 +30,32 @@
 // ---------------------------------------------------------------------------
 // 1. centring
 // ---------------------------------------------------------------------------
+// Block sum of N float partials: FP32 shuffle tree inside each warp (FP64
+// issues at a small fraction of the FP32 rate on this GPU), then the warps'
+// sums added in FP64 in warp order. red holds (blockDim/32) * N doubles.
+template <int N>
+__device__ __forceinline__ void block_sum_vecf(const float (&p)[N], double (&out)[N], double* red) {
+  float v[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    v[i] = p[i];
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (l == 0)
+#pragma unroll
+    for (int i = 0; i < N; ++i) red[w * N + i] = (double)v[i];
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    double s = 0;
+    for (int j = 0; j < nw; ++j) s += red[j * N + i];
+    out[i] = s;
+  }
+  __syncthreads();
+}
+
 // Block sum of N values at once: every warp reduces its N partial sums with
 // shuffles, lane 0 stores them in red[warp * N + i], one barrier, then every
 // thread adds the warps' rows in order. red holds (blockDim/32) * N doubles.
@@ -199,8 +225,8 @@ __global__ void k_prep(const float* __restrict__ raw, int n, int natoms, int Ap,
       const float mm = mass[a];
       for (int c = 0; c < 3; ++c) p[c] = fmaf(mm, x[3 * a + c], p[c]);
     }
-    double sc[3] = {p[0], p[1], p[2]};
-    block_sum_vec<3>(sc, red);
+    double sc[3];
+    block_sum_vecf<3>(p, sc, red);
     for (int c = 0; c < 3; ++c) com[c] = (float)(sc[c] / (double)tm);
   }
   if (!nofit) {
@@ -214,8 +240,7 @@ __global__ void k_prep(const float* __restrict__ raw, int n, int natoms, int Ap,
         for (int d = 0; d < 3; ++d) p[1 + 3 * c + d] = fmaf(yc[c], mc[d], p[1 + 3 * c + d]);
     }
     double sv[10];
-    for (int i = 0; i < 10; ++i) sv[i] = p[i];
-    block_sum_vec<10>(sv, red);
+    block_sum_vecf<10>(p, sv, red);
     if (threadIdx.x == 0) {
       double R[9];
       qcp_rotation_fp64(sv + 1, 0.5 * (sv[0] + M0[0] + M0[4] + M0[8]), R);
@@ -247,8 +272,9 @@ __global__ void k_prep(const float* __restrict__ raw, int n, int natoms, int Ap,
       for (int c = 0; c < 3; ++c) o[c * Ap + a] = 0.0f;
     }
   }
-  double eu[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
-  block_sum_vec<10>(eu, red);
+  const float eup[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
+  double eu[10];
+  block_sum_vecf<10>(eup, eu, red);
   if (threadIdx.x == 0) {
     const double* U = eu + 1;
     float* r = rec + (int64_t)f * MDS_REC;
@@ -490,19 +516,33 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
                               const float* __restrict__ Ar, int Ap, int natoms, const int* cj, int nc, bool nofit,
                               float* sd) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // four atoms per lane and load (Ap is a multiple of 64; padding atoms are
+  // zero in a_i, a_j and mu, so they add nothing)
+  const int Ap4 = Ap >> 2;
+  const float4* sa4 = reinterpret_cast<const float4*>(sa);
+  const float4* sx4 = reinterpret_cast<const float4*>(sx);
+  (void)natoms;
   for (int c = warp; c < nc; c += nw) {
-    const float* aj = Ar + (int64_t)cj[c] * 3 * Ap;
+    const float4* aj4 = reinterpret_cast<const float4*>(Ar + (int64_t)cj[c] * 3 * Ap);
     float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // D, P[9]
-    for (int a = lane; a < natoms; a += 32) {
-      const float d0 = sa[a] - __ldg(aj + a);
-      const float d1 = sa[Ap + a] - __ldg(aj + Ap + a);
-      const float d2 = sa[2 * Ap + a] - __ldg(aj + 2 * Ap + a);
-      v[0] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, v[0])));
+    for (int q = lane; q < Ap4; q += 32) {
+      const float4 ia = sa4[q], ib = sa4[Ap4 + q], ic = sa4[2 * Ap4 + q];
+      const float4 ja = __ldg(aj4 + q), jb = __ldg(aj4 + Ap4 + q), jc = __ldg(aj4 + 2 * Ap4 + q);
+      const float d0[4] = {ia.x - ja.x, ia.y - ja.y, ia.z - ja.z, ia.w - ja.w};
+      const float d1[4] = {ib.x - jb.x, ib.y - jb.y, ib.z - jb.z, ib.w - jb.w};
+      const float d2[4] = {ic.x - jc.x, ic.y - jc.y, ic.z - jc.z, ic.w - jc.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) v[0] = fmaf(d0[e], d0[e], fmaf(d1[e], d1[e], fmaf(d2[e], d2[e], v[0])));
       if (!nofit) {
-        const float x0 = sx[a], x1 = sx[Ap + a], x2 = sx[2 * Ap + a];
-        v[1] = fmaf(x0, d0, v[1]); v[2] = fmaf(x0, d1, v[2]); v[3] = fmaf(x0, d2, v[3]);
-        v[4] = fmaf(x1, d0, v[4]); v[5] = fmaf(x1, d1, v[5]); v[6] = fmaf(x1, d2, v[6]);
-        v[7] = fmaf(x2, d0, v[7]); v[8] = fmaf(x2, d1, v[8]); v[9] = fmaf(x2, d2, v[9]);
+        const float4 xa = sx4[q], xb = sx4[Ap4 + q], xc = sx4[2 * Ap4 + q];
+        const float x0[4] = {xa.x, xa.y, xa.z, xa.w}, x1[4] = {xb.x, xb.y, xb.z, xb.w};
+        const float x2[4] = {xc.x, xc.y, xc.z, xc.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          v[1] = fmaf(x0[e], d0[e], v[1]); v[2] = fmaf(x0[e], d1[e], v[2]); v[3] = fmaf(x0[e], d2[e], v[3]);
+          v[4] = fmaf(x1[e], d0[e], v[4]); v[5] = fmaf(x1[e], d1[e], v[5]); v[6] = fmaf(x1[e], d2[e], v[6]);
+          v[7] = fmaf(x2[e], d0[e], v[7]); v[8] = fmaf(x2[e], d1[e], v[8]); v[9] = fmaf(x2[e], d2[e], v[9]);
+        }
       }
     }
 #pragma unroll
@@ -557,8 +597,8 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
       p[0] = fmaf(x0, x0, p[0]); p[1] = fmaf(x1, x1, p[1]); p[2] = fmaf(x2, x2, p[2]);
       p[3] = fmaf(x0, x1, p[3]); p[4] = fmaf(x0, x2, p[4]); p[5] = fmaf(x1, x2, p[5]);
     }
-    double c[6] = {p[0], p[1], p[2], p[3], p[4], p[5]};
-    block_sum_vec<6>(c, s_red);
+    double c[6];
+    block_sum_vecf<6>(p, c, s_red);
     if (threadIdx.x < 6) C6[threadIdx.x] = (float)c[threadIdx.x];
     __syncthreads();
   }
@@ -948,9 +988,21 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
                                cand.as<uint64_t>(), cand_n.as<int>()));
     st.screen_launches = 1;
   } else {
+    // tile skipping by the triangle inequality once there are tiles to skip
+    TcSkip sk;
+    TcPivots pv;
+    DevBuf lb(ctx);
+    const bool skipping = !pl.screen_keys && (nref + 79) / 80 >= 4;
+    if (skipping) {
+      MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv));
+      MDS_TRY(lb.alloc(ctx, sizeof(float) * (size_t)pv.nC * nfit));
+      MDS_TRY(tc_skip_bounds(ctx, pl, same ? tcr : tcf, Rfp, nfit, pv, lb.as<float>()));
+      sk.pivlb = lb.as<float>();
+      sk.prad = pv.rad.as<float>();
+    }
     MDS_TRY(launch_screen_tc(ctx, pl, same ? tcr : tcf, tcr, Rfp, Rr.as<float>(), nfit, Kp, nseg,
-                             cand.as<uint64_t>(), cand_n.as<int>()));
-    st.screen_launches = 1;
+                             cand.as<uint64_t>(), cand_n.as<int>(), nullptr, skipping ? &sk : nullptr));
+    st.screen_launches = skipping ? 2 : 1;
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
   if (pl.screen_keys) {

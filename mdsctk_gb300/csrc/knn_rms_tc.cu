@@ -10,7 +10,7 @@
 // CTA tile: M = 128 TMEM lanes = 40 fit frames (each 32-lane quarter holds
 // 10 frames x 3 coordinates, two padding lanes), N = 240 columns = 80
 // reference frames stored coordinate-major (x of 80 frames, then y, then z).
-// Reduction in K-blocks of 32 atoms through a 3-stage TMA pipeline
+// Reduction in K-blocks of 32 atoms through a 4-stage TMA pipeline
 // (64-byte swizzle). Two TMEM accumulators (2 x 240 of 512 columns) let the
 // MMA of one column tile run under the epilogue of the previous one.
 //
@@ -45,7 +45,7 @@
 #define TC_M 128
 #define TC_N 240
 #define TC_KB 32
-#define TC_STAGES 3
+#define TC_STAGES 4
 #define TC_THREADS 576
 #define TC_EPI_WARPS 16
 #define TC_CAPG 512
@@ -124,17 +124,26 @@ int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOp
 // ---------------------------------------------------------------------------
 // the screen kernel
 // ---------------------------------------------------------------------------
+#define TC_TQ 8  // depth of the task ring (producer -> MMA thread and epilogue warps)
 struct TcShared {
   uint64_t full[TC_STAGES], empty[TC_STAGES], tfull[2], tempty[2], done;
+  uint64_t tq_full[TC_TQ], tq_empty[TC_TQ];
+  int2 task[TC_TQ];  // (item, column tile); tile -1 ends an item, item -1 the stream
+  int thr_item;      // the item whose rows' thresholds thr[] holds (-1: none)
   uint32_t tmem_base;
   int abortf;
   int bar_count, bar_gen;
   int cnt[TC_FR_M];
   float thr[TC_FR_M];
-  float colrec[TC_FR_N * MDS_REC];
+  float colrec[TC_FR_N * MDS_REC];  // records of the current column tile
+  float rowrec[TC_FR_M * MDS_REC];  // records of the current row tile
 };
 
-#define TC_SMEM_BYTES (TC_STAGES * TC_STAGE_BYTES + sizeof(TcShared) + TC_EPI_WARPS * TC_CAPG * 8 + 1024)
+// per-warp shared scratch: the radix-select histogram, and the final sort of a
+// row's list when it holds at most TC_SCR keys
+#define TC_SCR 256
+#define TC_SMEM_BYTES (TC_STAGES * TC_STAGE_BYTES + sizeof(TcShared) + TC_EPI_WARPS * TC_SCR * 8 + 1024)
+static_assert(TC_SMEM_BYTES <= 227 * 1024, "screen shared memory exceeds the per-block limit");
 
 __device__ __forceinline__ float sel3(int i, float a0, float a1, float a2) {
   return i == 0 ? a0 : (i == 1 ? a1 : a2);
@@ -267,7 +276,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
             int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
+            const float* __restrict__ pivlb, const float* __restrict__ prad, float* __restrict__ dense,
             uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
+  // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
+  // Work items (row tile, column segment) are claimed dynamically by each
+  // CTA's producer, which also decides which column tiles of the item to
+  // compute and passes (item, tile) tasks in order to the MMA thread and the
+  // epilogue warps through the task ring.
+  //
+  // Tile skipping (pivlb != null): RMSD is a metric, so for row i and any
+  // frame j of column tile T with pivot p_T, RMSD(i, j) >= RMSD(i, p_T) -
+  // RMSD(j, p_T) >= pivlb[T][i] - prad[T] = L. When every row of the row tile
+  // has L > 0 and L^2 above its current threshold (the K'-th smallest bound
+  // of its list, which only decreases), no pair of the tile can enter the
+  // lists, and every such pair's true RMSD^2 exceeds the final threshold the
+  // recheck verifies against -- the tile is not computed.
+  //
+  // Dense mode (dense != null; the pivot pass): every pair's lower bound of
+  // RMSD (sqrt of the screen value) is written to dense[j][i]; no lists.
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -289,9 +315,14 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       mbar_init(&S->tempty[b], TC_EPI_WARPS);
     }
     mbar_init(&S->done, 1);
+    for (int i = 0; i < TC_TQ; ++i) {
+      mbar_init(&S->tq_full[i], 1);
+      mbar_init(&S->tq_empty[i], 1 + TC_EPI_WARPS);
+    }
     S->abortf = 0;
     S->bar_count = 0;
     S->bar_gen = 0;
+    S->thr_item = -1;
     mbar_fence_init();
   }
   if (warp == 1) {
@@ -306,17 +337,63 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
+    // The whole warp runs the loop (the skip test uses every lane); lane 0
+    // claims items, pushes tasks and issues the TMA loads.
     if (lane == 0) {
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
-      uint32_t stage = 0, phase = 0;
-      bool ok = true;
-      for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-        const int rt = item / nseg, seg = item % nseg;
-        const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
-        const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
-        for (int ti = 0; ti < t1 - t0 && ok; ++ti) {
-          const int tile = tile_order(ti, t0, t1, td);
+    }
+    uint32_t stage = 0, phase = 0, qs = 0;
+    bool ok = true;
+    // push one task; false if the wait timed out or the kernel aborts
+    auto push = [&](int item, int tile) -> bool {
+      const uint32_t slot = qs % TC_TQ, ph = (qs / TC_TQ) & 1;
+      int good = 1;
+      if (lane == 0) {
+        good = mbar_wait(&S->tq_empty[slot], ph ^ 1, abortf, 1000000000ull, 1024) ? 1 : 0;
+        if (good) {
+          S->task[slot] = make_int2(item, tile);
+          mbar_arrive(&S->tq_full[slot]);
+        }
+      }
+      ++qs;
+      return __shfl_sync(0xffffffffu, good, 0) != 0;
+    };
+    while (ok) {
+      int item = 0;
+      if (lane == 0) {
+        item = atomicAdd(err + 1, 1);
+        if (item >= nitems) item = -1;
+      }
+      item = __shfl_sync(0xffffffffu, item, 0);
+      if (item < 0) {
+        ok = push(-1, -1);
+        break;
+      }
+      const int rt = item / nseg, seg = item % nseg;
+      const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+      const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
+      for (int ti = 0; ti < t1 - t0 && ok; ++ti) {
+        const int tile = tile_order(ti, t0, t1, td);
+        if (pivlb) {
+          bool can = false;
+          if (*(volatile int*)&S->thr_item == item) {
+            __threadfence_block();
+            can = true;
+            const float rad = __ldg(prad + tile);
+            for (int r = lane; r < TC_FR_M; r += 32) {
+              const int gi = rt * TC_FR_M + r;
+              if (gi >= nfit) continue;
+              const float thr = *(volatile float*)&S->thr[r];
+              const float L = __ldg(pivlb + (int64_t)tile * nfit + gi) - rad;
+              if (!(L > 0.0f && L * L > thr)) can = false;
+            }
+            if (*(volatile int*)&S->thr_item != item) can = false;  // moved on meanwhile
+          }
+          if (__all_sync(0xffffffffu, can)) continue;
+        }
+        if (!(ok = push(item, tile))) break;
+        if (lane == 0) {
           for (int kb = 0; kb < nkb; ++kb) {
             if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
             unsigned char* st = stages + stage * TC_STAGE_BYTES;
@@ -328,51 +405,62 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             if (++stage == TC_STAGES) { stage = 0; phase ^= 1; }
           }
         }
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
       }
-      if (!ok) {
-        atomicMax(err, 1);
-        // drain: every issued stage completes or times out
-        for (int s = 0; s < TC_STAGES; ++s) {
-          volatile int dummy = 0;
-          mbar_wait(&S->full[s], 0, &dummy, 50000000ull);
-        }
+      if (ok) ok = push(item, -1);
+    }
+    if (!ok && lane == 0) {
+      atomicMax(err, 1);
+      *abortf = 1;
+      // drain: every issued stage completes or times out
+      for (int s = 0; s < TC_STAGES; ++s) {
+        volatile int dummy = 0;
+        mbar_wait(&S->full[s], 0, &dummy, 50000000ull);
       }
     }
+    __syncwarp();
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
       uint32_t stage = 0, phase = 0, acc = 0;
       bool ok = true;
       const uint32_t sbase = smem_u32(stages);
-      for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-        const int seg = item % nseg;
-        const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
-        for (int tile = t0; tile < t1 && ok; ++tile, ++acc) {
-          const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
-          if (!mbar_wait(&S->tempty[b], aph ^ 1, abortf, 1000000000ull, 64)) { ok = false; break; }
+      for (uint32_t qs = 0; ok; ++qs) {
+        const uint32_t slot = qs % TC_TQ, qph = (qs / TC_TQ) & 1;
+        if (!mbar_wait(&S->tq_full[slot], qph, abortf, 1000000000ull, 64)) { ok = false; break; }
+        const volatile int* tv = reinterpret_cast<volatile int*>(&S->task[slot]);
+        const int2 t = make_int2(tv[0], tv[1]);
+        mbar_arrive(&S->tq_empty[slot]);
+        if (t.x < 0) break;
+        if (t.y < 0) continue;
+        const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
+        if (!mbar_wait(&S->tempty[b], aph ^ 1, abortf, 1000000000ull, 64)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tbase + b * 256;
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&S->full[stage], phase, abortf, 1000000000ull, 64)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t d = tbase + b * 256;
-          for (int kb = 0; kb < nkb; ++kb) {
-            if (!mbar_wait(&S->full[stage], phase, abortf, 1000000000ull, 64)) { ok = false; break; }
-            tc_fence_after();
-            const uint32_t st = sbase + stage * TC_STAGE_BYTES;
+          const uint32_t st = sbase + stage * TC_STAGE_BYTES;
 #pragma unroll
-            for (int ks = 0; ks < TC_KB / 16; ++ks) {
-              const uint64_t ahi = umma_desc_sw64(st + ks * 32);
-              const uint64_t alo = umma_desc_sw64(st + TC_A_BYTES + ks * 32);
-              const uint64_t bhi = umma_desc_sw64(st + 2 * TC_A_BYTES + ks * 32);
-              const uint64_t blo = umma_desc_sw64(st + 2 * TC_A_BYTES + TC_B_BYTES + ks * 32);
-              umma_f16(d, ahi, bhi, idesc, (kb | ks) != 0);
-              umma_f16(d, ahi, blo, idesc, 1);
-              umma_f16(d, alo, bhi, idesc, 1);
-            }
-            umma_commit(&S->empty[stage]);
-            if (++stage == TC_STAGES) { stage = 0; phase ^= 1; }
+          for (int ks = 0; ks < TC_KB / 16; ++ks) {
+            const uint64_t ahi = umma_desc_sw64(st + ks * 32);
+            const uint64_t alo = umma_desc_sw64(st + TC_A_BYTES + ks * 32);
+            const uint64_t bhi = umma_desc_sw64(st + 2 * TC_A_BYTES + ks * 32);
+            const uint64_t blo = umma_desc_sw64(st + 2 * TC_A_BYTES + TC_B_BYTES + ks * 32);
+            umma_f16(d, ahi, bhi, idesc, (kb | ks) != 0);
+            umma_f16(d, ahi, blo, idesc, 1);
+            umma_f16(d, alo, bhi, idesc, 1);
           }
-          if (ok) umma_commit(&S->tfull[b]);
+          umma_commit(&S->empty[stage]);
+          if (++stage == TC_STAGES) { stage = 0; phase ^= 1; }
         }
+        if (ok) umma_commit(&S->tfull[b]);
+        ++acc;
       }
-      if (!ok) atomicMax(err, 2);
+      if (!ok) {
+        atomicMax(err, 2);
+        *abortf = 1;
+      }
       // all MMAs of this thread retire before TMEM is freed
       umma_commit(&S->done);
       volatile int dummy = 0;
@@ -387,81 +475,131 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int ci0 = (h * 10) / 4, ci1 = ((h + 1) * 10) / 4;
     const int f = lane / 3, c = lane % 3;
     const int rloc = q * 10 + f;     // row within the 40-frame tile (f < 10)
-    uint64_t* scratch = scratch_all + ew * TC_CAPG;
+    uint64_t* scratch = scratch_all + ew * TC_SCR;
     const float INF = __int_as_float(0x7f800000);
+    const float* rrec = S->rowrec + min(rloc, TC_FR_M - 1) * MDS_REC;  // lanes 30, 31 (f = 10) are padding
     uint32_t acc = 0;
     bool ok = true;
-    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-      const int rt = item / nseg, seg = item % nseg;
-      const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
-      const int grow = rt * TC_FR_M + rloc;
-      const bool rowok = (f < 10) && grow < nfit;
-      float rrec[MDS_REC];
-#pragma unroll
-      for (int i = 0; i < MDS_REC; ++i) rrec[i] = rowok ? __ldg(recf + (int64_t)grow * MDS_REC + i) : 0.f;
-      // rows owned by this warp for resets and compaction: f = h, h+2, ...
-      if (lane < 3 && h + 4 * lane < 10) {
-        int fr = h + 4 * lane;
-        S->cnt[q * 10 + fr] = 0;
-        S->thr[q * 10 + fr] = INF;
-      }
-      const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
-      for (int ti = 0; ti < t1 - t0; ++ti, ++acc) {
-        const int tile = tile_order(ti, t0, t1, td);
-        const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
-        // column records of this tile
-        for (int e = ew * 32 + lane; e < TC_FR_N * MDS_REC; e += TC_EPI_WARPS * 32) {
-          int j = tile * TC_FR_N + e / MDS_REC;
-          S->colrec[e] = (j < Nr) ? __ldg(recr + (int64_t)j * MDS_REC + e % MDS_REC) : 0.f;
+    int cur = -1, rt = 0, seg = 0, grow = 0, ntile = 0;
+    bool rowok = false;
+    for (uint32_t qs = 0; ok; ++qs) {
+      const uint32_t slot = qs % TC_TQ, qph = (qs / TC_TQ) & 1;
+      if (!mbar_wait(&S->tq_full[slot], qph, abortf)) { ok = false; break; }
+      const volatile int* tv = reinterpret_cast<volatile int*>(&S->task[slot]);
+      const int2 task = make_int2(tv[0], tv[1]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S->tq_empty[slot]);
+      if (task.x < 0) break;
+      if (task.x != cur) {
+        // start of an item: row records and this warp's rows' lists (every
+        // warp has passed the previous item's final barrier)
+        cur = task.x;
+        rt = cur / nseg;
+        seg = cur % nseg;
+        grow = rt * TC_FR_M + rloc;
+        rowok = (f < 10) && grow < nfit;
+        ntile = 0;
+        for (int e = ew * 32 + lane; e < TC_FR_M * MDS_REC; e += TC_EPI_WARPS * 32) {
+          const int r = rt * TC_FR_M + e / MDS_REC;
+          S->rowrec[e] = (r < nfit) ? __ldg(recf + (int64_t)r * MDS_REC + e % MDS_REC) : 0.f;
         }
-        if (!mbar_wait(&S->tfull[b], aph, abortf)) { ok = false; break; }
-        tc_fence_after();
+        if (lane < 3 && h + 4 * lane < 10) {
+          const int fr = h + 4 * lane;
+          S->cnt[q * 10 + fr] = 0;
+          S->thr[q * 10 + fr] = INF;
+        }
+      }
+      if (task.y < 0) {
+        // end of the item: sort and publish this warp's rows
         if (!ep_sync(S, lane)) { ok = false; break; }
-        const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256;
-        uint64_t* rowbuf = candbuf + ((int64_t)grow * nseg + seg) * TC_CAPG;
+        if (!dense)
+          for (int fr = h; fr < 10; fr += 4) {
+            const int r = q * 10 + fr;
+            const int gr = rt * TC_FR_M + r;
+            if (gr >= nfit) continue;
+            int n = min(S->cnt[r], TC_CAPG);
+            uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
+            if (n > Kp) {
+              warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
+              n = Kp;
+            }
+            if (n <= TC_SCR) {
+              for (int x = lane; x < n; x += 32) scratch[x] = src[x];
+              warp_bitonic_sort(scratch, n, TC_SCR, lane);
+              for (int x = lane; x < n; x += 32) src[x] = scratch[x];
+            } else {
+              warp_bitonic_sort(src, n, TC_CAPG, lane);  // in place (global; __syncwarp orders it)
+            }
+            if (lane == 0) cand_n[(int64_t)gr * nseg + seg] = n;
+            __syncwarp();
+          }
+        if (!ep_sync(S, lane)) { ok = false; break; }
+        continue;
+      }
+      const int tile = task.y;
+      const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
+      // column records of this tile (the previous tile's readers passed the
+      // end-of-tile barrier)
+      for (int e = ew * 32 + lane; e < TC_FR_N * MDS_REC; e += TC_EPI_WARPS * 32) {
+        const int j = tile * TC_FR_N + e / MDS_REC;
+        S->colrec[e] = (j < Nr) ? __ldg(recr + (int64_t)j * MDS_REC + e % MDS_REC) : 0.f;
+      }
+      if (!mbar_wait(&S->tfull[b], aph, abortf)) { ok = false; break; }
+      tc_fence_after();
+      if (!ep_sync(S, lane)) { ok = false; break; }
+      if (ntile++ == 0 && ew == 0 && lane == 0) {
+        __threadfence_block();
+        *(volatile int*)&S->thr_item = cur;  // this item's thresholds are live
+      }
+      const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256;
+      uint64_t* rowbuf = dense ? nullptr : candbuf + ((int64_t)grow * nseg + seg) * TC_CAPG;
 #pragma unroll 1
-        for (int ci = ci0; ci < ci1; ++ci) {
-          float vx[8], vy[8], vz[8];
-          tmem_ld8(tq + 8 * ci, vx);
-          tmem_ld8(tq + TC_FR_N + 8 * ci, vy);
-          tmem_ld8(tq + 2 * TC_FR_N + 8 * ci, vz);
-          tmem_wait_ld();
+      for (int ci = ci0; ci < ci1; ++ci) {
+        float vx[8], vy[8], vz[8];
+        tmem_ld8(tq + 8 * ci, vx);
+        tmem_ld8(tq + TC_FR_N + 8 * ci, vy);
+        tmem_ld8(tq + 2 * TC_FR_N + 8 * ci, vz);
+        tmem_wait_ld();
 #pragma unroll
-          for (int g0 = 0; g0 < 8; g0 += 3) {
-            // v[g][d]: row (f, c) of the Gram of pair (f, column frame g0+g)
-            float v[3][3];
+        for (int g0 = 0; g0 < 8; g0 += 3) {
+          // v[g][d]: row (f, c) of the Gram of pair (f, column frame g0+g)
+          float v[3][3];
 #pragma unroll
-            for (int g = 0; g < 3; ++g) {
-              v[g][0] = (g0 + g < 8) ? vx[(g0 + g) & 7] : 0.f;
-              v[g][1] = (g0 + g < 8) ? vy[(g0 + g) & 7] : 0.f;
-              v[g][2] = (g0 + g < 8) ? vz[(g0 + g) & 7] : 0.f;
-            }
-            // 3-lane transpose: lane (f, m=c) gathers rows 0..2 of block m
-            float R[3][3];
+          for (int g = 0; g < 3; ++g) {
+            v[g][0] = (g0 + g < 8) ? vx[(g0 + g) & 7] : 0.f;
+            v[g][1] = (g0 + g < 8) ? vy[(g0 + g) & 7] : 0.f;
+            v[g][2] = (g0 + g < 8) ? vz[(g0 + g) & 7] : 0.f;
+          }
+          // 3-lane transpose: lane (f, m=c) gathers rows 0..2 of block m
+          float R[3][3];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) R[0][d] = sel3(c, v[0][d], v[1][d], v[2][d]);
+          for (int d = 0; d < 3; ++d) R[0][d] = sel3(c, v[0][d], v[1][d], v[2][d]);
 #pragma unroll
-            for (int s = 1; s < 3; ++s) {
-              const int src = 3 * f + (c + s) % 3;
-              const int gi = (c + 3 - s) % 3;
-#pragma unroll
-              for (int d = 0; d < 3; ++d) {
-                float send = sel3(gi, v[0][d], v[1][d], v[2][d]);
-                R[s][d] = __shfl_sync(0xffffffffu, send, src & 31);
-              }
-            }
-            // row (c + s) % 3 of block m is R[s]
-            float G[9];
+          for (int s = 1; s < 3; ++s) {
+            const int src = 3 * f + (c + s) % 3;
+            const int gi = (c + 3 - s) % 3;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-              G[0 + d] = sel3(c, R[0][d], R[2][d], R[1][d]) * ginv;
-              G[3 + d] = sel3(c, R[1][d], R[0][d], R[2][d]) * ginv;
-              G[6 + d] = sel3(c, R[2][d], R[1][d], R[0][d]) * ginv;
+              float send = sel3(gi, v[0][d], v[1][d], v[2][d]);
+              R[s][d] = __shfl_sync(0xffffffffu, send, src & 31);
             }
-            const int gl = 8 * ci + g0 + c;
-            const int j = tile * TC_FR_N + gl;
-            if (rowok && (g0 + c < 8) && j < Nr) {
-              const float* cr = S->colrec + gl * MDS_REC;
+          }
+          // row (c + s) % 3 of block m is R[s]
+          float G[9];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            G[0 + d] = sel3(c, R[0][d], R[2][d], R[1][d]) * ginv;
+            G[3 + d] = sel3(c, R[1][d], R[0][d], R[2][d]) * ginv;
+            G[6 + d] = sel3(c, R[2][d], R[1][d], R[0][d]) * ginv;
+          }
+          const int gl = 8 * ci + g0 + c;
+          const int j = tile * TC_FR_N + gl;
+          if (rowok && (g0 + c < 8) && j < Nr) {
+            const float* cr = S->colrec + gl * MDS_REC;
+            if (dense) {
+              const float sv = screen_shifted_f32(G, rrec, cr, nofit != 0, guard * (rrec[15] + cr[15]));
+              dense[(int64_t)j * nfit + grow] = sqrtf(fmaxf(sv, 0.0f));
+            } else {
               const float thr = *(volatile float*)&S->thr[rloc];
               float sv = screen_shifted_f32(G, rrec, cr, nofit != 0, guard * (rrec[15] + cr[15]), thr);
               sv = fmaxf(sv, 0.0f);
@@ -475,47 +613,35 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             }
           }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&S->tempty[b]);
-        if (!ep_sync(S, lane)) { ok = false; break; }
-        // compaction of this warp's rows
-        for (int fr = h; fr < 10; fr += 4) {
-          const int r = q * 10 + fr;
-          const int gr = rt * TC_FR_M + r;
-          if (gr >= nfit) continue;
-          int n = S->cnt[r];
-          bool need = (n > Kp) && (n > TC_CAPG - TC_FR_N || S->thr[r] == INF);
-          if (!need) continue;
-          uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
-          n = min(n, TC_CAPG);
-          const float t = warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
-          if (lane == 0) {
-            S->cnt[r] = Kp;
-            S->thr[r] = t;
-          }
-          __syncwarp();
-        }
       }
-      if (!ok) break;
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S->tempty[b]);
+      ++acc;
       if (!ep_sync(S, lane)) { ok = false; break; }
-      // final: sort and publish this warp's rows of the item
+      if (dense) continue;
+      // compaction of this warp's rows
       for (int fr = h; fr < 10; fr += 4) {
         const int r = q * 10 + fr;
         const int gr = rt * TC_FR_M + r;
         if (gr >= nfit) continue;
-        int n = min(S->cnt[r], TC_CAPG);
+        int n = S->cnt[r];
+        bool need = (n > Kp) && (n > TC_CAPG - TC_FR_N || S->thr[r] == INF);
+        if (!need) continue;
         uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
-        for (int x = lane; x < n; x += 32) scratch[x] = src[x];
-        warp_bitonic_sort(scratch, n, TC_CAPG, lane);
-        int keep = min(n, Kp);
-        for (int x = lane; x < keep; x += 32) src[x] = scratch[x];
-        if (lane == 0) cand_n[(int64_t)gr * nseg + seg] = keep;
+        n = min(n, TC_CAPG);
+        const float t = warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
+        if (lane == 0) {
+          S->cnt[r] = Kp;
+          S->thr[r] = t;
+        }
         __syncwarp();
       }
-      if (!ep_sync(S, lane)) { ok = false; break; }
     }
-    if (!ok && lane == 0) atomicMax(err, 3);
+    if (!ok && lane == 0) {
+      atomicMax(err, 3);
+      *abortf = 1;
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -578,7 +704,7 @@ int tc_seg_stride() { return TC_CAPG; }
 
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
-                     int* cand_n, int* derr) {
+                     int* cand_n, int* derr, const TcSkip* skip, float* dense) {
   if (Kp + 2 * TC_FR_N > TC_CAPG)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen supports K' <= %d (k too large)",
                     TC_CAPG - 2 * TC_FR_N);
@@ -600,16 +726,17 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
   DevBuf err(ctx);
   int* e = derr;
   if (!e) {
-    MDS_TRY(err.alloc(ctx, sizeof(int)));
+    MDS_TRY(err.alloc(ctx, 2 * sizeof(int)));
     e = err.as<int>();
   }
-  MDS_CUDA(ctx, cudaMemsetAsync(e, 0, sizeof(int), ctx->stream));
+  MDS_CUDA(ctx, cudaMemsetAsync(e, 0, 2 * sizeof(int), ctx->stream));  // error code, work counter
   const float s = tc_scale(pl.prec);
   const uint32_t idesc = umma_idesc_f16(TC_M, TC_N, pl.prec == MDS_PREC_FP16X3 ? 0 : 1);
   ctx->stats.launches++;
   k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
-                                                       &fit == &ref ? 1 : 0, cand, cand_n, e);
+                                                       &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
+                                                       skip ? skip->prad : nullptr, dense, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
   int herr = 0;
@@ -617,4 +744,85 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
   MDS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (herr) return mds_fail(ctx, MDS_ERR_TIMEOUT, "tensor-core screen: a bounded wait timed out (role %d)", herr);
   return MDS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// tile skipping: pivots, radii and the dense pivot pass
+// ---------------------------------------------------------------------------
+// copy the deviations and records of the frames idx[] (pivots)
+__global__ void k_gather_frames(const float* __restrict__ A, const float* __restrict__ R, const int* __restrict__ idx,
+                                int n, int Ap, float* __restrict__ Ao, float* __restrict__ Ro) {
+  const int t = blockIdx.x;
+  if (t >= n) return;
+  const int f = idx[t];
+  for (int e = threadIdx.x; e < 3 * Ap; e += blockDim.x) Ao[(int64_t)t * 3 * Ap + e] = A[(int64_t)f * 3 * Ap + e];
+  for (int e = threadIdx.x; e < MDS_REC; e += blockDim.x) Ro[(int64_t)t * MDS_REC + e] = R[(int64_t)f * MDS_REC + e];
+}
+
+// prad[T] >= max over frames j of column tile T of RMSD(j, pivot T): the
+// distance of the two superposed copies, |a_j - a_p| (one feasible
+// superposition, so an upper bound of the minimum), rounded up.
+__global__ void k_tile_radius(const float* __restrict__ A, int Nr, int Ap, const int* __restrict__ idx,
+                              float* __restrict__ prad) {
+  __shared__ float wmax[8];
+  const int T = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float4* ap = reinterpret_cast<const float4*>(A + (int64_t)idx[T] * 3 * Ap);
+  float best = 0.0f;
+  for (int g = warp; g < TC_FR_N; g += blockDim.x >> 5) {
+    const int j = T * TC_FR_N + g;
+    if (j >= Nr) break;
+    const float4* aj = reinterpret_cast<const float4*>(A + (int64_t)j * 3 * Ap);
+    float acc = 0.0f;
+    for (int q = lane; q < 3 * Ap / 4; q += 32) {
+      const float4 u = __ldg(aj + q), v = __ldg(ap + q);
+      const float d0 = u.x - v.x, d1 = u.y - v.y, d2 = u.z - v.z, d3 = u.w - v.w;
+      acc = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc))));
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    best = fmaxf(best, acc);
+  }
+  if (lane == 0) wmax[warp] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, wmax[w]);
+    prad[T] = sqrtf(m) * (1.0f + 1e-5f) + 1e-7f;  // FP32 sums: round up
+  }
+}
+
+// Pivot of every column tile of the reference set (its middle frame), the
+// pivots' operands and records, and the tiles' radii: once per reference set.
+int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv) {
+  const int Nr = pl.nref, Ap = pl.Ap;
+  const int nC = (Nr + TC_FR_N - 1) / TC_FR_N;
+  cudaStream_t s = ctx->stream;
+  std::vector<int> piv(nC);
+  for (int T = 0; T < nC; ++T) piv[T] = std::min(T * TC_FR_N + TC_FR_N / 2, Nr - 1);
+  DevBuf dpiv(ctx);
+  MDS_TRY(dpiv.alloc(ctx, sizeof(int) * nC));
+  MDS_TRY(pv.A.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nC));
+  MDS_TRY(pv.R.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nC));
+  MDS_TRY(pv.rad.alloc(ctx, sizeof(float) * nC));
+  MDS_CUDA(ctx, cudaMemcpyAsync(dpiv.p, piv.data(), sizeof(int) * nC, cudaMemcpyHostToDevice, s));
+  ctx->stats.launches += 2;
+  k_gather_frames<<<nC, 128, 0, s>>>(Ar, Rr, dpiv.as<int>(), nC, Ap, pv.A.as<float>(), pv.R.as<float>());
+  k_tile_radius<<<nC, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), pv.rad.as<float>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  pv.nC = nC;
+  KnnRmsPlan pp = pl;
+  pp.nref = nC;
+  MDS_TRY(tc_prepare(ctx, pp, pv.A.as<float>(), nC, pv.tc, 1));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));  // dpiv is released on return
+  return MDS_OK;
+}
+
+// Lower bounds of RMSD from every fit frame to every pivot (the screen in
+// dense mode over the pivots) into lb [nC][nfit]. With derr (2 ints) the call
+// does not synchronise and can be captured in a CUDA graph.
+int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
+                   const TcPivots& pv, float* lb, int* derr) {
+  KnnRmsPlan pp = pl;
+  pp.nref = pv.nC;
+  return launch_screen_tc(ctx, pp, fit, pv.tc, recf, pv.R.as<float>(), nfit, 32, 1, nullptr, nullptr, derr,
+                          nullptr, lb);
 }

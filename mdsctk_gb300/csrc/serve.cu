@@ -99,13 +99,13 @@ struct Request {
 struct Slot {
   mds_ctx* ctx = nullptr;
   int cap = 0;
-  DevBuf raw, A, R, cand, cand_n, out_d, out_i, flagged, nflag, derr, ext;
+  DevBuf raw, A, R, cand, cand_n, out_d, out_i, flagged, nflag, derr, ext, lb;
   TcOperands tcq;
   float* h_raw = nullptr;
   double* h_d = nullptr;
   double* h_ext = nullptr;
   int* h_i = nullptr;
-  int* h_small = nullptr;  // [0] flagged rows, [1] screen error
+  int* h_small = nullptr;  // [0] flagged rows, [1] screen error, [2] pivot-pass error
   int* h_flagrows = nullptr;
   cudaEvent_t done = nullptr;
   std::map<int, cudaGraphExec_t> graphs;
@@ -128,6 +128,7 @@ struct mds_server {
   unsigned prec = MDS_PREC_FP32;
   float tm = 0;
   DevBuf dmass, dswn, dmu, dM0, Y, E, A, R, dZ, ddinv, dlam;
+  TcPivots pv;  // landmark pivots for tile skipping (pv.nC = 0: off)
   TcOperands tc;
   std::vector<double> evals;
   std::list<Slot> slots;  // slots own device buffers and never move
@@ -178,8 +179,16 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
   if (S->prec != MDS_PREC_FP32) {
     nseg = std::min(tc_choose_nseg(c, pl, bucket), S->nseg_max);
     MDS_TRY(tc_prepare(c, pl, sl.A.as<float>(), bucket, sl.tcq, 0));
+    TcSkip sk;
+    if (S->pv.nC > 0) {  // tile skipping: bounds of the batch's frames to the landmark pivots
+      MDS_TRY(tc_skip_bounds(c, pl, sl.tcq, sl.R.as<float>(), bucket, S->pv, sl.lb.as<float>(),
+                             sl.derr.as<int>() + 2));
+      sk.pivlb = sl.lb.as<float>();
+      sk.prad = S->pv.rad.as<float>();
+    }
     MDS_TRY(launch_screen_tc(c, pl, sl.tcq, S->tc, sl.R.as<float>(), S->R.as<float>(), bucket, S->Kp, nseg,
-                             sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), sl.derr.as<int>()));
+                             sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), sl.derr.as<int>(),
+                             S->pv.nC > 0 ? &sk : nullptr));
   } else {
     nseg = std::min(choose_nseg_fp32(bucket, c->num_sms, S->n), S->nseg_max);
     MDS_CUDA(c, cudaMemsetAsync(sl.derr.p, 0, sizeof(int), c->stream));
@@ -203,6 +212,8 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
                               cudaMemcpyDeviceToHost, c->stream));
   MDS_CUDA(c, cudaMemcpyAsync(sl.h_small, sl.nflag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MDS_CUDA(c, cudaMemcpyAsync(sl.h_small + 1, sl.derr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MDS_CUDA(c, cudaMemcpyAsync(sl.h_small + 2, sl.derr.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost,
+                              c->stream));
   return MDS_OK;
 }
 
@@ -211,7 +222,7 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
 // extension is recomputed with the others.
 static int finish_batch(mds_server* S, Slot& sl) {
   mds_ctx* c = sl.ctx;
-  if (sl.h_small[1]) return mds_fail(c, MDS_ERR_TIMEOUT, "screen reported a timed-out wait");
+  if (sl.h_small[1] || sl.h_small[2]) return mds_fail(c, MDS_ERR_TIMEOUT, "screen reported a timed-out wait");
   int nf = sl.h_small[0];
   if (nf <= 0) return MDS_OK;
   std::vector<int> rows(nf);
@@ -404,6 +415,7 @@ static size_t slot_bytes(const mds_server* S, int cap) {
   b += ((size_t)cap / 40 + 1) * 128 * 2 * ap * 2;            // split operands
   b += (size_t)cap * S->nseg_max * S->segstride * 8 + (size_t)cap * S->nseg_max * 4;
   b += (size_t)cap * S->k * 12 + (size_t)cap * S->nev * 8 + (size_t)cap * 4;
+  b += (size_t)cap * S->pv.nC * 4;                            // pivot bounds
   return b + (64u << 20);
 }
 
@@ -473,7 +485,10 @@ static int build_model(mds_server* S, const float* hxyz, const float* hmass) {
   MDS_TRY(launch_prep(c, raw.as<float>(), n, natoms, Ap, S->dmass.as<float>(), S->dswn.as<float>(), tm,
                       S->dmu.as<float>(), S->dM0.as<double>(), (S->cfg.flags & MDS_NOFIT) ? 1 : 0, S->A.as<float>(),
                       S->R.as<float>()));
-  if (S->prec != MDS_PREC_FP32) MDS_TRY(tc_prepare(c, S->plan(n), S->A.as<float>(), n, S->tc, 1));
+  if (S->prec != MDS_PREC_FP32) {
+    MDS_TRY(tc_prepare(c, S->plan(n), S->A.as<float>(), n, S->tc, 1));
+    if ((n + 79) / 80 >= 4) MDS_TRY(tc_skip_pivots(c, S->plan(n), S->A.as<float>(), S->R.as<float>(), S->pv));
+  }
   MDS_CUDA(c, cudaStreamSynchronize(s));
   return MDS_OK;
 }
@@ -525,7 +540,9 @@ extern "C" int mds_server_create(const mds_server_config* cfg, const float* land
               sl.out_d.alloc(c, sizeof(double) * (size_t)cap * S->k) == MDS_OK &&
               sl.out_i.alloc(c, sizeof(int) * (size_t)cap * S->k) == MDS_OK &&
               sl.flagged.alloc(c, sizeof(int) * cap) == MDS_OK && sl.nflag.alloc(c, sizeof(int)) == MDS_OK &&
-              sl.derr.alloc(c, sizeof(int)) == MDS_OK && sl.ext.alloc(c, sizeof(double) * (size_t)cap * S->nev) == MDS_OK;
+              sl.derr.alloc(c, 4 * sizeof(int)) == MDS_OK &&
+              (S->pv.nC == 0 || sl.lb.alloc(c, sizeof(float) * (size_t)S->pv.nC * cap) == MDS_OK) &&
+              sl.ext.alloc(c, sizeof(double) * (size_t)cap * S->nev) == MDS_OK;
     if (!ok) {
       S->last_error = mds_last_error(c);
       return MDS_ERR_NOMEM;
@@ -565,12 +582,13 @@ extern "C" int mds_server_destroy(mds_server* S) {
     // buffers return to the slot context's cache, then the context frees them
     sl.raw.release(); sl.A.release(); sl.R.release(); sl.cand.release();
     sl.cand_n.release(); sl.out_d.release(); sl.out_i.release(); sl.flagged.release(); sl.nflag.release();
-    sl.derr.release(); sl.ext.release(); sl.tcq.A.release(); sl.tcq.B.release();
+    sl.derr.release(); sl.ext.release(); sl.tcq.A.release(); sl.tcq.B.release(); sl.lb.release();
     mds_destroy(sl.ctx);
   }
   S->dmass.release(); S->dswn.release(); S->dmu.release(); S->dM0.release(); S->Y.release(); S->E.release();
   S->A.release(); S->R.release(); S->dZ.release(); S->ddinv.release(); S->dlam.release(); S->tc.A.release();
   S->tc.B.release();
+  S->pv.A.release(); S->pv.R.release(); S->pv.rad.release(); S->pv.tc.A.release(); S->pv.tc.B.release();
   mds_destroy(S->main);
   delete S;
   return MDS_OK;

@@ -67,3 +67,20 @@ def test_knn_rms_k_clamp_and_tiny(ctx, oracle):
     _check_knn(d, i, od, oi)
     d, i = ctx.knn_rms(x[:1], None, m, 3)  # one frame: k = 0
     assert d.shape == (1, 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["bf16x3", "fp16x3"])
+def test_knn_rms_tile_skipping_exact(ctx, oracle, precision):
+    """Multi-basin data on enough column tiles that the tensor-core screen
+    skips tiles by the triangle inequality (pivot pass + main screen): the
+    result must still equal the FP64 oracle, self and query sets alike."""
+    x = synth.trajectory(2400, 64, seed=77, basins=6, dwell=120, drift_sigma=0.06)
+    q = synth.trajectory(300, 64, seed=78, basins=6, dwell=120, drift_sigma=0.06, off_manifold=0.1)
+    m = synth.uniform_masses(64)
+    for fit in (None, q):
+        d, i = ctx.knn_rms(x, fit, m, 20, precision=precision)
+        assert ctx.stats()["screen_launches"] == 2  # pivot pass + screen
+        od, oi = oracle.knn_rms(x, fit, m, 20)
+        assert np.max(np.abs(d - od)) <= 1e-4
+        assert np.mean(i == oi) > 0.999
