@@ -136,4 +136,4 @@ int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, co
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
                      int* cand_n, int* derr = nullptr, const TcSkip* skip = nullptr,
-                     float* dense = nullptr);
+                     float* dense = nullptr, float* rowthr = nullptr);

@@ -33,6 +33,8 @@
 // Block sum of N float partials: FP32 shuffle tree inside each warp (FP64
 // issues at a small fraction of the FP32 rate on this GPU), then the warps'
 // sums added in FP64 in warp order. red holds (blockDim/32) * N doubles.
+// red holds (blockDim/32 + 1) * N doubles; thread i < N forms sum i (the
+// only FP64 work) and every thread reads the N sums back.
 template <int N>
 __device__ __forceinline__ void block_sum_vecf(const float (&p)[N], double (&out)[N], double* red) {
   float v[N];
@@ -47,12 +49,14 @@ __device__ __forceinline__ void block_sum_vecf(const float (&p)[N], double (&out
 #pragma unroll
     for (int i = 0; i < N; ++i) red[w * N + i] = (double)v[i];
   __syncthreads();
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
+  if (threadIdx.x < N) {
     double s = 0;
-    for (int j = 0; j < nw; ++j) s += red[j * N + i];
-    out[i] = s;
+    for (int j = 0; j < nw; ++j) s += red[j * N + threadIdx.x];
+    red[nw * N + threadIdx.x] = s;
   }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < N; ++i) out[i] = red[nw * N + i];
   __syncthreads();
 }
 
@@ -1000,8 +1004,11 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
       sk.pivlb = lb.as<float>();
       sk.prad = pv.rad.as<float>();
     }
+    DevBuf rowthr(ctx);
+    MDS_TRY(rowthr.alloc(ctx, sizeof(float) * std::max(nfit, 1)));
     MDS_TRY(launch_screen_tc(ctx, pl, same ? tcr : tcf, tcr, Rfp, Rr.as<float>(), nfit, Kp, nseg,
-                             cand.as<uint64_t>(), cand_n.as<int>(), nullptr, skipping ? &sk : nullptr));
+                             cand.as<uint64_t>(), cand_n.as<int>(), nullptr, skipping ? &sk : nullptr, nullptr,
+                             rowthr.as<float>()));
     st.screen_launches = skipping ? 2 : 1;
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));

@@ -137,6 +137,7 @@ struct TcShared {
   float thr[TC_FR_M];
   float colrec[TC_FR_N * MDS_REC];  // records of the current column tile
   float rowrec[TC_FR_M * MDS_REC];  // records of the current row tile
+  float gthr[TC_FR_M];              // rows' global thresholds, refreshed per tile
 };
 
 // per-warp shared scratch: the radix-select histogram, and the final sort of a
@@ -277,7 +278,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
             int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
             const float* __restrict__ pivlb, const float* __restrict__ prad, float* __restrict__ dense,
-            uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
+            float* __restrict__ rowthr, uint64_t* __restrict__ candbuf, int* __restrict__ cand_n,
+            int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
   // Work items (row tile, column segment) are claimed dynamically by each
   // CTA's producer, which also decides which column tiles of the item to
@@ -291,6 +293,12 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   // of its list, which only decreases), no pair of the tile can enter the
   // lists, and every such pair's true RMSD^2 exceeds the final threshold the
   // recheck verifies against -- the tile is not computed.
+  //
+  // Row thresholds across segments (rowthr != null): each compaction lowers
+  // rowthr[row] to its segment's K'-th bound (atomicMin). Every segment then
+  // appends only below min(own threshold, rowthr), and the skip test uses it:
+  // a segment holding K' keys below rowthr exists, so the recheck's final
+  // threshold is at most rowthr and every pair left out lies above it.
   //
   // Dense mode (dense != null; the pivot pass): every pair's lower bound of
   // RMSD (sqrt of the screen value) is written to dense[j][i]; no lists.
@@ -384,7 +392,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             for (int r = lane; r < TC_FR_M; r += 32) {
               const int gi = rt * TC_FR_M + r;
               if (gi >= nfit) continue;
-              const float thr = *(volatile float*)&S->thr[r];
+              float thr = *(volatile float*)&S->thr[r];
+              if (rowthr) thr = fminf(thr, __ldcg(rowthr + gi));
               const float L = __ldg(pivlb + (int64_t)tile * nfit + gi) - rad;
               if (!(L > 0.0f && L * L > thr)) can = false;
             }
@@ -544,6 +553,11 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const int j = tile * TC_FR_N + e / MDS_REC;
         S->colrec[e] = (j < Nr) ? __ldg(recr + (int64_t)j * MDS_REC + e % MDS_REC) : 0.f;
       }
+      if (ew == 0)
+        for (int r = lane; r < TC_FR_M; r += 32) {
+          const int gi = rt * TC_FR_M + r;
+          S->gthr[r] = (rowthr && gi < nfit) ? __ldcg(rowthr + gi) : INF;
+        }
       if (!mbar_wait(&S->tfull[b], aph, abortf)) { ok = false; break; }
       tc_fence_after();
       if (!ep_sync(S, lane)) { ok = false; break; }
@@ -600,7 +614,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
               const float sv = screen_shifted_f32(G, rrec, cr, nofit != 0, guard * (rrec[15] + cr[15]));
               dense[(int64_t)j * nfit + grow] = sqrtf(fmaxf(sv, 0.0f));
             } else {
-              const float thr = *(volatile float*)&S->thr[rloc];
+              const float thr = fminf(*(volatile float*)&S->thr[rloc], S->gthr[rloc]);
               float sv = screen_shifted_f32(G, rrec, cr, nofit != 0, guard * (rrec[15] + cr[15]), thr);
               sv = fmaxf(sv, 0.0f);
               if (sv < thr) {
@@ -634,6 +648,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         if (lane == 0) {
           S->cnt[r] = Kp;
           S->thr[r] = t;
+          if (rowthr) atomicMin(reinterpret_cast<int*>(rowthr + gr), __float_as_int(t));  // t >= 0
         }
         __syncwarp();
       }
@@ -704,7 +719,7 @@ int tc_seg_stride() { return TC_CAPG; }
 
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
-                     int* cand_n, int* derr, const TcSkip* skip, float* dense) {
+                     int* cand_n, int* derr, const TcSkip* skip, float* dense, float* rowthr) {
   if (Kp + 2 * TC_FR_N > TC_CAPG)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen supports K' <= %d (k too large)",
                     TC_CAPG - 2 * TC_FR_N);
@@ -730,13 +745,15 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
     e = err.as<int>();
   }
   MDS_CUDA(ctx, cudaMemsetAsync(e, 0, 2 * sizeof(int), ctx->stream));  // error code, work counter
+  if (rowthr)  // 0x7f7f7f7f = 3.4e38: above every bound
+    MDS_CUDA(ctx, cudaMemsetAsync(rowthr, 0x7f, sizeof(float) * (size_t)nfit, ctx->stream));
   const float s = tc_scale(pl.prec);
   const uint32_t idesc = umma_idesc_f16(TC_M, TC_N, pl.prec == MDS_PREC_FP16X3 ? 0 : 1);
   ctx->stats.launches++;
   k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
-                                                       skip ? skip->prad : nullptr, dense, cand, cand_n, e);
+                                                       skip ? skip->prad : nullptr, dense, rowthr, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
   int herr = 0;

@@ -99,7 +99,7 @@ struct Request {
 struct Slot {
   mds_ctx* ctx = nullptr;
   int cap = 0;
-  DevBuf raw, A, R, cand, cand_n, out_d, out_i, flagged, nflag, derr, ext, lb;
+  DevBuf raw, A, R, cand, cand_n, out_d, out_i, flagged, nflag, derr, ext, lb, rowthr;
   TcOperands tcq;
   float* h_raw = nullptr;
   double* h_d = nullptr;
@@ -188,7 +188,7 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
     }
     MDS_TRY(launch_screen_tc(c, pl, sl.tcq, S->tc, sl.R.as<float>(), S->R.as<float>(), bucket, S->Kp, nseg,
                              sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), sl.derr.as<int>(),
-                             S->pv.nC > 0 ? &sk : nullptr));
+                             S->pv.nC > 0 ? &sk : nullptr, nullptr, sl.rowthr.as<float>()));
   } else {
     nseg = std::min(choose_nseg_fp32(bucket, c->num_sms, S->n), S->nseg_max);
     MDS_CUDA(c, cudaMemsetAsync(sl.derr.p, 0, sizeof(int), c->stream));
@@ -540,7 +540,7 @@ extern "C" int mds_server_create(const mds_server_config* cfg, const float* land
               sl.out_d.alloc(c, sizeof(double) * (size_t)cap * S->k) == MDS_OK &&
               sl.out_i.alloc(c, sizeof(int) * (size_t)cap * S->k) == MDS_OK &&
               sl.flagged.alloc(c, sizeof(int) * cap) == MDS_OK && sl.nflag.alloc(c, sizeof(int)) == MDS_OK &&
-              sl.derr.alloc(c, 4 * sizeof(int)) == MDS_OK &&
+              sl.derr.alloc(c, 4 * sizeof(int)) == MDS_OK && sl.rowthr.alloc(c, sizeof(float) * cap) == MDS_OK &&
               (S->pv.nC == 0 || sl.lb.alloc(c, sizeof(float) * (size_t)S->pv.nC * cap) == MDS_OK) &&
               sl.ext.alloc(c, sizeof(double) * (size_t)cap * S->nev) == MDS_OK;
     if (!ok) {
@@ -582,7 +582,7 @@ extern "C" int mds_server_destroy(mds_server* S) {
     // buffers return to the slot context's cache, then the context frees them
     sl.raw.release(); sl.A.release(); sl.R.release(); sl.cand.release();
     sl.cand_n.release(); sl.out_d.release(); sl.out_i.release(); sl.flagged.release(); sl.nflag.release();
-    sl.derr.release(); sl.ext.release(); sl.tcq.A.release(); sl.tcq.B.release(); sl.lb.release();
+    sl.derr.release(); sl.ext.release(); sl.tcq.A.release(); sl.tcq.B.release(); sl.lb.release(); sl.rowthr.release();
     mds_destroy(sl.ctx);
   }
   S->dmass.release(); S->dswn.release(); S->dmu.release(); S->dM0.release(); S->Y.release(); S->E.release();
