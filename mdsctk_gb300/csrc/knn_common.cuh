@@ -2,6 +2,8 @@
 // kNN pipelines (knn_rms.cu, knn_rms_tc.cu, knn_data.cu, knn_api.cu).
 #pragma once
 
+#include <cuda.h>
+
 #include "mds_common.cuh"
 
 // Screen guards: the lower bound of RMSD^2 is the screen value minus
@@ -116,6 +118,17 @@ int choose_nseg_fp32(int nfit, int num_sms, int nref);
 int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout);
 int tc_seg_stride();
 int tc_choose_nseg(mds_ctx* ctx, const KnnRmsPlan& pl, int nfit);
+// 2-D tensor map of a split hi|lo operand: rows x (2 * half) 16-bit values,
+// boxes of 32 x boxrows, 64-byte swizzle (knn_rms_tc.cu).
+int encode_map(mds_ctx* ctx, CUtensorMap* map, const void* ptr, int rows, int half, int boxrows, unsigned prec);
+
+// tensor-core screen of knn_data (knn_data_tc.cu)
+int tcv_max_kprime();
+int tcv_max_dp();
+int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref);
+int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
+                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n);
+
 // Tile skipping data of the tensor-core screen (knn_rms_tc.cu): lower
 // bounds of RMSD from every fit frame to the pivot of every column tile
 // (pivlb [ncoltiles][nfit]) and the tiles' radii (prad [ncoltiles]).

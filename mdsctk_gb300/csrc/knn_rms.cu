@@ -518,7 +518,7 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
 // (Cxx, Cyy, Czz, Cxy, Cxz, Cyz).
 __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restrict__ sx, const float* C6,
                               const float* __restrict__ Ar, int Ap, int natoms, const int* cj, int nc, bool nofit,
-                              float* sd) {
+                              float* sd, float* ssum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   // four atoms per lane and load (Ap is a multiple of 64; padding atoms are
   // zero in a_i, a_j and mu, so they add nothing)
@@ -552,16 +552,22 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
 #pragma unroll
     for (int i = 0; i < 10; ++i)
       for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
-    if (lane == 0) {
-      float r2 = v[0];
-      if (!nofit) {
-        const float* P = v + 1;  // P[3r+s] = sum x~_r d_s
-        r2 = shifted_rmsd2_f32(v[0], C6[0] - P[0], C6[1] - P[4], C6[2] - P[8], 2.0f * C6[3] - (P[1] + P[3]),
-                               2.0f * C6[4] - (P[2] + P[6]), 2.0f * C6[5] - (P[5] + P[7]), P[7] - P[5],
-                               P[2] - P[6], P[3] - P[1]);
-      }
-      sd[c] = sqrtf(fmaxf(r2, 0.0f));
+#pragma unroll
+    for (int i = 0; i < 10; ++i)
+      if (lane == i) ssum[c * 10 + i] = v[i];
+  }
+  __syncthreads();
+  // the eigenvalue solves, one pair per thread
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    const float* w = ssum + c * 10;
+    float r2 = w[0];
+    if (!nofit) {
+      const float* P = w + 1;  // P[3r+s] = sum x~_r d_s
+      r2 = shifted_rmsd2_f32(w[0], C6[0] - P[0], C6[1] - P[4], C6[2] - P[8], 2.0f * C6[3] - (P[1] + P[3]),
+                             2.0f * C6[4] - (P[2] + P[6]), 2.0f * C6[5] - (P[5] + P[7]), P[7] - P[5], P[2] - P[6],
+                             P[3] - P[1]);
     }
+    sd[c] = sqrtf(fmaxf(r2, 0.0f));
   }
   __syncthreads();
 }
@@ -570,7 +576,7 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
 // K' keys, recheck, select k+1. mode 1: every reference is a candidate
 // (exact row). mode 2 (full matrix): write every exact distance in reference
 // order. Output: out_d/out_i rows of width `width` at row index grow.
-__global__ void __launch_bounds__(RC_THREADS)
+__global__ void __launch_bounds__(RC_THREADS, 4)
 k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const float* __restrict__ mu, int nrows,
           const int* __restrict__ rowlist, int Nr, int Ap, int natoms, int nofit, int mode,
           const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int segstride, int Kp, int k,
@@ -584,6 +590,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
   __shared__ int s_total;
   __shared__ double s_red[32 * 6];
   __shared__ float C6[6];
+  __shared__ float ssum[RC_CHUNK * 10];  // per candidate: D, P[9]
 
   int lr = blockIdx.x;
   if (lr >= nrows) return;
@@ -614,7 +621,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
       int nc = min(RC_CHUNK, Nr - base);
       for (int c = threadIdx.x; c < nc; c += blockDim.x) cj[c] = base + c;
       __syncthreads();
-      recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd);
+      recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd, ssum);
       for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         out_d[(int64_t)grow * Nr + base + c] = (double)sd[c] * 10.0;
         out_i[(int64_t)grow * Nr + base + c] = base + c;
@@ -674,7 +681,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
     for (int c = threadIdx.x; c < nc; c += blockDim.x)
       cj[c] = (mode == 0) ? mds_key_index(keys[base + c]) : base + c;
     __syncthreads();
-    recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd);
+    recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd, ssum);
     // place the chunk after the current k1 best and re-sort
     for (int c = threadIdx.x; c < RC_CHUNK; c += blockDim.x)
       top[k1 + c] = (c < nc) ? mds_pack_key(sd[c], cj[c]) : MDS_KEY_INF;

@@ -39,6 +39,7 @@
 #include "knn_common.cuh"
 #include "qcp.cuh"
 #include "tc_ptx.cuh"
+#include "tc_select.cuh"
 
 #define TC_FR_M 40
 #define TC_FR_N 80
@@ -48,7 +49,7 @@
 #define TC_STAGES 4
 #define TC_THREADS 576
 #define TC_EPI_WARPS 16
-#define TC_CAPG 512
+// TC_CAPG (keys per list) comes from tc_select.cuh
 #define TC_A_BYTES (TC_M * TC_KB * 2)
 #define TC_B_BYTES (TC_N * TC_KB * 2)
 #define TC_STAGE_BYTES (2 * TC_A_BYTES + 2 * TC_B_BYTES)
@@ -194,83 +195,6 @@ __device__ __forceinline__ int tile_order(int i, int t0, int t1, int td) {
   if (i <= 2 * m) return (i & 1) ? td + (i + 1) / 2 : td - i / 2;
   const int j = i - 2 * m;
   return (Rn > L) ? td + m + j : td - m - j;
-}
-
-// Keep the Kp smallest of the n (<= TC_CAPG) keys in src (unsorted, in
-// src[0..Kp)) and return the largest kept value: a most-significant-digit
-// radix select over the 64-bit keys (8-bit digits, stopping as soon as the
-// digit bucket holding the Kp-th key is kept whole), then a ballot
-// compaction. hist: 256 ints of this warp's shared scratch.
-__device__ float warp_select_keep(uint64_t* src, int n, int Kp, int* hist, int lane) {
-  constexpr int PER = TC_CAPG / 32;
-  uint64_t kv[PER];
-#pragma unroll
-  for (int i = 0; i < PER; ++i) {
-    const int x = lane + 32 * i;
-    kv[i] = (x < n) ? src[x] : MDS_KEY_INF;
-  }
-  uint64_t prefix = 0, mask = 0;
-  int need = Kp;
-  for (int pass = 7; pass >= 0; --pass) {
-    const int sh = pass * 8;
-    for (int b = lane; b < 256; b += 32) hist[b] = 0;
-    __syncwarp();
-#pragma unroll
-    for (int i = 0; i < PER; ++i)
-      if ((kv[i] & mask) == prefix) atomicAdd(&hist[(int)((kv[i] >> sh) & 255u)], 1);
-    __syncwarp();
-    int c[8], loc = 0;
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      c[b] = hist[8 * lane + b];
-      loc += c[b];
-    }
-    int inc = loc;
-    for (int o = 1; o < 32; o <<= 1) {
-      int t = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += t;
-    }
-    const int exc = inc - loc;
-    int digit = -1, before = 0, cnt = 0;
-    if (exc < need && need <= inc) {
-      int acc = exc;
-#pragma unroll
-      for (int b = 0; b < 8; ++b) {
-        if (digit < 0 && acc + c[b] >= need) {
-          digit = 8 * lane + b;
-          before = acc;
-          cnt = c[b];
-        }
-        acc += c[b];
-      }
-    }
-    const unsigned own = __ballot_sync(0xffffffffu, digit >= 0);
-    const int src_lane = __ffs(own) - 1;
-    digit = __shfl_sync(0xffffffffu, digit, src_lane);
-    before = __shfl_sync(0xffffffffu, before, src_lane);
-    cnt = __shfl_sync(0xffffffffu, cnt, src_lane);
-    __syncwarp();
-    need -= before;
-    prefix |= (uint64_t)digit << sh;
-    mask |= (uint64_t)255 << sh;
-    if (cnt == need) break;  // the whole bucket is kept
-  }
-  // keep every key whose processed digits are <= prefix's
-  int base = 0;
-  float vmax = 0.0f;
-#pragma unroll
-  for (int i = 0; i < PER; ++i) {
-    const bool keep = kv[i] != MDS_KEY_INF && (kv[i] & mask) <= prefix;
-    const unsigned bal = __ballot_sync(0xffffffffu, keep);
-    if (keep) {
-      src[base + __popc(bal & ((1u << lane) - 1u))] = kv[i];
-      vmax = fmaxf(vmax, mds_key_value(kv[i]));
-    }
-    base += __popc(bal);
-  }
-  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-  __syncwarp();
-  return vmax;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -675,8 +599,7 @@ typedef CUresult (*PFN_encodeTiled_t)(CUtensorMap*, CUtensorMapDataType, cuuint3
                                       CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
                                       CUtensorMapFloatOOBfill);
 
-static int encode_map(mds_ctx* ctx, CUtensorMap* map, const void* ptr, int rows, int Ap, int boxrows,
-                      unsigned prec) {
+int encode_map(mds_ctx* ctx, CUtensorMap* map, const void* ptr, int rows, int Ap, int boxrows, unsigned prec) {
   static PFN_encodeTiled_t fn = nullptr;
   if (!fn) {
     void* p = nullptr;

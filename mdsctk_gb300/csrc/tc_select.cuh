@@ -1,0 +1,84 @@
+// tc_select.cuh -- warp radix selection of the best K' keys of a candidate
+// list (the compaction step of the tensor-core screens).
+#pragma once
+
+#include "knn_common.cuh"
+
+#define TC_CAPG 512  // keys per (row, column segment) list
+// Keep the Kp smallest of the n (<= TC_CAPG) keys in src (unsorted, in
+// src[0..Kp)) and return the largest kept value: a most-significant-digit
+// radix select over the 64-bit keys (8-bit digits, stopping as soon as the
+// digit bucket holding the Kp-th key is kept whole), then a ballot
+// compaction. hist: 256 ints of this warp's shared scratch.
+__device__ inline float warp_select_keep(uint64_t* src, int n, int Kp, int* hist, int lane) {
+  constexpr int PER = TC_CAPG / 32;
+  uint64_t kv[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int x = lane + 32 * i;
+    kv[i] = (x < n) ? src[x] : MDS_KEY_INF;
+  }
+  uint64_t prefix = 0, mask = 0;
+  int need = Kp;
+  for (int pass = 7; pass >= 0; --pass) {
+    const int sh = pass * 8;
+    for (int b = lane; b < 256; b += 32) hist[b] = 0;
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+      if ((kv[i] & mask) == prefix) atomicAdd(&hist[(int)((kv[i] >> sh) & 255u)], 1);
+    __syncwarp();
+    int c[8], loc = 0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      c[b] = hist[8 * lane + b];
+      loc += c[b];
+    }
+    int inc = loc;
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    const int exc = inc - loc;
+    int digit = -1, before = 0, cnt = 0;
+    if (exc < need && need <= inc) {
+      int acc = exc;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        if (digit < 0 && acc + c[b] >= need) {
+          digit = 8 * lane + b;
+          before = acc;
+          cnt = c[b];
+        }
+        acc += c[b];
+      }
+    }
+    const unsigned own = __ballot_sync(0xffffffffu, digit >= 0);
+    const int src_lane = __ffs(own) - 1;
+    digit = __shfl_sync(0xffffffffu, digit, src_lane);
+    before = __shfl_sync(0xffffffffu, before, src_lane);
+    cnt = __shfl_sync(0xffffffffu, cnt, src_lane);
+    __syncwarp();
+    need -= before;
+    prefix |= (uint64_t)digit << sh;
+    mask |= (uint64_t)255 << sh;
+    if (cnt == need) break;  // the whole bucket is kept
+  }
+  // keep every key whose processed digits are <= prefix's
+  int base = 0;
+  float vmax = 0.0f;
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const bool keep = kv[i] != MDS_KEY_INF && (kv[i] & mask) <= prefix;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (keep) {
+      src[base + __popc(bal & ((1u << lane) - 1u))] = kv[i];
+      vmax = fmaxf(vmax, mds_key_value(kv[i]));
+    }
+    base += __popc(bal);
+  }
+  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  __syncwarp();
+  return vmax;
+}
+
