@@ -282,8 +282,8 @@ def run_pipeline(args):
         else:
             n, dim, k = 200_000, 64, 32
             x = synth.dihedral_vectors(n, dim, seed=SEED + 13).astype(np.float64)
-            out["config"] = {"workload": f"knn_data {n} x {dim} (f64), k={k}"}
-            d, i = timed("knn_data", lambda: c.knn_data(x, None, k), c)
+            out["config"] = {"workload": f"knn_data {n} x {dim} (f64), k={k}", "precision": args.precision}
+            d, i = timed("knn_data", lambda: c.knn_data(x, None, k, precision=args.precision), c)
             st["pairs_per_s"] = n * n / st["knn_data"]
             rows = np.linspace(0, n - 1, 256).astype(int)
             od, oi = O.knn_data(x, x[rows], k)

@@ -180,7 +180,8 @@ extern "C" int mds_knn_data(mds_ctx* ctx, const double* ref, int n_ref, const do
   const bool full = (flags & MDS_FULL) != 0, dev = (flags & MDS_DEVICE_IO) != 0;
   const bool corr = (flags & MDS_CORRELATION) != 0;
   const unsigned prec = flags & MDS_PREC_MASK;
-  if (prec != MDS_PREC_FP32) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "knn_data screen precision 0x%x", prec);
+  if (prec != MDS_PREC_FP32 && prec != MDS_PREC_BF16X3)
+    return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "knn_data screen precision 0x%x", prec);
   if (!fit) n_fit = n_ref;
   // knn_data.cpp:186-188: k clamped to N_ref - 1, k1 recomputed
   if (!full) {

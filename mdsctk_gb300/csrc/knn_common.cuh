@@ -95,12 +95,10 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
 // pieces of the knn_rms pipeline (knn_rms.cu), reused by the serving loop
 int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass,
                   const float* dswn, float tm, float* Y, double* E);
-// Centring + superposition of n raw frames in one kernel: deviations and
-// records only (knn_rms.cu).
+// Centring + superposition of n raw frames (three kernels, no scratch
+// buffer): deviations and records only (knn_rms.cu).
 int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
                 float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R);
-int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const float* dmu,
-                    const double* dM0, int nofit, float* A, float* R);
 int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit, std::vector<double>& mu,
                    double M0[9]);
 int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* recf,

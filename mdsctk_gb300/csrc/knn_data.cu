@@ -28,6 +28,7 @@
 #define DT_KC 32
 #define DT_THREADS 256
 #define DT_FS 36  // floats per vector per stage (32 + 4: bank spread, 16-byte rows)
+#define DT_MAX_KP 192  // largest K' whose pools (64 rows x (K' + 64) keys) fit in shared memory
 
 // ---------------------------------------------------------------------------
 // 1. per-vector preparation
@@ -343,8 +344,10 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
       }
   }
   if (threadIdx.x == 0 && mode == 0) {
+    // strict: a pair left out of the list has a lower bound >= tau, so only
+    // dk < tau proves that no left-out pair ties with or beats the k+1-th
     double dk = bval[k1 - 1];
-    if (!(dk <= (double)tau)) {
+    if (!(dk < (double)tau)) {
       int pos = atomicAdd(nflag, 1);
       flagged[pos] = grow;
     }
@@ -431,7 +434,24 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
     st.recheck_ms = ms;
     return MDS_OK;
   }
-  int Kp = std::min(mds_round_up(std::max(k + 1 + 32, (k + 1) * 3 / 2), 32), 448);
+  // K': the FP32 screen keeps a row's pool (K' + one tile) in shared memory,
+  // which holds at most DT_MAX_KP; the tensor-core screen keeps its lists in
+  // global memory and takes up to tcv_max_kprime()
+  const int kp_want = mds_round_up(std::max(k + 1 + 32, (k + 1) * 3 / 2), 32);
+  const bool tc = prec == MDS_PREC_BF16X3 && Dp <= tcv_max_dp() && kp_want <= tcv_max_kprime();
+  int Kp = tc ? kp_want : std::min(kp_want, DT_MAX_KP);
+  if (Kp < k + 1 + 16) {
+    // k too large for a screen to pay off: every row is rechecked exactly
+    st.kprime = 0;
+    st.passes = 1;
+    MDS_TRY(recheck(nfit, nullptr, 1, nullptr, nullptr, 1, 1));
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    st.recheck_ms = ms;
+    return MDS_OK;
+  }
   const int nrt = (nfit + DT_TM - 1) / DT_TM, nct = (nref + DT_TN - 1) / DT_TN;
   int nseg = 1;
   {
@@ -445,18 +465,24 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
       if (eff >= 0.95) break;
     }
   }
-  const float guard = corr ? 1.0f / 65536.0f : 1.0f / 65536.0f;
+  const float guard = MDS_GUARD_FP32;
+  if (tc) nseg = tcv_choose_nseg(ctx, nfit, nref);
   DevBuf cand(ctx), cand_n(ctx), rows(ctx);
   MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)nfit * nseg * Kp));
   MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)nfit * nseg));
   size_t smem = screen_dot_smem(Kp);
-  MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  st.launches++;
   st.screen_launches = 1;
-  k_screen_dot<<<nrt * nseg, DT_THREADS, smem, s>>>(xf, Xr.as<float>(), nfp, Nrm.as<float>(), nfit, nullptr, nref,
-                                                     Dp, corr, guard, Kp, nseg, cand.as<uint64_t>(),
-                                                     cand_n.as<int>());
-  MDS_CUDA(ctx, cudaGetLastError());
+  if (tc) {
+    MDS_TRY(launch_screen_tcv(ctx, xf, nfp, nfit, Xr.as<float>(), Nrm.as<float>(), nref, Dp, corr, Kp, nseg, same,
+                              cand.as<uint64_t>(), cand_n.as<int>()));
+  } else {
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    st.launches++;
+    k_screen_dot<<<nrt * nseg, DT_THREADS, smem, s>>>(xf, Xr.as<float>(), nfp, Nrm.as<float>(), nfit, nullptr,
+                                                       nref, Dp, corr, guard, Kp, nseg, cand.as<uint64_t>(),
+                                                       cand_n.as<int>());
+    MDS_CUDA(ctx, cudaGetLastError());
+  }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
   MDS_TRY(recheck(nfit, nullptr, 0, cand.as<uint64_t>(), cand_n.as<int>(), nseg, Kp));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
@@ -480,12 +506,13 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
     MDS_CUDA(ctx, cudaMemcpyAsync(rows.p, hrows.data(), sizeof(int) * hflag, cudaMemcpyHostToDevice, s));
     MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
     st.passes++;
-    Kp = std::min(Kp * 4, 448);
-    if (Kp >= nref || st.passes > 3) {
+    const int wider = std::min(Kp * 4, DT_MAX_KP);
+    if (wider <= Kp || wider >= nref || st.passes > 3) {
       MDS_TRY(recheck(hflag, rows.as<int>(), 1, nullptr, nullptr, 1, 1));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
       break;
     }
+    Kp = wider;
     MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)hflag * Kp));
     MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)hflag));
     smem = screen_dot_smem(Kp);

@@ -1,0 +1,495 @@
+// knn_data_tc.cu -- the all-pairs candidate screen of knn_data on the 5th
+// generation tensor cores (precision flag MDS_PREC_BF16X3).
+//
+// x.y is one GEMM of the vectors split into BF16 parts, x = hi + lo:
+// hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM. The screen value of a
+// pair is a lower bound of its squared distance,
+//   Euclidean:   |x|^2 + |y|^2 - 2 x.y - c (|x|^2 + |y|^2)
+//   correlation: (1 - z_x.z_y) / 2     - c (|z_x|^2 + |z_y|^2)
+// (z: standardised vectors, |z| = 1; c = MDS_GUARD_TC covers the rounding of
+// the split products and of the FP32 operands).
+//
+// Work item = (row pair tile of 256 fit vectors, column segment). The row
+// pair tile stays resident in shared memory for the whole item (two 128-row
+// MMA operands); reference vectors stream through a 3-4 stage TMA pipeline in
+// tiles of 128 (64-byte swizzle, K-blocks of 32 dimensions). Per tile the MMA
+// warp writes two 128 x 128 FP32 accumulators; TMEM holds two such pairs
+// (512 columns) so the epilogue of one tile overlaps the MMAs of the next.
+// Warp 0 claims items from a global counter, loads the resident rows and the
+// reference tiles and publishes (item, tile) tasks in a ring; warp 1 issues
+// the MMAs; 16 epilogue warps (4 per TMEM lane quarter: row half x column
+// half) append the pairs below the row's threshold to the row's list in
+// global memory and cut a list back to K' by a warp radix select when it
+// fills. Rows share their thresholds across column segments through
+// rowthr. Every mbarrier wait is bounded; the epilogue warps synchronise on a
+// hardware named barrier that carries each wait's outcome, so on a timeout
+// all roles leave together: the kernel records an error, drains, frees its
+// TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "knn_common.cuh"
+#include "tc_ptx.cuh"
+#include "tc_select.cuh"
+
+#define TV_ROWS 256         // fit vectors per work item (two MMA row tiles)
+#define TV_N 128            // reference vectors per column tile
+#define TV_KB 32            // dimensions per K-block (64-byte rows)
+#define TV_THREADS 576      // producer, MMA, 16 epilogue warps
+#define TV_EPI 16
+#define TV_SUB_BYTES 8192   // one 128-row x 32-dimension BF16 operand tile
+#define TV_STAGE_BYTES (2 * TV_SUB_BYTES)  // reference hi + lo of one K-block
+#define TV_MAXST 4
+#define TV_TQ 8
+#define TV_SCR 256          // keys of per-warp shared scratch
+#define TV_MAX_DP 128
+
+// FP32 vectors [n][Dp] -> BF16 split rows [rows][hi(Dp) | lo(Dp)], rows
+// beyond n zero.
+__global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows, __nv_bfloat16* __restrict__ out) {
+  const int64_t total = (int64_t)rows * Dp;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / Dp;
+    const int d = (int)(e % Dp);
+    const float x = (r < n) ? X[r * Dp + d] : 0.0f;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+    out[r * 2 * Dp + d] = hi;
+    out[r * 2 * Dp + Dp + d] = lo;
+  }
+}
+
+struct TvShared {
+  uint64_t full[TV_MAXST], empty[TV_MAXST], tfull[2], tempty[2], afull, aempty, done;
+  uint64_t tq_full[TV_TQ], tq_empty[TV_TQ];
+  int2 task[TV_TQ];
+  uint32_t tmem_base;
+  int abortf;
+  int cnt[TV_ROWS];
+  float thr[TV_ROWS], gthr[TV_ROWS], rowc[TV_ROWS];
+  alignas(16) float colc[TV_N];  // read as float4
+};
+
+static size_t tv_smem_bytes(int Dp, int nst) {
+  return (size_t)TV_ROWS * 2 * Dp * 2 + (size_t)nst * TV_STAGE_BYTES + sizeof(TvShared) +
+         (size_t)TV_EPI * TV_SCR * 8 + 1024;
+}
+
+// Column tiles of a segment [t0, t1) in visiting order: outward from td.
+__device__ __forceinline__ int tv_tile_order(int i, int t0, int t1, int td) {
+  const int L = td - t0, Rn = t1 - 1 - td, m = min(L, Rn);
+  if (i == 0) return td;
+  if (i <= 2 * m) return (i & 1) ? td + (i + 1) / 2 : td - i / 2;
+  const int j = i - 2 * m;
+  return (Rn > L) ? td + m + j : td - m - j;
+}
+
+
+// One fit row's list: keep the Kp best, sort them and write the segment's
+// candidate list (called by the warp that owns the row).
+__device__ __forceinline__ void tv_publish(uint64_t* src, int n, int Kp, uint64_t* scratch, uint64_t* dst,
+                                           int* dst_n, int lane) {
+  n = min(n, TC_CAPG);
+  if (n > Kp) {
+    warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
+    n = Kp;
+  }
+  if (n <= TV_SCR) {
+    for (int e = lane; e < n; e += 32) scratch[e] = src[e];
+    __syncwarp();
+    warp_bitonic_sort(scratch, n, TV_SCR, lane);
+    for (int e = lane; e < n; e += 32) dst[e] = scratch[e];
+  } else {
+    warp_bitonic_sort(src, n, TC_CAPG, lane);
+    for (int e = lane; e < n; e += 32) dst[e] = src[e];
+  }
+  if (lane == 0) *dst_n = n;
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(TV_THREADS, 1)
+k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+             const float* __restrict__ nf, const float* __restrict__ nr, int nfit, int Nr, int Dp, int nst,
+             int corr, float guard, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
+             float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
+             int* __restrict__ cand_n, int* __restrict__ err) {
+  // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
+  // work: [gridDim.x][TV_ROWS][TC_CAPG] list buffers of the CTAs;
+  // candout: [nfit][nseg][Kp] sorted lists, cand_n [nfit][nseg] their sizes.
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  const int nkb = Dp / TV_KB;
+  unsigned char* arows = base;                                   // [2][nkb][hi, lo] 8 KB tiles
+  unsigned char* stages = base + (size_t)TV_ROWS * 2 * Dp * 2;   // nst x (hi, lo)
+  TvShared* S = reinterpret_cast<TvShared*>(stages + (size_t)nst * TV_STAGE_BYTES);
+  uint64_t* scratch_all = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(S) + sizeof(TvShared));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ncoltiles = (Nr + TV_N - 1) / TV_N;
+  const float INF = __int_as_float(0x7f800000);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < nst; ++s) {
+      mbar_init(&S->full[s], 1);
+      mbar_init(&S->empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&S->tfull[b], 1);
+      mbar_init(&S->tempty[b], TV_EPI);
+    }
+    mbar_init(&S->afull, 1);
+    mbar_init(&S->aempty, 1);
+    mbar_init(&S->done, 1);
+    for (int i = 0; i < TV_TQ; ++i) {
+      mbar_init(&S->tq_full[i], 1);
+      mbar_init(&S->tq_empty[i], 1 + TV_EPI);
+    }
+    S->abortf = 0;
+    mbar_fence_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(&S->tmem_base, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S->tmem_base;
+  volatile int* abortf = &S->abortf;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      uint32_t stage = 0, phase = 0, qs = 0, na = 0;
+      bool ok = true;
+      auto push = [&](int item, int tile) -> bool {
+        const uint32_t slot = qs % TV_TQ, ph = (qs / TV_TQ) & 1;
+        ++qs;
+        if (!mbar_wait(&S->tq_empty[slot], ph ^ 1, abortf, 1000000000ull, 1024)) return false;
+        S->task[slot] = make_int2(item, tile);
+        mbar_arrive(&S->tq_full[slot]);
+        return true;
+      };
+      while (ok) {
+        const int item = atomicAdd(err + 1, 1);
+        if (item >= nitems) {
+          ok = push(-1, -1);
+          break;
+        }
+        const int rp = item / nseg, seg = item % nseg;
+        const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+        const int td = diag ? min(max((rp * TV_ROWS + TV_ROWS / 2) / TV_N, t0), t1 - 1) : t0;
+        // the resident rows: wait until the MMAs of the previous item are done
+        if (na > 0 && !mbar_wait(&S->aempty, (na - 1) & 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
+        mbar_expect_tx(&S->afull, (uint32_t)(TV_ROWS * 2 * Dp * 2));
+        for (int u = 0; u < 2; ++u)
+          for (int kb = 0; kb < nkb; ++kb)
+            for (int p = 0; p < 2; ++p)
+              tma_load_2d(arows + (size_t)((u * nkb + kb) * 2 + p) * TV_SUB_BYTES, &tmA, &S->afull,
+                          p * Dp + kb * TV_KB, (2 * rp + u) * 128);
+        ++na;
+        for (int ti = 0; ti < t1 - t0 && ok; ++ti) {
+          const int tile = tv_tile_order(ti, t0, t1, td);
+          if (!(ok = push(item, tile))) break;
+          for (int kb = 0; kb < nkb; ++kb) {
+            if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
+            unsigned char* st = stages + stage * TV_STAGE_BYTES;
+            mbar_expect_tx(&S->full[stage], TV_STAGE_BYTES);
+            tma_load_2d(st, &tmB, &S->full[stage], kb * TV_KB, tile * TV_N);
+            tma_load_2d(st + TV_SUB_BYTES, &tmB, &S->full[stage], Dp + kb * TV_KB, tile * TV_N);
+            if (++stage == (uint32_t)nst) { stage = 0; phase ^= 1; }
+          }
+        }
+        if (ok) ok = push(item, -1);
+      }
+      if (!ok) {
+        atomicMax(err, 1);
+        *abortf = 1;
+        // let the copies in flight land before the CTA exits
+        volatile int dummy = 0;
+        if (na > 0) mbar_wait(&S->afull, (na - 1) & 1, &dummy, 50000000ull);
+        for (int s = 0; s < nst; ++s) mbar_wait(&S->full[s], 0, &dummy, 50000000ull);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      uint32_t stage = 0, phase = 0, acc = 0, na = 0;
+      int cur = -1;
+      bool ok = true;
+      const uint32_t abase = smem_u32(arows), sbase = smem_u32(stages);
+      for (uint32_t qs = 0; ok; ++qs) {
+        const uint32_t slot = qs % TV_TQ, qph = (qs / TV_TQ) & 1;
+        if (!mbar_wait(&S->tq_full[slot], qph, abortf, 1000000000ull, 64)) { ok = false; break; }
+        const volatile int* tv = reinterpret_cast<volatile int*>(&S->task[slot]);
+        const int2 t = make_int2(tv[0], tv[1]);
+        mbar_arrive(&S->tq_empty[slot]);
+        if (t.x < 0) break;
+        if (t.y < 0) {  // end of the item: the resident rows are free when these MMAs are done
+          umma_commit(&S->aempty);
+          continue;
+        }
+        if (t.x != cur) {
+          cur = t.x;
+          if (!mbar_wait(&S->afull, na & 1, abortf, 1000000000ull, 64)) { ok = false; break; }
+          ++na;
+        }
+        const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
+        if (!mbar_wait(&S->tempty[b], aph ^ 1, abortf, 1000000000ull, 64)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tbase + b * 256;
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&S->full[stage], phase, abortf, 1000000000ull, 64)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t st = sbase + stage * TV_STAGE_BYTES;
+#pragma unroll
+          for (int ks = 0; ks < TV_KB / 16; ++ks) {
+            const uint64_t bhi = umma_desc_sw64(st + ks * 32);
+            const uint64_t blo = umma_desc_sw64(st + TV_SUB_BYTES + ks * 32);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+              const uint32_t at = abase + ((u * nkb + kb) * 2) * TV_SUB_BYTES + ks * 32;
+              const uint64_t ahi = umma_desc_sw64(at);
+              const uint64_t alo = umma_desc_sw64(at + TV_SUB_BYTES);
+              umma_f16(d + u * TV_N, ahi, bhi, idesc, (kb | ks) != 0);
+              umma_f16(d + u * TV_N, ahi, blo, idesc, 1);
+              umma_f16(d + u * TV_N, alo, bhi, idesc, 1);
+            }
+          }
+          umma_commit(&S->empty[stage]);
+          if (++stage == (uint32_t)nst) { stage = 0; phase ^= 1; }
+        }
+        if (ok) umma_commit(&S->tfull[b]);
+        ++acc;
+      }
+      if (!ok) {
+        atomicMax(err, 2);
+        *abortf = 1;
+      }
+      umma_commit(&S->done);
+      volatile int dummy = 0;
+      mbar_wait(&S->done, 0, &dummy, 200000000ull);
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int ew = warp - 2;
+    const int q = warp & 3;          // TMEM lane quarter: rows 32q .. 32q + 31 of a row tile
+    const int u = (ew >> 2) >> 1;    // row tile of the pair
+    const int half = (ew >> 2) & 1;  // column half: 64 * half .. + 63
+    const int r = u * 128 + 32 * q + lane;  // this lane's row of the item
+    uint64_t* scratch = scratch_all + ew * TV_SCR;
+    // rows this warp compacts and publishes: 16 of its lane quarter
+    const int own0 = u * 128 + 32 * q + 16 * half;
+    uint64_t* lists = work + (size_t)blockIdx.x * TV_ROWS * TC_CAPG;
+    const float mul = corr ? -0.5f : -2.0f;
+    uint32_t acc = 0;
+    bool ok = true;
+    int cur = -1, rp = 0, seg = 0;
+    // The epilogue warps meet at named barrier 1 three times per tile: after
+    // the task read (every warp has finished the previous tile, its
+    // compactions and any publishing), after the accumulator is ready, and
+    // after the pairs are appended (before compaction). A failed bounded
+    // wait is ANDed into the first two, so all warps leave together.
+    for (uint32_t qs = 0;; ++qs) {
+      const uint32_t slot = qs % TV_TQ, qph = (qs / TV_TQ) & 1;
+      const bool got = mbar_wait(&S->tq_full[slot], qph, abortf);
+      int2 task = make_int2(-1, -1);
+      if (got) {
+        const volatile int* tv = reinterpret_cast<volatile int*>(&S->task[slot]);
+        task = make_int2(tv[0], tv[1]);
+      }
+      __syncwarp();
+      if (!bar_and(1, TV_EPI * 32, got)) { ok = false; break; }
+      if (lane == 0) mbar_arrive(&S->tq_empty[slot]);
+      if (task.x < 0) break;
+      if (task.x != cur) {
+        cur = task.x;
+        rp = cur / nseg;
+        seg = cur % nseg;
+        if (half == 0) {  // one warp of each row quarter resets its 32 rows
+          const int g = rp * TV_ROWS + r;
+          S->cnt[r] = 0;
+          S->thr[r] = INF;
+          const float rn = (g < nfit) ? __ldg(nf + g) : 0.0f;
+          S->rowc[r] = (g >= nfit) ? INF : corr ? 0.5f - guard * rn : rn * (1.0f - guard);
+        }
+      }
+      if (task.y < 0) {
+        // end of the item: keep, sort and publish the rows this warp owns
+        // (their appends and compactions are complete; the next task's
+        // barrier separates this from the next item's resets)
+        for (int x = 0; x < 16; ++x) {
+          const int rr = own0 + x;
+          const int g = rp * TV_ROWS + rr;
+          if (g >= nfit) break;
+          tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt[rr], Kp, scratch,
+                     candout + ((int64_t)g * nseg + seg) * Kp, cand_n + (int64_t)g * nseg + seg, lane);
+        }
+        continue;
+      }
+      const int tile = task.y;
+      const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
+      // the column terms of this tile and the rows' shared thresholds
+      for (int e = ew * 32 + lane; e < TV_N; e += TV_EPI * 32) {
+        const int j = tile * TV_N + e;
+        const float cn = (j < Nr) ? __ldg(nr + j) : 0.0f;
+        S->colc[e] = (j >= Nr) ? INF : corr ? -guard * cn : cn * (1.0f - guard);
+      }
+      if (half == 0) {
+        const int g = rp * TV_ROWS + r;
+        S->gthr[r] = (g < nfit) ? __ldcg(rowthr + g) : INF;
+      }
+      const bool ready = mbar_wait(&S->tfull[b], aph, abortf);
+      tc_fence_after();
+      __syncwarp();
+      if (!bar_and(1, TV_EPI * 32, ready)) { ok = false; break; }
+      const float rc = S->rowc[r];
+      // screen value = rc + colc - 2g (or - g/2); pass if below the row's threshold
+      const float lim = fminf(S->thr[r], S->gthr[r]) - rc;
+      uint64_t* rowbuf = lists + (size_t)r * TC_CAPG;
+      const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256 + u * TV_N + 64 * half;
+      const float4* colc4 = reinterpret_cast<const float4*>(S->colc + 64 * half);
+#pragma unroll 1
+      for (int cc = 0; cc < 2; ++cc) {
+        uint32_t gv[32];
+        tmem_ld32(tq + 32 * cc, gv);
+        tmem_wait_ld();
+#pragma unroll
+        for (int t4 = 0; t4 < 8; ++t4) {
+          const float4 c4 = colc4[cc * 8 + t4];
+          const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const float v = fmaf(mul, __uint_as_float(gv[4 * t4 + t]), cv[t]);
+            if (v < lim) {
+              const int pos = atomicAdd(&S->cnt[r], 1);
+              const int j = tile * TV_N + 64 * half + 32 * cc + 4 * t4 + t;
+              if (pos < TC_CAPG)
+                rowbuf[pos] = mds_pack_key(fmaxf(v + rc, 0.0f), j);
+              else
+                atomicMax(err, 4);  // cannot happen: compaction keeps room for a whole tile
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S->tempty[b]);
+      ++acc;
+      bar_named(1, TV_EPI * 32);  // every append of this tile is done
+      // compaction of the owned rows whose lists are full (or first filled)
+      for (int x = 0; x < 16; ++x) {
+        const int rr = own0 + x;
+        const int g = rp * TV_ROWS + rr;
+        if (g >= nfit) break;
+        const int n = S->cnt[rr];
+        if (!(n > Kp && (n > TC_CAPG - TV_N || S->thr[rr] == INF))) continue;
+        const float t = warp_select_keep(lists + (size_t)rr * TC_CAPG, min(n, TC_CAPG), Kp,
+                                         reinterpret_cast<int*>(scratch), lane);
+        if (lane == 0) {
+          S->cnt[rr] = Kp;
+          S->thr[rr] = t;
+          atomicMin(reinterpret_cast<int*>(rowthr + g), __float_as_int(t));
+        }
+        __syncwarp();
+      }
+    }
+    if (!ok && lane == 0) {
+      atomicMax(err, 3);
+      *abortf = 1;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tbase, 512);
+  }
+}
+
+// Largest K' of the vector screen: a list keeps room for one more tile.
+int tcv_max_kprime() { return TC_CAPG - TV_N; }
+// Largest padded dimension: the resident rows must fit in shared memory.
+int tcv_max_dp() { return TV_MAX_DP; }
+
+// Column segments per row pair tile: enough work items that the last wave of
+// the dynamic schedule is short (about 16 items per SM), at most 8.
+int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref) {
+  const int nrp = (nfit + TV_ROWS - 1) / TV_ROWS, nct = (nref + TV_N - 1) / TV_N;
+  int nseg = (16 * ctx->num_sms + nrp - 1) / nrp;
+  return std::max(1, std::min({nseg, 8, nct}));
+}
+
+// The tensor-core screen of knn_data. Xf/Xr: FP32 vectors [n][Dp] (Dp a
+// multiple of 32, at most TV_MAX_DP), nf/nr their squared norms. same: Xf is
+// Xr (a set screened against itself; the visit starts at the diagonal).
+// Writes the sorted candidate lists candout [nfit][nseg][Kp] and cand_n
+// [nfit][nseg].
+int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
+                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n) {
+  if (Kp > tcv_max_kprime()) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: K' too large");
+  if (Dp % TV_KB || Dp > TV_MAX_DP)
+    return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: padded dimension %d", Dp);
+  const int ncoltiles = (nref + TV_N - 1) / TV_N;
+  if (nseg < 1 || nseg > ncoltiles) return mds_fail(ctx, MDS_ERR_INTERNAL, "bad segment count %d", nseg);
+  cudaStream_t s = ctx->stream;
+  const int rowsA = (nfit + TV_ROWS - 1) / TV_ROWS * TV_ROWS, rowsB = ncoltiles * TV_N;
+  const int rowsS = std::max(rowsA, rowsB);
+  DevBuf A(ctx), B(ctx), work(ctx), rowthr(ctx), err(ctx);
+  auto split = [&](const float* X, int n, int rows, DevBuf& out) -> int {
+    MDS_TRY(out.alloc(ctx, sizeof(__nv_bfloat16) * 2 * (size_t)Dp * rows));
+    const int64_t total = (int64_t)rows * Dp;
+    const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 16);
+    ctx->stats.launches++;
+    k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    return MDS_OK;
+  };
+  const void* pA;
+  if (same) {  // one split array serves both roles (rows padded to the larger tiling)
+    MDS_TRY(split(Xr, nref, rowsS, B));
+    pA = B.p;
+  } else {
+    MDS_TRY(split(Xr, nref, rowsB, B));
+    MDS_TRY(split(Xf, nfit, rowsA, A));
+    pA = A.p;
+  }
+  CUtensorMap mA, mB;
+  MDS_TRY(encode_map(ctx, &mA, pA, same ? rowsS : rowsA, Dp, 128, MDS_PREC_BF16X3));
+  MDS_TRY(encode_map(ctx, &mB, B.p, same ? rowsS : rowsB, Dp, TV_N, MDS_PREC_BF16X3));
+  const int nitems = rowsA / TV_ROWS * nseg;
+  const int grid = std::min(nitems, ctx->num_sms);
+  MDS_TRY(work.alloc(ctx, sizeof(uint64_t) * (size_t)grid * TV_ROWS * TC_CAPG));
+  MDS_TRY(rowthr.alloc(ctx, sizeof(float) * (size_t)std::max(nfit, 1)));
+  MDS_TRY(err.alloc(ctx, 2 * sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, 2 * sizeof(int), s));
+  MDS_CUDA(ctx, cudaMemsetAsync(rowthr.p, 0x7f, sizeof(float) * (size_t)nfit, s));
+  const int nst = (Dp <= 96) ? 4 : 3;
+  const size_t smem = tv_smem_bytes(Dp, nst);
+  static bool attr_done = false;
+  static size_t attr_limit = 0;
+  MDS_TRY(mds_allow_dyn_smem(ctx, k_screen_tcv, &attr_done, &attr_limit));
+  if (smem > attr_limit)
+    return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "vector screen needs %zu bytes of shared memory", smem);
+  const uint32_t idesc = umma_idesc_f16(128, TV_N, 1);
+  ctx->stats.launches++;
+  k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nf, nr, nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC,
+                                              idesc, Kp, nseg, nitems, same ? 1 : 0, rowthr.as<float>(),
+                                              work.as<uint64_t>(), candout, cand_n, err.as<int>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  int herr = 0;
+  MDS_CUDA(ctx, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  if (herr)
+    return mds_fail(ctx, herr == 4 ? MDS_ERR_INTERNAL : MDS_ERR_TIMEOUT,
+                    "tensor-core vector screen failed (code %d)", herr);
+  return MDS_OK;
+}

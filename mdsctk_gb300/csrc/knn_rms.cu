@@ -4,13 +4,15 @@
 // :186-206 and the OpenMP row loop with permutation::sort(k+1) :213-293).
 //
 // Pipeline (all on ctx->stream):
-//  1. k_center      reset_x centring (knn_rms.cpp:189,199) of every frame,
-//                   scaled by sqrt(w/M) so that every sum below is per unit
-//                   mass; layout [frame][xyz][Ap] float (atom-major, Ap =
-//                   natoms rounded up to 64, zero padded).
-//  2. k_prealign    superpose every frame once onto a template mu (first
-//                   reference frame in its principal axes), store deviations
-//                   a = R y - mu and the per-frame screen record.
+//  1. k_center      reset_x centring (knn_rms.cpp:189,199) of the first
+//                   reference frame, from which the template mu (that frame
+//                   in its principal axes) is built; coordinates scaled by
+//                   sqrt(w/M) so that every sum below is per unit mass;
+//                   layout [frame][xyz][Ap] float (atom-major, Ap = natoms
+//                   rounded up to 64, zero padded).
+//  2. k_prep_sums, k_prep_rot, k_prep_out
+//                   centre every frame and superpose it once onto mu, store
+//                   deviations a = R y - mu and the per-frame screen record.
 //  3. screen        all pairs: deviation Gram + shifted QCP lower bound of
 //                   RMSD^2, fused per-row top-K' (never an N x N matrix).
 //                   FP32 CUDA cores (k_screen_fp32) or tcgen05 split BF16
@@ -124,107 +126,33 @@ __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int A
 }
 
 // ---------------------------------------------------------------------------
-// 2. superposition onto the template
+// 2. centring and superposition onto the template, in three kernels
 // ---------------------------------------------------------------------------
-// mu: [3][Ap] float (template, principal axes). M0: sum mu mu^T (9 doubles).
-// dev: [n][3][Ap] float deviations a = R y - mu (FP32 screen operand).
-// rec: [n][MDS_REC] screen record. The rotation only has to be a proper
-// rotation (x~ = mu + a is an exact rigid copy of the frame for any R; a
-// better fit only makes |a| smaller), so per-atom work is FP32; the 3x3 sums
-// are reduced in FP64 and the quaternion is solved in FP64 by one thread.
-__global__ void k_prealign(const float* __restrict__ Y, const double* __restrict__ E, int n,
-                           int natoms, int Ap, const float* __restrict__ mu,
-                           const double* __restrict__ M0, int nofit, float* __restrict__ dev,
-                           float* __restrict__ rec) {
-  __shared__ double red[32 * 10];
-  __shared__ float Rsh[9];
-  int f = blockIdx.x;
-  if (f >= n) return;
-  const float* y = Y + (int64_t)f * 3 * Ap;
-  if (!nofit) {
-    float p[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
-      float yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
-      float mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
-      for (int c = 0; c < 3; ++c)
-        for (int d = 0; d < 3; ++d) p[3 * c + d] = fmaf(yc[c], mc[d], p[3 * c + d]);
-    }
-    double s[9];
-    for (int i = 0; i < 9; ++i) s[i] = p[i];
-    block_sum_vec<9>(s, red);
-    if (threadIdx.x == 0) {
-      double emu = M0[0] + M0[4] + M0[8];
-      double R[9];
-      qcp_rotation_fp64(s, 0.5 * (E[f] + emu), R);
-      for (int i = 0; i < 9; ++i) Rsh[i] = (float)R[i];
-    }
-  } else if (threadIdx.x == 0) {
-    for (int i = 0; i < 9; ++i) Rsh[i] = (i % 4 == 0) ? 1.0f : 0.0f;
-  }
-  __syncthreads();
-  float R[9];
-  for (int i = 0; i < 9; ++i) R[i] = Rsh[i];
-  float ea = 0.f, u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  float* o = dev + (int64_t)f * 3 * Ap;
-  for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
-    if (a < natoms) {
-      float yc[3] = {y[a], y[Ap + a], y[2 * Ap + a]};
-      float mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
-      float av[3];
-      for (int c = 0; c < 3; ++c) {
-        float ry = fmaf(R[3 * c], yc[0], fmaf(R[3 * c + 1], yc[1], R[3 * c + 2] * yc[2]));
-        av[c] = ry - mc[c];
-        o[c * Ap + a] = av[c];
-      }
-      for (int c = 0; c < 3; ++c) {
-        ea = fmaf(av[c], av[c], ea);
-        for (int d = 0; d < 3; ++d) u[3 * c + d] = fmaf(av[c], mc[d], u[3 * c + d]);
-      }
-    } else {
-      for (int c = 0; c < 3; ++c) o[c * Ap + a] = 0.0f;
-    }
-  }
-  double eu[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
-  block_sum_vec<10>(eu, red);
-  ea = (float)eu[0];
-  if (threadIdx.x == 0) {
-    const double* U = eu + 1;
-    float* r = rec + (int64_t)f * MDS_REC;
-    double sxx = U[0], syy = U[4], szz = U[8];
-    double sxy = 0.5 * (U[1] + U[3]), sxz = 0.5 * (U[2] + U[6]), syz = 0.5 * (U[5] + U[7]);
-    r[0] = (float)(M0[0] + sxx);
-    r[1] = (float)(M0[4] + syy);
-    r[2] = (float)(M0[8] + szz);
-    r[3] = (float)(0.5 * (M0[1] + M0[3]) + sxy);
-    r[4] = (float)(0.5 * (M0[2] + M0[6]) + sxz);
-    r[5] = (float)(0.5 * (M0[5] + M0[7]) + syz);
-    r[6] = (float)sxx; r[7] = (float)syy; r[8] = (float)szz;
-    r[9] = (float)sxy; r[10] = (float)sxz; r[11] = (float)syz;
-    r[12] = (float)(U[5] - U[7]);
-    r[13] = (float)(U[6] - U[2]);
-    r[14] = (float)(U[1] - U[3]);
-    r[15] = (float)eu[0];
-  }
-}
+// The centred, mass-scaled coordinates y = (x - com) sqrt(w/M) of a frame are
+// recomputed from the raw frame in each pass, so only the deviations
+// a = R y - mu [n][3][Ap] and the screen records [n][MDS_REC] are written.
+// The rotation only has to be a proper rotation (x~ = mu + a is an exact
+// rigid copy of the frame for any R; a better fit only makes |a| smaller), so
+// the per-atom work is FP32 with FP64 sums across warps. The quaternion is
+// solved in FP64 by one thread per frame in a kernel of its own, so the
+// per-atom kernels keep few registers and many frames in flight per SM.
+// Between the kernels the record row carries com (0..2) and the sums of the
+// rotation fit (3..12, then R in 3..11).
 
-// Centring and superposition in one kernel (one block per frame): the
-// centred, mass-scaled coordinates y = (x - com) sqrt(w/M) are recomputed from
-// the raw frame (L1-resident) in each of three passes -- centre of mass;
-// covariance with the template and |y|^2; deviations a = R y - mu with the
-// record sums -- so only the deviations and records are written. Arithmetic
-// as k_center and k_prealign.
-__global__ void k_prep(const float* __restrict__ raw, int n, int natoms, int Ap, const float* __restrict__ mass,
-                       const float* __restrict__ swn, float tm, const float* __restrict__ mu,
-                       const double* __restrict__ M0, int nofit, float* __restrict__ dev,
-                       float* __restrict__ rec) {
+// Pass 1 + 2 (one block per frame): centre of mass, then |y|^2 and the
+// covariance sum y mu^T.
+__global__ void __launch_bounds__(128) k_prep_sums(const float* __restrict__ raw, int n, int natoms, int Ap,
+                                                   const float* __restrict__ mass, const float* __restrict__ swn,
+                                                   float tm, const float* __restrict__ mu, int nofit,
+                                                   float* __restrict__ rec) {
   __shared__ double red[32 * 10];
-  __shared__ float Rsh[9];
   const int f = blockIdx.x;
   if (f >= n) return;
   const float* x = raw + (int64_t)f * natoms * 3;
   float com[3];
   {
     float p[3] = {0.f, 0.f, 0.f};
+#pragma unroll 4
     for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
       const float mm = mass[a];
       for (int c = 0; c < 3; ++c) p[c] = fmaf(mm, x[3 * a + c], p[c]);
@@ -233,31 +161,55 @@ __global__ void k_prep(const float* __restrict__ raw, int n, int natoms, int Ap,
     block_sum_vecf<3>(p, sc, red);
     for (int c = 0; c < 3; ++c) com[c] = (float)(sc[c] / (double)tm);
   }
-  if (!nofit) {
-    float p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // |y|^2, sum y mu^T
-    for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
-      const float w = swn[a];
-      float yc[3], mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
-      for (int c = 0; c < 3; ++c) yc[c] = (x[3 * a + c] - com[c]) * w;
-      p[0] = fmaf(yc[0], yc[0], fmaf(yc[1], yc[1], fmaf(yc[2], yc[2], p[0])));
-      for (int c = 0; c < 3; ++c)
-        for (int d = 0; d < 3; ++d) p[1 + 3 * c + d] = fmaf(yc[c], mc[d], p[1 + 3 * c + d]);
-    }
-    double sv[10];
-    block_sum_vecf<10>(p, sv, red);
-    if (threadIdx.x == 0) {
-      double R[9];
-      qcp_rotation_fp64(sv + 1, 0.5 * (sv[0] + M0[0] + M0[4] + M0[8]), R);
-      for (int i = 0; i < 9; ++i) Rsh[i] = (float)R[i];
-    }
-  } else if (threadIdx.x == 0) {
-    for (int i = 0; i < 9; ++i) Rsh[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+  float* r = rec + (int64_t)f * MDS_REC;
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; ++c) r[c] = com[c];
+  if (nofit) return;
+  float p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // |y|^2, sum y mu^T
+#pragma unroll 2
+  for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
+    const float w = swn[a];
+    float yc[3], mc[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]};
+    for (int c = 0; c < 3; ++c) yc[c] = (x[3 * a + c] - com[c]) * w;
+    p[0] = fmaf(yc[0], yc[0], fmaf(yc[1], yc[1], fmaf(yc[2], yc[2], p[0])));
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 3; ++d) p[1 + 3 * c + d] = fmaf(yc[c], mc[d], p[1 + 3 * c + d]);
   }
-  __syncthreads();
+  double sv[10];
+  block_sum_vecf<10>(p, sv, red);
+  if (threadIdx.x == 0)
+    for (int i = 0; i < 10; ++i) r[3 + i] = (float)sv[i];
+}
+
+// The rotation of every frame (one thread per frame, FP64 QCP): record
+// entries 3..12 (|y|^2, y mu^T) -> 3..11 (R, row-major).
+__global__ void k_prep_rot(int n, const double* __restrict__ M0, float* __restrict__ rec) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n) return;
+  float* r = rec + (int64_t)f * MDS_REC;
+  double S[9], R[9];
+  for (int i = 0; i < 9; ++i) S[i] = r[4 + i];
+  qcp_rotation_fp64(S, 0.5 * ((double)r[3] + M0[0] + M0[4] + M0[8]), R);
+  for (int i = 0; i < 9; ++i) r[3 + i] = (float)R[i];
+}
+
+// Pass 3 (one block per frame): deviations a = R y - mu and the record sums
+// (|a|^2, a mu^T with the template's M0), which replace the record row.
+__global__ void __launch_bounds__(128) k_prep_out(const float* __restrict__ raw, int n, int natoms, int Ap,
+                                                  const float* __restrict__ swn, const float* __restrict__ mu,
+                                                  const double* __restrict__ M0, int nofit, float* __restrict__ dev,
+                                                  float* __restrict__ rec) {
+  __shared__ double red[32 * 10];
+  const int f = blockIdx.x;
+  if (f >= n) return;
+  const float* x = raw + (int64_t)f * natoms * 3;
+  float* r = rec + (int64_t)f * MDS_REC;
+  const float com[3] = {r[0], r[1], r[2]};
   float R[9];
-  for (int i = 0; i < 9; ++i) R[i] = Rsh[i];
+  for (int i = 0; i < 9; ++i) R[i] = nofit ? ((i % 4 == 0) ? 1.0f : 0.0f) : r[3 + i];
   float ea = 0.f, u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float* o = dev + (int64_t)f * 3 * Ap;
+#pragma unroll 2
   for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
     if (a < natoms) {
       const float w = swn[a];
@@ -278,10 +230,9 @@ __global__ void k_prep(const float* __restrict__ raw, int n, int natoms, int Ap,
   }
   const float eup[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
   double eu[10];
-  block_sum_vecf<10>(eup, eu, red);
+  block_sum_vecf<10>(eup, eu, red);  // every thread has read the record row before this barrier
   if (threadIdx.x == 0) {
     const double* U = eu + 1;
-    float* r = rec + (int64_t)f * MDS_REC;
     double sxx = U[0], syy = U[4], szz = U[8];
     double sxy = 0.5 * (U[1] + U[3]), sxz = 0.5 * (U[2] + U[6]), syz = 0.5 * (U[5] + U[7]);
     r[0] = (float)(M0[0] + sxx);
@@ -520,16 +471,22 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
                               const float* __restrict__ Ar, int Ap, int natoms, const int* cj, int nc, bool nofit,
                               float* sd, float* ssum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // four atoms per lane and load (Ap is a multiple of 64; padding atoms are
-  // zero in a_i, a_j and mu, so they add nothing)
+  // A warp takes four candidates at a time, eight lanes each; the lanes of
+  // the four groups read the same atoms of the row (shared memory
+  // broadcast), so the row is read once per four candidates. Four atoms per
+  // lane and load (Ap is a multiple of 64; padding atoms are zero in a_i,
+  // a_j and mu, so they add nothing).
+  const int grp = lane >> 3, gl = lane & 7;
   const int Ap4 = Ap >> 2;
   const float4* sa4 = reinterpret_cast<const float4*>(sa);
   const float4* sx4 = reinterpret_cast<const float4*>(sx);
   (void)natoms;
-  for (int c = warp; c < nc; c += nw) {
-    const float4* aj4 = reinterpret_cast<const float4*>(Ar + (int64_t)cj[c] * 3 * Ap);
+  for (int c0 = 4 * warp; c0 < nc; c0 += 4 * nw) {
+    const int c = c0 + grp;
+    const bool valid = c < nc;
+    const float4* aj4 = reinterpret_cast<const float4*>(Ar + (int64_t)cj[valid ? c : c0] * 3 * Ap);
     float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // D, P[9]
-    for (int q = lane; q < Ap4; q += 32) {
+    for (int q = gl; q < Ap4; q += 8) {
       const float4 ia = sa4[q], ib = sa4[Ap4 + q], ic = sa4[2 * Ap4 + q];
       const float4 ja = __ldg(aj4 + q), jb = __ldg(aj4 + Ap4 + q), jc = __ldg(aj4 + 2 * Ap4 + q);
       const float d0[4] = {ia.x - ja.x, ia.y - ja.y, ia.z - ja.z, ia.w - ja.w};
@@ -549,12 +506,15 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
         }
       }
     }
+    // sums over the eight lanes of each group (one shuffle serves all four)
 #pragma unroll
     for (int i = 0; i < 10; ++i)
-      for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+      for (int o = 4; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    if (valid && gl == 0) {
+      float2* w2 = reinterpret_cast<float2*>(ssum + c * 10);
 #pragma unroll
-    for (int i = 0; i < 10; ++i)
-      if (lane == i) ssum[c * 10 + i] = v[i];
+      for (int i = 0; i < 5; ++i) w2[i] = make_float2(v[2 * i], v[2 * i + 1]);
+    }
   }
   __syncthreads();
   // the eigenvalue solves, one pair per thread
@@ -590,7 +550,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
   __shared__ int s_total;
   __shared__ double s_red[32 * 6];
   __shared__ float C6[6];
-  __shared__ float ssum[RC_CHUNK * 10];  // per candidate: D, P[9]
+  __shared__ __align__(16) float ssum[RC_CHUNK * 10];  // per candidate: D, P[9] (float2 stores)
 
   int lr = blockIdx.x;
   if (lr >= nrows) return;
@@ -843,20 +803,13 @@ int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, co
   return MDS_OK;
 }
 
-int launch_prealign(mds_ctx* ctx, const float* Y, const double* E, int n, int natoms, int Ap, const float* dmu,
-                    const double* dM0, int nofit, float* A, float* R) {
-  if (n <= 0) return MDS_OK;
-  ctx->stats.launches++;
-  k_prealign<<<n, 128, 0, ctx->stream>>>(Y, E, n, natoms, Ap, dmu, dM0, nofit, A, R);
-  MDS_CUDA(ctx, cudaGetLastError());
-  return MDS_OK;
-}
-
 int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
                 float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R) {
   if (n <= 0) return MDS_OK;
-  ctx->stats.launches++;
-  k_prep<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dmass, dswn, tm, dmu, dM0, nofit, A, R);
+  ctx->stats.launches += nofit ? 2 : 3;
+  k_prep_sums<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dmass, dswn, tm, dmu, nofit, R);
+  if (!nofit) k_prep_rot<<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, dM0, R);
+  k_prep_out<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dswn, dmu, dM0, nofit, A, R);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }

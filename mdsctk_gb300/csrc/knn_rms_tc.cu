@@ -133,7 +133,6 @@ struct TcShared {
   int thr_item;      // the item whose rows' thresholds thr[] holds (-1: none)
   uint32_t tmem_base;
   int abortf;
-  int bar_count, bar_gen;
   int cnt[TC_FR_M];
   float thr[TC_FR_M];
   float colrec[TC_FR_N * MDS_REC];  // records of the current column tile
@@ -151,38 +150,6 @@ __device__ __forceinline__ float sel3(int i, float a0, float a1, float a2) {
   return i == 0 ? a0 : (i == 1 ? a1 : a2);
 }
 
-// Barrier of the eight epilogue warps (spin on a generation counter,
-// bounded). Returns false if it timed out or the kernel aborts.
-__device__ __forceinline__ bool ep_sync(TcShared* S, int lane) {
-  __threadfence_block();
-  __syncwarp();
-  int ok = 1;
-  if (lane == 0) {
-    volatile int* gen = &S->bar_gen;
-    int g = *gen;
-    __threadfence_block();
-    if (atomicAdd(&S->bar_count, 1) == TC_EPI_WARPS - 1) {
-      S->bar_count = 0;
-      __threadfence_block();
-      atomicAdd(&S->bar_gen, 1);
-    } else {
-      uint64_t t0 = gtimer_ns();
-      while (*gen == g) {
-        __nanosleep(64);
-        if (*(volatile int*)&S->abortf) { ok = 0; break; }
-        if (gtimer_ns() - t0 > 1000000000ull) {
-          *(volatile int*)&S->abortf = 1;
-          ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence_block();
-  }
-  ok = __shfl_sync(0xffffffffu, ok, 0);
-  __syncwarp();
-  return ok != 0;
-}
 
 // Column tiles of a segment [t0, t1) in the order the screen visits them:
 // outward from tile td (td, td+1, td-1, td+2, ...). For a frame set screened
@@ -252,8 +219,6 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       mbar_init(&S->tq_empty[i], 1 + TC_EPI_WARPS);
     }
     S->abortf = 0;
-    S->bar_count = 0;
-    S->bar_gen = 0;
     S->thr_item = -1;
     mbar_fence_init();
   }
@@ -415,17 +380,25 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     bool ok = true;
     int cur = -1, rt = 0, seg = 0, grow = 0, ntile = 0;
     bool rowok = false;
-    for (uint32_t qs = 0; ok; ++qs) {
+    // The epilogue warps meet at named barrier 1 three times per tile: after
+    // the task read (every warp has finished the previous tile, its
+    // compactions and any publishing), after the accumulator is ready, and
+    // after the pairs are appended (before compaction). A failed bounded
+    // wait is ANDed into the first two, so all warps leave together.
+    for (uint32_t qs = 0;; ++qs) {
       const uint32_t slot = qs % TC_TQ, qph = (qs / TC_TQ) & 1;
-      if (!mbar_wait(&S->tq_full[slot], qph, abortf)) { ok = false; break; }
-      const volatile int* tv = reinterpret_cast<volatile int*>(&S->task[slot]);
-      const int2 task = make_int2(tv[0], tv[1]);
+      const bool got = mbar_wait(&S->tq_full[slot], qph, abortf);
+      int2 task = make_int2(-1, -1);
+      if (got) {
+        const volatile int* tv = reinterpret_cast<volatile int*>(&S->task[slot]);
+        task = make_int2(tv[0], tv[1]);
+      }
       __syncwarp();
+      if (!bar_and(1, TC_EPI_WARPS * 32, got)) { ok = false; break; }
       if (lane == 0) mbar_arrive(&S->tq_empty[slot]);
       if (task.x < 0) break;
       if (task.x != cur) {
-        // start of an item: row records and this warp's rows' lists (every
-        // warp has passed the previous item's final barrier)
+        // start of an item: row records and this warp's rows' lists
         cur = task.x;
         rt = cur / nseg;
         seg = cur % nseg;
@@ -443,8 +416,9 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         }
       }
       if (task.y < 0) {
-        // end of the item: sort and publish this warp's rows
-        if (!ep_sync(S, lane)) { ok = false; break; }
+        // end of the item: sort and publish this warp's rows (their appends
+        // and compactions are complete; the next task's barrier separates
+        // this from the next item's resets)
         if (!dense)
           for (int fr = h; fr < 10; fr += 4) {
             const int r = q * 10 + fr;
@@ -466,13 +440,12 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             if (lane == 0) cand_n[(int64_t)gr * nseg + seg] = n;
             __syncwarp();
           }
-        if (!ep_sync(S, lane)) { ok = false; break; }
         continue;
       }
       const int tile = task.y;
       const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
       // column records of this tile (the previous tile's readers passed the
-      // end-of-tile barrier)
+      // task barrier)
       for (int e = ew * 32 + lane; e < TC_FR_N * MDS_REC; e += TC_EPI_WARPS * 32) {
         const int j = tile * TC_FR_N + e / MDS_REC;
         S->colrec[e] = (j < Nr) ? __ldg(recr + (int64_t)j * MDS_REC + e % MDS_REC) : 0.f;
@@ -482,9 +455,10 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
           const int gi = rt * TC_FR_M + r;
           S->gthr[r] = (rowthr && gi < nfit) ? __ldcg(rowthr + gi) : INF;
         }
-      if (!mbar_wait(&S->tfull[b], aph, abortf)) { ok = false; break; }
+      const bool ready = mbar_wait(&S->tfull[b], aph, abortf);
       tc_fence_after();
-      if (!ep_sync(S, lane)) { ok = false; break; }
+      __syncwarp();
+      if (!bar_and(1, TC_EPI_WARPS * 32, ready)) { ok = false; break; }
       if (ntile++ == 0 && ew == 0 && lane == 0) {
         __threadfence_block();
         *(volatile int*)&S->thr_item = cur;  // this item's thresholds are live
@@ -556,8 +530,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->tempty[b]);
       ++acc;
-      if (!ep_sync(S, lane)) { ok = false; break; }
       if (dense) continue;
+      bar_named(1, TC_EPI_WARPS * 32);  // every append of this tile is done
       // compaction of this warp's rows
       for (int fr = h; fr < 10; fr += 4) {
         const int r = q * 10 + fr;

@@ -33,6 +33,8 @@ int main(int argc, char** argv) {
   p.add("fit-file", 'f', cli::STRING, "Input:  Fitting data file (string:filename)");
   p.add("distance-file", 'd', cli::STRING, "Output: K-nn distances file (string:filename)", "distances.dat");
   p.add("index-file", 'i', cli::STRING, "Output: K-nn indices file (string:filename)", "indices.dat");
+  p.add("precision", 0, cli::STRING, "Input:  candidate screen: fp32 or bf16x3 (outputs are exact either way)",
+        "bf16x3");
   p.add("device", 0, cli::INT, "Input:  CUDA device (int)", "0");
   int pr = p.parse(argc, argv);
   if (pr == 1) return 1;
@@ -45,6 +47,13 @@ int main(int argc, char** argv) {
   }
   if (!p.is_set("vector-size")) {
     std::cout << "ERROR: --vector-size not supplied." << std::endl << std::endl;
+    ok = false;
+  }
+  unsigned prec = MDS_PREC_BF16X3;
+  const std::string ps = p.str("precision");
+  if (ps == "fp32") prec = MDS_PREC_FP32;
+  else if (ps != "bf16x3") {
+    std::cout << "ERROR: --precision must be fp32 or bf16x3" << std::endl;
     ok = false;
   }
   if (!ok) return -1;
@@ -84,7 +93,7 @@ int main(int argc, char** argv) {
   mds_ctx* ctx = nullptr;
   int rc = mds_create(p.i("device"), 0, &ctx);
   if (rc) return cli::fail(ctx, rc);
-  unsigned flags = (p.b("correlation") ? MDS_CORRELATION : 0u) | (sort ? 0u : MDS_FULL);
+  unsigned flags = (p.b("correlation") ? MDS_CORRELATION : 0u) | (sort ? 0u : MDS_FULL) | prec;
   int kk = sort ? std::max(0, std::min(k, nr - 1)) : nr;
   std::vector<double> d((size_t)nf * kk);
   std::vector<int32_t> idx((size_t)nf * kk);

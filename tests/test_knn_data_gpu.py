@@ -51,3 +51,93 @@ def test_knn_data_reference_fixtures(ctx, oracle, name, dim, k):
     d, i = ctx.knn_data(x, None, k)
     od, oi = oracle.knn_data(x, None, k)
     _check(d, i, od, oi)
+
+
+# ---------------------------------------------------------------------------
+# tensor-core screen (split BF16, precision "bf16x3"): the recheck makes the
+# output bit-identical to the oracle's whatever the screen keeps; these cases
+# cover the kernel's tiling edges (row pair tiles of 256, column tiles of
+# 128, K-blocks of 32 dimensions, 3 and 4 pipeline stages) and its fallbacks.
+@pytest.mark.gpu
+@pytest.mark.parametrize("corr", [False, True])
+def test_knn_data_tc_vonmises(ctx, oracle, corr):
+    x = synth.dihedral_vectors(700, 64, seed=3).astype(np.float64)
+    d, i = ctx.knn_data(x, None, 20, correlation=corr, precision="bf16x3")
+    st = ctx.stats()
+    od, oi = oracle.knn_data(x, None, 20, correlation=corr)
+    _check(d, i, od, oi)
+    assert st["rows_flagged"] == 0
+    assert st["launches"] == 4  # prep, BF16 split, tensor-core screen, recheck
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nref,nfit,dim,k", [(300, 77, 3, 10), (1000, 513, 100, 25), (129, 255, 32, 7),
+                                             (2000, 300, 17, 200)])
+def test_knn_data_tc_fit_vs_ref(ctx, oracle, nref, nfit, dim, k):
+    rng = np.random.default_rng(nref + dim)
+    ref = rng.normal(size=(nref, dim))
+    fit = rng.normal(size=(nfit, dim))
+    d, i = ctx.knn_data(ref, fit, k, precision="bf16x3")
+    st = ctx.stats()
+    od, oi = oracle.knn_data(ref, fit, k)
+    _check(d, i, od, oi)
+    assert st["launches"] == 6  # two preps, two splits, screen, recheck
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_ties_and_duplicates(ctx, oracle):
+    """Repeated vectors and zero vectors: exact ties at distance 0 and between
+    neighbours; the row guard must send rows whose k+1-th distance equals the
+    screen's cut to a wider pass."""
+    rng = np.random.default_rng(11)
+    base = rng.integers(-3, 4, size=(90, 8)).astype(np.float64)
+    x = np.concatenate([base, base, base[:40], np.zeros((30, 8))])
+    d, i = ctx.knn_data(x, None, 15, precision="bf16x3")
+    od, oi = oracle.knn_data(x, None, 15)
+    _check(d, i, od, oi)
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_matches_fp32_screen_large(ctx):
+    """5,000 x 64 von Mises vectors, k=32: both screens give the same output
+    (each is checked against the oracle at small sizes above)."""
+    x = synth.dihedral_vectors(5000, 64, seed=8).astype(np.float64)
+    d1, i1 = ctx.knn_data(x, None, 32, precision="bf16x3")
+    assert ctx.stats()["rows_flagged"] == 0
+    d0, i0 = ctx.knn_data(x, None, 32)
+    assert np.array_equal(d1, d0)
+    bad = np.argwhere(i1 != i0)
+    for r, c in bad:
+        assert np.sum(d0[r] == d0[r, c]) >= 2
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_fallback_shapes(ctx, oracle):
+    """Shapes outside the tensor-core screen's limits: a dimension above 128
+    runs the FP32 screen; a k whose K' exceeds both screens' list sizes is
+    rechecked exactly against every reference vector."""
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=(400, 130))
+    d, i = ctx.knn_data(x, None, 9, precision="bf16x3")
+    assert ctx.stats()["launches"] == 3  # prep, FP32 screen, recheck
+    od, oi = oracle.knn_data(x, None, 9)
+    _check(d, i, od, oi)
+    x = rng.normal(size=(600, 4))
+    for prec in ("bf16x3", "fp32"):
+        d, i = ctx.knn_data(x, None, 300, precision=prec)
+        st = ctx.stats()
+        assert st["launches"] == 2 and st["kprime"] == 0  # prep, exact recheck of every pair
+        od, oi = oracle.knn_data(x, None, 300)
+        _check(d, i, od, oi)
+
+
+@pytest.mark.gpu
+def test_knn_data_fp32_large_k(ctx, oracle):
+    """k = 150: K' is capped at the FP32 screen's pool size (192) and the rows
+    still come out exact."""
+    rng = np.random.default_rng(6)
+    x = rng.normal(size=(1500, 6))
+    d, i = ctx.knn_data(x, None, 150)
+    assert ctx.stats()["kprime"] == 192
+    od, oi = oracle.knn_data(x, None, 150)
+    _check(d, i, od, oi)
