@@ -17,14 +17,16 @@
 // (512 columns) so the epilogue of one tile overlaps the MMAs of the next.
 // Warp 0 claims items from a global counter, loads the resident rows and the
 // reference tiles and publishes (item, tile) tasks in a ring; warp 1 issues
-// the MMAs; 16 epilogue warps (4 per TMEM lane quarter: row half x column
-// half) append the pairs below the row's threshold to the row's list in
-// global memory and cut a list back to K' by a warp radix select when it
-// fills. Rows share their thresholds across column segments through
-// rowthr. Every mbarrier wait is bounded; the epilogue warps synchronise on a
-// hardware named barrier that carries each wait's outcome, so on a timeout
-// all roles leave together: the kernel records an error, drains, frees its
-// TMEM and returns.
+// the MMAs; 16 epilogue warps, a pair per 32 rows (one warp per column
+// half), append the pairs below the row's threshold to the row's list in
+// global memory: each (row, column half) owns a region of the list and
+// counts in a register, so an append is a compare and a store. When a
+// region nears full, the warp owning the row cuts its two regions back to
+// K' by a warp radix select. Rows share their thresholds across column
+// segments through rowthr. Every mbarrier wait is bounded; the two warps of
+// a pair synchronise on their own hardware named barrier, which carries each
+// wait's outcome, so on a timeout all roles leave together: the kernel
+// records an error, drains, frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -44,16 +46,22 @@
 #define TV_STAGE_BYTES (2 * TV_SUB_BYTES)  // reference hi + lo of one K-block
 #define TV_MAXST 4
 #define TV_TQ 8
-#define TV_SCR 256          // keys of per-warp shared scratch
+#define TV_SCR 256          // ints of per-warp shared scratch (radix histogram)
+#define TV_LCAP 256         // keys per (row, column half) list region; a row's list is 2 regions
 #define TV_MAX_DP 128
 
 // FP32 vectors [n][Dp] -> BF16 split rows [rows][hi(Dp) | lo(Dp)], rows
-// beyond n zero.
-__global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows, __nv_bfloat16* __restrict__ out) {
+// beyond n zero. With terms != nullptr also the column term of each row as a
+// reference vector (the screen value is row term + column term - 2 x.y, or
+// - x.y/2 for correlation): |y|^2 (1 - c), or -c |y|^2; +inf beyond n.
+__global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows, __nv_bfloat16* __restrict__ out,
+                            const float* __restrict__ nrm, float guard, int corr, float* __restrict__ terms) {
   const int64_t total = (int64_t)rows * Dp;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = e / Dp;
     const int d = (int)(e % Dp);
+    if (terms && d == 0)
+      terms[r] = (r < n) ? (corr ? -guard * nrm[r] : nrm[r] * (1.0f - guard)) : __int_as_float(0x7f800000);
     const float x = (r < n) ? X[r * Dp + d] : 0.0f;
     const __nv_bfloat16 hi = __float2bfloat16_rn(x);
     const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
@@ -68,14 +76,13 @@ struct TvShared {
   int2 task[TV_TQ];
   uint32_t tmem_base;
   int abortf;
-  int cnt[TV_ROWS];
-  float thr[TV_ROWS], gthr[TV_ROWS], rowc[TV_ROWS];
-  alignas(16) float colc[TV_N];  // read as float4
+  int cnt2[TV_ROWS][2];   // keys in each (row, column half) region
+  float thr[TV_ROWS];     // the row's list threshold (+inf until its list first fills)
 };
 
 static size_t tv_smem_bytes(int Dp, int nst) {
   return (size_t)TV_ROWS * 2 * Dp * 2 + (size_t)nst * TV_STAGE_BYTES + sizeof(TvShared) +
-         (size_t)TV_EPI * TV_SCR * 8 + 1024;
+         (size_t)TV_EPI * TV_SCR * 4 + 1024;
 }
 
 // Column tiles of a segment [t0, t1) in visiting order: outward from td.
@@ -88,35 +95,30 @@ __device__ __forceinline__ int tv_tile_order(int i, int t0, int t1, int td) {
 }
 
 
-// One fit row's list: keep the Kp best, sort them and write the segment's
-// candidate list (called by the warp that owns the row).
-__device__ __forceinline__ void tv_publish(uint64_t* src, int n, int Kp, uint64_t* scratch, uint64_t* dst,
+// One fit row's list (regions src[0, c0) and src[TV_LCAP, TV_LCAP + c1)):
+// keep the Kp best and write them, unsorted, as the segment's candidate list
+// (the recheck sorts the merged lists). Called by the warp owning the row.
+__device__ __forceinline__ void tv_publish(uint64_t* src, int c0, int c1, int Kp, int* hist, uint64_t* dst,
                                            int* dst_n, int lane) {
-  n = min(n, TC_CAPG);
-  if (n > Kp) {
-    warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
-    n = Kp;
+  if (c0 + c1 > Kp) {
+    warp_select_keep2(src, c0, TV_LCAP, c1, Kp, hist, lane);
+    c0 = Kp;
+    c1 = 0;
   }
-  if (n <= TV_SCR) {
-    for (int e = lane; e < n; e += 32) scratch[e] = src[e];
-    __syncwarp();
-    warp_bitonic_sort(scratch, n, TV_SCR, lane);
-    for (int e = lane; e < n; e += 32) dst[e] = scratch[e];
-  } else {
-    warp_bitonic_sort(src, n, TC_CAPG, lane);
-    for (int e = lane; e < n; e += 32) dst[e] = src[e];
-  }
-  if (lane == 0) *dst_n = n;
+  for (int e = lane; e < c0; e += 32) dst[e] = src[e];
+  for (int e = lane; e < c1; e += 32) dst[c0 + e] = src[TV_LCAP + e];
+  if (lane == 0) *dst_n = c0 + c1;
   __syncwarp();
 }
 
 __global__ void __launch_bounds__(TV_THREADS, 1)
 k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-             const float* __restrict__ nf, const float* __restrict__ nr, int nfit, int Nr, int Dp, int nst,
+             const float* __restrict__ nf, const float* __restrict__ colterm, int nfit, int Nr, int Dp, int nst,
              int corr, float guard, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
              float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
              int* __restrict__ cand_n, int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
+  // colterm: [ncoltiles * TV_N] column terms (+inf past Nr).
   // work: [gridDim.x][TV_ROWS][TC_CAPG] list buffers of the CTAs;
   // candout: [nfit][nseg][Kp] sorted lists, cand_n [nfit][nseg] their sizes.
   extern __shared__ unsigned char smem_raw[];
@@ -126,7 +128,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   unsigned char* arows = base;                                   // [2][nkb][hi, lo] 8 KB tiles
   unsigned char* stages = base + (size_t)TV_ROWS * 2 * Dp * 2;   // nst x (hi, lo)
   TvShared* S = reinterpret_cast<TvShared*>(stages + (size_t)nst * TV_STAGE_BYTES);
-  uint64_t* scratch_all = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(S) + sizeof(TvShared));
+  int* scratch_all = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(S) + sizeof(TvShared));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncoltiles = (Nr + TV_N - 1) / TV_N;
   const float INF = __int_as_float(0x7f800000);
@@ -149,6 +151,11 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     }
     S->abortf = 0;
     mbar_fence_init();
+  }
+  for (int r = threadIdx.x; r < TV_ROWS; r += blockDim.x) {
+    S->cnt2[r][0] = 0;
+    S->cnt2[r][1] = 0;
+    S->thr[r] = INF;
   }
   if (warp == 1) {
     tmem_alloc(&S->tmem_base, 512);
@@ -280,23 +287,23 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   } else {
     // ------------------------------------------------------------ epilogue
     const int ew = warp - 2;
-    const int q = warp & 3;          // TMEM lane quarter: rows 32q .. 32q + 31 of a row tile
-    const int u = (ew >> 2) >> 1;    // row tile of the pair
-    const int half = (ew >> 2) & 1;  // column half: 64 * half .. + 63
+    const int q = warp & 3;            // TMEM lane quarter: rows 32q .. 32q + 31 of a row tile
+    const int u = (ew >> 2) >> 1;      // row tile of the pair
+    const int half = (ew >> 2) & 1;    // column half: 64 * half .. + 63
     const int r = u * 128 + 32 * q + lane;  // this lane's row of the item
-    uint64_t* scratch = scratch_all + ew * TV_SCR;
-    // rows this warp compacts and publishes: 16 of its lane quarter
-    const int own0 = u * 128 + 32 * q + 16 * half;
+    const int pbar = 2 + 4 * u + q;    // named barrier of the two warps sharing these 32 rows
+    int* hist = scratch_all + ew * TV_SCR;
+    const int own0 = u * 128 + 32 * q + 16 * half;  // the 16 rows this warp compacts and publishes
     uint64_t* lists = work + (size_t)blockIdx.x * TV_ROWS * TC_CAPG;
+    uint64_t* mylist = lists + (size_t)r * TC_CAPG + half * TV_LCAP;
     const float mul = corr ? -0.5f : -2.0f;
     uint32_t acc = 0;
     bool ok = true;
-    int cur = -1, rp = 0, seg = 0;
-    // The epilogue warps meet at named barrier 1 three times per tile: after
-    // the task read (every warp has finished the previous tile, its
-    // compactions and any publishing), after the accumulator is ready, and
-    // after the pairs are appended (before compaction). A failed bounded
-    // wait is ANDed into the first two, so all warps leave together.
+    int cur = -1, rp = 0, seg = 0, g = 0;
+    float rc = INF;
+    // The two warps of a pair meet at their named barrier twice per tile:
+    // after the task read and the accumulator wait (whose outcomes are ANDed,
+    // so both leave together), and after the appends (before compaction).
     for (uint32_t qs = 0;; ++qs) {
       const uint32_t slot = qs % TV_TQ, qph = (qs / TV_TQ) & 1;
       const bool got = mbar_wait(&S->tq_full[slot], qph, abortf);
@@ -305,57 +312,47 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const volatile int* tv = reinterpret_cast<volatile int*>(&S->task[slot]);
         task = make_int2(tv[0], tv[1]);
       }
+      const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
+      bool ready = true;
+      if (got && task.x >= 0 && task.y >= 0) ready = mbar_wait(&S->tfull[b], aph, abortf);
+      tc_fence_after();
       __syncwarp();
-      if (!bar_and(1, TV_EPI * 32, got)) { ok = false; break; }
+      if (!bar_and(pbar, 64, got && ready)) { ok = false; break; }
       if (lane == 0) mbar_arrive(&S->tq_empty[slot]);
       if (task.x < 0) break;
       if (task.x != cur) {
         cur = task.x;
         rp = cur / nseg;
         seg = cur % nseg;
-        if (half == 0) {  // one warp of each row quarter resets its 32 rows
-          const int g = rp * TV_ROWS + r;
-          S->cnt[r] = 0;
-          S->thr[r] = INF;
-          const float rn = (g < nfit) ? __ldg(nf + g) : 0.0f;
-          S->rowc[r] = (g >= nfit) ? INF : corr ? 0.5f - guard * rn : rn * (1.0f - guard);
-        }
+        g = rp * TV_ROWS + r;
+        const float rn = (g < nfit) ? __ldg(nf + g) : 0.0f;
+        rc = (g >= nfit) ? INF : corr ? 0.5f - guard * rn : rn * (1.0f - guard);
       }
       if (task.y < 0) {
-        // end of the item: keep, sort and publish the rows this warp owns
-        // (their appends and compactions are complete; the next task's
-        // barrier separates this from the next item's resets)
+        // end of the item: publish the owned rows and clear their state
         for (int x = 0; x < 16; ++x) {
           const int rr = own0 + x;
-          const int g = rp * TV_ROWS + rr;
-          if (g >= nfit) break;
-          tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt[rr], Kp, scratch,
-                     candout + ((int64_t)g * nseg + seg) * Kp, cand_n + (int64_t)g * nseg + seg, lane);
+          const int gg = rp * TV_ROWS + rr;
+          if (gg < nfit)
+            tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], S->cnt2[rr][1], Kp, hist,
+                       candout + ((int64_t)gg * nseg + seg) * Kp, cand_n + (int64_t)gg * nseg + seg, lane);
+          if (lane == 0) {
+            S->cnt2[rr][0] = 0;
+            S->cnt2[rr][1] = 0;
+            S->thr[rr] = INF;
+          }
         }
+        __syncwarp();
         continue;
       }
       const int tile = task.y;
-      const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
-      // the column terms of this tile and the rows' shared thresholds
-      for (int e = ew * 32 + lane; e < TV_N; e += TV_EPI * 32) {
-        const int j = tile * TV_N + e;
-        const float cn = (j < Nr) ? __ldg(nr + j) : 0.0f;
-        S->colc[e] = (j >= Nr) ? INF : corr ? -guard * cn : cn * (1.0f - guard);
-      }
-      if (half == 0) {
-        const int g = rp * TV_ROWS + r;
-        S->gthr[r] = (g < nfit) ? __ldcg(rowthr + g) : INF;
-      }
-      const bool ready = mbar_wait(&S->tfull[b], aph, abortf);
-      tc_fence_after();
-      __syncwarp();
-      if (!bar_and(1, TV_EPI * 32, ready)) { ok = false; break; }
-      const float rc = S->rowc[r];
-      // screen value = rc + colc - 2g (or - g/2); pass if below the row's threshold
-      const float lim = fminf(S->thr[r], S->gthr[r]) - rc;
-      uint64_t* rowbuf = lists + (size_t)r * TC_CAPG;
+      int cnt = S->cnt2[r][half];
+      // screen value = rc + colterm + mul * x.y; a pair passes below the
+      // row's threshold (its own list's or another segment's)
+      const float lim = fminf(S->thr[r], (g < nfit) ? __ldcg(rowthr + g) : INF) - rc;
       const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256 + u * TV_N + 64 * half;
-      const float4* colc4 = reinterpret_cast<const float4*>(S->colc + 64 * half);
+      const int j0 = tile * TV_N + 64 * half;
+      const float4* ct4 = reinterpret_cast<const float4*>(colterm + j0);
 #pragma unroll 1
       for (int cc = 0; cc < 2; ++cc) {
         uint32_t gv[32];
@@ -363,18 +360,14 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         tmem_wait_ld();
 #pragma unroll
         for (int t4 = 0; t4 < 8; ++t4) {
-          const float4 c4 = colc4[cc * 8 + t4];
+          const float4 c4 = __ldg(ct4 + cc * 8 + t4);
           const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
           for (int t = 0; t < 4; ++t) {
             const float v = fmaf(mul, __uint_as_float(gv[4 * t4 + t]), cv[t]);
             if (v < lim) {
-              const int pos = atomicAdd(&S->cnt[r], 1);
-              const int j = tile * TV_N + 64 * half + 32 * cc + 4 * t4 + t;
-              if (pos < TC_CAPG)
-                rowbuf[pos] = mds_pack_key(fmaxf(v + rc, 0.0f), j);
-              else
-                atomicMax(err, 4);  // cannot happen: compaction keeps room for a whole tile
+              if (cnt < TV_LCAP) mylist[cnt] = mds_pack_key(fmaxf(v + rc, 0.0f), j0 + 32 * cc + 4 * t4 + t);
+              ++cnt;
             }
           }
         }
@@ -383,20 +376,22 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->tempty[b]);
       ++acc;
-      bar_named(1, TV_EPI * 32);  // every append of this tile is done
-      // compaction of the owned rows whose lists are full (or first filled)
+      if (cnt > TV_LCAP) atomicMax(err, 4);  // cannot happen: compaction keeps room for a tile
+      S->cnt2[r][half] = min(cnt, TV_LCAP);
+      bar_named(pbar, 64);  // both halves of these rows are appended
+      // compaction of the owned rows whose regions near full (or first fill)
       for (int x = 0; x < 16; ++x) {
         const int rr = own0 + x;
-        const int g = rp * TV_ROWS + rr;
-        if (g >= nfit) break;
-        const int n = S->cnt[rr];
-        if (!(n > Kp && (n > TC_CAPG - TV_N || S->thr[rr] == INF))) continue;
-        const float t = warp_select_keep(lists + (size_t)rr * TC_CAPG, min(n, TC_CAPG), Kp,
-                                         reinterpret_cast<int*>(scratch), lane);
+        const int gg = rp * TV_ROWS + rr;
+        if (gg >= nfit) break;
+        const int c0 = S->cnt2[rr][0], c1 = S->cnt2[rr][1];
+        if (!(c0 + c1 > Kp && (c0 > TV_LCAP - 64 || c1 > TV_LCAP - 64 || S->thr[rr] == INF))) continue;
+        const float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, c0, TV_LCAP, c1, Kp, hist, lane);
         if (lane == 0) {
-          S->cnt[rr] = Kp;
+          S->cnt2[rr][0] = Kp;
+          S->cnt2[rr][1] = 0;
           S->thr[rr] = t;
-          atomicMin(reinterpret_cast<int*>(rowthr + g), __float_as_int(t));
+          atomicMin(reinterpret_cast<int*>(rowthr + gg), __float_as_int(t));
         }
         __syncwarp();
       }
@@ -415,8 +410,9 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   }
 }
 
-// Largest K' of the vector screen: a list keeps room for one more tile.
-int tcv_max_kprime() { return TC_CAPG - TV_N; }
+// Largest K' of the vector screen: after a compaction the first region of a
+// row's list keeps room for one more tile's half (64 keys).
+int tcv_max_kprime() { return TV_LCAP - TV_N / 2; }
 // Largest padded dimension: the resident rows must fit in shared memory.
 int tcv_max_dp() { return TV_MAX_DP; }
 
@@ -431,8 +427,8 @@ int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref) {
 // The tensor-core screen of knn_data. Xf/Xr: FP32 vectors [n][Dp] (Dp a
 // multiple of 32, at most TV_MAX_DP), nf/nr their squared norms. same: Xf is
 // Xr (a set screened against itself; the visit starts at the diagonal).
-// Writes the sorted candidate lists candout [nfit][nseg][Kp] and cand_n
-// [nfit][nseg].
+// Writes the candidate lists candout [nfit][nseg][Kp] (each unsorted) and
+// their sizes cand_n [nfit][nseg].
 int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
                       int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n) {
   if (Kp > tcv_max_kprime()) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: K' too large");
@@ -443,23 +439,24 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   cudaStream_t s = ctx->stream;
   const int rowsA = (nfit + TV_ROWS - 1) / TV_ROWS * TV_ROWS, rowsB = ncoltiles * TV_N;
   const int rowsS = std::max(rowsA, rowsB);
-  DevBuf A(ctx), B(ctx), work(ctx), rowthr(ctx), err(ctx);
-  auto split = [&](const float* X, int n, int rows, DevBuf& out) -> int {
+  DevBuf A(ctx), B(ctx), work(ctx), rowthr(ctx), err(ctx), terms(ctx);
+  MDS_TRY(terms.alloc(ctx, sizeof(float) * (size_t)rowsS));
+  auto split = [&](const float* X, int n, int rows, DevBuf& out, float* t) -> int {
     MDS_TRY(out.alloc(ctx, sizeof(__nv_bfloat16) * 2 * (size_t)Dp * rows));
     const int64_t total = (int64_t)rows * Dp;
     const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 16);
     ctx->stats.launches++;
-    k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>());
+    k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>(), nr, MDS_GUARD_TC, corr ? 1 : 0, t);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
   const void* pA;
   if (same) {  // one split array serves both roles (rows padded to the larger tiling)
-    MDS_TRY(split(Xr, nref, rowsS, B));
+    MDS_TRY(split(Xr, nref, rowsS, B, terms.as<float>()));
     pA = B.p;
   } else {
-    MDS_TRY(split(Xr, nref, rowsB, B));
-    MDS_TRY(split(Xf, nfit, rowsA, A));
+    MDS_TRY(split(Xr, nref, rowsB, B, terms.as<float>()));
+    MDS_TRY(split(Xf, nfit, rowsA, A, nullptr));
     pA = A.p;
   }
   CUtensorMap mA, mB;
@@ -481,7 +478,8 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "vector screen needs %zu bytes of shared memory", smem);
   const uint32_t idesc = umma_idesc_f16(128, TV_N, 1);
   ctx->stats.launches++;
-  k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nf, nr, nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC,
+  k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nf, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0,
+                                              MDS_GUARD_TC,
                                               idesc, Kp, nseg, nitems, same ? 1 : 0, rowthr.as<float>(),
                                               work.as<uint64_t>(), candout, cand_n, err.as<int>());
   MDS_CUDA(ctx, cudaGetLastError());

@@ -5,18 +5,19 @@
 #include "knn_common.cuh"
 
 #define TC_CAPG 512  // keys per (row, column segment) list
-// Keep the Kp smallest of the n (<= TC_CAPG) keys in src (unsorted, in
-// src[0..Kp)) and return the largest kept value: a most-significant-digit
-// radix select over the 64-bit keys (8-bit digits, stopping as soon as the
-// digit bucket holding the Kp-th key is kept whole), then a ballot
-// compaction. hist: 256 ints of this warp's shared scratch.
-__device__ inline float warp_select_keep(uint64_t* src, int n, int Kp, int* hist, int lane) {
+// Keep the Kp smallest of the keys src[0, n0) and src[off1, off1 + n1) (at
+// most TC_CAPG slots in all: off1 + n1 <= TC_CAPG) in src[0..Kp), unsorted,
+// and return the largest kept value: a most-significant-digit radix select
+// over the 64-bit keys (8-bit digits, stopping as soon as the digit bucket
+// holding the Kp-th key is kept whole), then a ballot compaction. hist: 256
+// ints of this warp's shared scratch.
+__device__ inline float warp_select_keep2(uint64_t* src, int n0, int off1, int n1, int Kp, int* hist, int lane) {
   constexpr int PER = TC_CAPG / 32;
   uint64_t kv[PER];
 #pragma unroll
   for (int i = 0; i < PER; ++i) {
     const int x = lane + 32 * i;
-    kv[i] = (x < n) ? src[x] : MDS_KEY_INF;
+    kv[i] = (x < n0 || (x >= off1 && x < off1 + n1)) ? src[x] : MDS_KEY_INF;
   }
   uint64_t prefix = 0, mask = 0;
   int need = Kp;
@@ -82,3 +83,7 @@ __device__ inline float warp_select_keep(uint64_t* src, int n, int Kp, int* hist
   return vmax;
 }
 
+// One contiguous list src[0, n), n <= TC_CAPG.
+__device__ inline float warp_select_keep(uint64_t* src, int n, int Kp, int* hist, int lane) {
+  return warp_select_keep2(src, n, TC_CAPG, 0, Kp, hist, lane);
+}

@@ -72,7 +72,7 @@ def test_knn_data_tc_vonmises(ctx, oracle, corr):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("nref,nfit,dim,k", [(300, 77, 3, 10), (1000, 513, 100, 25), (129, 255, 32, 7),
-                                             (2000, 300, 17, 200)])
+                                             (2000, 300, 17, 120)])
 def test_knn_data_tc_fit_vs_ref(ctx, oracle, nref, nfit, dim, k):
     rng = np.random.default_rng(nref + dim)
     ref = rng.normal(size=(nref, dim))
@@ -114,8 +114,8 @@ def test_knn_data_tc_matches_fp32_screen_large(ctx):
 @pytest.mark.gpu
 def test_knn_data_tc_fallback_shapes(ctx, oracle):
     """Shapes outside the tensor-core screen's limits: a dimension above 128
-    runs the FP32 screen; a k whose K' exceeds both screens' list sizes is
-    rechecked exactly against every reference vector."""
+    runs the FP32 screen; a k whose K' exceeds both screens' list sizes (192)
+    is rechecked exactly against every reference vector."""
     rng = np.random.default_rng(5)
     x = rng.normal(size=(400, 130))
     d, i = ctx.knn_data(x, None, 9, precision="bf16x3")
