@@ -294,13 +294,15 @@ def run_pipeline(args):
     return 0
 
 
-# DRAM bytes (read + write) of one k_screen_tc launch on the default workload
+# DRAM bytes (read + write) of one k_screen_tc screen launch (the second of
+# the call; the first is the 0.08 ms pivot pass) on the default workload
 # (20,000 x 1,000 atoms, k = 100, bf16x3), from one ncu capture of
 # dram__bytes_read.sum + dram__bytes_write.sum (a 1-pass metric pair) with
 # the command `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
-# --clock-control none -k regex:k_screen_tc -s 3 -c 1 python bench.py --steps 2
-# --warmup 3 --no-cpu`. Other workloads report null.
-SCREEN_TRAFFIC_BYTES = 3.94e9 + 0.52e9
+# --clock-control none -k regex:"k_prep_sums|k_prep_out|k_screen_tc|k_recheck"
+# -s 15 -c 5 --csv python bench.py --steps 2 --warmup 3 --no-cpu`. Other
+# workloads report null.
+SCREEN_TRAFFIC_BYTES = 13.305e9 + 0.350e9
 
 
 def screen_traffic(args):

@@ -25,6 +25,33 @@ void mds_trim_cache(mds_ctx* ctx, size_t keep) {
   }
 }
 
+int mds_upload_chunked(mds_ctx* ctx, void* dst, const void* src, int n, size_t frame_bytes, int ev0,
+                       std::vector<int>& bounds, int* nchunks) {
+  if (!ctx->order_ev) {
+    for (auto& cs : ctx->copy_stream) MDS_CUDA(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    for (auto& e : ctx->chunk_ev) MDS_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    MDS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->order_ev, cudaEventDisableTiming));
+  }
+  // chunks of at least 4 MiB, at most MDS_MAX_CHUNKS
+  const size_t total = frame_bytes * (size_t)n;
+  int c = (int)std::min<size_t>(MDS_MAX_CHUNKS, std::max<size_t>(1, total >> 22));
+  c = std::max(1, std::min(c, n));
+  bounds.resize(c + 1);
+  for (int i = 0; i <= c; ++i) bounds[i] = (int)((int64_t)n * i / c);
+  // the destination may be a cached block last used by work on ctx->stream
+  MDS_CUDA(ctx, cudaEventRecord(ctx->order_ev, ctx->stream));
+  for (auto cs : ctx->copy_stream) MDS_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->order_ev, 0));
+  for (int i = 0; i < c; ++i) {
+    cudaStream_t cs = ctx->copy_stream[i & 1];
+    const size_t off = frame_bytes * (size_t)bounds[i], bytes = frame_bytes * (size_t)(bounds[i + 1] - bounds[i]);
+    MDS_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, bytes,
+                                  cudaMemcpyHostToDevice, cs));
+    MDS_CUDA(ctx, cudaEventRecord(ctx->chunk_ev[ev0 + i], cs));
+  }
+  *nchunks = c;
+  return MDS_OK;
+}
+
 extern "C" const char* mds_version(void) { return "mdsgpu 0.1 (sm_103a)"; }
 
 extern "C" int mds_create(int device, size_t hbm_budget, mds_ctx** out) {
@@ -54,6 +81,14 @@ extern "C" int mds_destroy(mds_ctx* ctx) {
   mds_trim_cache(ctx, 0);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->chunk_ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->order_ev) cudaEventDestroy(ctx->order_ev);
+  for (auto cs : ctx->copy_stream)
+    if (cs) {
+      cudaStreamSynchronize(cs);
+      cudaStreamDestroy(cs);
+    }
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return MDS_OK;

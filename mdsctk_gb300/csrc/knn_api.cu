@@ -133,15 +133,15 @@ static int knn_rms_impl(mds_ctx* ctx, const float* ref_xyz, int n_ref, const flo
   int* pi = out_i;
   std::vector<float> hmass(natoms);
   if (!dev) {
+    // the frames are uploaded by knn_rms_run in chunks, overlapped with the
+    // superposition of the chunks already on the device
     MDS_TRY(dref.alloc(ctx, sizeof(float) * 3 * (size_t)natoms * n_ref));
-    MDS_CUDA(ctx, cudaMemcpyAsync(dref.p, ref_xyz, sizeof(float) * 3 * (size_t)natoms * n_ref,
-                                  cudaMemcpyHostToDevice, s));
     pref = dref.as<float>();
+    pl.href = ref_xyz;
     if (fit_xyz) {
       MDS_TRY(dfit.alloc(ctx, sizeof(float) * 3 * (size_t)natoms * n_fit));
-      MDS_CUDA(ctx, cudaMemcpyAsync(dfit.p, fit_xyz, sizeof(float) * 3 * (size_t)natoms * n_fit,
-                                    cudaMemcpyHostToDevice, s));
       pfit = dfit.as<float>();
+      pl.hfit = fit_xyz;
     }
     MDS_TRY(dd.alloc(ctx, sizeof(double) * width * n_fit));
     MDS_TRY(di.alloc(ctx, sizeof(int) * width * n_fit));

@@ -34,6 +34,11 @@ struct KnnRmsPlan {
   // onto the template and copy the reference set's deviations and records
   float* prep_dev = nullptr;  // [nref][3][Ap]
   float* prep_rec = nullptr;  // [nref][16]
+  // host copies of the frames: when set, the device frame buffers passed to
+  // knn_rms_run are filled here in chunks on the copy streams, and each chunk
+  // is superposed as soon as it has landed
+  const float* href = nullptr;
+  const float* hfit = nullptr;
 };
 
 // Split hi/lo tensor-core operands of one frame set (knn_rms_tc.cu).
@@ -125,7 +130,8 @@ int tcv_max_kprime();
 int tcv_max_dp();
 int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref);
 int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
-                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n);
+                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n,
+                      float* rowthr);
 
 // Tile skipping data of the tensor-core screen (knn_rms_tc.cu): lower
 // bounds of RMSD from every fit frame to the pivot of every column tile

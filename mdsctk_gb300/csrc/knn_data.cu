@@ -250,8 +250,8 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
                const double* __restrict__ sfv, const double* __restrict__ mr, const double* __restrict__ srv,
                const float* __restrict__ nf, int nrows, const int* __restrict__ rowlist, int Nr, int dim, int corr,
                int mode, const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int Kp, int k,
-               double* __restrict__ out_d, int* __restrict__ out_i, int* __restrict__ flagged,
-               int* __restrict__ nflag) {
+               const float* __restrict__ rowthr, double* __restrict__ out_d, int* __restrict__ out_i,
+               int* __restrict__ flagged, int* __restrict__ nflag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* sa = reinterpret_cast<double*>(smem_raw);              // [dim]
   uint64_t* keys = reinterpret_cast<uint64_t*>(sa + dim);        // merge buffer, then candidates
@@ -294,7 +294,12 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
     __syncthreads();
     block_bitonic_sort(keys, P2);
     total = min(t, Kp);
-    if (t >= Kp) tau = mds_key_value(keys[Kp - 1]);
+    // the bound of every pair left out: the K'-th candidate's, or, when the
+    // lists hold fewer than K', the threshold the screen filtered them with
+    if (t >= Kp)
+      tau = mds_key_value(keys[Kp - 1]);
+    else if (rowthr)
+      tau = rowthr[grow];
   } else {
     total = Nr;
   }
@@ -412,7 +417,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   MDS_TRY(nflag.alloc(ctx, sizeof(int)));
   MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
   auto recheck = [&](int nrows, const int* rowlist, int mode, const uint64_t* cand, const int* cand_n, int nseg,
-                     int Kp) -> int {
+                     int Kp, const float* rowthr) -> int {
     size_t smem = data_recheck_smem(dim, Kp, nseg, k, mode);
     if (smem > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "knn_data recheck: dim/k too large");
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -420,13 +425,13 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
     if (nrows > 0)
       k_data_recheck<<<nrows, DR_THREADS, smem, s>>>(dfit, dref, mf, sf, Mr.as<double>(), Sr.as<double>(), nfp,
                                                      nrows, rowlist, nref, dim, corr, mode, cand, cand_n, nseg, Kp,
-                                                     k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>());
+                                                     k, rowthr, dout_d, dout_i, flagged.as<int>(), nflag.as<int>());
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
   if (full) {
-    MDS_TRY(recheck(nfit, nullptr, 2, nullptr, nullptr, 1, 1));
+    MDS_TRY(recheck(nfit, nullptr, 2, nullptr, nullptr, 1, 1, nullptr));
     MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
     float ms = 0;
@@ -444,7 +449,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
     // k too large for a screen to pay off: every row is rechecked exactly
     st.kprime = 0;
     st.passes = 1;
-    MDS_TRY(recheck(nfit, nullptr, 1, nullptr, nullptr, 1, 1));
+    MDS_TRY(recheck(nfit, nullptr, 1, nullptr, nullptr, 1, 1, nullptr));
     MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
     float ms = 0;
@@ -467,14 +472,15 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   }
   const float guard = MDS_GUARD_FP32;
   if (tc) nseg = tcv_choose_nseg(ctx, nfit, nref);
-  DevBuf cand(ctx), cand_n(ctx), rows(ctx);
+  DevBuf cand(ctx), cand_n(ctx), rows(ctx), rthr(ctx);
   MDS_TRY(cand.alloc(ctx, sizeof(uint64_t) * (size_t)nfit * nseg * Kp));
   MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)nfit * nseg));
   size_t smem = screen_dot_smem(Kp);
   st.screen_launches = 1;
   if (tc) {
+    MDS_TRY(rthr.alloc(ctx, sizeof(float) * (size_t)nfit));
     MDS_TRY(launch_screen_tcv(ctx, xf, nfp, nfit, Xr.as<float>(), Nrm.as<float>(), nref, Dp, corr, Kp, nseg, same,
-                              cand.as<uint64_t>(), cand_n.as<int>()));
+                              cand.as<uint64_t>(), cand_n.as<int>(), rthr.as<float>()));
   } else {
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     st.launches++;
@@ -484,7 +490,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
     MDS_CUDA(ctx, cudaGetLastError());
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
-  MDS_TRY(recheck(nfit, nullptr, 0, cand.as<uint64_t>(), cand_n.as<int>(), nseg, Kp));
+  MDS_TRY(recheck(nfit, nullptr, 0, cand.as<uint64_t>(), cand_n.as<int>(), nseg, Kp, tc ? rthr.as<float>() : nullptr));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0;
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -508,7 +514,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
     st.passes++;
     const int wider = std::min(Kp * 4, DT_MAX_KP);
     if (wider <= Kp || wider >= nref || st.passes > 3) {
-      MDS_TRY(recheck(hflag, rows.as<int>(), 1, nullptr, nullptr, 1, 1));
+      MDS_TRY(recheck(hflag, rows.as<int>(), 1, nullptr, nullptr, 1, 1, nullptr));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
       break;
     }
@@ -522,7 +528,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
                                                                        hflag, rows.as<int>(), nref, Dp, corr, guard,
                                                                        Kp, 1, cand.as<uint64_t>(), cand_n.as<int>());
     MDS_CUDA(ctx, cudaGetLastError());
-    MDS_TRY(recheck(hflag, rows.as<int>(), 0, cand.as<uint64_t>(), cand_n.as<int>(), 1, Kp));
+    MDS_TRY(recheck(hflag, rows.as<int>(), 0, cand.as<uint64_t>(), cand_n.as<int>(), 1, Kp, nullptr));
     MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
   }
@@ -642,7 +648,7 @@ extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, 
   if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
   MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
   k_data_recheck<<<n_fit, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, n_fit, nullptr, n_ref, dim, corr, 0,
-                                                cand, cand_n, 1, Kp, k, out_d, out_i, flagged, nflag);
+                                                cand, cand_n, 1, Kp, k, nullptr, out_d, out_i, flagged, nflag);
   MDS_CUDA(ctx, cudaGetLastError());
   int hflag = 0;
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -654,7 +660,7 @@ extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, 
     if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
     k_data_recheck<<<hflag, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, hflag, flagged, n_ref, dim, corr, 1,
-                                                  nullptr, nullptr, 1, 1, k, out_d, out_i, flagged, nflag);
+                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, flagged, nflag);
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
   }

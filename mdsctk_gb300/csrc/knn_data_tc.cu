@@ -46,9 +46,11 @@
 #define TV_STAGE_BYTES (2 * TV_SUB_BYTES)  // reference hi + lo of one K-block
 #define TV_MAXST 4
 #define TV_TQ 8
-#define TV_SCR 256          // ints of per-warp shared scratch (radix histogram)
+#define TV_SCR 512          // words of per-warp shared scratch: 16 columns x 32 lanes of screen values, or
+                            // the radix histogram of a compaction (256 ints)
 #define TV_LCAP 256         // keys per (row, column half) list region; a row's list is 2 regions
 #define TV_MAX_DP 128
+#define TV_PILOT 16         // column tiles each row pair visits in the threshold-seeding pass
 
 // FP32 vectors [n][Dp] -> BF16 split rows [rows][hi(Dp) | lo(Dp)], rows
 // beyond n zero. With terms != nullptr also the column term of each row as a
@@ -114,10 +116,15 @@ __device__ __forceinline__ void tv_publish(uint64_t* src, int c0, int c1, int Kp
 __global__ void __launch_bounds__(TV_THREADS, 1)
 k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
              const float* __restrict__ nf, const float* __restrict__ colterm, int nfit, int Nr, int Dp, int nst,
-             int corr, float guard, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
+             int corr, float guard, uint32_t idesc, int Kp, int nseg, int nitems, int diag, int pilot,
              float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
              int* __restrict__ cand_n, int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
+  // pilot > 0: a pass that only seeds rowthr: each item (one per row pair
+  // tile, nseg = 1) visits `pilot` column tiles (outward from the diagonal
+  // for a set against itself, else spread over the set) and lowers each
+  // row's rowthr to the K'-th smallest screen value it saw, an upper bound of
+  // the row's final K'-th smallest; nothing else is written.
   // colterm: [ncoltiles * TV_N] column terms (+inf past Nr).
   // work: [gridDim.x][TV_ROWS][TC_CAPG] list buffers of the CTAs;
   // candout: [nfit][nseg][Kp] sorted lists, cand_n [nfit][nseg] their sizes.
@@ -189,7 +196,9 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           break;
         }
         const int rp = item / nseg, seg = item % nseg;
-        const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+        const int t0 = pilot ? 0 : (int)((int64_t)ncoltiles * seg / nseg);
+        const int t1 = pilot ? ncoltiles : (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+        const int nvisit = pilot ? pilot : t1 - t0;
         const int td = diag ? min(max((rp * TV_ROWS + TV_ROWS / 2) / TV_N, t0), t1 - 1) : t0;
         // the resident rows: wait until the MMAs of the previous item are done
         if (na > 0 && !mbar_wait(&S->aempty, (na - 1) & 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
@@ -200,8 +209,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
               tma_load_2d(arows + (size_t)((u * nkb + kb) * 2 + p) * TV_SUB_BYTES, &tmA, &S->afull,
                           p * Dp + kb * TV_KB, (2 * rp + u) * 128);
         ++na;
-        for (int ti = 0; ti < t1 - t0 && ok; ++ti) {
-          const int tile = tv_tile_order(ti, t0, t1, td);
+        for (int ti = 0; ti < nvisit && ok; ++ti) {
+          const int tile = (pilot && !diag) ? (int)((int64_t)ti * ncoltiles / pilot) : tv_tile_order(ti, t0, t1, td);
           if (!(ok = push(item, tile))) break;
           for (int kb = 0; kb < nkb; ++kb) {
             if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
@@ -293,6 +302,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     const int r = u * 128 + 32 * q + lane;  // this lane's row of the item
     const int pbar = 2 + 4 * u + q;    // named barrier of the two warps sharing these 32 rows
     int* hist = scratch_all + ew * TV_SCR;
+    float* sv = reinterpret_cast<float*>(hist);  // [16][32]: a chunk's screen values, column-major
     const int own0 = u * 128 + 32 * q + 16 * half;  // the 16 rows this warp compacts and publishes
     uint64_t* lists = work + (size_t)blockIdx.x * TV_ROWS * TC_CAPG;
     uint64_t* mylist = lists + (size_t)r * TC_CAPG + half * TV_LCAP;
@@ -333,9 +343,14 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         for (int x = 0; x < 16; ++x) {
           const int rr = own0 + x;
           const int gg = rp * TV_ROWS + rr;
-          if (gg < nfit)
+          if (gg < nfit && !pilot) {
             tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], S->cnt2[rr][1], Kp, hist,
                        candout + ((int64_t)gg * nseg + seg) * Kp, cand_n + (int64_t)gg * nseg + seg, lane);
+          } else if (gg < nfit && S->cnt2[rr][0] + S->cnt2[rr][1] >= Kp) {
+            const float t =
+                warp_select_keep2(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], TV_LCAP, S->cnt2[rr][1], Kp, hist, lane);
+            if (lane == 0) atomicMin(reinterpret_cast<int*>(rowthr + gg), __float_as_int(t));
+          }
           if (lane == 0) {
             S->cnt2[rr][0] = 0;
             S->cnt2[rr][1] = 0;
@@ -353,24 +368,43 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256 + u * TV_N + 64 * half;
       const int j0 = tile * TV_N + 64 * half;
       const float4* ct4 = reinterpret_cast<const float4*>(colterm + j0);
-#pragma unroll 1
-      for (int cc = 0; cc < 2; ++cc) {
-        uint32_t gv[32];
-        tmem_ld32(tq + 32 * cc, gv);
-        tmem_wait_ld();
+      // Four chunks of 16 columns; the next chunk's TMEM load is in flight
+      // while this one is screened. A chunk's passes go into a per-lane bit
+      // mask (no branch per pair) and its values into shared memory; only if
+      // some lane has a pass does the warp run the append loop, over the set
+      // bits of each lane's mask.
+      uint32_t ga[16], gb[16];
+      tmem_ld16(tq, ga);
+      tmem_wait_ld();
 #pragma unroll
-        for (int t4 = 0; t4 < 8; ++t4) {
-          const float4 c4 = __ldg(ct4 + cc * 8 + t4);
-          const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+      for (int cc = 0; cc < 4; ++cc) {
+        uint32_t* cur = (cc & 1) ? gb : ga;
+        uint32_t* nxt = (cc & 1) ? ga : gb;
+        if (cc < 3) tmem_ld16(tq + 16 * (cc + 1), nxt);
+        float4 c4[4];
+#pragma unroll
+        for (int t4 = 0; t4 < 4; ++t4) c4[t4] = __ldg(ct4 + cc * 4 + t4);
+        uint32_t mask = 0;
+#pragma unroll
+        for (int t4 = 0; t4 < 4; ++t4) {
+          const float cv[4] = {c4[t4].x, c4[t4].y, c4[t4].z, c4[t4].w};
 #pragma unroll
           for (int t = 0; t < 4; ++t) {
-            const float v = fmaf(mul, __uint_as_float(gv[4 * t4 + t]), cv[t]);
-            if (v < lim) {
-              if (cnt < TV_LCAP) mylist[cnt] = mds_pack_key(fmaxf(v + rc, 0.0f), j0 + 32 * cc + 4 * t4 + t);
-              ++cnt;
-            }
+            const float v = fmaf(mul, __uint_as_float(cur[4 * t4 + t]), cv[t]);
+            sv[(4 * t4 + t) * 32 + lane] = v;
+            mask |= (v < lim ? 1u : 0u) << (4 * t4 + t);
           }
         }
+        if (__any_sync(0xffffffffu, mask != 0u)) {
+          while (mask) {
+            const int t = __ffs(mask) - 1;
+            mask &= mask - 1;
+            if (cnt < TV_LCAP) mylist[cnt] = mds_pack_key(fmaxf(sv[t * 32 + lane] + rc, 0.0f), j0 + 16 * cc + t);
+            ++cnt;
+          }
+        }
+        __syncwarp();
+        if (cc < 3) tmem_wait_ld();
       }
       tc_fence_before();
       __syncwarp();
@@ -427,10 +461,13 @@ int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref) {
 // The tensor-core screen of knn_data. Xf/Xr: FP32 vectors [n][Dp] (Dp a
 // multiple of 32, at most TV_MAX_DP), nf/nr their squared norms. same: Xf is
 // Xr (a set screened against itself; the visit starts at the diagonal).
-// Writes the candidate lists candout [nfit][nseg][Kp] (each unsorted) and
-// their sizes cand_n [nfit][nseg].
+// Writes the candidate lists candout [nfit][nseg][Kp] (each unsorted), their
+// sizes cand_n [nfit][nseg], and rowthr [nfit]: the threshold below which a
+// row's pairs were kept (the bound of every pair left out when a row's lists
+// hold fewer than K' in all).
 int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
-                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n) {
+                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n,
+                      float* rowthr) {
   if (Kp > tcv_max_kprime()) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: K' too large");
   if (Dp % TV_KB || Dp > TV_MAX_DP)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: padded dimension %d", Dp);
@@ -439,7 +476,7 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   cudaStream_t s = ctx->stream;
   const int rowsA = (nfit + TV_ROWS - 1) / TV_ROWS * TV_ROWS, rowsB = ncoltiles * TV_N;
   const int rowsS = std::max(rowsA, rowsB);
-  DevBuf A(ctx), B(ctx), work(ctx), rowthr(ctx), err(ctx), terms(ctx);
+  DevBuf A(ctx), B(ctx), work(ctx), err(ctx), terms(ctx);
   MDS_TRY(terms.alloc(ctx, sizeof(float) * (size_t)rowsS));
   auto split = [&](const float* X, int n, int rows, DevBuf& out, float* t) -> int {
     MDS_TRY(out.alloc(ctx, sizeof(__nv_bfloat16) * 2 * (size_t)Dp * rows));
@@ -465,11 +502,10 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   const int nitems = rowsA / TV_ROWS * nseg;
   const int grid = std::min(nitems, ctx->num_sms);
   MDS_TRY(work.alloc(ctx, sizeof(uint64_t) * (size_t)grid * TV_ROWS * TC_CAPG));
-  MDS_TRY(rowthr.alloc(ctx, sizeof(float) * (size_t)std::max(nfit, 1)));
   MDS_TRY(err.alloc(ctx, 2 * sizeof(int)));
   MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, 2 * sizeof(int), s));
-  MDS_CUDA(ctx, cudaMemsetAsync(rowthr.p, 0x7f, sizeof(float) * (size_t)nfit, s));
-  const int nst = (Dp <= 96) ? 4 : 3;
+  MDS_CUDA(ctx, cudaMemsetAsync(rowthr, 0x7f, sizeof(float) * (size_t)nfit, s));
+  const int nst = (Dp <= 64) ? 4 : (Dp <= 96 ? 3 : 2);
   const size_t smem = tv_smem_bytes(Dp, nst);
   static bool attr_done = false;
   static size_t attr_limit = 0;
@@ -477,10 +513,20 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   if (smem > attr_limit)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "vector screen needs %zu bytes of shared memory", smem);
   const uint32_t idesc = umma_idesc_f16(128, TV_N, 1);
+  // pilot pass: seed every row's threshold from TV_PILOT column tiles, so the
+  // main pass appends few pairs from its first tile on
+  if (ncoltiles >= 4 * TV_PILOT) {
+    const int npilot = rowsA / TV_ROWS;
+    ctx->stats.launches++;
+    k_screen_tcv<<<std::min(npilot, ctx->num_sms), TV_THREADS, smem, s>>>(
+        mA, mB, nf, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC, idesc, Kp, 1, npilot,
+        same ? 1 : 0, TV_PILOT, rowthr, work.as<uint64_t>(), candout, cand_n, err.as<int>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_CUDA(ctx, cudaMemsetAsync(err.as<int>() + 1, 0, sizeof(int), s));
+  }
   ctx->stats.launches++;
   k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nf, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0,
-                                              MDS_GUARD_TC,
-                                              idesc, Kp, nseg, nitems, same ? 1 : 0, rowthr.as<float>(),
+                                              MDS_GUARD_TC, idesc, Kp, nseg, nitems, same ? 1 : 0, 0, rowthr,
                                               work.as<uint64_t>(), candout, cand_n, err.as<int>());
   MDS_CUDA(ctx, cudaGetLastError());
   int herr = 0;

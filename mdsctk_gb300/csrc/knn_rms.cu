@@ -62,6 +62,36 @@ __device__ __forceinline__ void block_sum_vecf(const float (&p)[N], double (&out
   __syncthreads();
 }
 
+// Block sum of N float partials entirely in FP32 (shuffle tree per warp, then
+// the warps' sums added in warp order by thread i < N). For the prep sums,
+// whose accuracy only sets how close the pre-alignment rotation is to the
+// optimum; a conversion or add on the FP64 pipe costs a whole warp's issue on
+// this GPU. red holds (blockDim/32 + 1) * N floats.
+template <int N>
+__device__ __forceinline__ void block_sum_vec32(const float (&p)[N], float (&out)[N], float* red) {
+  float v[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    v[i] = p[i];
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (l == 0)
+#pragma unroll
+    for (int i = 0; i < N; ++i) red[w * N + i] = v[i];
+  __syncthreads();
+  if (threadIdx.x < N) {
+    float s = 0.f;
+    for (int j = 0; j < nw; ++j) s += red[j * N + threadIdx.x];
+    red[nw * N + threadIdx.x] = s;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < N; ++i) out[i] = red[nw * N + i];
+  __syncthreads();
+}
+
 // Block sum of N values at once: every warp reduces its N partial sums with
 // shuffles, lane 0 stores them in red[warp * N + i], one barrier, then every
 // thread adds the warps' rows in order. red holds (blockDim/32) * N doubles.
@@ -145,7 +175,7 @@ __global__ void __launch_bounds__(128) k_prep_sums(const float* __restrict__ raw
                                                    const float* __restrict__ mass, const float* __restrict__ swn,
                                                    float tm, const float* __restrict__ mu, int nofit,
                                                    float* __restrict__ rec) {
-  __shared__ double red[32 * 10];
+  __shared__ float red[5 * 10];
   const int f = blockIdx.x;
   if (f >= n) return;
   const float* x = raw + (int64_t)f * natoms * 3;
@@ -157,9 +187,9 @@ __global__ void __launch_bounds__(128) k_prep_sums(const float* __restrict__ raw
       const float mm = mass[a];
       for (int c = 0; c < 3; ++c) p[c] = fmaf(mm, x[3 * a + c], p[c]);
     }
-    double sc[3];
-    block_sum_vecf<3>(p, sc, red);
-    for (int c = 0; c < 3; ++c) com[c] = (float)(sc[c] / (double)tm);
+    float sc[3];
+    block_sum_vec32<3>(p, sc, red);
+    for (int c = 0; c < 3; ++c) com[c] = sc[c] / tm;
   }
   float* r = rec + (int64_t)f * MDS_REC;
   if (threadIdx.x == 0)
@@ -175,10 +205,10 @@ __global__ void __launch_bounds__(128) k_prep_sums(const float* __restrict__ raw
     for (int c = 0; c < 3; ++c)
       for (int d = 0; d < 3; ++d) p[1 + 3 * c + d] = fmaf(yc[c], mc[d], p[1 + 3 * c + d]);
   }
-  double sv[10];
-  block_sum_vecf<10>(p, sv, red);
+  float sv[10];
+  block_sum_vec32<10>(p, sv, red);
   if (threadIdx.x == 0)
-    for (int i = 0; i < 10; ++i) r[3 + i] = (float)sv[i];
+    for (int i = 0; i < 10; ++i) r[3 + i] = sv[i];
 }
 
 // The rotation of every frame (one thread per frame, FP64 QCP): record
@@ -199,7 +229,7 @@ __global__ void __launch_bounds__(128) k_prep_out(const float* __restrict__ raw,
                                                   const float* __restrict__ swn, const float* __restrict__ mu,
                                                   const double* __restrict__ M0, int nofit, float* __restrict__ dev,
                                                   float* __restrict__ rec) {
-  __shared__ double red[32 * 10];
+  __shared__ float red[5 * 10];
   const int f = blockIdx.x;
   if (f >= n) return;
   const float* x = raw + (int64_t)f * natoms * 3;
@@ -229,24 +259,25 @@ __global__ void __launch_bounds__(128) k_prep_out(const float* __restrict__ raw,
     }
   }
   const float eup[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
-  double eu[10];
-  block_sum_vecf<10>(eup, eu, red);  // every thread has read the record row before this barrier
+  float eu[10];
+  block_sum_vec32<10>(eup, eu, red);  // every thread has read the record row before this barrier
   if (threadIdx.x == 0) {
-    const double* U = eu + 1;
-    double sxx = U[0], syy = U[4], szz = U[8];
-    double sxy = 0.5 * (U[1] + U[3]), sxz = 0.5 * (U[2] + U[6]), syz = 0.5 * (U[5] + U[7]);
+    // the template's M0 in FP64 once per frame (one thread)
+    const float* U = eu + 1;
+    const float sxx = U[0], syy = U[4], szz = U[8];
+    const float sxy = 0.5f * (U[1] + U[3]), sxz = 0.5f * (U[2] + U[6]), syz = 0.5f * (U[5] + U[7]);
     r[0] = (float)(M0[0] + sxx);
     r[1] = (float)(M0[4] + syy);
     r[2] = (float)(M0[8] + szz);
     r[3] = (float)(0.5 * (M0[1] + M0[3]) + sxy);
     r[4] = (float)(0.5 * (M0[2] + M0[6]) + sxz);
     r[5] = (float)(0.5 * (M0[5] + M0[7]) + syz);
-    r[6] = (float)sxx; r[7] = (float)syy; r[8] = (float)szz;
-    r[9] = (float)sxy; r[10] = (float)sxz; r[11] = (float)syz;
-    r[12] = (float)(U[5] - U[7]);
-    r[13] = (float)(U[6] - U[2]);
-    r[14] = (float)(U[1] - U[3]);
-    r[15] = (float)eu[0];
+    r[6] = sxx; r[7] = syy; r[8] = szz;
+    r[9] = sxy; r[10] = sxz; r[11] = syz;
+    r[12] = U[5] - U[7];
+    r[13] = U[6] - U[2];
+    r[14] = U[1] - U[3];
+    r[15] = eu[0];
   }
 }
 
@@ -868,12 +899,23 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
 
   const bool same = (draw_fit == nullptr);
   const int nref = pl.nref, nfit = same ? nref : pl.nfit;
+  const size_t frame_bytes = sizeof(float) * 3 * (size_t)natoms;
+  // frames still on the host: chunked uploads that the superposition below
+  // consumes chunk by chunk
+  std::vector<int> cb_ref{0, nref}, cb_fit{0, nfit};
+  int nc_ref = 1, nc_fit = 1;
+  if (pl.href)
+    MDS_TRY(mds_upload_chunked(ctx, const_cast<float*>(draw_ref), pl.href, nref, frame_bytes, 0, cb_ref, &nc_ref));
+  if (pl.hfit && !same)
+    MDS_TRY(mds_upload_chunked(ctx, const_cast<float*>(draw_fit), pl.hfit, nfit, frame_bytes, MDS_MAX_CHUNKS,
+                               cb_fit, &nc_fit));
   // the first reference frame, centred, defines the template
   DevBuf Y0(ctx), E0(ctx);
   MDS_TRY(Y0.alloc(ctx, sizeof(float) * 3 * Ap));
   MDS_TRY(E0.alloc(ctx, sizeof(double)));
   st.launches = 0;
   st.launches++;
+  if (pl.href) MDS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->chunk_ev[0], 0));
   k_center<<<1, 128, 0, s>>>(draw_ref, 1, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm, Y0.as<float>(),
                              E0.as<double>());
   MDS_CUDA(ctx, cudaGetLastError());
@@ -896,15 +938,26 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_CUDA(ctx, cudaMemcpyAsync(dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(Ar.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
   MDS_TRY(Rr.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nref));
-  MDS_TRY(launch_prep(ctx, draw_ref, nref, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm, dmu.as<float>(),
-                      dM0.as<double>(), pl.nofit, Ar.as<float>(), Rr.as<float>()));
+  // superposition, one upload chunk at a time
+  auto prep_chunks = [&](const float* draw, bool host, const std::vector<int>& cb, int nc, int ev0, float* A,
+                         float* R) -> int {
+    for (int c = 0; c < nc; ++c) {
+      if (host) MDS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->chunk_ev[ev0 + c], 0));
+      const int f0 = cb[c], nf = cb[c + 1] - cb[c];
+      MDS_TRY(launch_prep(ctx, draw + (size_t)f0 * 3 * natoms, nf, natoms, Ap, dmass.as<float>(), dswn.as<float>(),
+                          tm, dmu.as<float>(), dM0.as<double>(), pl.nofit, A + (size_t)f0 * 3 * Ap,
+                          R + (size_t)f0 * MDS_REC));
+    }
+    return MDS_OK;
+  };
+  MDS_TRY(prep_chunks(draw_ref, pl.href != nullptr, cb_ref, nc_ref, 0, Ar.as<float>(), Rr.as<float>()));
   const float* Afp = Ar.as<float>();
   const float* Rfp = Rr.as<float>();
   if (!same) {
     MDS_TRY(Af.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
     MDS_TRY(Rf.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nfit));
-    MDS_TRY(launch_prep(ctx, draw_fit, nfit, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
-                        dmu.as<float>(), dM0.as<double>(), pl.nofit, Af.as<float>(), Rf.as<float>()));
+    MDS_TRY(prep_chunks(draw_fit, pl.hfit != nullptr, cb_fit, nc_fit, MDS_MAX_CHUNKS, Af.as<float>(),
+                        Rf.as<float>()));
     Afp = Af.as<float>();
     Rfp = Rf.as<float>();
   }

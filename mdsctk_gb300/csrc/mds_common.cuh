@@ -15,6 +15,8 @@
 
 #include "../../include/mdsgpu.h"
 
+#define MDS_MAX_CHUNKS 8  // chunks of a pipelined frame upload
+
 struct mds_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -30,10 +32,26 @@ struct mds_ctx {
   mds_knn_stats stats{};
   // timing of the last call's dominant kernel (CUDA events on ctx->stream)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // host-to-device uploads in chunks (created on first use): two copy
+  // streams, one event per chunk, one event ordering the copies after the
+  // work already queued on `stream`
+  cudaStream_t copy_stream[2] = {nullptr, nullptr};
+  cudaEvent_t chunk_ev[MDS_MAX_CHUNKS * 2] = {};
+  cudaEvent_t order_ev = nullptr;
 };
 
 // Record an error message on the context and return `code`.
 int mds_fail(mds_ctx* ctx, int code, const char* fmt, ...);
+
+// Upload n frames of `frame_bytes` each from host memory to dst in up to
+// MDS_MAX_CHUNKS chunks, alternating between the context's two copy streams
+// and ordered after the work already queued on ctx->stream. Chunk c covers
+// frames [bounds[c], bounds[c+1]) and completes event ctx->chunk_ev[ev0 + c];
+// the consumer waits on that event before reading the chunk. From pageable
+// host memory the copies are correct but do not overlap. Returns the number
+// of chunks through *nchunks.
+int mds_upload_chunked(mds_ctx* ctx, void* dst, const void* src, int n, size_t frame_bytes, int ev0,
+                       std::vector<int>& bounds, int* nchunks);
 
 // Free cached device blocks until at most `keep` bytes remain cached
 // (synchronises the context's stream first).

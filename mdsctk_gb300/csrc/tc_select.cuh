@@ -19,15 +19,30 @@ __device__ inline float warp_select_keep2(uint64_t* src, int n0, int off1, int n
     const int x = lane + 32 * i;
     kv[i] = (x < n0 || (x >= off1 && x < off1 + n1)) ? src[x] : MDS_KEY_INF;
   }
-  uint64_t prefix = 0, mask = 0;
+  // Leading bytes that every valid key shares (values of one magnitude share
+  // their sign/exponent byte) are skipped: their histogram would put all keys
+  // in one bucket, one shared-memory atomic after another.
+  uint32_t hmin = 0xffffffffu, hmax = 0u;
+#pragma unroll
+  for (int i = 0; i < PER; ++i)
+    if (kv[i] != MDS_KEY_INF) {
+      const uint32_t hv = (uint32_t)(kv[i] >> 32);
+      hmin = min(hmin, hv);
+      hmax = max(hmax, hv);
+    }
+  hmin = __reduce_min_sync(0xffffffffu, hmin);
+  hmax = __reduce_max_sync(0xffffffffu, hmax);
+  const int same_bytes = (hmin <= hmax) ? ((hmin == hmax) ? 4 : __clz(hmin ^ hmax) / 8) : 0;
+  uint64_t mask = same_bytes ? (~0ull << (64 - 8 * same_bytes)) : 0ull;
+  uint64_t prefix = ((uint64_t)hmin << 32) & mask;
   int need = Kp;
-  for (int pass = 7; pass >= 0; --pass) {
+  for (int pass = 7 - same_bytes; pass >= 0; --pass) {
     const int sh = pass * 8;
     for (int b = lane; b < 256; b += 32) hist[b] = 0;
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < PER; ++i)
-      if ((kv[i] & mask) == prefix) atomicAdd(&hist[(int)((kv[i] >> sh) & 255u)], 1);
+      if (kv[i] != MDS_KEY_INF && (kv[i] & mask) == prefix) atomicAdd(&hist[(int)((kv[i] >> sh) & 255u)], 1);
     __syncwarp();
     int c[8], loc = 0;
 #pragma unroll

@@ -141,3 +141,19 @@ def test_knn_data_fp32_large_k(ctx, oracle):
     assert ctx.stats()["kprime"] == 192
     od, oi = oracle.knn_data(x, None, 150)
     _check(d, i, od, oi)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fit_rows", [None, 700])
+def test_knn_data_tc_pilot_pass(ctx, oracle, fit_rows):
+    """9,000 reference vectors (71 column tiles): the screen first seeds every
+    row's threshold from 16 tiles (around the diagonal for a set against
+    itself, spread over the set for separate fit vectors)."""
+    rng = np.random.default_rng(21)
+    ref = synth.dihedral_vectors(9000, 16, seed=12).astype(np.float64)
+    fit = None if fit_rows is None else rng.normal(scale=0.7, size=(fit_rows, 16))
+    d, i = ctx.knn_data(ref, fit, 12, precision="bf16x3")
+    st = ctx.stats()
+    od, oi = oracle.knn_data(ref, fit, 12)
+    _check(d, i, od, oi)
+    assert st["launches"] == (5 if fit is None else 7)  # prep(s), split(s), pilot, screen, recheck
