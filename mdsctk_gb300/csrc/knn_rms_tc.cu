@@ -73,31 +73,56 @@ __device__ __forceinline__ float from_lp<__half>(__half x) { return __half2float
 
 // layout 0 (fit side, A): row t*128 + q*32 + 3f + c  <- frame t*40 + q*10 + f
 // layout 1 (ref side, B): row t*240 + c*80 + g        <- frame t*80 + g
+// One thread per 8 consecutive atoms of a row: two 16-byte loads, two
+// 16-byte stores (hi, lo).
+template <class T>
+__device__ __forceinline__ unsigned short lp_bits(T x);
+template <>
+__device__ __forceinline__ unsigned short lp_bits<__nv_bfloat16>(__nv_bfloat16 x) { return __bfloat16_as_ushort(x); }
+template <>
+__device__ __forceinline__ unsigned short lp_bits<__half>(__half x) { return __half_as_ushort(x); }
+
 template <class T>
 __global__ void k_tc_split(const float* __restrict__ dev, int n, int Ap, int layout, int rows, float scale,
                            T* __restrict__ out) {
-  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t total = (int64_t)rows * Ap;
-  if (idx >= total) return;
-  int r = (int)(idx / Ap), k = (int)(idx % Ap);
+  const int A8 = Ap >> 3;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)rows * A8) return;
+  const int r = (int)(idx / A8), k = (int)(idx % A8) * 8;
   int frame, c;
   bool valid;
   if (layout == 0) {
-    int t = r / TC_M, w = r % TC_M, q = w / 32, l = w % 32;
+    const int t = r / TC_M, w = r % TC_M, q = w / 32, l = w % 32;
     frame = t * TC_FR_M + q * 10 + l / 3;
     c = l % 3;
     valid = (l < 30) && frame < n;
   } else {
-    int t = r / TC_N, w = r % TC_N;
+    const int t = r / TC_N, w = r % TC_N;
     c = w / TC_FR_N;
     frame = t * TC_FR_N + w % TC_FR_N;
     valid = frame < n;
   }
-  float x = valid ? dev[((int64_t)frame * 3 + c) * Ap + k] * scale : 0.0f;
-  T hi = to_lp<T>(x);
-  T lo = to_lp<T>(x - from_lp<T>(hi));
-  out[(int64_t)r * 2 * Ap + k] = hi;
-  out[(int64_t)r * 2 * Ap + Ap + k] = lo;
+  float x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (valid) {
+    const float4* src = reinterpret_cast<const float4*>(dev + ((int64_t)frame * 3 + c) * Ap + k);
+    const float4 a = __ldg(src), b = __ldg(src + 1);
+    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+  }
+  unsigned short hb[8], lb[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const float v = x[e] * scale;
+    const T hi = to_lp<T>(v);
+    hb[e] = lp_bits<T>(hi);
+    lb[e] = lp_bits<T>(to_lp<T>(v - from_lp<T>(hi)));
+  }
+  uint4 h4, l4;
+  h4.x = hb[0] | ((unsigned)hb[1] << 16); h4.y = hb[2] | ((unsigned)hb[3] << 16);
+  h4.z = hb[4] | ((unsigned)hb[5] << 16); h4.w = hb[6] | ((unsigned)hb[7] << 16);
+  l4.x = lb[0] | ((unsigned)lb[1] << 16); l4.y = lb[2] | ((unsigned)lb[3] << 16);
+  l4.z = lb[4] | ((unsigned)lb[5] << 16); l4.w = lb[6] | ((unsigned)lb[7] << 16);
+  *reinterpret_cast<uint4*>(out + (int64_t)r * 2 * Ap + k) = h4;
+  *reinterpret_cast<uint4*>(out + (int64_t)r * 2 * Ap + Ap + k) = l4;
 }
 
 static float tc_scale(unsigned prec) { return prec == MDS_PREC_FP16X3 ? 64.0f : 1.0f; }
@@ -109,7 +134,7 @@ int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOp
   if (layout == 0) op.rowsA = rows; else op.rowsB = rows;
   op.n = n;
   op.K = pl.Ap;
-  int64_t total = (int64_t)rows * pl.Ap;
+  int64_t total = (int64_t)rows * (pl.Ap / 8);
   int blocks = (int)((total + 255) / 256);
   ctx->stats.launches++;
   if (pl.prec == MDS_PREC_FP16X3)
@@ -270,26 +295,43 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       const int rt = item / nseg, seg = item % nseg;
       const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
       const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
+      uint32_t skipbits = 0;  // bit b: tile ti0 + b of the current batch of 8 is skipped
       for (int ti = 0; ti < t1 - t0 && ok; ++ti) {
         const int tile = tile_order(ti, t0, t1, td);
-        if (pivlb) {
-          bool can = false;
-          if (*(volatile int*)&S->thr_item == item) {
+        if (pivlb && (ti & 7) == 0) {
+          // skip test of the next 8 tiles at once (4 lanes per tile, 10 rows
+          // per lane: one round of loads instead of one per tile), against
+          // the rows' thresholds now, which only tighten later
+          skipbits = 0;
+          int live = (lane == 0) ? (*(volatile int*)&S->thr_item == item) : 0;
+          live = __shfl_sync(0xffffffffu, live, 0);
+          if (live) {
             __threadfence_block();
-            can = true;
-            const float rad = __ldg(prad + tile);
-            for (int r = lane; r < TC_FR_M; r += 32) {
-              const int gi = rt * TC_FR_M + r;
-              if (gi >= nfit) continue;
-              float thr = *(volatile float*)&S->thr[r];
-              if (rowthr) thr = fminf(thr, __ldcg(rowthr + gi));
-              const float L = __ldg(pivlb + (int64_t)tile * nfit + gi) - rad;
-              if (!(L > 0.0f && L * L > thr)) can = false;
+            const int tj = ti + (lane >> 2), r0 = (lane & 3) * 10;
+            bool can = tj < t1 - t0;
+            if (can) {
+              const int tb = tile_order(tj, t0, t1, td);
+              const float rad = __ldg(prad + tb);
+#pragma unroll
+              for (int x = 0; x < 10; ++x) {
+                const int gi = rt * TC_FR_M + r0 + x;
+                if (gi < nfit) {
+                  float thr = *(volatile float*)&S->thr[r0 + x];
+                  if (rowthr) thr = fminf(thr, __ldcg(rowthr + gi));
+                  const float L = __ldg(pivlb + (int64_t)tb * nfit + gi) - rad;
+                  if (!(L > 0.0f && L * L > thr)) can = false;
+                }
+              }
             }
-            if (*(volatile int*)&S->thr_item != item) can = false;  // moved on meanwhile
+            const unsigned bal = __ballot_sync(0xffffffffu, can);
+            int still = (lane == 0) ? (*(volatile int*)&S->thr_item == item) : 0;  // not moved on meanwhile
+            still = __shfl_sync(0xffffffffu, still, 0);
+            if (still)
+              for (int b = 0; b < 8; ++b)
+                if (((bal >> (4 * b)) & 0xFu) == 0xFu) skipbits |= 1u << b;
           }
-          if (__all_sync(0xffffffffu, can)) continue;
         }
+        if ((skipbits >> (ti & 7)) & 1u) continue;
         if (!(ok = push(item, tile))) break;
         if (lane == 0) {
           for (int kb = 0; kb < nkb; ++kb) {
