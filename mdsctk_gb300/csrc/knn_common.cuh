@@ -102,8 +102,10 @@ int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, co
                   const float* dswn, float tm, float* Y, double* E);
 // Centring + superposition of n raw frames (three kernels, no scratch
 // buffer): deviations and records only (knn_rms.cu).
+// Uhl (optional): the frames' U = sum a mu^T as double-float pairs [n][18],
+// which the recheck needs for the reference frames.
 int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
-                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R);
+                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R, float* Uhl = nullptr);
 int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit, std::vector<double>& mu,
                    double M0[9]);
 int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* recf,
@@ -111,8 +113,9 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
                        int* cand_n);
 // Exact recheck from the superposed deviations (Af/Ar [n][3][Ap]) and the
 // template mu [3][Ap] (knn_rms.cu).
+// Ur: the reference frames' U as written by launch_prep (unused with nofit).
 int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
-                   int nrows, const int* rowlist, int mode, const uint64_t* cand,
+                   const float* Ur, int nrows, const int* rowlist, int mode, const uint64_t* cand,
                    const int* cand_n, int nseg, int segstride, int Kp, int k, double* out_d, int* out_i,
                    int* flagged, int* nflag);
 int choose_nseg_fp32(int nfit, int num_sms, int nref);

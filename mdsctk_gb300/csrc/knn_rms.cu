@@ -92,6 +92,53 @@ __device__ __forceinline__ void block_sum_vec32(const float (&p)[N], float (&out
   __syncthreads();
 }
 
+// Double-float accumulation (hi + lo, an unevaluated sum): products by an
+// FMA-exact TwoProduct, additions by Knuth's TwoSum. The _rn intrinsics keep
+// the compiler from contracting the steps into FMAs, which would break the
+// error terms.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float bh, float bl) {
+  const float t = __fadd_rn(hi, bh);
+  const float z = __fsub_rn(t, hi);
+  const float te = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(bh, z));
+  hi = t;
+  lo = __fadd_rn(lo, __fadd_rn(te, bl));
+}
+__device__ __forceinline__ void df_add_prod(float& hi, float& lo, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  df_add(hi, lo, p, fmaf(a, b, -p));
+}
+// The 9 sums U[3c+d] = sum_atoms a_c mu_d of a frame as double-float pairs,
+// over the block: out[2i] = hi, out[2i+1] = lo of U[i] (thread 0; red holds
+// (blockDim/32) * 18 floats). Their differences between two frames,
+// sum mu (a_i - a_j)^T, cancel to the size of the frames' difference, so they
+// are kept to about 2^-48 relative.
+__device__ __forceinline__ void block_sum_df9(float (&h)[9], float (&l)[9], float* red, float* out) {
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < 9; ++i)
+    for (int o = 16; o > 0; o >>= 1) {
+      const float bh = __shfl_xor_sync(0xffffffffu, h[i], o), bl = __shfl_xor_sync(0xffffffffu, l[i], o);
+      df_add(h[i], l[i], bh, bl);
+    }
+  __syncthreads();
+  if (ln == 0)
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      red[w * 18 + 2 * i] = h[i];
+      red[w * 18 + 2 * i + 1] = l[i];
+    }
+  __syncthreads();
+  if (threadIdx.x < 9) {
+    const int i = threadIdx.x;
+    float sh = red[2 * i], sl = red[2 * i + 1];
+    for (int j = 1; j < nw; ++j) df_add(sh, sl, red[j * 18 + 2 * i], red[j * 18 + 2 * i + 1]);
+    const float t = __fadd_rn(sh, sl);  // renormalise: hi = fl(hi + lo)
+    out[2 * i] = t;
+    out[2 * i + 1] = __fsub_rn(sl, __fsub_rn(t, sh));
+  }
+  __syncthreads();
+}
+
 // Block sum of N values at once: every warp reduces its N partial sums with
 // shuffles, lane 0 stores them in red[warp * N + i], one barrier, then every
 // thread adds the warps' rows in order. red holds (blockDim/32) * N doubles.
@@ -228,8 +275,9 @@ __global__ void k_prep_rot(int n, const double* __restrict__ M0, float* __restri
 __global__ void __launch_bounds__(128) k_prep_out(const float* __restrict__ raw, int n, int natoms, int Ap,
                                                   const float* __restrict__ swn, const float* __restrict__ mu,
                                                   const double* __restrict__ M0, int nofit, float* __restrict__ dev,
-                                                  float* __restrict__ rec) {
+                                                  float* __restrict__ rec, float* __restrict__ uhl) {
   __shared__ float red[5 * 10];
+  __shared__ float redu[4 * 18];
   const int f = blockIdx.x;
   if (f >= n) return;
   const float* x = raw + (int64_t)f * natoms * 3;
@@ -238,6 +286,7 @@ __global__ void __launch_bounds__(128) k_prep_out(const float* __restrict__ raw,
   float R[9];
   for (int i = 0; i < 9; ++i) R[i] = nofit ? ((i % 4 == 0) ? 1.0f : 0.0f) : r[3 + i];
   float ea = 0.f, u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float uh[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ul[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float* o = dev + (int64_t)f * 3 * Ap;
 #pragma unroll 2
   for (int a = threadIdx.x; a < Ap; a += blockDim.x) {
@@ -254,10 +303,14 @@ __global__ void __launch_bounds__(128) k_prep_out(const float* __restrict__ raw,
         ea = fmaf(av[c], av[c], ea);
         for (int d = 0; d < 3; ++d) u[3 * c + d] = fmaf(av[c], mc[d], u[3 * c + d]);
       }
+      if (uhl)
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d) df_add_prod(uh[3 * c + d], ul[3 * c + d], av[c], mc[d]);
     } else {
       for (int c = 0; c < 3; ++c) o[c * Ap + a] = 0.0f;
     }
   }
+  if (uhl) block_sum_df9(uh, ul, redu, uhl + (int64_t)f * 18);  // uniform branch: all threads or none
   const float eup[10] = {ea, u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
   float eu[10];
   block_sum_vec32<10>(eup, eu, red);  // every thread has read the record row before this barrier
@@ -498,37 +551,34 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
 // is formed from the small d, so FP32 keeps them accurate; RMSD^2 = D - 2 nu
 // (qcp.cuh: shifted_rmsd2_f32). sa = a_i, sx = x~_i (shared memory), C6 =
 // (Cxx, Cyy, Czz, Cxy, Cxz, Cyz).
-__device__ void recheck_chunk(const float* __restrict__ sa, const float* __restrict__ sx, const float* C6,
-                              const float* __restrict__ Ar, int Ap, int natoms, const int* cj, int nc, bool nofit,
-                              float* sd, float* ssum) {
+__device__ void recheck_chunk(const float* __restrict__ sa, const float* __restrict__ ui, const float* C6,
+                              const float* __restrict__ Ar, const float* __restrict__ Ur, int Ap, const int* cj,
+                              int nc, bool nofit, float* sd, float* ssum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // A warp takes four candidates at a time, eight lanes each; the lanes of
-  // the four groups read the same atoms of the row (shared memory
-  // broadcast), so the row is read once per four candidates. Four atoms per
-  // lane and load (Ap is a multiple of 64; padding atoms are zero in a_i,
-  // a_j and mu, so they add nothing).
+  // A warp takes four candidates at a time, eight lanes each; four atoms per
+  // lane and load (Ap is a multiple of 64; padding atoms are zero in a_i and
+  // a_j, so they add nothing). Per candidate: D = sum |d|^2 and
+  // Q[3r+s] = sum a_i,r d_s with d = a_i - a_j; the row's deviations are the
+  // only shared-memory reads.
   const int grp = lane >> 3, gl = lane & 7;
   const int Ap4 = Ap >> 2;
   const float4* sa4 = reinterpret_cast<const float4*>(sa);
-  const float4* sx4 = reinterpret_cast<const float4*>(sx);
-  (void)natoms;
   for (int c0 = 4 * warp; c0 < nc; c0 += 4 * nw) {
     const int c = c0 + grp;
     const bool valid = c < nc;
     const float4* aj4 = reinterpret_cast<const float4*>(Ar + (int64_t)cj[valid ? c : c0] * 3 * Ap);
-    float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // D, P[9]
+    float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // D, Q[9]
     for (int q = gl; q < Ap4; q += 8) {
       const float4 ia = sa4[q], ib = sa4[Ap4 + q], ic = sa4[2 * Ap4 + q];
       const float4 ja = __ldg(aj4 + q), jb = __ldg(aj4 + Ap4 + q), jc = __ldg(aj4 + 2 * Ap4 + q);
+      const float x0[4] = {ia.x, ia.y, ia.z, ia.w}, x1[4] = {ib.x, ib.y, ib.z, ib.w};
+      const float x2[4] = {ic.x, ic.y, ic.z, ic.w};
       const float d0[4] = {ia.x - ja.x, ia.y - ja.y, ia.z - ja.z, ia.w - ja.w};
       const float d1[4] = {ib.x - jb.x, ib.y - jb.y, ib.z - jb.z, ib.w - jb.w};
       const float d2[4] = {ic.x - jc.x, ic.y - jc.y, ic.z - jc.z, ic.w - jc.w};
 #pragma unroll
       for (int e = 0; e < 4; ++e) v[0] = fmaf(d0[e], d0[e], fmaf(d1[e], d1[e], fmaf(d2[e], d2[e], v[0])));
       if (!nofit) {
-        const float4 xa = sx4[q], xb = sx4[Ap4 + q], xc = sx4[2 * Ap4 + q];
-        const float x0[4] = {xa.x, xa.y, xa.z, xa.w}, x1[4] = {xb.x, xb.y, xb.z, xb.w};
-        const float x2[4] = {xc.x, xc.y, xc.z, xc.w};
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           v[1] = fmaf(x0[e], d0[e], v[1]); v[2] = fmaf(x0[e], d1[e], v[2]); v[3] = fmaf(x0[e], d2[e], v[3]);
@@ -553,7 +603,19 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
     const float* w = ssum + c * 10;
     float r2 = w[0];
     if (!nofit) {
-      const float* P = w + 1;  // P[3r+s] = sum x~_r d_s
+      // P[3r+s] = sum x~_r d_s = Q[3r+s] + sum mu_r d_s, and
+      // sum mu_r d_s = U_i[3s+r] - U_j[3s+r] from the frames' double-float U
+      const float* uj = Ur + (int64_t)cj[c] * 18;
+      float P[9];
+#pragma unroll
+      for (int rr = 0; rr < 3; ++rr)
+#pragma unroll
+        for (int ss = 0; ss < 3; ++ss) {
+          const int iu = 3 * ss + rr;
+          float dh = ui[2 * iu], dl = ui[2 * iu + 1];
+          df_add(dh, dl, -__ldg(uj + 2 * iu), -__ldg(uj + 2 * iu + 1));
+          P[3 * rr + ss] = w[1 + 3 * rr + ss] + (dh + dl);
+        }
       r2 = shifted_rmsd2_f32(w[0], C6[0] - P[0], C6[1] - P[4], C6[2] - P[8], 2.0f * C6[3] - (P[1] + P[3]),
                              2.0f * C6[4] - (P[2] + P[6]), 2.0f * C6[5] - (P[5] + P[7]), P[7] - P[5], P[2] - P[6],
                              P[3] - P[1]);
@@ -568,40 +630,46 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
 // (exact row). mode 2 (full matrix): write every exact distance in reference
 // order. Output: out_d/out_i rows of width `width` at row index grow.
 __global__ void __launch_bounds__(RC_THREADS, 4)
-k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const float* __restrict__ mu, int nrows,
+k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const float* __restrict__ mu,
+          const float* __restrict__ Ur, int nrows,
           const int* __restrict__ rowlist, int Nr, int Ap, int natoms, int nofit, int mode,
           const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int segstride, int Kp, int k,
           double* __restrict__ out_d, int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* sa = reinterpret_cast<float*>(smem_raw);                 // [3*Ap] a_i
-  float* sx = sa + 3 * Ap;                                        // [3*Ap] mu + a_i
-  float* sd = sx + 3 * Ap;                                        // [CHUNK]
+  float* sd = sa + 3 * Ap;                                        // [CHUNK]
   int* cj = reinterpret_cast<int*>(sd + RC_CHUNK);                // [CHUNK]
   uint64_t* keys = reinterpret_cast<uint64_t*>(cj + RC_CHUNK);    // merge buffer / top list
   __shared__ int s_total;
   __shared__ double s_red[32 * 6];
   __shared__ float C6[6];
-  __shared__ __align__(16) float ssum[RC_CHUNK * 10];  // per candidate: D, P[9] (float2 stores)
+  __shared__ __align__(16) float ssum[RC_CHUNK * 10];  // per candidate: D, Q[9] (float2 stores)
+  __shared__ float ui[18];                              // the row's U as double-float pairs
+  __shared__ float redu[(RC_THREADS / 32) * 18];
 
   int lr = blockIdx.x;
   if (lr >= nrows) return;
   int grow = rowlist ? rowlist[lr] : lr;
   const float* af = Af + (int64_t)grow * 3 * Ap;
-  for (int e = threadIdx.x; e < 3 * Ap; e += blockDim.x) {
-    const float av = af[e];
-    sa[e] = av;
-    sx[e] = mu[e] + av;
-  }
+  for (int e = threadIdx.x; e < 3 * Ap; e += blockDim.x) sa[e] = af[e];
   {
+    // C6 = sum x~ x~^T of the row (x~ = mu + a_i), and its U = sum a_i mu^T
+    // as double-float pairs, the same sums as the reference frames' Ur
     float p[6] = {0, 0, 0, 0, 0, 0};
+    float uh[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ul[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
-      const float x0 = mu[a] + af[a], x1 = mu[Ap + a] + af[Ap + a], x2 = mu[2 * Ap + a] + af[2 * Ap + a];
+      const float m[3] = {mu[a], mu[Ap + a], mu[2 * Ap + a]}, av[3] = {af[a], af[Ap + a], af[2 * Ap + a]};
+      const float x0 = m[0] + av[0], x1 = m[1] + av[1], x2 = m[2] + av[2];
       p[0] = fmaf(x0, x0, p[0]); p[1] = fmaf(x1, x1, p[1]); p[2] = fmaf(x2, x2, p[2]);
       p[3] = fmaf(x0, x1, p[3]); p[4] = fmaf(x0, x2, p[4]); p[5] = fmaf(x1, x2, p[5]);
+      if (!nofit)
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d) df_add_prod(uh[3 * c + d], ul[3 * c + d], av[c], m[d]);
     }
     double c[6];
     block_sum_vecf<6>(p, c, s_red);
     if (threadIdx.x < 6) C6[threadIdx.x] = (float)c[threadIdx.x];
+    if (!nofit) block_sum_df9(uh, ul, redu, ui);
     __syncthreads();
   }
   const int k1 = k + 1;
@@ -612,7 +680,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
       int nc = min(RC_CHUNK, Nr - base);
       for (int c = threadIdx.x; c < nc; c += blockDim.x) cj[c] = base + c;
       __syncthreads();
-      recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd, ssum);
+      recheck_chunk(sa, ui, C6, Ar, Ur, Ap, cj, nc, nofit, sd, ssum);
       for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         out_d[(int64_t)grow * Nr + base + c] = (double)sd[c] * 10.0;
         out_i[(int64_t)grow * Nr + base + c] = base + c;
@@ -672,7 +740,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
     for (int c = threadIdx.x; c < nc; c += blockDim.x)
       cj[c] = (mode == 0) ? mds_key_index(keys[base + c]) : base + c;
     __syncthreads();
-    recheck_chunk(sa, sx, C6, Ar, Ap, natoms, cj, nc, nofit, sd, ssum);
+    recheck_chunk(sa, ui, C6, Ar, Ur, Ap, cj, nc, nofit, sd, ssum);
     // place the chunk after the current k1 best and re-sort
     for (int c = threadIdx.x; c < RC_CHUNK; c += blockDim.x)
       top[k1 + c] = (c < nc) ? mds_pack_key(sd[c], cj[c]) : MDS_KEY_INF;
@@ -718,7 +786,7 @@ size_t recheck_smem(int Ap, int Kp, int k, int mode) {
     merge = (size_t)std::max(Kp, 1);
   }
   size_t keys = std::max(merge + TP2, (size_t)0);
-  return sizeof(float) * (6 * Ap + RC_CHUNK) + sizeof(int) * RC_CHUNK + sizeof(uint64_t) * keys;
+  return sizeof(float) * (3 * Ap + RC_CHUNK) + sizeof(int) * RC_CHUNK + sizeof(uint64_t) * keys;
 }
 
 // ---------------------------------------------------------------------------
@@ -797,7 +865,7 @@ int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofi
 }
 
 int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
-                   int nrows, const int* rowlist, int mode,
+                   const float* Ur, int nrows, const int* rowlist, int mode,
                    const uint64_t* cand, const int* cand_n, int nseg, int segstride, int Kp, int k,
                    double* out_d, int* out_i, int* flagged, int* nflag) {
   size_t smem = recheck_smem(pl.Ap, Kp, k, mode);
@@ -807,7 +875,7 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const fl
     int TP2 = 1;
     while (TP2 < k + 1 + RC_CHUNK) TP2 <<= 1;
     size_t keys = std::max((size_t)P2, (size_t)Kp + TP2);
-    smem = sizeof(float) * (6 * pl.Ap + RC_CHUNK) + sizeof(int) * RC_CHUNK + sizeof(uint64_t) * keys;
+    smem = sizeof(float) * (3 * pl.Ap + RC_CHUNK) + sizeof(int) * RC_CHUNK + sizeof(uint64_t) * keys;
   }
   if (smem > 227 * 1024)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck needs %zu bytes of shared memory (natoms/k too large)", smem);
@@ -817,7 +885,7 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const fl
   if (smem > limit) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "recheck shared memory %zu > %zu", smem, limit);
   if (nrows > 0) ctx->stats.launches++;
   if (nrows > 0)
-    k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Af, Ar, mu, nrows, rowlist, pl.nref, pl.Ap, pl.natoms,
+    k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Af, Ar, mu, Ur, nrows, rowlist, pl.nref, pl.Ap, pl.natoms,
                                                         pl.nofit, mode, cand, cand_n, nseg, segstride, Kp, k,
                                                         out_d, out_i, flagged, nflag);
   MDS_CUDA(ctx, cudaGetLastError());
@@ -835,12 +903,12 @@ int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, co
 }
 
 int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
-                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R) {
+                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R, float* Uhl) {
   if (n <= 0) return MDS_OK;
   ctx->stats.launches += nofit ? 2 : 3;
   k_prep_sums<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dmass, dswn, tm, dmu, nofit, R);
   if (!nofit) k_prep_rot<<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, dM0, R);
-  k_prep_out<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dswn, dmu, dM0, nofit, A, R);
+  k_prep_out<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dswn, dmu, dM0, nofit, A, R, Uhl);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
@@ -938,26 +1006,29 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_CUDA(ctx, cudaMemcpyAsync(dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(Ar.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nref));
   MDS_TRY(Rr.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nref));
+  DevBuf Ur(ctx);  // the reference frames' U = sum a mu^T as double-float pairs (recheck)
+  MDS_TRY(Ur.alloc(ctx, sizeof(float) * 18 * (size_t)nref));
   // superposition, one upload chunk at a time
   auto prep_chunks = [&](const float* draw, bool host, const std::vector<int>& cb, int nc, int ev0, float* A,
-                         float* R) -> int {
+                         float* R, float* U) -> int {
     for (int c = 0; c < nc; ++c) {
       if (host) MDS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->chunk_ev[ev0 + c], 0));
       const int f0 = cb[c], nf = cb[c + 1] - cb[c];
       MDS_TRY(launch_prep(ctx, draw + (size_t)f0 * 3 * natoms, nf, natoms, Ap, dmass.as<float>(), dswn.as<float>(),
                           tm, dmu.as<float>(), dM0.as<double>(), pl.nofit, A + (size_t)f0 * 3 * Ap,
-                          R + (size_t)f0 * MDS_REC));
+                          R + (size_t)f0 * MDS_REC, U ? U + (size_t)f0 * 18 : nullptr));
     }
     return MDS_OK;
   };
-  MDS_TRY(prep_chunks(draw_ref, pl.href != nullptr, cb_ref, nc_ref, 0, Ar.as<float>(), Rr.as<float>()));
+  MDS_TRY(prep_chunks(draw_ref, pl.href != nullptr, cb_ref, nc_ref, 0, Ar.as<float>(), Rr.as<float>(),
+                      pl.nofit ? nullptr : Ur.as<float>()));
   const float* Afp = Ar.as<float>();
   const float* Rfp = Rr.as<float>();
   if (!same) {
     MDS_TRY(Af.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
     MDS_TRY(Rf.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nfit));
     MDS_TRY(prep_chunks(draw_fit, pl.hfit != nullptr, cb_fit, nc_fit, MDS_MAX_CHUNKS, Af.as<float>(),
-                        Rf.as<float>()));
+                        Rf.as<float>(), nullptr));
     Afp = Af.as<float>();
     Rfp = Rf.as<float>();
   }
@@ -971,7 +1042,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   }
   if (pl.full) {
     MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
-    MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), nfit, nullptr, 2, nullptr, nullptr, 1, 1,
+    MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 2, nullptr, nullptr, 1, 1,
                            1, 0, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
     MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
     MDS_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
@@ -1036,7 +1107,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.kprime = Kp;
     return MDS_OK;
   }
-  MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), nfit, nullptr, 0, cand.as<uint64_t>(),
+  MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 0, cand.as<uint64_t>(),
                          cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i, flagged.as<int>(),
                          nflag.as<int>()));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
@@ -1067,7 +1138,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.passes++;
     if (Kp >= nref || st.passes > 3) {
       // exact rows: every reference is a candidate
-      MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), hflag, rows.as<int>(), 1, nullptr,
+      MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), hflag, rows.as<int>(), 1, nullptr,
                              nullptr, 1, 1, 1, k, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
       break;
@@ -1079,7 +1150,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)hflag * nseg2));
     MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), hflag, rows.as<int>(), Kp,
                                nseg2, cand.as<uint64_t>(), cand_n.as<int>()));
-    MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), hflag, rows.as<int>(), 0,
+    MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), hflag, rows.as<int>(), 0,
                            cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, Kp, k, dout_d, dout_i,
                            flagged.as<int>(), nflag.as<int>()));
     MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -127,7 +127,7 @@ struct mds_server {
   int n = 0, natoms = 0, Ap = 0, k = 0, nev = 0, Kp = 0, nseg_max = 1, segstride = 0;
   unsigned prec = MDS_PREC_FP32;
   float tm = 0;
-  DevBuf dmass, dswn, dmu, dM0, Y, E, A, R, dZ, ddinv, dlam;
+  DevBuf dmass, dswn, dmu, dM0, Y, E, A, R, U, dZ, ddinv, dlam;
   TcPivots pv;  // landmark pivots for tile skipping (pv.nC = 0: off)
   TcOperands tc;
   std::vector<double> evals;
@@ -196,7 +196,7 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
                                nullptr, S->Kp, nseg, sl.cand.as<uint64_t>(), sl.cand_n.as<int>()));
   }
   const int segstride = (S->prec == MDS_PREC_FP32) ? S->Kp : tc_seg_stride();
-  MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), bucket,
+  MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), S->U.as<float>(), bucket,
                          nullptr, 0, sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), nseg, segstride, S->Kp, S->k,
                          sl.out_d.as<double>(), sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>()));
   c->stats.launches++;
@@ -249,7 +249,7 @@ static int finish_batch(mds_server* S, Slot& sl) {
     MDS_CUDA(c, cudaMemsetAsync(sl.nflag.p, 0, sizeof(int), c->stream));
     MDS_TRY(launch_screen_fp32(c, pl, sl.A.as<float>(), S->A.as<float>(), sl.R.as<float>(), S->R.as<float>(), h,
                                drows.as<int>(), Kp, nseg2, cand.as<uint64_t>(), cand_n.as<int>()));
-    MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), h,
+    MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), S->U.as<float>(), h,
                            drows.as<int>(), 0, cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, Kp, S->k,
                            sl.out_d.as<double>(), sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>()));
     MDS_CUDA(c, cudaMemcpyAsync(&nflag, sl.nflag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -262,7 +262,7 @@ static int finish_batch(mds_server* S, Slot& sl) {
     }
   }
   if (nflag > 0)
-    MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), nflag,
+    MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), S->U.as<float>(), nflag,
                            drows.as<int>(), 1, nullptr, nullptr, 1, 1, 1, S->k, sl.out_d.as<double>(),
                            sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>()));
   k_serve_ext<<<(sl.bucket + 127) / 128, 128, 0, c->stream>>>(
@@ -482,9 +482,10 @@ static int build_model(mds_server* S, const float* hxyz, const float* hmass) {
   MDS_CUDA(c, cudaMemcpyAsync(S->dM0.p, M0, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   MDS_TRY(S->A.alloc(c, sizeof(float) * 3 * (size_t)Ap * n));
   MDS_TRY(S->R.alloc(c, sizeof(float) * MDS_REC * (size_t)n));
+  MDS_TRY(S->U.alloc(c, sizeof(float) * 18 * (size_t)n));
   MDS_TRY(launch_prep(c, raw.as<float>(), n, natoms, Ap, S->dmass.as<float>(), S->dswn.as<float>(), tm,
                       S->dmu.as<float>(), S->dM0.as<double>(), (S->cfg.flags & MDS_NOFIT) ? 1 : 0, S->A.as<float>(),
-                      S->R.as<float>()));
+                      S->R.as<float>(), (S->cfg.flags & MDS_NOFIT) ? nullptr : S->U.as<float>()));
   if (S->prec != MDS_PREC_FP32) {
     MDS_TRY(tc_prepare(c, S->plan(n), S->A.as<float>(), n, S->tc, 1));
     if ((n + 79) / 80 >= 4) MDS_TRY(tc_skip_pivots(c, S->plan(n), S->A.as<float>(), S->R.as<float>(), S->pv));
@@ -586,7 +587,7 @@ extern "C" int mds_server_destroy(mds_server* S) {
     mds_destroy(sl.ctx);
   }
   S->dmass.release(); S->dswn.release(); S->dmu.release(); S->dM0.release(); S->Y.release(); S->E.release();
-  S->A.release(); S->R.release(); S->dZ.release(); S->ddinv.release(); S->dlam.release(); S->tc.A.release();
+  S->A.release(); S->R.release(); S->U.release(); S->dZ.release(); S->ddinv.release(); S->dlam.release(); S->tc.A.release();
   S->tc.B.release();
   S->pv.A.release(); S->pv.R.release(); S->pv.rad.release(); S->pv.tc.A.release(); S->pv.tc.B.release();
   mds_destroy(S->main);
