@@ -153,6 +153,38 @@ int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, const doubl
                          unsigned flags, double* out_d, int32_t* out_i, int* k_used);
 
 /*
+ * knn_data_sparse: k nearest sparse vectors by euclidean_distance_sparse
+ * (mdsctk.cpp:362-386). Replaces knn_data_sparse.cpp:176-260 (the reference
+ * reads the vectors from an index file of [int n][int idx[n]] records and a
+ * data file of [double val[n]] records; the tool knn_data_sparse does).
+ *   ref: CSR rows ref_off[n_ref+1] (int64, ref_off[0] = 0), ref_idx, ref_val.
+ *   fit: the same, or fit_off NULL for fit = ref.
+ *   flags: 0, or MDS_FULL for the full row of distances in reference order
+ *   (the reference's -s false; out_i then holds 0..n_ref-1).
+ * Distances are the reference's FP64 walk, operation for operation, so the
+ * written values are bit-identical to the reference's; indices of equal
+ * distances are ordered by index (the reference leaves that order open).
+ * Host buffers; k is clamped to n_ref - 1 and returned in k_used.
+ */
+int mds_knn_data_sparse(mds_ctx* ctx, const int64_t* ref_off, const int32_t* ref_idx, const double* ref_val,
+                        int n_ref, const int64_t* fit_off, const int32_t* fit_idx, const double* fit_val, int n_fit,
+                        int k, unsigned flags, double* out_d, int32_t* out_i, int* k_used);
+
+/*
+ * contact_profile: sparse binary contact maps (contact_profile.cpp:200-262).
+ * For every frame of xyz [nframes][natoms][3] (float, nm) the atom pairs
+ * (g1[i], g2[j]) (0-based atom indices) at distance * 10 < eps (Angstrom)
+ * are contacts; a frame's vector holds the ascending grid indices i*n2 + j
+ * of its contacts, each with value 1.0. Writes offsets[nframes+1] (int64,
+ * offsets[0] = 0); with idx != NULL and idx_cap >= offsets[nframes] also the
+ * indices (call first with idx = NULL to size the buffer). Contacts are
+ * decided in the reference's arithmetic (float differences and squares, a
+ * double sum, sqrt, times 10), so the sets are identical.
+ */
+int mds_contact_profile(mds_ctx* ctx, const float* xyz, int nframes, int natoms, const int32_t* g1, int n1,
+                        const int32_t* g2, int n2, double eps, int64_t* offsets, int32_t* idx, int64_t idx_cap);
+
+/*
  * GROMACS .xtc trajectories, the input format of knn_rms (read through
  * GROMACS in the reference: read_first_xtc / read_next_xtc,
  * knn_rms.cpp:155-203; XTC_file, mdsctk.cpp:217-267).

@@ -87,6 +87,8 @@ SIGNATURES = {
     "mds_knn_rms_superpose": ([_vp, _vp, _i, _i, _vp, _u, _vp, _vp], _i),
     "mds_knn_data": ([_vp, _vp, _i, _vp, _i, _i, _i, _u, _vp, _vp, _ip], _i),
     "mds_knn_data_noalloc": ([_vp, _vp, _i, _vp, _i, _i, _i, _u, _vp, _vp, _ip], _i),
+    "mds_knn_data_sparse": ([_vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _i, _u, _vp, _vp, _ip], _i),
+    "mds_contact_profile": ([_vp, _vp, _i, _i, _vp, _i, _vp, _i, _d, _vp, _vp, ctypes.c_int64], _i),
     "mds_sysparse": ([_vp, _vp, _vp, _i, _i, _i, _u, _vp, _vp, _vp, ctypes.c_int64, _i64p], _i),
     "mds_gesparse": ([_vp, _vp, _vp, _i, _i, _i, _i, _u, _vp, _vp, _vp, ctypes.c_int64, _i64p], _i),
     "mds_decomp_sparse": ([_vp, _i, _vp, _vp, _vp, _d, _i, _i, _d, _i, _u, _vp, _vp, _vp, _ip], _i),

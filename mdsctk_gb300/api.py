@@ -194,6 +194,50 @@ class Context:
         L.check(self.h, rc)
         return d, i
 
+    def knn_data_sparse(self, ref, fit=None, k: int = 1, sort: bool = True):
+        """knn_data_sparse: k nearest sparse vectors (Euclidean). ref/fit:
+        CSR triplets (off int64[n+1], idx int32, val float64), e.g. from
+        sparse_vectors(); fit None = ref. Returns (distances, indices), or the
+        full rows when sort=False."""
+        ro, ri, rv = (np.ascontiguousarray(ref[0], np.int64), np.ascontiguousarray(ref[1], np.int32),
+                      np.ascontiguousarray(ref[2], np.float64))
+        n_ref = len(ro) - 1
+        if fit is None:
+            fo = fi = fv = None
+            n_fit = n_ref
+        else:
+            fo, fi, fv = (np.ascontiguousarray(fit[0], np.int64), np.ascontiguousarray(fit[1], np.int32),
+                          np.ascontiguousarray(fit[2], np.float64))
+            n_fit = len(fo) - 1
+        kk = n_ref if not sort else max(0, min(k, n_ref - 1))
+        d = np.empty((n_fit, kk), np.float64)
+        i = np.empty((n_fit, kk), np.int32)
+        ku = ctypes.c_int(0)
+        rc = self._lib.mds_knn_data_sparse(self.h, _ptr(ro), _ptr(ri), _ptr(rv), n_ref, _ptr(fo), _ptr(fi),
+                                           _ptr(fv), n_fit, int(k), 0 if sort else L.MDS_FULL, _ptr(d), _ptr(i),
+                                           ctypes.byref(ku))
+        L.check(self.h, rc)
+        return d, i
+
+    def contact_profile(self, xyz, g1, g2, eps: float = 9.0):
+        """contact_profile: xyz [nframes, natoms, 3] float32 nm; g1/g2 0-based
+        atom indices. Returns (offsets int64[nframes+1], indices int32): frame
+        f's contacts are indices[offsets[f]:offsets[f+1]] (grid index
+        i * len(g2) + j, ascending), each of value 1.0."""
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        g1 = np.ascontiguousarray(g1, np.int32)
+        g2 = np.ascontiguousarray(g2, np.int32)
+        nframes, natoms = int(xyz.shape[0]), int(xyz.shape[1])
+        off = np.zeros(nframes + 1, np.int64)
+        rc = self._lib.mds_contact_profile(self.h, _ptr(xyz), nframes, natoms, _ptr(g1), len(g1), _ptr(g2), len(g2),
+                                           float(eps), _ptr(off), None, 0)
+        L.check(self.h, rc)
+        idx = np.empty(max(1, int(off[-1])), np.int32)
+        rc = self._lib.mds_contact_profile(self.h, _ptr(xyz), nframes, natoms, _ptr(g1), len(g1), _ptr(g2), len(g2),
+                                           float(eps), _ptr(off), _ptr(idx), int(len(idx)))
+        L.check(self.h, rc)
+        return off, idx[:int(off[-1])]
+
     # ------------------------------------------------------------ sparse
     def sysparse(self, dist, idx, k=None):
         """make_sysparse: returns (n, pcol, irow, val) of the strict lower

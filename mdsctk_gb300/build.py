@@ -65,8 +65,8 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     return LIB
 
 
-TOOLS = ("knn_rms", "knn_data", "make_sysparse", "make_gesparse", "decomp_sparse", "decomp_sparse_nystrom",
-         "auto_decomp_sparse", "auto_decomp_sparse_nystrom")
+TOOLS = ("knn_rms", "knn_data", "knn_data_sparse", "contact_profile", "make_sysparse", "make_gesparse",
+         "decomp_sparse", "decomp_sparse_nystrom", "auto_decomp_sparse", "auto_decomp_sparse_nystrom")
 BINDIR = os.path.join(HERE, "bin")
 
 

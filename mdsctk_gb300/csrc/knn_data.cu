@@ -309,14 +309,19 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
   const int BP2 = next_pow2(k1 + CH);
   double* bval = reinterpret_cast<double*>(keys + (mode == 0 ? Kp : 0));
   int* bidx = reinterpret_cast<int*>(bval + BP2);
-  const int step = (mode == 0) ? max(total, 1) : CH;
+  // mode 0: candidates in order of their bound; the first k+1 + k/4 are
+  // rechecked, the rest only if the next bound is below the (k+1)-th exact
+  // value so far (then nothing later can enter the k+1 best)
+  const int first = (mode == 0) ? min(max(total, 1), k1 + max(8, k1 / 4)) : CH;
+  __shared__ int s_stop;
+  bool stopped = false;
   for (int x = threadIdx.x; x < BP2; x += blockDim.x) {
     bval[x] = __longlong_as_double(0x7ff0000000000000ll);
     bidx[x] = 0x7fffffff;
   }
   __syncthreads();
-  for (int base = 0; base < total; base += step) {
-    int nc = min(step, total - base);
+  for (int base = 0; base < total;) {
+    const int nc = (mode == 0) ? (base == 0 ? first : total - base) : min(CH, total - base);
     for (int c = threadIdx.x; c < BP2 - k1; c += blockDim.x) {
       double v = __longlong_as_double(0x7ff0000000000000ll);
       int j = 0x7fffffff;
@@ -337,7 +342,10 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
           if (ixj > i) {
             double va = bval[i], vb = bval[ixj];
             int ia = bidx[i], ib = bidx[ixj];
-            bool gt = (va > vb) || (va == vb && ia > ib);
+            // the values are non-negative (or +inf): their bit patterns order
+            // as unsigned integers, so the compare stays off the FP64 pipe
+            const unsigned long long ua = __double_as_longlong(va), ub = __double_as_longlong(vb);
+            bool gt = (ua > ub) || (ua == ub && ia > ib);
             bool up = (i & kk) == 0;
             if (gt == up) {
               bval[i] = vb; bval[ixj] = va;
@@ -347,8 +355,17 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
         }
         __syncthreads();
       }
+    base += nc;
+    if (mode == 0 && base < total) {
+      if (threadIdx.x == 0) s_stop = (bval[k1 - 1] < (double)mds_key_value(keys[base])) ? 1 : 0;
+      __syncthreads();
+      if (s_stop) {
+        stopped = true;
+        break;
+      }
+    }
   }
-  if (threadIdx.x == 0 && mode == 0) {
+  if (threadIdx.x == 0 && mode == 0 && !stopped) {
     // strict: a pair left out of the list has a lower bound >= tau, so only
     // dk < tau proves that no left-out pair ties with or beats the k+1-th
     double dk = bval[k1 - 1];

@@ -384,17 +384,21 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         float4 c4[4];
 #pragma unroll
         for (int t4 = 0; t4 < 4; ++t4) c4[t4] = __ldg(ct4 + cc * 4 + t4);
-        uint32_t mask = 0;
+        // four independent mask chains; only passing values are parked
+        uint32_t m4[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
         for (int t4 = 0; t4 < 4; ++t4) {
           const float cv[4] = {c4[t4].x, c4[t4].y, c4[t4].z, c4[t4].w};
 #pragma unroll
           for (int t = 0; t < 4; ++t) {
             const float v = fmaf(mul, __uint_as_float(cur[4 * t4 + t]), cv[t]);
-            sv[(4 * t4 + t) * 32 + lane] = v;
-            mask |= (v < lim ? 1u : 0u) << (4 * t4 + t);
+            if (v < lim) {
+              sv[(4 * t4 + t) * 32 + lane] = v;
+              m4[t4] |= 1u << (4 * t4 + t);
+            }
           }
         }
+        uint32_t mask = (m4[0] | m4[1]) | (m4[2] | m4[3]);
         if (__any_sync(0xffffffffu, mask != 0u)) {
           while (mask) {
             const int t = __ffs(mask) - 1;

@@ -13,90 +13,8 @@
 #include <sstream>
 
 #include "cli.h"
-
-static float element_mass(const std::string& el) {
-  static const std::pair<const char*, float> table[] = {
-      {"H", 1.008f},     {"C", 12.011f},   {"N", 14.0067f}, {"O", 15.9994f}, {"S", 32.06f},
-      {"P", 30.973762f}, {"F", 18.9984f},  {"CL", 35.45f},  {"BR", 79.904f}, {"I", 126.904f},
-      {"NA", 22.98977f}, {"K", 39.0983f},  {"MG", 24.305f}, {"CA", 40.078f}, {"ZN", 65.38f},
-      {"FE", 55.845f},   {"SE", 78.971f}};
-  for (auto& e : table)
-    if (el == e.first) return e.second;
-  return 0.0f;
-}
-
-// element from a PDB/GRO atom name: leading digits skipped, the first letter
-// (protein atom names: CA = alpha carbon, not calcium)
-static std::string element_from_name(const std::string& name) {
-  std::string s;
-  for (char c : name)
-    if (std::isalpha((unsigned char)c)) s += (char)std::toupper((unsigned char)c);
-  if (s.empty()) return s;
-  return s.substr(0, 1);
-}
-
-static bool read_topology(const std::string& path, std::vector<float>& mass) {
-  std::ifstream f(path.c_str());
-  if (!f.good()) return false;
-  mass.clear();
-  std::string line;
-  bool gro = path.size() > 4 && path.substr(path.size() - 4) == ".gro";
-  if (gro) {
-    std::getline(f, line);  // title
-    std::getline(f, line);
-    int n = std::atoi(line.c_str());
-    for (int i = 0; i < n && std::getline(f, line); ++i) {
-      std::string name = line.size() >= 15 ? line.substr(10, 5) : "";
-      mass.push_back(element_mass(element_from_name(name)));
-    }
-    return true;
-  }
-  while (std::getline(f, line)) {
-    if (line.rfind("ATOM", 0) != 0 && line.rfind("HETATM", 0) != 0) continue;
-    std::string el;
-    if (line.size() >= 78) {
-      for (char c : line.substr(76, 2))
-        if (std::isalpha((unsigned char)c)) el += (char)std::toupper((unsigned char)c);
-    }
-    if (el.empty()) el = element_from_name(line.size() >= 16 ? line.substr(12, 4) : "");
-    float m = element_mass(el);
-    if (m == 0.0f) m = element_mass(el.substr(0, 1));
-    mass.push_back(m);
-  }
-  return true;
-}
-
-// Returns 0, -1 (cannot open), -3 (malformed .xtc), or -4 (the .xtc holds
-// `*xtc_atoms` atoms, not natoms).
-static int read_frames(mds_ctx* ctx, const std::string& path, int natoms, std::vector<float>& x, int& n,
-                       int* xtc_atoms) {
-  std::vector<char> b;
-  if (!cli::read_file(path, b)) return -1;
-  const unsigned char* u = reinterpret_cast<const unsigned char*>(b.data());
-  if (b.size() >= 4 && ((u[0] << 24) | (u[1] << 16) | (u[2] << 8) | u[3]) == 1995) {
-    int nfr = 0, na = 0;
-    if (mds_xtc_index(u, b.size(), nullptr, 0, &nfr, &na) != MDS_OK) return -3;
-    if (na != natoms) {
-      *xtc_atoms = na;
-      return -4;
-    }
-    std::vector<int64_t> off(nfr + 1);
-    if (mds_xtc_index(u, b.size(), off.data(), nfr + 1, &nfr, &na) != MDS_OK) return -3;
-    x.resize((size_t)nfr * 3 * natoms);
-    if (nfr && mds_xtc_decode(ctx, u, b.size(), off.data(), nfr, natoms, 0, x.data(), nullptr, nullptr,
-                              nullptr) != MDS_OK) {
-      std::cout << "*** ERROR *** " << mds_last_error(ctx) << std::endl;
-      return -3;
-    }
-    n = nfr;
-    return 0;
-  }
-  size_t fr = sizeof(float) * 3 * (size_t)natoms;
-  n = (int)(b.size() / fr);
-  x.resize((size_t)n * 3 * natoms);
-  if (n) std::memcpy(x.data(), b.data(), fr * n);
-  return 0;
-}
+#include "frames.h"
+#include "topology.h"
 
 int main(int argc, char** argv) {
   const char* prog = "knn_rms";
@@ -145,13 +63,14 @@ int main(int argc, char** argv) {
     std::cout << "ERROR: --precision must be fp32, bf16x3 or fp16x3" << std::endl;
     return -1;
   }
-  std::vector<float> mass;
   std::cout << "Reading topology information from " << p.str("topology-file") << " ... ";
-  if (!read_topology(p.str("topology-file"), mass) || mass.empty()) {
+  Topology top;
+  if (!read_topology(p.str("topology-file"), top) || top.mass.empty()) {
     std::cout << std::endl << "*** ERROR *** could not read atoms from " << p.str("topology-file") << std::endl;
     return -1;
   }
   std::cout << "done." << std::endl;
+  const std::vector<float>& mass = top.mass;
   const int natoms = (int)mass.size();
   mds_ctx* ctx = nullptr;
   int rc = mds_create(p.i("device"), 0, &ctx);

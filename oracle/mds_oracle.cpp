@@ -1,8 +1,9 @@
 // mds_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
 //
 // A CPU restatement, in FP64 where the reference's result depends on it, of
-// the MDSCTK 1.2.5 hot path: knn_rms, knn_data, make_sysparse, make_gesparse
-// and the affinity / sparse mat-vec steps of decomp_sparse(_nystrom).
+// the MDSCTK 1.2.5 hot path: knn_rms, knn_data, knn_data_sparse,
+// contact_profile, make_sysparse, make_gesparse and the affinity / sparse
+// mat-vec steps of decomp_sparse(_nystrom).
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
 // load this library, and only as the checker or the timed CPU baseline.
 // The product (libmdsgpu) never links or calls it.
@@ -372,6 +373,73 @@ int orc_knn_data(const double* ref, int nref, const double* fit, int nfit, int d
   };
   if (correlation) return knn_driver(nref, nfit, k, sort, nthreads, co, out_d, out_i);
   return knn_driver(nref, nfit, k, sort, nthreads, eu, out_d, out_i);
+}
+
+// knn_data_sparse (knn_data_sparse.cpp:141-260): k nearest sparse vectors by
+// euclidean_distance_sparse (mdsctk.cpp:362-386), restated operation for
+// operation: the merge walk over the reference vector's entries, fit-only
+// entries before each reference entry, squares and differences in FP64 added
+// in walk order. Vectors are CSR rows (off[n+1] int64, idx int32, val f64);
+// the distance is called as distance(ref row, fit row).
+int orc_knn_data_sparse(const int64_t* ref_off, const int* ref_idx, const double* ref_val, int nref,
+                        const int64_t* fit_off, const int* fit_idx, const double* fit_val, int nfit, int k,
+                        int sort, int nthreads, double* out_d, int* out_i) {
+  auto sp = [&](int i, int j) {
+    const int ref_size = (int)(ref_off[j + 1] - ref_off[j]), fit_size = (int)(fit_off[i + 1] - fit_off[i]);
+    const int* ri = ref_idx + ref_off[j];
+    const double* rd = ref_val + ref_off[j];
+    const int* fi = fit_idx + fit_off[i];
+    const double* fd = fit_val + fit_off[i];
+    double value = 0.0;
+    int f = 0;
+    for (int r = 0; r < ref_size; r++) {
+      while (f < fit_size && fi[f] < ri[r]) {
+        value += fd[f] * fd[f];
+        f++;
+      }
+      if (f < fit_size && ri[r] == fi[f]) {
+        value += (rd[r] - fd[f]) * (rd[r] - fd[f]);
+        f++;
+      } else {
+        value += rd[r] * rd[r];
+      }
+    }
+    for (; f < fit_size; f++) value += fd[f] * fd[f];
+    return std::sqrt(value);
+  };
+  return knn_driver(nref, nfit, k, sort, nthreads, sp, out_d, out_i);
+}
+
+// contact_profile (contact_profile.cpp:200-262): for every frame, atom pairs
+// (g1[i], g2[j]) closer than eps Angstrom, as sparse binary vectors over the
+// grid index i * n2 + j. Distance as the reference forms it: float
+// differences and squares, summed into a double, sqrt, times 10. Coordinates
+// [nframes][natoms][3] in nm. offsets[nframes+1] (int64) and, when idx is not
+// null, the ascending grid indices of every frame's contacts.
+void orc_contact_profile(const float* xyz, int nframes, int natoms, const int* g1, int n1, const int* g2, int n2,
+                         double eps, int64_t* offsets, int* idx) {
+  int64_t pos = 0;
+  for (int f = 0; f < nframes; ++f) {
+    offsets[f] = pos;
+    const float* x = xyz + (int64_t)f * natoms * 3;
+    for (int i = 0; i < n1; ++i)
+      for (int j = 0; j < n2; ++j) {
+        const float* a = x + 3 * (int64_t)g1[i];
+        const float* b = x + 3 * (int64_t)g2[j];
+        double d = 0.0;
+        for (int c = 0; c < 3; ++c) {
+          const float t = a[c] - b[c];
+          const float t2 = t * t;
+          d += (double)t2;
+        }
+        d = std::sqrt(d) * 10.0;
+        if (d < eps) {
+          if (idx) idx[pos] = i * n2 + j;
+          ++pos;
+        }
+      }
+  }
+  offsets[nframes] = pos;
 }
 
 // make_sysparse (make_sysparse.cpp:225-329; compare_edge mdsctk.cpp:567-577;

@@ -57,6 +57,13 @@ def lib():
         L.orc_knn_data.argtypes = [_f64p, c_int, _f64p, c_int, c_int, c_int, c_int, c_int,
                                    c_int, _f64p, _i32p]
         L.orc_knn_data.restype = c_int
+        _i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+        L.orc_knn_data_sparse.argtypes = [_i64p, _i32p, _f64p, c_int, _i64p, _i32p, _f64p, c_int, c_int,
+                                          c_int, c_int, _f64p, _i32p]
+        L.orc_knn_data_sparse.restype = c_int
+        L.orc_contact_profile.argtypes = [_f32p, c_int, c_int, _i32p, c_int, _i32p, c_int, c_dbl, _i64p,
+                                          ctypes.c_void_p]
+        L.orc_contact_profile.restype = None
         L.orc_sysparse.argtypes = [_f64p, _i32p, c_int, c_int, c_int, _i32p, _i32p, _f64p]
         L.orc_sysparse.restype = ctypes.c_int64
         L.orc_gesparse.argtypes = [_f64p, _i32p, c_int, c_int, c_int, c_int, _i32p, _i32p, _f64p]
@@ -151,6 +158,47 @@ def knn_data(ref, fit, k, correlation=False, sort=True, threads=0):
     lib().orc_knn_data(ref.reshape(-1), nref, fit.reshape(-1), nfit, dim, int(k),
                        int(correlation), int(sort), int(threads), d, i)
     return d.reshape(nfit, width), i.reshape(nfit, width)
+
+
+def csr(vectors):
+    """Sparse vectors [(indices, values), ...] -> (off int64[n+1], idx int32, val f64)."""
+    off = np.zeros(len(vectors) + 1, np.int64)
+    for r, (ii, _) in enumerate(vectors):
+        off[r + 1] = off[r] + len(ii)
+    idx = np.concatenate([np.asarray(ii, np.int32) for ii, _ in vectors]) if vectors else np.zeros(0, np.int32)
+    val = np.concatenate([np.asarray(vv, np.float64) for _, vv in vectors]) if vectors else np.zeros(0)
+    return off, np.ascontiguousarray(idx, np.int32), np.ascontiguousarray(val, np.float64)
+
+
+def knn_data_sparse(ref, fit, k, sort=True, threads=0):
+    """knn_data_sparse oracle (bit-exact FP64 restatement). ref/fit: CSR
+    triplets (off, idx, val) as made by csr(); fit None = ref."""
+    ro, ri, rv = ref
+    fo, fi, fv = ref if fit is None else fit
+    nref, nfit = len(ro) - 1, len(fo) - 1
+    kk = min(k, nref - 1)
+    width = kk if sort else nref
+    d = np.zeros(max(1, nfit * width), np.float64)
+    i = np.zeros(max(1, nfit * width), np.int32)
+    c = lambda a, t: np.ascontiguousarray(a, t)
+    lib().orc_knn_data_sparse(c(ro, np.int64), c(ri, np.int32), c(rv, np.float64), nref, c(fo, np.int64),
+                              c(fi, np.int32), c(fv, np.float64), nfit, int(k), int(sort), int(threads), d, i)
+    return d[:nfit * width].reshape(nfit, width), i[:nfit * width].reshape(nfit, width)
+
+
+def contact_profile(xyz, g1, g2, eps=9.0):
+    """contact_profile oracle: xyz [nframes, natoms, 3] float32 nm; g1, g2
+    0-based atom indices. Returns (offsets int64[nframes+1], idx int32)."""
+    xyz = _c(xyz, np.float32)
+    nframes, natoms = xyz.shape[0], xyz.shape[1]
+    g1 = _c(g1, np.int32)
+    g2 = _c(g2, np.int32)
+    off = np.zeros(nframes + 1, np.int64)
+    lib().orc_contact_profile(xyz.reshape(-1), nframes, natoms, g1, len(g1), g2, len(g2), float(eps), off, None)
+    idx = np.zeros(max(1, int(off[-1])), np.int32)
+    lib().orc_contact_profile(xyz.reshape(-1), nframes, natoms, g1, len(g1), g2, len(g2), float(eps), off,
+                              idx.ctypes.data_as(ctypes.c_void_p))
+    return off, idx[:int(off[-1])]
 
 
 def sysparse(dist, idx, k=None):

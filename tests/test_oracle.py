@@ -248,3 +248,33 @@ def test_oracle_xtc_synthetic_paths(oracle):
     groups += [(0, 0, True)] * (60 - sum(g[0] + 1 for g in groups))
     xyz, _, _ = oracle.xtc_read(X.encode_frame(q, prec=1000.0, groups=groups, smallidx=12))
     assert np.array_equal(xyz[0], q.astype(np.int32).astype(np.float32) * np.float32(1.0 / 1000.0))
+
+
+def test_sparse_distance_oracle_matches_dense(oracle):
+    """euclidean_distance_sparse restated: on sorted, repeat-free indices it
+    equals the dense Euclidean distance (to rounding; the orders differ)."""
+    rng = np.random.default_rng(0)
+    vecs = []
+    for _ in range(60):
+        m = rng.integers(0, 25)
+        ii = np.sort(rng.choice(120, m, replace=False))
+        vecs.append((ii, rng.normal(size=m)))
+    dense = np.zeros((60, 120))
+    for r, (ii, vv) in enumerate(vecs):
+        dense[r, ii] = vv
+    d, i = oracle.knn_data_sparse(oracle.csr(vecs), None, 6)
+    full = np.sqrt(((dense[:, None, :] - dense[None, :, :]) ** 2).sum(-1))
+    ref = np.take_along_axis(full, i, axis=1)
+    assert np.allclose(d, ref, rtol=1e-13, atol=1e-13)
+    assert np.allclose(d, np.sort(full, axis=1)[:, 1:7], rtol=1e-13, atol=1e-13)
+
+
+def test_contact_profile_oracle(oracle):
+    rng = np.random.default_rng(1)
+    x = rng.uniform(0, 2.5, size=(5, 40, 3)).astype(np.float32)
+    g1, g2 = np.arange(10), np.arange(20, 40)
+    off, idx = oracle.contact_profile(x, g1, g2, 7.5)
+    for f in range(5):
+        dd = np.sqrt(((x[f, g1][:, None, :] - x[f, g2][None, :, :]) ** 2).sum(-1).astype(np.float64)) * 10.0
+        want = np.flatnonzero((dd < 7.5).reshape(-1))
+        assert np.array_equal(idx[off[f]:off[f + 1]], want)
