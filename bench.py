@@ -57,10 +57,12 @@ def parse():
                    help="Nystrom serving benchmark (50,000 landmarks x 304 atoms, k=50, nev=10)")
     p.add_argument("--serve-seconds", type=float, default=8.0)
     p.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate, requests/s")
-    p.add_argument("--pipeline", choices=["small", "scale", "euclid"],
+    p.add_argument("--pipeline", choices=["small", "scale", "euclid", "sparse"],
                    help="per-stage wall time of a whole pipeline: small = 2,000 x 304 frames (parity vs the oracle), "
                         "scale = 100,000 x 304 (kNN k=64, sysparse, Lanczos nev=20 ncv=60 tol=1e-8), "
-                        "euclid = knn_data 200,000 x 64, k=32")
+                        "euclid = knn_data 200,000 x 64, k=32, "
+                        "sparse = contact_profile of 20,000 x 304 frames (atoms 0-151 vs 152-303, 12 A) "
+                        "-> knn_data_sparse, k=32")
     p.add_argument("--pipeline-cpu", action="store_true", help="also time the CPU oracle's sysparse and eigsh")
     p.add_argument("--precision-report", action="store_true",
                    help="per-pair screen RMSD error vs FP64 and output agreement on sampled rows")
@@ -279,6 +281,31 @@ def run_pipeline(args):
                 t0 = time.perf_counter()
                 O.decomp_sparse(nn, pcol, irow, val, sigma, nev, ncv=ncv or None, tol=tol)
                 st["cpu_decomp_sparse_eigsh"] = time.perf_counter() - t0
+        elif args.pipeline == "sparse":
+            n, na, k, eps = 20_000, 304, 32, 12.0
+            x = synth.trajectory(n, na, seed=SEED + 17, basins=4, drift_sigma=0.05, dwell=500.0)
+            g1 = np.arange(0, na // 2, dtype=np.int32)
+            g2 = np.arange(na // 2, na, dtype=np.int32)
+            out["config"] = {"workload": f"contact_profile {n} x {na} (groups {len(g1)} x {len(g2)}, eps {eps} A) "
+                                         f"-> knn_data_sparse k={k}"}
+            off, idx = timed("contact_profile", lambda: c.contact_profile(x, g1, g2, eps))
+            st["contacts_per_frame"] = float(off[-1]) / n
+            vecs = (off, idx, np.ones(len(idx), np.float64))
+            d, i = timed("knn_data_sparse", lambda: c.knn_data_sparse(vecs, None, k), c)
+            st["pairs_per_s"] = n * n / st["knn_data_sparse"]
+            rows = np.linspace(0, n - 1, 64).astype(int)
+            ooff, oidx = O.contact_profile(x[:200], g1, g2, eps)
+            st["parity_contacts_frames_checked"] = 200
+            st["parity_contacts_identical"] = bool(np.array_equal(ooff, off[:201] - off[0])
+                                                   and np.array_equal(oidx, idx[:off[200]]))
+            fit = (np.concatenate([[0], np.cumsum(off[rows + 1] - off[rows])]).astype(np.int64),
+                   np.concatenate([idx[off[r]:off[r + 1]] for r in rows]).astype(np.int32),
+                   np.ones(int(np.sum(off[rows + 1] - off[rows])), np.float64))
+            t0 = time.perf_counter()
+            od, oi = O.knn_data_sparse(vecs, fit, k)  # each sampled row finds itself at position 0, dropped
+            st["cpu_oracle_knn_data_sparse_64_rows_s"] = time.perf_counter() - t0
+            st["parity_rows_checked"] = len(rows)
+            st["parity_bit_exact_distances"] = bool(np.array_equal(d[rows], od))
         else:
             n, dim, k = 200_000, 64, 32
             x = synth.dihedral_vectors(n, dim, seed=SEED + 13).astype(np.float64)

@@ -137,6 +137,172 @@ static size_t sparse_knn_smem(int k, int mode) {
 }
 
 // ---------------------------------------------------------------------------
+// knn_data_sparse on binary vectors (every value 1.0, indices strictly
+// ascending: what contact_profile writes). The reference's walk then adds
+// 1.0 for every index in one vector only and 0.0 for every shared index, so
+// its FP64 sum is the integer |A| + |B| - 2 |A & B| whatever the order, and
+// sqrt of it is the reference's distance bit for bit. The vectors become
+// bit sets and |A & B| a popcount tile product: 32 fit rows x 64 reference
+// rows per block tile, 2 x 4 pairs per thread, bit-set words staged through
+// shared memory by cp.async; the squared distances are exact integers, so
+// each row's k+1 smallest (value, index) keys are kept directly (reference
+// tiles are visited in index order, so a later tie never displaces an earlier
+// one) and no recheck is needed.
+// ---------------------------------------------------------------------------
+#define BN_TM 32
+#define BN_TN 64
+#define BN_KW 32  // words per K-chunk
+#define BN_WS 36  // words per staged row (bank spread, 16-byte rows)
+
+// CSR rows -> bit sets [n][W] (W words of 32 bits, zero padded)
+__global__ void k_bitset(const int64_t* __restrict__ off, const int* __restrict__ idx, int W,
+                         unsigned* __restrict__ bits) {
+  const int r = blockIdx.x;
+  unsigned* b = bits + (int64_t)r * W;
+  for (int64_t e = off[r] + threadIdx.x; e < off[r + 1]; e += blockDim.x) {
+    const int i = idx[e];
+    atomicOr(b + (i >> 5), 1u << (i & 31));
+  }
+}
+
+__device__ __forceinline__ void cpa16b(void* smem, const void* gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 16 : 0));
+}
+
+__global__ void __launch_bounds__(SP_THREADS)
+k_bin_knn(const unsigned* __restrict__ Bf, const int* __restrict__ cf, int nfit, const unsigned* __restrict__ Br,
+          const int* __restrict__ cr, int nref, int W, int k, double* __restrict__ out_d, int* __restrict__ out_i) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned* sf = reinterpret_cast<unsigned*>(smem_raw);  // [2][BN_TM * BN_WS]
+  unsigned* sr = sf + 2 * BN_TM * BN_WS;                   // [2][BN_TN * BN_WS]
+  int* scr = reinterpret_cast<int*>(sr + 2 * BN_TN * BN_WS);  // [BN_TN] column counts
+  int* scnt = scr + BN_TN;                                   // [BN_TM]
+  float* sthr = reinterpret_cast<float*>(scnt + BN_TM);      // [BN_TM]
+  uint64_t* pool = reinterpret_cast<uint64_t*>(sthr + BN_TM);
+  const int k1 = k + 1;
+  const int P2 = next_pow2(k1 + BN_TN);
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4, lane = tid & 31, warp = tid >> 5;
+  const int row0 = blockIdx.x * BN_TM;
+  int cnt_f[2];
+  for (int p = 0; p < 2; ++p) {
+    const int r = row0 + ty + 16 * p;
+    cnt_f[p] = (r < nfit) ? cf[r] : 0;
+  }
+  if (tid < BN_TM) {
+    scnt[tid] = 0;
+    sthr[tid] = __int_as_float(0x7f800000);
+  }
+  const int nch = W / BN_KW;
+  const int ntiles = (nref + BN_TN - 1) / BN_TN;
+  auto load = [&](int stage, int tile, int kc) {
+    unsigned* df = sf + stage * BN_TM * BN_WS;
+    unsigned* dr = sr + stage * BN_TN * BN_WS;
+    for (int e = tid; e < BN_TM * 8; e += SP_THREADS) {
+      const int v = e >> 3, h = e & 7, r = row0 + v;
+      cpa16b(df + v * BN_WS + 4 * h, Bf + (int64_t)(r < nfit ? r : 0) * W + kc * BN_KW + 4 * h, r < nfit);
+    }
+    for (int e = tid; e < BN_TN * 8; e += SP_THREADS) {
+      const int v = e >> 3, h = e & 7, j = tile * BN_TN + v;
+      cpa16b(dr + v * BN_WS + 4 * h, Br + (int64_t)(j < nref ? j : 0) * W + kc * BN_KW + 4 * h, j < nref);
+    }
+  };
+  for (int tile = 0; tile < ntiles; ++tile) {
+    __syncthreads();
+    if (tid < BN_TN) {
+      const int j = tile * BN_TN + tid;
+      scr[tid] = (j < nref) ? cr[j] : 0;
+    }
+    int acc[2][4];
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = 0;
+    load(0, tile, 0);
+    asm volatile("cp.async.commit_group;\n" ::);
+    for (int kc = 0; kc < nch; ++kc) {
+      if (kc + 1 < nch) {
+        load((kc + 1) & 1, tile, kc + 1);
+        asm volatile("cp.async.commit_group;\n" ::);
+        asm volatile("cp.async.wait_group 1;\n" ::);
+      } else {
+        asm volatile("cp.async.wait_group 0;\n" ::);
+      }
+      __syncthreads();
+      const unsigned* df = sf + (kc & 1) * BN_TM * BN_WS;
+      const unsigned* dr = sr + (kc & 1) * BN_TN * BN_WS;
+#pragma unroll
+      for (int a = 0; a < BN_KW; a += 4) {
+        uint4 fv[2], rv[4];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) fv[p] = *reinterpret_cast<const uint4*>(df + (ty + 16 * p) * BN_WS + a);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) rv[q] = *reinterpret_cast<const uint4*>(dr + (tx + 16 * q) * BN_WS + a);
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            acc[p][q] += __popc(fv[p].x & rv[q].x) + __popc(fv[p].y & rv[q].y) + __popc(fv[p].z & rv[q].z) +
+                         __popc(fv[p].w & rv[q].w);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      const int lr = ty + 16 * p;
+      if (row0 + lr >= nfit) continue;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = tile * BN_TN + tx + 16 * q;
+        if (j >= nref) continue;
+        const float s = (float)(cnt_f[p] + scr[tx + 16 * q] - 2 * acc[p][q]);  // exact below 2^24
+        if (s < sthr[lr]) {
+          const int pos = atomicAdd(&scnt[lr], 1);
+          pool[lr * P2 + pos] = mds_pack_key(s, j);
+        }
+      }
+    }
+    __syncthreads();
+    for (int r = warp; r < BN_TM; r += SP_THREADS / 32) {
+      const int n = scnt[r];
+      if (n <= k1) continue;
+      warp_bitonic_sort(pool + r * P2, n, P2, lane);
+      if (lane == 0) {
+        scnt[r] = k1;
+        sthr[r] = mds_key_value(pool[r * P2 + k1 - 1]);
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int r = warp; r < BN_TM; r += SP_THREADS / 32) {
+    const int row = row0 + r;
+    if (row >= nfit) continue;
+    warp_bitonic_sort(pool + r * P2, scnt[r], P2, lane);
+    for (int x = lane; x < k; x += 32) {
+      const uint64_t key = pool[r * P2 + x + 1];
+      out_d[(int64_t)row * k + x] = sqrt((double)mds_key_value(key));
+      out_i[(int64_t)row * k + x] = mds_key_index(key);
+    }
+  }
+}
+
+static size_t bin_knn_smem(int k) {
+  return sizeof(unsigned) * 2 * (BN_TM + BN_TN) * BN_WS + sizeof(int) * (BN_TN + BN_TM) + sizeof(float) * BN_TM +
+         sizeof(uint64_t) * BN_TM * next_pow2(k + 1 + BN_TN) + 16;
+}
+
+// every value exactly 1.0 and every row's indices strictly ascending and >= 0
+static bool binary_rows(const int64_t* off, const int32_t* idx, const double* val, int n, int* dmax) {
+  for (int r = 0; r < n; ++r)
+    for (int64_t e = off[r]; e < off[r + 1]; ++e) {
+      if (val[e] != 1.0 || idx[e] < 0 || (e > off[r] && idx[e] <= idx[e - 1])) return false;
+      *dmax = std::max(*dmax, idx[e]);
+    }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // contact_profile
 // ---------------------------------------------------------------------------
 // distance(a, b) * 10 < eps exactly as the reference decides it
@@ -281,6 +447,54 @@ extern "C" int mds_knn_data_sparse(mds_ctx* ctx, const int64_t* ref_off, const i
   }
   MDS_TRY(dd.alloc(ctx, sizeof(double) * width * n_fit));
   MDS_TRY(di.alloc(ctx, sizeof(int) * width * n_fit));
+  // binary vectors: bit sets and popcount tiles (exact, no walk per pair)
+  int dmax = -1;
+  const bool binary = !full && binary_rows(ref_off, ref_idx, ref_val, n_ref, &dmax) &&
+                      (same || binary_rows(fit_off, fit_idx, fit_val, n_fit, &dmax)) && dmax < (1 << 24) - 1;
+  const int W = mds_round_up(std::max(dmax + 1, 1), 32 * BN_KW) / 32;
+  if (binary && (size_t)W * 4 * ((size_t)n_ref + (same ? 0 : n_fit)) <= ((size_t)8 << 30)) {
+    DevBuf br(ctx), bf(ctx), cr(ctx), cf(ctx);
+    MDS_TRY(br.alloc(ctx, sizeof(unsigned) * (size_t)W * n_ref));
+    MDS_TRY(cr.alloc(ctx, sizeof(int) * n_ref));
+    MDS_CUDA(ctx, cudaMemsetAsync(br.p, 0, sizeof(unsigned) * (size_t)W * n_ref, s));
+    std::vector<int> hc(std::max(n_ref, n_fit));
+    for (int r = 0; r < n_ref; ++r) hc[r] = (int)(ref_off[r + 1] - ref_off[r]);
+    MDS_CUDA(ctx, cudaMemcpyAsync(cr.p, hc.data(), sizeof(int) * n_ref, cudaMemcpyHostToDevice, s));
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+    k_bitset<<<n_ref, 128, 0, s>>>(dro.as<int64_t>(), dri.as<int>(), W, br.as<unsigned>());
+    const unsigned* pbf = br.as<unsigned>();
+    const int* pcf = cr.as<int>();
+    if (!same) {
+      MDS_TRY(bf.alloc(ctx, sizeof(unsigned) * (size_t)W * n_fit));
+      MDS_TRY(cf.alloc(ctx, sizeof(int) * n_fit));
+      MDS_CUDA(ctx, cudaMemsetAsync(bf.p, 0, sizeof(unsigned) * (size_t)W * n_fit, s));
+      MDS_CUDA(ctx, cudaStreamSynchronize(s));  // hc is reused
+      for (int r = 0; r < n_fit; ++r) hc[r] = (int)(fit_off[r + 1] - fit_off[r]);
+      MDS_CUDA(ctx, cudaMemcpyAsync(cf.p, hc.data(), sizeof(int) * n_fit, cudaMemcpyHostToDevice, s));
+      k_bitset<<<n_fit, 128, 0, s>>>(pfo, pfi, W, bf.as<unsigned>());
+      pbf = bf.as<unsigned>();
+      pcf = cf.as<int>();
+    }
+    MDS_CUDA(ctx, cudaGetLastError());
+    const size_t bsm = bin_knn_smem(k);
+    static bool bin_done = false;
+    static size_t bin_limit = 0;
+    MDS_TRY(mds_allow_dyn_smem(ctx, k_bin_knn, &bin_done, &bin_limit));
+    if (bsm > bin_limit) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k=%d too large", k);
+    ctx->stats.launches = same ? 2 : 3;
+    k_bin_knn<<<(n_fit + BN_TM - 1) / BN_TM, SP_THREADS, bsm, s>>>(pbf, pcf, n_fit, br.as<unsigned>(), cr.as<int>(),
+                                                                    n_ref, W, k, dd.as<double>(), di.as<int>());
+    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    MDS_CUDA(ctx, cudaMemcpyAsync(out_d, dd.p, sizeof(double) * width * n_fit, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaMemcpyAsync(out_i, di.p, sizeof(int) * width * n_fit, cudaMemcpyDeviceToHost, s));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    ctx->stats.screen_ms = ms;
+    ctx->stats.passes = 1;
+    return MDS_OK;
+  }
   const size_t smem = sparse_knn_smem(k, mode);
   static bool attr_done = false;
   static size_t attr_limit = 0;

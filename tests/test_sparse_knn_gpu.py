@@ -83,14 +83,6 @@ def _run(bindir, tmp, name, *args, stdin=None):
     return r.stdout
 
 
-def _write_sparse(tmp, stem, vecs):
-    with open(tmp / f"{stem}.svi", "wb") as fi, open(tmp / f"{stem}.svd", "wb") as fd:
-        for ii, vv in vecs:
-            fi.write(np.int32(len(ii)).tobytes())
-            fi.write(np.asarray(ii, np.int32).tobytes())
-            fd.write(np.asarray(vv, np.float64).tobytes())
-
-
 @pytest.mark.gpu
 def test_sparse_tools(ctx, oracle, tmp_path):
     """contact_profile (.pdb topology, raw frames, .ndx groups chosen on
@@ -114,7 +106,7 @@ def test_sparse_tools(ctx, oracle, tmp_path):
     ooff, oidx = oracle.contact_profile(x, np.arange(0, 12), np.arange(15, 30), 8.0)
     ib = np.fromfile(tmp_path / "reference.svi", np.int32)
     db = np.fromfile(tmp_path / "reference.svd", np.float64)
-    want_i, p = [], 0
+    want_i = []
     for f in range(nf):
         n = ooff[f + 1] - ooff[f]
         want_i.append(np.int32(n))
@@ -127,3 +119,29 @@ def test_sparse_tools(ctx, oracle, tmp_path):
     d = np.fromfile(tmp_path / "distances.dat", np.float64).reshape(nf, 5)
     i = np.fromfile(tmp_path / "indices.dat", np.int32).reshape(nf, 5)
     _check(d, i, od, oi)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fit_rows,k", [(None, 9), (150, 33)])
+def test_knn_data_sparse_binary(ctx, oracle, fit_rows, k):
+    """Binary vectors (values 1.0, ascending unique indices: contact maps) take
+    the bit-set popcount path; distances stay bit-identical to the walk.
+    Repeated vectors make ties at distance 0 and between neighbours."""
+    rng = np.random.default_rng(17 + k)
+    n, dim = 1300, 3000
+
+    def binvec(m):
+        ii = np.sort(rng.choice(dim, m, replace=False)).astype(np.int32)
+        return ii, np.ones(m)
+
+    vecs = [binvec(int(rng.integers(0, 200))) for _ in range(n)]
+    for a in range(0, 60, 3):
+        vecs[a + 1] = vecs[a]
+    vecs[5] = (np.zeros(0, np.int32), np.zeros(0))
+    ref = oracle.csr(vecs)
+    fit = None if fit_rows is None else oracle.csr([binvec(int(rng.integers(1, 200))) for _ in range(fit_rows)])
+    d, i = ctx.knn_data_sparse(ref, fit, k)
+    st = ctx.stats()
+    od, oi = oracle.knn_data_sparse(ref, fit, k)
+    _check(d, i, od, oi)
+    assert st["launches"] == (2 if fit is None else 3)  # bit sets (per set) + popcount tiles
