@@ -84,3 +84,22 @@ def test_knn_rms_tile_skipping_exact(ctx, oracle, precision):
         od, oi = oracle.knn_rms(x, fit, m, 20)
         assert np.max(np.abs(d - od)) <= 1e-4
         assert np.mean(i == oi) > 0.999
+
+
+@pytest.mark.gpu
+def test_knn_rms_pinned_host_frames(ctx):
+    """Page-locked host frames (the chunked upload overlaps the copies with
+    the superposition) give the results of ordinary (pageable) host memory,
+    for a set against itself and for a separate fit set."""
+    import torch
+
+    x = synth.trajectory(3000, 200, seed=5, drift_sigma=0.05)
+    m = np.ones(200, np.float32)
+    d0, i0 = ctx.knn_rms(x, None, m, 20, precision="bf16x3")
+    xp = torch.from_numpy(x).pin_memory()
+    d1, i1 = ctx.knn_rms(xp, None, m, 20, precision="bf16x3")
+    assert np.array_equal(d0, d1) and np.array_equal(i0, i1)
+    f = x[::6].copy()
+    d2, i2 = ctx.knn_rms(xp, torch.from_numpy(f).pin_memory(), m, 20, precision="bf16x3")
+    d3, i3 = ctx.knn_rms(x, f, m, 20, precision="bf16x3")
+    assert np.array_equal(d2, d3) and np.array_equal(i2, i3)
