@@ -702,18 +702,34 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
     }
     __syncthreads();
     const int t = s_total;
-    // streaming merge: keys[0, Kp) holds the best K' so far (sorted), each
-    // segment's list (at most K' keys) is placed after it and the whole
-    // buffer re-sorted; shared memory stays O(K') for any segment count.
+    // streaming merge: keys[0, Kp) holds the best K' so far (ascending), each
+    // segment's list (ascending, at most K' keys, as every screen publishes
+    // it) is placed after it reversed, behind +inf padding, so the buffer is
+    // bitonic and one merge pass (log2 P2 barriers instead of a full sort's
+    // log2 P2 (log2 P2 + 1) / 2) sorts it; shared memory stays O(K').
     const int P2 = next_pow2(2 * Kp);
     for (int x = threadIdx.x; x < P2; x += blockDim.x) keys[x] = MDS_KEY_INF;
     __syncthreads();
     for (int s = 0; s < nseg; ++s) {
       const int ns = min(cand_n[(int64_t)lr * nseg + s], Kp);
       const uint64_t* src = cand + ((int64_t)lr * nseg + s) * segstride;
-      for (int x = threadIdx.x; x < P2 - Kp; x += blockDim.x) keys[Kp + x] = (x < ns) ? src[x] : MDS_KEY_INF;
+      const int tail = P2 - Kp;
+      for (int x = threadIdx.x; x < tail; x += blockDim.x)
+        keys[Kp + x] = (x >= tail - ns) ? src[tail - 1 - x] : MDS_KEY_INF;
       __syncthreads();
-      block_bitonic_sort(keys, P2);
+      for (int j = P2 >> 1; j > 0; j >>= 1) {
+        for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+          const int ixj = i ^ j;
+          if (ixj > i) {
+            const uint64_t a = keys[i], b = keys[ixj];
+            if (a > b) {
+              keys[i] = b;
+              keys[ixj] = a;
+            }
+          }
+        }
+        __syncthreads();
+      }
     }
     total = min(t, Kp);
     tau = (t >= Kp) ? mds_key_value(keys[Kp - 1]) : __int_as_float(0x7f800000);
