@@ -142,15 +142,20 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
 struct TcSkip {
   const float* pivlb = nullptr;
   const float* prad = nullptr;
+  const float* rowlo = nullptr;  // [nrowtiles][ncoltiles] row-tile bounds, or null
 };
 // The pivots of a reference set: the middle frame of every column tile
-// (their deviations, records and split operands) and the tiles' radii.
+// (their deviations, records and split operands) and the tiles' radii; for a
+// set screened against itself also the middle frame of every row tile, after
+// them (nP = nC + row tiles).
 struct TcPivots {
   DevBuf A, R, rad;
   TcOperands tc;
-  int nC = 0;
+  int nC = 0, nP = 0;
 };
-int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv);
+int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv,
+                   bool rowpiv = false);
+int tc_skip_rowlo(mds_ctx* ctx, const TcPivots& pv, const float* lb, int n, float* rowlo);
 int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
                    const TcPivots& pv, float* lb, int* derr = nullptr);
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,

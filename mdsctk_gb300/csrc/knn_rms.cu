@@ -1093,16 +1093,22 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.screen_launches = 1;
   } else {
     // tile skipping by the triangle inequality once there are tiles to skip
+    // (a set screened against itself also gets row-tile pivots)
     TcSkip sk;
     TcPivots pv;
-    DevBuf lb(ctx);
+    DevBuf lb(ctx), rowlo(ctx);
     const bool skipping = !pl.screen_keys && (nref + 79) / 80 >= 4;
     if (skipping) {
-      MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv));
-      MDS_TRY(lb.alloc(ctx, sizeof(float) * (size_t)pv.nC * nfit));
+      MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv, same));
+      MDS_TRY(lb.alloc(ctx, sizeof(float) * (size_t)pv.nP * nfit));
       MDS_TRY(tc_skip_bounds(ctx, pl, same ? tcr : tcf, Rfp, nfit, pv, lb.as<float>()));
       sk.pivlb = lb.as<float>();
       sk.prad = pv.rad.as<float>();
+      if (same) {
+        MDS_TRY(rowlo.alloc(ctx, sizeof(float) * (size_t)(pv.nP - pv.nC) * pv.nC));
+        MDS_TRY(tc_skip_rowlo(ctx, pv, lb.as<float>(), nfit, rowlo.as<float>()));
+        sk.rowlo = rowlo.as<float>();
+      }
     }
     DevBuf rowthr(ctx);
     MDS_TRY(rowthr.alloc(ctx, sizeof(float) * std::max(nfit, 1)));

@@ -54,6 +54,7 @@
 #define TC_B_BYTES (TC_N * TC_KB * 2)
 #define TC_STAGE_BYTES (2 * TC_A_BYTES + 2 * TC_B_BYTES)
 #define TC_TMEM_COLS 512
+#define TC_SLACK 16  // keys beyond K' that trigger a compaction (K' + 16 + 80 <= TC_CAPG)
 
 // ---------------------------------------------------------------------------
 // operand preparation: FP32 deviations [n][3][Ap] -> split hi|lo rows
@@ -189,13 +190,42 @@ __device__ __forceinline__ int tile_order(int i, int t0, int t1, int td) {
   return (Rn > L) ? td + m + j : td - m - j;
 }
 
+// Column segment holding the column tile of row tile rt's middle frame.
+__device__ __forceinline__ int diag_seg(int rt, int nseg, int nct) {
+  const int dt = min((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, nct - 1);
+  int s = 0;
+  while (s + 1 < nseg && (int)((int64_t)nct * (s + 1) / nseg) <= dt) ++s;
+  return s;
+}
+
+// Work item -> (row tile, column segment). A set screened against itself
+// (diag) first hands out, row tile by row tile, the segment holding the row
+// tile's own frames, and only then the other segments: by the time those
+// start, the near tiles have set the shared row thresholds they skip by.
+__device__ __forceinline__ void item_split(int item, int nrt, int nseg, int nct, int diag, int& rt, int& seg) {
+  if (!diag || nseg == 1) {
+    rt = item / nseg;
+    seg = item % nseg;
+    return;
+  }
+  if (item < nrt) {
+    rt = item;
+    seg = diag_seg(rt, nseg, nct);
+    return;
+  }
+  const int k = item - nrt;
+  rt = k / (nseg - 1);
+  const int s = k % (nseg - 1), sd = diag_seg(rt, nseg, nct);
+  seg = s < sd ? s : s + 1;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
             int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
-            const float* __restrict__ pivlb, const float* __restrict__ prad, float* __restrict__ dense,
-            float* __restrict__ rowthr, uint64_t* __restrict__ candbuf, int* __restrict__ cand_n,
-            int* __restrict__ err) {
+            const float* __restrict__ pivlb, const float* __restrict__ prad, const float* __restrict__ rowlo,
+            float* __restrict__ dense, float* __restrict__ rowthr, uint64_t* __restrict__ candbuf,
+            int* __restrict__ cand_n, int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
   // Work items (row tile, column segment) are claimed dynamically by each
   // CTA's producer, which also decides which column tiles of the item to
@@ -209,6 +239,10 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   // of its list, which only decreases), no pair of the tile can enter the
   // lists, and every such pair's true RMSD^2 exceeds the final threshold the
   // recheck verifies against -- the tile is not computed.
+  // With row-tile pivots (rowlo != null; a set screened against itself):
+  // row tile R has a pivot p_R with RMSD(i, p_R) <= r_R for its frames i, so
+  // RMSD(i, j) >= RMSD(j, p_R) - r_R >= rowlo[R][T] = min over j in T of the
+  // lower bound of RMSD(j, p_R), minus r_R. L is the larger of the two.
   //
   // Row thresholds across segments (rowthr != null): each compaction lowers
   // rowthr[row] to its segment's K'-th bound (atomicMin). Every segment then
@@ -292,7 +326,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         ok = push(-1, -1);
         break;
       }
-      const int rt = item / nseg, seg = item % nseg;
+      int rt, seg;
+      item_split(item, nitems / nseg, nseg, ncoltiles, diag, rt, seg);
       const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
       const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
       uint32_t skipbits = 0;  // bit b: tile ti0 + b of the current batch of 8 is skipped
@@ -302,30 +337,37 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
           // skip test of the next 8 tiles at once (4 lanes per tile, 10 rows
           // per lane: one round of loads instead of one per tile), against
           // the rows' thresholds now, which only tighten later
+          // Before the epilogue has loaded this item's list thresholds
+          // (S->thr still holds the previous item's rows), the shared row
+          // thresholds alone are used: each is itself a valid threshold.
           skipbits = 0;
           int live = (lane == 0) ? (*(volatile int*)&S->thr_item == item) : 0;
           live = __shfl_sync(0xffffffffu, live, 0);
-          if (live) {
+          if (live || rowthr) {
             __threadfence_block();
             const int tj = ti + (lane >> 2), r0 = (lane & 3) * 10;
             bool can = tj < t1 - t0;
             if (can) {
               const int tb = tile_order(tj, t0, t1, td);
               const float rad = __ldg(prad + tb);
+              const float Lrow = rowlo ? __ldg(rowlo + (int64_t)rt * ncoltiles + tb) : 0.0f;
 #pragma unroll
               for (int x = 0; x < 10; ++x) {
                 const int gi = rt * TC_FR_M + r0 + x;
                 if (gi < nfit) {
-                  float thr = *(volatile float*)&S->thr[r0 + x];
+                  float thr = live ? *(volatile float*)&S->thr[r0 + x] : INFINITY;
                   if (rowthr) thr = fminf(thr, __ldcg(rowthr + gi));
-                  const float L = __ldg(pivlb + (int64_t)tb * nfit + gi) - rad;
+                  const float L = fmaxf(__ldg(pivlb + (int64_t)tb * nfit + gi) - rad, Lrow);
                   if (!(L > 0.0f && L * L > thr)) can = false;
                 }
               }
             }
             const unsigned bal = __ballot_sync(0xffffffffu, can);
-            int still = (lane == 0) ? (*(volatile int*)&S->thr_item == item) : 0;  // not moved on meanwhile
-            still = __shfl_sync(0xffffffffu, still, 0);
+            int still = 1;
+            if (live) {  // the list thresholds read belong to this item: not moved on meanwhile
+              still = (lane == 0) ? (*(volatile int*)&S->thr_item == item) : 0;
+              still = __shfl_sync(0xffffffffu, still, 0);
+            }
             if (still)
               for (int b = 0; b < 8; ++b)
                 if (((bal >> (4 * b)) & 0xFu) == 0xFu) skipbits |= 1u << b;
@@ -442,8 +484,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       if (task.x != cur) {
         // start of an item: row records and this warp's rows' lists
         cur = task.x;
-        rt = cur / nseg;
-        seg = cur % nseg;
+        item_split(cur, nitems / nseg, nseg, ncoltiles, diag, rt, seg);
         grow = rt * TC_FR_M + rloc;
         rowok = (f < 10) && grow < nfit;
         ntile = 0;
@@ -579,8 +620,11 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const int r = q * 10 + fr;
         const int gr = rt * TC_FR_M + r;
         if (gr >= nfit) continue;
+        // Cut back to K' as soon as TC_SLACK keys beyond K' have arrived: the
+        // threshold then follows the K'-th bound closely, which is what the
+        // skip test and the append filter run on.
         int n = S->cnt[r];
-        bool need = (n > Kp) && (n > TC_CAPG - TC_FR_N || S->thr[r] == INF);
+        bool need = n > Kp + TC_SLACK || (n > Kp && S->thr[r] == INF);
         if (!need) continue;
         uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
         n = min(n, TC_CAPG);
@@ -692,7 +736,8 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
   k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
-                                                       skip ? skip->prad : nullptr, dense, rowthr, cand, cand_n, e);
+                                                       skip ? skip->prad : nullptr, skip ? skip->rowlo : nullptr,
+                                                       dense, rowthr, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
   int herr = 0;
@@ -746,39 +791,130 @@ __global__ void k_tile_radius(const float* __restrict__ A, int Nr, int Ap, const
   }
 }
 
+// Both radii of a set screened against itself, in one pass over its frames:
+// block R takes row tile R (TC_FR_M frames), which lies in column tile
+// T = R / 2. prad[nC + R] bounds RMSD(i, row pivot R) over the row tile, and
+// prad[T] (zeroed beforehand; non-negative floats order as their bits) the
+// column tile's radius around its pivot, both rounded up as above.
+__global__ void k_tile_radius_rc(const float* __restrict__ A, int N, int Ap, const int* __restrict__ idx, int nC,
+                                 float* __restrict__ prad) {
+  static_assert(TC_FR_N == 2 * TC_FR_M, "a column tile is two row tiles");
+  __shared__ float wmax[2][8];
+  const int R = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int T = R / 2;
+  const float4* pc = reinterpret_cast<const float4*>(A + (int64_t)idx[T] * 3 * Ap);
+  const float4* pr = reinterpret_cast<const float4*>(A + (int64_t)idx[nC + R] * 3 * Ap);
+  float bc = 0.0f, br = 0.0f;
+  for (int g = warp; g < TC_FR_M; g += blockDim.x >> 5) {
+    const int j = R * TC_FR_M + g;
+    if (j >= N) break;
+    const float4* aj = reinterpret_cast<const float4*>(A + (int64_t)j * 3 * Ap);
+    float ac = 0.0f, ar = 0.0f;
+    for (int q = lane; q < 3 * Ap / 4; q += 32) {
+      const float4 u = __ldg(aj + q), v = __ldg(pc + q), w = __ldg(pr + q);
+      float d0 = u.x - v.x, d1 = u.y - v.y, d2 = u.z - v.z, d3 = u.w - v.w;
+      ac = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, ac))));
+      d0 = u.x - w.x, d1 = u.y - w.y, d2 = u.z - w.z, d3 = u.w - w.w;
+      ar = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, ar))));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      ac += __shfl_xor_sync(0xffffffffu, ac, o);
+      ar += __shfl_xor_sync(0xffffffffu, ar, o);
+    }
+    bc = fmaxf(bc, ac);
+    br = fmaxf(br, ar);
+  }
+  if (lane == 0) {
+    wmax[0][warp] = bc;
+    wmax[1][warp] = br;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float mc = 0.0f, mr = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      mc = fmaxf(mc, wmax[0][w]);
+      mr = fmaxf(mr, wmax[1][w]);
+    }
+    prad[nC + R] = sqrtf(mr) * (1.0f + 1e-5f) + 1e-7f;
+    atomicMax(reinterpret_cast<int*>(prad + T), __float_as_int(sqrtf(mc) * (1.0f + 1e-5f) + 1e-7f));
+  }
+}
+
+// rowlo[R][T] = min over the frames j of column tile T of lb(j, row pivot R)
+// (row nC + R of the dense pass) minus the row tile's radius: one warp per
+// (R, T) pair.
+__global__ void k_row_lo(const float* __restrict__ lb, int N, int nC, int nR, const float* __restrict__ prad,
+                         float* __restrict__ rowlo) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= nR * nC) return;
+  const int R = w / nC, T = w % nC;
+  const float* row = lb + (int64_t)(nC + R) * N;
+  float m = INFINITY;
+  for (int j = T * TC_FR_N + lane; j < min(N, (T + 1) * TC_FR_N); j += 32) m = fminf(m, __ldg(row + j));
+  for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) rowlo[w] = m - __ldg(prad + nC + R);
+}
+
 // Pivot of every column tile of the reference set (its middle frame), the
 // pivots' operands and records, and the tiles' radii: once per reference set.
-int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv) {
+// With rowpiv (a set screened against itself) every row tile of TC_FR_M
+// frames also gets a pivot (its middle frame) and a radius, after the column
+// pivots: pv.nP = nC + number of row tiles.
+int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv, bool rowpiv) {
   const int Nr = pl.nref, Ap = pl.Ap;
   const int nC = (Nr + TC_FR_N - 1) / TC_FR_N;
+  const int nR = rowpiv ? (Nr + TC_FR_M - 1) / TC_FR_M : 0;
+  const int nP = nC + nR;
   cudaStream_t s = ctx->stream;
-  std::vector<int> piv(nC);
+  std::vector<int> piv(nP);
   for (int T = 0; T < nC; ++T) piv[T] = std::min(T * TC_FR_N + TC_FR_N / 2, Nr - 1);
+  for (int R = 0; R < nR; ++R) piv[nC + R] = R * TC_FR_M + std::min(TC_FR_M, Nr - R * TC_FR_M) / 2;
   DevBuf dpiv(ctx);
-  MDS_TRY(dpiv.alloc(ctx, sizeof(int) * nC));
-  MDS_TRY(pv.A.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nC));
-  MDS_TRY(pv.R.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nC));
-  MDS_TRY(pv.rad.alloc(ctx, sizeof(float) * nC));
-  MDS_CUDA(ctx, cudaMemcpyAsync(dpiv.p, piv.data(), sizeof(int) * nC, cudaMemcpyHostToDevice, s));
+  MDS_TRY(dpiv.alloc(ctx, sizeof(int) * nP));
+  MDS_TRY(pv.A.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nP));
+  MDS_TRY(pv.R.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nP));
+  MDS_TRY(pv.rad.alloc(ctx, sizeof(float) * nP));
+  MDS_CUDA(ctx, cudaMemcpyAsync(dpiv.p, piv.data(), sizeof(int) * nP, cudaMemcpyHostToDevice, s));
   ctx->stats.launches += 2;
-  k_gather_frames<<<nC, 128, 0, s>>>(Ar, Rr, dpiv.as<int>(), nC, Ap, pv.A.as<float>(), pv.R.as<float>());
-  k_tile_radius<<<nC, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), pv.rad.as<float>());
+  k_gather_frames<<<nP, 128, 0, s>>>(Ar, Rr, dpiv.as<int>(), nP, Ap, pv.A.as<float>(), pv.R.as<float>());
+  if (rowpiv) {
+    MDS_CUDA(ctx, cudaMemsetAsync(pv.rad.p, 0, sizeof(float) * nC, s));
+    k_tile_radius_rc<<<nR, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), nC, pv.rad.as<float>());
+  } else {
+    k_tile_radius<<<nC, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), pv.rad.as<float>());
+  }
   MDS_CUDA(ctx, cudaGetLastError());
   pv.nC = nC;
+  pv.nP = nP;
   KnnRmsPlan pp = pl;
-  pp.nref = nC;
-  MDS_TRY(tc_prepare(ctx, pp, pv.A.as<float>(), nC, pv.tc, 1));
+  pp.nref = nP;
+  MDS_TRY(tc_prepare(ctx, pp, pv.A.as<float>(), nP, pv.tc, 1));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));  // dpiv is released on return
   return MDS_OK;
 }
 
 // Lower bounds of RMSD from every fit frame to every pivot (the screen in
-// dense mode over the pivots) into lb [nC][nfit]. With derr (2 ints) the call
+// dense mode over the pivots) into lb [nP][nfit]. With derr (2 ints) the call
 // does not synchronise and can be captured in a CUDA graph.
 int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
                    const TcPivots& pv, float* lb, int* derr) {
   KnnRmsPlan pp = pl;
-  pp.nref = pv.nC;
-  return launch_screen_tc(ctx, pp, fit, pv.tc, recf, pv.R.as<float>(), nfit, 32, 1, nullptr, nullptr, derr,
+  pp.nref = pv.nP;
+  // column segments (no lists in dense mode) so that there are >= 4 items per SM
+  const int nrt = (nfit + TC_FR_M - 1) / TC_FR_M, nct = (pv.nP + TC_FR_N - 1) / TC_FR_N;
+  const int nseg = std::max(1, std::min(nct, (4 * ctx->num_sms + nrt - 1) / nrt));
+  return launch_screen_tc(ctx, pp, fit, pv.tc, recf, pv.R.as<float>(), nfit, 32, nseg, nullptr, nullptr, derr,
                           nullptr, lb);
+}
+
+// The row-tile bounds of a set screened against itself (pivots with rowpiv,
+// lb from tc_skip_bounds): rowlo [nR][nC].
+int tc_skip_rowlo(mds_ctx* ctx, const TcPivots& pv, const float* lb, int n, float* rowlo) {
+  const int nR = pv.nP - pv.nC;
+  if (nR <= 0) return mds_fail(ctx, MDS_ERR_INTERNAL, "row-tile pivots were not built");
+  const int warps = nR * pv.nC;
+  ctx->stats.launches++;
+  k_row_lo<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(lb, n, pv.nC, nR, pv.rad.as<float>(), rowlo);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
 }
