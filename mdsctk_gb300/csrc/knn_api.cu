@@ -104,7 +104,10 @@ static int knn_rms_impl(mds_ctx* ctx, const float* ref_xyz, int n_ref, const flo
   pl.full = full ? 1 : 0;
   pl.prec = prec;
   // K' = 2(k+1) (at least k+33): the recheck stops early once the k+1 best
-  // are settled, so a wide K' mainly makes the guard hold on the first pass.
+  // are settled, so a wide K' mainly makes the guard hold on the first pass
+  // where neighbours crowd within the guard of one another. The tensor-core
+  // screen's thresholds also follow the (k+1)-th bound, so a wide K' does not
+  // loosen its tile skipping.
   const int kpmax = (prec == MDS_PREC_FP32) ? 448 : 352;
   pl.kprime = std::min(mds_round_up(std::max(k + 1 + 32, 2 * (k + 1)), 32), kpmax);
   if (!full && pl.kprime < k + 1 + 16)

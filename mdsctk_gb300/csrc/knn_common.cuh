@@ -117,7 +117,7 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
 int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
                    const float* Ur, int nrows, const int* rowlist, int mode, const uint64_t* cand,
                    const int* cand_n, int nseg, int segstride, int Kp, int k, double* out_d, int* out_i,
-                   int* flagged, int* nflag);
+                   int* flagged, int* nflag, const float* rowthr = nullptr);
 int choose_nseg_fp32(int nfit, int num_sms, int nref);
 
 // tensor-core screen (knn_rms_tc.cu)
@@ -161,4 +161,6 @@ int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, co
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
                      int* cand_n, int* derr = nullptr, const TcSkip* skip = nullptr,
-                     float* dense = nullptr, float* rowthr = nullptr);
+                     float* dense = nullptr, float* rowthr = nullptr, const float* nmax = nullptr);
+// *out = the largest |a|^2 over the records rec[n] (a device float).
+int tc_rec_nmax(mds_ctx* ctx, const float* rec, int n, float* out);

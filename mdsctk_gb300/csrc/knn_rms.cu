@@ -634,7 +634,8 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
           const float* __restrict__ Ur, int nrows,
           const int* __restrict__ rowlist, int Nr, int Ap, int natoms, int nofit, int mode,
           const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int segstride, int Kp, int k,
-          double* __restrict__ out_d, int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag) {
+          double* __restrict__ out_d, int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag,
+          const float* __restrict__ rowthr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* sa = reinterpret_cast<float*>(smem_raw);                 // [3*Ap] a_i
   float* sd = sa + 3 * Ap;                                        // [CHUNK]
@@ -733,6 +734,10 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
     }
     total = min(t, Kp);
     tau = (t >= Kp) ? mds_key_value(keys[Kp - 1]) : __int_as_float(0x7f800000);
+    // The screen's final shared threshold of the row: every pair it left out
+    // has a bound at or above it (when it came from the (k+1)-th bound, the
+    // lists may hold fewer than K' keys).
+    if (rowthr) tau = fminf(tau, __ldcg(rowthr + grow));
   } else {
     total = Nr;
     tau = __int_as_float(0x7f800000);
@@ -745,8 +750,9 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
   for (int x = threadIdx.x; x < TP2; x += blockDim.x) top[x] = MDS_KEY_INF;
   __syncthreads();
   // Candidates come in ascending order of their lower bound; once the (k+1)-th
-  // exact RMSD^2 is below the next candidate's bound, no later candidate (nor
-  // any excluded pair, whose bound is at least tau) can enter the k+1 best.
+  // exact RMSD^2 is below the next candidate's bound and not above tau, no
+  // later candidate (nor any excluded pair, whose bound is at least tau) can
+  // enter the k+1 best.
   __shared__ int s_stop;
   bool stopped = false;
   int base = 0;
@@ -768,7 +774,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
       if (threadIdx.x == 0) {
         double dk = (double)mds_key_value(top[k1 - 1]);
         double next = (double)mds_key_value(keys[base]);
-        s_stop = (dk * dk * (1.0 + 1e-6) < next) ? 1 : 0;
+        s_stop = (dk * dk * (1.0 + 1e-6) < next && dk * dk * (1.0 + 1e-6) <= (double)tau) ? 1 : 0;
       }
       __syncthreads();
       if (s_stop) {
@@ -883,7 +889,7 @@ int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofi
 int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
                    const float* Ur, int nrows, const int* rowlist, int mode,
                    const uint64_t* cand, const int* cand_n, int nseg, int segstride, int Kp, int k,
-                   double* out_d, int* out_i, int* flagged, int* nflag) {
+                   double* out_d, int* out_i, int* flagged, int* nflag, const float* rowthr) {
   size_t smem = recheck_smem(pl.Ap, Kp, k, mode);
   if (mode == 0) {
     // the streaming merge works on the best K' plus one segment's K'
@@ -903,7 +909,7 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const fl
   if (nrows > 0)
     k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Af, Ar, mu, Ur, nrows, rowlist, pl.nref, pl.Ap, pl.natoms,
                                                         pl.nofit, mode, cand, cand_n, nseg, segstride, Kp, k,
-                                                        out_d, out_i, flagged, nflag);
+                                                        out_d, out_i, flagged, nflag, rowthr);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
@@ -1087,6 +1093,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)nfit * nseg));
   MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  DevBuf rowthr(ctx), nmax(ctx);  // shared row thresholds of the tensor-core screen, max |a_j|^2
   if (pl.prec == MDS_PREC_FP32) {
     MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), nfit, nullptr, Kp, nseg,
                                cand.as<uint64_t>(), cand_n.as<int>()));
@@ -1110,11 +1117,13 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
         sk.rowlo = rowlo.as<float>();
       }
     }
-    DevBuf rowthr(ctx);
+    // (the candidate-screen diagnostic keeps plain K' lists: no (k+1)-th rule)
     MDS_TRY(rowthr.alloc(ctx, sizeof(float) * std::max(nfit, 1)));
+    MDS_TRY(nmax.alloc(ctx, sizeof(float)));
+    MDS_TRY(tc_rec_nmax(ctx, Rr.as<float>(), nref, nmax.as<float>()));
     MDS_TRY(launch_screen_tc(ctx, pl, same ? tcr : tcf, tcr, Rfp, Rr.as<float>(), nfit, Kp, nseg,
                              cand.as<uint64_t>(), cand_n.as<int>(), nullptr, skipping ? &sk : nullptr, nullptr,
-                             rowthr.as<float>()));
+                             rowthr.as<float>(), pl.screen_keys ? nullptr : nmax.as<float>()));
     st.screen_launches = skipping ? 2 : 1;
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
@@ -1131,7 +1140,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   }
   MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 0, cand.as<uint64_t>(),
                          cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i, flagged.as<int>(),
-                         nflag.as<int>()));
+                         nflag.as<int>(), pl.prec == MDS_PREC_FP32 ? nullptr : rowthr.as<float>()));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0;
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -224,8 +224,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
             int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
             const float* __restrict__ pivlb, const float* __restrict__ prad, const float* __restrict__ rowlo,
-            float* __restrict__ dense, float* __restrict__ rowthr, uint64_t* __restrict__ candbuf,
-            int* __restrict__ cand_n, int* __restrict__ err) {
+            float* __restrict__ dense, float* __restrict__ rowthr, const float* __restrict__ nmax, int k1,
+            uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
   // Work items (row tile, column segment) are claimed dynamically by each
   // CTA's producer, which also decides which column tiles of the item to
@@ -249,6 +249,16 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   // appends only below min(own threshold, rowthr), and the skip test uses it:
   // a segment holding K' keys below rowthr exists, so the recheck's final
   // threshold is at most rowthr and every pair left out lies above it.
+  //
+  // Thresholds from the (k+1)-th bound (nmax != null: the largest |a_j|^2 of
+  // the reference set): a bound b is the screen value minus the guard
+  // g (|a_i|^2 + |a_j|^2), and the screen value is within the guard of the
+  // exact RMSD^2, so the exact value is at most b + 2g (|a_i|^2 + |a_j|^2).
+  // With k+1 keys of a list at or below b_(k+1), the (k+1)-th exact RMSD^2 of
+  // the row is at most b_(k+1) + 2g (|a_i|^2 + nmax) = t': no pair whose
+  // bound is above t' can be among the k+1 best, so a compaction sets the
+  // row threshold to min(K'-th bound, t'). The recheck verifies the (k+1)-th
+  // exact value against the final shared threshold, as against the K'-th.
   //
   // Dense mode (dense != null; the pivot pass): every pair's lower bound of
   // RMSD (sqrt of the screen value) is written to dense[j][i]; no lists.
@@ -628,7 +638,10 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         if (!need) continue;
         uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
         n = min(n, TC_CAPG);
-        const float t = warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
+        float tk1 = INF;
+        float t = warp_select_keep2(src, n, TC_CAPG, 0, Kp, reinterpret_cast<int*>(scratch), lane,
+                                    nmax ? k1 : 0, &tk1);
+        if (nmax) t = fminf(t, tk1 + 2.0f * guard * (S->rowrec[r * MDS_REC + 15] + __ldg(nmax)));
         if (lane == 0) {
           S->cnt[r] = Kp;
           S->thr[r] = t;
@@ -702,7 +715,7 @@ int tc_seg_stride() { return TC_CAPG; }
 
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
-                     int* cand_n, int* derr, const TcSkip* skip, float* dense, float* rowthr) {
+                     int* cand_n, int* derr, const TcSkip* skip, float* dense, float* rowthr, const float* nmax) {
   if (Kp + 2 * TC_FR_N > TC_CAPG)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen supports K' <= %d (k too large)",
                     TC_CAPG - 2 * TC_FR_N);
@@ -737,7 +750,7 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
                                                        skip ? skip->prad : nullptr, skip ? skip->rowlo : nullptr,
-                                                       dense, rowthr, cand, cand_n, e);
+                                                       dense, rowthr, nmax, pl.k + 1, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
   int herr = 0;
@@ -853,6 +866,24 @@ __global__ void k_row_lo(const float* __restrict__ lb, int N, int nC, int nR, co
   for (int j = T * TC_FR_N + lane; j < min(N, (T + 1) * TC_FR_N); j += 32) m = fminf(m, __ldg(row + j));
   for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) rowlo[w] = m - __ldg(prad + nC + R);
+}
+
+// *out = max over frames of rec[15] = |a|^2 (out zeroed beforehand;
+// non-negative floats order as their bits).
+__global__ void k_rec_nmax(const float* __restrict__ rec, int n, float* __restrict__ out) {
+  float m = 0.0f;
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x)
+    m = fmaxf(m, __ldg(rec + (int64_t)f * MDS_REC + 15));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(m));
+}
+
+int tc_rec_nmax(mds_ctx* ctx, const float* rec, int n, float* out) {
+  MDS_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(float), ctx->stream));
+  ctx->stats.launches++;
+  k_rec_nmax<<<std::max(1, std::min((n + 255) / 256, 2 * ctx->num_sms)), 256, 0, ctx->stream>>>(rec, n, out);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
 }
 
 // Pivot of every column tile of the reference set (its middle frame), the

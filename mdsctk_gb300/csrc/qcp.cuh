@@ -19,7 +19,8 @@
 //    small antisymmetric part b of S and the 3x3 block D' of K', so FP32
 //    keeps relative accuracy in nu and D; E0 - 2 lambda never cancels.
 //    Newton from nu = D/2 stays above the root, so the result never exceeds
-//    the exact RMSD^2 (a lower bound, as the top-k guard needs).
+//    the exact RMSD^2 (a lower bound, as the top-k guard needs); pairs below
+//    the threshold are iterated to convergence, so their bounds are tight.
 #pragma once
 
 __device__ __forceinline__ double det3d(double a, double b, double c, double d, double e, double f,
@@ -214,7 +215,24 @@ __device__ __forceinline__ float screen_shifted_f32(const float* G, const float*
     float step = (qd > 0.0f) ? qv / qd : 0.0f;
     nu = fmaxf(nu - fmaxf(step, 0.0f), 0.0f);
   }
-  return fmaxf(D - 2.0f * nu - guard, 0.0f);
+  float res = D - 2.0f * nu - guard;
+  if (res < thr) {
+    // A candidate: far above the root Newton on the quartic removes only about
+    // a quarter of the gap per step, so iterate on until the step is at
+    // rounding level; the bound of a kept pair is then within the guard of
+    // its exact value (the (k+1)-th bound threshold relies on that). From
+    // above, every step keeps nu above the root.
+#pragma unroll 1
+    for (int it = 0; it < 16; ++it) {
+      float qv = (((nu + k3) * nu + k2) * nu + k1) * nu + k0;
+      float qd = ((4.0f * nu + 3.0f * k3) * nu + 2.0f * k2) * nu + k1;
+      float step = (qd > 0.0f) ? qv / qd : 0.0f;
+      if (!(step > 1e-7f * nu)) break;
+      nu = fmaxf(nu - step, 0.0f);
+    }
+    res = D - 2.0f * nu - guard;
+  }
+  return fmaxf(res, 0.0f);
 }
 
 // Exact RMSD^2 (per unit mass) of a frame pair from the shifted key matrix:

@@ -128,6 +128,7 @@ struct mds_server {
   unsigned prec = MDS_PREC_FP32;
   float tm = 0;
   DevBuf dmass, dswn, dmu, dM0, Y, E, A, R, U, dZ, ddinv, dlam;
+  DevBuf nmax;  // largest |a|^2 of the landmarks (tensor-core screen thresholds)
   TcPivots pv;  // landmark pivots for tile skipping (pv.nC = 0: off)
   TcOperands tc;
   std::vector<double> evals;
@@ -188,7 +189,7 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
     }
     MDS_TRY(launch_screen_tc(c, pl, sl.tcq, S->tc, sl.R.as<float>(), S->R.as<float>(), bucket, S->Kp, nseg,
                              sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), sl.derr.as<int>(),
-                             S->pv.nC > 0 ? &sk : nullptr, nullptr, sl.rowthr.as<float>()));
+                             S->pv.nC > 0 ? &sk : nullptr, nullptr, sl.rowthr.as<float>(), S->nmax.as<float>()));
   } else {
     nseg = std::min(choose_nseg_fp32(bucket, c->num_sms, S->n), S->nseg_max);
     MDS_CUDA(c, cudaMemsetAsync(sl.derr.p, 0, sizeof(int), c->stream));
@@ -198,7 +199,8 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
   const int segstride = (S->prec == MDS_PREC_FP32) ? S->Kp : tc_seg_stride();
   MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), S->U.as<float>(), bucket,
                          nullptr, 0, sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), nseg, segstride, S->Kp, S->k,
-                         sl.out_d.as<double>(), sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>()));
+                         sl.out_d.as<double>(), sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>(),
+                         S->prec == MDS_PREC_FP32 ? nullptr : sl.rowthr.as<float>()));
   c->stats.launches++;
   k_serve_ext<<<(bucket + 127) / 128, 128, 0, c->stream>>>(sl.out_d.as<double>(), sl.out_i.as<int>(), bucket, S->k,
                                                           S->cfg.sigma, S->ddinv.as<double>(), S->dZ.as<double>(),
@@ -489,6 +491,8 @@ static int build_model(mds_server* S, const float* hxyz, const float* hmass) {
   if (S->prec != MDS_PREC_FP32) {
     MDS_TRY(tc_prepare(c, S->plan(n), S->A.as<float>(), n, S->tc, 1));
     if ((n + 79) / 80 >= 4) MDS_TRY(tc_skip_pivots(c, S->plan(n), S->A.as<float>(), S->R.as<float>(), S->pv));
+    MDS_TRY(S->nmax.alloc(c, sizeof(float)));
+    MDS_TRY(tc_rec_nmax(c, S->R.as<float>(), n, S->nmax.as<float>()));
   }
   MDS_CUDA(c, cudaStreamSynchronize(s));
   return MDS_OK;
@@ -588,7 +592,7 @@ extern "C" int mds_server_destroy(mds_server* S) {
   }
   S->dmass.release(); S->dswn.release(); S->dmu.release(); S->dM0.release(); S->Y.release(); S->E.release();
   S->A.release(); S->R.release(); S->U.release(); S->dZ.release(); S->ddinv.release(); S->dlam.release(); S->tc.A.release();
-  S->tc.B.release();
+  S->tc.B.release(); S->nmax.release();
   S->pv.A.release(); S->pv.R.release(); S->pv.rad.release(); S->pv.tc.A.release(); S->pv.tc.B.release();
   mds_destroy(S->main);
   delete S;

@@ -5,38 +5,15 @@
 #include "knn_common.cuh"
 
 #define TC_CAPG 512  // keys per (row, column segment) list
-// Keep the Kp smallest of the keys src[0, n0) and src[off1, off1 + n1) (at
-// most TC_CAPG slots in all: off1 + n1 <= TC_CAPG) in src[0..Kp), unsorted,
-// and return the largest kept value: a most-significant-digit radix select
-// over the 64-bit keys (8-bit digits, stopping as soon as the digit bucket
-// holding the Kp-th key is kept whole), then a ballot compaction. hist: 256
-// ints of this warp's shared scratch.
-__device__ inline float warp_select_keep2(uint64_t* src, int n0, int off1, int n1, int Kp, int* hist, int lane) {
-  constexpr int PER = TC_CAPG / 32;
-  uint64_t kv[PER];
-#pragma unroll
-  for (int i = 0; i < PER; ++i) {
-    const int x = lane + 32 * i;
-    kv[i] = (x < n0 || (x >= off1 && x < off1 + n1)) ? src[x] : MDS_KEY_INF;
-  }
-  // Leading bytes that every valid key shares (values of one magnitude share
-  // their sign/exponent byte) are skipped: their histogram would put all keys
-  // in one bucket, one shared-memory atomic after another.
-  uint32_t hmin = 0xffffffffu, hmax = 0u;
-#pragma unroll
-  for (int i = 0; i < PER; ++i)
-    if (kv[i] != MDS_KEY_INF) {
-      const uint32_t hv = (uint32_t)(kv[i] >> 32);
-      hmin = min(hmin, hv);
-      hmax = max(hmax, hv);
-    }
-  hmin = __reduce_min_sync(0xffffffffu, hmin);
-  hmax = __reduce_max_sync(0xffffffffu, hmax);
-  const int same_bytes = (hmin <= hmax) ? ((hmin == hmax) ? 4 : __clz(hmin ^ hmax) / 8) : 0;
-  uint64_t mask = same_bytes ? (~0ull << (64 - 8 * same_bytes)) : 0ull;
-  uint64_t prefix = ((uint64_t)hmin << 32) & mask;
-  int need = Kp;
-  for (int pass = 7 - same_bytes; pass >= 0; --pass) {
+// Radix search over the keys held in registers (PER per lane, invalid keys
+// = MDS_KEY_INF): starting from the digits (mask, prefix) that every valid
+// key shares, refine (mask, prefix) byte by byte until the keys whose
+// processed digits are <= prefix's are exactly the `need` smallest (the
+// search stops as soon as the digit bucket holding the need-th key is whole).
+template <int PER>
+__device__ inline void warp_radix_find(const uint64_t (&kv)[PER], int start_pass, uint64_t& mask, uint64_t& prefix,
+                                       int need, int* hist, int lane) {
+  for (int pass = start_pass; pass >= 0; --pass) {
     const int sh = pass * 8;
     for (int b = lane; b < 256; b += 32) hist[b] = 0;
     __syncwarp();
@@ -80,6 +57,53 @@ __device__ inline float warp_select_keep2(uint64_t* src, int n0, int off1, int n
     mask |= (uint64_t)255 << sh;
     if (cnt == need) break;  // the whole bucket is kept
   }
+}
+
+// Keep the Kp smallest of the keys src[0, n0) and src[off1, off1 + n1) (at
+// most TC_CAPG slots in all: off1 + n1 <= TC_CAPG) in src[0..Kp), unsorted,
+// and return the largest kept value: a most-significant-digit radix select
+// over the 64-bit keys (8-bit digits, stopping as soon as the digit bucket
+// holding the Kp-th key is kept whole), then a ballot compaction. hist: 256
+// ints of this warp's shared scratch. With rank2 (1 <= rank2 <= Kp, and at
+// least rank2 keys present), *v2 receives the value of the rank2-th smallest
+// key, found by a second search over the same registers.
+__device__ inline float warp_select_keep2(uint64_t* src, int n0, int off1, int n1, int Kp, int* hist, int lane,
+                                          int rank2 = 0, float* v2 = nullptr) {
+  constexpr int PER = TC_CAPG / 32;
+  uint64_t kv[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int x = lane + 32 * i;
+    kv[i] = (x < n0 || (x >= off1 && x < off1 + n1)) ? src[x] : MDS_KEY_INF;
+  }
+  // Leading bytes that every valid key shares (values of one magnitude share
+  // their sign/exponent byte) are skipped: their histogram would put all keys
+  // in one bucket, one shared-memory atomic after another.
+  uint32_t hmin = 0xffffffffu, hmax = 0u;
+#pragma unroll
+  for (int i = 0; i < PER; ++i)
+    if (kv[i] != MDS_KEY_INF) {
+      const uint32_t hv = (uint32_t)(kv[i] >> 32);
+      hmin = min(hmin, hv);
+      hmax = max(hmax, hv);
+    }
+  hmin = __reduce_min_sync(0xffffffffu, hmin);
+  hmax = __reduce_max_sync(0xffffffffu, hmax);
+  const int same_bytes = (hmin <= hmax) ? ((hmin == hmax) ? 4 : __clz(hmin ^ hmax) / 8) : 0;
+  const uint64_t mask0 = same_bytes ? (~0ull << (64 - 8 * same_bytes)) : 0ull;
+  const uint64_t prefix0 = ((uint64_t)hmin << 32) & mask0;
+  if (rank2 > 0) {
+    uint64_t mask = mask0, prefix = prefix0;
+    warp_radix_find(kv, 7 - same_bytes, mask, prefix, rank2, hist, lane);
+    float vm = 0.0f;
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+      if (kv[i] != MDS_KEY_INF && (kv[i] & mask) <= prefix) vm = fmaxf(vm, mds_key_value(kv[i]));
+    for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+    *v2 = vm;
+  }
+  uint64_t mask = mask0, prefix = prefix0;
+  warp_radix_find(kv, 7 - same_bytes, mask, prefix, Kp, hist, lane);
   // keep every key whose processed digits are <= prefix's
   int base = 0;
   float vmax = 0.0f;
