@@ -143,15 +143,17 @@ struct TcSkip {
   const float* pivlb = nullptr;
   const float* prad = nullptr;
   const float* rowlo = nullptr;  // [nrowtiles][ncoltiles] row-tile bounds, or null
+  int piv2 = 0;                  // pivots are the row tiles' (two per column tile)
 };
-// The pivots of a reference set: the middle frame of every column tile
-// (their deviations, records and split operands) and the tiles' radii; for a
-// set screened against itself also the middle frame of every row tile, after
-// them (nP = nC + row tiles).
+// The pivots of a reference set (their deviations, records and split
+// operands) and the radii: the middle frame of every column tile (nP = nC),
+// or, for a set screened against itself (rowpiv), of every row tile
+// (nP = row tiles, rad = two radii per column tile, rrad = the row tiles').
 struct TcPivots {
-  DevBuf A, R, rad;
+  DevBuf A, R, rad, rrad;
   TcOperands tc;
   int nC = 0, nP = 0;
+  bool rowpiv = false;
 };
 int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv,
                    bool rowpiv = false);

@@ -1100,7 +1100,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.screen_launches = 1;
   } else {
     // tile skipping by the triangle inequality once there are tiles to skip
-    // (a set screened against itself also gets row-tile pivots)
+    // (a set screened against itself uses row-tile pivots)
     TcSkip sk;
     TcPivots pv;
     DevBuf lb(ctx), rowlo(ctx);
@@ -1112,9 +1112,10 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
       sk.pivlb = lb.as<float>();
       sk.prad = pv.rad.as<float>();
       if (same) {
-        MDS_TRY(rowlo.alloc(ctx, sizeof(float) * (size_t)(pv.nP - pv.nC) * pv.nC));
+        MDS_TRY(rowlo.alloc(ctx, sizeof(float) * (size_t)pv.nP * pv.nC));
         MDS_TRY(tc_skip_rowlo(ctx, pv, lb.as<float>(), nfit, rowlo.as<float>()));
         sk.rowlo = rowlo.as<float>();
+        sk.piv2 = 1;
       }
     }
     // (the candidate-screen diagnostic keeps plain K' lists: no (k+1)-th rule)

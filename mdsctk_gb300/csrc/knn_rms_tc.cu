@@ -224,6 +224,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
             int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
             const float* __restrict__ pivlb, const float* __restrict__ prad, const float* __restrict__ rowlo,
+            int piv2,
             float* __restrict__ dense, float* __restrict__ rowthr, const float* __restrict__ nmax, int k1,
             uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
@@ -239,10 +240,13 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   // of its list, which only decreases), no pair of the tile can enter the
   // lists, and every such pair's true RMSD^2 exceeds the final threshold the
   // recheck verifies against -- the tile is not computed.
-  // With row-tile pivots (rowlo != null; a set screened against itself):
-  // row tile R has a pivot p_R with RMSD(i, p_R) <= r_R for its frames i, so
-  // RMSD(i, j) >= RMSD(j, p_R) - r_R >= rowlo[R][T] = min over j in T of the
-  // lower bound of RMSD(j, p_R), minus r_R. L is the larger of the two.
+  // With row-tile pivots (piv2, a set screened against itself): pivot R is
+  // the middle frame of row tile R and pivlb[R][i] bounds RMSD(i, p_R); column
+  // tile T holds row tiles 2T and 2T+1, and prad[2T], prad[2T+1] bound the
+  // distances of its frames to their pivots, so L is the larger of the two
+  // pivots' bounds. Row tile R also has RMSD(i, p_R) <= r_R for its frames i,
+  // so RMSD(i, j) >= RMSD(j, p_R) - r_R >= rowlo[R][T] = min over j in T of
+  // the lower bound of RMSD(j, p_R), minus r_R. L is the largest of these.
   //
   // Row thresholds across segments (rowthr != null): each compaction lowers
   // rowthr[row] to its segment's K'-th bound (atomicMin). Every segment then
@@ -359,7 +363,9 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             bool can = tj < t1 - t0;
             if (can) {
               const int tb = tile_order(tj, t0, t1, td);
-              const float rad = __ldg(prad + tb);
+              const int pa = piv2 ? 2 * tb : tb;
+              const bool pb = piv2 && 2 * tb + 1 < (nfit + TC_FR_M - 1) / TC_FR_M;
+              const float rada = __ldg(prad + pa), radb = pb ? __ldg(prad + pa + 1) : 0.0f;
               const float Lrow = rowlo ? __ldg(rowlo + (int64_t)rt * ncoltiles + tb) : 0.0f;
 #pragma unroll
               for (int x = 0; x < 10; ++x) {
@@ -367,7 +373,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 if (gi < nfit) {
                   float thr = live ? *(volatile float*)&S->thr[r0 + x] : INFINITY;
                   if (rowthr) thr = fminf(thr, __ldcg(rowthr + gi));
-                  const float L = fmaxf(__ldg(pivlb + (int64_t)tb * nfit + gi) - rad, Lrow);
+                  float L = fmaxf(__ldg(pivlb + (int64_t)pa * nfit + gi) - rada, Lrow);
+                  if (pb) L = fmaxf(L, __ldg(pivlb + (int64_t)(pa + 1) * nfit + gi) - radb);
                   if (!(L > 0.0f && L * L > thr)) can = false;
                 }
               }
@@ -750,6 +757,7 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
                                                        skip ? skip->prad : nullptr, skip ? skip->rowlo : nullptr,
+                                                       skip ? skip->piv2 : 0,
                                                        dense, rowthr, nmax, pl.k + 1, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
@@ -804,27 +812,29 @@ __global__ void k_tile_radius(const float* __restrict__ A, int Nr, int Ap, const
   }
 }
 
-// Both radii of a set screened against itself, in one pass over its frames:
-// block R takes row tile R (TC_FR_M frames), which lies in column tile
-// T = R / 2. prad[nC + R] bounds RMSD(i, row pivot R) over the row tile, and
-// prad[T] (zeroed beforehand; non-negative floats order as their bits) the
-// column tile's radius around its pivot, both rounded up as above.
-__global__ void k_tile_radius_rc(const float* __restrict__ A, int N, int Ap, const int* __restrict__ idx, int nC,
-                                 float* __restrict__ prad) {
+// Radii of a set screened against itself with row-tile pivots, in one pass
+// over its frames: block R takes row tile R (TC_FR_M frames), which lies in
+// column tile T = R / 2 with the pivots p_2T and p_2T+1 (idx). rrad[R] bounds
+// RMSD(i, p_R) over the row tile; prad[2T] and prad[2T+1] (zeroed beforehand;
+// non-negative floats order as their bits) bound the distances of the column
+// tile's frames to p_2T and p_2T+1. All rounded up as above.
+__global__ void k_tile_radius_rc(const float* __restrict__ A, int N, int Ap, const int* __restrict__ idx, int nR,
+                                 float* __restrict__ prad, float* __restrict__ rrad) {
   static_assert(TC_FR_N == 2 * TC_FR_M, "a column tile is two row tiles");
   __shared__ float wmax[2][8];
   const int R = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int T = R / 2;
-  const float4* pc = reinterpret_cast<const float4*>(A + (int64_t)idx[T] * 3 * Ap);
-  const float4* pr = reinterpret_cast<const float4*>(A + (int64_t)idx[nC + R] * 3 * Ap);
-  float bc = 0.0f, br = 0.0f;
+  const bool hasb = 2 * T + 1 < nR;
+  const float4* pa = reinterpret_cast<const float4*>(A + (int64_t)idx[2 * T] * 3 * Ap);
+  const float4* pb = reinterpret_cast<const float4*>(A + (int64_t)idx[hasb ? 2 * T + 1 : 2 * T] * 3 * Ap);
+  float ba = 0.0f, bb = 0.0f;
   for (int g = warp; g < TC_FR_M; g += blockDim.x >> 5) {
     const int j = R * TC_FR_M + g;
     if (j >= N) break;
     const float4* aj = reinterpret_cast<const float4*>(A + (int64_t)j * 3 * Ap);
     float ac = 0.0f, ar = 0.0f;
     for (int q = lane; q < 3 * Ap / 4; q += 32) {
-      const float4 u = __ldg(aj + q), v = __ldg(pc + q), w = __ldg(pr + q);
+      const float4 u = __ldg(aj + q), v = __ldg(pa + q), w = __ldg(pb + q);
       float d0 = u.x - v.x, d1 = u.y - v.y, d2 = u.z - v.z, d3 = u.w - v.w;
       ac = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, ac))));
       d0 = u.x - w.x, d1 = u.y - w.y, d2 = u.z - w.z, d3 = u.w - w.w;
@@ -834,38 +844,39 @@ __global__ void k_tile_radius_rc(const float* __restrict__ A, int N, int Ap, con
       ac += __shfl_xor_sync(0xffffffffu, ac, o);
       ar += __shfl_xor_sync(0xffffffffu, ar, o);
     }
-    bc = fmaxf(bc, ac);
-    br = fmaxf(br, ar);
+    ba = fmaxf(ba, ac);
+    bb = fmaxf(bb, ar);
   }
   if (lane == 0) {
-    wmax[0][warp] = bc;
-    wmax[1][warp] = br;
+    wmax[0][warp] = ba;
+    wmax[1][warp] = bb;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    float mc = 0.0f, mr = 0.0f;
+    float ma = 0.0f, mb = 0.0f;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      mc = fmaxf(mc, wmax[0][w]);
-      mr = fmaxf(mr, wmax[1][w]);
+      ma = fmaxf(ma, wmax[0][w]);
+      mb = fmaxf(mb, wmax[1][w]);
     }
-    prad[nC + R] = sqrtf(mr) * (1.0f + 1e-5f) + 1e-7f;
-    atomicMax(reinterpret_cast<int*>(prad + T), __float_as_int(sqrtf(mc) * (1.0f + 1e-5f) + 1e-7f));
+    const float ra = sqrtf(ma) * (1.0f + 1e-5f) + 1e-7f, rb = sqrtf(mb) * (1.0f + 1e-5f) + 1e-7f;
+    rrad[R] = (R == 2 * T) ? ra : rb;
+    atomicMax(reinterpret_cast<int*>(prad + 2 * T), __float_as_int(ra));
+    if (hasb) atomicMax(reinterpret_cast<int*>(prad + 2 * T + 1), __float_as_int(rb));
   }
 }
 
 // rowlo[R][T] = min over the frames j of column tile T of lb(j, row pivot R)
-// (row nC + R of the dense pass) minus the row tile's radius: one warp per
-// (R, T) pair.
-__global__ void k_row_lo(const float* __restrict__ lb, int N, int nC, int nR, const float* __restrict__ prad,
+// (row R of the dense pass) minus the row tile's radius: one warp per (R, T).
+__global__ void k_row_lo(const float* __restrict__ lb, int N, int nC, int nR, const float* __restrict__ rrad,
                          float* __restrict__ rowlo) {
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= nR * nC) return;
   const int R = w / nC, T = w % nC;
-  const float* row = lb + (int64_t)(nC + R) * N;
+  const float* row = lb + (int64_t)R * N;
   float m = INFINITY;
   for (int j = T * TC_FR_N + lane; j < min(N, (T + 1) * TC_FR_N); j += 32) m = fminf(m, __ldg(row + j));
   for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (lane == 0) rowlo[w] = m - __ldg(prad + nC + R);
+  if (lane == 0) rowlo[w] = m - __ldg(rrad + R);
 }
 
 // *out = max over frames of rec[15] = |a|^2 (out zeroed beforehand;
@@ -886,37 +897,42 @@ int tc_rec_nmax(mds_ctx* ctx, const float* rec, int n, float* out) {
   return MDS_OK;
 }
 
-// Pivot of every column tile of the reference set (its middle frame), the
-// pivots' operands and records, and the tiles' radii: once per reference set.
-// With rowpiv (a set screened against itself) every row tile of TC_FR_M
-// frames also gets a pivot (its middle frame) and a radius, after the column
-// pivots: pv.nP = nC + number of row tiles.
+// Pivots of a reference set, their operands and records, and the radii:
+// once per reference set. By default the middle frame of every column tile
+// (nP = nC pivots, prad[T] the tile's radius). With rowpiv (a set screened
+// against itself) the middle frame of every row tile of TC_FR_M frames
+// instead (nP = row tiles): prad[2T], prad[2T+1] bound column tile T's
+// distances to its two row pivots and rrad[R] row tile R's radius.
 int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv, bool rowpiv) {
   const int Nr = pl.nref, Ap = pl.Ap;
   const int nC = (Nr + TC_FR_N - 1) / TC_FR_N;
-  const int nR = rowpiv ? (Nr + TC_FR_M - 1) / TC_FR_M : 0;
-  const int nP = nC + nR;
+  const int nR = (Nr + TC_FR_M - 1) / TC_FR_M;
+  const int nP = rowpiv ? nR : nC;
   cudaStream_t s = ctx->stream;
   std::vector<int> piv(nP);
-  for (int T = 0; T < nC; ++T) piv[T] = std::min(T * TC_FR_N + TC_FR_N / 2, Nr - 1);
-  for (int R = 0; R < nR; ++R) piv[nC + R] = R * TC_FR_M + std::min(TC_FR_M, Nr - R * TC_FR_M) / 2;
+  if (rowpiv)
+    for (int R = 0; R < nR; ++R) piv[R] = R * TC_FR_M + std::min(TC_FR_M, Nr - R * TC_FR_M) / 2;
+  else
+    for (int T = 0; T < nC; ++T) piv[T] = std::min(T * TC_FR_N + TC_FR_N / 2, Nr - 1);
   DevBuf dpiv(ctx);
   MDS_TRY(dpiv.alloc(ctx, sizeof(int) * nP));
   MDS_TRY(pv.A.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nP));
   MDS_TRY(pv.R.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nP));
-  MDS_TRY(pv.rad.alloc(ctx, sizeof(float) * nP));
+  MDS_TRY(pv.rad.alloc(ctx, sizeof(float) * (rowpiv ? 2 * nC : nC)));
+  if (rowpiv) MDS_TRY(pv.rrad.alloc(ctx, sizeof(float) * nR));
   MDS_CUDA(ctx, cudaMemcpyAsync(dpiv.p, piv.data(), sizeof(int) * nP, cudaMemcpyHostToDevice, s));
   ctx->stats.launches += 2;
   k_gather_frames<<<nP, 128, 0, s>>>(Ar, Rr, dpiv.as<int>(), nP, Ap, pv.A.as<float>(), pv.R.as<float>());
   if (rowpiv) {
-    MDS_CUDA(ctx, cudaMemsetAsync(pv.rad.p, 0, sizeof(float) * nC, s));
-    k_tile_radius_rc<<<nR, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), nC, pv.rad.as<float>());
+    MDS_CUDA(ctx, cudaMemsetAsync(pv.rad.p, 0, sizeof(float) * 2 * nC, s));
+    k_tile_radius_rc<<<nR, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), nR, pv.rad.as<float>(), pv.rrad.as<float>());
   } else {
     k_tile_radius<<<nC, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), pv.rad.as<float>());
   }
   MDS_CUDA(ctx, cudaGetLastError());
   pv.nC = nC;
   pv.nP = nP;
+  pv.rowpiv = rowpiv;
   KnnRmsPlan pp = pl;
   pp.nref = nP;
   MDS_TRY(tc_prepare(ctx, pp, pv.A.as<float>(), nP, pv.tc, 1));
@@ -939,13 +955,13 @@ int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, co
 }
 
 // The row-tile bounds of a set screened against itself (pivots with rowpiv,
-// lb from tc_skip_bounds): rowlo [nR][nC].
+// lb [nR][n] from tc_skip_bounds): rowlo [nR][nC].
 int tc_skip_rowlo(mds_ctx* ctx, const TcPivots& pv, const float* lb, int n, float* rowlo) {
-  const int nR = pv.nP - pv.nC;
-  if (nR <= 0) return mds_fail(ctx, MDS_ERR_INTERNAL, "row-tile pivots were not built");
+  if (!pv.rowpiv) return mds_fail(ctx, MDS_ERR_INTERNAL, "row-tile pivots were not built");
+  const int nR = pv.nP;
   const int warps = nR * pv.nC;
   ctx->stats.launches++;
-  k_row_lo<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(lb, n, pv.nC, nR, pv.rad.as<float>(), rowlo);
+  k_row_lo<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(lb, n, pv.nC, nR, pv.rrad.as<float>(), rowlo);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
