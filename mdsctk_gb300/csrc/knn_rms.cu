@@ -713,6 +713,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
     __syncthreads();
     for (int s = 0; s < nseg; ++s) {
       const int ns = min(cand_n[(int64_t)lr * nseg + s], Kp);
+      if (ns == 0) continue;  // (uniform over the block)
       const uint64_t* src = cand + ((int64_t)lr * nseg + s) * segstride;
       const int tail = P2 - Kp;
       for (int x = threadIdx.x; x < tail; x += blockDim.x)
@@ -738,6 +739,16 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
     // has a bound at or above it (when it came from the (k+1)-th bound, the
     // lists may hold fewer than K' keys).
     if (rowthr) tau = fminf(tau, __ldcg(rowthr + grow));
+    // Candidates whose bound is above tau cannot enter the k+1 best once the
+    // (k+1)-th exact value is at most tau, which the guard check requires:
+    // recheck only those at or below it (at least k+1 of them, so that a
+    // failed guard is still seen).
+    int within = 0;
+    for (int b0 = 0; b0 < total; b0 += blockDim.x) {
+      const int x = b0 + threadIdx.x;
+      within += __syncthreads_count(x < total && mds_key_value(keys[x]) <= tau);
+    }
+    total = max(within, min(total, k1));
   } else {
     total = Nr;
     tau = __int_as_float(0x7f800000);
@@ -1085,7 +1096,16 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   int Kp = pl.kprime;
   int ncoltiles = (nref + 63) / 64;
   int nseg = choose_nseg((nfit + 31) / 32, ctx->num_sms, ncoltiles);
-  if (pl.prec != MDS_PREC_FP32) nseg = tc_choose_nseg(ctx, pl, nfit);
+  if (pl.prec != MDS_PREC_FP32) {
+    nseg = tc_choose_nseg(ctx, pl, nfit);
+    // A set screened against itself skips most tiles and its items differ
+    // widely in cost: smaller items (about 12 per SM; the row tile's own
+    // segment is handed out first) keep the CTAs' finishing times together.
+    if (same) {
+      const int nrt = (nfit + 39) / 40, nct = (nref + 79) / 80;
+      nseg = std::min(std::max(nseg, (12 * ctx->num_sms + nrt - 1) / nrt), std::min(8, nct));
+    }
+  }
   if (pl.screen_keys) nseg = 1;
   DevBuf cand(ctx), cand_n(ctx), rows(ctx);
   const int segstride = (pl.prec == MDS_PREC_FP32) ? Kp : tc_seg_stride();

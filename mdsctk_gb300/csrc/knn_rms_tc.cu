@@ -344,23 +344,29 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       item_split(item, nitems / nseg, nseg, ncoltiles, diag, rt, seg);
       const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
       const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
-      uint32_t skipbits = 0;  // bit b: tile ti0 + b of the current batch of 8 is skipped
+      uint32_t skipbits = 0;  // bit b: tile tbase + b of the current batch of 8 is skipped
+      int tbase = 0, test_at = 0;
       for (int ti = 0; ti < t1 - t0 && ok; ++ti) {
         const int tile = tile_order(ti, t0, t1, td);
-        if (pivlb && (ti & 7) == 0) {
+        if (pivlb && ti == test_at) {
           // skip test of the next 8 tiles at once (4 lanes per tile, 10 rows
           // per lane: one round of loads instead of one per tile), against
-          // the rows' thresholds now, which only tighten later
+          // the rows' thresholds now, which only tighten later. While some
+          // row has no threshold yet (an item's first tiles), the test is
+          // repeated at every tile, so tiles are skipped as soon as the first
+          // thresholds arrive.
           // Before the epilogue has loaded this item's list thresholds
           // (S->thr still holds the previous item's rows), the shared row
           // thresholds alone are used: each is itself a valid threshold.
           skipbits = 0;
+          tbase = ti;
+          test_at = ti + 1;
           int live = (lane == 0) ? (*(volatile int*)&S->thr_item == item) : 0;
           live = __shfl_sync(0xffffffffu, live, 0);
           if (live || rowthr) {
             __threadfence_block();
             const int tj = ti + (lane >> 2), r0 = (lane & 3) * 10;
-            bool can = tj < t1 - t0;
+            bool can = tj < t1 - t0, open = false;
             if (can) {
               const int tb = tile_order(tj, t0, t1, td);
               const int pa = piv2 ? 2 * tb : tb;
@@ -373,6 +379,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 if (gi < nfit) {
                   float thr = live ? *(volatile float*)&S->thr[r0 + x] : INFINITY;
                   if (rowthr) thr = fminf(thr, __ldcg(rowthr + gi));
+                  open |= !(thr < 1e30f);
                   float L = fmaxf(__ldg(pivlb + (int64_t)pa * nfit + gi) - rada, Lrow);
                   if (pb) L = fmaxf(L, __ldg(pivlb + (int64_t)(pa + 1) * nfit + gi) - radb);
                   if (!(L > 0.0f && L * L > thr)) can = false;
@@ -380,6 +387,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
               }
             }
             const unsigned bal = __ballot_sync(0xffffffffu, can);
+            if (!__any_sync(0xffffffffu, open)) test_at = ti + 8;
             int still = 1;
             if (live) {  // the list thresholds read belong to this item: not moved on meanwhile
               still = (lane == 0) ? (*(volatile int*)&S->thr_item == item) : 0;
@@ -390,7 +398,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 if (((bal >> (4 * b)) & 0xFu) == 0xFu) skipbits |= 1u << b;
           }
         }
-        if ((skipbits >> (ti & 7)) & 1u) continue;
+        if ((skipbits >> (ti - tbase)) & 1u) continue;
         if (!(ok = push(item, tile))) break;
         if (lane == 0) {
           for (int kb = 0; kb < nkb; ++kb) {
@@ -526,13 +534,33 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             if (gr >= nfit) continue;
             int n = min(S->cnt[r], TC_CAPG);
             uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
+            // keys above the row's threshold now (appended under a looser
+            // one) are dropped: the recheck's threshold is at most this one
+            const float tp = fminf(S->thr[r], rowthr ? __ldcg(rowthr + gr) : INF);
+            if (tp < INF) {
+              int m = 0;
+              for (int x0 = 0; x0 < n; x0 += 32) {
+                const int x = x0 + lane;
+                const uint64_t key = (x < n) ? src[x] : MDS_KEY_INF;
+                const bool keep = x < n && mds_key_value(key) <= tp;
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) src[m + __popc(bal & ((1u << lane) - 1u))] = key;  // at or below the lane's own slot
+                m += __popc(bal);
+                __syncwarp();
+              }
+              n = m;
+            }
             if (n > Kp) {
               warp_select_keep(src, n, Kp, reinterpret_cast<int*>(scratch), lane);
               n = Kp;
             }
-            if (n <= TC_SCR) {
+            int P2 = 32;
+            while (P2 < n) P2 <<= 1;
+            if (n <= 1) {
+            } else if (P2 <= TC_SCR) {
               for (int x = lane; x < n; x += 32) scratch[x] = src[x];
-              warp_bitonic_sort(scratch, n, TC_SCR, lane);
+              __syncwarp();
+              warp_bitonic_sort(scratch, n, P2, lane);
               for (int x = lane; x < n; x += 32) src[x] = scratch[x];
             } else {
               warp_bitonic_sort(src, n, TC_CAPG, lane);  // in place (global; __syncwarp orders it)
@@ -640,17 +668,21 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         // Cut back to K' as soon as TC_SLACK keys beyond K' have arrived: the
         // threshold then follows the K'-th bound closely, which is what the
         // skip test and the append filter run on.
+        // With the (k+1)-th rule, a row without a threshold gets one as soon
+        // as k+1 keys are there (no keys dropped while fewer than K').
         int n = S->cnt[r];
-        bool need = n > Kp + TC_SLACK || (n > Kp && S->thr[r] == INF);
-        if (!need) continue;
+        const bool inf = S->thr[r] == INF;
+        const bool need = n > Kp + TC_SLACK || (n > Kp && inf);
+        const bool early = !need && nmax && inf && n >= k1;
+        if (!need && !early) continue;
         uint64_t* src = candbuf + ((int64_t)gr * nseg + seg) * TC_CAPG;
         n = min(n, TC_CAPG);
         float tk1 = INF;
-        float t = warp_select_keep2(src, n, TC_CAPG, 0, Kp, reinterpret_cast<int*>(scratch), lane,
+        float t = warp_select_keep2(src, n, TC_CAPG, 0, need ? Kp : 0, reinterpret_cast<int*>(scratch), lane,
                                     nmax ? k1 : 0, &tk1);
         if (nmax) t = fminf(t, tk1 + 2.0f * guard * (S->rowrec[r * MDS_REC + 15] + __ldg(nmax)));
         if (lane == 0) {
-          S->cnt[r] = Kp;
+          if (need) S->cnt[r] = Kp;
           S->thr[r] = t;
           if (rowthr) atomicMin(reinterpret_cast<int*>(rowthr + gr), __float_as_int(t));  // t >= 0
         }

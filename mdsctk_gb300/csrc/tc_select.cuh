@@ -66,7 +66,8 @@ __device__ inline void warp_radix_find(const uint64_t (&kv)[PER], int start_pass
 // holding the Kp-th key is kept whole), then a ballot compaction. hist: 256
 // ints of this warp's shared scratch. With rank2 (1 <= rank2 <= Kp, and at
 // least rank2 keys present), *v2 receives the value of the rank2-th smallest
-// key, found by a second search over the same registers.
+// key, found by a second search over the same registers; with Kp = 0 only
+// that value is found (the list is left as it is, the return value is +inf).
 __device__ inline float warp_select_keep2(uint64_t* src, int n0, int off1, int n1, int Kp, int* hist, int lane,
                                           int rank2 = 0, float* v2 = nullptr) {
   constexpr int PER = TC_CAPG / 32;
@@ -101,6 +102,10 @@ __device__ inline float warp_select_keep2(uint64_t* src, int n0, int off1, int n
       if (kv[i] != MDS_KEY_INF && (kv[i] & mask) <= prefix) vm = fmaxf(vm, mds_key_value(kv[i]));
     for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
     *v2 = vm;
+  }
+  if (Kp <= 0) {  // the rank2 value only: nothing kept or moved
+    __syncwarp();
+    return INFINITY;
   }
   uint64_t mask = mask0, prefix = prefix0;
   warp_radix_find(kv, 7 - same_bytes, mask, prefix, Kp, hist, lane);
