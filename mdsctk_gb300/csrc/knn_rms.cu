@@ -1099,11 +1099,11 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   if (pl.prec != MDS_PREC_FP32) {
     nseg = tc_choose_nseg(ctx, pl, nfit);
     // A set screened against itself skips most tiles and its items differ
-    // widely in cost: smaller items (about 12 per SM; the row tile's own
+    // widely in cost: smaller items (about 24 per SM; the row tile's own
     // segment is handed out first) keep the CTAs' finishing times together.
     if (same) {
       const int nrt = (nfit + 39) / 40, nct = (nref + 79) / 80;
-      nseg = std::min(std::max(nseg, (12 * ctx->num_sms + nrt - 1) / nrt), std::min(8, nct));
+      nseg = std::min(std::max(nseg, (24 * ctx->num_sms + nrt - 1) / nrt), std::min(8, nct));
     }
   }
   if (pl.screen_keys) nseg = 1;
