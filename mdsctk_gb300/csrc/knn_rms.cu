@@ -567,26 +567,37 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
     const int c = c0 + grp;
     const bool valid = c < nc;
     const float4* aj4 = reinterpret_cast<const float4*>(Ar + (int64_t)cj[valid ? c : c0] * 3 * Ap);
-    float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // D, Q[9]
+    // Packed FP32 arithmetic (two atoms per instruction, each lane keeping
+    // two partial sums per quantity): d = a_i - a_j as fma(a_j, -1, a_i),
+    // exact in the product, one rounding like the subtraction.
+    float2 w[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) w[i] = make_float2(0.0f, 0.0f);
+    const float2 m1 = make_float2(-1.0f, -1.0f);
     for (int q = gl; q < Ap4; q += 8) {
       const float4 ia = sa4[q], ib = sa4[Ap4 + q], ic = sa4[2 * Ap4 + q];
       const float4 ja = __ldg(aj4 + q), jb = __ldg(aj4 + Ap4 + q), jc = __ldg(aj4 + 2 * Ap4 + q);
-      const float x0[4] = {ia.x, ia.y, ia.z, ia.w}, x1[4] = {ib.x, ib.y, ib.z, ib.w};
-      const float x2[4] = {ic.x, ic.y, ic.z, ic.w};
-      const float d0[4] = {ia.x - ja.x, ia.y - ja.y, ia.z - ja.z, ia.w - ja.w};
-      const float d1[4] = {ib.x - jb.x, ib.y - jb.y, ib.z - jb.z, ib.w - jb.w};
-      const float d2[4] = {ic.x - jc.x, ic.y - jc.y, ic.z - jc.z, ic.w - jc.w};
+      const float2 x0[2] = {make_float2(ia.x, ia.y), make_float2(ia.z, ia.w)};
+      const float2 x1[2] = {make_float2(ib.x, ib.y), make_float2(ib.z, ib.w)};
+      const float2 x2[2] = {make_float2(ic.x, ic.y), make_float2(ic.z, ic.w)};
+      const float2 y0[2] = {make_float2(ja.x, ja.y), make_float2(ja.z, ja.w)};
+      const float2 y1[2] = {make_float2(jb.x, jb.y), make_float2(jb.z, jb.w)};
+      const float2 y2[2] = {make_float2(jc.x, jc.y), make_float2(jc.z, jc.w)};
 #pragma unroll
-      for (int e = 0; e < 4; ++e) v[0] = fmaf(d0[e], d0[e], fmaf(d1[e], d1[e], fmaf(d2[e], d2[e], v[0])));
-      if (!nofit) {
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          v[1] = fmaf(x0[e], d0[e], v[1]); v[2] = fmaf(x0[e], d1[e], v[2]); v[3] = fmaf(x0[e], d2[e], v[3]);
-          v[4] = fmaf(x1[e], d0[e], v[4]); v[5] = fmaf(x1[e], d1[e], v[5]); v[6] = fmaf(x1[e], d2[e], v[6]);
-          v[7] = fmaf(x2[e], d0[e], v[7]); v[8] = fmaf(x2[e], d1[e], v[8]); v[9] = fmaf(x2[e], d2[e], v[9]);
+      for (int e = 0; e < 2; ++e) {
+        const float2 d0 = __ffma2_rn(y0[e], m1, x0[e]), d1 = __ffma2_rn(y1[e], m1, x1[e]);
+        const float2 d2 = __ffma2_rn(y2[e], m1, x2[e]);
+        w[0] = __ffma2_rn(d0, d0, __ffma2_rn(d1, d1, __ffma2_rn(d2, d2, w[0])));
+        if (!nofit) {
+          w[1] = __ffma2_rn(x0[e], d0, w[1]); w[2] = __ffma2_rn(x0[e], d1, w[2]); w[3] = __ffma2_rn(x0[e], d2, w[3]);
+          w[4] = __ffma2_rn(x1[e], d0, w[4]); w[5] = __ffma2_rn(x1[e], d1, w[5]); w[6] = __ffma2_rn(x1[e], d2, w[6]);
+          w[7] = __ffma2_rn(x2[e], d0, w[7]); w[8] = __ffma2_rn(x2[e], d1, w[8]); w[9] = __ffma2_rn(x2[e], d2, w[9]);
         }
       }
     }
+    float v[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) v[i] = w[i].x + w[i].y;
     // sums over the eight lanes of each group (one shuffle serves all four)
 #pragma unroll
     for (int i = 0; i < 10; ++i)

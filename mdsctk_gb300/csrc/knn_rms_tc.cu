@@ -637,7 +637,9 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
           if (rowok && (g0 + c < 8) && j < Nr) {
             const float* cr = S->colrec + gl * MDS_REC;
             if (dense) {
-              const float sv = screen_shifted_f32(G, rrec, cr, nofit != 0, guard * (rrec[15] + cr[15]));
+              // (pivot bounds: no refinement, a loose bound only weakens a skip)
+              const float sv = screen_shifted_f32(G, rrec, cr, nofit != 0, guard * (rrec[15] + cr[15]),
+                                                  __builtin_huge_valf(), false);
               dense[(int64_t)j * nfit + grow] = sqrtf(fmaxf(sv, 0.0f));
             } else {
               const float thr = fminf(*(volatile float*)&S->thr[rloc], S->gthr[rloc]);

@@ -168,7 +168,7 @@ __device__ inline double qcp_rotation_fp64(const double* S, double e0half, doubl
 // the largest eigenvalue of [[0, |b|], [|b|, g]], which dominates K'.
 __device__ __forceinline__ float screen_shifted_f32(const float* G, const float* r, const float* q,
                                                     bool nofit, float guard = 0.0f,
-                                                    float thr = __builtin_huge_valf()) {
+                                                    float thr = __builtin_huge_valf(), bool refine = true) {
   float D = r[15] + q[15] - 2.0f * (G[0] + G[4] + G[8]);
   if (nofit) return fmaxf(D - guard, 0.0f);
   // symmetric part of S
@@ -216,7 +216,7 @@ __device__ __forceinline__ float screen_shifted_f32(const float* G, const float*
     nu = fmaxf(nu - fmaxf(step, 0.0f), 0.0f);
   }
   float res = D - 2.0f * nu - guard;
-  if (res < thr) {
+  if (refine && res < thr) {
     // A candidate: far above the root Newton on the quartic removes only about
     // a quarter of the gap per step, so iterate on until the step is at
     // rounding level; the bound of a kept pair is then within the guard of
