@@ -144,6 +144,7 @@ struct TcSkip {
   const float* prad = nullptr;
   const float* rowlo = nullptr;  // [nrowtiles][ncoltiles] row-tile bounds, or null
   int piv2 = 0;                  // pivots are the row tiles' (two per column tile)
+  const int* far_perm = nullptr; // order of the non-diagonal items, or null
 };
 // The pivots of a reference set (their deviations, records and split
 // operands) and the radii: the middle frame of every column tile (nP = nC),
@@ -158,6 +159,11 @@ struct TcPivots {
 int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv,
                    bool rowpiv = false);
 int tc_skip_rowlo(mds_ctx* ctx, const TcPivots& pv, const float* lb, int n, float* rowlo);
+// Order of the non-diagonal work items of a self screen with nseg segments,
+// estimated heaviest first (work: 3 * 1024 + row tiles * (nseg - 1) ints;
+// perm: row tiles * (nseg - 1) ints).
+int tc_far_order(mds_ctx* ctx, const TcPivots& pv, const float* lb, const float* rowlo, int n, int nseg,
+                 int* work, int* perm);
 int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
                    const TcPivots& pv, float* lb, int* derr = nullptr);
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,

@@ -1134,7 +1134,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     // (a set screened against itself uses row-tile pivots)
     TcSkip sk;
     TcPivots pv;
-    DevBuf lb(ctx), rowlo(ctx);
+    DevBuf lb(ctx), rowlo(ctx), farw(ctx), farp(ctx);
     const bool skipping = !pl.screen_keys && (nref + 79) / 80 >= 4;
     if (skipping) {
       MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv, same));
@@ -1147,6 +1147,14 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
         MDS_TRY(tc_skip_rowlo(ctx, pv, lb.as<float>(), nfit, rowlo.as<float>()));
         sk.rowlo = rowlo.as<float>();
         sk.piv2 = 1;
+        if (nseg > 1) {
+          const size_t nfar = (size_t)pv.nP * (nseg - 1);
+          MDS_TRY(farw.alloc(ctx, sizeof(int) * (3 * 1024 + nfar)));
+          MDS_TRY(farp.alloc(ctx, sizeof(int) * nfar));
+          MDS_TRY(tc_far_order(ctx, pv, lb.as<float>(), rowlo.as<float>(), nfit, nseg, farw.as<int>(),
+                               farp.as<int>()));
+          sk.far_perm = farp.as<int>();
+        }
       }
     }
     // (the candidate-screen diagnostic keeps plain K' lists: no (k+1)-th rule)

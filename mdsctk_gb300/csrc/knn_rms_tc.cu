@@ -202,7 +202,10 @@ __device__ __forceinline__ int diag_seg(int rt, int nseg, int nct) {
 // (diag) first hands out, row tile by row tile, the segment holding the row
 // tile's own frames, and only then the other segments: by the time those
 // start, the near tiles have set the shared row thresholds they skip by.
-__device__ __forceinline__ void item_split(int item, int nrt, int nseg, int nct, int diag, int& rt, int& seg) {
+// The other segments come in the order far_perm gives (when not null: the
+// estimated heaviest first, so that the longest items do not start last).
+__device__ __forceinline__ void item_split(int item, int nrt, int nseg, int nct, int diag, const int* far_perm,
+                                           int& rt, int& seg) {
   if (!diag || nseg == 1) {
     rt = item / nseg;
     seg = item % nseg;
@@ -213,7 +216,7 @@ __device__ __forceinline__ void item_split(int item, int nrt, int nseg, int nct,
     seg = diag_seg(rt, nseg, nct);
     return;
   }
-  const int k = item - nrt;
+  const int k = far_perm ? __ldg(far_perm + (item - nrt)) : item - nrt;
   rt = k / (nseg - 1);
   const int s = k % (nseg - 1), sd = diag_seg(rt, nseg, nct);
   seg = s < sd ? s : s + 1;
@@ -224,7 +227,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
             int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
             const float* __restrict__ pivlb, const float* __restrict__ prad, const float* __restrict__ rowlo,
-            int piv2,
+            int piv2, const int* __restrict__ far_perm,
             float* __restrict__ dense, float* __restrict__ rowthr, const float* __restrict__ nmax, int k1,
             uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
@@ -341,7 +344,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         break;
       }
       int rt, seg;
-      item_split(item, nitems / nseg, nseg, ncoltiles, diag, rt, seg);
+      item_split(item, nitems / nseg, nseg, ncoltiles, diag, far_perm, rt, seg);
       const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
       const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
       uint32_t skipbits = 0;  // bit b: tile tbase + b of the current batch of 8 is skipped
@@ -509,7 +512,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       if (task.x != cur) {
         // start of an item: row records and this warp's rows' lists
         cur = task.x;
-        item_split(cur, nitems / nseg, nseg, ncoltiles, diag, rt, seg);
+        item_split(cur, nitems / nseg, nseg, ncoltiles, diag, far_perm, rt, seg);
         grow = rt * TC_FR_M + rloc;
         rowok = (f < 10) && grow < nfit;
         ntile = 0;
@@ -791,7 +794,7 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
                                                        skip ? skip->prad : nullptr, skip ? skip->rowlo : nullptr,
-                                                       skip ? skip->piv2 : 0,
+                                                       skip ? skip->piv2 : 0, skip ? skip->far_perm : nullptr,
                                                        dense, rowthr, nmax, pl.k + 1, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
@@ -990,6 +993,82 @@ int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, co
 
 // The row-tile bounds of a set screened against itself (pivots with rowpiv,
 // lb [nR][n] from tc_skip_bounds): rowlo [nR][nC].
+// Order of the non-diagonal items (row tile R, other segment s'), heaviest
+// estimate first. Estimate: with t_R = twice the smallest bound from pivot R
+// to another pivot (a scale of R's neighbour distances), the number of
+// column tiles T of the segment with rowlo[R][T] < t_R. est[k] and a
+// histogram first (one warp per row tile), then a descending exclusive scan
+// of the histogram, then a scatter (order within one estimate unspecified:
+// the results do not depend on the order of the items).
+#define TC_EST_BUCKETS 1024
+__global__ void k_far_est(const float* __restrict__ lb, const float* __restrict__ rowlo, int N, int nR, int nC,
+                          int nseg, int* __restrict__ est, int* __restrict__ hist) {
+  const int R = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (R >= nR) return;
+  const int pf = R * TC_FR_M + min(TC_FR_M, N - R * TC_FR_M) / 2;  // pivot frame of R
+  float m = INFINITY;
+  for (int r2 = lane; r2 < nR; r2 += 32)
+    if (r2 != R) m = fminf(m, __ldg(lb + (int64_t)r2 * N + pf));
+  for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const float t = 2.0f * m;
+  const int sd = diag_seg(R, nseg, nC);
+  for (int sp = 0; sp < nseg - 1; ++sp) {
+    const int seg = sp < sd ? sp : sp + 1;
+    const int t0 = (int)((int64_t)nC * seg / nseg), t1 = (int)((int64_t)nC * (seg + 1) / nseg);
+    int c = 0;
+    for (int T = t0 + lane; T < t1; T += 32) c += (__ldg(rowlo + (int64_t)R * nC + T) < t) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    c = min(c, TC_EST_BUCKETS - 1);
+    if (lane == 0) {
+      est[R * (nseg - 1) + sp] = c;
+      atomicAdd(hist + c, 1);
+    }
+  }
+}
+
+__global__ void k_far_scan(const int* __restrict__ hist, int* __restrict__ off) {
+  // one block of TC_EST_BUCKETS threads: off[v] = number of items with est > v
+  __shared__ int sh[TC_EST_BUCKETS];
+  const int v = threadIdx.x;
+  sh[v] = hist[TC_EST_BUCKETS - 1 - v];  // descending order of v
+  __syncthreads();
+  for (int o = 1; o < TC_EST_BUCKETS; o <<= 1) {
+    const int add = (v >= o) ? sh[v - o] : 0;
+    __syncthreads();
+    sh[v] += add;
+    __syncthreads();
+  }
+  const int inc = sh[v];                               // items with est >= TC_EST_BUCKETS-1-v
+  off[TC_EST_BUCKETS - 1 - v] = inc - hist[TC_EST_BUCKETS - 1 - v];
+}
+
+__global__ void k_far_scatter(const int* __restrict__ est, int nfar, const int* __restrict__ off,
+                              int* __restrict__ cnt, int* __restrict__ perm) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nfar) return;
+  const int e = est[k];
+  perm[off[e] + atomicAdd(cnt + e, 1)] = k;
+}
+
+int tc_far_order(mds_ctx* ctx, const TcPivots& pv, const float* lb, const float* rowlo, int n, int nseg,
+                 int* work, int* perm) {
+  // work: 3 * TC_EST_BUCKETS + nR * (nseg - 1) ints
+  if (!pv.rowpiv || nseg < 2) return mds_fail(ctx, MDS_ERR_INTERNAL, "far order needs row pivots and segments");
+  const int nR = pv.nP, nfar = nR * (nseg - 1);
+  int* hist = work;
+  int* off = work + TC_EST_BUCKETS;
+  int* cnt = work + 2 * TC_EST_BUCKETS;
+  int* est = work + 3 * TC_EST_BUCKETS;
+  cudaStream_t s = ctx->stream;
+  MDS_CUDA(ctx, cudaMemsetAsync(work, 0, sizeof(int) * 3 * TC_EST_BUCKETS, s));
+  ctx->stats.launches += 3;
+  k_far_est<<<(nR + 7) / 8, 256, 0, s>>>(lb, rowlo, n, nR, pv.nC, nseg, est, hist);
+  k_far_scan<<<1, TC_EST_BUCKETS, 0, s>>>(hist, off);
+  k_far_scatter<<<(nfar + 255) / 256, 256, 0, s>>>(est, nfar, off, cnt, perm);
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
 int tc_skip_rowlo(mds_ctx* ctx, const TcPivots& pv, const float* lb, int n, float* rowlo) {
   if (!pv.rowpiv) return mds_fail(ctx, MDS_ERR_INTERNAL, "row-tile pivots were not built");
   const int nR = pv.nP;
