@@ -9,9 +9,12 @@ candidate screen, fused top-k, exact recheck and output.
   e2e    pairs/s through the C ABI with pinned host buffers: the host->device
          copy of the frames and the device->host copy of the k-NN lists are
          inside the timed region
-  roofline  the screen kernel: 18*A algorithmic flops per pair (nine A-long
-         contractions) / its CUDA-event time, against the measured dense
-         bf16 tensor peak
+  roofline  the screen kernel: 18*A algorithmic flops (nine A-long
+         contractions) per frame pair it computes -- the column tiles it does
+         not skip (40 x 80 frame pairs each, counted by the kernel) plus the
+         pivot pass -- over the screen stage's CUDA-event time, against the
+         measured dense bf16 tensor peak. About 5% of the N^2 pairs are
+         computed; pairs_equivalent / flops_equivalent give the N^2 figures
   cpu_baseline  the reference's per-pair procedure and OpenMP row loop
          restated in C++ (oracle/mds_oracle.cpp, orc_knn_rms_port) on a bounded
          sample of fit rows against all reference frames, all host cores
@@ -322,14 +325,14 @@ def run_pipeline(args):
 
 
 # DRAM bytes (read + write) of one k_screen_tc screen launch (the second of
-# the call; the first is the 0.08 ms pivot pass) on the default workload
+# the call; the first is the pivot pass, 0.27 + 0.03 GB) on the default workload
 # (20,000 x 1,000 atoms, k = 100, bf16x3), from one ncu capture of
 # dram__bytes_read.sum + dram__bytes_write.sum (a 1-pass metric pair) with
 # the command `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
 # --clock-control none -k regex:<the five kernels below> -s 24 -c 8 --csv python bench.py --steps 2 --warmup 3 --no-cpu` (regex
 # "k_prep_sums|k_prep_out|k_screen_tc|k_recheck|k_tc_split"). Other
 # workloads report null.
-SCREEN_TRAFFIC_BYTES = 14.727e9 + 0.353e9
+SCREEN_TRAFFIC_BYTES = 5.540e9 + 0.077e9
 
 
 def screen_traffic(args):
@@ -517,10 +520,12 @@ def main():
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
     screen_ms, recheck_ms, prep_ms, total_ms, launches, flagged = [], [], [], [], 0, 0
+    screen_pairs = []
     for _ in range(args.steps):
         step_dev()
         st = ctx.stats()
         screen_ms.append(st["screen_ms"])
+        screen_pairs.append(st["screen_pairs"])
         recheck_ms.append(st["recheck_ms"])
         prep_ms.append(st["prep_ms"])
         total_ms.append(st["total_ms"])
@@ -548,7 +553,8 @@ def main():
     e2e = pairs * world / (e2e_ms / 1000.0)
     peaks, pk_kind = measured_peaks()
     scr = sorted(screen_ms)[len(screen_ms) // 2]
-    flops = 18.0 * a * pairs
+    computed = float(sorted(screen_pairs)[len(screen_pairs) // 2]) or pairs
+    flops = 18.0 * a * computed
     achieved = flops / (scr / 1000.0) / 1e12
     peak = float(peaks.get("bf16_tflops", 1900.0))
     # correctness spot check of the last device run: a few rows vs the oracle
@@ -564,6 +570,8 @@ def main():
            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                         "frac": achieved / peak, "traffic": screen_traffic(args),
                         "kernel": "screen", "kernel_ms": scr, "flops_per_launch": flops,
+                        "pairs_computed": computed, "pairs_equivalent": pairs,
+                        "flops_equivalent": 18.0 * a * pairs,
                         "peak_kind": f"{pk_kind} bf16 burst"},
            "stages_ms": {"prep": sorted(prep_ms)[len(prep_ms) // 2], "screen": scr,
                          "recheck": sorted(recheck_ms)[len(recheck_ms) // 2],

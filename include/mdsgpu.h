@@ -64,6 +64,8 @@ typedef struct mds_knn_stats {
   int passes;          /* screen passes (1 + re-screens of flagged rows) */
   int screen_launches; /* kernel launches of the screen */
   int launches;        /* all kernel launches of the call */
+  long long screen_pairs; /* pairs the first-pass screen computed: tiles not
+                             skipped (40 x 80 frames each) plus the pivot pass */
 } mds_knn_stats;
 
 /* Library version string. */

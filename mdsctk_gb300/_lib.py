@@ -42,7 +42,8 @@ class KnnStats(ctypes.Structure):
                 ("recheck_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("pairs", ctypes.c_longlong), ("kprime", ctypes.c_int),
                 ("rows_flagged", ctypes.c_int), ("passes", ctypes.c_int),
-                ("screen_launches", ctypes.c_int), ("launches", ctypes.c_int)]
+                ("screen_launches", ctypes.c_int), ("launches", ctypes.c_int),
+                ("screen_pairs", ctypes.c_longlong)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -169,6 +169,7 @@ int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, co
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
                      int* cand_n, int* derr = nullptr, const TcSkip* skip = nullptr,
-                     float* dense = nullptr, float* rowthr = nullptr, const float* nmax = nullptr);
+                     float* dense = nullptr, float* rowthr = nullptr, const float* nmax = nullptr,
+                     unsigned long long* ntiles = nullptr);
 // *out = the largest |a|^2 over the records rec[n] (a device float).
 int tc_rec_nmax(mds_ctx* ctx, const float* rec, int n, float* out);

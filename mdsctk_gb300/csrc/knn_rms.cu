@@ -1125,6 +1125,9 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
   DevBuf rowthr(ctx), nmax(ctx);  // shared row thresholds of the tensor-core screen, max |a_j|^2
+  DevBuf ntiles(ctx);             // tiles the tensor-core screen computed
+  unsigned long long ht = 0;      // (read back after the recheck)
+  long long dense_pairs = 0;
   if (pl.prec == MDS_PREC_FP32) {
     MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), nfit, nullptr, Kp, nseg,
                                cand.as<uint64_t>(), cand_n.as<int>()));
@@ -1161,10 +1164,14 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(rowthr.alloc(ctx, sizeof(float) * std::max(nfit, 1)));
     MDS_TRY(nmax.alloc(ctx, sizeof(float)));
     MDS_TRY(tc_rec_nmax(ctx, Rr.as<float>(), nref, nmax.as<float>()));
+    MDS_TRY(ntiles.alloc(ctx, sizeof(unsigned long long)));
+    MDS_CUDA(ctx, cudaMemsetAsync(ntiles.p, 0, sizeof(unsigned long long), s));
     MDS_TRY(launch_screen_tc(ctx, pl, same ? tcr : tcf, tcr, Rfp, Rr.as<float>(), nfit, Kp, nseg,
                              cand.as<uint64_t>(), cand_n.as<int>(), nullptr, skipping ? &sk : nullptr, nullptr,
-                             rowthr.as<float>(), pl.screen_keys ? nullptr : nmax.as<float>()));
+                             rowthr.as<float>(), pl.screen_keys ? nullptr : nmax.as<float>(),
+                             ntiles.as<unsigned long long>()));
     st.screen_launches = skipping ? 2 : 1;
+    dense_pairs = skipping ? (long long)pv.nP * nfit : 0;
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
   if (pl.screen_keys) {
@@ -1183,6 +1190,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
                          nflag.as<int>(), pl.prec == MDS_PREC_FP32 ? nullptr : rowthr.as<float>()));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0;
+  if (ntiles.p) MDS_CUDA(ctx, cudaMemcpyAsync(&ht, ntiles.p, sizeof(ht), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));
   float t01 = 0, t12 = 0, t23 = 0;
@@ -1195,6 +1203,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   st.kprime = Kp;
   st.rows_flagged = hflag;
   st.passes = 1;
+  st.screen_pairs = (long long)ht * 40 * 80 + dense_pairs;  // (ht landed with the sync above)
 
   // re-screen flagged rows with more candidates (FP32 screen), then exact rows
   while (hflag > 0) {

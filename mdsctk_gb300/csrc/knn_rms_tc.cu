@@ -229,6 +229,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             const float* __restrict__ pivlb, const float* __restrict__ prad, const float* __restrict__ rowlo,
             int piv2, const int* __restrict__ far_perm,
             float* __restrict__ dense, float* __restrict__ rowthr, const float* __restrict__ nmax, int k1,
+            unsigned long long* __restrict__ ntiles,
             uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
   // Work items (row tile, column segment) are claimed dynamically by each
@@ -471,6 +472,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         atomicMax(err, 2);
         *abortf = 1;
       }
+      if (ntiles && acc) atomicAdd(ntiles, (unsigned long long)acc);  // tiles computed
       // all MMAs of this thread retire before TMEM is freed
       umma_commit(&S->done);
       volatile int dummy = 0;
@@ -759,7 +761,8 @@ int tc_seg_stride() { return TC_CAPG; }
 
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
-                     int* cand_n, int* derr, const TcSkip* skip, float* dense, float* rowthr, const float* nmax) {
+                     int* cand_n, int* derr, const TcSkip* skip, float* dense, float* rowthr, const float* nmax,
+                     unsigned long long* ntiles) {
   if (Kp + 2 * TC_FR_N > TC_CAPG)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen supports K' <= %d (k too large)",
                     TC_CAPG - 2 * TC_FR_N);
@@ -795,7 +798,7 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
                                                        skip ? skip->prad : nullptr, skip ? skip->rowlo : nullptr,
                                                        skip ? skip->piv2 : 0, skip ? skip->far_perm : nullptr,
-                                                       dense, rowthr, nmax, pl.k + 1, cand, cand_n, e);
+                                                       dense, rowthr, nmax, pl.k + 1, ntiles, cand, cand_n, e);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
   int herr = 0;

@@ -80,7 +80,16 @@ def test_knn_rms_tile_skipping_exact(ctx, oracle, precision):
     m = synth.uniform_masses(64)
     for fit in (None, q):
         d, i = ctx.knn_rms(x, fit, m, 20, precision=precision)
-        assert ctx.stats()["screen_launches"] == 2  # pivot pass + screen
+        st = ctx.stats()
+        assert st["screen_launches"] == 2  # pivot pass + screen
+        nf = len(x) if fit is None else len(fit)
+        npiv = (len(x) + 39) // 40 if fit is None else (len(x) + 79) // 80
+        tiles = ((nf + 39) // 40) * ((len(x) + 79) // 80)
+        # pairs computed: the pivot pass plus at least one tile, at most every tile; the
+        # trajectory screened against itself skips some
+        assert npiv * nf + 3200 <= st["screen_pairs"] <= npiv * nf + tiles * 3200
+        if fit is None:
+            assert st["screen_pairs"] < npiv * nf + tiles * 3200
         od, oi = oracle.knn_rms(x, fit, m, 20)
         assert np.max(np.abs(d - od)) <= 1e-4
         assert np.mean(i == oi) > 0.999
