@@ -538,6 +538,7 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
 // ---------------------------------------------------------------------------
 #define RC_THREADS 256
 #define RC_CHUNK 128
+#define RC_GW 8  // lanes per candidate in the recheck's atom loop (32 / RC_GW candidates per warp)
 
 // Exact RMSD (nm) of fit frame (in shared memory) vs reference frame j for a
 // chunk of candidates: covariance per warp, FP64 rotation per thread, then
@@ -555,15 +556,18 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
                               const float* __restrict__ Ar, const float* __restrict__ Ur, int Ap, const int* cj,
                               int nc, bool nofit, float* sd, float* ssum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // A warp takes four candidates at a time, eight lanes each; four atoms per
-  // lane and load (Ap is a multiple of 64; padding atoms are zero in a_i and
-  // a_j, so they add nothing). Per candidate: D = sum |d|^2 and
+  // A warp takes 32 / RC_GW candidates at a time, RC_GW lanes each; four
+  // atoms per lane and load (Ap is a multiple of 64; padding atoms are zero
+  // in a_i and a_j, so they add nothing). Per candidate: D = sum |d|^2 and
   // Q[3r+s] = sum a_i,r d_s with d = a_i - a_j; the row's deviations are the
-  // only shared-memory reads.
-  const int grp = lane >> 3, gl = lane & 7;
+  // only shared-memory reads. A 128-bit shared load costs one wavefront per
+  // quarter warp however many groups read the same address, so more, narrower
+  // groups share each load of the row among more candidates.
+  constexpr int CPW = 32 / RC_GW;
+  const int grp = lane / RC_GW, gl = lane % RC_GW;
   const int Ap4 = Ap >> 2;
   const float4* sa4 = reinterpret_cast<const float4*>(sa);
-  for (int c0 = 4 * warp; c0 < nc; c0 += 4 * nw) {
+  for (int c0 = CPW * warp; c0 < nc; c0 += CPW * nw) {
     const int c = c0 + grp;
     const bool valid = c < nc;
     const float4* aj4 = reinterpret_cast<const float4*>(Ar + (int64_t)cj[valid ? c : c0] * 3 * Ap);
@@ -574,7 +578,7 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
 #pragma unroll
     for (int i = 0; i < 10; ++i) w[i] = make_float2(0.0f, 0.0f);
     const float2 m1 = make_float2(-1.0f, -1.0f);
-    for (int q = gl; q < Ap4; q += 8) {
+    for (int q = gl; q < Ap4; q += RC_GW) {
       const float4 ia = sa4[q], ib = sa4[Ap4 + q], ic = sa4[2 * Ap4 + q];
       const float4 ja = __ldg(aj4 + q), jb = __ldg(aj4 + Ap4 + q), jc = __ldg(aj4 + 2 * Ap4 + q);
       const float2 x0[2] = {make_float2(ia.x, ia.y), make_float2(ia.z, ia.w)};
@@ -598,10 +602,10 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
     float v[10];
 #pragma unroll
     for (int i = 0; i < 10; ++i) v[i] = w[i].x + w[i].y;
-    // sums over the eight lanes of each group (one shuffle serves all four)
+    // sums over the lanes of each group (one shuffle serves every group)
 #pragma unroll
     for (int i = 0; i < 10; ++i)
-      for (int o = 4; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+      for (int o = RC_GW / 2; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
     if (valid && gl == 0) {
       float2* w2 = reinterpret_cast<float2*>(ssum + c * 10);
 #pragma unroll
