@@ -107,9 +107,9 @@ static int knn_rms_impl(mds_ctx* ctx, const float* ref_xyz, int n_ref, const flo
   // are settled, so a wide K' mainly makes the guard hold on the first pass
   // where neighbours crowd within the guard of one another. The tensor-core
   // screen's thresholds also follow the (k+1)-th bound, so a wide K' does not
-  // loosen its tile skipping.
+  // loosen its tile skipping: there K' is 4(k+1) up to 256.
   const int kpmax = (prec == MDS_PREC_FP32) ? 448 : 352;
-  pl.kprime = std::min(mds_round_up(std::max(k + 1 + 32, 2 * (k + 1)), 32), kpmax);
+  pl.kprime = std::min(mds_round_up(tc_kprime_want(k, prec != MDS_PREC_FP32), 32), kpmax);
   if (!full && pl.kprime < k + 1 + 16)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k=%d is too large for the %s screen (use fp32 precision)", k,
                     prec == MDS_PREC_FP32 ? "fp32" : "tensor-core");

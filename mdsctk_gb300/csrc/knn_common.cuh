@@ -120,6 +120,15 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const fl
                    int* flagged, int* nflag, const float* rowthr = nullptr);
 int choose_nseg_fp32(int nfit, int num_sms, int nref);
 
+// Candidates wanted per row before rounding: k+33, 2(k+1), and with the
+// tensor-core screen 4(k+1) up to 256 (its thresholds follow the (k+1)-th
+// bound, so a deeper list only helps the guard check of crowded rows).
+inline int tc_kprime_want(int k, bool tc) {
+  int w = std::max(k + 1 + 32, 2 * (k + 1));
+  if (tc) w = std::max(w, std::min(4 * (k + 1), 256));
+  return w;
+}
+
 // tensor-core screen (knn_rms_tc.cu)
 int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout);
 int tc_seg_stride();

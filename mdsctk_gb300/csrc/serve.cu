@@ -512,10 +512,9 @@ extern "C" int mds_server_create(const mds_server_config* cfg, const float* land
   S->k = std::min(cfg->k, n - 1);
   S->nev = cfg->nev;
   S->prec = cfg->flags & MDS_PREC_MASK;
-  // K' = 4(k+1): off-manifold queries whose neighbours crowd within the guard
-  // of one another need a deep list for the guard check; the tensor-core
-  // screen's thresholds follow the (k+1)-th bound, so depth costs little
-  S->Kp = std::min(mds_round_up(std::max(S->k + 1 + 32, (S->prec == MDS_PREC_FP32 ? 2 : 4) * (S->k + 1)), 32),
+  // as knn_rms: off-manifold queries whose neighbours crowd within the guard
+  // of one another need the deep tensor-core lists for the guard check
+  S->Kp = std::min(mds_round_up(tc_kprime_want(S->k, S->prec != MDS_PREC_FP32), 32),
                    S->prec == MDS_PREC_FP32 ? 448 : 352);
   if (S->Kp < S->k + 1 + 16) return MDS_ERR_UNSUPPORTED;
   S->segstride = (S->prec == MDS_PREC_FP32) ? S->Kp : tc_seg_stride();
