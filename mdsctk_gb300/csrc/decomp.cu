@@ -19,7 +19,8 @@
 //     restarts, start vector from a fixed seed. Full reorthogonalisation
 //     (classical Gram-Schmidt applied twice) by FP64 GEMV kernels; the
 //     projected matrix (ncv x ncv, arrowhead + tridiagonal) is solved on the
-//     host by Householder reduction and the implicit QL algorithm.
+//     host by Householder tridiagonalisation and implicit symmetric QR steps
+//     with Wilkinson shifts (sym_eig.h).
 //  4. Eigenvalues descending, eigenvectors in the same order, residuals
 //     ||A z - lambda z||_2 / |lambda| (decomp_sparse.cpp:242-270).
 //  5. Nystrom: B (general CSC, columns = queries) kernelised with the
@@ -33,6 +34,7 @@
 #include <vector>
 
 #include "mds_common.cuh"
+#include "sym_eig.h"
 
 // ---------------------------------------------------------------------------
 // 1. symmetrise + kernelise
@@ -396,142 +398,6 @@ __global__ void k_gemm_vy(const double* __restrict__ V, int64_t ld, int n, int m
       if (c0 + c < nout) X[i + (int64_t)(c0 + c) * ldx] = acc[c];
 }
 
-// ---------------------------------------------------------------------------
-// small dense symmetric eigensolver (host, FP64): Householder reduction to
-// tridiagonal form followed by the implicit QL algorithm with Wilkinson
-// shifts (the classical tred2 / tql2 procedures, written from the
-// published method).
-// ---------------------------------------------------------------------------
-namespace {
-
-void householder_tridiag(std::vector<double>& a, int n, std::vector<double>& d, std::vector<double>& e) {
-  // a: row-major n x n, on exit holds the orthogonal transform Q (a = Q)
-  d.assign(n, 0.0);
-  e.assign(n, 0.0);
-  for (int i = n - 1; i > 0; --i) {
-    int l = i - 1;
-    double h = 0.0, scale = 0.0;
-    if (l > 0) {
-      for (int k = 0; k <= l; ++k) scale += std::fabs(a[i * n + k]);
-      if (scale == 0.0) {
-        e[i] = a[i * n + l];
-      } else {
-        for (int k = 0; k <= l; ++k) {
-          a[i * n + k] /= scale;
-          h += a[i * n + k] * a[i * n + k];
-        }
-        double f = a[i * n + l];
-        double g = (f >= 0.0) ? -std::sqrt(h) : std::sqrt(h);
-        e[i] = scale * g;
-        h -= f * g;
-        a[i * n + l] = f - g;
-        f = 0.0;
-        for (int j = 0; j <= l; ++j) {
-          a[j * n + i] = a[i * n + j] / h;
-          g = 0.0;
-          for (int k = 0; k <= j; ++k) g += a[j * n + k] * a[i * n + k];
-          for (int k = j + 1; k <= l; ++k) g += a[k * n + j] * a[i * n + k];
-          e[j] = g / h;
-          f += e[j] * a[i * n + j];
-        }
-        double hh = f / (h + h);
-        for (int j = 0; j <= l; ++j) {
-          f = a[i * n + j];
-          e[j] = g = e[j] - hh * f;
-          for (int k = 0; k <= j; ++k) a[j * n + k] -= (f * e[k] + g * a[i * n + k]);
-        }
-      }
-    } else {
-      e[i] = a[i * n + l];
-    }
-    d[i] = h;
-  }
-  d[0] = 0.0;
-  e[0] = 0.0;
-  for (int i = 0; i < n; ++i) {
-    int l = i - 1;
-    if (d[i] != 0.0) {
-      for (int j = 0; j <= l; ++j) {
-        double g = 0.0;
-        for (int k = 0; k <= l; ++k) g += a[i * n + k] * a[k * n + j];
-        for (int k = 0; k <= l; ++k) a[k * n + j] -= g * a[k * n + i];
-      }
-    }
-    d[i] = a[i * n + i];
-    a[i * n + i] = 1.0;
-    for (int j = 0; j <= l; ++j) a[j * n + i] = a[i * n + j] = 0.0;
-  }
-}
-
-bool implicit_ql(std::vector<double>& d, std::vector<double>& e, int n, std::vector<double>& z) {
-  for (int i = 1; i < n; ++i) e[i - 1] = e[i];
-  e[n - 1] = 0.0;
-  for (int l = 0; l < n; ++l) {
-    int iter = 0, m;
-    do {
-      for (m = l; m < n - 1; ++m) {
-        double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
-        if (std::fabs(e[m]) <= 1e-300 + std::numeric_limits<double>::epsilon() * dd) break;
-      }
-      if (m != l) {
-        if (iter++ == 60) return false;
-        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-        double r = std::hypot(g, 1.0);
-        g = d[m] - d[l] + e[l] / (g + (g >= 0 ? std::fabs(r) : -std::fabs(r)));
-        double s = 1.0, c = 1.0, p = 0.0;
-        int i;
-        for (i = m - 1; i >= l; --i) {
-          double f = s * e[i], b = c * e[i];
-          e[i + 1] = (r = std::hypot(f, g));
-          if (r == 0.0) {
-            d[i + 1] -= p;
-            e[m] = 0.0;
-            break;
-          }
-          s = f / r;
-          c = g / r;
-          g = d[i + 1] - p;
-          r = (d[i] - g) * s + 2.0 * c * b;
-          d[i + 1] = g + (p = s * r);
-          g = c * r - b;
-          for (int k = 0; k < n; ++k) {
-            f = z[k * n + i + 1];
-            z[k * n + i + 1] = s * z[k * n + i] + c * f;
-            z[k * n + i] = c * z[k * n + i] - s * f;
-          }
-        }
-        if (r == 0.0 && i >= l) continue;
-        d[l] -= p;
-        e[l] = g;
-        e[m] = 0.0;
-      }
-    } while (m != l);
-  }
-  return true;
-}
-
-// eigen-decomposition of symmetric T (row-major m x m): ascending values,
-// vectors as columns of Z (row-major).
-bool sym_eig(const std::vector<double>& T, int m, std::vector<double>& w, std::vector<double>& Z) {
-  Z = T;
-  std::vector<double> e;
-  householder_tridiag(Z, m, w, e);
-  if (!implicit_ql(w, e, m, Z)) return false;
-  // sort ascending
-  std::vector<int> ord(m);
-  for (int i = 0; i < m; ++i) ord[i] = i;
-  std::sort(ord.begin(), ord.end(), [&](int a, int b) { return w[a] < w[b]; });
-  std::vector<double> w2(m), Z2((size_t)m * m);
-  for (int c = 0; c < m; ++c) {
-    w2[c] = w[ord[c]];
-    for (int r = 0; r < m; ++r) Z2[r * m + c] = Z[r * m + ord[c]];
-  }
-  w.swap(w2);
-  Z.swap(Z2);
-  return true;
-}
-
-}  // namespace
 
 // ---------------------------------------------------------------------------
 // device-resident symmetric operator
@@ -848,7 +714,7 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
       T[j * m + j] = alpha[j];
       if (j + 1 < m) T[j * m + j + 1] = T[(j + 1) * m + j] = beta[j];
     }
-    if (!sym_eig(T, m, th, Z)) return mds_fail(ctx, MDS_ERR_INTERNAL, "projected eigenproblem did not converge");
+    if (!mds_symeig::sym_eig(T, m, th, Z)) return mds_fail(ctx, MDS_ERR_INTERNAL, "projected eigenproblem did not converge");
     const double bm = beta[m - 1];
     // wanted: the nev largest (ascending order -> last nev)
     int nconv = 0;
