@@ -136,20 +136,25 @@ int mds_knn_data(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, 
 /*
  * knn_data without device allocation. This entry point has no counterpart in
  * the reference. It is for callers that cannot allocate device memory where
- * they call: a thread that is capturing a CUDA stream into a graph (cudaMalloc
- * is not allowed during a global-mode capture), or a process whose device
- * memory is held entirely by another allocator. It computes what mds_knn_data
- * computes (same outputs), takes DEVICE pointers for every array, and keeps
- * all of its scratch in one fixed 32 MiB array inside the library, so it
- * calls no cudaMalloc/cudaFree. Problems whose scratch would exceed 32 MiB
- * (about n_fit * (2(k+1) rounded up to 32) * 8 bytes of candidates plus n *
- * dim * 4 bytes of vectors) are rejected with MDS_ERR_UNSUPPORTED.
+ * they call, such as a plugin running inside another framework whose caching
+ * allocator has reserved the device memory in full (a cudaMalloc there fails
+ * or takes memory the host framework counts on). It computes what
+ * mds_knn_data computes (same outputs), takes DEVICE pointers for every
+ * array, and keeps all of its scratch in one fixed 32 MiB array inside the
+ * library, so it calls no cudaMalloc/cudaFree and no allocating library
+ * routine. Problems whose scratch would exceed 32 MiB (about n_fit * K' * 8
+ * bytes of candidates, K' = 1.5(k+1) rounded up to 32 and at most 192, plus
+ * n * dim * 4 bytes of vectors) are rejected with MDS_ERR_UNSUPPORTED. When
+ * K' < k + 17 every row is rechecked exactly, as mds_knn_data does.
  *   flags: 0 or MDS_CORRELATION (sorted output only).
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture. Calls share the array: calls that
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, once per device); make that first call before any
+ * stream capture. The call synchronises ctx's stream before it returns.
+ * Calls share the array and it keeps the last call's contents: calls that
  * may overlap on the GPU (other contexts or threads) race and must be
- * serialised by the caller. Every GPU that loads the library holds the 32 MiB
- * until the process exits.
+ * serialised by the caller. The caller's current device is restored on
+ * return. Every GPU that loads the library holds the 32 MiB until the
+ * process exits.
  */
 int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, int n_fit, int dim, int k,
                          unsigned flags, double* out_d, int32_t* out_i, int* k_used);

@@ -18,6 +18,7 @@
 //                  multiply-add, sequential sum), select k+1 by (value, index),
 //                  drop position 0, verify the guard.
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <vector>
 
@@ -554,35 +555,54 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
 
 // ---------------------------------------------------------------------------
 // Allocation-free variant (mds_knn_data_noalloc). Some callers cannot obtain
-// device memory at the point of the call: a host thread capturing a stream
-// into a CUDA graph (cudaMalloc is not allowed during a global-mode capture),
-// or a process whose device memory is reserved in full by another allocator.
-// This entry point takes device inputs and outputs and keeps every scratch
-// buffer in one file-scope device array of fixed size, so it never calls
-// cudaMalloc or cudaFree. Every GPU that loads this library holds the array
-// until the process exits.
+// device memory at the point of the call: a plugin running inside another
+// framework whose caching allocator has reserved the device memory in full
+// (a cudaMalloc there fails, or takes memory the host framework counts on),
+// or an embedding that forbids the library its own allocations. This entry
+// point takes device inputs and outputs and keeps every scratch buffer in
+// one file-scope device array of fixed size, so it never calls cudaMalloc
+// or cudaFree. Every GPU that loads this library holds the array until the
+// process exits.
 // ---------------------------------------------------------------------------
 #define MDS_NOALLOC_SCRATCH_BYTES (32u << 20)  // 32 MiB
+#define MDS_NOALLOC_MAX_DEVICES 64
 
 static __device__ __align__(256) unsigned char g_knn_data_scratch[MDS_NOALLOC_SCRATCH_BYTES];
 
-// Device address of the array, taken once per device with that device
-// current (the host symbol g_knn_data_scratch is only a stand-in for it).
-static void* noalloc_scratch(mds_ctx* ctx) {
-  static void* addr[256] = {nullptr};
-  int dev = ctx->device;
-  if (dev < 0 || dev >= 256) return nullptr;
-  if (!addr[dev]) {
-    cudaSetDevice(dev);
+// Device address of the array. In host code g_knn_data_scratch names a
+// host-side stand-in, so the address is taken with cudaGetSymbolAddress,
+// once per device (std::call_once: safe from several host threads), with
+// that device current. The caller's current device is left as it was.
+static void* noalloc_scratch(int dev) {
+  static std::once_flag once[MDS_NOALLOC_MAX_DEVICES];
+  static void* addr[MDS_NOALLOC_MAX_DEVICES];
+  if (dev < 0 || dev >= MDS_NOALLOC_MAX_DEVICES) return nullptr;
+  std::call_once(once[dev], [dev] {
+    int prev = -1;
+    const bool had = cudaGetDevice(&prev) == cudaSuccess;
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_knn_data_scratch) != cudaSuccess) {
+    if (cudaSetDevice(dev) == cudaSuccess && cudaGetSymbolAddress(&p, g_knn_data_scratch) == cudaSuccess)
+      addr[dev] = p;
+    else
       cudaGetLastError();
-      return nullptr;
-    }
-    addr[dev] = p;
-  }
+    if (had) cudaSetDevice(prev);
+  });
   return addr[dev];
 }
+
+// Makes ctx's device current for the call and puts the caller's back on
+// every return path.
+struct NoallocDeviceScope {
+  int prev = -1;
+  bool had = false;
+  explicit NoallocDeviceScope(int dev) {
+    had = cudaGetDevice(&prev) == cudaSuccess;
+    cudaSetDevice(dev);
+  }
+  ~NoallocDeviceScope() {
+    if (had) cudaSetDevice(prev);
+  }
+};
 
 extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, int n_fit,
                                     int dim, int k, unsigned flags, double* out_d, int32_t* out_i, int* k_used) {
@@ -601,8 +621,11 @@ extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, 
   if (k_used) *k_used = k;
   if (n_fit == 0 || k == 0) return MDS_OK;
   const int Dp = mds_round_up(dim, DT_KC);
-  const int Kp = std::min(mds_round_up(std::max(k + 1 + 32, 2 * (k + 1)), 32), 448);
-  if (Kp < k + 1 + 16) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k=%d too large", k);
+  // K' as mds_knn_data's FP32 screen chooses it, within the screen's shared
+  // memory pools; when that leaves fewer than 16 spare candidates the screen
+  // does not pay off and every row is rechecked exactly (as mds_knn_data)
+  const int Kp = std::min(mds_round_up(std::max(k + 1 + 32, (k + 1) * 3 / 2), 32), DT_MAX_KP);
+  const bool exact_rows = Kp < k + 1 + 16;
   // scratch layout, 256-byte aligned pieces
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t need = 0;
@@ -617,67 +640,90 @@ extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, 
     o_mf = need;  need += up(sizeof(double) * (size_t)n_fit);
     o_sf = need;  need += up(sizeof(double) * (size_t)n_fit);
   }
-  const size_t o_cand = need;  need += up(sizeof(uint64_t) * (size_t)n_fit * Kp);
-  const size_t o_cn = need;    need += up(sizeof(int) * (size_t)n_fit);
+  size_t o_cand = 0, o_cn = 0;
+  if (!exact_rows) {
+    o_cand = need;  need += up(sizeof(uint64_t) * (size_t)n_fit * Kp);
+    o_cn = need;    need += up(sizeof(int) * (size_t)n_fit);
+  }
   const size_t o_fl = need;    need += up(sizeof(int) * (size_t)n_fit);
   const size_t o_nfl = need;   need += up(sizeof(int));
   if (need > MDS_NOALLOC_SCRATCH_BYTES)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED,
                     "mds_knn_data_noalloc: this problem needs %zu bytes of scratch, more than the fixed %u bytes "
                     "(use mds_knn_data)", need, (unsigned)MDS_NOALLOC_SCRATCH_BYTES);
-  unsigned char* base = static_cast<unsigned char*>(noalloc_scratch(ctx));
+  unsigned char* base = static_cast<unsigned char*>(noalloc_scratch(ctx->device));
   if (!base) return mds_fail(ctx, MDS_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
-  cudaSetDevice(ctx->device);
+  NoallocDeviceScope scope(ctx->device);
   cudaStream_t s = ctx->stream;
   float* xr = reinterpret_cast<float*>(base + o_xr);
   float* nr = reinterpret_cast<float*>(base + o_nr);
   double* mr = reinterpret_cast<double*>(base + o_mr);
   double* sr = reinterpret_cast<double*>(base + o_sr);
-  const float* xf = xr;
   const float* nf = nr;
   const double* mf = mr;
   const double* sf = sr;
+  const float* xf = xr;
   k_vec_prep<<<(n_ref + 127) / 128, 128, 0, s>>>(ref, n_ref, dim, Dp, corr, xr, nr, mr, sr);
+  ctx->stats.launches++;
   if (!same) {
     float* xf2 = reinterpret_cast<float*>(base + o_xf);
     float* nf2 = reinterpret_cast<float*>(base + o_nf);
     double* mf2 = reinterpret_cast<double*>(base + o_mf);
     double* sf2 = reinterpret_cast<double*>(base + o_sf);
     k_vec_prep<<<(n_fit + 127) / 128, 128, 0, s>>>(fit, n_fit, dim, Dp, corr, xf2, nf2, mf2, sf2);
+    ctx->stats.launches++;
     xf = xf2; nf = nf2; mf = mf2; sf = sf2;
   }
   MDS_CUDA(ctx, cudaGetLastError());
-  uint64_t* cand = reinterpret_cast<uint64_t*>(base + o_cand);
-  int* cand_n = reinterpret_cast<int*>(base + o_cn);
+  const double* dfit = same ? ref : fit;
   int* flagged = reinterpret_cast<int*>(base + o_fl);
   int* nflag = reinterpret_cast<int*>(base + o_nfl);
+  if (exact_rows) {
+    size_t rsm = data_recheck_smem(dim, 1, 1, k, 1);
+    if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
+    MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
+    k_data_recheck<<<n_fit, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, n_fit, nullptr, n_ref, dim, corr, 1,
+                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, nullptr, nullptr);
+    ctx->stats.launches++;
+    MDS_CUDA(ctx, cudaGetLastError());
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->stats.passes = 1;
+    return MDS_OK;
+  }
+  uint64_t* cand = reinterpret_cast<uint64_t*>(base + o_cand);
+  int* cand_n = reinterpret_cast<int*>(base + o_cn);
   // the array keeps the previous call's contents: the flag counter restarts at zero
   MDS_CUDA(ctx, cudaMemsetAsync(nflag, 0, sizeof(int), s));
   const size_t ssm = screen_dot_smem(Kp);
-  if (ssm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "k too large");
   MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
   const int nrt = (n_fit + DT_TM - 1) / DT_TM;
-  k_screen_dot<<<nrt, DT_THREADS, ssm, s>>>(xf, xr, nf, nr, n_fit, nullptr, n_ref, Dp, corr, 1.0f / 65536.0f, Kp, 1,
+  k_screen_dot<<<nrt, DT_THREADS, ssm, s>>>(xf, xr, nf, nr, n_fit, nullptr, n_ref, Dp, corr, MDS_GUARD_FP32, Kp, 1,
                                             cand, cand_n);
+  ctx->stats.launches++;
   MDS_CUDA(ctx, cudaGetLastError());
-  const double* dfit = same ? ref : fit;
   size_t rsm = data_recheck_smem(dim, Kp, 1, k, 0);
   if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
   MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
   k_data_recheck<<<n_fit, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, n_fit, nullptr, n_ref, dim, corr, 0,
                                                 cand, cand_n, 1, Kp, k, nullptr, out_d, out_i, flagged, nflag);
+  ctx->stats.launches++;
   MDS_CUDA(ctx, cudaGetLastError());
   int hflag = 0;
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag, sizeof(int), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  ctx->stats.kprime = Kp;
   ctx->stats.rows_flagged = hflag;
+  ctx->stats.passes = 1;
   if (hflag > 0) {
-    // rows whose guard failed: every reference vector is rechecked exactly
+    // rows whose guard check failed: every reference vector is rechecked
+    // exactly; the flagged list is only read here (exact rows flag nothing)
     rsm = data_recheck_smem(dim, 1, 1, k, 1);
     if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
     k_data_recheck<<<hflag, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, hflag, flagged, n_ref, dim, corr, 1,
-                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, flagged, nflag);
+                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, nullptr, nullptr);
+    ctx->stats.launches++;
+    ctx->stats.passes = 2;
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
   }
