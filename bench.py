@@ -15,9 +15,29 @@ candidate screen, fused top-k, exact recheck and output.
          pivot pass -- over the screen stage's CUDA-event time, against the
          measured dense bf16 tensor peak. About 5% of the N^2 pairs are
          computed; pairs_equivalent / flops_equivalent give the N^2 figures
+  roofline_recheck  the exact recheck stage: 30*A FP32 flops per candidate
+         it computes (counted by the kernel) over its CUDA-event time, against
+         the nominal FP32 rate; its operand bytes (12*A per candidate, served
+         mostly from L2) as a rate beside it
+  screen_guard  the recheck's audit of the screen's lower bound on every
+         candidate it rechecks: the largest screen error per unit of
+         |a_i|^2 + |a_j|^2 (which the guard coefficient must exceed) and the
+         number of bounds found above their exact value (rows so found are
+         finished by the wider FP32 screen or exactly)
+  tc_vs_fp32  screen-stage times of the tensor-core screen with tile
+         skipping switched off (every tile computed) and of the FP32
+         CUDA-core screen (every tile computed), on this workload
+  parity  after the timed loops, 256 rows of the timed run's output (and of
+         the FP32 path's) against the FP64 oracle (oracle/): largest distance
+         error, index agreement, swaps inside tie bands of 1e-4 Angstrom
   cpu_baseline  the reference's per-pair procedure and OpenMP row loop
          restated in C++ (oracle/mds_oracle.cpp, orc_knn_rms_port) on a bounded
          sample of fit rows against all reference frames, all host cores
+
+With --gpus N > 1 (one process per GPU under torchrun) every rank computes a
+contiguous block of the fit rows against all reference frames (the kNN
+stage's row sharding: no collective on the data path, strong scaling);
+--replicas runs the whole workload on every rank instead.
 
 `--impl reference` times that CPU restatement alone (the reference itself
 needs GROMACS, Boost and Berkeley DB and cannot be built here).
@@ -56,6 +76,11 @@ def parse():
     p.add_argument("--k", type=int, default=K)
     p.add_argument("--cpu-rows", type=int, default=0, help="fit rows of the CPU sample (0 = auto)")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-parity", action="store_true", help="skip the oracle check of sampled rows")
+    p.add_argument("--parity-rows", type=int, default=256)
+    p.add_argument("--no-compare", action="store_true", help="skip the dense TC / FP32 screen comparison")
+    p.add_argument("--replicas", action="store_true",
+                   help="N > 1: every rank runs the whole workload (default: row shards)")
     p.add_argument("--serve", action="store_true",
                    help="Nystrom serving benchmark (50,000 landmarks x 304 atoms, k=50, nev=10)")
     p.add_argument("--serve-seconds", type=float, default=8.0)
@@ -437,6 +462,14 @@ def cpu_sample(x, rows, k, threads):
     return rows * x.shape[0] / dt, dt
 
 
+def bench_config(args, n, a, k, world, replicas):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": f"knn_rms all-pairs N={n} A={a} k={k}", "frames": n, "atoms": a, "k": k,
+            "basins": 8, "drift_nm": 0.08,
+            "l2": "inputs (240 MB of frames) larger than L2 every step",
+            "parallelism": (f"replicas x{world}" if replicas else f"row shards x{world}")}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -455,13 +488,53 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp32/fp64", "data": "synthetic",
-           "config": {"workload": f"knn_rms all-pairs N={args.frames} A={args.atoms} k={args.k}",
-                      "frames": args.frames, "atoms": args.atoms, "k": args.k},
+           "config": bench_config(args, args.frames, args.atoms, args.k, args.gpus, args.replicas),
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": sample},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
+
+
+TOL_A = 1e-4  # 1e-5 nm in the output's Angstrom units
+
+
+def parity_rows(x, rows, k):
+    """GPU rows against the FP64 oracle (outside every timed region). The
+    oracle gives k+1 columns so that a swap at the k-th position can be
+    recognised as a tie with the (k+1)-th."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    m = np.ones(x.shape[1], np.float32)
+    t0 = time.perf_counter()
+    od1, oi1 = O.knn_rms(x, x[rows], m, k + 1)
+    dt = time.perf_counter() - t0
+    return od1, oi1, dt
+
+
+def parity_summary(d, i, od1, oi1, k):
+    import numpy as np
+
+    od, oi = od1[:, :k], oi1[:, :k]
+    err = float(np.max(np.abs(d - od)))
+    swaps, bad = 0, 0
+    for r, c in np.argwhere(i != oi):
+        v = od[r, c]
+        near = np.abs(od1[r] - v) <= 2 * TOL_A
+        if abs(d[r, c] - v) <= TOL_A and near.sum() >= 2:
+            swaps += 1
+        else:
+            bad += 1
+    return {"rows": int(d.shape[0]), "max_abs_err_A": err, "tolerance_A": TOL_A,
+            "index_agreement": float(np.mean(i == oi)), "tie_swaps": swaps, "index_errors": bad,
+            "ok": bool(err <= TOL_A and bad == 0)}
+
+
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
 
 
 def main():
@@ -484,53 +557,62 @@ def main():
 
         dist.init_process_group("nccl")
     from mdsctk_gb300 import Context
+    from mdsctk_gb300.shard import row_range
 
     x = workload(args.frames, args.atoms)
     n, a, k = x.shape[0], x.shape[1], args.k
-    # rows of this rank (weak scaling: every rank runs the whole workload's
-    # row count against all reference frames; units = its own pairs)
+    # N > 1: each rank computes a contiguous block of fit rows against every
+    # reference frame (the row sharding of the kNN stage, no collective on the
+    # data path; total work fixed = strong scaling); --replicas runs the whole
+    # workload on every rank instead (weak scaling)
+    replicas = args.replicas or world == 1
+    r0, r1 = (0, n) if replicas else row_range(n, rank, world)
     ctx = Context(local)
     dev = torch.device("cuda", local)
     xd = torch.from_numpy(x).to(dev)
+    fitd = None if (r0, r1) == (0, n) else xd[r0:r1]
     md = torch.ones(a, dtype=torch.float32, device=dev)
     kk = min(k, n - 1)
-    out = (torch.empty((n, kk), dtype=torch.float64, device=dev),
-           torch.empty((n, kk), dtype=torch.int32, device=dev))
+    nrow = r1 - r0
+    out = (torch.empty((nrow, kk), dtype=torch.float64, device=dev),
+           torch.empty((nrow, kk), dtype=torch.int32, device=dev))
     # host side for e2e: pinned frames in, pinned k-NN lists out
     xh = torch.from_numpy(x).pin_memory()
-    dh = torch.empty((n, kk), dtype=torch.float64).pin_memory()
-    ih = torch.empty((n, kk), dtype=torch.int32).pin_memory()
+    fith = None if fitd is None else xh[r0:r1]
+    dh = torch.empty((nrow, kk), dtype=torch.float64).pin_memory()
+    ih = torch.empty((nrow, kk), dtype=torch.int32).pin_memory()
     mh = np.ones(a, np.float32)
 
-    def step_dev():
-        ctx.knn_rms(xd, None, md, k, precision=args.precision, out=out)
+    def step_dev(precision=args.precision, skip=True):
+        ctx.knn_rms(xd, fitd, md, k, precision=precision, out=out, skip=skip)
 
     def step_e2e():
-        ctx.knn_rms(xh.numpy(), None, mh, k, precision=args.precision, out=(dh.numpy(), ih.numpy()))
+        ctx.knn_rms(xh.numpy(), None if fith is None else fith.numpy(), mh, k, precision=args.precision,
+                    out=(dh.numpy(), ih.numpy()))
 
-    for _ in range(max(args.warmup, 3)):
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
         step_dev()
     torch.cuda.synchronize()
     sampler = ClockSampler(local)
     sampler.start()
     sampler.wait_first()
+    # identical steps back to back for ~2 s before the timed region, so the
+    # clock record holds samples under this load (they count as warm-up)
+    t_soak = time.perf_counter()
+    while time.perf_counter() - t_soak < 2.0:
+        step_dev()
+        warm += 1
+    torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
-    screen_ms, recheck_ms, prep_ms, total_ms, launches, flagged = [], [], [], [], 0, 0
-    screen_pairs = []
+    stats = []
     for _ in range(args.steps):
         step_dev()
-        st = ctx.stats()
-        screen_ms.append(st["screen_ms"])
-        screen_pairs.append(st["screen_pairs"])
-        recheck_ms.append(st["recheck_ms"])
-        prep_ms.append(st["prep_ms"])
-        total_ms.append(st["total_ms"])
-        launches += st["launches"]
-        flagged = max(flagged, st["rows_flagged"])
+        stats.append(ctx.stats())
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
@@ -540,48 +622,106 @@ def main():
         torch.distributed.barrier()
         ms = float(t.item())
     clocks = sampler.stop()
+    clocks["window"] = "2 s of identical steps immediately before the timed region, and the timed region"
+
+    def med(key, st=None):
+        v = sorted(s_[key] for s_ in (st or stats))
+        return v[len(v) // 2]
+
+    launches = sum(s_["launches"] for s_ in stats)
+    flagged = max(s_["rows_flagged"] for s_ in stats)
+    d_last, i_last = out[0].cpu().numpy(), out[1].cpu().numpy()
     # end to end through the C ABI with host buffers
-    for _ in range(1):
-        step_e2e()
+    step_e2e()
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step_e2e()
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
-    pairs = float(n) * n
-    value = pairs * world / (ms / 1000.0)
-    e2e = pairs * world / (e2e_ms / 1000.0)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    pairs_rank = float(nrow) * n
+    pairs_all = pairs_rank * world if replicas else float(n) * n
+    value = pairs_all / (ms / 1000.0)
+    e2e = pairs_all / (e2e_ms / 1000.0)
     peaks, pk_kind = measured_peaks()
-    scr = sorted(screen_ms)[len(screen_ms) // 2]
-    computed = float(sorted(screen_pairs)[len(screen_pairs) // 2]) or pairs
+    scr = med("screen_ms")
+    computed = float(med("screen_pairs")) or pairs_rank
     flops = 18.0 * a * computed
     achieved = flops / (scr / 1000.0) / 1e12
     peak = float(peaks.get("bf16_tflops", 1900.0))
-    # correctness spot check of the last device run: a few rows vs the oracle
+    rc_ms = med("recheck_ms")
+    rp = float(med("recheck_pairs"))
+    Ap = (a + 63) // 64 * 64
+    r_flops = 30.0 * a * rp  # per candidate and atom: d (3), D (3) and Q (9) FMAs
+    r_bytes = 12.0 * a * rp + nrow * 12.0 * Ap
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None,
+           "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak" if replicas else "strong", "vs_baseline": None,
            "dtype": {"fp32": "fp32", "bf16x3": "bf16x3+fp32", "fp16x3": "fp16x3+fp32"}[args.precision],
            "data": "synthetic",
-           "config": {"workload": f"knn_rms all-pairs N={n} A={a} k={k}", "frames": n, "atoms": a,
-                      "k": k, "precision": args.precision, "basins": 8, "drift_nm": 0.08,
-                      "l2": "inputs (240 MB of frames) larger than L2 every step",
-                      "parallelism": f"replicas x{world}"},
+           "config": bench_config(args, n, a, k, world, replicas),
+           "precision": args.precision,
            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                        "frac": achieved / peak, "traffic": screen_traffic(args),
+                        "frac": achieved / peak, "traffic": screen_traffic(args) if replicas else None,
                         "kernel": "screen", "kernel_ms": scr, "flops_per_launch": flops,
-                        "pairs_computed": computed, "pairs_equivalent": pairs,
-                        "flops_equivalent": 18.0 * a * pairs,
+                        "pairs_computed": computed, "pairs_equivalent": pairs_rank,
+                        "flops_equivalent": 18.0 * a * pairs_rank,
                         "peak_kind": f"{pk_kind} bf16 burst"},
-           "stages_ms": {"prep": sorted(prep_ms)[len(prep_ms) // 2], "screen": scr,
-                         "recheck": sorted(recheck_ms)[len(recheck_ms) // 2],
-                         "call": sorted(total_ms)[len(total_ms) // 2]},
+           "roofline_recheck": {"bound": "fp32", "achieved": r_flops / (rc_ms / 1000.0) / 1e12,
+                                "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                                "frac": r_flops / (rc_ms / 1000.0) / 1e12 / FP32_NOMINAL_TFLOPS,
+                                "peak_kind": "nominal FP32 (152 SMs x 128 lanes x 2 x 2.07 GHz)",
+                                "kernel": "recheck stage", "kernel_ms": rc_ms, "candidates": rp,
+                                "candidates_per_row": rp / max(nrow, 1), "flops_per_launch": r_flops,
+                                "bytes_per_launch": r_bytes, "l2_gbs": r_bytes / (rc_ms / 1000.0) / 1e9},
+           "stages_ms": {"prep": med("prep_ms"), "screen": scr, "recheck": rc_ms, "call": med("total_ms")},
            "rows_flagged": flagged,
+           "screen_guard": {"guard_coef": stats[-1]["guard_coef"],
+                            "screen_err_max": max(s_["screen_err_max"] for s_ in stats),
+                            "violations": max(s_["guard_violations"] for s_ in stats),
+                            "rows_flagged_by_violation": max(s_["rows_audit_flagged"] for s_ in stats),
+                            "pairs_audited_per_call": rp},
            "clocks": clocks,
            "gpu_launches": launches,
            "e2e": {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms,
                    "h2d_bytes_per_step": int(x.nbytes + a * 4),
-                   "d2h_bytes_per_step": int(n * kk * 12)}}
+                   "d2h_bytes_per_step": int(nrow * kk * 12)}}
+    # Like-for-like screens on this workload: both dense (every tile), and
+    # each as it runs by default (tensor-core with tile skipping, FP32 dense).
+    cmp = {}
+    if not args.no_compare:
+        def screen_runs(precision, skip, reps):
+            step_dev(precision, skip)
+            sts = []
+            for _ in range(reps):
+                step_dev(precision, skip)
+                sts.append(ctx.stats())
+            return sts
+
+        tcd = screen_runs(args.precision, False, 3)
+        fpd = screen_runs("fp32", True, 2)
+        d_fp32, i_fp32 = out[0].cpu().numpy(), out[1].cpu().numpy()
+        cmp = {"tc_dense_screen_ms": med("screen_ms", tcd), "tc_dense_screen_pairs": med("screen_pairs", tcd),
+               "fp32_dense_screen_ms": med("screen_ms", fpd),
+               "tc_skip_screen_ms": scr,
+               "tc_vs_fp32_dense": med("screen_ms", fpd) / med("screen_ms", tcd),
+               "tc_call_ms": med("total_ms"), "fp32_call_ms": med("total_ms", fpd),
+               "tc_vs_fp32_call": med("total_ms", fpd) / med("total_ms"),
+               "note": "screen stage times by CUDA events; the FP32 screen computes every tile"}
+        res["tc_vs_fp32"] = cmp
+    # parity of the timed run: sampled rows against the FP64 oracle
+    if rank == 0 and not args.no_parity:
+        rows = np.linspace(0, nrow - 1, min(args.parity_rows, nrow)).astype(int)
+        od1, oi1, pdt = parity_rows(x, rows + r0, k)
+        res["parity"] = parity_summary(d_last[rows], i_last[rows], od1, oi1, kk)
+        res["parity"]["oracle"] = f"FP64 QCP restatement, {len(rows)} rows x {n} frames ({pdt:.1f} s)"
+        if cmp:
+            res["parity_fp32_path"] = parity_summary(d_fp32[rows], i_fp32[rows], od1, oi1, kk)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rows = args.cpu_rows or 16 * threads

@@ -49,6 +49,9 @@ extern "C" {
 #define MDS_PREC_BF16X3 0x10u /* candidate screen on tcgen05, split BF16 (3 products) */
 #define MDS_PREC_FP16X3 0x20u /* candidate screen on tcgen05, split FP16 (3 products) */
 #define MDS_PREC_MASK 0xF0u
+#define MDS_NO_SKIP 0x100u    /* knn_rms, tensor-core screen: compute every tile
+                                 (no triangle-inequality tile skipping). Same
+                                 results; for timing the screens like for like */
 
 typedef struct mds_ctx mds_ctx;
 
@@ -66,6 +69,14 @@ typedef struct mds_knn_stats {
   int launches;        /* all kernel launches of the call */
   long long screen_pairs; /* pairs the first-pass screen computed: tiles not
                              skipped (40 x 80 frames each) plus the pivot pass */
+  long long recheck_pairs; /* candidates the first-pass recheck computed exactly */
+  int guard_violations;    /* rechecked candidates whose screen lower bound was
+                              above their exact RMSD^2 (rows flagged; expected 0) */
+  float screen_err_max;    /* largest screen error over the rechecked pairs,
+                              (screen RMSD^2 - exact) / (|a_i|^2 + |a_j|^2): the
+                              quantity the guard coefficient must exceed */
+  float guard_coef;        /* guard coefficient of the first-pass screen */
+  int rows_audit_flagged;  /* rows flagged because of a guard violation */
 } mds_knn_stats;
 
 /* Library version string. */

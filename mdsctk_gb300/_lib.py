@@ -27,6 +27,7 @@ MDS_CORRELATION = 0x8
 MDS_PREC_FP32 = 0x00
 MDS_PREC_BF16X3 = 0x10
 MDS_PREC_FP16X3 = 0x20
+MDS_NO_SKIP = 0x100
 
 PRECISIONS = {"fp32": MDS_PREC_FP32, "bf16x3": MDS_PREC_BF16X3, "fp16x3": MDS_PREC_FP16X3}
 
@@ -43,7 +44,9 @@ class KnnStats(ctypes.Structure):
                 ("pairs", ctypes.c_longlong), ("kprime", ctypes.c_int),
                 ("rows_flagged", ctypes.c_int), ("passes", ctypes.c_int),
                 ("screen_launches", ctypes.c_int), ("launches", ctypes.c_int),
-                ("screen_pairs", ctypes.c_longlong)]
+                ("screen_pairs", ctypes.c_longlong), ("recheck_pairs", ctypes.c_longlong),
+                ("guard_violations", ctypes.c_int), ("screen_err_max", ctypes.c_float),
+                ("guard_coef", ctypes.c_float), ("rows_audit_flagged", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -89,11 +89,12 @@ class Context:
 
     # ------------------------------------------------------------------ kNN
     def knn_rms(self, ref, fit=None, mass=None, k: int = 1, nofit: bool = False, sort: bool = True,
-                precision: str = "fp32", out=None):
+                precision: str = "fp32", out=None, skip: bool = True):
         """knn_rms: k nearest reference frames of every fit frame by minimum
         RMSD (Angstrom). ref/fit: [n, natoms, 3] float32 nm (uncentred).
         Returns (distances [n_fit, k] f64, indices [n_fit, k] i32), or the
-        full [n_fit, n_ref] rows when sort=False."""
+        full [n_fit, n_ref] rows when sort=False. skip=False makes the screen
+        compute every tile (same results; for like-for-like timing)."""
         dev = _is_device(ref)
         n_ref, natoms = int(ref.shape[0]), int(ref.shape[1])
         n_fit = n_ref if fit is None else int(fit.shape[0])
@@ -102,6 +103,8 @@ class Context:
             flags |= L.MDS_NOFIT
         if not sort:
             flags |= L.MDS_FULL
+        if not skip:
+            flags |= L.MDS_NO_SKIP
         if dev:
             import torch
 

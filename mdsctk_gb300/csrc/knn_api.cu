@@ -102,6 +102,7 @@ static int knn_rms_impl(mds_ctx* ctx, const float* ref_xyz, int n_ref, const flo
   pl.k = k;
   pl.nofit = (flags & MDS_NOFIT) ? 1 : 0;
   pl.full = full ? 1 : 0;
+  pl.noskip = (flags & MDS_NO_SKIP) ? 1 : 0;
   pl.prec = prec;
   // K' = 2(k+1) (at least k+33): the recheck stops early once the k+1 best
   // are settled, so a wide K' mainly makes the guard hold on the first pass

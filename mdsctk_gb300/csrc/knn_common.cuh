@@ -23,6 +23,7 @@ struct KnnRmsPlan {
   int k = 0;       // clamped k
   int kprime = 0;  // candidates kept per row by the screen
   int nofit = 0, full = 0;
+  int noskip = 0;  // MDS_NO_SKIP: the tensor-core screen computes every tile
   unsigned prec = MDS_PREC_FP32;
   float guard_fp32 = 0.f;  // lower-bound margin per unit of |a_i|^2+|a_j|^2
   float guard_tc = 0.f;
@@ -114,10 +115,21 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
 // Exact recheck from the superposed deviations (Af/Ar [n][3][Ap]) and the
 // template mu [3][Ap] (knn_rms.cu).
 // Ur: the reference frames' U as written by launch_prep (unused with nofit).
+// Audit of the screen's bounds by the recheck (mode 0): the fit and
+// reference records (|a|^2 in entry 15), the guard coefficient of the screen
+// that produced the candidates, and four device counters: candidates
+// rechecked, bounds above their exact value, the largest screen error per
+// unit of |a_i|^2 + |a_j|^2 (float bits), rows flagged for a violation.
+struct RecheckAudit {
+  const float* recf = nullptr;
+  const float* recr = nullptr;
+  float guard = 0.f;
+  unsigned long long* counters = nullptr;
+};
 int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
                    const float* Ur, int nrows, const int* rowlist, int mode, const uint64_t* cand,
                    const int* cand_n, int nseg, int segstride, int Kp, int k, double* out_d, int* out_i,
-                   int* flagged, int* nflag, const float* rowthr = nullptr);
+                   int* flagged, int* nflag, const float* rowthr = nullptr, const RecheckAudit* audit = nullptr);
 int choose_nseg_fp32(int nfit, int num_sms, int nref);
 
 // Candidates wanted per row before rounding: k+33, 2(k+1), and with the

@@ -23,6 +23,7 @@
 //                   select k+1, drop position 0, verify the guard.
 //  5. rows whose guard failed are screened again with 4x the candidates.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
@@ -650,7 +651,8 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
           const int* __restrict__ rowlist, int Nr, int Ap, int natoms, int nofit, int mode,
           const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int segstride, int Kp, int k,
           double* __restrict__ out_d, int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag,
-          const float* __restrict__ rowthr) {
+          const float* __restrict__ rowthr, const float* __restrict__ recf, const float* __restrict__ recr,
+          float guard, unsigned long long* __restrict__ audit) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* sa = reinterpret_cast<float*>(smem_raw);                 // [3*Ap] a_i
   float* sd = sa + 3 * Ap;                                        // [CHUNK]
@@ -783,12 +785,33 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
   bool stopped = false;
   int base = 0;
   const int first = min(RC_CHUNK, (k1 + 8 + 31) / 32 * 32);
+  // Audit of the screen's lower bound: every rechecked candidate has both
+  // its bound b (screen value minus the guard) and its exact RMSD^2, so the
+  // screen error the guard must cover, (b + guard E - exact) / E with E =
+  // |a_i|^2 + |a_j|^2, is measured on exactly the pairs near the row's
+  // threshold. A bound above the exact value (beyond the recheck's own
+  // ~1e-6 relative error) is a guard violation: the row is flagged and
+  // finished by the wider FP32 screen or exactly, and the call reports it.
+  const bool auditing = audit != nullptr && mode == 0;
+  const float Ei = auditing ? __ldg(recf + (int64_t)grow * MDS_REC + 15) : 0.0f;
+  float a_coef = 0.0f;
+  int a_viol = 0;
   while (base < total) {
     int nc = min((mode == 0 && base == 0) ? first : RC_CHUNK, total - base);
     for (int c = threadIdx.x; c < nc; c += blockDim.x)
       cj[c] = (mode == 0) ? mds_key_index(keys[base + c]) : base + c;
     __syncthreads();
     recheck_chunk(sa, ui, C6, Ar, Ur, Ap, cj, nc, nofit, sd, ssum);
+    if (auditing)
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const float b = mds_key_value(keys[base + c]);
+        if (b > 0.0f) {  // (bounds clamped at zero carry no error information)
+          const float r2 = sd[c] * sd[c];
+          const float E = Ei + __ldg(recr + (int64_t)cj[c] * MDS_REC + 15);
+          if (E > 0.0f) a_coef = fmaxf(a_coef, (b + guard * E - r2) / E);
+          a_viol += (b > r2 * (1.0f + 4e-6f)) ? 1 : 0;
+        }
+      }
     // place the chunk after the current k1 best and re-sort
     for (int c = threadIdx.x; c < RC_CHUNK; c += blockDim.x)
       top[k1 + c] = (c < nc) ? mds_pack_key(sd[c], cj[c]) : MDS_KEY_INF;
@@ -809,13 +832,27 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
       }
     }
   }
+  int violated = 0;
+  if (audit) {
+    // one atomic per warp: candidates rechecked, violations, largest error
+    const int lane = threadIdx.x & 31;
+    const unsigned cb = __reduce_max_sync(0xffffffffu, __float_as_uint(fmaxf(a_coef, 0.0f)));
+    const int vs = __reduce_add_sync(0xffffffffu, (unsigned)a_viol);
+    if (lane == 0) {
+      if (cb) atomicMax(audit + 2, (unsigned long long)cb);
+      if (vs) atomicAdd(audit + 1, (unsigned long long)vs);
+    }
+    if (threadIdx.x == 0) atomicAdd(audit + 0, (unsigned long long)base);
+    violated = __syncthreads_or(a_viol > 0);
+  }
   // guard: the (k+1)-th exact RMSD^2 must not exceed the smallest lower bound
-  // of every excluded pair.
+  // of every excluded pair, and no rechecked bound may exceed its exact value.
   if (threadIdx.x == 0) {
     double dk = (double)mds_key_value(top[k1 - 1]);
-    if (mode == 0 && !stopped && !(dk * dk * (1.0 + 1e-6) <= (double)tau)) {
+    if (mode == 0 && (violated || (!stopped && !(dk * dk * (1.0 + 1e-6) <= (double)tau)))) {
       int pos = atomicAdd(nflag, 1);
       flagged[pos] = grow;
+      if (violated) atomicAdd(audit + 3, 1ull);
     }
   }
   for (int x = threadIdx.x; x < k; x += blockDim.x) {
@@ -915,7 +952,8 @@ int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofi
 int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
                    const float* Ur, int nrows, const int* rowlist, int mode,
                    const uint64_t* cand, const int* cand_n, int nseg, int segstride, int Kp, int k,
-                   double* out_d, int* out_i, int* flagged, int* nflag, const float* rowthr) {
+                   double* out_d, int* out_i, int* flagged, int* nflag, const float* rowthr,
+                   const RecheckAudit* audit) {
   size_t smem = recheck_smem(pl.Ap, Kp, k, mode);
   if (mode == 0) {
     // the streaming merge works on the best K' plus one segment's K'
@@ -935,7 +973,10 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const fl
   if (nrows > 0)
     k_recheck<<<nrows, RC_THREADS, smem, ctx->stream>>>(Af, Ar, mu, Ur, nrows, rowlist, pl.nref, pl.Ap, pl.natoms,
                                                         pl.nofit, mode, cand, cand_n, nseg, segstride, Kp, k,
-                                                        out_d, out_i, flagged, nflag, rowthr);
+                                                        out_d, out_i, flagged, nflag, rowthr,
+                                                        audit ? audit->recf : nullptr, audit ? audit->recr : nullptr,
+                                                        audit ? audit->guard : 0.0f,
+                                                        audit ? audit->counters : nullptr);
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
@@ -1142,7 +1183,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     TcSkip sk;
     TcPivots pv;
     DevBuf lb(ctx), rowlo(ctx), farw(ctx), farp(ctx);
-    const bool skipping = !pl.screen_keys && (nref + 79) / 80 >= 4;
+    const bool skipping = !pl.screen_keys && !pl.noskip && (nref + 79) / 80 >= 4;
     if (skipping) {
       MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv, same));
       MDS_TRY(lb.alloc(ctx, sizeof(float) * (size_t)pv.nP * nfit));
@@ -1189,14 +1230,35 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     st.kprime = Kp;
     return MDS_OK;
   }
+  // the recheck audits the screen's bounds on the pairs it rechecks
+  DevBuf audit_c(ctx);
+  MDS_TRY(audit_c.alloc(ctx, 4 * sizeof(unsigned long long)));
+  MDS_CUDA(ctx, cudaMemsetAsync(audit_c.p, 0, 4 * sizeof(unsigned long long), s));
+  RecheckAudit audit;
+  audit.recf = Rfp;
+  audit.recr = Rr.as<float>();
+  audit.guard = (pl.prec == MDS_PREC_FP32) ? pl.guard_fp32 : pl.guard_tc;
+  audit.counters = audit_c.as<unsigned long long>();
   MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 0, cand.as<uint64_t>(),
                          cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i, flagged.as<int>(),
-                         nflag.as<int>(), pl.prec == MDS_PREC_FP32 ? nullptr : rowthr.as<float>()));
+                         nflag.as<int>(), pl.prec == MDS_PREC_FP32 ? nullptr : rowthr.as<float>(), &audit));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0;
+  unsigned long long hc[4] = {0, 0, 0, 0};
   if (ntiles.p) MDS_CUDA(ctx, cudaMemcpyAsync(&ht, ntiles.p, sizeof(ht), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaMemcpyAsync(hc, audit_c.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  st.recheck_pairs = (long long)hc[0];
+  st.guard_violations = (int)hc[1];
+  {
+    const unsigned bits = (unsigned)hc[2];
+    float f;
+    std::memcpy(&f, &bits, sizeof(f));
+    st.screen_err_max = f;
+  }
+  st.guard_coef = audit.guard;
+  st.rows_audit_flagged = (int)hc[3];
   float t01 = 0, t12 = 0, t23 = 0;
   cudaEventElapsedTime(&t01, ctx->ev[0], ctx->ev[1]);
   cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
@@ -1234,9 +1296,11 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(cand_n.alloc(ctx, sizeof(int) * (size_t)hflag * nseg2));
     MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), hflag, rows.as<int>(), Kp,
                                nseg2, cand.as<uint64_t>(), cand_n.as<int>()));
+    RecheckAudit audit2 = audit;  // the re-screen's bounds carry the FP32 guard
+    audit2.guard = pl.guard_fp32;
     MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), hflag, rows.as<int>(), 0,
                            cand.as<uint64_t>(), cand_n.as<int>(), nseg2, Kp, Kp, k, dout_d, dout_i,
-                           flagged.as<int>(), nflag.as<int>()));
+                           flagged.as<int>(), nflag.as<int>(), nullptr, &audit2));
     MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
   }
