@@ -5,6 +5,13 @@ Loads ``oracle/_build/libmds_oracle.so`` (built from ``mds_oracle.cpp`` by
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import
 this module; the product library never does.
 
+Pinned on the reference's own code (ref_build.py compiles its functions
+from the checkout into _ref/, where one is present): euclidean_distance,
+correlation_distance, euclidean_distance_sparse with permutation::sort in
+the kNN loops, sp_dsymv, sp_dgemv, decomp_sparse's affinity block and
+entropic_affinity_sigmas; tests/test_ref_pin.py checks the restatements
+below against them bit for bit.
+
 Parity status: **parity unpinned** for the RMSD values (GROMACS do_fit /
 rmsdev / reset_x are third-party and absent; the reference cannot be built
 here and ships no golden outputs). The eigensolve is anchored on ARPACK, the
@@ -378,3 +385,78 @@ def nystrom_extend(evals, evecs, m, pcolB, irowB, B):
     for x in range(len(evals)):
         out[x] = sp_dgemv(m, pcolB, irowB, B, evecs[x] / evals[x])
     return out
+
+
+# ---------------------------------------------------------------------------
+# The reference's own functions, compiled from its checkout by ref_build.py
+# (oracle/_ref/libmds_ref.so). Present only where the checkout is; the tests
+# that pin the oracle on it skip elsewhere.
+# ---------------------------------------------------------------------------
+_ref_lib = None
+
+
+def ref_lib():
+    """The library built by ref_build.py, or None."""
+    global _ref_lib
+    if _ref_lib is None:
+        import sys
+
+        if _HERE not in sys.path:
+            sys.path.insert(0, _HERE)
+        import ref_build
+
+        path = ref_build.build()
+        if path is None or not os.path.exists(path):
+            return None
+        L = ctypes.CDLL(path)
+        c_int, c_dbl = ctypes.c_int, ctypes.c_double
+        _i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+        for nm in ("ref_euclidean_distance", "ref_correlation_distance"):
+            getattr(L, nm).argtypes = [c_int, _f64p, _f64p]
+            getattr(L, nm).restype = c_dbl
+        L.ref_euclidean_distance_sparse.argtypes = [c_int, _i32p, _f64p, c_int, _i32p, _f64p]
+        L.ref_euclidean_distance_sparse.restype = c_dbl
+        for nm in ("ref_sp_dsymv", "ref_sp_dgemv"):
+            getattr(L, nm).argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+            getattr(L, nm).restype = None
+        L.ref_affinity.argtypes = [c_int, _i32p, _i32p, _f64p, c_dbl, _f64p]
+        L.ref_affinity.restype = None
+        L.ref_entropic_sigmas.argtypes = [c_int, c_int, c_dbl, _f64p, _f64p]
+        L.ref_entropic_sigmas.restype = None
+        L.ref_knn_data.argtypes = [_f64p, c_int, _f64p, c_int, c_int, c_int, c_int, c_int, _f64p, _i32p]
+        L.ref_knn_data.restype = None
+        L.ref_knn_data_sparse.argtypes = [_i64p, _i32p, _f64p, c_int, _i64p, _i32p, _f64p, c_int, c_int,
+                                          _f64p, _i32p]
+        L.ref_knn_data_sparse.restype = None
+        _ref_lib = L
+    return _ref_lib
+
+
+def ref_knn_data(ref, fit, k, correlation=False, sort=True):
+    """knn_data's row loop around the reference's own distance functions and
+    permutation::sort (entries [1..k] of the k+1 smallest)."""
+    ref = _c(ref, np.float64)
+    fit = ref if fit is None else _c(fit, np.float64)
+    nref, dim = ref.shape
+    nfit = fit.shape[0]
+    kk = min(k, nref - 1)
+    width = kk if sort else nref
+    d = np.zeros(nfit * width, np.float64)
+    i = np.zeros(nfit * width, np.int32)
+    ref_lib().ref_knn_data(ref.reshape(-1), nref, fit.reshape(-1), nfit, dim, int(k), int(correlation),
+                           int(sort), d, i)
+    return d.reshape(nfit, width), i.reshape(nfit, width)
+
+
+def ref_knn_data_sparse(ref, fit, k):
+    """knn_data_sparse's row loop around the reference's
+    euclidean_distance_sparse; ref / fit as for knn_data_sparse (CSR)."""
+    ro, ri, rv = ref
+    fo, fi, fv = ref if fit is None else fit
+    nref, nfit = len(ro) - 1, len(fo) - 1
+    kk = min(k, nref - 1)
+    d = np.zeros(nfit * kk, np.float64)
+    i = np.zeros(nfit * kk, np.int32)
+    ref_lib().ref_knn_data_sparse(_c(ro, np.int64), _c(ri, np.int32), _c(rv, np.float64), nref,
+                                  _c(fo, np.int64), _c(fi, np.int32), _c(fv, np.float64), nfit, int(k), d, i)
+    return d.reshape(nfit, kk), i.reshape(nfit, kk)

@@ -10,7 +10,9 @@
   oracle; the reference itself cannot be built without GROMACS, Boost,
   Berkeley DB and ARPACK).
 
-Run from the repository root: python tests/golden/make_golden.py
+Run from the repository root:
+    python tests/golden/make_golden.py [REFERENCE_CHECKOUT]
+The reference checkout defaults to $MDS_REFERENCE, else /root/reference.
 """
 import os
 import shutil
@@ -20,10 +22,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REFERENCE_EXAMPLES = "/root/reference/examples"
 
 
 def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MDS_REFERENCE", "/root/reference")
+    REFERENCE_EXAMPLES = os.path.join(ref, "examples")
     for name in ("rings.pts", "swissroll.pts", "trp-cage.xtc", "trp-cage.pdb"):
         src = os.path.join(REFERENCE_EXAMPLES, name)
         if os.path.exists(src):
