@@ -600,9 +600,10 @@ def main():
     # identical steps back to back for ~2 s before the timed region, so the
     # clock record holds samples under this load (they count as warm-up)
     t_soak = time.perf_counter()
+    soak = 0
     while time.perf_counter() - t_soak < 2.0:
         step_dev()
-        warm += 1
+        soak += 1
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -622,7 +623,8 @@ def main():
         torch.distributed.barrier()
         ms = float(t.item())
     clocks = sampler.stop()
-    clocks["window"] = "2 s of identical steps immediately before the timed region, and the timed region"
+    clocks["window"] = "2 s of identical untimed steps immediately before the timed region, and the timed region"
+    clocks["soak_steps"] = soak
 
     def med(key, st=None):
         v = sorted(s_[key] for s_ in (st or stats))

@@ -373,6 +373,11 @@ int mds_server_submit(mds_server* s, const float* query_xyz, int m, int64_t* tic
 int mds_server_wait(mds_server* s, int64_t ticket, int timeout_ms, double* ext, double* knn_d, int32_t* knn_i,
                     mds_request_info* info);
 int mds_server_get_stats(mds_server* s, mds_server_stats* out);
+/* hold != 0: admit no queued request into a batch until called again with
+ * 0 (batches already running finish; submissions keep queueing). Lets an
+ * operator drain the device or gather a burst into shared batches. No
+ * reference counterpart (the reference runs the Nystrom chain per file). */
+int mds_server_hold(mds_server* s, int hold);
 
 #ifdef __cplusplus
 }

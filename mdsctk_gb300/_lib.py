@@ -103,6 +103,7 @@ SIGNATURES = {
     "mds_server_submit": ([_vp, _vp, _i, _i64p], _i),
     "mds_server_wait": ([_vp, ctypes.c_int64, _i, _vp, _vp, _vp, ctypes.POINTER(RequestInfo)], _i),
     "mds_server_get_stats": ([_vp, ctypes.POINTER(ServerStats)], _i),
+    "mds_server_hold": ([_vp, _i], _i),
     "mds_decomp_sparse_nystrom": ([_vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _d, _i, _i, _d, _i, _u, _vp, _vp,
                                    _vp, _vp, _ip], _i),
     "mds_xtc_index": ([_vp, _sz, _vp, _i, _ip, _ip], _i),

@@ -789,9 +789,10 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
   // its bound b (screen value minus the guard) and its exact RMSD^2, so the
   // screen error the guard must cover, (b + guard E - exact) / E with E =
   // |a_i|^2 + |a_j|^2, is measured on exactly the pairs near the row's
-  // threshold. A bound above the exact value (beyond the recheck's own
-  // ~1e-6 relative error) is a guard violation: the row is flagged and
-  // finished by the wider FP32 screen or exactly, and the call reports it.
+  // threshold. A bound above the exact value by more than the FP32
+  // recheck's own error (RMSD^2 to ~1.7e-5 relative in the worst case seen;
+  // 3e-5 is allowed) is a guard violation: the row is flagged and finished
+  // by the wider FP32 screen or exactly, and the call reports it.
   const bool auditing = audit != nullptr && mode == 0;
   const float Ei = auditing ? __ldg(recf + (int64_t)grow * MDS_REC + 15) : 0.0f;
   float a_coef = 0.0f;
@@ -809,7 +810,7 @@ k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const floa
           const float r2 = sd[c] * sd[c];
           const float E = Ei + __ldg(recr + (int64_t)cj[c] * MDS_REC + 15);
           if (E > 0.0f) a_coef = fmaxf(a_coef, (b + guard * E - r2) / E);
-          a_viol += (b > r2 * (1.0f + 4e-6f)) ? 1 : 0;
+          a_viol += (b > r2 * (1.0f + 3e-5f)) ? 1 : 0;
         }
       }
     // place the chunk after the current k1 best and re-sort

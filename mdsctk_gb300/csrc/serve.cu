@@ -139,6 +139,7 @@ struct mds_server {
   std::condition_variable cv_work, cv_done;
   std::thread worker;
   bool stop = false;
+  bool hold = false;  // mds_server_hold: admit nothing while set
   int64_t next_ticket = 1;
   mds_server_stats st{};
   KnnRmsPlan plan(int nfit) const {
@@ -373,7 +374,7 @@ static void worker_loop(mds_server* S) {
       std::unique_lock<std::mutex> lk(S->mu);
       if (S->stop && S->queue.empty() && !any_busy) break;
       for (auto& sl : S->slots) {
-        if (sl.busy || S->queue.empty()) continue;
+        if (sl.busy || S->queue.empty() || (S->hold && !S->stop)) continue;
         sl.reqs.clear();
         sl.m = 0;
         while (!S->queue.empty() && sl.m + S->queue.front()->m <= sl.cap) {
@@ -400,7 +401,7 @@ static void worker_loop(mds_server* S) {
           any_busy = true;
         }
       }
-      if (!any_busy && S->queue.empty() && !S->stop) {
+      if (!any_busy && (S->queue.empty() || S->hold) && !S->stop) {
         S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
         continue;
       }
@@ -655,6 +656,16 @@ extern "C" int mds_server_wait(mds_server* S, int64_t ticket, int timeout_ms, do
     info->batch = rq->batch;
     info->batch_frames = rq->batch_frames;
   }
+  return MDS_OK;
+}
+
+extern "C" int mds_server_hold(mds_server* S, int hold) {
+  if (!S) return MDS_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->hold = hold != 0;
+  }
+  S->cv_work.notify_all();
   return MDS_OK;
 }
 

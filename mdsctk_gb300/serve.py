@@ -74,6 +74,11 @@ class Server:
         return ext, d, i, {"queue_ms": info.queue_ms, "total_ms": info.total_ms, "batch": info.batch,
                            "batch_frames": info.batch_frames}
 
+    def hold(self, on: bool = True):
+        """Admit no queued request into a batch while on (running batches
+        finish, submissions keep queueing); hold(False) resumes."""
+        self._check(self._lib.mds_server_hold(self.h, int(bool(on))))
+
     def stats(self) -> dict:
         s = L.ServerStats()
         self._check(self._lib.mds_server_get_stats(self.h, ctypes.byref(s)))

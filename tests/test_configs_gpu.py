@@ -88,8 +88,8 @@ def test_config_headline_sampled_rows(ctx, headline, precision):
     d, i = ctx.knn_rms(x, None, m, k, precision=precision)
     st = ctx.stats()
     _check_rows(d[rows], i[rows], od1, oi1, k)
-    assert st["guard_violations"] == 0
-    assert st["screen_err_max"] < st["guard_coef"]
+    assert st["guard_violations"] == 0, st
+    assert st["screen_err_max"] < st["guard_coef"], st
     if precision == "bf16x3":
         # every tile computed: the same output
         d2, i2 = ctx.knn_rms(x, None, m, k, precision=precision, skip=False)
