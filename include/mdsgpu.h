@@ -90,6 +90,19 @@ const char* mds_last_error(const mds_ctx* ctx);
 int mds_get_knn_stats(const mds_ctx* ctx, mds_knn_stats* out);
 
 /*
+ * Fault injection for tests of the failure paths (no reference
+ * counterpart: the reference's tools only return exit codes). Arms a fault
+ * for the next call on ctx that reaches it; each fires once.
+ *   MDS_INJECT_SCREEN_STALL: the next tensor-core screen launch withholds its
+ *   end-of-work marker, so the kernel's bounded waits run out after about a
+ *   second; the kernel then releases its resources and reports it, and the
+ *   call returns MDS_ERR_TIMEOUT. The context stays usable.
+ * what = 0 disarms.
+ */
+#define MDS_INJECT_SCREEN_STALL 0x1u
+int mds_test_inject(mds_ctx* ctx, unsigned what);
+
+/*
  * knn_rms: for each fit frame, the k nearest reference frames by minimum
  * mass-weighted RMSD after optimal superposition.
  * Replaces knn_rms.cpp:38-41 (distance = do_fit + rmsdev x 10) and the row

@@ -28,6 +28,7 @@ MDS_PREC_FP32 = 0x00
 MDS_PREC_BF16X3 = 0x10
 MDS_PREC_FP16X3 = 0x20
 MDS_NO_SKIP = 0x100
+MDS_INJECT_SCREEN_STALL = 0x1
 
 PRECISIONS = {"fp32": MDS_PREC_FP32, "bf16x3": MDS_PREC_BF16X3, "fp16x3": MDS_PREC_FP16X3}
 
@@ -85,6 +86,7 @@ SIGNATURES = {
     "mds_create": ([_i, _sz, ctypes.POINTER(_vp)], _i),
     "mds_destroy": ([_vp], _i),
     "mds_last_error": ([_vp], ctypes.c_char_p),
+    "mds_test_inject": ([_vp, _u], _i),
     "mds_get_knn_stats": ([_vp, ctypes.POINTER(KnnStats)], _i),
     "mds_knn_rms": ([_vp, _vp, _i, _vp, _i, _i, _vp, _i, _u, _vp, _vp, _ip], _i),
     "mds_knn_rms_screen": ([_vp, _vp, _i, _vp, _i, _i, _vp, _i, _u, _vp, _vp], _i),

@@ -103,3 +103,10 @@ extern "C" int mds_get_knn_stats(const mds_ctx* ctx, mds_knn_stats* out) {
   *out = ctx->stats;
   return MDS_OK;
 }
+
+extern "C" int mds_test_inject(mds_ctx* ctx, unsigned what) {
+  if (!ctx) return MDS_ERR_ARG;
+  if (what & ~MDS_INJECT_SCREEN_STALL) return mds_fail(ctx, MDS_ERR_ARG, "unknown fault 0x%x", what);
+  ctx->inject = what;
+  return MDS_OK;
+}

@@ -106,7 +106,8 @@ int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, co
 // Uhl (optional): the frames' U = sum a mu^T as double-float pairs [n][18],
 // which the recheck needs for the reference frames.
 int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
-                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R, float* Uhl = nullptr);
+                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R, float* Uhl = nullptr,
+                int* bad = nullptr, int fbase = 0);
 int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit, std::vector<double>& mu,
                    double M0[9]);
 int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* recf,
@@ -154,7 +155,7 @@ int tcv_max_kprime();
 int tcv_max_dp();
 int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref);
 int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
-                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n,
+                      int nref, int Dp, bool corr, int Kp, int k, int nseg, bool same, uint64_t* candout, int* cand_n,
                       float* rowthr);
 
 // Tile skipping data of the tensor-core screen (knn_rms_tc.cu): lower

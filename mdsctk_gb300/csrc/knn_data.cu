@@ -295,12 +295,12 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
     __syncthreads();
     block_bitonic_sort(keys, P2);
     total = min(t, Kp);
-    // the bound of every pair left out: the K'-th candidate's, or, when the
-    // lists hold fewer than K', the threshold the screen filtered them with
-    if (t >= Kp)
-      tau = mds_key_value(keys[Kp - 1]);
-    else if (rowthr)
-      tau = rowthr[grow];
+    // the bound of every pair left out: the K'-th candidate's, or the
+    // threshold the screen filtered them with, whichever is smaller (the
+    // tensor-core screen's thresholds follow the (k+1)-th bound, so its
+    // final threshold can lie below the K'-th candidate)
+    if (t >= Kp) tau = mds_key_value(keys[Kp - 1]);
+    if (rowthr) tau = fminf(tau, rowthr[grow]);
   } else {
     total = Nr;
   }
@@ -497,7 +497,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   st.screen_launches = 1;
   if (tc) {
     MDS_TRY(rthr.alloc(ctx, sizeof(float) * (size_t)nfit));
-    MDS_TRY(launch_screen_tcv(ctx, xf, nfp, nfit, Xr.as<float>(), Nrm.as<float>(), nref, Dp, corr, Kp, nseg, same,
+    MDS_TRY(launch_screen_tcv(ctx, xf, nfp, nfit, Xr.as<float>(), Nrm.as<float>(), nref, Dp, corr, Kp, k, nseg, same,
                               cand.as<uint64_t>(), cand_n.as<int>(), rthr.as<float>()));
   } else {
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -79,7 +79,8 @@ struct TvShared {
   uint32_t tmem_base;
   int abortf;
   int cnt2[TV_ROWS][2];   // keys in each (row, column half) region
-  float thr[TV_ROWS];     // the row's list threshold (+inf until its list first fills)
+  float thr[TV_ROWS];     // the row's list threshold (+inf until its list first holds k+1 keys)
+  float rslack[TV_ROWS][2];  // 2 g (|x|^2 + nmax): the (k+1)-th bound's slack of the row
 };
 
 static size_t tv_smem_bytes(int Dp, int nst) {
@@ -97,19 +98,33 @@ __device__ __forceinline__ int tv_tile_order(int i, int t0, int t1, int td) {
 }
 
 
-// One fit row's list (regions src[0, c0) and src[TV_LCAP, TV_LCAP + c1)):
-// keep the Kp best and write them, unsorted, as the segment's candidate list
-// (the recheck sorts the merged lists). Called by the warp owning the row.
-__device__ __forceinline__ void tv_publish(uint64_t* src, int c0, int c1, int Kp, int* hist, uint64_t* dst,
-                                           int* dst_n, int lane) {
+// One fit row's list (regions src[0, c0) and src[lcap, lcap + c1)): keep
+// the Kp best, drop those above the row's threshold tp (appended under a
+// looser one: every pair the screen left out lies at or above the final
+// threshold, which the recheck verifies against), and write the rest,
+// unsorted, as the segment's candidate list (the recheck sorts the merged
+// lists). Called by the warp owning the row.
+__device__ __forceinline__ void tv_publish(uint64_t* src, int c0, int c1, int lcap, int Kp, float tp, int* hist,
+                                           uint64_t* dst, int* dst_n, int lane) {
   if (c0 + c1 > Kp) {
-    warp_select_keep2(src, c0, TV_LCAP, c1, Kp, hist, lane);
+    warp_select_keep2(src, c0, lcap, c1, Kp, hist, lane);
     c0 = Kp;
     c1 = 0;
   }
-  for (int e = lane; e < c0; e += 32) dst[e] = src[e];
-  for (int e = lane; e < c1; e += 32) dst[c0 + e] = src[TV_LCAP + e];
-  if (lane == 0) *dst_n = c0 + c1;
+  int m = 0;
+  for (int r = 0; r < 2; ++r) {
+    const int n = r ? c1 : c0;
+    const uint64_t* from = src + (r ? lcap : 0);
+    for (int x0 = 0; x0 < n; x0 += 32) {
+      const int x = x0 + lane;
+      const uint64_t key = (x < n) ? from[x] : MDS_KEY_INF;
+      const bool keep = x < n && mds_key_value(key) <= tp;
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (keep) dst[m + __popc(bal & ((1u << lane) - 1u))] = key;
+      m += __popc(bal);
+    }
+  }
+  if (lane == 0) *dst_n = m;
   __syncwarp();
 }
 
@@ -118,7 +133,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
              const float* __restrict__ nf, const float* __restrict__ colterm, int nfit, int Nr, int Dp, int nst,
              int corr, float guard, uint32_t idesc, int Kp, int nseg, int nitems, int diag, int pilot,
              float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
-             int* __restrict__ cand_n, int* __restrict__ err) {
+             int* __restrict__ cand_n, int* __restrict__ err, int lcap, int k1, const float* __restrict__ nmax) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
   // pilot > 0: a pass that only seeds rowthr: each item (one per row pair
   // tile, nseg = 1) visits `pilot` column tiles (outward from the diagonal
@@ -126,8 +141,16 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   // row's rowthr to the K'-th smallest screen value it saw, an upper bound of
   // the row's final K'-th smallest; nothing else is written.
   // colterm: [ncoltiles * TV_N] column terms (+inf past Nr).
-  // work: [gridDim.x][TV_ROWS][TC_CAPG] list buffers of the CTAs;
-  // candout: [nfit][nseg][Kp] sorted lists, cand_n [nfit][nseg] their sizes.
+  // work: [gridDim.x][TV_ROWS][TC_CAPG] list buffers of the CTAs; a row's
+  // list is two regions of lcap keys (K' + one tile's half, rounded up): a
+  // smaller region keeps the CTAs' lists resident in L2.
+  // candout: [nfit][nseg][Kp] lists, cand_n [nfit][nseg] their sizes.
+  // Thresholds from the (k+1)-th bound (nmax: the largest norm term of the
+  // reference set): a key's value b is the screen value minus the guard
+  // g (|x|^2 + |y|^2), and the screen value is within the guard of the exact
+  // one, so the row's (k+1)-th exact value is at most b_(k+1) +
+  // 2 g (|x|^2 + nmax); a compaction sets the row threshold to the smaller of
+  // that and the K'-th bound, and the first one runs when k1 keys arrive.
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -305,7 +328,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     float* sv = reinterpret_cast<float*>(hist);  // [16][32]: a chunk's screen values, column-major
     const int own0 = u * 128 + 32 * q + 16 * half;  // the 16 rows this warp compacts and publishes
     uint64_t* lists = work + (size_t)blockIdx.x * TV_ROWS * TC_CAPG;
-    uint64_t* mylist = lists + (size_t)r * TC_CAPG + half * TV_LCAP;
+    uint64_t* mylist = lists + (size_t)r * TC_CAPG + half * lcap;
+    const float slack = 2.0f * guard * __ldg(nmax);  // + 2 g |x|^2 of the row, at each item's start
     const float mul = corr ? -0.5f : -2.0f;
     uint32_t acc = 0;
     bool ok = true;
@@ -337,6 +361,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         g = rp * TV_ROWS + r;
         const float rn = (g < nfit) ? __ldg(nf + g) : 0.0f;
         rc = (g >= nfit) ? INF : corr ? 0.5f - guard * rn : rn * (1.0f - guard);
+        S->rslack[r][half] = slack + 2.0f * guard * rn;  // (each half's warp keeps its own copy)
       }
       if (task.y < 0) {
         // end of the item: publish the owned rows and clear their state
@@ -344,11 +369,15 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           const int rr = own0 + x;
           const int gg = rp * TV_ROWS + rr;
           if (gg < nfit && !pilot) {
-            tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], S->cnt2[rr][1], Kp, hist,
+            const float tp = fminf(S->thr[rr], __ldcg(rowthr + gg));
+            tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], S->cnt2[rr][1], lcap, Kp, tp, hist,
                        candout + ((int64_t)gg * nseg + seg) * Kp, cand_n + (int64_t)gg * nseg + seg, lane);
-          } else if (gg < nfit && S->cnt2[rr][0] + S->cnt2[rr][1] >= Kp) {
-            const float t =
-                warp_select_keep2(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], TV_LCAP, S->cnt2[rr][1], Kp, hist, lane);
+          } else if (gg < nfit && S->cnt2[rr][0] + S->cnt2[rr][1] >= k1) {
+            const int c = S->cnt2[rr][0] + S->cnt2[rr][1];
+            float tk1 = INF;
+            float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], lcap, S->cnt2[rr][1],
+                                        c >= Kp ? Kp : 0, hist, lane, k1, &tk1);
+            t = fminf(t, tk1 + S->rslack[rr][half]);
             if (lane == 0) atomicMin(reinterpret_cast<int*>(rowthr + gg), __float_as_int(t));
           }
           if (lane == 0) {
@@ -403,7 +432,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           while (mask) {
             const int t = __ffs(mask) - 1;
             mask &= mask - 1;
-            if (cnt < TV_LCAP) mylist[cnt] = mds_pack_key(fmaxf(sv[t * 32 + lane] + rc, 0.0f), j0 + 16 * cc + t);
+            if (cnt < lcap) mylist[cnt] = mds_pack_key(fmaxf(sv[t * 32 + lane] + rc, 0.0f), j0 + 16 * cc + t);
             ++cnt;
           }
         }
@@ -414,8 +443,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->tempty[b]);
       ++acc;
-      if (cnt > TV_LCAP) atomicMax(err, 4);  // cannot happen: compaction keeps room for a tile
-      S->cnt2[r][half] = min(cnt, TV_LCAP);
+      if (cnt > lcap) atomicMax(err, 4);  // cannot happen: compaction keeps room for a tile
+      S->cnt2[r][half] = min(cnt, lcap);
       bar_named(pbar, 64);  // both halves of these rows are appended
       // compaction of the owned rows whose regions near full (or first fill)
       for (int x = 0; x < 16; ++x) {
@@ -423,11 +452,19 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const int gg = rp * TV_ROWS + rr;
         if (gg >= nfit) break;
         const int c0 = S->cnt2[rr][0], c1 = S->cnt2[rr][1];
-        if (!(c0 + c1 > Kp && (c0 > TV_LCAP - 64 || c1 > TV_LCAP - 64 || S->thr[rr] == INF))) continue;
-        const float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, c0, TV_LCAP, c1, Kp, hist, lane);
+        const bool over = c0 + c1 > Kp && (c0 > lcap - 64 || c1 > lcap - 64);
+        const bool first = S->thr[rr] == INF && c0 + c1 >= k1;
+        if (!over && !first) continue;
+        const bool cut = c0 + c1 > Kp;
+        float tk1 = INF;
+        float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, c0, lcap, c1, cut ? Kp : 0, hist, lane, k1,
+                                    &tk1);
+        t = fminf(t, tk1 + S->rslack[rr][half]);
         if (lane == 0) {
-          S->cnt2[rr][0] = Kp;
-          S->cnt2[rr][1] = 0;
+          if (cut) {
+            S->cnt2[rr][0] = Kp;
+            S->cnt2[rr][1] = 0;
+          }
           S->thr[rr] = t;
           atomicMin(reinterpret_cast<int*>(rowthr + gg), __float_as_int(t));
         }
@@ -446,6 +483,14 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     tc_fence_after();
     tmem_dealloc(tbase, 512);
   }
+}
+
+// *out = max(*out, x[0..n)) for non-negative x (as int bits; *out starts at 0).
+__global__ void k_max_nonneg(const float* __restrict__ x, int n, float* __restrict__ out) {
+  float m = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = fmaxf(m, x[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(m));
 }
 
 // Largest K' of the vector screen: after a compaction the first region of a
@@ -470,7 +515,7 @@ int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref) {
 // row's pairs were kept (the bound of every pair left out when a row's lists
 // hold fewer than K' in all).
 int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
-                      int nref, int Dp, bool corr, int Kp, int nseg, bool same, uint64_t* candout, int* cand_n,
+                      int nref, int Dp, bool corr, int Kp, int k, int nseg, bool same, uint64_t* candout, int* cand_n,
                       float* rowthr) {
   if (Kp > tcv_max_kprime()) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: K' too large");
   if (Dp % TV_KB || Dp > TV_MAX_DP)
@@ -480,8 +525,15 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   cudaStream_t s = ctx->stream;
   const int rowsA = (nfit + TV_ROWS - 1) / TV_ROWS * TV_ROWS, rowsB = ncoltiles * TV_N;
   const int rowsS = std::max(rowsA, rowsB);
-  DevBuf A(ctx), B(ctx), work(ctx), err(ctx), terms(ctx);
+  DevBuf A(ctx), B(ctx), work(ctx), err(ctx), terms(ctx), nmax(ctx);
   MDS_TRY(terms.alloc(ctx, sizeof(float) * (size_t)rowsS));
+  MDS_TRY(nmax.alloc(ctx, sizeof(float)));
+  MDS_CUDA(ctx, cudaMemsetAsync(nmax.p, 0, sizeof(float), s));
+  ctx->stats.launches++;
+  k_max_nonneg<<<std::max(1, std::min((nref + 255) / 256, 2 * ctx->num_sms)), 256, 0, s>>>(nr, nref, nmax.as<float>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  // list regions: K' plus one tile's half, in whole 32-key steps
+  const int lcap = std::min(TV_LCAP, (Kp + TV_N / 2 + 31) / 32 * 32);
   auto split = [&](const float* X, int n, int rows, DevBuf& out, float* t) -> int {
     MDS_TRY(out.alloc(ctx, sizeof(__nv_bfloat16) * 2 * (size_t)Dp * rows));
     const int64_t total = (int64_t)rows * Dp;
@@ -524,14 +576,16 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
     ctx->stats.launches++;
     k_screen_tcv<<<std::min(npilot, ctx->num_sms), TV_THREADS, smem, s>>>(
         mA, mB, nf, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC, idesc, Kp, 1, npilot,
-        same ? 1 : 0, TV_PILOT, rowthr, work.as<uint64_t>(), candout, cand_n, err.as<int>());
+        same ? 1 : 0, TV_PILOT, rowthr, work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
+        nmax.as<float>());
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaMemsetAsync(err.as<int>() + 1, 0, sizeof(int), s));
   }
   ctx->stats.launches++;
   k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nf, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0,
                                               MDS_GUARD_TC, idesc, Kp, nseg, nitems, same ? 1 : 0, 0, rowthr,
-                                              work.as<uint64_t>(), candout, cand_n, err.as<int>());
+                                              work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
+                                              nmax.as<float>());
   MDS_CUDA(ctx, cudaGetLastError());
   int herr = 0;
   MDS_CUDA(ctx, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));

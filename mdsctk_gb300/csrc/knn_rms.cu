@@ -219,10 +219,12 @@ __global__ void k_center(const float* __restrict__ raw, int n, int natoms, int A
 
 // Pass 1 + 2 (one block per frame): centre of mass, then |y|^2 and the
 // covariance sum y mu^T.
+// bad (optional): receives the smallest index (fbase + f) of a frame with a
+// non-finite coordinate.
 __global__ void __launch_bounds__(128) k_prep_sums(const float* __restrict__ raw, int n, int natoms, int Ap,
                                                    const float* __restrict__ mass, const float* __restrict__ swn,
                                                    float tm, const float* __restrict__ mu, int nofit,
-                                                   float* __restrict__ rec) {
+                                                   float* __restrict__ rec, int* __restrict__ bad, int fbase) {
   __shared__ float red[5 * 10];
   const int f = blockIdx.x;
   if (f >= n) return;
@@ -230,11 +232,17 @@ __global__ void __launch_bounds__(128) k_prep_sums(const float* __restrict__ raw
   float com[3];
   {
     float p[3] = {0.f, 0.f, 0.f};
+    bool fin = true;
 #pragma unroll 4
     for (int a = threadIdx.x; a < natoms; a += blockDim.x) {
       const float mm = mass[a];
-      for (int c = 0; c < 3; ++c) p[c] = fmaf(mm, x[3 * a + c], p[c]);
+      for (int c = 0; c < 3; ++c) {
+        const float v = x[3 * a + c];
+        fin &= isfinite(v);
+        p[c] = fmaf(mm, v, p[c]);
+      }
     }
+    if (bad && __syncthreads_or(!fin) && threadIdx.x == 0) atomicMin(bad, fbase + f);
     float sc[3];
     block_sum_vec32<3>(p, sc, red);
     for (int c = 0; c < 3; ++c) com[c] = sc[c] / tm;
@@ -993,10 +1001,11 @@ int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, co
 }
 
 int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
-                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R, float* Uhl) {
+                float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R, float* Uhl, int* bad,
+                int fbase) {
   if (n <= 0) return MDS_OK;
   ctx->stats.launches += nofit ? 2 : 3;
-  k_prep_sums<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dmass, dswn, tm, dmu, nofit, R);
+  k_prep_sums<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dmass, dswn, tm, dmu, nofit, R, bad, fbase);
   if (!nofit) k_prep_rot<<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, dM0, R);
   k_prep_out<<<n, 128, 0, ctx->stream>>>(draw, n, natoms, Ap, dswn, dmu, dM0, nofit, A, R, Uhl);
   MDS_CUDA(ctx, cudaGetLastError());
@@ -1098,27 +1107,32 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_TRY(Rr.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nref));
   DevBuf Ur(ctx);  // the reference frames' U = sum a mu^T as double-float pairs (recheck)
   MDS_TRY(Ur.alloc(ctx, sizeof(float) * 18 * (size_t)nref));
+  // frames with a non-finite coordinate (reference set, fit set): smallest
+  // index, checked at the call's first synchronisation after the screen
+  DevBuf badf(ctx);
+  MDS_TRY(badf.alloc(ctx, 2 * sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(badf.p, 0x7f, 2 * sizeof(int), s));
   // superposition, one upload chunk at a time
   auto prep_chunks = [&](const float* draw, bool host, const std::vector<int>& cb, int nc, int ev0, float* A,
-                         float* R, float* U) -> int {
+                         float* R, float* U, int* bad) -> int {
     for (int c = 0; c < nc; ++c) {
       if (host) MDS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->chunk_ev[ev0 + c], 0));
       const int f0 = cb[c], nf = cb[c + 1] - cb[c];
       MDS_TRY(launch_prep(ctx, draw + (size_t)f0 * 3 * natoms, nf, natoms, Ap, dmass.as<float>(), dswn.as<float>(),
                           tm, dmu.as<float>(), dM0.as<double>(), pl.nofit, A + (size_t)f0 * 3 * Ap,
-                          R + (size_t)f0 * MDS_REC, U ? U + (size_t)f0 * 18 : nullptr));
+                          R + (size_t)f0 * MDS_REC, U ? U + (size_t)f0 * 18 : nullptr, bad, f0));
     }
     return MDS_OK;
   };
   MDS_TRY(prep_chunks(draw_ref, pl.href != nullptr, cb_ref, nc_ref, 0, Ar.as<float>(), Rr.as<float>(),
-                      pl.nofit ? nullptr : Ur.as<float>()));
+                      pl.nofit ? nullptr : Ur.as<float>(), badf.as<int>()));
   const float* Afp = Ar.as<float>();
   const float* Rfp = Rr.as<float>();
   if (!same) {
     MDS_TRY(Af.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nfit));
     MDS_TRY(Rf.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nfit));
     MDS_TRY(prep_chunks(draw_fit, pl.hfit != nullptr, cb_fit, nc_fit, MDS_MAX_CHUNKS, Af.as<float>(),
-                        Rf.as<float>(), nullptr));
+                        Rf.as<float>(), nullptr, badf.as<int>() + 1));
     Afp = Af.as<float>();
     Rfp = Rf.as<float>();
   }
@@ -1135,11 +1149,18 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 2, nullptr, nullptr, 1, 1,
                            1, 0, dout_d, dout_i, flagged.as<int>(), nflag.as<int>()));
     MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    int hbad[2] = {0, 0};
+    MDS_CUDA(ctx, cudaMemcpyAsync(hbad, badf.p, sizeof(hbad), cudaMemcpyDeviceToHost, s));
     MDS_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    MDS_CUDA(ctx, cudaStreamSynchronize(s));
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
     st.recheck_ms = ms;
     st.passes = 0;
+    if (hbad[0] != 0x7f7f7f7f)
+      return mds_fail(ctx, MDS_ERR_ARG, "reference frame %d has a non-finite coordinate", hbad[0]);
+    if (hbad[1] != 0x7f7f7f7f)
+      return mds_fail(ctx, MDS_ERR_ARG, "fit frame %d has a non-finite coordinate", hbad[1]);
     return MDS_OK;
   }
   // tensor-core operands (split hi/lo), when that screen is selected
@@ -1244,12 +1265,19 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
                          cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i, flagged.as<int>(),
                          nflag.as<int>(), pl.prec == MDS_PREC_FP32 ? nullptr : rowthr.as<float>(), &audit));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
-  int hflag = 0;
+  int hflag = 0, hbad[2] = {0, 0};
   unsigned long long hc[4] = {0, 0, 0, 0};
   if (ntiles.p) MDS_CUDA(ctx, cudaMemcpyAsync(&ht, ntiles.p, sizeof(ht), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(hc, audit_c.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  MDS_CUDA(ctx, cudaMemcpyAsync(hbad, badf.p, sizeof(hbad), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  // (every loop of the screen and recheck is bounded, so such frames only
+  // make their own values meaningless; the call reports them as an error)
+  if (hbad[0] != 0x7f7f7f7f)
+    return mds_fail(ctx, MDS_ERR_ARG, "reference frame %d has a non-finite coordinate", hbad[0]);
+  if (hbad[1] != 0x7f7f7f7f)
+    return mds_fail(ctx, MDS_ERR_ARG, "fit frame %d has a non-finite coordinate", hbad[1]);
   st.recheck_pairs = (long long)hc[0];
   st.guard_violations = (int)hc[1];
   {

@@ -230,7 +230,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             int piv2, const int* __restrict__ far_perm,
             float* __restrict__ dense, float* __restrict__ rowthr, const float* __restrict__ nmax, int k1,
             unsigned long long* __restrict__ ntiles,
-            uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err) {
+            uint64_t* __restrict__ candbuf, int* __restrict__ cand_n, int* __restrict__ err, int stall) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
   // Work items (row tile, column segment) are claimed dynamically by each
   // CTA's producer, which also decides which column tiles of the item to
@@ -341,7 +341,10 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       }
       item = __shfl_sync(0xffffffffu, item, 0);
       if (item < 0) {
-        ok = push(-1, -1);
+        // (stall: an injected fault for the failure-path tests -- the end
+        // marker is withheld, every load issued has been consumed, and the
+        // other roles' bounded waits run out)
+        if (!stall) ok = push(-1, -1);
         break;
       }
       int rt, seg;
@@ -792,13 +795,16 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
     MDS_CUDA(ctx, cudaMemsetAsync(rowthr, 0x7f, sizeof(float) * (size_t)nfit, ctx->stream));
   const float s = tc_scale(pl.prec);
   const uint32_t idesc = umma_idesc_f16(TC_M, TC_N, pl.prec == MDS_PREC_FP16X3 ? 0 : 1);
+  const int stall = (ctx->inject & MDS_INJECT_SCREEN_STALL) ? 1 : 0;
+  ctx->inject &= ~MDS_INJECT_SCREEN_STALL;
   ctx->stats.launches++;
   k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
                                                        pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
                                                        skip ? skip->prad : nullptr, skip ? skip->rowlo : nullptr,
                                                        skip ? skip->piv2 : 0, skip ? skip->far_perm : nullptr,
-                                                       dense, rowthr, nmax, pl.k + 1, ntiles, cand, cand_n, e);
+                                                       dense, rowthr, nmax, pl.k + 1, ntiles, cand, cand_n, e,
+                                                       stall);
   MDS_CUDA(ctx, cudaGetLastError());
   if (derr) return MDS_OK;
   int herr = 0;

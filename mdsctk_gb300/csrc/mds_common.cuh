@@ -38,6 +38,8 @@ struct mds_ctx {
   cudaStream_t copy_stream[2] = {nullptr, nullptr};
   cudaEvent_t chunk_ev[MDS_MAX_CHUNKS * 2] = {};
   cudaEvent_t order_ev = nullptr;
+  // mds_test_inject: faults armed for the next call that reaches them
+  unsigned inject = 0;
 };
 
 // Record an error message on the context and return `code`.
