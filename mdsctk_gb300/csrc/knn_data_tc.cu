@@ -56,12 +56,17 @@
 // beyond n zero. With terms != nullptr also the column term of each row as a
 // reference vector (the screen value is row term + column term - 2 x.y, or
 // - x.y/2 for correlation): |y|^2 (1 - c), or -c |y|^2; +inf beyond n.
+// With nmax != nullptr (zeroed by the caller) also the largest norm of the n
+// vectors, as the float's bits (norms are non-negative).
 __global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows, __nv_bfloat16* __restrict__ out,
-                            const float* __restrict__ nrm, float guard, int corr, float* __restrict__ terms) {
+                            const float* __restrict__ nrm, float guard, int corr, float* __restrict__ terms,
+                            float* __restrict__ nmax) {
   const int64_t total = (int64_t)rows * Dp;
+  float mx = 0.0f;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = e / Dp;
     const int d = (int)(e % Dp);
+    if (nmax && d == 0 && r < n) mx = fmaxf(mx, nrm[r]);
     if (terms && d == 0)
       terms[r] = (r < n) ? (corr ? -guard * nrm[r] : nrm[r] * (1.0f - guard)) : __int_as_float(0x7f800000);
     const float x = (r < n) ? X[r * Dp + d] : 0.0f;
@@ -69,6 +74,10 @@ __global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows
     const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
     out[r * 2 * Dp + d] = hi;
     out[r * 2 * Dp + Dp + d] = lo;
+  }
+  if (nmax) {
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(reinterpret_cast<int*>(nmax), __float_as_int(mx));
   }
 }
 
@@ -485,14 +494,6 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   }
 }
 
-// *out = max(*out, x[0..n)) for non-negative x (as int bits; *out starts at 0).
-__global__ void k_max_nonneg(const float* __restrict__ x, int n, float* __restrict__ out) {
-  float m = 0.0f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = fmaxf(m, x[i]);
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(m));
-}
-
 // Largest K' of the vector screen: after a compaction the first region of a
 // row's list keeps room for one more tile's half (64 keys).
 int tcv_max_kprime() { return TV_LCAP - TV_N / 2; }
@@ -529,17 +530,17 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   MDS_TRY(terms.alloc(ctx, sizeof(float) * (size_t)rowsS));
   MDS_TRY(nmax.alloc(ctx, sizeof(float)));
   MDS_CUDA(ctx, cudaMemsetAsync(nmax.p, 0, sizeof(float), s));
-  ctx->stats.launches++;
-  k_max_nonneg<<<std::max(1, std::min((nref + 255) / 256, 2 * ctx->num_sms)), 256, 0, s>>>(nr, nref, nmax.as<float>());
-  MDS_CUDA(ctx, cudaGetLastError());
-  // list regions: K' plus one tile's half, in whole 32-key steps
-  const int lcap = std::min(TV_LCAP, (Kp + TV_N / 2 + 31) / 32 * 32);
+  // list regions: a compaction is due once a region holds more than
+  // lcap - 64 keys (room for one tile's half); lcap - 64 - K' appends
+  // between compactions keep them rare
+  const int lcap = TV_LCAP;
   auto split = [&](const float* X, int n, int rows, DevBuf& out, float* t) -> int {
     MDS_TRY(out.alloc(ctx, sizeof(__nv_bfloat16) * 2 * (size_t)Dp * rows));
     const int64_t total = (int64_t)rows * Dp;
     const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 16);
     ctx->stats.launches++;
-    k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>(), nr, MDS_GUARD_TC, corr ? 1 : 0, t);
+    k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>(), nr, MDS_GUARD_TC, corr ? 1 : 0, t,
+                                     t ? nmax.as<float>() : nullptr);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
