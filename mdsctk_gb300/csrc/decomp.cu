@@ -363,6 +363,188 @@ __global__ void k_scale_copy(const double* __restrict__ w, double a, int n, doub
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = w[i] * a;
 }
+// ---------------------------------------------------------------------------
+// Lanczos steps j0..m-1 as one cooperative launch
+// ---------------------------------------------------------------------------
+// Every block owns a contiguous range of rows [r0, r1) and keeps w there in
+// shared memory. Per step:
+//   w = A v_j on its rows (a warp per row; x = v_j is read from L2, written
+//   by every block in the previous step), then the partial projections of w
+//   onto the nc = nlock + j + 1 basis columns over its rows -> part1;
+//   barrier; every block reduces part1 in the same fixed order (so all hold
+//   identical h1), w -= V h1 on its rows, partial projections of the new w
+//   -> part2;
+//   barrier; reduce part2 -> h2, w -= V h2, partial |w|^2 -> part3;
+//   barrier; reduce part3: alpha_j = h1[nlock + j] + h2[nlock + j], beta_j =
+//   |w|, breakdown when beta_j <= btol max(|alpha_j|, 1); v_{j+1} = w / beta_j
+//   on its rows (zeros after a breakdown: the host redoes those steps);
+//   barrier before the next step's product reads v_{j+1}.
+// This is the step of the separate-kernel sequence (SpMV, classical
+// Gram-Schmidt twice, norm, scale) with the same arithmetic per element; the
+// sums are grouped by block instead of by 256-row chunk, and stay
+// deterministic. Values written during the launch are read with ld.global.cg
+// (L2), never through the non-coherent L1 of another SM.
+struct LzSync {
+  unsigned count;
+  unsigned gen;
+  int err;
+  int pad;
+};
+
+// Grid-wide barrier (the launch is cooperative, so every block is resident).
+// A block waiting longer than limit_ns records an error and leaves; blocks
+// see the error at their next barrier and leave the step loop there.
+__device__ __forceinline__ bool lz_grid_sync(LzSync* g, unsigned nblocks, uint64_t limit_ns) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = &g->gen;
+    const unsigned my = *gen;
+    __threadfence();
+    if (atomicAdd(&g->count, 1u) == nblocks - 1) {
+      atomicExch(&g->count, 0u);
+      __threadfence();
+      atomicAdd(&g->gen, 1u);
+    } else {
+      uint64_t t0;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (*gen == my) {
+        if (*(volatile int*)&g->err) break;
+        uint64_t t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) {
+          atomicExch(&g->err, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile int*)&g->err == 0;
+}
+
+// Sum of part[q * stride + c] over q = 0..G-1 by one warp, in a fixed order.
+__device__ __forceinline__ double lz_warp_colsum(const double* part, int G, int stride, int c, int lane) {
+  double s = 0.0;
+  for (int q = lane; q < G; q += 32) s += __ldcg(part + (int64_t)q * stride + c);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+#define LZ_THREADS 512
+__global__ void __launch_bounds__(LZ_THREADS) k_lanczos_cycle(
+    const int64_t* __restrict__ rp, const int* __restrict__ col, const double* __restrict__ aw, int n,
+    double* __restrict__ Vl, int64_t ld, int nlock, int j0, int m, int ncmax, double* __restrict__ part1,
+    double* __restrict__ part2, double* __restrict__ part3, double* __restrict__ ab, int* __restrict__ brk,
+    double btol, LzSync* __restrict__ gs, uint64_t limit_ns) {
+  extern __shared__ double lz_sm[];
+  const int G = gridDim.x, b = blockIdx.x;
+  const int r0 = (int)((int64_t)n * b / G), r1 = (int)((int64_t)n * (b + 1) / G), nr = r1 - r0;
+  const int rmax = (n + G - 1) / G;
+  double* ws = lz_sm;            // w on this block's rows
+  double* hs = lz_sm + rmax;     // projections, reduced
+  double* red = hs + ncmax;      // block reduction scratch [LZ_THREADS / 32]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double* Vp = Vl + (int64_t)nlock * ld;
+  for (int j = j0; j < m; ++j) {
+    const int nc = nlock + j + 1;
+    const double* x = Vp + (int64_t)j * ld;
+    // w = A v_j on the block's rows, a warp per row, four elements per lane
+    // in flight
+    for (int r = r0 + warp; r < r1; r += nw) {
+      const int64_t e0 = rp[r], e1 = rp[r + 1];
+      double s0 = 0.0, s1 = 0.0;
+      int64_t e = e0 + lane;
+      for (; e + 96 < e1; e += 128) {
+        const int c0 = col[e], c1 = col[e + 32], c2 = col[e + 64], c3 = col[e + 96];
+        const double w0 = aw[e], w1 = aw[e + 32], w2 = aw[e + 64], w3 = aw[e + 96];
+        s0 += w0 * __ldcg(x + c0);
+        s1 += w1 * __ldcg(x + c1);
+        s0 += w2 * __ldcg(x + c2);
+        s1 += w3 * __ldcg(x + c3);
+      }
+      for (; e < e1; e += 32) s0 += aw[e] * __ldcg(x + col[e]);
+      double sum = s0 + s1;
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) ws[r - r0] = sum;
+    }
+    __syncthreads();
+    // partial projections onto the nc columns over the block's rows
+    for (int c = warp; c < nc; c += nw) {
+      const double* vc = Vl + (int64_t)c * ld + r0;
+      double s = 0.0;
+      for (int i = lane; i < nr; i += 32) s += __ldcg(vc + i) * ws[i];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) part1[(int64_t)b * ncmax + c] = s;
+    }
+    if (!lz_grid_sync(gs, G, limit_ns)) break;
+    // h1, the first subtraction, and the partial projections of the new w
+    for (int c = warp; c < nc; c += nw) {
+      const double v = lz_warp_colsum(part1, G, ncmax, c, lane);
+      if (lane == 0) hs[c] = v;
+    }
+    __syncthreads();
+    const double a1 = hs[nlock + j];
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      double s = 0.0;
+      for (int c = 0; c < nc; ++c) s += __ldcg(Vl + (int64_t)c * ld + r0 + i) * hs[c];
+      ws[i] -= s;
+    }
+    __syncthreads();
+    for (int c = warp; c < nc; c += nw) {
+      const double* vc = Vl + (int64_t)c * ld + r0;
+      double s = 0.0;
+      for (int i = lane; i < nr; i += 32) s += __ldcg(vc + i) * ws[i];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) part2[(int64_t)b * ncmax + c] = s;
+    }
+    if (!lz_grid_sync(gs, G, limit_ns)) break;
+    // h2, the second subtraction, the partial |w|^2
+    for (int c = warp; c < nc; c += nw) {
+      const double v = lz_warp_colsum(part2, G, ncmax, c, lane);
+      if (lane == 0) hs[c] = v;
+    }
+    __syncthreads();
+    const double a2 = hs[nlock + j];
+    double q = 0.0;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      double s = 0.0;
+      for (int c = 0; c < nc; ++c) s += __ldcg(Vl + (int64_t)c * ld + r0 + i) * hs[c];
+      const double wi = ws[i] - s;
+      ws[i] = wi;
+      q += wi * wi;
+    }
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if (lane == 0) red[warp] = q;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int x2 = 0; x2 < nw; ++x2) t += red[x2];
+      part3[b] = t;
+    }
+    if (!lz_grid_sync(gs, G, limit_ns)) break;
+    // alpha_j, beta_j, breakdown, v_{j+1}
+    if (warp == 0) {
+      const double v = lz_warp_colsum(part3, G, 1, 0, lane);
+      if (lane == 0) red[0] = v;
+    }
+    __syncthreads();
+    const double alpha = a1 + a2;
+    const double beta = sqrt(fmax(red[0], 0.0));
+    const bool bk = beta <= btol * fmax(fabs(alpha), 1.0);
+    if (b == 0 && threadIdx.x == 0) {
+      ab[j] = alpha;
+      ab[m + j] = beta;
+      brk[j] = bk ? 1 : 0;
+    }
+    double* vn = Vp + (int64_t)(j + 1) * ld + r0;
+    const double inv = 1.0 / beta;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) vn[i] = bk ? 0.0 : ws[i] * inv;
+    if (!lz_grid_sync(gs, G, limit_ns)) break;
+  }
+}
+
 // X[:, 0:nout] = V[:, 0:m] * Y (Y: m x nout, column-major on device). One
 // thread per row and GV_CB output columns per block (grid.y); Y is staged in
 // shared memory GV_JT rows at a time, so every V element is read once per
@@ -554,6 +736,33 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   MDS_TRY(Yd.alloc(ctx, sizeof(double) * (size_t)m * m));
   MDS_TRY(tmp.alloc(ctx, sizeof(double) * (size_t)n * m));
   DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx);
+  // The steps of a cycle as one cooperative launch (k_lanczos_cycle): two
+  // blocks per SM when they fit, rows split evenly; each block keeps w on
+  // its rows in shared memory. Beyond that size the steps run as the
+  // separate kernels below, replayed from a CUDA graph.
+  const int ncmax = nlock + m + 1;
+  int lz_grid = 0;
+  size_t lz_smem = 0;
+  DevBuf lz_p1(ctx), lz_p2(ctx), lz_p3(ctx), lz_sync(ctx);
+  for (int per_sm = 2; per_sm >= 1 && !lz_grid; --per_sm) {
+    const int G = per_sm * ctx->num_sms;
+    const size_t smem = sizeof(double) * ((size_t)(n + G - 1) / G + ncmax + LZ_THREADS / 32);
+    if (smem > 200 * 1024) continue;
+    if (smem > 48 * 1024)
+      MDS_CUDA(ctx, cudaFuncSetAttribute(k_lanczos_cycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nb = 0;
+    MDS_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lanczos_cycle, LZ_THREADS, smem));
+    if (nb >= per_sm) {
+      lz_grid = G;
+      lz_smem = smem;
+    }
+  }
+  if (lz_grid) {
+    MDS_TRY(lz_p1.alloc(ctx, sizeof(double) * (size_t)lz_grid * ncmax));
+    MDS_TRY(lz_p2.alloc(ctx, sizeof(double) * (size_t)lz_grid * ncmax));
+    MDS_TRY(lz_p3.alloc(ctx, sizeof(double) * (size_t)lz_grid));
+    MDS_TRY(lz_sync.alloc(ctx, sizeof(LzSync)));
+  }
   // step graphs by first step of the cycle; destroyed on every return path
   struct Graphs : std::map<int, cudaGraphExec_t> {
     ~Graphs() {
@@ -633,11 +842,35 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
     // (invariant subspace, beta_j ~ 0) found then restarts the steps after
     // it from a fresh direction orthogonal to the basis.
     for (int j0 = k; j0 < m;) {
+      if (lz_grid) {
+        // one cooperative launch for the steps j0..m-1
+        const int64_t* a_rp = op.rp.as<int64_t>();
+        const int* a_col = op.col.as<int>();
+        const double* a_w = op.w.as<double>();
+        int a_n = n, a_nlock = nlock, a_j0 = j0, a_m = m, a_nc = ncmax;
+        int64_t a_ld = ld;
+        double* a_V = Vl;
+        double* a_p1 = lz_p1.as<double>();
+        double* a_p2 = lz_p2.as<double>();
+        double* a_p3 = lz_p3.as<double>();
+        double* a_ab = ab.as<double>();
+        int* a_brk = brk.as<int>();
+        double a_btol = eps * 10.0;
+        LzSync* a_sync = lz_sync.as<LzSync>();
+        uint64_t a_limit = 1000000000ull;  // 1 s per barrier wait
+        void* args[] = {&a_rp, &a_col, &a_w, &a_n, &a_V, &a_ld, &a_nlock, &a_j0, &a_m, &a_nc,
+                        &a_p1, &a_p2, &a_p3, &a_ab, &a_brk, &a_btol, &a_sync, &a_limit};
+        MDS_CUDA(ctx, cudaMemsetAsync(lz_sync.p, 0, sizeof(LzSync), s));
+        MDS_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_lanczos_cycle, dim3(lz_grid), dim3(LZ_THREADS),
+                                                  args, lz_smem, s));
+        ctx->stats.launches++;
+        out.matvecs += m - j0;
+      }
       // The steps j0..m-1 are one CUDA graph, captured the first time a cycle
       // starts at j0 (every pointer and size is fixed within this call) and
       // replayed afterwards: one launch instead of ~11 per step.
-      auto git = graphs.find(j0);
-      if (git == graphs.end()) {
+      auto git = lz_grid ? graphs.end() : graphs.find(j0);
+      if (!lz_grid && git == graphs.end()) {
         MDS_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         for (int j = j0; j < m; ++j) {
           const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
@@ -666,15 +899,20 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
         if (ce != cudaSuccess) return mds_fail(ctx, MDS_ERR_CUDA, "Lanczos step graph: %s", cudaGetErrorString(ce));
         git = graphs.emplace(j0, ge).first;
       }
-      MDS_CUDA(ctx, cudaGraphLaunch(git->second, s));
-      out.matvecs += m - j0;
-      ctx->stats.launches += 12 * (m - j0);
+      if (!lz_grid) {
+        MDS_CUDA(ctx, cudaGraphLaunch(git->second, s));
+        out.matvecs += m - j0;
+        ctx->stats.launches += 12 * (m - j0);
+      }
       MDS_CUDA(ctx, cudaGetLastError());
       std::vector<double> hab(2 * m);
       std::vector<int> hbrk(m);
+      LzSync hsync{};
       MDS_CUDA(ctx, cudaMemcpyAsync(hab.data(), ab.p, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, s));
       MDS_CUDA(ctx, cudaMemcpyAsync(hbrk.data(), brk.p, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+      if (lz_grid) MDS_CUDA(ctx, cudaMemcpyAsync(&hsync, lz_sync.p, sizeof(LzSync), cudaMemcpyDeviceToHost, s));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      if (hsync.err) return mds_fail(ctx, MDS_ERR_TIMEOUT, "Lanczos steps: a grid barrier wait timed out");
       int jb = -1;
       for (int j = j0; j < m; ++j) {
         alpha[j] = hab[j];
