@@ -24,9 +24,9 @@ candidate screen, fused top-k, exact recheck and output.
          |a_i|^2 + |a_j|^2 (which the guard coefficient must exceed) and the
          number of bounds found above their exact value (rows so found are
          finished by the wider FP32 screen or exactly)
-  tc_vs_fp32  screen-stage times of the tensor-core screen with tile
-         skipping switched off (every tile computed) and of the FP32
-         CUDA-core screen (every tile computed), on this workload
+  tc_vs_fp32  screen-stage times of the tensor-core screen and of the FP32
+         CUDA-core screen on this workload, both with tile skipping switched
+         off (every tile computed) and both skipping as they do by default
   parity  after the timed loops, 256 rows of the timed run's output (and of
          the FP32 path's) against the FP64 oracle (oracle/): largest distance
          error, index agreement, swaps inside tie bands of 1e-4 Angstrom
@@ -83,8 +83,9 @@ def parse():
                    help="N > 1: every rank runs the whole workload (default: row shards)")
     p.add_argument("--serve", action="store_true",
                    help="Nystrom serving benchmark (50,000 landmarks x 304 atoms, k=50, nev=10)")
-    p.add_argument("--serve-seconds", type=float, default=8.0)
-    p.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate, requests/s")
+    p.add_argument("--serve-seconds", type=float, default=6.0, help="arrivals per rate, seconds")
+    p.add_argument("--serve-rates", default="50,200,500,1000,2000", help="Poisson arrival rates, requests/s")
+    p.add_argument("--serve-max-requests", type=int, default=3000)
     p.add_argument("--pipeline", choices=["small", "scale", "euclid", "sparse"],
                    help="per-stage wall time of a whole pipeline: small = 2,000 x 304 frames (parity vs the oracle), "
                         "scale = 100,000 x 304 (kNN k=64, sysparse, Lanczos nev=20 ncv=60 tol=1e-8), "
@@ -100,8 +101,11 @@ def parse():
 def run_serve(args):
     """Serving: landmarks stay resident; requests of 1-4096 frames (log-uniform
     sizes, 90% from the basin generator, 10% off-manifold) arrive as a Poisson
-    stream; latency = submit -> results. The plain path serves one request at a
-    time (one slot, no batching, no CUDA graphs) on the same arrival stream."""
+    stream; latency = submit -> results. Swept over the arrival rates of
+    --serve-rates (each rate: up to --serve-seconds of arrivals, at most
+    --serve-max-requests requests). The plain path serves one request at a
+    time (one slot, no batching, no CUDA graphs): every request's service time
+    is measured alone once, and each rate's arrivals are queued FIFO on them."""
     import numpy as np
     import threading
 
@@ -114,21 +118,31 @@ def run_serve(args):
     with Context(0) as c:
         d, _ = c.knn_rms(land, None, m, k, precision=args.precision)
     sigma = float(np.median(d))
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    nmax = max(8, min(args.serve_max_requests, int(max(rates) * args.serve_seconds)))
     rng = np.random.default_rng(SEED + 6)
-    nreq = max(8, int(args.serve_rate * args.serve_seconds))
-    sizes = np.exp(rng.uniform(0, np.log(4096), nreq)).astype(int).clip(1, 4096)
-    gaps = rng.exponential(1.0 / args.serve_rate, nreq)
+    sizes = np.exp(rng.uniform(0, np.log(4096), nmax)).astype(int).clip(1, 4096)
     pool = synth.trajectory(8192, natoms, seed=SEED + 7, basins=16, dwell=500.0, off_manifold=0.1, off_sigma=0.3)
-    starts = rng.integers(0, 8192 - 4096, nreq)
+    starts = rng.integers(0, 8192 - 4096, nmax)
+    unit_gaps = rng.exponential(1.0, nmax)  # scaled by 1/rate
 
-    def run(batched):
-        srv = Server(land, m, k=k, sigma=sigma, nev=nev, precision=args.precision, max_batch_frames=4096)
-        # warm every size bucket of every slot (graph capture happens on first use)
-        for b in (1, 2, 4, 8, 16, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096):
-            for t in [srv.submit(pool[:b]) for _ in range(srv.stats()["slots"])]:
-                srv.wait(t)
+    def nreq_of(rate):
+        return max(8, min(nmax, int(rate * args.serve_seconds)))
+
+    srv = Server(land, m, k=k, sigma=sigma, nev=nev, precision=args.precision, max_batch_frames=4096)
+    # warm every size bucket of every slot (graph capture happens on first use)
+    for bsz in (1, 2, 4, 8, 16, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096):
+        for t in [srv.submit(pool[:bsz]) for _ in range(srv.stats()["slots"])]:
+            srv.wait(t)
+    model = srv.stats()
+
+    def run_batched(rate):
+        nreq = nreq_of(rate)
+        gaps = unit_gaps[:nreq] / rate
+        st0 = srv.stats()
         lat, done = [None] * nreq, threading.Event()
         tickets = [None] * nreq
+        bfr = [0] * nreq
 
         def waiter():
             for j in range(nreq):
@@ -136,6 +150,7 @@ def run_serve(args):
                     time.sleep(1e-4)
                 _, _, _, info = srv.wait(tickets[j])
                 lat[j] = info["total_ms"]
+                bfr[j] = info["batch_frames"]
             done.set()
 
         th = threading.Thread(target=waiter)
@@ -151,44 +166,47 @@ def run_serve(args):
         wall = time.perf_counter() - t0
         th.join()
         st = srv.stats()
-        srv.close()
         lat = np.array(lat)
-        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "mean_ms": float(lat.mean()), "queries_per_s": float(sizes.sum() / wall),
-                "requests_per_s": float(nreq / wall), "batches": st["batches"],
-                "graph_launches": st["graph_launches"], "slots": st["slots"], "rows_flagged": st["rows_flagged"],
-                "model_knn_ms": st["model_knn_ms"], "model_decomp_ms": st["model_decomp_ms"]}
+        return {"requests": nreq, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "queries_per_s": float(sizes[:nreq].sum() / wall),
+                "requests_per_s": float(nreq / wall), "offered_queries_per_s": float(sizes[:nreq].sum() / gaps.sum()),
+                "batches": st["batches"] - st0["batches"],
+                "shared_batch_fraction": float(np.mean(np.array(bfr) > sizes[:nreq])),
+                "rows_flagged": st["rows_flagged"] - st0["rows_flagged"]}
 
-    def run_plain():
-        # one request at a time, no batching and no graphs: measure each
-        # request's service time alone, then queue them FIFO on the same
-        # Poisson arrival times (latency = finish - arrival)
-        srv = Server(land, m, k=k, sigma=sigma, nev=nev, precision=args.precision, max_batch_frames=4096,
-                     slots=1, use_graphs=False)
-        srv.wait(srv.submit(pool[:4096]))
-        svc = np.zeros(nreq)
-        for j in range(nreq):
-            t0 = time.perf_counter()
-            srv.wait(srv.submit(pool[starts[j]:starts[j] + sizes[j]]))
-            svc[j] = time.perf_counter() - t0
-        srv.close()
-        arr = np.cumsum(gaps)
+    # plain path: service time of every request alone, once
+    plain = Server(land, m, k=k, sigma=sigma, nev=nev, precision=args.precision, max_batch_frames=4096,
+                   slots=1, use_graphs=False)
+    plain.wait(plain.submit(pool[:4096]))
+    svc = np.zeros(nmax)
+    for j in range(nmax):
+        t0 = time.perf_counter()
+        plain.wait(plain.submit(pool[starts[j]:starts[j] + sizes[j]]))
+        svc[j] = time.perf_counter() - t0
+    plain.close()
+
+    def run_plain(rate):
+        nreq = nreq_of(rate)
+        arr = np.cumsum(unit_gaps[:nreq] / rate)
         fin, lat = 0.0, np.zeros(nreq)
         for j in range(nreq):
             fin = max(arr[j], fin) + svc[j]
             lat[j] = (fin - arr[j]) * 1e3
-        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "mean_ms": float(lat.mean()), "queries_per_s": float(sizes.sum() / max(fin, arr[-1])),
-                "service_ms_mean": float(svc.mean() * 1e3)}
+        return {"requests": nreq, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "queries_per_s": float(sizes[:nreq].sum() / max(fin, arr[-1])),
+                "service_ms_mean": float(svc[:nreq].mean() * 1e3)}
 
-    res_b = run(True)
-    res_p = run_plain()
-    out = {"metric": "Nystrom serving latency", "unit": "ms", "higher_is_better": False, "value": res_b["p99_ms"],
-           "data": "synthetic", "dtype": args.precision,
+    sweep = []
+    for rate in rates:
+        sweep.append({"rate_req_per_s": rate, "batched": run_batched(rate), "plain_per_request": run_plain(rate)})
+    srv.close()
+    out = {"metric": "Nystrom serving latency", "unit": "ms", "higher_is_better": False,
+           "value": sweep[0]["batched"]["p99_ms"], "data": "synthetic", "dtype": args.precision,
            "config": {"workload": f"Nystrom serving: {n_land} landmarks x {natoms} atoms, k={k}, nev={nev}, "
-                                  f"requests of 1-4096 frames (log-uniform), Poisson {args.serve_rate}/s, "
-                                  f"10% off-manifold", "requests": nreq, "sigma_A": sigma},
-           "batched": res_b, "plain_per_request": res_p}
+                                  f"requests of 1-4096 frames (log-uniform), Poisson arrivals, 10% off-manifold",
+                      "rates_req_per_s": rates, "sigma_A": sigma, "slots": model["slots"],
+                      "model_knn_ms": model["model_knn_ms"], "model_decomp_ms": model["model_decomp_ms"]},
+           "sweep": sweep}
     print(json.dumps(out))
     return 0
 
@@ -706,15 +724,20 @@ def main():
             return sts
 
         tcd = screen_runs(args.precision, False, 3)
-        fpd = screen_runs("fp32", True, 2)
+        fpd = screen_runs("fp32", False, 1)
+        fps = screen_runs("fp32", True, 3)
         d_fp32, i_fp32 = out[0].cpu().numpy(), out[1].cpu().numpy()
         cmp = {"tc_dense_screen_ms": med("screen_ms", tcd), "tc_dense_screen_pairs": med("screen_pairs", tcd),
-               "fp32_dense_screen_ms": med("screen_ms", fpd),
-               "tc_skip_screen_ms": scr,
+               "fp32_dense_screen_ms": med("screen_ms", fpd), "fp32_dense_screen_pairs": med("screen_pairs", fpd),
+               "tc_skip_screen_ms": scr, "tc_skip_screen_pairs": computed,
+               "fp32_skip_screen_ms": med("screen_ms", fps), "fp32_skip_screen_pairs": med("screen_pairs", fps),
                "tc_vs_fp32_dense": med("screen_ms", fpd) / med("screen_ms", tcd),
-               "tc_call_ms": med("total_ms"), "fp32_call_ms": med("total_ms", fpd),
-               "tc_vs_fp32_call": med("total_ms", fpd) / med("total_ms"),
-               "note": "screen stage times by CUDA events; the FP32 screen computes every tile"}
+               "tc_vs_fp32_skip": med("screen_ms", fps) / scr,
+               "tc_call_ms": med("total_ms"), "fp32_call_ms": med("total_ms", fps),
+               "tc_vs_fp32_call": med("total_ms", fps) / med("total_ms"),
+               "note": "screen stage times by CUDA events (pivot pass included when skipping); dense = every "
+                       "tile computed (MDS_NO_SKIP), skip = the default tile skipping of each screen; "
+                       "*_pairs: frame pairs each screen computed"}
         res["tc_vs_fp32"] = cmp
     # parity of the timed run: sampled rows against the FP64 oracle
     if rank == 0 and not args.no_parity:

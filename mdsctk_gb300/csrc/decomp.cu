@@ -433,6 +433,70 @@ __device__ __forceinline__ double lz_warp_colsum(const double* part, int G, int 
 }
 
 #define LZ_THREADS 512
+#define LZ_WARPS (LZ_THREADS / 32)
+#define LZ_U 8  // basis columns per unrolled group: loads in flight per thread
+
+// Partial projections of u (the block's rows, in shared memory) onto the
+// columns 0..nc-1 of V over the block's rows: a thread per row, LZ_U columns'
+// loads in flight at a time, each product summed over the warp's 32 rows by
+// shuffles and added to the warp's own partial wp[warp][c] (so every sum has
+// a fixed order), then wp summed over the warps into out[c].
+__device__ __forceinline__ void lz_block_dots(const double* __restrict__ V, int64_t ld, int r0, int nr, int nc,
+                                              const double* __restrict__ u, double* __restrict__ wp,
+                                              double* __restrict__ out, int ncmax) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = lane; c < nc; c += 32) wp[warp * ncmax + c] = 0.0;
+  __syncwarp();
+  for (int i0 = 0; i0 < nr; i0 += LZ_THREADS) {
+    const int i = i0 + threadIdx.x;
+    const bool valid = i < nr;
+    const double ui = valid ? u[i] : 0.0;
+    const double* vi = V + r0 + (valid ? i : 0);
+    for (int c0 = 0; c0 < nc; c0 += LZ_U) {
+      double p[LZ_U];
+#pragma unroll
+      for (int x = 0; x < LZ_U; ++x) p[x] = (valid && c0 + x < nc) ? __ldcg(vi + (int64_t)(c0 + x) * ld) : 0.0;
+#pragma unroll
+      for (int x = 0; x < LZ_U; ++x) {
+        double q = p[x] * ui;
+        for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+        if (lane == 0 && c0 + x < nc) wp[warp * ncmax + c0 + x] += q;
+      }
+    }
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nc; c += LZ_THREADS) {
+    double t = 0.0;
+    for (int w = 0; w < LZ_WARPS; ++w) t += wp[w * ncmax + c];
+    out[c] = t;
+  }
+}
+
+// u[i] -= sum_c V[i, c] h[c] on the block's rows (a thread per row, LZ_U
+// loads in flight); returns this thread's sum of the new u[i]^2.
+__device__ __forceinline__ double lz_block_sub(const double* __restrict__ V, int64_t ld, int r0, int nr, int nc,
+                                               const double* __restrict__ h, double* __restrict__ u) {
+  double q = 0.0;
+  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) {
+    const double* vi = V + r0 + i;
+    double s0 = 0.0, s1 = 0.0;
+    for (int c0 = 0; c0 < nc; c0 += LZ_U) {
+      double p[LZ_U];
+#pragma unroll
+      for (int x = 0; x < LZ_U; ++x) p[x] = (c0 + x < nc) ? __ldcg(vi + (int64_t)(c0 + x) * ld) : 0.0;
+#pragma unroll
+      for (int x = 0; x < LZ_U; x += 2) {
+        s0 += p[x] * ((c0 + x < nc) ? h[c0 + x] : 0.0);
+        s1 += p[x + 1] * ((c0 + x + 1 < nc) ? h[c0 + x + 1] : 0.0);
+      }
+    }
+    const double ui = u[i] - (s0 + s1);
+    u[i] = ui;
+    q += ui * ui;
+  }
+  return q;
+}
+
 __global__ void __launch_bounds__(LZ_THREADS) k_lanczos_cycle(
     const int64_t* __restrict__ rp, const int* __restrict__ col, const double* __restrict__ aw, int n,
     double* __restrict__ Vl, int64_t ld, int nlock, int j0, int m, int ncmax, double* __restrict__ part1,
@@ -442,85 +506,71 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lanczos_cycle(
   const int G = gridDim.x, b = blockIdx.x;
   const int r0 = (int)((int64_t)n * b / G), r1 = (int)((int64_t)n * (b + 1) / G), nr = r1 - r0;
   const int rmax = (n + G - 1) / G;
-  double* ws = lz_sm;            // w on this block's rows
-  double* hs = lz_sm + rmax;     // projections, reduced
-  double* red = hs + ncmax;      // block reduction scratch [LZ_THREADS / 32]
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double* ws = lz_sm;                   // w on this block's rows
+  double* hs = ws + rmax;               // projections, reduced over the grid
+  double* hb = hs + ncmax;              // the block's partial projections
+  double* wp = hb + ncmax;              // per-warp partials [LZ_WARPS][ncmax]
+  double* red = wp + LZ_WARPS * ncmax;  // [LZ_WARPS]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double* Vp = Vl + (int64_t)nlock * ld;
   for (int j = j0; j < m; ++j) {
     const int nc = nlock + j + 1;
     const double* x = Vp + (int64_t)j * ld;
-    // w = A v_j on the block's rows, a warp per row, four elements per lane
-    // in flight
-    for (int r = r0 + warp; r < r1; r += nw) {
-      const int64_t e0 = rp[r], e1 = rp[r + 1];
-      double s0 = 0.0, s1 = 0.0;
-      int64_t e = e0 + lane;
-      for (; e + 96 < e1; e += 128) {
-        const int c0 = col[e], c1 = col[e + 32], c2 = col[e + 64], c3 = col[e + 96];
-        const double w0 = aw[e], w1 = aw[e + 32], w2 = aw[e + 64], w3 = aw[e + 96];
-        s0 += w0 * __ldcg(x + c0);
-        s1 += w1 * __ldcg(x + c1);
-        s0 += w2 * __ldcg(x + c2);
-        s1 += w3 * __ldcg(x + c3);
+    // w = A v_j on the block's rows: two rows per warp, a half-warp each,
+    // four elements per lane in flight
+    {
+      const int half = lane >> 4, hl = lane & 15;
+      for (int rb = r0 + 2 * warp; rb < r1; rb += 2 * LZ_WARPS) {
+        const int r = rb + half;
+        double s0 = 0.0, s1 = 0.0;
+        if (r < r1) {
+          const int64_t e1 = rp[r + 1];
+          int64_t e = rp[r] + hl;
+          for (; e + 48 < e1; e += 64) {
+            const int c0 = col[e], c1 = col[e + 16], c2 = col[e + 32], c3 = col[e + 48];
+            const double w0 = aw[e], w1 = aw[e + 16], w2 = aw[e + 32], w3 = aw[e + 48];
+            s0 += w0 * __ldcg(x + c0);
+            s1 += w1 * __ldcg(x + c1);
+            s0 += w2 * __ldcg(x + c2);
+            s1 += w3 * __ldcg(x + c3);
+          }
+          for (; e < e1; e += 16) s0 += aw[e] * __ldcg(x + col[e]);
+        }
+        double sum = s0 + s1;
+        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);  // within each half
+        if (hl == 0 && r < r1) ws[r - r0] = sum;
       }
-      for (; e < e1; e += 32) s0 += aw[e] * __ldcg(x + col[e]);
-      double sum = s0 + s1;
-      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      if (lane == 0) ws[r - r0] = sum;
     }
     __syncthreads();
-    // partial projections onto the nc columns over the block's rows
-    for (int c = warp; c < nc; c += nw) {
-      const double* vc = Vl + (int64_t)c * ld + r0;
-      double s = 0.0;
-      for (int i = lane; i < nr; i += 32) s += __ldcg(vc + i) * ws[i];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) part1[(int64_t)b * ncmax + c] = s;
-    }
+    lz_block_dots(Vl, ld, r0, nr, nc, ws, wp, hb, ncmax);
+    for (int c = threadIdx.x; c < nc; c += LZ_THREADS) part1[(int64_t)b * ncmax + c] = hb[c];
     if (!lz_grid_sync(gs, G, limit_ns)) break;
-    // h1, the first subtraction, and the partial projections of the new w
-    for (int c = warp; c < nc; c += nw) {
+    // h1; the first subtraction; the projections of the new w
+    for (int c = warp; c < nc; c += LZ_WARPS) {
       const double v = lz_warp_colsum(part1, G, ncmax, c, lane);
       if (lane == 0) hs[c] = v;
     }
     __syncthreads();
     const double a1 = hs[nlock + j];
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      double s = 0.0;
-      for (int c = 0; c < nc; ++c) s += __ldcg(Vl + (int64_t)c * ld + r0 + i) * hs[c];
-      ws[i] -= s;
-    }
+    lz_block_sub(Vl, ld, r0, nr, nc, hs, ws);
     __syncthreads();
-    for (int c = warp; c < nc; c += nw) {
-      const double* vc = Vl + (int64_t)c * ld + r0;
-      double s = 0.0;
-      for (int i = lane; i < nr; i += 32) s += __ldcg(vc + i) * ws[i];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) part2[(int64_t)b * ncmax + c] = s;
-    }
+    lz_block_dots(Vl, ld, r0, nr, nc, ws, wp, hb, ncmax);
+    for (int c = threadIdx.x; c < nc; c += LZ_THREADS) part2[(int64_t)b * ncmax + c] = hb[c];
     if (!lz_grid_sync(gs, G, limit_ns)) break;
-    // h2, the second subtraction, the partial |w|^2
-    for (int c = warp; c < nc; c += nw) {
+    // h2; the second subtraction with |w|^2
+    for (int c = warp; c < nc; c += LZ_WARPS) {
       const double v = lz_warp_colsum(part2, G, ncmax, c, lane);
       if (lane == 0) hs[c] = v;
     }
     __syncthreads();
     const double a2 = hs[nlock + j];
-    double q = 0.0;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      double s = 0.0;
-      for (int c = 0; c < nc; ++c) s += __ldcg(Vl + (int64_t)c * ld + r0 + i) * hs[c];
-      const double wi = ws[i] - s;
-      ws[i] = wi;
-      q += wi * wi;
-    }
+    double q = lz_block_sub(Vl, ld, r0, nr, nc, hs, ws);
     for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
     if (lane == 0) red[warp] = q;
     __syncthreads();
     if (threadIdx.x == 0) {
       double t = 0.0;
-      for (int x2 = 0; x2 < nw; ++x2) t += red[x2];
+      for (int w = 0; w < LZ_WARPS; ++w) t += red[w];
       part3[b] = t;
     }
     if (!lz_grid_sync(gs, G, limit_ns)) break;
@@ -540,7 +590,7 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lanczos_cycle(
     }
     double* vn = Vp + (int64_t)(j + 1) * ld + r0;
     const double inv = 1.0 / beta;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) vn[i] = bk ? 0.0 : ws[i] * inv;
+    for (int i = threadIdx.x; i < nr; i += LZ_THREADS) vn[i] = bk ? 0.0 : ws[i] * inv;
     if (!lz_grid_sync(gs, G, limit_ns)) break;
   }
 }
@@ -746,7 +796,7 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   DevBuf lz_p1(ctx), lz_p2(ctx), lz_p3(ctx), lz_sync(ctx);
   for (int per_sm = 2; per_sm >= 1 && !lz_grid; --per_sm) {
     const int G = per_sm * ctx->num_sms;
-    const size_t smem = sizeof(double) * ((size_t)(n + G - 1) / G + ncmax + LZ_THREADS / 32);
+    const size_t smem = sizeof(double) * ((size_t)(n + G - 1) / G + (2 + LZ_WARPS) * (size_t)ncmax + LZ_WARPS);
     if (smem > 200 * 1024) continue;
     if (smem > 48 * 1024)
       MDS_CUDA(ctx, cudaFuncSetAttribute(k_lanczos_cycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

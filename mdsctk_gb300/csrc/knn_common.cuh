@@ -110,9 +110,32 @@ int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, cons
                 int* bad = nullptr, int fbase = 0);
 int build_template(mds_ctx* ctx, const float* dY0, int Ap, int natoms, bool nofit, std::vector<double>& mu,
                    double M0[9]);
+// Frames per row tile (40: 128 MMA rows, 10 frames per 32-lane quarter) and
+// per column tile (80: 240 MMA columns) of the tensor-core screen; the tile
+// skipping data (pivots, radii, row-tile bounds) is laid out on these tiles.
+#define TC_FR_M 40
+#define TC_FR_N 80
+
+// Optional parts of the FP32 screen (k_screen_fp32, knn_rms.cu): tile
+// skipping with the tensor-core screen's row-tile pivots (pivlb [nR][nfit]
+// lower bounds of RMSD to the pivots, prad [2 nC] radii of the 80-frame
+// column tiles, rowlo [nR][nC]), shared row thresholds, thresholds from the
+// (k+1)-th bound, outward column order, and the dense pivot pass.
+struct Fp32ScreenExtra {
+  const float* pivlb = nullptr;
+  const float* prad = nullptr;
+  const float* rowlo = nullptr;
+  int nR = 0, nC = 0, nfit = 0;
+  float* rowthr = nullptr;
+  const float* nmax = nullptr;
+  int k1 = 0;
+  int diag = 0;
+  float* dense = nullptr;  // [nref][nrows]
+  unsigned long long* ntiles = nullptr;  // tiles computed (32 x 64 frames each)
+};
 int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* recf,
                        const float* recr, int nrows, const int* rowlist, int Kp, int nseg, uint64_t* cand,
-                       int* cand_n);
+                       int* cand_n, const Fp32ScreenExtra* extra = nullptr);
 // Exact recheck from the superposed deviations (Af/Ar [n][3][Ap]) and the
 // template mu [3][Ap] (knn_rms.cu).
 // Ur: the reference frames' U as written by launch_prep (unused with nofit).

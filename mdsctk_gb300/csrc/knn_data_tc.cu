@@ -462,9 +462,9 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         if (gg >= nfit) break;
         const int c0 = S->cnt2[rr][0], c1 = S->cnt2[rr][1];
         const bool over = c0 + c1 > Kp && (c0 > lcap - 64 || c1 > lcap - 64);
-        // (the first threshold of a row comes from its k1-th key as soon as
-        // those arrive, unless a seeded shared threshold already bounds it)
-        const bool first = S->thr[rr] == INF && c0 + c1 >= k1 && !(__ldcg(rowthr + gg) < INF);
+        // (the row's first own threshold comes from its k1-th key as soon as
+        // those arrive: tighter than the seeded shared one, it cuts appends)
+        const bool first = S->thr[rr] == INF && c0 + c1 >= k1;
         if (!over && !first) continue;
         const bool cut = c0 + c1 > Kp;
         float tk1 = INF;

@@ -363,11 +363,42 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
+// Column tiles of a segment [t0, t1) visited outward from tile td (td,
+// td+1, td-1, ...): for a set screened against itself td holds the row
+// tile's own frames, so a row's threshold tightens early.
+__device__ __forceinline__ int sc_tile_order(int i, int t0, int t1, int td) {
+  const int L = td - t0, Rn = t1 - 1 - td, m = min(L, Rn);
+  if (i == 0) return td;
+  if (i <= 2 * m) return (i & 1) ? td + (i + 1) / 2 : td - i / 2;
+  const int j = i - 2 * m;
+  return (Rn > L) ? td + m + j : td - m - j;
+}
+
 __global__ void __launch_bounds__(SC_THREADS, 1)
 k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
               const float* __restrict__ recf, const float* __restrict__ recr, int nrows,
               const int* __restrict__ rowlist, int Nr, int Ap, int nofit, float guard, int Kp,
-              int nseg, uint64_t* __restrict__ cand, int* __restrict__ cand_n) {
+              int nseg, uint64_t* __restrict__ cand, int* __restrict__ cand_n, const Fp32ScreenExtra ex) {
+  // Tile skipping (ex.pivlb != null, a set screened against itself): the
+  // tensor-core screen's row-tile pivots (the middle frame of every 40-frame
+  // tile) and 80-frame column tiles. RMSD is a metric, so for row i and any
+  // frame j of 80-frame tile T, RMSD(i, j) >= max over the pivots p of T's
+  // two row tiles of lb(i, p) - r_T(p), and >= rowlo[R(i)][T]. A 64-frame
+  // tile of this screen overlaps one or two 80-frame tiles; the smaller of
+  // their bounds holds for all its frames. The tile is skipped when every
+  // row has that bound L > 0 with L^2 above its threshold.
+  // Shared row thresholds (ex.rowthr): each compaction lowers rowthr[row]
+  // (atomicMin on the float's bits, values >= 0), and every segment appends
+  // only below min(own threshold, rowthr) and skips by it.
+  // Thresholds from the (k+1)-th bound (ex.nmax): a bound b is the screen
+  // value minus the guard g (|a_i|^2 + |a_j|^2), and the screen value is
+  // within the guard of the exact RMSD^2, so the row's (k+1)-th exact value
+  // is at most b_(k+1) + 2 g (|a_i|^2 + nmax); a compaction sets the row
+  // threshold to the smaller of that and the K'-th bound, and the first one
+  // runs as soon as k1 keys have arrived.
+  // Dense mode (ex.dense != null; the pivot pass of this screen): every
+  // pair's lower bound of RMSD (sqrt of the bound of RMSD^2) is written to
+  // dense[j][i] (j: reference frame); no lists.
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* sfit = reinterpret_cast<float*>(smem_raw);                 // [2][32*98]
   float* sref = sfit + 2 * SC_TM * SC_FS;                           // [2][64*98]
@@ -375,6 +406,7 @@ k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
   int* scnt = reinterpret_cast<int*>(scol + SC_TN * MDS_REC);       // [32]
   float* sthr = reinterpret_cast<float*>(scnt + SC_TM);             // [32]
   uint64_t* pool = reinterpret_cast<uint64_t*>(sthr + SC_TM);       // [32][P2]
+  __shared__ float sgthr[SC_TM];  // the rows' shared thresholds, read per tile
   // a row's pool holds its K' best plus one tile of new entries; its stride
   // is the power of two the sort works on
   const int P2 = next_pow2(Kp + SC_TN);
@@ -387,6 +419,9 @@ k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
   // column segment [c0, c1) in whole tiles
   const int ntiles = (Nr + SC_TN - 1) / SC_TN;
   const int t0 = (int)((int64_t)ntiles * seg / nseg), t1 = (int)((int64_t)ntiles * (seg + 1) / nseg);
+  const int td = ex.diag ? min(max((row0 + SC_TM / 2) / SC_TN, t0), max(t1 - 1, t0)) : t0;
+  const bool dense = ex.dense != nullptr;
+  const float INF = __int_as_float(0x7f800000);
 
   int grow[2];
   float rrec[2][MDS_REC];
@@ -397,7 +432,7 @@ k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
   }
   if (tid < SC_TM) {
     scnt[tid] = 0;
-    sthr[tid] = __int_as_float(0x7f800000);
+    sthr[tid] = INF;
   }
   const int nchunks = Ap / SC_KC;
 
@@ -420,9 +455,41 @@ k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
     }
   };
 
-  for (int tile = t0; tile < t1; ++tile) {
-    // column records of this tile
+  for (int ti = 0; ti < t1 - t0; ++ti) {
+    const int tile = ex.diag ? sc_tile_order(ti, t0, t1, td) : t0 + ti;
     __syncthreads();
+    // the rows' shared thresholds now (they only decrease)
+    if (tid < SC_TM) {
+      const int lr = row0 + tid;
+      const int g = (lr < nrows) ? (rowlist ? rowlist[lr] : lr) : -1;
+      sgthr[tid] = (ex.rowthr && g >= 0) ? __ldcg(ex.rowthr + g) : INF;
+    }
+    if (ex.pivlb && !dense) {
+      // skip test: one lane per row
+      bool can = true;
+      if (tid < SC_TM) {
+        const int lr = row0 + tid;
+        const int g = (lr < nrows) ? (rowlist ? rowlist[lr] : lr) : -1;
+        if (g >= 0) {
+          const float thr = fminf(sthr[tid], __ldcg(ex.rowthr + g));
+          const int jlo = tile * SC_TN, jhi = min(jlo + SC_TN, Nr) - 1;
+          const int Ta = jlo / TC_FR_N, Tb = jhi / TC_FR_N;
+          const int R = g / TC_FR_M;
+          float L = INF;
+          for (int T = Ta; T <= Tb; ++T) {
+            const int pa = 2 * T;
+            float LT = __ldg(ex.rowlo + (int64_t)R * ex.nC + T);
+            LT = fmaxf(LT, __ldg(ex.pivlb + (int64_t)pa * ex.nfit + g) - __ldg(ex.prad + pa));
+            if (pa + 1 < ex.nR) LT = fmaxf(LT, __ldg(ex.pivlb + (int64_t)(pa + 1) * ex.nfit + g) - __ldg(ex.prad + pa + 1));
+            L = fminf(L, LT);
+          }
+          can = L > 0.0f && L * L > thr;
+        }
+      }
+      if (__syncthreads_and(can)) continue;
+    }
+    if (ex.ntiles && !dense && tid == 0) atomicAdd(ex.ntiles, 1ull);
+    // column records of this tile
     for (int e = tid; e < SC_TN * MDS_REC; e += SC_THREADS) {
       int fr = e / MDS_REC, i = e % MDS_REC;
       int j = tile * SC_TN + fr;
@@ -476,7 +543,7 @@ k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
       }
       __syncthreads();
     }
-    // epilogue: lower bounds and top-K' insertion
+    // epilogue: lower bounds and top-K' insertion (or the dense bounds)
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
       if (grow[p] < 0) continue;
@@ -486,28 +553,40 @@ k_screen_fp32(const float* __restrict__ Af, const float* __restrict__ Ar,
         int j = tile * SC_TN + tx + 16 * q;
         if (j >= Nr) continue;
         const float* cr = scol + (tx + 16 * q) * MDS_REC;
-        const float thr = sthr[lr];
+        const float thr = dense ? INF : fminf(sthr[lr], sgthr[lr]);
         float s = screen_shifted_f32(acc[p][q], rrec[p], cr, nofit != 0, guard * (rrec[p][15] + cr[15]), thr);
         s = fmaxf(s, 0.0f);
-        if (s < thr) {
+        if (dense) {
+          ex.dense[(int64_t)j * nrows + row0 + lr] = sqrtf(s);
+        } else if (s < thr) {
           int pos = atomicAdd(&scnt[lr], 1);
           pool[lr * P2 + pos] = mds_pack_key(s, j);
         }
       }
     }
     __syncthreads();
-    // compaction of rows whose pool exceeds K'
+    if (dense) continue;
+    // compaction of rows whose pool exceeds K' (or first holds k1 keys)
     for (int r = warp; r < SC_TM; r += SC_THREADS / 32) {
-      int n = scnt[r];
-      if (n <= Kp) continue;
+      const int n = scnt[r];
+      const bool first = ex.nmax && sthr[r] == INF && n >= ex.k1;
+      if (n <= Kp && !first) continue;
       warp_bitonic_sort(pool + r * P2, n, P2, lane);
       if (lane == 0) {
-        scnt[r] = Kp;
-        sthr[r] = mds_key_value(pool[r * P2 + Kp - 1]);
+        float t = (n >= Kp) ? mds_key_value(pool[r * P2 + Kp - 1]) : INF;
+        const int lr = row0 + r;
+        const int g = (lr < nrows) ? (rowlist ? rowlist[lr] : lr) : -1;
+        if (ex.nmax && g >= 0)
+          t = fminf(t, mds_key_value(pool[r * P2 + ex.k1 - 1]) +
+                           2.0f * guard * (__ldg(recf + (int64_t)g * MDS_REC + 15) + __ldg(ex.nmax)));
+        scnt[r] = min(n, Kp);
+        sthr[r] = t;
+        if (ex.rowthr && g >= 0) atomicMin(reinterpret_cast<int*>(ex.rowthr + g), __float_as_int(t));
       }
       __syncwarp();
     }
   }
+  if (dense) return;
   __syncthreads();
   // final: sort each row's pool and write it out
   for (int r = warp; r < SC_TM; r += SC_THREADS / 32) {
@@ -528,7 +607,7 @@ size_t screen_fp32_smem(int Kp) {
 
 int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar,
                        const float* recf, const float* recr, int nrows, const int* rowlist, int Kp,
-                       int nseg, uint64_t* cand, int* cand_n) {
+                       int nseg, uint64_t* cand, int* cand_n, const Fp32ScreenExtra* extra) {
   size_t smem = screen_fp32_smem(Kp);
   static bool attr_set = false;  // once: launches may also happen while a stream is captured
   static size_t limit = 0;
@@ -537,7 +616,8 @@ int launch_screen_fp32(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, cons
   int nrt = (nrows + SC_TM - 1) / SC_TM;
   ctx->stats.launches++;
   k_screen_fp32<<<nrt * nseg, SC_THREADS, smem, ctx->stream>>>(
-      Af, Ar, recf, recr, nrows, rowlist, pl.nref, pl.Ap, pl.nofit, pl.guard_fp32, Kp, nseg, cand, cand_n);
+      Af, Ar, recf, recr, nrows, rowlist, pl.nref, pl.Ap, pl.nofit, pl.guard_fp32, Kp, nseg, cand, cand_n,
+      extra ? *extra : Fp32ScreenExtra{});
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }
@@ -1195,10 +1275,51 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   DevBuf ntiles(ctx);             // tiles the tensor-core screen computed
   unsigned long long ht = 0;      // (read back after the recheck)
   long long dense_pairs = 0;
+  DevBuf f_lb(ctx), f_rowlo(ctx);
+  TcPivots f_pv;
   if (pl.prec == MDS_PREC_FP32) {
-    MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), nfit, nullptr, Kp, nseg,
-                               cand.as<uint64_t>(), cand_n.as<int>()));
+    // shared row thresholds and the (k+1)-th rule; for a set screened
+    // against itself, tile skipping with the row-tile pivots, whose bounds
+    // come from a dense pass of this screen over the pivots
+    Fp32ScreenExtra ex;
+    const bool keys_only = pl.screen_keys != nullptr;
+    if (!keys_only) {
+      MDS_TRY(rowthr.alloc(ctx, sizeof(float) * std::max(nfit, 1)));
+      MDS_CUDA(ctx, cudaMemsetAsync(rowthr.p, 0x7f, sizeof(float) * std::max(nfit, 1), s));
+      MDS_TRY(nmax.alloc(ctx, sizeof(float)));
+      MDS_TRY(tc_rec_nmax(ctx, Rr.as<float>(), nref, nmax.as<float>()));
+      MDS_TRY(ntiles.alloc(ctx, sizeof(unsigned long long)));
+      MDS_CUDA(ctx, cudaMemsetAsync(ntiles.p, 0, sizeof(unsigned long long), s));
+      ex.rowthr = rowthr.as<float>();
+      ex.nmax = nmax.as<float>();
+      ex.k1 = k + 1;
+      ex.ntiles = ntiles.as<unsigned long long>();
+    }
+    ex.diag = same ? 1 : 0;
+    const bool skipping = !keys_only && !pl.noskip && same && (nref + TC_FR_N - 1) / TC_FR_N >= 4;
     st.screen_launches = 1;
+    if (skipping) {
+      MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), f_pv, true));
+      MDS_TRY(f_lb.alloc(ctx, sizeof(float) * (size_t)f_pv.nP * nfit));
+      Fp32ScreenExtra dx;
+      dx.dense = f_lb.as<float>();
+      KnnRmsPlan pp = pl;
+      pp.nref = f_pv.nP;
+      MDS_TRY(launch_screen_fp32(ctx, pp, Afp, f_pv.A.as<float>(), Rfp, f_pv.R.as<float>(), nfit, nullptr, 32,
+                                 choose_nseg_fp32(nfit, ctx->num_sms, f_pv.nP), nullptr, nullptr, &dx));
+      MDS_TRY(f_rowlo.alloc(ctx, sizeof(float) * (size_t)f_pv.nP * f_pv.nC));
+      MDS_TRY(tc_skip_rowlo(ctx, f_pv, f_lb.as<float>(), nfit, f_rowlo.as<float>()));
+      ex.pivlb = f_lb.as<float>();
+      ex.prad = f_pv.rad.as<float>();
+      ex.rowlo = f_rowlo.as<float>();
+      ex.nR = f_pv.nP;
+      ex.nC = f_pv.nC;
+      ex.nfit = nfit;
+      dense_pairs = (long long)f_pv.nP * nfit;
+      st.screen_launches = 2;
+    }
+    MDS_TRY(launch_screen_fp32(ctx, pl, Afp, Ar.as<float>(), Rfp, Rr.as<float>(), nfit, nullptr, Kp, nseg,
+                               cand.as<uint64_t>(), cand_n.as<int>(), &ex));
   } else {
     // tile skipping by the triangle inequality once there are tiles to skip
     // (a set screened against itself uses row-tile pivots)
@@ -1263,7 +1384,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   audit.counters = audit_c.as<unsigned long long>();
   MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 0, cand.as<uint64_t>(),
                          cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i, flagged.as<int>(),
-                         nflag.as<int>(), pl.prec == MDS_PREC_FP32 ? nullptr : rowthr.as<float>(), &audit));
+                         nflag.as<int>(), rowthr.p ? rowthr.as<float>() : nullptr, &audit));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0, hbad[2] = {0, 0};
   unsigned long long hc[4] = {0, 0, 0, 0};
@@ -1298,7 +1419,8 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   st.kprime = Kp;
   st.rows_flagged = hflag;
   st.passes = 1;
-  st.screen_pairs = (long long)ht * 40 * 80 + dense_pairs;  // (ht landed with the sync above)
+  // (ht landed with the sync above)
+  st.screen_pairs = (long long)ht * (pl.prec == MDS_PREC_FP32 ? 32 * 64 : TC_FR_M * TC_FR_N) + dense_pairs;
 
   // re-screen flagged rows with more candidates (FP32 screen), then exact rows
   while (hflag > 0) {

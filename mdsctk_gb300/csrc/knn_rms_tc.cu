@@ -41,8 +41,7 @@
 #include "tc_ptx.cuh"
 #include "tc_select.cuh"
 
-#define TC_FR_M 40
-#define TC_FR_N 80
+// TC_FR_M / TC_FR_N (frames per row / column tile) come from knn_common.cuh
 #define TC_M 128
 #define TC_N 240
 #define TC_KB 32

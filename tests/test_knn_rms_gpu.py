@@ -96,6 +96,28 @@ def test_knn_rms_tile_skipping_exact(ctx, oracle, precision):
 
 
 @pytest.mark.gpu
+def test_knn_rms_fp32_tile_skipping_exact(ctx, oracle):
+    """The FP32 CUDA-core screen skips tiles of a set screened against itself
+    with the same row-tile pivots (its own dense pass over them): fewer pairs
+    than every tile, the same result as with skipping off, and the oracle's."""
+    x = synth.trajectory(2400, 64, seed=77, basins=6, dwell=120, drift_sigma=0.06)
+    m = synth.uniform_masses(64)
+    d, i = ctx.knn_rms(x, None, m, 20, precision="fp32")
+    st = ctx.stats()
+    assert st["screen_launches"] == 2  # pivot pass + screen
+    npiv = (len(x) + 39) // 40
+    tiles = ((len(x) + 31) // 32) * ((len(x) + 63) // 64)
+    assert npiv * len(x) < st["screen_pairs"] < npiv * len(x) + tiles * 2048
+    d2, i2 = ctx.knn_rms(x, None, m, 20, precision="fp32", skip=False)
+    st2 = ctx.stats()
+    assert st2["screen_launches"] == 1 and st2["screen_pairs"] == tiles * 2048
+    assert np.array_equal(d, d2) and np.array_equal(i, i2)
+    od, oi = oracle.knn_rms(x, None, m, 20)
+    assert np.max(np.abs(d - od)) <= 1e-4
+    assert np.mean(i == oi) > 0.999
+
+
+@pytest.mark.gpu
 def test_knn_rms_pinned_host_frames(ctx):
     """Page-locked host frames (the chunked upload overlaps the copies with
     the superposition) give the results of ordinary (pageable) host memory,
