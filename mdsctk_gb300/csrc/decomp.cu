@@ -364,70 +364,29 @@ __global__ void k_scale_copy(const double* __restrict__ w, double a, int n, doub
   if (i < n) out[i] = w[i] * a;
 }
 // ---------------------------------------------------------------------------
-// Lanczos steps j0..m-1 as one cooperative launch
+// One Lanczos step as four kernels over the same row blocks
 // ---------------------------------------------------------------------------
-// Every block owns a contiguous range of rows [r0, r1) and keeps w there in
-// shared memory. Per step:
-//   w = A v_j on its rows (a warp per row; x = v_j is read from L2, written
-//   by every block in the previous step), then the partial projections of w
-//   onto the nc = nlock + j + 1 basis columns over its rows -> part1;
-//   barrier; every block reduces part1 in the same fixed order (so all hold
-//   identical h1), w -= V h1 on its rows, partial projections of the new w
-//   -> part2;
-//   barrier; reduce part2 -> h2, w -= V h2, partial |w|^2 -> part3;
-//   barrier; reduce part3: alpha_j = h1[nlock + j] + h2[nlock + j], beta_j =
-//   |w|, breakdown when beta_j <= btol max(|alpha_j|, 1); v_{j+1} = w / beta_j
-//   on its rows (zeros after a breakdown: the host redoes those steps);
-//   barrier before the next step's product reads v_{j+1}.
-// This is the step of the separate-kernel sequence (SpMV, classical
-// Gram-Schmidt twice, norm, scale) with the same arithmetic per element; the
-// sums are grouped by block instead of by 256-row chunk, and stay
-// deterministic. Values written during the launch are read with ld.global.cg
-// (L2), never through the non-coherent L1 of another SM.
-struct LzSync {
-  unsigned count;
-  unsigned gen;
-  int err;
-  int pad;
-};
-
-// Grid-wide barrier (the launch is cooperative, so every block is resident).
-// A block waiting longer than limit_ns records an error and leaves; blocks
-// see the error at their next barrier and leave the step loop there.
-__device__ __forceinline__ bool lz_grid_sync(LzSync* g, unsigned nblocks, uint64_t limit_ns) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned* gen = &g->gen;
-    const unsigned my = *gen;
-    __threadfence();
-    if (atomicAdd(&g->count, 1u) == nblocks - 1) {
-      atomicExch(&g->count, 0u);
-      __threadfence();
-      atomicAdd(&g->gen, 1u);
-    } else {
-      uint64_t t0;
-      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-      while (*gen == my) {
-        if (*(volatile int*)&g->err) break;
-        uint64_t t;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        if (t - t0 > limit_ns) {
-          atomicExch(&g->err, 1);
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return *(volatile int*)&g->err == 0;
-}
-
+// Every block owns a contiguous range of rows [r0, r1). Per step j:
+//   k_lz_product:  w = A v_j on the block's rows (two rows per warp), and the
+//                  partial projections of w onto the nc = nlock + j + 1 basis
+//                  columns over its rows -> part1[b];
+//   k_lz_orth1:    every block reduces part1 in the same fixed order (all
+//                  hold identical h1), w -= V h1 on its rows, partial
+//                  projections of the new w -> part2[b];
+//   k_lz_orth2:    reduce part2 -> h2, w -= V h2, partial |w|^2 -> part3[b];
+//   k_lz_next:     reduce part3: alpha_j = h1[nlock + j] + h2[nlock + j],
+//                  beta_j = |w|, breakdown when beta_j <= btol max(|alpha_j|, 1);
+//                  v_{j+1} = w / beta_j on its rows (zeros after a breakdown:
+//                  the host redoes those steps).
+// The kernel boundaries are the grid-wide barriers. The arithmetic per
+// element is that of the separate SpMV / classical Gram-Schmidt (twice) /
+// norm / scale kernels; the sums are grouped by row block and stay
+// deterministic (fixed orders everywhere). The projection passes keep
+// LZ_U loads in flight per thread.
 // Sum of part[q * stride + c] over q = 0..G-1 by one warp, in a fixed order.
 __device__ __forceinline__ double lz_warp_colsum(const double* part, int G, int stride, int c, int lane) {
   double s = 0.0;
-  for (int q = lane; q < G; q += 32) s += __ldcg(part + (int64_t)q * stride + c);
+  for (int q = lane; q < G; q += 32) s += part[(int64_t)q * stride + c];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
 }
@@ -455,7 +414,7 @@ __device__ __forceinline__ void lz_block_dots(const double* __restrict__ V, int6
     for (int c0 = 0; c0 < nc; c0 += LZ_U) {
       double p[LZ_U];
 #pragma unroll
-      for (int x = 0; x < LZ_U; ++x) p[x] = (valid && c0 + x < nc) ? __ldcg(vi + (int64_t)(c0 + x) * ld) : 0.0;
+      for (int x = 0; x < LZ_U; ++x) p[x] = (valid && c0 + x < nc) ? __ldg(vi + (int64_t)(c0 + x) * ld) : 0.0;
 #pragma unroll
       for (int x = 0; x < LZ_U; ++x) {
         double q = p[x] * ui;
@@ -483,7 +442,7 @@ __device__ __forceinline__ double lz_block_sub(const double* __restrict__ V, int
     for (int c0 = 0; c0 < nc; c0 += LZ_U) {
       double p[LZ_U];
 #pragma unroll
-      for (int x = 0; x < LZ_U; ++x) p[x] = (c0 + x < nc) ? __ldcg(vi + (int64_t)(c0 + x) * ld) : 0.0;
+      for (int x = 0; x < LZ_U; ++x) p[x] = (c0 + x < nc) ? __ldg(vi + (int64_t)(c0 + x) * ld) : 0.0;
 #pragma unroll
       for (int x = 0; x < LZ_U; x += 2) {
         s0 += p[x] * ((c0 + x < nc) ? h[c0 + x] : 0.0);
@@ -497,102 +456,122 @@ __device__ __forceinline__ double lz_block_sub(const double* __restrict__ V, int
   return q;
 }
 
-__global__ void __launch_bounds__(LZ_THREADS) k_lanczos_cycle(
-    const int64_t* __restrict__ rp, const int* __restrict__ col, const double* __restrict__ aw, int n,
-    double* __restrict__ Vl, int64_t ld, int nlock, int j0, int m, int ncmax, double* __restrict__ part1,
-    double* __restrict__ part2, double* __restrict__ part3, double* __restrict__ ab, int* __restrict__ brk,
-    double btol, LzSync* __restrict__ gs, uint64_t limit_ns) {
-  extern __shared__ double lz_sm[];
-  const int G = gridDim.x, b = blockIdx.x;
-  const int r0 = (int)((int64_t)n * b / G), r1 = (int)((int64_t)n * (b + 1) / G), nr = r1 - r0;
-  const int rmax = (n + G - 1) / G;
-  double* ws = lz_sm;                   // w on this block's rows
-  double* hs = ws + rmax;               // projections, reduced over the grid
-  double* hb = hs + ncmax;              // the block's partial projections
-  double* wp = hb + ncmax;              // per-warp partials [LZ_WARPS][ncmax]
-  double* red = wp + LZ_WARPS * ncmax;  // [LZ_WARPS]
+__device__ __forceinline__ void lz_rows(int n, int& r0, int& nr) {
+  r0 = (int)((int64_t)n * blockIdx.x / gridDim.x);
+  nr = (int)((int64_t)n * (blockIdx.x + 1) / gridDim.x) - r0;
+}
+
+// Reduce part[0..G)[0..nc) into hs (shared), every block the same way.
+__device__ __forceinline__ void lz_reduce_into(const double* __restrict__ part, int nc, int ncmax, double* hs) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double* Vp = Vl + (int64_t)nlock * ld;
-  for (int j = j0; j < m; ++j) {
-    const int nc = nlock + j + 1;
-    const double* x = Vp + (int64_t)j * ld;
-    // w = A v_j on the block's rows: two rows per warp, a half-warp each,
-    // four elements per lane in flight
-    {
-      const int half = lane >> 4, hl = lane & 15;
-      for (int rb = r0 + 2 * warp; rb < r1; rb += 2 * LZ_WARPS) {
-        const int r = rb + half;
-        double s0 = 0.0, s1 = 0.0;
-        if (r < r1) {
-          const int64_t e1 = rp[r + 1];
-          int64_t e = rp[r] + hl;
-          for (; e + 48 < e1; e += 64) {
-            const int c0 = col[e], c1 = col[e + 16], c2 = col[e + 32], c3 = col[e + 48];
-            const double w0 = aw[e], w1 = aw[e + 16], w2 = aw[e + 32], w3 = aw[e + 48];
-            s0 += w0 * __ldcg(x + c0);
-            s1 += w1 * __ldcg(x + c1);
-            s0 += w2 * __ldcg(x + c2);
-            s1 += w3 * __ldcg(x + c3);
-          }
-          for (; e < e1; e += 16) s0 += aw[e] * __ldcg(x + col[e]);
-        }
-        double sum = s0 + s1;
-        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);  // within each half
-        if (hl == 0 && r < r1) ws[r - r0] = sum;
+  for (int c = warp; c < nc; c += LZ_WARPS) {
+    const double v = lz_warp_colsum(part, gridDim.x, ncmax, c, lane);
+    if (lane == 0) hs[c] = v;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(LZ_THREADS) k_lz_product(const int64_t* __restrict__ rp, const int* __restrict__ col,
+                                                           const double* __restrict__ aw, int n,
+                                                           const double* __restrict__ V, int64_t ld, int nc,
+                                                           const double* __restrict__ x, double* __restrict__ w,
+                                                           double* __restrict__ part1, int ncmax) {
+  extern __shared__ double lz_sm[];
+  int r0, nr;
+  lz_rows(n, r0, nr);
+  double* ws = lz_sm;                     // [rmax]
+  double* hb = ws + ((n + gridDim.x - 1) / gridDim.x);
+  double* wp = hb + ncmax;                // [LZ_WARPS][ncmax]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int half = lane >> 4, hl = lane & 15;
+  for (int rb = 2 * warp; rb < nr; rb += 2 * LZ_WARPS) {
+    const int rl = rb + half, r = r0 + rl;
+    double s0 = 0.0, s1 = 0.0;
+    if (rl < nr) {
+      const int64_t e1 = rp[r + 1];
+      int64_t e = rp[r] + hl;
+      for (; e + 48 < e1; e += 64) {
+        const int c0 = col[e], c1 = col[e + 16], c2 = col[e + 32], c3 = col[e + 48];
+        const double w0 = aw[e], w1 = aw[e + 16], w2 = aw[e + 32], w3 = aw[e + 48];
+        s0 += w0 * __ldg(x + c0);
+        s1 += w1 * __ldg(x + c1);
+        s0 += w2 * __ldg(x + c2);
+        s1 += w3 * __ldg(x + c3);
       }
+      for (; e < e1; e += 16) s0 += aw[e] * __ldg(x + col[e]);
     }
-    __syncthreads();
-    lz_block_dots(Vl, ld, r0, nr, nc, ws, wp, hb, ncmax);
-    for (int c = threadIdx.x; c < nc; c += LZ_THREADS) part1[(int64_t)b * ncmax + c] = hb[c];
-    if (!lz_grid_sync(gs, G, limit_ns)) break;
-    // h1; the first subtraction; the projections of the new w
-    for (int c = warp; c < nc; c += LZ_WARPS) {
-      const double v = lz_warp_colsum(part1, G, ncmax, c, lane);
-      if (lane == 0) hs[c] = v;
+    double sum = s0 + s1;
+    for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);  // within each half
+    if (hl == 0 && rl < nr) {
+      ws[rl] = sum;
+      w[r] = sum;
     }
-    __syncthreads();
-    const double a1 = hs[nlock + j];
-    lz_block_sub(Vl, ld, r0, nr, nc, hs, ws);
-    __syncthreads();
-    lz_block_dots(Vl, ld, r0, nr, nc, ws, wp, hb, ncmax);
-    for (int c = threadIdx.x; c < nc; c += LZ_THREADS) part2[(int64_t)b * ncmax + c] = hb[c];
-    if (!lz_grid_sync(gs, G, limit_ns)) break;
-    // h2; the second subtraction with |w|^2
-    for (int c = warp; c < nc; c += LZ_WARPS) {
-      const double v = lz_warp_colsum(part2, G, ncmax, c, lane);
-      if (lane == 0) hs[c] = v;
-    }
-    __syncthreads();
-    const double a2 = hs[nlock + j];
-    double q = lz_block_sub(Vl, ld, r0, nr, nc, hs, ws);
+  }
+  __syncthreads();
+  lz_block_dots(V, ld, r0, nr, nc, ws, wp, hb, ncmax);
+  for (int c = threadIdx.x; c < nc; c += LZ_THREADS) part1[(int64_t)blockIdx.x * ncmax + c] = hb[c];
+}
+
+// w -= V (reduce of partin); then either the partial projections of the new
+// w -> partout (second = 0), or its partial |w|^2 -> partout[b] (second = 1).
+// Block 0 keeps h[idx] (the projection onto v_j) in a_out.
+__global__ void __launch_bounds__(LZ_THREADS) k_lz_orth(int n, const double* __restrict__ V, int64_t ld, int nc,
+                                                        int ncmax, const double* __restrict__ partin,
+                                                        double* __restrict__ w, double* __restrict__ partout,
+                                                        int second, int idx, double* __restrict__ a_out) {
+  extern __shared__ double lz_sm[];
+  int r0, nr;
+  lz_rows(n, r0, nr);
+  double* ws = lz_sm;
+  double* hs = ws + ((n + gridDim.x - 1) / gridDim.x);
+  double* hb = hs + ncmax;
+  double* wp = hb + ncmax;
+  double* red = wp + LZ_WARPS * ncmax;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) ws[i] = w[r0 + i];
+  lz_reduce_into(partin, nc, ncmax, hs);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a_out = hs[idx];
+  double q = lz_block_sub(V, ld, r0, nr, nc, hs, ws);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) w[r0 + i] = ws[i];
+  if (!second) {
+    lz_block_dots(V, ld, r0, nr, nc, ws, wp, hb, ncmax);
+    for (int c = threadIdx.x; c < nc; c += LZ_THREADS) partout[(int64_t)blockIdx.x * ncmax + c] = hb[c];
+  } else {
     for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
     if (lane == 0) red[warp] = q;
     __syncthreads();
     if (threadIdx.x == 0) {
       double t = 0.0;
-      for (int w = 0; w < LZ_WARPS; ++w) t += red[w];
-      part3[b] = t;
+      for (int x2 = 0; x2 < LZ_WARPS; ++x2) t += red[x2];
+      partout[blockIdx.x] = t;
     }
-    if (!lz_grid_sync(gs, G, limit_ns)) break;
-    // alpha_j, beta_j, breakdown, v_{j+1}
-    if (warp == 0) {
-      const double v = lz_warp_colsum(part3, G, 1, 0, lane);
-      if (lane == 0) red[0] = v;
-    }
-    __syncthreads();
-    const double alpha = a1 + a2;
-    const double beta = sqrt(fmax(red[0], 0.0));
-    const bool bk = beta <= btol * fmax(fabs(alpha), 1.0);
-    if (b == 0 && threadIdx.x == 0) {
-      ab[j] = alpha;
-      ab[m + j] = beta;
-      brk[j] = bk ? 1 : 0;
-    }
-    double* vn = Vp + (int64_t)(j + 1) * ld + r0;
-    const double inv = 1.0 / beta;
-    for (int i = threadIdx.x; i < nr; i += LZ_THREADS) vn[i] = bk ? 0.0 : ws[i] * inv;
-    if (!lz_grid_sync(gs, G, limit_ns)) break;
   }
+}
+
+// alpha_j, beta_j, the breakdown flag and v_{j+1} = w / beta_j.
+__global__ void __launch_bounds__(LZ_THREADS) k_lz_next(int n, const double* __restrict__ part3,
+                                                        const double* __restrict__ a12, const double* __restrict__ w,
+                                                        double* __restrict__ vn, int j, int m, double btol,
+                                                        double* __restrict__ ab, int* __restrict__ brk) {
+  __shared__ double sb;
+  int r0, nr;
+  lz_rows(n, r0, nr);
+  if (threadIdx.x < 32) {
+    const double v = lz_warp_colsum(part3, gridDim.x, 1, 0, threadIdx.x);
+    if (threadIdx.x == 0) sb = v;
+  }
+  __syncthreads();
+  const double alpha = a12[0] + a12[1];
+  const double beta = sqrt(fmax(sb, 0.0));
+  const bool bk = beta <= btol * fmax(fabs(alpha), 1.0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ab[j] = alpha;
+    ab[m + j] = beta;
+    brk[j] = bk ? 1 : 0;
+  }
+  const double inv = 1.0 / beta;
+  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) vn[r0 + i] = bk ? 0.0 : w[r0 + i] * inv;
 }
 
 // X[:, 0:nout] = V[:, 0:m] * Y (Y: m x nout, column-major on device). One
@@ -786,32 +765,25 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   MDS_TRY(Yd.alloc(ctx, sizeof(double) * (size_t)m * m));
   MDS_TRY(tmp.alloc(ctx, sizeof(double) * (size_t)n * m));
   DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx);
-  // The steps of a cycle as one cooperative launch (k_lanczos_cycle): two
-  // blocks per SM when they fit, rows split evenly; each block keeps w on
-  // its rows in shared memory. Beyond that size the steps run as the
-  // separate kernels below, replayed from a CUDA graph.
+  // Each step as four fused kernels over row blocks (two blocks per SM; a
+  // block keeps w on its rows in shared memory); beyond that size the
+  // separate kernels. Either way the steps of a cycle are replayed from a
+  // CUDA graph.
   const int ncmax = nlock + m + 1;
-  int lz_grid = 0;
-  size_t lz_smem = 0;
-  DevBuf lz_p1(ctx), lz_p2(ctx), lz_p3(ctx), lz_sync(ctx);
-  for (int per_sm = 2; per_sm >= 1 && !lz_grid; --per_sm) {
-    const int G = per_sm * ctx->num_sms;
-    const size_t smem = sizeof(double) * ((size_t)(n + G - 1) / G + (2 + LZ_WARPS) * (size_t)ncmax + LZ_WARPS);
-    if (smem > 200 * 1024) continue;
-    if (smem > 48 * 1024)
-      MDS_CUDA(ctx, cudaFuncSetAttribute(k_lanczos_cycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int nb = 0;
-    MDS_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lanczos_cycle, LZ_THREADS, smem));
-    if (nb >= per_sm) {
-      lz_grid = G;
-      lz_smem = smem;
+  const int lz_G = 2 * ctx->num_sms;
+  const size_t lz_smem =
+      sizeof(double) * ((size_t)(n + lz_G - 1) / lz_G + (2 + LZ_WARPS) * (size_t)ncmax + LZ_WARPS);
+  const bool fused = lz_smem <= 200 * 1024;
+  DevBuf lz_p1(ctx), lz_p2(ctx), lz_p3(ctx), lz_a(ctx);
+  if (fused) {
+    MDS_TRY(lz_p1.alloc(ctx, sizeof(double) * (size_t)lz_G * ncmax));
+    MDS_TRY(lz_p2.alloc(ctx, sizeof(double) * (size_t)lz_G * ncmax));
+    MDS_TRY(lz_p3.alloc(ctx, sizeof(double) * (size_t)lz_G));
+    MDS_TRY(lz_a.alloc(ctx, 2 * sizeof(double)));
+    if (lz_smem > 48 * 1024) {
+      MDS_CUDA(ctx, cudaFuncSetAttribute(k_lz_product, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lz_smem));
+      MDS_CUDA(ctx, cudaFuncSetAttribute(k_lz_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lz_smem));
     }
-  }
-  if (lz_grid) {
-    MDS_TRY(lz_p1.alloc(ctx, sizeof(double) * (size_t)lz_grid * ncmax));
-    MDS_TRY(lz_p2.alloc(ctx, sizeof(double) * (size_t)lz_grid * ncmax));
-    MDS_TRY(lz_p3.alloc(ctx, sizeof(double) * (size_t)lz_grid));
-    MDS_TRY(lz_sync.alloc(ctx, sizeof(LzSync)));
   }
   // step graphs by first step of the cycle; destroyed on every return path
   struct Graphs : std::map<int, cudaGraphExec_t> {
@@ -892,37 +864,26 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
     // (invariant subspace, beta_j ~ 0) found then restarts the steps after
     // it from a fresh direction orthogonal to the basis.
     for (int j0 = k; j0 < m;) {
-      if (lz_grid) {
-        // one cooperative launch for the steps j0..m-1
-        const int64_t* a_rp = op.rp.as<int64_t>();
-        const int* a_col = op.col.as<int>();
-        const double* a_w = op.w.as<double>();
-        int a_n = n, a_nlock = nlock, a_j0 = j0, a_m = m, a_nc = ncmax;
-        int64_t a_ld = ld;
-        double* a_V = Vl;
-        double* a_p1 = lz_p1.as<double>();
-        double* a_p2 = lz_p2.as<double>();
-        double* a_p3 = lz_p3.as<double>();
-        double* a_ab = ab.as<double>();
-        int* a_brk = brk.as<int>();
-        double a_btol = eps * 10.0;
-        LzSync* a_sync = lz_sync.as<LzSync>();
-        uint64_t a_limit = 1000000000ull;  // 1 s per barrier wait
-        void* args[] = {&a_rp, &a_col, &a_w, &a_n, &a_V, &a_ld, &a_nlock, &a_j0, &a_m, &a_nc,
-                        &a_p1, &a_p2, &a_p3, &a_ab, &a_brk, &a_btol, &a_sync, &a_limit};
-        MDS_CUDA(ctx, cudaMemsetAsync(lz_sync.p, 0, sizeof(LzSync), s));
-        MDS_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_lanczos_cycle, dim3(lz_grid), dim3(LZ_THREADS),
-                                                  args, lz_smem, s));
-        ctx->stats.launches++;
-        out.matvecs += m - j0;
-      }
       // The steps j0..m-1 are one CUDA graph, captured the first time a cycle
       // starts at j0 (every pointer and size is fixed within this call) and
       // replayed afterwards: one launch instead of ~11 per step.
-      auto git = lz_grid ? graphs.end() : graphs.find(j0);
-      if (!lz_grid && git == graphs.end()) {
+      auto git = graphs.find(j0);
+      if (git == graphs.end()) {
         MDS_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int j = j0; j < m; ++j) {
+        for (int j = j0; j < m && fused; ++j) {
+          const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
+          k_lz_product<<<lz_G, LZ_THREADS, lz_smem, s>>>(op.rp.as<int64_t>(), op.col.as<int>(), op.w.as<double>(), n,
+                                                         Vl, ld, nc, Vp + (int64_t)j * ld, w, lz_p1.as<double>(),
+                                                         ncmax);
+          k_lz_orth<<<lz_G, LZ_THREADS, lz_smem, s>>>(n, Vl, ld, nc, ncmax, lz_p1.as<double>(), w,
+                                                      lz_p2.as<double>(), 0, nlock + j, lz_a.as<double>());
+          k_lz_orth<<<lz_G, LZ_THREADS, lz_smem, s>>>(n, Vl, ld, nc, ncmax, lz_p2.as<double>(), w,
+                                                      lz_p3.as<double>(), 1, nlock + j, lz_a.as<double>() + 1);
+          k_lz_next<<<lz_G, LZ_THREADS, 0, s>>>(n, lz_p3.as<double>(), lz_a.as<double>(), w,
+                                                Vp + (int64_t)(j + 1) * ld, j, m, eps * 10.0, ab.as<double>(),
+                                                brk.as<int>());
+        }
+        for (int j = j0; j < m && !fused; ++j) {
           const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
           k_spmv<<<(int)(((int64_t)op.n * 32 + 255) / 256), 256, 0, s>>>(op.rp.as<int64_t>(), op.col.as<int>(),
                                                                          op.w.as<double>(), Vp + (int64_t)j * ld,
@@ -949,20 +910,15 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
         if (ce != cudaSuccess) return mds_fail(ctx, MDS_ERR_CUDA, "Lanczos step graph: %s", cudaGetErrorString(ce));
         git = graphs.emplace(j0, ge).first;
       }
-      if (!lz_grid) {
-        MDS_CUDA(ctx, cudaGraphLaunch(git->second, s));
-        out.matvecs += m - j0;
-        ctx->stats.launches += 12 * (m - j0);
-      }
+      MDS_CUDA(ctx, cudaGraphLaunch(git->second, s));
+      out.matvecs += m - j0;
+      ctx->stats.launches += (fused ? 4 : 12) * (m - j0);
       MDS_CUDA(ctx, cudaGetLastError());
       std::vector<double> hab(2 * m);
       std::vector<int> hbrk(m);
-      LzSync hsync{};
       MDS_CUDA(ctx, cudaMemcpyAsync(hab.data(), ab.p, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, s));
       MDS_CUDA(ctx, cudaMemcpyAsync(hbrk.data(), brk.p, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
-      if (lz_grid) MDS_CUDA(ctx, cudaMemcpyAsync(&hsync, lz_sync.p, sizeof(LzSync), cudaMemcpyDeviceToHost, s));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
-      if (hsync.err) return mds_fail(ctx, MDS_ERR_TIMEOUT, "Lanczos steps: a grid barrier wait timed out");
       int jb = -1;
       for (int j = j0; j < m; ++j) {
         alpha[j] = hab[j];
