@@ -382,7 +382,7 @@ __global__ void k_scale_copy(const double* __restrict__ w, double a, int n, doub
 // element is that of the separate SpMV / classical Gram-Schmidt (twice) /
 // norm / scale kernels; the sums are grouped by row block and stay
 // deterministic (fixed orders everywhere). The projection passes keep
-// LZ_U loads in flight per thread.
+// projection and subtraction passes keep several loads in flight per thread.
 // Sum of part[q * stride + c] over q = 0..G-1 by one warp, in a fixed order.
 __device__ __forceinline__ double lz_warp_colsum(const double* part, int G, int stride, int c, int lane) {
   double s = 0.0;
@@ -393,63 +393,54 @@ __device__ __forceinline__ double lz_warp_colsum(const double* part, int G, int 
 
 #define LZ_THREADS 512
 #define LZ_WARPS (LZ_THREADS / 32)
-#define LZ_U 8  // basis columns per unrolled group: loads in flight per thread
 
 // Partial projections of u (the block's rows, in shared memory) onto the
-// columns 0..nc-1 of V over the block's rows: a thread per row, LZ_U columns'
-// loads in flight at a time, each product summed over the warp's 32 rows by
-// shuffles and added to the warp's own partial wp[warp][c] (so every sum has
-// a fixed order), then wp summed over the warps into out[c].
+// columns 0..nc-1 of V over the block's rows, into out[c]: a warp per
+// column, its lanes over the rows with four independent partial sums (four
+// loads in flight per lane), then the warp's shuffle tree -- a fixed order.
 __device__ __forceinline__ void lz_block_dots(const double* __restrict__ V, int64_t ld, int r0, int nr, int nc,
-                                              const double* __restrict__ u, double* __restrict__ wp,
-                                              double* __restrict__ out, int ncmax) {
+                                              const double* __restrict__ u, double* __restrict__ out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = lane; c < nc; c += 32) wp[warp * ncmax + c] = 0.0;
-  __syncwarp();
-  for (int i0 = 0; i0 < nr; i0 += LZ_THREADS) {
-    const int i = i0 + threadIdx.x;
-    const bool valid = i < nr;
-    const double ui = valid ? u[i] : 0.0;
-    const double* vi = V + r0 + (valid ? i : 0);
-    for (int c0 = 0; c0 < nc; c0 += LZ_U) {
-      double p[LZ_U];
-#pragma unroll
-      for (int x = 0; x < LZ_U; ++x) p[x] = (valid && c0 + x < nc) ? __ldg(vi + (int64_t)(c0 + x) * ld) : 0.0;
-#pragma unroll
-      for (int x = 0; x < LZ_U; ++x) {
-        double q = p[x] * ui;
-        for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-        if (lane == 0 && c0 + x < nc) wp[warp * ncmax + c0 + x] += q;
-      }
+  for (int c = warp; c < nc; c += LZ_WARPS) {
+    const double* vc = V + (int64_t)c * ld + r0;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = lane;
+    for (; i + 96 < nr; i += 128) {
+      const double v0 = __ldg(vc + i), v1 = __ldg(vc + i + 32), v2 = __ldg(vc + i + 64), v3 = __ldg(vc + i + 96);
+      s0 += v0 * u[i];
+      s1 += v1 * u[i + 32];
+      s2 += v2 * u[i + 64];
+      s3 += v3 * u[i + 96];
     }
+    for (; i < nr; i += 32) s0 += __ldg(vc + i) * u[i];
+    double t = (s0 + s1) + (s2 + s3);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[c] = t;
   }
   __syncthreads();
-  for (int c = threadIdx.x; c < nc; c += LZ_THREADS) {
-    double t = 0.0;
-    for (int w = 0; w < LZ_WARPS; ++w) t += wp[w * ncmax + c];
-    out[c] = t;
-  }
 }
 
-// u[i] -= sum_c V[i, c] h[c] on the block's rows (a thread per row, LZ_U
-// loads in flight); returns this thread's sum of the new u[i]^2.
+// u[i] -= sum_c V[i, c] h[c] on the block's rows (a thread per row, four
+// independent partial sums, eight loads in flight); returns this thread's
+// sum of the new u[i]^2.
 __device__ __forceinline__ double lz_block_sub(const double* __restrict__ V, int64_t ld, int r0, int nr, int nc,
                                                const double* __restrict__ h, double* __restrict__ u) {
   double q = 0.0;
   for (int i = threadIdx.x; i < nr; i += LZ_THREADS) {
     const double* vi = V + r0 + i;
-    double s0 = 0.0, s1 = 0.0;
-    for (int c0 = 0; c0 < nc; c0 += LZ_U) {
-      double p[LZ_U];
-#pragma unroll
-      for (int x = 0; x < LZ_U; ++x) p[x] = (c0 + x < nc) ? __ldg(vi + (int64_t)(c0 + x) * ld) : 0.0;
-#pragma unroll
-      for (int x = 0; x < LZ_U; x += 2) {
-        s0 += p[x] * ((c0 + x < nc) ? h[c0 + x] : 0.0);
-        s1 += p[x + 1] * ((c0 + x + 1 < nc) ? h[c0 + x + 1] : 0.0);
-      }
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int c = 0;
+#pragma unroll 2
+    for (; c + 3 < nc; c += 4) {
+      const double v0 = __ldg(vi + (int64_t)c * ld), v1 = __ldg(vi + (int64_t)(c + 1) * ld);
+      const double v2 = __ldg(vi + (int64_t)(c + 2) * ld), v3 = __ldg(vi + (int64_t)(c + 3) * ld);
+      s0 += v0 * h[c];
+      s1 += v1 * h[c + 1];
+      s2 += v2 * h[c + 2];
+      s3 += v3 * h[c + 3];
     }
-    const double ui = u[i] - (s0 + s1);
+    for (; c < nc; ++c) s0 += __ldg(vi + (int64_t)c * ld) * h[c];
+    const double ui = u[i] - ((s0 + s1) + (s2 + s3));
     u[i] = ui;
     q += ui * ui;
   }
@@ -481,7 +472,6 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz_product(const int64_t* __rest
   lz_rows(n, r0, nr);
   double* ws = lz_sm;                     // [rmax]
   double* hb = ws + ((n + gridDim.x - 1) / gridDim.x);
-  double* wp = hb + ncmax;                // [LZ_WARPS][ncmax]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int half = lane >> 4, hl = lane & 15;
   for (int rb = 2 * warp; rb < nr; rb += 2 * LZ_WARPS) {
@@ -508,7 +498,7 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz_product(const int64_t* __rest
     }
   }
   __syncthreads();
-  lz_block_dots(V, ld, r0, nr, nc, ws, wp, hb, ncmax);
+  lz_block_dots(V, ld, r0, nr, nc, ws, hb);
   for (int c = threadIdx.x; c < nc; c += LZ_THREADS) part1[(int64_t)blockIdx.x * ncmax + c] = hb[c];
 }
 
@@ -525,8 +515,7 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz_orth(int n, const double* __r
   double* ws = lz_sm;
   double* hs = ws + ((n + gridDim.x - 1) / gridDim.x);
   double* hb = hs + ncmax;
-  double* wp = hb + ncmax;
-  double* red = wp + LZ_WARPS * ncmax;
+  double* red = hb + ncmax;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < nr; i += LZ_THREADS) ws[i] = w[r0 + i];
   lz_reduce_into(partin, nc, ncmax, hs);
@@ -535,7 +524,7 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz_orth(int n, const double* __r
   __syncthreads();
   for (int i = threadIdx.x; i < nr; i += LZ_THREADS) w[r0 + i] = ws[i];
   if (!second) {
-    lz_block_dots(V, ld, r0, nr, nc, ws, wp, hb, ncmax);
+    lz_block_dots(V, ld, r0, nr, nc, ws, hb);
     for (int c = threadIdx.x; c < nc; c += LZ_THREADS) partout[(int64_t)blockIdx.x * ncmax + c] = hb[c];
   } else {
     for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
@@ -771,8 +760,7 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   // CUDA graph.
   const int ncmax = nlock + m + 1;
   const int lz_G = 2 * ctx->num_sms;
-  const size_t lz_smem =
-      sizeof(double) * ((size_t)(n + lz_G - 1) / lz_G + (2 + LZ_WARPS) * (size_t)ncmax + LZ_WARPS);
+  const size_t lz_smem = sizeof(double) * ((size_t)(n + lz_G - 1) / lz_G + 2 * (size_t)ncmax + LZ_WARPS);
   const bool fused = lz_smem <= 200 * 1024;
   DevBuf lz_p1(ctx), lz_p2(ctx), lz_p3(ctx), lz_a(ctx);
   if (fused) {
