@@ -325,8 +325,20 @@ def run_pipeline(args):
                 O.sysparse(d, i)
                 st["cpu_make_sysparse"] = time.perf_counter() - t0
                 t0 = time.perf_counter()
-                O.decomp_sparse(nn, pcol, irow, val, sigma, nev, ncv=ncv or None, tol=tol)
+                wo, Vo, reso = O.decomp_sparse(nn, pcol, irow, val, sigma, nev, ncv=ncv or None, tol=tol)
                 st["cpu_decomp_sparse_eigsh"] = time.perf_counter() - t0
+                # parity of the eigenpairs against ARPACK (scipy eigsh, same ncv/tol)
+                st["parity_evals_max_rel_err_vs_eigsh"] = float(np.max(np.abs(w - wo) / np.abs(wo)))
+                Qg = np.linalg.qr(np.asarray(V).T)[0]
+                Qo = np.linalg.qr(np.asarray(Vo).T)[0]
+                sv = np.linalg.svd(Qg.T @ Qo, compute_uv=False)
+                st["parity_subspace_min_cos_vs_eigsh"] = float(np.min(sv))
+                gaps = [min(abs(wo[x] - wo[y]) for y in range(nev) if y != x) for x in range(nev)]
+                errs = [float(np.max(np.abs(V[x] * np.sign(V[x] @ Vo[x]) - Vo[x])))
+                        for x in range(nev) if gaps[x] > 1e-4]
+                st["parity_evecs_max_abs_err_vs_eigsh_gapped"] = max(errs) if errs else None
+                st["parity_evecs_gapped_count"] = len(errs)
+                st["eigsh_max_residual"] = float(np.max(reso))
         elif args.pipeline == "sparse":
             n, na, k, eps = 20_000, 304, 32, 12.0
             x = synth.trajectory(n, na, seed=SEED + 17, basins=4, drift_sigma=0.05, dwell=500.0)
