@@ -292,15 +292,32 @@ __global__ void k_auto_sigma_entropic(const double* __restrict__ lists, int n, i
 // ---------------------------------------------------------------------------
 // 2. SpMV and dense vector kernels
 // ---------------------------------------------------------------------------
+// y = A x, two rows per warp (a half-warp each), four elements per lane in
+// flight; each row's sum in a fixed order (lane partials, then the
+// half-warp's shuffle tree).
 __global__ void k_spmv(const int64_t* __restrict__ rp, const int* __restrict__ col, const double* __restrict__ w,
                        const double* __restrict__ x, int n, double* __restrict__ y) {
-  int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (row >= n) return;
-  double s = 0.0;
-  for (int64_t e = rp[row] + lane; e < rp[row + 1]; e += 32) s += w[e] * __ldg(x + col[e]);
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) y[row] = s;
+  const int lane = threadIdx.x & 31, hl = lane & 15;
+  const int row = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2 + (lane >> 4);
+  double s0 = 0.0, s1 = 0.0;
+  if (row < n) {
+    const int64_t e1 = rp[row + 1];
+    int64_t e = rp[row] + hl;
+    for (; e + 48 < e1; e += 64) {
+      const int c0 = col[e], c1 = col[e + 16], c2 = col[e + 32], c3 = col[e + 48];
+      const double w0 = w[e], w1 = w[e + 16], w2 = w[e + 32], w3 = w[e + 48];
+      s0 += w0 * __ldg(x + c0);
+      s1 += w1 * __ldg(x + c1);
+      s0 += w2 * __ldg(x + c2);
+      s1 += w3 * __ldg(x + c3);
+    }
+    for (; e < e1; e += 16) s0 += w[e] * __ldg(x + col[e]);
+  }
+  double s = s0 + s1;
+  for (int o = 8; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);  // within each half
+  if (hl == 0 && row < n) y[row] = s;
 }
+static inline int spmv_blocks(int n) { return (int)(((int64_t)(n + 1) / 2 * 32 + 255) / 256); }
 
 // h[j] = sum_i V[i + j*ld] * w[i], j < ncols; partial sums per block then a
 // second kernel reduces them (deterministic order).
@@ -328,26 +345,47 @@ __global__ void k_reduce_part(const double* __restrict__ part, int nparts, int n
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) h[j] = s;
 }
-// w -= V[:, 0:ncols] h
+// w -= V[:, 0:ncols] h. With npart (blockDim.x = 256) also each block's sum
+// of the new w_i^2, in a fixed order, into npart[blockIdx.x] (the norm of w
+// without another pass over it).
 __global__ void k_gemv_sub(const double* __restrict__ V, int64_t ld, int n, int ncols,
-                           const double* __restrict__ h, double* __restrict__ w) {
+                           const double* __restrict__ h, double* __restrict__ w, double* __restrict__ npart) {
   extern __shared__ double hs[];
+  __shared__ double red[8];
   for (int j = threadIdx.x; j < ncols; j += blockDim.x) hs[j] = h[j];
   __syncthreads();
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double s = 0.0;
-  for (int j = 0; j < ncols; ++j) s += V[i + j * ld] * hs[j];
-  w[i] -= s;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double q = 0.0;
+  if (i < n) {
+    double s = 0.0;
+    for (int j = 0; j < ncols; ++j) s += V[i + j * ld] * hs[j];
+    const double wi = w[i] - s;
+    w[i] = wi;
+    q = wi * wi;
+  }
+  if (!npart) return;
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = q;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int x = 0; x < (int)(blockDim.x >> 5); ++x) t += red[x];
+    npart[blockIdx.x] = t;
+  }
 }
-// alpha_j = both projections onto v_j; beta_j = ||w||; breakdown when beta_j
-// <= tol * max(|alpha_j|, 1)
+// alpha_j = both projections onto v_j; beta_j = ||w|| from the per-block
+// partial sums of w_i^2 (one warp, fixed order); breakdown when beta_j <=
+// tol * max(|alpha_j|, 1)
 __global__ void k_lz_finish(const double* __restrict__ h1, const double* __restrict__ h2,
-                            const double* __restrict__ nrm, int idx, int j, double tol, double* __restrict__ alpha,
-                            double* __restrict__ beta, int* __restrict__ brk) {
+                            const double* __restrict__ npart, int nparts, int idx, int j, double tol,
+                            double* __restrict__ alpha, double* __restrict__ beta, int* __restrict__ brk) {
+  const int lane = threadIdx.x & 31;
+  double q = 0.0;
+  for (int b = lane; b < nparts; b += 32) q += npart[b];
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
   if (threadIdx.x != 0) return;
   double a = h1[idx] + h2[idx];
-  double b = sqrt(fmax(nrm[0], 0.0));
+  double b = sqrt(fmax(q, 0.0));
   alpha[j] = a;
   beta[j] = b;
   brk[j] = (b <= tol * fmax(fabs(a), 1.0)) ? 1 : 0;
@@ -363,206 +401,6 @@ __global__ void k_scale_copy(const double* __restrict__ w, double a, int n, doub
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = w[i] * a;
 }
-// ---------------------------------------------------------------------------
-// One Lanczos step as four kernels over the same row blocks
-// ---------------------------------------------------------------------------
-// Every block owns a contiguous range of rows [r0, r1). Per step j:
-//   k_lz_product:  w = A v_j on the block's rows (two rows per warp), and the
-//                  partial projections of w onto the nc = nlock + j + 1 basis
-//                  columns over its rows -> part1[b];
-//   k_lz_orth1:    every block reduces part1 in the same fixed order (all
-//                  hold identical h1), w -= V h1 on its rows, partial
-//                  projections of the new w -> part2[b];
-//   k_lz_orth2:    reduce part2 -> h2, w -= V h2, partial |w|^2 -> part3[b];
-//   k_lz_next:     reduce part3: alpha_j = h1[nlock + j] + h2[nlock + j],
-//                  beta_j = |w|, breakdown when beta_j <= btol max(|alpha_j|, 1);
-//                  v_{j+1} = w / beta_j on its rows (zeros after a breakdown:
-//                  the host redoes those steps).
-// The kernel boundaries are the grid-wide barriers. The arithmetic per
-// element is that of the separate SpMV / classical Gram-Schmidt (twice) /
-// norm / scale kernels; the sums are grouped by row block and stay
-// deterministic (fixed orders everywhere). The projection passes keep
-// projection and subtraction passes keep several loads in flight per thread.
-// Sum of part[q * stride + c] over q = 0..G-1 by one warp, in a fixed order.
-__device__ __forceinline__ double lz_warp_colsum(const double* part, int G, int stride, int c, int lane) {
-  double s = 0.0;
-  for (int q = lane; q < G; q += 32) s += part[(int64_t)q * stride + c];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  return s;
-}
-
-#define LZ_THREADS 512
-#define LZ_WARPS (LZ_THREADS / 32)
-
-// Partial projections of u (the block's rows, in shared memory) onto the
-// columns 0..nc-1 of V over the block's rows, into out[c]: a warp per
-// column, its lanes over the rows with four independent partial sums (four
-// loads in flight per lane), then the warp's shuffle tree -- a fixed order.
-__device__ __forceinline__ void lz_block_dots(const double* __restrict__ V, int64_t ld, int r0, int nr, int nc,
-                                              const double* __restrict__ u, double* __restrict__ out) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = warp; c < nc; c += LZ_WARPS) {
-    const double* vc = V + (int64_t)c * ld + r0;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    int i = lane;
-    for (; i + 96 < nr; i += 128) {
-      const double v0 = __ldg(vc + i), v1 = __ldg(vc + i + 32), v2 = __ldg(vc + i + 64), v3 = __ldg(vc + i + 96);
-      s0 += v0 * u[i];
-      s1 += v1 * u[i + 32];
-      s2 += v2 * u[i + 64];
-      s3 += v3 * u[i + 96];
-    }
-    for (; i < nr; i += 32) s0 += __ldg(vc + i) * u[i];
-    double t = (s0 + s1) + (s2 + s3);
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (lane == 0) out[c] = t;
-  }
-  __syncthreads();
-}
-
-// u[i] -= sum_c V[i, c] h[c] on the block's rows (a thread per row, four
-// independent partial sums, eight loads in flight); returns this thread's
-// sum of the new u[i]^2.
-__device__ __forceinline__ double lz_block_sub(const double* __restrict__ V, int64_t ld, int r0, int nr, int nc,
-                                               const double* __restrict__ h, double* __restrict__ u) {
-  double q = 0.0;
-  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) {
-    const double* vi = V + r0 + i;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    int c = 0;
-#pragma unroll 2
-    for (; c + 3 < nc; c += 4) {
-      const double v0 = __ldg(vi + (int64_t)c * ld), v1 = __ldg(vi + (int64_t)(c + 1) * ld);
-      const double v2 = __ldg(vi + (int64_t)(c + 2) * ld), v3 = __ldg(vi + (int64_t)(c + 3) * ld);
-      s0 += v0 * h[c];
-      s1 += v1 * h[c + 1];
-      s2 += v2 * h[c + 2];
-      s3 += v3 * h[c + 3];
-    }
-    for (; c < nc; ++c) s0 += __ldg(vi + (int64_t)c * ld) * h[c];
-    const double ui = u[i] - ((s0 + s1) + (s2 + s3));
-    u[i] = ui;
-    q += ui * ui;
-  }
-  return q;
-}
-
-__device__ __forceinline__ void lz_rows(int n, int& r0, int& nr) {
-  r0 = (int)((int64_t)n * blockIdx.x / gridDim.x);
-  nr = (int)((int64_t)n * (blockIdx.x + 1) / gridDim.x) - r0;
-}
-
-// Reduce part[0..G)[0..nc) into hs (shared), every block the same way.
-__device__ __forceinline__ void lz_reduce_into(const double* __restrict__ part, int nc, int ncmax, double* hs) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = warp; c < nc; c += LZ_WARPS) {
-    const double v = lz_warp_colsum(part, gridDim.x, ncmax, c, lane);
-    if (lane == 0) hs[c] = v;
-  }
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(LZ_THREADS) k_lz_product(const int64_t* __restrict__ rp, const int* __restrict__ col,
-                                                           const double* __restrict__ aw, int n,
-                                                           const double* __restrict__ V, int64_t ld, int nc,
-                                                           const double* __restrict__ x, double* __restrict__ w,
-                                                           double* __restrict__ part1, int ncmax) {
-  extern __shared__ double lz_sm[];
-  int r0, nr;
-  lz_rows(n, r0, nr);
-  double* ws = lz_sm;                     // [rmax]
-  double* hb = ws + ((n + gridDim.x - 1) / gridDim.x);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int half = lane >> 4, hl = lane & 15;
-  for (int rb = 2 * warp; rb < nr; rb += 2 * LZ_WARPS) {
-    const int rl = rb + half, r = r0 + rl;
-    double s0 = 0.0, s1 = 0.0;
-    if (rl < nr) {
-      const int64_t e1 = rp[r + 1];
-      int64_t e = rp[r] + hl;
-      for (; e + 48 < e1; e += 64) {
-        const int c0 = col[e], c1 = col[e + 16], c2 = col[e + 32], c3 = col[e + 48];
-        const double w0 = aw[e], w1 = aw[e + 16], w2 = aw[e + 32], w3 = aw[e + 48];
-        s0 += w0 * __ldg(x + c0);
-        s1 += w1 * __ldg(x + c1);
-        s0 += w2 * __ldg(x + c2);
-        s1 += w3 * __ldg(x + c3);
-      }
-      for (; e < e1; e += 16) s0 += aw[e] * __ldg(x + col[e]);
-    }
-    double sum = s0 + s1;
-    for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);  // within each half
-    if (hl == 0 && rl < nr) {
-      ws[rl] = sum;
-      w[r] = sum;
-    }
-  }
-  __syncthreads();
-  lz_block_dots(V, ld, r0, nr, nc, ws, hb);
-  for (int c = threadIdx.x; c < nc; c += LZ_THREADS) part1[(int64_t)blockIdx.x * ncmax + c] = hb[c];
-}
-
-// w -= V (reduce of partin); then either the partial projections of the new
-// w -> partout (second = 0), or its partial |w|^2 -> partout[b] (second = 1).
-// Block 0 keeps h[idx] (the projection onto v_j) in a_out.
-__global__ void __launch_bounds__(LZ_THREADS) k_lz_orth(int n, const double* __restrict__ V, int64_t ld, int nc,
-                                                        int ncmax, const double* __restrict__ partin,
-                                                        double* __restrict__ w, double* __restrict__ partout,
-                                                        int second, int idx, double* __restrict__ a_out) {
-  extern __shared__ double lz_sm[];
-  int r0, nr;
-  lz_rows(n, r0, nr);
-  double* ws = lz_sm;
-  double* hs = ws + ((n + gridDim.x - 1) / gridDim.x);
-  double* hb = hs + ncmax;
-  double* red = hb + ncmax;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) ws[i] = w[r0 + i];
-  lz_reduce_into(partin, nc, ncmax, hs);
-  if (blockIdx.x == 0 && threadIdx.x == 0) *a_out = hs[idx];
-  double q = lz_block_sub(V, ld, r0, nr, nc, hs, ws);
-  __syncthreads();
-  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) w[r0 + i] = ws[i];
-  if (!second) {
-    lz_block_dots(V, ld, r0, nr, nc, ws, hb);
-    for (int c = threadIdx.x; c < nc; c += LZ_THREADS) partout[(int64_t)blockIdx.x * ncmax + c] = hb[c];
-  } else {
-    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-    if (lane == 0) red[warp] = q;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int x2 = 0; x2 < LZ_WARPS; ++x2) t += red[x2];
-      partout[blockIdx.x] = t;
-    }
-  }
-}
-
-// alpha_j, beta_j, the breakdown flag and v_{j+1} = w / beta_j.
-__global__ void __launch_bounds__(LZ_THREADS) k_lz_next(int n, const double* __restrict__ part3,
-                                                        const double* __restrict__ a12, const double* __restrict__ w,
-                                                        double* __restrict__ vn, int j, int m, double btol,
-                                                        double* __restrict__ ab, int* __restrict__ brk) {
-  __shared__ double sb;
-  int r0, nr;
-  lz_rows(n, r0, nr);
-  if (threadIdx.x < 32) {
-    const double v = lz_warp_colsum(part3, gridDim.x, 1, 0, threadIdx.x);
-    if (threadIdx.x == 0) sb = v;
-  }
-  __syncthreads();
-  const double alpha = a12[0] + a12[1];
-  const double beta = sqrt(fmax(sb, 0.0));
-  const bool bk = beta <= btol * fmax(fabs(alpha), 1.0);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ab[j] = alpha;
-    ab[m + j] = beta;
-    brk[j] = bk ? 1 : 0;
-  }
-  const double inv = 1.0 / beta;
-  for (int i = threadIdx.x; i < nr; i += LZ_THREADS) vn[r0 + i] = bk ? 0.0 : w[r0 + i] * inv;
-}
-
 // X[:, 0:nout] = V[:, 0:m] * Y (Y: m x nout, column-major on device). One
 // thread per row and GV_CB output columns per block (grid.y); Y is staged in
 // shared memory GV_JT rows at a time, so every V element is read once per
@@ -721,7 +559,7 @@ static int build_symop(mds_ctx* ctx, int n, const int* dpcol, const int* dirow, 
 
 static void spmv(mds_ctx* ctx, const SymOp& op, const double* x, double* y) {
   ctx->stats.launches++;
-  k_spmv<<<(int)(((int64_t)op.n * 32 + 255) / 256), 256, 0, ctx->stream>>>(op.rp.as<int64_t>(), op.col.as<int>(),
+  k_spmv<<<spmv_blocks(op.n), 256, 0, ctx->stream>>>(op.rp.as<int64_t>(), op.col.as<int>(),
                                                                            op.w.as<double>(), x, op.n, y);
 }
 
@@ -753,26 +591,8 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   MDS_TRY(part.alloc(ctx, sizeof(double) * (size_t)nparts * (nlock + m + 1)));
   MDS_TRY(Yd.alloc(ctx, sizeof(double) * (size_t)m * m));
   MDS_TRY(tmp.alloc(ctx, sizeof(double) * (size_t)n * m));
-  DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx);
-  // Each step as four fused kernels over row blocks (two blocks per SM; a
-  // block keeps w on its rows in shared memory); beyond that size the
-  // separate kernels. Either way the steps of a cycle are replayed from a
-  // CUDA graph.
-  const int ncmax = nlock + m + 1;
-  const int lz_G = 2 * ctx->num_sms;
-  const size_t lz_smem = sizeof(double) * ((size_t)(n + lz_G - 1) / lz_G + 2 * (size_t)ncmax + LZ_WARPS);
-  const bool fused = lz_smem <= 200 * 1024;
-  DevBuf lz_p1(ctx), lz_p2(ctx), lz_p3(ctx), lz_a(ctx);
-  if (fused) {
-    MDS_TRY(lz_p1.alloc(ctx, sizeof(double) * (size_t)lz_G * ncmax));
-    MDS_TRY(lz_p2.alloc(ctx, sizeof(double) * (size_t)lz_G * ncmax));
-    MDS_TRY(lz_p3.alloc(ctx, sizeof(double) * (size_t)lz_G));
-    MDS_TRY(lz_a.alloc(ctx, 2 * sizeof(double)));
-    if (lz_smem > 48 * 1024) {
-      MDS_CUDA(ctx, cudaFuncSetAttribute(k_lz_product, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lz_smem));
-      MDS_CUDA(ctx, cudaFuncSetAttribute(k_lz_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lz_smem));
-    }
-  }
+  DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx), npart(ctx);
+  MDS_TRY(npart.alloc(ctx, sizeof(double) * (size_t)((n + 255) / 256)));
   // step graphs by first step of the cycle; destroyed on every return path
   struct Graphs : std::map<int, cudaGraphExec_t> {
     ~Graphs() {
@@ -806,7 +626,8 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   auto subtract = [&](int ncols, const std::vector<double>& hh) -> int {
     MDS_CUDA(ctx, cudaMemcpyAsync(h.p, hh.data(), sizeof(double) * ncols, cudaMemcpyHostToDevice, s));
     ctx->stats.launches++;
-    k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * ncols, s>>>(Vl, ld, n, ncols, h.as<double>(), w);
+    k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * ncols, s>>>(Vl, ld, n, ncols, h.as<double>(), w,
+                                                                      nullptr);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
@@ -854,38 +675,24 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
     for (int j0 = k; j0 < m;) {
       // The steps j0..m-1 are one CUDA graph, captured the first time a cycle
       // starts at j0 (every pointer and size is fixed within this call) and
-      // replayed afterwards: one launch instead of ~11 per step.
+      // replayed afterwards: one launch instead of 9 per step.
       auto git = graphs.find(j0);
       if (git == graphs.end()) {
         MDS_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int j = j0; j < m && fused; ++j) {
+        for (int j = j0; j < m; ++j) {
           const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
-          k_lz_product<<<lz_G, LZ_THREADS, lz_smem, s>>>(op.rp.as<int64_t>(), op.col.as<int>(), op.w.as<double>(), n,
-                                                         Vl, ld, nc, Vp + (int64_t)j * ld, w, lz_p1.as<double>(),
-                                                         ncmax);
-          k_lz_orth<<<lz_G, LZ_THREADS, lz_smem, s>>>(n, Vl, ld, nc, ncmax, lz_p1.as<double>(), w,
-                                                      lz_p2.as<double>(), 0, nlock + j, lz_a.as<double>());
-          k_lz_orth<<<lz_G, LZ_THREADS, lz_smem, s>>>(n, Vl, ld, nc, ncmax, lz_p2.as<double>(), w,
-                                                      lz_p3.as<double>(), 1, nlock + j, lz_a.as<double>() + 1);
-          k_lz_next<<<lz_G, LZ_THREADS, 0, s>>>(n, lz_p3.as<double>(), lz_a.as<double>(), w,
-                                                Vp + (int64_t)(j + 1) * ld, j, m, eps * 10.0, ab.as<double>(),
-                                                brk.as<int>());
-        }
-        for (int j = j0; j < m && !fused; ++j) {
-          const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
-          k_spmv<<<(int)(((int64_t)op.n * 32 + 255) / 256), 256, 0, s>>>(op.rp.as<int64_t>(), op.col.as<int>(),
-                                                                         op.w.as<double>(), Vp + (int64_t)j * ld,
-                                                                         op.n, w);
+          k_spmv<<<spmv_blocks(op.n), 256, 0, s>>>(op.rp.as<int64_t>(), op.col.as<int>(), op.w.as<double>(),
+                                                   Vp + (int64_t)j * ld, op.n, w);
           k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
           k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h1.as<double>());
-          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h1.as<double>(), w);
+          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h1.as<double>(), w, nullptr);
           k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
           k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h2.as<double>());
-          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h2.as<double>(), w);
-          k_gemv_t_part<<<nparts, 256, 0, s>>>(w, ld, n, 1, w, part.as<double>());
-          k_reduce_part<<<1, 128, 0, s>>>(part.as<double>(), nparts, 1, h.as<double>());
-          k_lz_finish<<<1, 32, 0, s>>>(h1.as<double>(), h2.as<double>(), h.as<double>(), nlock + j, j,
-                                       eps * 10.0, ab.as<double>(), ab.as<double>() + m, brk.as<int>());
+          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h2.as<double>(), w,
+                                                                       npart.as<double>());
+          k_lz_finish<<<1, 32, 0, s>>>(h1.as<double>(), h2.as<double>(), npart.as<double>(), (n + 255) / 256,
+                                       nlock + j, j, eps * 10.0, ab.as<double>(), ab.as<double>() + m,
+                                       brk.as<int>());
           k_lz_scale<<<(n + 255) / 256, 256, 0, s>>>(w, ab.as<double>() + m, brk.as<int>(), j, n,
                                                      Vp + (int64_t)(j + 1) * ld);
         }
@@ -900,7 +707,7 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
       }
       MDS_CUDA(ctx, cudaGraphLaunch(git->second, s));
       out.matvecs += m - j0;
-      ctx->stats.launches += (fused ? 4 : 12) * (m - j0);
+      ctx->stats.launches += 9 * (m - j0);
       MDS_CUDA(ctx, cudaGetLastError());
       std::vector<double> hab(2 * m);
       std::vector<int> hbrk(m);
