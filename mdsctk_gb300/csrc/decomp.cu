@@ -808,18 +808,25 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
 
 // Lanczos from one start vector sees one direction of each eigenspace, so a
 // wanted eigenvalue of multiplicity > 1 (e.g. 1.0 once per connected
-// component of the kNN graph) can be missed. After convergence, run a short
-// sequence (three restarts of 20 vectors) on the operator deflated by the nev
-// converged vectors: its top Ritz value is a lower bound of the deflated
-// spectrum's top, so a value more than 1e-10 (relative) above the nev-th
-// eigenvalue proves a missed eigenpair; it is then converged to the requested
-// tolerance, inserted in order (dropping the smallest) and the check repeats.
+// component of the kNN graph) can be missed. After convergence, run a
+// sequence on the operator deflated by the nev converged vectors, its top
+// Ritz value converged to 1e-8 (at most 30 restarts of 40 vectors): that
+// value is a lower bound of the deflated spectrum's top, so a value more than
+// 1e-10 (relative) above the nev-th eigenvalue proves a missed eigenpair; it
+// is then converged to the requested tolerance, inserted in order (dropping
+// the smallest) and the check repeats.
 // Eigenvalues within 1e-10 of the nev-th are interchangeable with it.
 static int lanczos_complete(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, int maxiter, double* dX,
                             LanczosOut& out) {
   MDS_TRY(lanczos(ctx, op, nev, ncv, tol, maxiter, dX, out));
   const int n = op.n;
-  const int ncv2 = std::min(20, n - nev);
+  // The check runs until the deflated top Ritz value converges (to 1e-8, at
+  // most 30 restarts of 40 vectors): crowded eigenvalues just below a missed
+  // one slow its convergence, and a Ritz value stopped early can sit below
+  // the nev-th eigenvalue although the missed one is above it (a graph of
+  // three components, triple eigenvalue 1 with 0.9996 next, asked for nev = 3:
+  // three restarts of 20 vectors reached 0.99977 < 0.99990; converged, 1.0).
+  const int ncv2 = std::min(40, n - nev);
   if (ncv2 < 3) return MDS_OK;
   cudaStream_t s = ctx->stream;
   DevBuf y(ctx);
@@ -829,7 +836,7 @@ static int lanczos_complete(mds_ctx* ctx, const SymOp& op, int nev, int ncv, dou
   for (int pass = 0; pass < nev; ++pass) {
     const uint64_t seed = 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull * (uint64_t)(pass + 1);
     LanczosOut o2;
-    MDS_TRY(lanczos(ctx, op, 1, ncv2, 1e-6, 3, y.as<double>(), o2, dX, nev, seed));
+    MDS_TRY(lanczos(ctx, op, 1, ncv2, 1e-8, 30, y.as<double>(), o2, dX, nev, seed));
     out.matvecs += o2.matvecs;
     const double th = o2.evals[0], lo = out.evals[nev - 1];
     if (!(th > lo + 1e-10 * std::max(1.0, std::fabs(lo)))) break;

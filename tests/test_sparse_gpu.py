@@ -195,3 +195,25 @@ def test_auto_nystrom(ctx, oracle):
     Bo = oracle.affinity_nystrom_auto(m, pb, ib, vb, osig, d_a)
     Eo = oracle.nystrom_extend(w, V, m, pb, ib, Bo)
     assert np.max(np.abs(E - Eo)) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nev", [3, 5])
+def test_decomp_triple_eigenvalue(ctx, oracle, nev):
+    """Three disconnected basins: eigenvalue 1 three times, with 0.99999996,
+    0.9999 and 0.9996 just below. Lanczos from one start vector finds one
+    copy; the completion on the deflated operator must find the others,
+    also when nev leaves no room beyond the three copies."""
+    from mdsctk_gb300 import synth
+
+    land = synth.trajectory(900, 64, seed=31, basins=3, dwell=150)
+    m = synth.uniform_masses(64)
+    d, i = oracle.knn_rms(land, None, m, 16)
+    sigma = float(np.median(d))
+    n, pcol, irow, val = oracle.sysparse(d, i)
+    exact = np.linalg.eigvalsh(oracle.dense_affinity(n, pcol, irow, val, sigma))[::-1][:nev]
+    assert np.sum(np.abs(exact - 1.0) < 1e-12) == 3
+    w, V, res, nconv = ctx.decomp_sparse(n, pcol, irow, val, sigma, nev)
+    assert np.allclose(w, exact, rtol=1e-6), (w, exact)
+    assert np.max(np.abs(V @ V.T - np.eye(nev))) < 1e-10
+    assert np.max(res) < 1e-8
