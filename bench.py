@@ -333,6 +333,14 @@ def run_pipeline(args):
                 Qo = np.linalg.qr(np.asarray(Vo).T)[0]
                 sv = np.linalg.svd(Qg.T @ Qo, compute_uv=False)
                 st["parity_subspace_min_cos_vs_eigsh"] = float(np.min(sv))
+                # the same for the leading nev-1 vectors, and the gap below the
+                # nev-th eigenvalue (from a GPU run with nev+1): when that gap is
+                # within the tolerance the nev-th direction is not determined
+                sv1 = np.linalg.svd(np.linalg.qr(np.asarray(V[:-1]).T)[0].T @ np.linalg.qr(np.asarray(Vo[:-1]).T)[0],
+                                    compute_uv=False)
+                st["parity_subspace_min_cos_vs_eigsh_first_nev_minus_1"] = float(np.min(sv1))
+                w1, _, _, _ = c.decomp_sparse(nn, pcol, irow, val, sigma, nev + 1, ncv=ncv, tol=tol)
+                st["gap_nev_to_next"] = float(w1[nev - 1] - w1[nev])
                 gaps = [min(abs(wo[x] - wo[y]) for y in range(nev) if y != x) for x in range(nev)]
                 errs = [float(np.max(np.abs(V[x] * np.sign(V[x] @ Vo[x]) - Vo[x])))
                         for x in range(nev) if gaps[x] > 1e-4]
