@@ -1275,6 +1275,11 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   DevBuf ntiles(ctx);             // tiles the tensor-core screen computed
   unsigned long long ht = 0;      // (read back after the recheck)
   long long dense_pairs = 0;
+  // error words of the tensor-core launches (pivot pass, screen), read at the
+  // call's synchronisation after the recheck instead of after each launch
+  DevBuf tcerr(ctx);
+  MDS_TRY(tcerr.alloc(ctx, 4 * sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(tcerr.p, 0, 4 * sizeof(int), s));
   DevBuf f_lb(ctx), f_rowlo(ctx);
   TcPivots f_pv;
   if (pl.prec == MDS_PREC_FP32) {
@@ -1330,7 +1335,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     if (skipping) {
       MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv, same));
       MDS_TRY(lb.alloc(ctx, sizeof(float) * (size_t)pv.nP * nfit));
-      MDS_TRY(tc_skip_bounds(ctx, pl, same ? tcr : tcf, Rfp, nfit, pv, lb.as<float>()));
+      MDS_TRY(tc_skip_bounds(ctx, pl, same ? tcr : tcf, Rfp, nfit, pv, lb.as<float>(), tcerr.as<int>()));
       sk.pivlb = lb.as<float>();
       sk.prad = pv.rad.as<float>();
       if (same) {
@@ -1355,7 +1360,8 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     MDS_TRY(ntiles.alloc(ctx, sizeof(unsigned long long)));
     MDS_CUDA(ctx, cudaMemsetAsync(ntiles.p, 0, sizeof(unsigned long long), s));
     MDS_TRY(launch_screen_tc(ctx, pl, same ? tcr : tcf, tcr, Rfp, Rr.as<float>(), nfit, Kp, nseg,
-                             cand.as<uint64_t>(), cand_n.as<int>(), nullptr, skipping ? &sk : nullptr, nullptr,
+                             cand.as<uint64_t>(), cand_n.as<int>(), pl.screen_keys ? nullptr : tcerr.as<int>() + 2,
+                             skipping ? &sk : nullptr, nullptr,
                              rowthr.as<float>(), pl.screen_keys ? nullptr : nmax.as<float>(),
                              ntiles.as<unsigned long long>()));
     st.screen_launches = skipping ? 2 : 1;
@@ -1386,13 +1392,17 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
                          cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i, flagged.as<int>(),
                          nflag.as<int>(), rowthr.p ? rowthr.as<float>() : nullptr, &audit));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
-  int hflag = 0, hbad[2] = {0, 0};
+  int hflag = 0, hbad[2] = {0, 0}, herr[4] = {0, 0, 0, 0};
   unsigned long long hc[4] = {0, 0, 0, 0};
+  MDS_CUDA(ctx, cudaMemcpyAsync(herr, tcerr.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
   if (ntiles.p) MDS_CUDA(ctx, cudaMemcpyAsync(&ht, ntiles.p, sizeof(ht), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(&hflag, nflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(hc, audit_c.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(hbad, badf.p, sizeof(hbad), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  if (herr[0] || herr[2])
+    return mds_fail(ctx, MDS_ERR_TIMEOUT, "tensor-core screen: a bounded wait timed out (pass %s, role %d)",
+                    herr[0] ? "pivots" : "screen", herr[0] ? herr[0] : herr[2]);
   // (every loop of the screen and recheck is bounded, so such frames only
   // make their own values meaningless; the call reports them as an error)
   if (hbad[0] != 0x7f7f7f7f)

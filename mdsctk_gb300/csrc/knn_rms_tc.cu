@@ -981,7 +981,9 @@ int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const fl
   KnnRmsPlan pp = pl;
   pp.nref = nP;
   MDS_TRY(tc_prepare(ctx, pp, pv.A.as<float>(), nP, pv.tc, 1));
-  MDS_CUDA(ctx, cudaStreamSynchronize(s));  // dpiv is released on return
+  // (dpiv goes back to the context's cache on return; its later users are
+  // ordered after these kernels on the same stream, and the host copy above
+  // was staged before cudaMemcpyAsync returned, so no synchronisation)
   return MDS_OK;
 }
 
