@@ -812,9 +812,10 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
 // sequence on the operator deflated by the nev converged vectors, its top
 // Ritz value converged to 1e-8 (at most 30 restarts of 40 vectors): that
 // value is a lower bound of the deflated spectrum's top, so a value more than
-// 1e-10 (relative) above the nev-th eigenvalue proves a missed eigenpair; it
-// is then converged to the requested tolerance, inserted in order (dropping
-// the smallest) and the check repeats.
+// 1e-10 (relative) above the nev-th eigenvalue proves a missed eigenpair. If
+// it is a further copy of an eigenvalue already found (within 1e-9
+// relative), it is converged to the requested tolerance, inserted in order
+// (dropping the smallest) and the check repeats.
 // Eigenvalues within 1e-10 of the nev-th are interchangeable with it.
 static int lanczos_complete(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, int maxiter, double* dX,
                             LanczosOut& out) {
@@ -840,6 +841,14 @@ static int lanczos_complete(mds_ctx* ctx, const SymOp& op, int nev, int ncv, dou
     out.matvecs += o2.matvecs;
     const double th = o2.evals[0], lo = out.evals[nev - 1];
     if (!(th > lo + 1e-10 * std::max(1.0, std::fabs(lo)))) break;
+    // Only a further copy of an eigenvalue already found is inserted: a
+    // multiple eigenvalue is what one start vector cannot see. A distinct
+    // eigenvalue above the nev-th that the sequence left out (crowded
+    // spectra near 1) is left out as ARPACK leaves it out.
+    bool copy = false;
+    for (int x = 0; x < nev && !copy; ++x)
+      copy = std::fabs(th - out.evals[x]) <= 1e-9 * std::max(1.0, std::fabs(out.evals[x]));
+    if (!copy) break;
     o2 = LanczosOut();  // converge the missed pair to the requested tolerance
     MDS_TRY(lanczos(ctx, op, 1, ncv2, tol, maxiter, y.as<double>(), o2, dX, nev, seed));
     out.matvecs += o2.matvecs;

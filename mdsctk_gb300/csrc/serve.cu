@@ -100,6 +100,7 @@ struct Slot {
   mds_ctx* ctx = nullptr;
   int cap = 0;
   DevBuf raw, A, R, cand, cand_n, out_d, out_i, flagged, nflag, derr, ext, lb, rowthr;
+  DevBuf audit;  // the recheck's audit counters of the screen's bounds (4 x u64)
   TcOperands tcq;
   float* h_raw = nullptr;
   double* h_d = nullptr;
@@ -175,6 +176,7 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
   mds_ctx* c = sl.ctx;
   KnnRmsPlan pl = S->plan(bucket);
   MDS_CUDA(c, cudaMemsetAsync(sl.nflag.p, 0, sizeof(int), c->stream));
+  MDS_CUDA(c, cudaMemsetAsync(sl.audit.p, 0, 4 * sizeof(unsigned long long), c->stream));
   MDS_TRY(launch_prep(c, sl.raw.as<float>(), bucket, S->natoms, S->Ap, S->dmass.as<float>(), S->dswn.as<float>(),
                       S->tm, S->dmu.as<float>(), S->dM0.as<double>(), pl.nofit, sl.A.as<float>(), sl.R.as<float>()));
   int nseg;
@@ -198,10 +200,18 @@ static int launch_batch(mds_server* S, Slot& sl, int bucket) {
                                nullptr, S->Kp, nseg, sl.cand.as<uint64_t>(), sl.cand_n.as<int>()));
   }
   const int segstride = (S->prec == MDS_PREC_FP32) ? S->Kp : tc_seg_stride();
+  // the recheck audits the screen's bounds on the pairs it rechecks; a row
+  // with a bound above its exact value is flagged and finished like a row
+  // whose guard check failed (finish_batch)
+  RecheckAudit audit;
+  audit.recf = sl.R.as<float>();
+  audit.recr = S->R.as<float>();
+  audit.guard = (S->prec == MDS_PREC_FP32) ? pl.guard_fp32 : pl.guard_tc;
+  audit.counters = sl.audit.as<unsigned long long>();
   MDS_TRY(launch_recheck(c, pl, sl.A.as<float>(), S->A.as<float>(), S->dmu.as<float>(), S->U.as<float>(), bucket,
                          nullptr, 0, sl.cand.as<uint64_t>(), sl.cand_n.as<int>(), nseg, segstride, S->Kp, S->k,
                          sl.out_d.as<double>(), sl.out_i.as<int>(), sl.flagged.as<int>(), sl.nflag.as<int>(),
-                         S->prec == MDS_PREC_FP32 ? nullptr : sl.rowthr.as<float>()));
+                         S->prec == MDS_PREC_FP32 ? nullptr : sl.rowthr.as<float>(), &audit));
   c->stats.launches++;
   k_serve_ext<<<(bucket + 127) / 128, 128, 0, c->stream>>>(sl.out_d.as<double>(), sl.out_i.as<int>(), bucket, S->k,
                                                           S->cfg.sigma, S->ddinv.as<double>(), S->dZ.as<double>(),
@@ -549,6 +559,7 @@ extern "C" int mds_server_create(const mds_server_config* cfg, const float* land
               sl.out_d.alloc(c, sizeof(double) * (size_t)cap * S->k) == MDS_OK &&
               sl.out_i.alloc(c, sizeof(int) * (size_t)cap * S->k) == MDS_OK &&
               sl.flagged.alloc(c, sizeof(int) * cap) == MDS_OK && sl.nflag.alloc(c, sizeof(int)) == MDS_OK &&
+              sl.audit.alloc(c, 4 * sizeof(unsigned long long)) == MDS_OK &&
               sl.derr.alloc(c, 4 * sizeof(int)) == MDS_OK && sl.rowthr.alloc(c, sizeof(float) * cap) == MDS_OK &&
               (S->pv.nC == 0 || sl.lb.alloc(c, sizeof(float) * (size_t)S->pv.nC * cap) == MDS_OK) &&
               sl.ext.alloc(c, sizeof(double) * (size_t)cap * S->nev) == MDS_OK;
