@@ -333,14 +333,29 @@ def run_pipeline(args):
                 Qo = np.linalg.qr(np.asarray(Vo).T)[0]
                 sv = np.linalg.svd(Qg.T @ Qo, compute_uv=False)
                 st["parity_subspace_min_cos_vs_eigsh"] = float(np.min(sv))
-                # the same for the leading nev-1 vectors, and the gap below the
-                # nev-th eigenvalue (from a GPU run with nev+1): when that gap is
-                # within the tolerance the nev-th direction is not determined
-                sv1 = np.linalg.svd(np.linalg.qr(np.asarray(V[:-1]).T)[0].T @ np.linalg.qr(np.asarray(Vo[:-1]).T)[0],
-                                    compute_uv=False)
-                st["parity_subspace_min_cos_vs_eigsh_first_nev_minus_1"] = float(np.min(sv1))
+                # Eigenvalues equal within 1e-6 (relative) span one space, in
+                # which any orthonormal basis is a valid answer: each GPU
+                # vector's component outside the span of eigsh's vectors of the
+                # same cluster. Vectors whose cluster reaches past the nev-th
+                # eigenvalue (compared with a GPU run for nev+1) are counted
+                # apart: there the last directions are not determined.
                 w1, _, _, _ = c.decomp_sparse(nn, pcol, irow, val, sigma, nev + 1, ncv=ncv, tol=tol)
                 st["gap_nev_to_next"] = float(w1[nev - 1] - w1[nev])
+                Vo_ = np.asarray(Vo)
+                res_c, nb = [], 0
+                for x in range(nev):
+                    d_ = 1e-6 * max(1.0, abs(w[x]))
+                    if abs(w[x] - w1[nev]) <= d_:
+                        nb += 1
+                        continue
+                    S = [y for y in range(nev) if abs(wo[y] - w[x]) <= d_]
+                    B = Vo_[S]
+                    v = np.asarray(V[x])
+                    res_c.append(float(np.linalg.norm(v - B.T @ (B @ v))))
+                st["parity_evecs_cluster_max_residual_vs_eigsh"] = max(res_c) if res_c else None
+                st["parity_evecs_clusters_checked"] = len(res_c)
+                st["parity_evecs_at_nev_boundary"] = nb
+                st["eigenvalues"] = [float(t) for t in w]
                 gaps = [min(abs(wo[x] - wo[y]) for y in range(nev) if y != x) for x in range(nev)]
                 errs = [float(np.max(np.abs(V[x] * np.sign(V[x] @ Vo[x]) - Vo[x])))
                         for x in range(nev) if gaps[x] > 1e-4]
