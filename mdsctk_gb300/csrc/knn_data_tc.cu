@@ -343,7 +343,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     uint32_t acc = 0;
     bool ok = true;
     int cur = -1, rp = 0, seg = 0, g = 0;
-    float rc = INF, gth = INF;
+    float rc = INF;
     // The two warps of a pair meet at their named barrier twice per tile:
     // after the task read and the accumulator wait (whose outcomes are ANDed,
     // so both leave together), and after the appends (before compaction).
@@ -371,7 +371,6 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const float rn = (g < nfit) ? __ldg(nf + g) : 0.0f;
         rc = (g >= nfit) ? INF : corr ? 0.5f - guard * rn : rn * (1.0f - guard);
         S->rslack[r][half] = slack + 2.0f * guard * rn;  // (each half's warp keeps its own copy)
-        gth = (g < nfit) ? __ldcg(rowthr + g) : INF;
       }
       if (task.y < 0) {
         // end of the item: publish the owned rows and clear their state
@@ -403,28 +402,23 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       int cnt = S->cnt2[r][half];
       // screen value = rc + colterm + mul * x.y; a pair passes below the
       // row's threshold (its own list's or another segment's)
-      // (the shared threshold is read one tile ahead, so its L2 latency
-      // overlaps this tile's work; an older value is only larger, which
-      // filters less and stays safe)
-      const float lim = fminf(S->thr[r], gth) - rc;
-      const float gnext = (g < nfit) ? __ldcg(rowthr + g) : INF;
+      const float lim = fminf(S->thr[r], (g < nfit) ? __ldcg(rowthr + g) : INF) - rc;
       const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256 + u * TV_N + 64 * half;
       const int j0 = tile * TV_N + 64 * half;
       const float4* ct4 = reinterpret_cast<const float4*>(colterm + j0);
-      // Four chunks of 16 columns from two 32-column TMEM loads: the second
-      // load is in flight while the first two chunks are screened (one wait
-      // for each). A chunk's passes go into a per-lane bit mask (no branch
-      // per pair) and its values into shared memory; only if some lane has a
-      // pass does the warp run the append loop, over the set bits of each
-      // lane's mask.
-      uint32_t ga[32], gb[32];
-      tmem_ld32(tq, ga);
+      // Four chunks of 16 columns; the next chunk's TMEM load is in flight
+      // while this one is screened. A chunk's passes go into a per-lane bit
+      // mask (no branch per pair) and its values into shared memory; only if
+      // some lane has a pass does the warp run the append loop, over the set
+      // bits of each lane's mask.
+      uint32_t ga[16], gb[16];
+      tmem_ld16(tq, ga);
       tmem_wait_ld();
-      tmem_ld32(tq + 32, gb);
 #pragma unroll
       for (int cc = 0; cc < 4; ++cc) {
-        if (cc == 2) tmem_wait_ld();
-        const uint32_t* cur = (cc < 2) ? (ga + 16 * cc) : (gb + 16 * (cc - 2));
+        uint32_t* cur = (cc & 1) ? gb : ga;
+        uint32_t* nxt = (cc & 1) ? ga : gb;
+        if (cc < 3) tmem_ld16(tq + 16 * (cc + 1), nxt);
         float4 c4[4];
 #pragma unroll
         for (int t4 = 0; t4 < 4; ++t4) c4[t4] = __ldg(ct4 + cc * 4 + t4);
@@ -452,6 +446,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           }
         }
         __syncwarp();
+        if (cc < 3) tmem_wait_ld();
       }
       tc_fence_before();
       __syncwarp();
@@ -459,7 +454,6 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       ++acc;
       if (cnt > lcap) atomicMax(err, 4);  // cannot happen: compaction keeps room for a tile
       S->cnt2[r][half] = min(cnt, lcap);
-      gth = gnext;
       bar_named(pbar, 64);  // both halves of these rows are appended
       // compaction of the owned rows whose regions near full (or first fill)
       for (int x = 0; x < 16; ++x) {
