@@ -318,7 +318,6 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     }
     uint32_t stage = 0, phase = 0, qs = 0;
     bool ok = true;
-    const uint64_t pol_a = l2_policy_evict_last();
     // push one task; false if the wait timed out or the kernel aborts
     auto push = [&](int item, int tile) -> bool {
       const uint32_t slot = qs % TC_TQ, ph = (qs / TC_TQ) & 1;
@@ -412,10 +411,8 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
             unsigned char* st = stages + stage * TC_STAGE_BYTES;
             mbar_expect_tx(&S->full[stage], TC_STAGE_BYTES);
-            // the row tile is read again for every column tile of the item:
-            // its lines are kept in L2 ahead of the streaming column tiles
-            tma_load_2d_hint(st, &tmA, &S->full[stage], kb * TC_KB, rt * TC_M, pol_a);
-            tma_load_2d_hint(st + TC_A_BYTES, &tmA, &S->full[stage], Ap + kb * TC_KB, rt * TC_M, pol_a);
+            tma_load_2d(st, &tmA, &S->full[stage], kb * TC_KB, rt * TC_M);
+            tma_load_2d(st + TC_A_BYTES, &tmA, &S->full[stage], Ap + kb * TC_KB, rt * TC_M);
             tma_load_2d(st + 2 * TC_A_BYTES, &tmB, &S->full[stage], kb * TC_KB, tile * TC_N);
             tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, &S->full[stage], Ap + kb * TC_KB, tile * TC_N);
             if (++stage == TC_STAGES) { stage = 0; phase ^= 1; }
