@@ -49,9 +49,11 @@ extern "C" {
 #define MDS_PREC_BF16X3 0x10u /* candidate screen on tcgen05, split BF16 (3 products) */
 #define MDS_PREC_FP16X3 0x20u /* candidate screen on tcgen05, split FP16 (3 products) */
 #define MDS_PREC_MASK 0xF0u
-#define MDS_NO_SKIP 0x100u    /* knn_rms, tensor-core screen: compute every tile
-                                 (no triangle-inequality tile skipping). Same
-                                 results; for timing the screens like for like */
+#define MDS_NO_SKIP 0x100u    /* knn_rms and knn_data, tensor-core screen:
+                                 compute every tile (no triangle-inequality tile
+                                 skipping; knn_data also keeps the input order).
+                                 Same results; for timing the screens like for
+                                 like */
 
 typedef struct mds_ctx mds_ctx;
 

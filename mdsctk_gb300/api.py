@@ -166,13 +166,17 @@ class Context:
         return dev, rec
 
     def knn_data(self, ref, fit=None, k: int = 1, correlation: bool = False, sort: bool = True,
-                 precision: str = "fp32", out=None):
+                 precision: str = "fp32", out=None, skip: bool = True):
         """knn_data: k nearest reference vectors (Euclidean, or correlation
-        distance). ref/fit: [n, dim] float64. Returns (distances, indices)."""
+        distance). ref/fit: [n, dim] float64. Returns (distances, indices).
+        skip=False: the tensor-core screen computes every tile in the input
+        order (same results; MDS_NO_SKIP)."""
         dev = _is_device(ref)
         n_ref, dim = int(ref.shape[0]), int(ref.shape[1])
         n_fit = n_ref if fit is None else int(fit.shape[0])
         flags = L.PRECISIONS[precision]
+        if not skip:
+            flags |= L.MDS_NO_SKIP
         if correlation:
             flags |= L.MDS_CORRELATION
         if not sort:

@@ -170,7 +170,7 @@ static int knn_rms_impl(mds_ctx* ctx, const float* ref_xyz, int n_ref, const flo
 }
 
 int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit, int nfit, int dim, int k,
-                 bool corr, bool full, unsigned prec, double* dout_d, int* dout_i);
+                 bool corr, bool full, unsigned prec, bool noskip, double* dout_d, int* dout_i);
 
 extern "C" int mds_knn_data(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, int n_fit, int dim,
                             int k, unsigned flags, double* out_d, int32_t* out_i, int* k_used) {
@@ -218,7 +218,8 @@ extern "C" int mds_knn_data(mds_ctx* ctx, const double* ref, int n_ref, const do
     pd = dd.as<double>();
     pi = di.as<int>();
   }
-  MDS_TRY(knn_data_run(ctx, pr, n_ref, fit ? pf : nullptr, n_fit, dim, k, corr, full, prec, pd, pi));
+  MDS_TRY(knn_data_run(ctx, pr, n_ref, fit ? pf : nullptr, n_fit, dim, k, corr, full, prec,
+                       (flags & MDS_NO_SKIP) != 0, pd, pi));
   if (!dev) {
     MDS_CUDA(ctx, cudaMemcpyAsync(out_d, pd, sizeof(double) * width * n_fit, cudaMemcpyDeviceToHost, s));
     MDS_CUDA(ctx, cudaMemcpyAsync(out_i, pi, sizeof(int) * width * n_fit, cudaMemcpyDeviceToHost, s));

@@ -178,8 +178,15 @@ int tcv_max_kprime();
 int tcv_max_dp();
 int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref);
 int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
-                      int nref, int Dp, bool corr, int Kp, int k, int nseg, bool same, uint64_t* candout, int* cand_n,
-                      float* rowthr);
+                      int nref, int Dp, bool corr, int Kp, int k, int nseg, bool same, bool order, uint64_t* candout,
+                      int* cand_n, float* rowthr, long long* tiles);
+
+// locality order and tile bounds of a vector set (vec_order.cu)
+int vec_order_max_dp();
+int vec_order(mds_ctx* ctx, const float* X, int n, int Dp, float* cent, bool fit, int* perm);
+int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
+                    int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall);
+int vec_unsort(mds_ctx* ctx, const float* src, const int* perm, int n, float* dst);
 
 // Tile skipping data of the tensor-core screen (knn_rms_tc.cu): lower
 // bounds of RMSD from every fit frame to the pivot of every column tile

@@ -394,7 +394,7 @@ static size_t data_recheck_smem(int dim, int Kp, int nseg, int k, int mode) {
 // host driver
 // ---------------------------------------------------------------------------
 int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit, int nfit, int dim, int k,
-                 bool corr, bool full, unsigned prec, double* dout_d, int* dout_i) {
+                 bool corr, bool full, unsigned prec, bool noskip, double* dout_d, int* dout_i) {
   cudaStream_t s = ctx->stream;
   mds_knn_stats& st = ctx->stats;
   const bool same = (dfit == nullptr);
@@ -497,8 +497,10 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   st.screen_launches = 1;
   if (tc) {
     MDS_TRY(rthr.alloc(ctx, sizeof(float) * (size_t)nfit));
+    long long tiles = 0;
     MDS_TRY(launch_screen_tcv(ctx, xf, nfp, nfit, Xr.as<float>(), Nrm.as<float>(), nref, Dp, corr, Kp, k, nseg, same,
-                              cand.as<uint64_t>(), cand_n.as<int>(), rthr.as<float>()));
+                              !noskip, cand.as<uint64_t>(), cand_n.as<int>(), rthr.as<float>(), &tiles));
+    st.screen_pairs = tiles * 256LL * 128LL;
   } else {
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_screen_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     st.launches++;

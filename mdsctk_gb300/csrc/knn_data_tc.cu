@@ -57,19 +57,23 @@
 // reference vector (the screen value is row term + column term - 2 x.y, or
 // - x.y/2 for correlation): |y|^2 (1 - c), or -c |y|^2; +inf beyond n.
 // With nmax != nullptr (zeroed by the caller) also the largest norm of the n
-// vectors, as the float's bits (norms are non-negative).
+// vectors, as the float's bits (norms are non-negative). perm (or null): row
+// r is vector perm[r] (the locality order of vec_order.cu); nsorted (or
+// null) receives the norms in that order.
 __global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows, __nv_bfloat16* __restrict__ out,
                             const float* __restrict__ nrm, float guard, int corr, float* __restrict__ terms,
-                            float* __restrict__ nmax) {
+                            float* __restrict__ nmax, const int* __restrict__ perm, float* __restrict__ nsorted) {
   const int64_t total = (int64_t)rows * Dp;
   float mx = 0.0f;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = e / Dp;
     const int d = (int)(e % Dp);
-    if (nmax && d == 0 && r < n) mx = fmaxf(mx, nrm[r]);
+    const int64_t src = (r < n && perm) ? (int64_t)perm[r] : r;
+    if (nmax && d == 0 && r < n) mx = fmaxf(mx, nrm[src]);
+    if (nsorted && d == 0 && r < n) nsorted[r] = nrm[src];
     if (terms && d == 0)
-      terms[r] = (r < n) ? (corr ? -guard * nrm[r] : nrm[r] * (1.0f - guard)) : __int_as_float(0x7f800000);
-    const float x = (r < n) ? X[r * Dp + d] : 0.0f;
+      terms[r] = (r < n) ? (corr ? -guard * nrm[src] : nrm[src] * (1.0f - guard)) : __int_as_float(0x7f800000);
+    const float x = (r < n) ? X[src * Dp + d] : 0.0f;
     const __nv_bfloat16 hi = __float2bfloat16_rn(x);
     const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
     out[r * 2 * Dp + d] = hi;
@@ -112,9 +116,10 @@ __device__ __forceinline__ int tv_tile_order(int i, int t0, int t1, int td) {
 // looser one: every pair the screen left out lies at or above the final
 // threshold, which the recheck verifies against), and write the rest,
 // unsorted, as the segment's candidate list (the recheck sorts the merged
-// lists). Called by the warp owning the row.
+// lists), with the column indices mapped through cperm when the columns are
+// in locality order. Called by the warp owning the row.
 __device__ __forceinline__ void tv_publish(uint64_t* src, int c0, int c1, int lcap, int Kp, float tp, int* hist,
-                                           uint64_t* dst, int* dst_n, int lane) {
+                                           uint64_t* dst, int* dst_n, int lane, const int* cperm) {
   if (c0 + c1 > Kp) {
     warp_select_keep2(src, c0, lcap, c1, Kp, hist, lane);
     c0 = Kp;
@@ -129,7 +134,9 @@ __device__ __forceinline__ void tv_publish(uint64_t* src, int c0, int c1, int lc
       const uint64_t key = (x < n) ? from[x] : MDS_KEY_INF;
       const bool keep = x < n && mds_key_value(key) <= tp;
       const unsigned bal = __ballot_sync(0xffffffffu, keep);
-      if (keep) dst[m + __popc(bal & ((1u << lane) - 1u))] = key;
+      if (keep)
+        dst[m + __popc(bal & ((1u << lane) - 1u))] =
+            cperm ? mds_pack_key(mds_key_value(key), __ldg(cperm + mds_key_index(key))) : key;
       m += __popc(bal);
     }
   }
@@ -142,8 +149,19 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
              const float* __restrict__ nf, const float* __restrict__ colterm, int nfit, int Nr, int Dp, int nst,
              int corr, float guard, uint32_t idesc, int Kp, int nseg, int nitems, int diag, int pilot,
              float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
-             int* __restrict__ cand_n, int* __restrict__ err, int lcap, int k1, const float* __restrict__ nmax) {
-  // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host).
+             int* __restrict__ cand_n, int* __restrict__ err, int lcap, int k1, const float* __restrict__ nmax,
+             const float* __restrict__ dlo, const int* __restrict__ tdv, const int* __restrict__ rperm,
+             const int* __restrict__ cperm) {
+  // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host);
+  // err[2]: column tiles computed (added to).
+  // Locality order (vec_order.cu; all four null without it): rows and columns
+  // are in sorted order, rperm/cperm map them to the original indices, which
+  // the published lists carry (rowthr stays in sorted order). dlo [row pair
+  // tile][column tile]: the lower bound of the distance of the tile's pairs;
+  // the producer skips a tile when dlo^2 is at least the largest threshold of
+  // the item's rows. tdv: the visit's start tile ([item] for the pilot,
+  // [row pair tile][segment] otherwise) when the set is not screened against
+  // itself.
   // pilot > 0: a pass that only seeds rowthr: each item (one per row pair
   // tile, nseg = 1) visits `pilot` column tiles (outward from the diagonal
   // for a set against itself, else spread over the set) and lowers each
@@ -208,53 +226,99 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
+    // Lane 0 claims items, issues the copies and publishes the tasks; with
+    // tile bounds the whole warp decides, 32 visit steps at a time, which
+    // tiles to skip.
+    uint32_t stage = 0, phase = 0, qs = 0, na = 0;
+    int ok = 1, nvis = 0;
     if (lane == 0) {
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
-      uint32_t stage = 0, phase = 0, qs = 0, na = 0;
-      bool ok = true;
-      auto push = [&](int item, int tile) -> bool {
-        const uint32_t slot = qs % TV_TQ, ph = (qs / TV_TQ) & 1;
-        ++qs;
-        if (!mbar_wait(&S->tq_empty[slot], ph ^ 1, abortf, 1000000000ull, 1024)) return false;
-        S->task[slot] = make_int2(item, tile);
-        mbar_arrive(&S->tq_full[slot]);
-        return true;
-      };
-      while (ok) {
-        const int item = atomicAdd(err + 1, 1);
-        if (item >= nitems) {
-          ok = push(-1, -1);
-          break;
+    }
+    auto push = [&](int item, int tile) -> bool {
+      const uint32_t slot = qs % TV_TQ, ph = (qs / TV_TQ) & 1;
+      ++qs;
+      if (!mbar_wait(&S->tq_empty[slot], ph ^ 1, abortf, 1000000000ull, 1024)) return false;
+      S->task[slot] = make_int2(item, tile);
+      mbar_arrive(&S->tq_full[slot]);
+      return true;
+    };
+    while (ok) {
+      int item = 0;
+      if (lane == 0) item = atomicAdd(err + 1, 1);
+      item = __shfl_sync(0xffffffffu, item, 0);
+      if (item >= nitems) {
+        if (lane == 0) ok = push(-1, -1);
+        break;
+      }
+      const int rp = item / nseg, seg = item % nseg;
+      const int t0 = pilot ? 0 : (int)((int64_t)ncoltiles * seg / nseg);
+      const int t1 = pilot ? ncoltiles : (int)((int64_t)ncoltiles * (seg + 1) / nseg);
+      const int nvisit = pilot ? pilot : t1 - t0;
+      const int td = diag ? min(max((rp * TV_ROWS + TV_ROWS / 2) / TV_N, t0), t1 - 1)
+                          : (tdv ? min(max(__ldg(tdv + (pilot ? rp : item)), t0), t1 - 1) : t0);
+      const bool spread = pilot && !diag && !tdv;
+      // the resident rows: wait until the MMAs of the previous item are done
+      if (lane == 0) {
+        if (na > 0 && !mbar_wait(&S->aempty, (na - 1) & 1, abortf, 1000000000ull, 1024)) {
+          ok = 0;
+        } else {
+          mbar_expect_tx(&S->afull, (uint32_t)(TV_ROWS * 2 * Dp * 2));
+          for (int u = 0; u < 2; ++u)
+            for (int kb = 0; kb < nkb; ++kb)
+              for (int p = 0; p < 2; ++p)
+                tma_load_2d(arows + (size_t)((u * nkb + kb) * 2 + p) * TV_SUB_BYTES, &tmA, &S->afull,
+                            p * Dp + kb * TV_KB, (2 * rp + u) * 128);
         }
-        const int rp = item / nseg, seg = item % nseg;
-        const int t0 = pilot ? 0 : (int)((int64_t)ncoltiles * seg / nseg);
-        const int t1 = pilot ? ncoltiles : (int)((int64_t)ncoltiles * (seg + 1) / nseg);
-        const int nvisit = pilot ? pilot : t1 - t0;
-        const int td = diag ? min(max((rp * TV_ROWS + TV_ROWS / 2) / TV_N, t0), t1 - 1) : t0;
-        // the resident rows: wait until the MMAs of the previous item are done
-        if (na > 0 && !mbar_wait(&S->aempty, (na - 1) & 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
-        mbar_expect_tx(&S->afull, (uint32_t)(TV_ROWS * 2 * Dp * 2));
-        for (int u = 0; u < 2; ++u)
-          for (int kb = 0; kb < nkb; ++kb)
-            for (int p = 0; p < 2; ++p)
-              tma_load_2d(arows + (size_t)((u * nkb + kb) * 2 + p) * TV_SUB_BYTES, &tmA, &S->afull,
-                          p * Dp + kb * TV_KB, (2 * rp + u) * 128);
-        ++na;
-        for (int ti = 0; ti < nvisit && ok; ++ti) {
-          const int tile = (pilot && !diag) ? (int)((int64_t)ti * ncoltiles / pilot) : tv_tile_order(ti, t0, t1, td);
-          if (!(ok = push(item, tile))) break;
-          for (int kb = 0; kb < nkb; ++kb) {
-            if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = false; break; }
-            unsigned char* st = stages + stage * TV_STAGE_BYTES;
-            mbar_expect_tx(&S->full[stage], TV_STAGE_BYTES);
-            tma_load_2d(st, &tmB, &S->full[stage], kb * TV_KB, tile * TV_N);
-            tma_load_2d(st + TV_SUB_BYTES, &tmB, &S->full[stage], Dp + kb * TV_KB, tile * TV_N);
-            if (++stage == (uint32_t)nst) { stage = 0; phase ^= 1; }
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      ++na;
+      const float* dl = (dlo && !pilot) ? dlo + (int64_t)rp * ncoltiles : nullptr;
+      for (int base = 0; base < nvisit && ok; base += 32) {
+        unsigned skip = 0u;
+        if (dl) {
+          // the largest threshold of the item's rows now (rowthr holds each
+          // row's smallest, its own list's included)
+          float mx = 0.0f;
+          for (int x = lane; x < TV_ROWS; x += 32) {
+            const int gx = rp * TV_ROWS + x;
+            if (gx < nfit) mx = fmaxf(mx, __ldcg(rowthr + gx));
+          }
+          for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+          bool sk = false;
+          if (base + lane < nvisit) {
+            const float b = __ldg(dl + tv_tile_order(base + lane, t0, t1, td));
+            sk = b > 0.0f && b * b >= mx;
+          }
+          skip = __ballot_sync(0xffffffffu, sk);
+        }
+        if (lane == 0) {
+          const int nb = min(32, nvisit - base);
+          for (int i = 0; i < nb && ok; ++i) {
+            if ((skip >> i) & 1u) continue;
+            const int ti = base + i;
+            const int tile = spread ? (int)((int64_t)ti * ncoltiles / pilot) : tv_tile_order(ti, t0, t1, td);
+            if (!(ok = push(item, tile))) break;
+            ++nvis;
+            for (int kb = 0; kb < nkb; ++kb) {
+              if (!mbar_wait(&S->empty[stage], phase ^ 1, abortf, 1000000000ull, 1024)) { ok = 0; break; }
+              unsigned char* st = stages + stage * TV_STAGE_BYTES;
+              mbar_expect_tx(&S->full[stage], TV_STAGE_BYTES);
+              tma_load_2d(st, &tmB, &S->full[stage], kb * TV_KB, tile * TV_N);
+              tma_load_2d(st + TV_SUB_BYTES, &tmB, &S->full[stage], Dp + kb * TV_KB, tile * TV_N);
+              if (++stage == (uint32_t)nst) { stage = 0; phase ^= 1; }
+            }
           }
         }
-        if (ok) ok = push(item, -1);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
       }
+      if (!ok) break;
+      if (lane == 0) ok = push(item, -1);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+    }
+    if (lane == 0) {
+      if (nvis) atomicAdd(err + 2, nvis);
       if (!ok) {
         atomicMax(err, 1);
         *abortf = 1;
@@ -279,14 +343,14 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const int2 t = make_int2(tv[0], tv[1]);
         mbar_arrive(&S->tq_empty[slot]);
         if (t.x < 0) break;
-        if (t.y < 0) {  // end of the item: the resident rows are free when these MMAs are done
-          umma_commit(&S->aempty);
-          continue;
-        }
-        if (t.x != cur) {
+        if (t.x != cur) {  // a new item's rows (consumed even when every tile was skipped)
           cur = t.x;
           if (!mbar_wait(&S->afull, na & 1, abortf, 1000000000ull, 64)) { ok = false; break; }
           ++na;
+        }
+        if (t.y < 0) {  // end of the item: the resident rows are free when these MMAs are done
+          umma_commit(&S->aempty);
+          continue;
         }
         const uint32_t b = acc & 1, aph = (acc >> 1) & 1;
         if (!mbar_wait(&S->tempty[b], aph ^ 1, abortf, 1000000000ull, 64)) { ok = false; break; }
@@ -379,8 +443,9 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           const int gg = rp * TV_ROWS + rr;
           if (gg < nfit && !pilot) {
             const float tp = fminf(S->thr[rr], __ldcg(rowthr + gg));
+            const int64_t go = rperm ? (int64_t)__ldg(rperm + gg) : gg;
             tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], S->cnt2[rr][1], lcap, Kp, tp, hist,
-                       candout + ((int64_t)gg * nseg + seg) * Kp, cand_n + (int64_t)gg * nseg + seg, lane);
+                       candout + (go * nseg + seg) * Kp, cand_n + go * nseg + seg, lane, cperm);
           } else if (gg < nfit && S->cnt2[rr][0] + S->cnt2[rr][1] >= k1) {
             const int c = S->cnt2[rr][0] + S->cnt2[rr][1];
             float tk1 = INF;
@@ -513,57 +578,96 @@ int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref) {
 // The tensor-core screen of knn_data. Xf/Xr: FP32 vectors [n][Dp] (Dp a
 // multiple of 32, at most TV_MAX_DP), nf/nr their squared norms. same: Xf is
 // Xr (a set screened against itself; the visit starts at the diagonal).
-// Writes the candidate lists candout [nfit][nseg][Kp] (each unsorted), their
-// sizes cand_n [nfit][nseg], and rowthr [nfit]: the threshold below which a
-// row's pairs were kept (the bound of every pair left out when a row's lists
-// hold fewer than K' in all).
+// order: screen in locality order with tile skipping (vec_order.cu; the
+// Euclidean metric only). Writes the candidate lists candout [nfit][nseg][Kp]
+// (each unsorted), their sizes cand_n [nfit][nseg], and rowthr [nfit]: the
+// threshold below which a row's pairs were kept (the bound of every pair left
+// out when a row's lists hold fewer than K' in all). *tiles: the column tiles
+// computed (TV_ROWS x TV_N pairs each), pilot pass included.
 int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, const float* Xr, const float* nr,
-                      int nref, int Dp, bool corr, int Kp, int k, int nseg, bool same, uint64_t* candout, int* cand_n,
-                      float* rowthr) {
+                      int nref, int Dp, bool corr, int Kp, int k, int nseg, bool same, bool order, uint64_t* candout,
+                      int* cand_n, float* rowthr, long long* tiles) {
   if (Kp > tcv_max_kprime()) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: K' too large");
   if (Dp % TV_KB || Dp > TV_MAX_DP)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core vector screen: padded dimension %d", Dp);
   const int ncoltiles = (nref + TV_N - 1) / TV_N;
   if (nseg < 1 || nseg > ncoltiles) return mds_fail(ctx, MDS_ERR_INTERNAL, "bad segment count %d", nseg);
+  // (below 16 column tiles the order is not worth its launches)
+  if (order && (corr || Dp > vec_order_max_dp() || nref < 16 * TV_N)) order = false;
   cudaStream_t s = ctx->stream;
   const int rowsA = (nfit + TV_ROWS - 1) / TV_ROWS * TV_ROWS, rowsB = ncoltiles * TV_N;
   const int rowsS = std::max(rowsA, rowsB);
+  const int nrp = rowsA / TV_ROWS;
   DevBuf A(ctx), B(ctx), work(ctx), err(ctx), terms(ctx), nmax(ctx);
+  DevBuf cent(ctx), permr(ctx), permf(ctx), nrs(ctx), nfs(ctx), dlo(ctx), tdseg(ctx), tdall(ctx), rts(ctx);
   MDS_TRY(terms.alloc(ctx, sizeof(float) * (size_t)rowsS));
   MDS_TRY(nmax.alloc(ctx, sizeof(float)));
   MDS_CUDA(ctx, cudaMemsetAsync(nmax.p, 0, sizeof(float), s));
+  const int* pr = nullptr;
+  const int* pf = nullptr;
+  if (order) {
+    MDS_TRY(cent.alloc(ctx, sizeof(float) * 16 * (size_t)Dp));
+    MDS_TRY(permr.alloc(ctx, sizeof(int) * (size_t)nref));
+    MDS_TRY(nrs.alloc(ctx, sizeof(float) * (size_t)nref));
+    MDS_TRY(vec_order(ctx, Xr, nref, Dp, cent.as<float>(), true, permr.as<int>()));
+    pr = permr.as<int>();
+    if (same) {
+      pf = pr;
+    } else {
+      MDS_TRY(permf.alloc(ctx, sizeof(int) * (size_t)nfit));
+      MDS_TRY(nfs.alloc(ctx, sizeof(float) * (size_t)nfit));
+      MDS_TRY(vec_order(ctx, Xf, nfit, Dp, cent.as<float>(), false, permf.as<int>()));
+      pf = permf.as<int>();
+    }
+  }
   // list regions: a compaction is due once a region holds more than
   // lcap - 64 keys (room for one tile's half); lcap - 64 - K' appends
   // between compactions keep them rare
   const int lcap = TV_LCAP;
-  auto split = [&](const float* X, int n, int rows, DevBuf& out, float* t) -> int {
+  auto split = [&](const float* X, const float* nrm, int n, int rows, DevBuf& out, float* t, const int* perm,
+                   float* nsorted) -> int {
     MDS_TRY(out.alloc(ctx, sizeof(__nv_bfloat16) * 2 * (size_t)Dp * rows));
     const int64_t total = (int64_t)rows * Dp;
     const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 16);
     ctx->stats.launches++;
-    k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>(), nr, MDS_GUARD_TC, corr ? 1 : 0, t,
-                                     t ? nmax.as<float>() : nullptr);
+    k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>(), nrm, MDS_GUARD_TC, corr ? 1 : 0, t,
+                                     t ? nmax.as<float>() : nullptr, perm, nsorted);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
   const void* pA;
+  const float* nfk = nf;  // row norms in the screen's row order
   if (same) {  // one split array serves both roles (rows padded to the larger tiling)
-    MDS_TRY(split(Xr, nref, rowsS, B, terms.as<float>()));
+    MDS_TRY(split(Xr, nr, nref, rowsS, B, terms.as<float>(), pr, order ? nrs.as<float>() : nullptr));
     pA = B.p;
+    if (order) nfk = nrs.as<float>();
   } else {
-    MDS_TRY(split(Xr, nref, rowsB, B, terms.as<float>()));
-    MDS_TRY(split(Xf, nfit, rowsA, A, nullptr));
+    MDS_TRY(split(Xr, nr, nref, rowsB, B, terms.as<float>(), pr, nullptr));
+    MDS_TRY(split(Xf, nf, nfit, rowsA, A, nullptr, pf, order ? nfs.as<float>() : nullptr));
     pA = A.p;
+    if (order) nfk = nfs.as<float>();
+  }
+  float* rt = rowthr;  // thresholds in the screen's row order
+  if (order) {
+    MDS_TRY(dlo.alloc(ctx, sizeof(float) * (size_t)nrp * ncoltiles));
+    if (!same) {
+      MDS_TRY(tdseg.alloc(ctx, sizeof(int) * (size_t)nrp * nseg));
+      MDS_TRY(tdall.alloc(ctx, sizeof(int) * (size_t)nrp));
+    }
+    MDS_TRY(vec_tile_bounds(ctx, Xr, pr, nref, Xf, pf, nfit, Dp, TV_N, nmax.as<float>(), dlo.as<float>(), nseg,
+                            same ? nullptr : tdseg.as<int>(), same ? nullptr : tdall.as<int>()));
+    MDS_TRY(rts.alloc(ctx, sizeof(float) * (size_t)nfit));
+    rt = rts.as<float>();
   }
   CUtensorMap mA, mB;
   MDS_TRY(encode_map(ctx, &mA, pA, same ? rowsS : rowsA, Dp, 128, MDS_PREC_BF16X3));
   MDS_TRY(encode_map(ctx, &mB, B.p, same ? rowsS : rowsB, Dp, TV_N, MDS_PREC_BF16X3));
-  const int nitems = rowsA / TV_ROWS * nseg;
+  const int nitems = nrp * nseg;
   const int grid = std::min(nitems, ctx->num_sms);
   MDS_TRY(work.alloc(ctx, sizeof(uint64_t) * (size_t)grid * TV_ROWS * TC_CAPG));
-  MDS_TRY(err.alloc(ctx, 2 * sizeof(int)));
-  MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, 2 * sizeof(int), s));
-  MDS_CUDA(ctx, cudaMemsetAsync(rowthr, 0x7f, sizeof(float) * (size_t)nfit, s));
+  MDS_TRY(err.alloc(ctx, 4 * sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, 4 * sizeof(int), s));
+  MDS_CUDA(ctx, cudaMemsetAsync(rt, 0x7f, sizeof(float) * (size_t)nfit, s));
   const int nst = (Dp <= 64) ? 4 : (Dp <= 96 ? 3 : 2);
   const size_t smem = tv_smem_bytes(Dp, nst);
   static bool attr_done = false;
@@ -572,29 +676,33 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   if (smem > attr_limit)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "vector screen needs %zu bytes of shared memory", smem);
   const uint32_t idesc = umma_idesc_f16(128, TV_N, 1);
+  const float* pdlo = order ? dlo.as<float>() : nullptr;
+  const int* ptdseg = (order && !same) ? tdseg.as<int>() : nullptr;
+  const int* ptdall = (order && !same) ? tdall.as<int>() : nullptr;
   // pilot pass: seed every row's threshold from TV_PILOT column tiles, so the
   // main pass appends few pairs from its first tile on
   if (ncoltiles >= 4 * TV_PILOT) {
-    const int npilot = rowsA / TV_ROWS;
     ctx->stats.launches++;
-    k_screen_tcv<<<std::min(npilot, ctx->num_sms), TV_THREADS, smem, s>>>(
-        mA, mB, nf, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC, idesc, Kp, 1, npilot,
-        same ? 1 : 0, TV_PILOT, rowthr, work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
-        nmax.as<float>());
+    k_screen_tcv<<<std::min(nrp, ctx->num_sms), TV_THREADS, smem, s>>>(
+        mA, mB, nfk, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC, idesc, Kp, 1, nrp,
+        same ? 1 : 0, TV_PILOT, rt, work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
+        nmax.as<float>(), pdlo, ptdall, pr ? pf : nullptr, pr);
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaMemsetAsync(err.as<int>() + 1, 0, sizeof(int), s));
   }
   ctx->stats.launches++;
-  k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nf, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0,
-                                              MDS_GUARD_TC, idesc, Kp, nseg, nitems, same ? 1 : 0, 0, rowthr,
+  k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nfk, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0,
+                                              MDS_GUARD_TC, idesc, Kp, nseg, nitems, same ? 1 : 0, 0, rt,
                                               work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
-                                              nmax.as<float>());
+                                              nmax.as<float>(), pdlo, ptdseg, pr ? pf : nullptr, pr);
   MDS_CUDA(ctx, cudaGetLastError());
-  int herr = 0;
-  MDS_CUDA(ctx, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (order) MDS_TRY(vec_unsort(ctx, rt, pf, nfit, rowthr));
+  int herr[3] = {0, 0, 0};
+  MDS_CUDA(ctx, cudaMemcpyAsync(herr, err.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));
-  if (herr)
-    return mds_fail(ctx, herr == 4 ? MDS_ERR_INTERNAL : MDS_ERR_TIMEOUT,
-                    "tensor-core vector screen failed (code %d)", herr);
+  if (herr[0])
+    return mds_fail(ctx, herr[0] == 4 ? MDS_ERR_INTERNAL : MDS_ERR_TIMEOUT,
+                    "tensor-core vector screen failed (code %d)", herr[0]);
+  if (tiles) *tiles = herr[2];
   return MDS_OK;
 }

@@ -1,0 +1,382 @@
+// vec_order.cu -- locality order and tile bounds for the tensor-core vector
+// screen of knn_data (knn_data_tc.cu).
+//
+// knn_data.cpp:195-250 compares every fit vector with every reference vector.
+// Its inputs (sin/cos of dihedral angles, or any feature vectors) need not be
+// stored in any useful order, so the screen's column tiles are, for a given
+// row, a random sample of the set: its threshold tightens slowly, and no tile
+// can be left out. This file reorders both sets so that tiles are compact,
+// and bounds, for every (row pair tile, column tile), the distance of any of
+// its pairs from below:
+//
+//  1. k-means with VO_CENT centroids (Lloyd iterations, the centroids seeded
+//     with evenly spaced vectors), then a stable sort by (centroid, distance
+//     to it quantised to 12 bits): a tile holds vectors of one cluster at
+//     about one distance from its centroid. The order changes which pairs the
+//     screen computes, never the result: the recheck works on the original
+//     indices and recomputes every candidate exactly.
+//  2. Per column tile, its centre c (FP32 mean of its vectors) and radius
+//     rho = max |y - c| (accumulated in FP64 against the FP32 centre, rounded
+//     up).
+//  3. Per row pair tile I and column tile T, dlo = min over the rows x of I of
+//     |x - c_T| (FP32, shrunk by a relative 3e-5 for its rounding) minus rho_T
+//     minus an absolute margin for the rounding of the inputs to FP32. By the
+//     triangle inequality every pair (x in I, y in T) has |x - y| >= dlo: when
+//     dlo > 0 and dlo^2 is at least every row's current threshold, none of
+//     the tile's pairs can enter any row's list, and the screen skips it.
+//     Also the start tile of each (row pair tile, column segment) visit: the
+//     one with the smallest dlo.
+#include <algorithm>
+
+#include "knn_common.cuh"
+
+#define VO_CENT 16
+#define VO_ITERS 6
+#define VO_MAXDP 128
+#define VO_QBITS 12
+
+// centroid c := vector (2c + 1) n / (2 VO_CENT)
+__global__ void k_vo_seed(const float* __restrict__ X, int n, int Dp, float* __restrict__ cent) {
+  const int c = blockIdx.x;
+  const int64_t v = (int64_t)(2 * c + 1) * n / (2 * VO_CENT);
+  for (int d = threadIdx.x; d < Dp; d += blockDim.x) cent[c * Dp + d] = X[v * Dp + d];
+}
+
+// Nearest centroid of each vector. sums/counts (zeroed by the caller): the
+// FP64 sums and counts of each centroid's vectors, for the next centroids.
+// keys/vals: (centroid << 12 | distance quantised against *dmax) and the
+// vector's index, for the sort; dist/dmax: the distance to the nearest
+// centroid and (float bits) the largest one, for that quantisation.
+__global__ void __launch_bounds__(256) k_vo_assign(const float* __restrict__ X, int n, int Dp,
+                                                   const float* __restrict__ cent, double* __restrict__ sums,
+                                                   int* __restrict__ counts, float* __restrict__ dist,
+                                                   unsigned* __restrict__ dmax, int* __restrict__ label) {
+  __shared__ float cs[VO_CENT * VO_MAXDP];
+  __shared__ double ss[VO_CENT * VO_MAXDP];
+  __shared__ int sc[VO_CENT];
+  for (int e = threadIdx.x; e < VO_CENT * Dp; e += blockDim.x) {
+    cs[e] = cent[e];
+    if (sums) ss[e] = 0.0;
+  }
+  if (threadIdx.x < VO_CENT) sc[threadIdx.x] = 0;
+  __syncthreads();
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  float best = __int_as_float(0x7f800000);
+  int bl = 0;
+  if (v < n) {
+    const float4* x4 = reinterpret_cast<const float4*>(X + (int64_t)v * Dp);
+    float acc[VO_CENT];
+#pragma unroll
+    for (int c = 0; c < VO_CENT; ++c) acc[c] = 0.0f;
+    for (int q = 0; q < Dp / 4; ++q) {
+      const float4 xv = x4[q];
+#pragma unroll
+      for (int c = 0; c < VO_CENT; ++c) {
+        const float* cc = cs + c * Dp + 4 * q;
+        float e = xv.x - cc[0];
+        acc[c] = fmaf(e, e, acc[c]);
+        e = xv.y - cc[1];
+        acc[c] = fmaf(e, e, acc[c]);
+        e = xv.z - cc[2];
+        acc[c] = fmaf(e, e, acc[c]);
+        e = xv.w - cc[3];
+        acc[c] = fmaf(e, e, acc[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < VO_CENT; ++c)
+      if (acc[c] < best) {
+        best = acc[c];
+        bl = c;
+      }
+    if (sums) {
+      for (int d = 0; d < Dp; ++d) atomicAdd(&ss[bl * Dp + d], (double)X[(int64_t)v * Dp + d]);
+      atomicAdd(&sc[bl], 1);
+    }
+    if (dist) {
+      const float dv = sqrtf(best);
+      dist[v] = dv;
+      label[v] = bl;
+      atomicMax(dmax, __float_as_uint(dv));
+    }
+  }
+  if (sums) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < VO_CENT * Dp; e += blockDim.x)
+      if (ss[e] != 0.0) atomicAdd(&sums[e], ss[e]);
+    if (threadIdx.x < VO_CENT && sc[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sc[threadIdx.x]);
+  }
+}
+
+// New centroids from the sums (a centroid without vectors stays); the sums
+// and counts are cleared for the next iteration.
+__global__ void k_vo_update(float* __restrict__ cent, double* __restrict__ sums, int* __restrict__ counts, int Dp) {
+  const int c = blockIdx.x;
+  const int cnt = counts[c];
+  for (int d = threadIdx.x; d < Dp; d += blockDim.x) {
+    if (cnt > 0) cent[c * Dp + d] = (float)(sums[c * Dp + d] / cnt);
+    sums[c * Dp + d] = 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) counts[c] = 0;
+}
+
+__global__ void k_vo_keys(const int* __restrict__ label, const float* __restrict__ dist,
+                          const unsigned* __restrict__ dmax, int n, unsigned long long* __restrict__ keys,
+                          int64_t* __restrict__ vals) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const float dm = __uint_as_float(*dmax);
+  const float qs = (dm > 0.0f) ? (float)(1 << VO_QBITS) / dm : 0.0f;
+  const int q = min((1 << VO_QBITS) - 1, (int)(dist[v] * qs));
+  keys[v] = ((unsigned long long)label[v] << VO_QBITS) | (unsigned)q;
+  vals[v] = v;
+}
+
+__global__ void k_vo_perm(const int64_t* __restrict__ vals, int n, int* __restrict__ perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) perm[i] = (int)vals[i];
+}
+
+// Column tile T = sorted vectors [T * tile, T * tile + tile): FP32 centre and
+// radius (rounded up). Block: `tile` threads.
+__global__ void k_vo_tile_geom(const float* __restrict__ X, const int* __restrict__ perm, int n, int Dp, int tile,
+                               float* __restrict__ center, float* __restrict__ rad) {
+  __shared__ float cf[VO_MAXDP];
+  __shared__ float red[32];
+  const int T = blockIdx.x, t = threadIdx.x;
+  const int j0 = T * tile, m = min(tile, n - j0);
+  for (int d = t; d < Dp; d += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < m; ++j) s += (double)X[(int64_t)perm[j0 + j] * Dp + d];
+    cf[d] = (float)(s / m);
+    center[(int64_t)T * Dp + d] = cf[d];
+  }
+  __syncthreads();
+  float r = 0.0f;
+  if (t < m) {
+    const float* y = X + (int64_t)perm[j0 + t] * Dp;
+    double s = 0.0;
+    for (int d = 0; d < Dp; ++d) {
+      const double e = (double)y[d] - (double)cf[d];
+      s += e * e;
+    }
+    r = __double2float_ru(sqrt(s) * (1.0 + 1e-7));
+  }
+  for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+  if ((t & 31) == 0) red[t >> 5] = r;
+  __syncthreads();
+  if (t == 0) {
+    float mx = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) mx = fmaxf(mx, red[w]);
+    rad[T] = mx;
+  }
+}
+
+// dlo[I][T] for the row pair tile I (blockDim.x = 256 sorted rows; rows past
+// n count as absent) and every column tile T. nmax: the reference set's
+// largest squared norm (float), for the absolute margin.
+template <int DP>
+__global__ void __launch_bounds__(256) k_vo_item_lb(const float* __restrict__ X, const int* __restrict__ perm, int n,
+                                                    const float* __restrict__ center, const float* __restrict__ rad,
+                                                    int nct, const float* __restrict__ nmax, float* __restrict__ dlo) {
+  __shared__ __align__(16) float cen[32 * DP];
+  __shared__ float wmin[8][33];
+  const int item = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int g = item * 256 + t;
+  const bool valid = g < n;
+  float x[DP];
+  if (valid) {
+    const float4* x4 = reinterpret_cast<const float4*>(X + (int64_t)perm[g] * DP);
+#pragma unroll
+    for (int q = 0; q < DP / 4; ++q) {
+      const float4 v = x4[q];
+      x[4 * q] = v.x;
+      x[4 * q + 1] = v.y;
+      x[4 * q + 2] = v.z;
+      x[4 * q + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int d = 0; d < DP; ++d) x[d] = 0.0f;
+  }
+  // |x32 - x| <= 2^-24 |x| for each input vector: 2e-6 (|x|max + |y|max)
+  // covers the rounding of both sides with room (nmax: the reference set's
+  // largest squared norm; the rows' own is found here)
+  float xn = 0.0f;
+#pragma unroll
+  for (int d = 0; d < DP; ++d) xn = fmaf(x[d], x[d], xn);
+  xn = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(xn)));
+  if (lane == 0) wmin[w][32] = xn;
+  __syncthreads();
+  for (int k = 0; k < 8; ++k) xn = fmaxf(xn, wmin[k][32]);
+  const float nabs = 2e-6f * (sqrtf(__ldg(nmax)) + sqrtf(xn));
+  for (int T0 = 0; T0 < nct; T0 += 32) {
+    const int nt = min(32, nct - T0);
+    __syncthreads();
+    for (int e = t; e < nt * DP; e += 256) cen[e] = center[(int64_t)T0 * DP + e];
+    __syncthreads();
+    for (int tt = 0; tt < nt; ++tt) {
+      const float4* c4 = reinterpret_cast<const float4*>(cen + tt * DP);
+      float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+      for (int q = 0; q < DP / 4; ++q) {
+        const float4 c = c4[q];
+        float e = x[4 * q] - c.x;
+        s0 = fmaf(e, e, s0);
+        e = x[4 * q + 1] - c.y;
+        s1 = fmaf(e, e, s1);
+        e = x[4 * q + 2] - c.z;
+        s0 = fmaf(e, e, s0);
+        e = x[4 * q + 3] - c.w;
+        s1 = fmaf(e, e, s1);
+      }
+      // squared distances are non-negative: their bits order as unsigned
+      unsigned u = valid ? __float_as_uint(s0 + s1) : 0x7f800000u;
+      u = __reduce_min_sync(0xffffffffu, u);
+      if (lane == 0) wmin[w][tt] = __uint_as_float(u);
+    }
+    __syncthreads();
+    if (w == 0 && lane < nt) {
+      float m = wmin[0][lane];
+#pragma unroll
+      for (int k = 1; k < 8; ++k) m = fminf(m, wmin[k][lane]);
+      const int T = T0 + lane;
+      dlo[(int64_t)item * nct + T] = sqrtf(m) * (1.0f - 3e-5f) - __ldg(rad + T) - nabs;
+    }
+  }
+}
+
+// Start tile of each (row pair tile, segment) visit: the smallest dlo in the
+// segment (lowest tile on ties). blockIdx.y == nseg: over all tiles (the
+// pilot's start). One warp per block.
+__global__ void k_vo_start(const float* __restrict__ dlo, int nct, int nseg, int* __restrict__ tdseg,
+                           int* __restrict__ tdall) {
+  const int item = blockIdx.x, sg = blockIdx.y, lane = threadIdx.x;
+  const int t0 = (sg == nseg) ? 0 : (int)((int64_t)nct * sg / nseg);
+  const int t1 = (sg == nseg) ? nct : (int)((int64_t)nct * (sg + 1) / nseg);
+  const float* row = dlo + (int64_t)item * nct;
+  float bv = __int_as_float(0x7f800000);
+  int bt = t0;
+  for (int T = t0 + lane; T < t1; T += 32) {
+    const float v = row[T];
+    if (v < bv) {
+      bv = v;
+      bt = T;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    const int ot = __shfl_xor_sync(0xffffffffu, bt, o);
+    if (ov < bv || (ov == bv && ot < bt)) {
+      bv = ov;
+      bt = ot;
+    }
+  }
+  if (lane == 0) {
+    if (sg == nseg)
+      tdall[item] = bt;
+    else
+      tdseg[(int64_t)item * nseg + sg] = bt;
+  }
+}
+
+__global__ void k_vo_unsort(const float* __restrict__ src, const int* __restrict__ perm, int n,
+                            float* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[perm[i]] = src[i];
+}
+
+int vec_order_max_dp() { return VO_MAXDP; }
+
+// perm[i] = original index of the i-th vector in locality order. cent
+// ([VO_CENT][Dp]): fit == true computes the centroids (k-means from seeds),
+// else they are given (a second set ordered by the first set's centroids).
+int vec_order(mds_ctx* ctx, const float* X, int n, int Dp, float* cent, bool fit, int* perm) {
+  if (Dp > VO_MAXDP || Dp % 4) return mds_fail(ctx, MDS_ERR_INTERNAL, "vec_order: padded dimension %d", Dp);
+  cudaStream_t s = ctx->stream;
+  DevBuf sums(ctx), counts(ctx), dist(ctx), label(ctx), dmax(ctx), k0(ctx), v0(ctx), k1(ctx), v1(ctx);
+  MDS_TRY(dist.alloc(ctx, sizeof(float) * (size_t)n));
+  MDS_TRY(label.alloc(ctx, sizeof(int) * (size_t)n));
+  MDS_TRY(dmax.alloc(ctx, sizeof(unsigned)));
+  MDS_CUDA(ctx, cudaMemsetAsync(dmax.p, 0, sizeof(unsigned), s));
+  const int nb = (n + 255) / 256;
+  if (fit) {
+    MDS_TRY(sums.alloc(ctx, sizeof(double) * VO_CENT * Dp));
+    MDS_TRY(counts.alloc(ctx, sizeof(int) * VO_CENT));
+    MDS_CUDA(ctx, cudaMemsetAsync(sums.p, 0, sizeof(double) * VO_CENT * Dp, s));
+    MDS_CUDA(ctx, cudaMemsetAsync(counts.p, 0, sizeof(int) * VO_CENT, s));
+    k_vo_seed<<<VO_CENT, 128, 0, s>>>(X, n, Dp, cent);
+    ctx->stats.launches++;
+    for (int it = 0; it < VO_ITERS; ++it) {
+      k_vo_assign<<<nb, 256, 0, s>>>(X, n, Dp, cent, sums.as<double>(), counts.as<int>(), nullptr, nullptr,
+                                     nullptr);
+      k_vo_update<<<VO_CENT, 128, 0, s>>>(cent, sums.as<double>(), counts.as<int>(), Dp);
+      ctx->stats.launches += 2;
+    }
+  }
+  k_vo_assign<<<nb, 256, 0, s>>>(X, n, Dp, cent, nullptr, nullptr, dist.as<float>(), dmax.as<unsigned>(),
+                                 label.as<int>());
+  MDS_TRY(k0.alloc(ctx, sizeof(unsigned long long) * (size_t)n));
+  MDS_TRY(v0.alloc(ctx, sizeof(int64_t) * (size_t)n));
+  MDS_TRY(k1.alloc(ctx, sizeof(unsigned long long) * (size_t)n));
+  MDS_TRY(v1.alloc(ctx, sizeof(int64_t) * (size_t)n));
+  k_vo_keys<<<nb, 256, 0, s>>>(label.as<int>(), dist.as<float>(), dmax.as<unsigned>(), n,
+                               k0.as<unsigned long long>(), v0.as<int64_t>());
+  ctx->stats.launches += 2;
+  MDS_CUDA(ctx, cudaGetLastError());
+  int which = 0;
+  MDS_TRY(radix_sort(ctx, k0.as<unsigned long long>(), v0.as<int64_t>(), k1.as<unsigned long long>(),
+                     v1.as<int64_t>(), n, (1ull << (VO_QBITS + 4)) - 1, &which));
+  k_vo_perm<<<nb, 256, 0, s>>>(which ? v1.as<int64_t>() : v0.as<int64_t>(), n, perm);
+  ctx->stats.launches++;
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+// Column tile geometry of the sorted reference set (tiles of `tile` vectors)
+// and dlo [nitems][nct] of the sorted fit set's row pair tiles (256 rows),
+// with the start tiles tdseg [nitems][nseg] and tdall [nitems] (either may be
+// null). nmax: device float, the reference set's largest squared norm.
+int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
+                    int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall) {
+  cudaStream_t s = ctx->stream;
+  const int nct = (nref + tile - 1) / tile, nitems = (nfit + 255) / 256;
+  DevBuf center(ctx), rad(ctx);
+  MDS_TRY(center.alloc(ctx, sizeof(float) * (size_t)nct * Dp));
+  MDS_TRY(rad.alloc(ctx, sizeof(float) * (size_t)nct));
+  k_vo_tile_geom<<<nct, tile, 0, s>>>(Xr, permr, nref, Dp, tile, center.as<float>(), rad.as<float>());
+  ctx->stats.launches++;
+  switch (Dp) {
+    case 32:
+      k_vo_item_lb<32><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      break;
+    case 64:
+      k_vo_item_lb<64><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      break;
+    case 96:
+      k_vo_item_lb<96><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      break;
+    case 128:
+      k_vo_item_lb<128><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      break;
+    default:
+      return mds_fail(ctx, MDS_ERR_INTERNAL, "vec_tile_bounds: padded dimension %d", Dp);
+  }
+  ctx->stats.launches++;
+  if (tdseg || tdall) {
+    k_vo_start<<<dim3(nitems, nseg + 1), 32, 0, s>>>(dlo, nct, nseg, tdseg, tdall);
+    ctx->stats.launches++;
+  }
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+// dst[perm[i]] = src[i]: a per-row array of the sorted set back in the
+// original order.
+int vec_unsort(mds_ctx* ctx, const float* src, const int* perm, int n, float* dst) {
+  k_vo_unsort<<<(n + 255) / 256, 256, 0, ctx->stream>>>(src, perm, n, dst);
+  ctx->stats.launches++;
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}

@@ -143,17 +143,84 @@ def test_knn_data_fp32_large_k(ctx, oracle):
     _check(d, i, od, oi)
 
 
+# launches of the locality order (vec_order.cu): k-means (seed, 6 x assign +
+# update, final assign, keys), 2 radix passes of 3, the permutation; for a
+# second set assign, keys, sort, permutation; tile geometry, bounds, (start
+# tiles), rowthr back to the input order
+ORDER_LAUNCHES_SAME = 22 + 2 + 1
+ORDER_LAUNCHES_FIT = 22 + 9 + 3 + 1
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("skip", [False, True])
 @pytest.mark.parametrize("fit_rows", [None, 700])
-def test_knn_data_tc_pilot_pass(ctx, oracle, fit_rows):
+def test_knn_data_tc_pilot_pass(ctx, oracle, fit_rows, skip):
     """9,000 reference vectors (71 column tiles): the screen first seeds every
     row's threshold from 16 tiles (around the diagonal for a set against
-    itself, spread over the set for separate fit vectors)."""
+    itself; spread over the set for separate fit vectors in input order, or
+    outward from the nearest tile in locality order)."""
     rng = np.random.default_rng(21)
     ref = synth.dihedral_vectors(9000, 16, seed=12).astype(np.float64)
     fit = None if fit_rows is None else rng.normal(scale=0.7, size=(fit_rows, 16))
-    d, i = ctx.knn_data(ref, fit, 12, precision="bf16x3")
+    d, i = ctx.knn_data(ref, fit, 12, precision="bf16x3", skip=skip)
     st = ctx.stats()
     od, oi = oracle.knn_data(ref, fit, 12)
     _check(d, i, od, oi)
-    assert st["launches"] == (5 if fit is None else 7)  # prep(s), split(s), pilot, screen, recheck
+    plain = 5 if fit is None else 7  # prep(s), split(s), pilot, screen, recheck
+    extra = (ORDER_LAUNCHES_SAME if fit is None else ORDER_LAUNCHES_FIT) if skip else 0
+    assert st["launches"] == plain + extra
+
+
+def _sampled(ctx, oracle, ref, fit, k, rows):
+    """Both tensor-core screens (locality order with tile skipping, and every
+    tile in input order) give the same output, and sampled rows match the
+    oracle bit for bit."""
+    d, i = ctx.knn_data(ref, fit, k, precision="bf16x3")
+    st = ctx.stats()
+    d0, i0 = ctx.knn_data(ref, fit, k, precision="bf16x3", skip=False)
+    st0 = ctx.stats()
+    assert np.array_equal(d, d0)
+    for r, c in np.argwhere(i != i0):
+        assert np.sum(d0[r] == d0[r, c]) >= 2
+    q = ref if fit is None else fit
+    od, oi = oracle.knn_data(ref, q[rows], k)
+    _check(d[rows], i[rows], od, oi)
+    return st, st0
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_ordered_mixture(ctx, oracle):
+    """20,000 x 64 von Mises mixture vectors against themselves, k = 32: in
+    locality order the screen skips most column tiles."""
+    x = synth.dihedral_vectors(20_000, 64, seed=31).astype(np.float64)
+    st, st0 = _sampled(ctx, oracle, x, None, 32, np.linspace(0, 19_999, 200).astype(int))
+    assert st["rows_flagged"] == 0
+    assert st["screen_pairs"] < 0.6 * st0["screen_pairs"], (st["screen_pairs"], st0["screen_pairs"])
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_ordered_fit_vs_ref(ctx, oracle):
+    """Separate fit vectors (another mixture draw) ordered by the reference
+    set's centroids; uneven sizes (12,345 references, 3,001 fit rows)."""
+    ref = synth.dihedral_vectors(12_345, 64, seed=32).astype(np.float64)
+    fit = synth.dihedral_vectors(3_001, 64, seed=33).astype(np.float64)
+    _sampled(ctx, oracle, ref, fit, 20, np.arange(3_001))
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_ordered_duplicates(ctx, oracle):
+    """1,500 vectors each present four times (exact ties at distance 0 and
+    between neighbours) plus 300 zero vectors."""
+    rng = np.random.default_rng(34)
+    base = rng.normal(size=(1_500, 24))
+    x = np.concatenate([base, base, base, base, np.zeros((300, 24))])[rng.permutation(6_300)]
+    _sampled(ctx, oracle, x, None, 10, np.arange(6_300))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [32, 100])
+def test_knn_data_tc_ordered_unstructured(ctx, oracle, dim):
+    """Gaussian vectors (no clusters: tiles overlap, little is skipped);
+    padded dimensions 32 and 128."""
+    x = np.random.default_rng(35 + dim).normal(size=(6_000, dim))
+    _sampled(ctx, oracle, x, None, 16, np.arange(0, 6_000, 3))
