@@ -252,7 +252,7 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
                const float* __restrict__ nf, int nrows, const int* __restrict__ rowlist, int Nr, int dim, int corr,
                int mode, const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int Kp, int k,
                const float* __restrict__ rowthr, double* __restrict__ out_d, int* __restrict__ out_i,
-               int* __restrict__ flagged, int* __restrict__ nflag) {
+               int* __restrict__ flagged, int* __restrict__ nflag, int cand_by_row) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* sa = reinterpret_cast<double*>(smem_raw);              // [dim]
   uint64_t* keys = reinterpret_cast<uint64_t*>(sa + dim);        // merge buffer, then candidates
@@ -275,10 +275,11 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
   }
   int total;
   float tau = __int_as_float(0x7f800000);
+  const int crow = cand_by_row ? grow : lr;  // candidate lists by fit row or by position in rowlist
   if (mode == 0) {
     if (threadIdx.x == 0) {
       int t = 0;
-      for (int s = 0; s < nseg; ++s) t += cand_n[(int64_t)lr * nseg + s];
+      for (int s = 0; s < nseg; ++s) t += cand_n[(int64_t)crow * nseg + s];
       s_total = t;
     }
     __syncthreads();
@@ -286,8 +287,8 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
     const int P2 = next_pow2(max(t, 1));
     int off = 0;
     for (int s = 0; s < nseg; ++s) {
-      int ns = cand_n[(int64_t)lr * nseg + s];
-      const uint64_t* src = cand + ((int64_t)lr * nseg + s) * Kp;
+      int ns = cand_n[(int64_t)crow * nseg + s];
+      const uint64_t* src = cand + ((int64_t)crow * nseg + s) * Kp;
       for (int x = threadIdx.x; x < ns; x += blockDim.x) keys[off + x] = src[x];
       off += ns;
     }
@@ -311,8 +312,9 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
   double* bval = reinterpret_cast<double*>(keys + (mode == 0 ? Kp : 0));
   int* bidx = reinterpret_cast<int*>(bval + BP2);
   // mode 0: candidates in order of their bound; the first k+1 + k/4 are
-  // rechecked, the rest only if the next bound is below the (k+1)-th exact
-  // value so far (then nothing later can enter the k+1 best)
+  // rechecked, the rest only if the next bound is not above the (k+1)-th
+  // exact value so far, or that value is not below tau (otherwise nothing
+  // later, and no pair left out, can enter the k+1 best)
   const int first = (mode == 0) ? min(max(total, 1), k1 + max(8, k1 / 4)) : CH;
   __shared__ int s_stop;
   bool stopped = false;
@@ -358,7 +360,8 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
       }
     base += nc;
     if (mode == 0 && base < total) {
-      if (threadIdx.x == 0) s_stop = (bval[k1 - 1] < (double)mds_key_value(keys[base])) ? 1 : 0;
+      if (threadIdx.x == 0)
+        s_stop = (bval[k1 - 1] < (double)mds_key_value(keys[base]) && bval[k1 - 1] < (double)tau) ? 1 : 0;
       __syncthreads();
       if (s_stop) {
         stopped = true;
@@ -379,6 +382,256 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
     out_d[(int64_t)grow * k + x] = sqrt(bval[x + 1]);
     out_i[(int64_t)grow * k + x] = bidx[x + 1];
   }
+}
+
+// ---------------------------------------------------------------------------
+// 3b. the candidate recheck (mode 0) with one warp per fit row
+// ---------------------------------------------------------------------------
+// The same result as k_data_recheck mode 0 with no block-wide barrier: the
+// merged candidate keys are sorted in registers (bitonic network over the
+// warp, element e = 32 i + lane), the exact values and indices of the
+// rechecked candidates are kept in shared memory and sorted the same way by
+// (value, index). Rows with more candidates than RW_MAXT, K' > RW_MAXC or
+// k + 1 > RW_MAXK1 are listed in big[] for k_data_recheck.
+#define RW_WARPS 8
+#define RW_MAXT 256
+#define RW_MAXC 128
+#define RW_MAXK1 64
+
+template <int PER>
+__device__ __forceinline__ void wsort_u64(uint64_t (&v)[PER], int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32 * PER; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int p = i ^ (j >> 5);
+          if (p > i) {
+            const bool up = ((i * 32 + lane) & k) == 0;
+            const uint64_t a = v[i], b = v[p];
+            if ((a > b) == up) {
+              v[i] = b;
+              v[p] = a;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int e = i * 32 + lane;
+          const uint64_t o = __shfl_xor_sync(0xffffffffu, v[i], j);
+          v[i] = (((e & j) == 0) == ((e & k) == 0)) ? min(v[i], o) : max(v[i], o);
+        }
+      }
+    }
+  }
+}
+
+// (value bits, index) pairs in ascending (value, index) order; the values
+// are non-negative or +inf, so their bits order as unsigned integers
+__device__ __forceinline__ bool pair_less(uint64_t a, int ia, uint64_t b, int ib) {
+  return a < b || (a == b && ia < ib);
+}
+template <int PER>
+__device__ __forceinline__ void wsort_pair(uint64_t (&v)[PER], int (&x)[PER], int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32 * PER; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int p = i ^ (j >> 5);
+          if (p > i) {
+            const bool up = ((i * 32 + lane) & k) == 0;
+            if (pair_less(v[p], x[p], v[i], x[i]) == up) {
+              const uint64_t tv = v[i];
+              const int tx = x[i];
+              v[i] = v[p];
+              x[i] = x[p];
+              v[p] = tv;
+              x[p] = tx;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int e = i * 32 + lane;
+          const uint64_t ov = __shfl_xor_sync(0xffffffffu, v[i], j);
+          const int ox = __shfl_xor_sync(0xffffffffu, x[i], j);
+          const bool keepmin = ((e & j) == 0) == ((e & k) == 0);
+          if (pair_less(ov, ox, v[i], x[i]) == keepmin) {
+            v[i] = ov;
+            x[i] = ox;
+          }
+        }
+      }
+    }
+  }
+}
+
+// Element e (any e < 32 PER, per lane) of a warp-distributed array.
+template <int PER>
+__device__ __forceinline__ uint64_t lane_elem(const uint64_t (&v)[PER], int e) {
+  uint64_t r = 0;
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const uint64_t y = __shfl_sync(0xffffffffu, v[i], e & 31);
+    if (i == (e >> 5)) r = y;
+  }
+  return r;
+}
+
+// Sorts the pairs (ev, ei)[0, n) (n <= 128) in place by (value, index).
+__device__ __forceinline__ void warp_sort_pairs_smem(double* ev, int* ei, int n, int lane) {
+  uint64_t v[4];
+  int x[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int e = i * 32 + lane;
+    v[i] = (e < n) ? (uint64_t)__double_as_longlong(ev[e]) : 0x7ff0000000000000ull;
+    x[i] = (e < n) ? ei[e] : 0x7fffffff;
+  }
+  wsort_pair<4>(v, x, lane);
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int e = i * 32 + lane;
+    if (e < n) {
+      ev[e] = __longlong_as_double((long long)v[i]);
+      ei[e] = x[i];
+    }
+  }
+  __syncwarp();
+}
+
+template <int PER>
+__device__ void recheck_row(const double* __restrict__ Xref, const double* sa, double ma, double sda,
+                            const double* __restrict__ mr, const double* __restrict__ srv, int dim, int corr,
+                            const uint64_t* __restrict__ cand, int row, int nseg, int Kp, int k, int t, int segoff,
+                            int segn, float rthr, double* ev, int* ei, double* __restrict__ out_d,
+                            int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag, int lane) {
+  const int k1 = k + 1;
+  // merge the segments' lists: element e < t comes from the segment s with
+  // off[s] <= e < off[s] + n[s]
+  uint64_t v[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = i * 32 + lane;
+    uint64_t key = MDS_KEY_INF;
+    for (int s = 0; s < nseg; ++s) {
+      const int o = __shfl_sync(0xffffffffu, segoff, s), nn = __shfl_sync(0xffffffffu, segn, s);
+      if (e >= o && e < o + nn) key = cand[((int64_t)row * nseg + s) * Kp + (e - o)];
+    }
+    v[i] = key;
+  }
+  wsort_u64<PER>(v, lane);
+  const int total = min(t, Kp);
+  // the bound of every pair left out: the K'-th candidate's, or the
+  // threshold the screen filtered them with, whichever is smaller
+  float tau = rthr;
+  if (t >= Kp) tau = fminf(tau, mds_key_value(lane_elem<PER>(v, Kp - 1)));
+  // candidates in order of their bound: the first k + 3 are rechecked, the
+  // rest only if the next bound is not above the (k+1)-th exact value so far
+  // or that value is not below tau
+  const int first = min(total, k1 + 2);
+  for (int base = 0; base < first; base += 32) {
+    const int e = base + lane;
+    const uint64_t key = lane_elem<PER>(v, min(e, 32 * PER - 1));
+    if (e < first) {
+      const int j = mds_key_index(key);
+      const double* b = Xref + (int64_t)j * dim;
+      ev[e] = corr ? exact_corr(sa, ma, sda, b, mr[j], srv[j], dim) : exact_euclid(sa, b, dim);
+      ei[e] = j;
+    }
+  }
+  __syncwarp();
+  int nd = first;
+  warp_sort_pairs_smem(ev, ei, nd, lane);
+  bool stopped = false;
+  if (nd < total) {
+    const double dk = (nd >= k1) ? ev[k1 - 1] : __longlong_as_double(0x7ff0000000000000ll);
+    const float nb = mds_key_value(lane_elem<PER>(v, nd));
+    if (dk < (double)nb && dk < (double)tau) {
+      stopped = true;
+    } else {
+      for (int base = nd; base < total; base += 32) {
+        const int e = base + lane;
+        const uint64_t key = lane_elem<PER>(v, min(e, 32 * PER - 1));
+        if (e < total) {
+          const int j = mds_key_index(key);
+          const double* b = Xref + (int64_t)j * dim;
+          ev[e] = corr ? exact_corr(sa, ma, sda, b, mr[j], srv[j], dim) : exact_euclid(sa, b, dim);
+          ei[e] = j;
+        }
+      }
+      __syncwarp();
+      nd = total;
+      warp_sort_pairs_smem(ev, ei, nd, lane);
+    }
+  }
+  // strict: a pair left out of the list has a lower bound >= tau, so only
+  // dk < tau proves that no left-out pair ties with or beats the k+1-th
+  if (lane == 0 && !stopped) {
+    const double dk = (nd >= k1) ? ev[k1 - 1] : __longlong_as_double(0x7ff0000000000000ll);
+    if (!(dk < (double)tau)) flagged[atomicAdd(nflag, 1)] = row;
+  }
+  for (int x = lane; x < k; x += 32) {
+    const bool have = x + 1 < nd;
+    out_d[(int64_t)row * k + x] = have ? sqrt(ev[x + 1]) : __longlong_as_double(0x7ff0000000000000ll);
+    out_i[(int64_t)row * k + x] = have ? ei[x + 1] : 0x7fffffff;
+  }
+}
+
+__global__ void __launch_bounds__(RW_WARPS * 32)
+k_data_recheck_warp(const double* __restrict__ Xfit, const double* __restrict__ Xref, const double* __restrict__ mf,
+                    const double* __restrict__ sfv, const double* __restrict__ mr, const double* __restrict__ srv,
+                    int nrows, int dim, int corr, const uint64_t* __restrict__ cand, const int* __restrict__ cand_n,
+                    int nseg, int Kp, int k, const float* __restrict__ rowthr, double* __restrict__ out_d,
+                    int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag,
+                    int* __restrict__ big, int* __restrict__ nbig) {
+  extern __shared__ __align__(16) double rsm[];  // per warp: fit row [dim], values [RW_MAXC]; then indices
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * RW_WARPS + w;
+  if (row >= nrows) return;
+  double* sa = rsm + (size_t)w * (dim + RW_MAXC);
+  double* ev = sa + dim;
+  int* ei = reinterpret_cast<int*>(rsm + (size_t)RW_WARPS * (dim + RW_MAXC)) + w * RW_MAXC;
+  const int segn = (lane < nseg) ? cand_n[(int64_t)row * nseg + lane] : 0;
+  int inc = segn;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const int t = __shfl_sync(0xffffffffu, inc, 31);
+  if (t > RW_MAXT || Kp > RW_MAXC || k + 1 > RW_MAXK1) {
+    if (lane == 0) big[atomicAdd(nbig, 1)] = row;
+    return;
+  }
+  for (int d = lane; d < dim; d += 32) sa[d] = Xfit[(int64_t)row * dim + d];
+  __syncwarp();
+  const double ma = corr ? mf[row] : 0.0, sda = corr ? sfv[row] : 0.0;
+  const float rthr = rowthr ? rowthr[row] : __int_as_float(0x7f800000);
+  const int segoff = inc - segn;
+  if (t <= 32)
+    recheck_row<1>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
+                   out_d, out_i, flagged, nflag, lane);
+  else if (t <= 64)
+    recheck_row<2>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
+                   out_d, out_i, flagged, nflag, lane);
+  else if (t <= 128)
+    recheck_row<4>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
+                   out_d, out_i, flagged, nflag, lane);
+  else
+    recheck_row<8>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
+                   out_d, out_i, flagged, nflag, lane);
+}
+
+static size_t data_recheck_warp_smem(int dim) {
+  return (size_t)RW_WARPS * ((dim + RW_MAXC) * sizeof(double) + RW_MAXC * sizeof(int));
 }
 
 static size_t data_recheck_smem(int dim, int Kp, int nseg, int k, int mode) {
@@ -434,16 +687,38 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   MDS_TRY(flagged.alloc(ctx, sizeof(int) * (size_t)std::max(nfit, 1)));
   MDS_TRY(nflag.alloc(ctx, sizeof(int)));
   MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
+  DevBuf big(ctx), nbig(ctx);
   auto recheck = [&](int nrows, const int* rowlist, int mode, const uint64_t* cand, const int* cand_n, int nseg,
                      int Kp, const float* rowthr) -> int {
     size_t smem = data_recheck_smem(dim, Kp, nseg, k, mode);
     if (smem > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "knn_data recheck: dim/k too large");
+    const size_t wsmem = data_recheck_warp_smem(dim);
+    if (mode == 0 && !rowlist && nrows > 0 && wsmem <= 96 * 1024) {
+      // a warp per row; the rows it cannot hold go to the block kernel
+      MDS_TRY(big.alloc(ctx, sizeof(int) * (size_t)nrows));
+      MDS_TRY(nbig.alloc(ctx, sizeof(int)));
+      MDS_CUDA(ctx, cudaMemsetAsync(nbig.p, 0, sizeof(int), s));
+      MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)wsmem));
+      st.launches++;
+      k_data_recheck_warp<<<(nrows + RW_WARPS - 1) / RW_WARPS, RW_WARPS * 32, wsmem, s>>>(
+          dfit, dref, mf, sf, Mr.as<double>(), Sr.as<double>(), nrows, dim, corr, cand, cand_n, nseg, Kp, k, rowthr,
+          dout_d, dout_i, flagged.as<int>(), nflag.as<int>(), big.as<int>(), nbig.as<int>());
+      MDS_CUDA(ctx, cudaGetLastError());
+      int hbig = 0;
+      MDS_CUDA(ctx, cudaMemcpyAsync(&hbig, nbig.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      if (hbig == 0) return MDS_OK;
+      rowlist = big.as<int>();
+      nrows = hbig;
+    }
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     st.launches++;
     if (nrows > 0)
       k_data_recheck<<<nrows, DR_THREADS, smem, s>>>(dfit, dref, mf, sf, Mr.as<double>(), Sr.as<double>(), nfp,
                                                      nrows, rowlist, nref, dim, corr, mode, cand, cand_n, nseg, Kp,
-                                                     k, rowthr, dout_d, dout_i, flagged.as<int>(), nflag.as<int>());
+                                                     k, rowthr, dout_d, dout_i, flagged.as<int>(), nflag.as<int>(),
+                                                     rowlist == big.p ? 1 : 0);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
@@ -685,7 +960,7 @@ extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, 
     if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
     k_data_recheck<<<n_fit, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, n_fit, nullptr, n_ref, dim, corr, 1,
-                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, nullptr, nullptr);
+                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, nullptr, nullptr, 0);
     ctx->stats.launches++;
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
@@ -707,7 +982,7 @@ extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, 
   if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
   MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
   k_data_recheck<<<n_fit, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, n_fit, nullptr, n_ref, dim, corr, 0,
-                                                cand, cand_n, 1, Kp, k, nullptr, out_d, out_i, flagged, nflag);
+                                                cand, cand_n, 1, Kp, k, nullptr, out_d, out_i, flagged, nflag, 0);
   ctx->stats.launches++;
   MDS_CUDA(ctx, cudaGetLastError());
   int hflag = 0;
@@ -723,7 +998,7 @@ extern "C" int mds_knn_data_noalloc(mds_ctx* ctx, const double* ref, int n_ref, 
     if (rsm > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "dim/k too large");
     MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
     k_data_recheck<<<hflag, DR_THREADS, rsm, s>>>(dfit, ref, mf, sf, mr, sr, nf, hflag, flagged, n_ref, dim, corr, 1,
-                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, nullptr, nullptr);
+                                                  nullptr, nullptr, 1, 1, k, nullptr, out_d, out_i, nullptr, nullptr, 0);
     ctx->stats.launches++;
     ctx->stats.passes = 2;
     MDS_CUDA(ctx, cudaGetLastError());

@@ -111,6 +111,24 @@ __device__ __forceinline__ int tv_tile_order(int i, int t0, int t1, int td) {
 }
 
 
+// Work item -> (row pair tile, segment). In locality order (near_first) the
+// segment holding each row pair tile's start tile comes first: items [0, nrp)
+// are those segments, items [nrp, nrp * nseg) the others. By the time a row
+// pair's far segments are claimed its near segment has set the rows'
+// thresholds, and most far tiles are skipped. Start tile: the diagonal's
+// (diag) or tdall[rp].
+__device__ __forceinline__ int2 tv_item(int item, int nseg, int nrp, int ncoltiles, int near_first, int diag,
+                                        const int* tdall) {
+  if (!near_first || nseg == 1) return make_int2(item / nseg, item % nseg);
+  const int rp = item < nrp ? item : (item - nrp) / (nseg - 1);
+  const int tstart = diag ? min((rp * TV_ROWS + TV_ROWS / 2) / TV_N, ncoltiles - 1) : __ldg(tdall + rp);
+  int near = 0;
+  while (near + 1 < nseg && (int)((int64_t)ncoltiles * (near + 1) / nseg) <= tstart) ++near;
+  if (item < nrp) return make_int2(rp, near);
+  const int j = (item - nrp) % (nseg - 1);
+  return make_int2(rp, j < near ? j : j + 1);
+}
+
 // One fit row's list (regions src[0, c0) and src[lcap, lcap + c1)): keep
 // the Kp best, drop those above the row's threshold tp (appended under a
 // looser one: every pair the screen left out lies at or above the final
@@ -150,8 +168,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
              int corr, float guard, uint32_t idesc, int Kp, int nseg, int nitems, int diag, int pilot,
              float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
              int* __restrict__ cand_n, int* __restrict__ err, int lcap, int k1, const float* __restrict__ nmax,
-             const float* __restrict__ dlo, const int* __restrict__ tdv, const int* __restrict__ rperm,
-             const int* __restrict__ cperm) {
+             const float* __restrict__ dlo, const int* __restrict__ tdv, const int* __restrict__ tdall,
+             int near_first, const int* __restrict__ rperm, const int* __restrict__ cperm) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host);
   // err[2]: column tiles computed (added to).
   // Locality order (vec_order.cu; all four null without it): rows and columns
@@ -161,7 +179,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   // the producer skips a tile when dlo^2 is at least the largest threshold of
   // the item's rows. tdv: the visit's start tile ([item] for the pilot,
   // [row pair tile][segment] otherwise) when the set is not screened against
-  // itself.
+  // itself, tdall [row pair tile] the start over all tiles; near_first: the
+  // item order of tv_item.
   // pilot > 0: a pass that only seeds rowthr: each item (one per row pair
   // tile, nseg = 1) visits `pilot` column tiles (outward from the diagonal
   // for a set against itself, else spread over the set) and lowers each
@@ -251,12 +270,13 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         if (lane == 0) ok = push(-1, -1);
         break;
       }
-      const int rp = item / nseg, seg = item % nseg;
+      const int2 rs = tv_item(item, nseg, nitems / nseg, ncoltiles, near_first, diag, tdall);
+      const int rp = rs.x, seg = rs.y;
       const int t0 = pilot ? 0 : (int)((int64_t)ncoltiles * seg / nseg);
       const int t1 = pilot ? ncoltiles : (int)((int64_t)ncoltiles * (seg + 1) / nseg);
       const int nvisit = pilot ? pilot : t1 - t0;
       const int td = diag ? min(max((rp * TV_ROWS + TV_ROWS / 2) / TV_N, t0), t1 - 1)
-                          : (tdv ? min(max(__ldg(tdv + (pilot ? rp : item)), t0), t1 - 1) : t0);
+                          : (tdv ? min(max(__ldg(tdv + (pilot ? rp : rp * nseg + seg)), t0), t1 - 1) : t0);
       const bool spread = pilot && !diag && !tdv;
       // the resident rows: wait until the MMAs of the previous item are done
       if (lane == 0) {
@@ -429,8 +449,9 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       if (task.x < 0) break;
       if (task.x != cur) {
         cur = task.x;
-        rp = cur / nseg;
-        seg = cur % nseg;
+        const int2 rs = tv_item(cur, nseg, nitems / nseg, ncoltiles, near_first, diag, tdall);
+        rp = rs.x;
+        seg = rs.y;
         g = rp * TV_ROWS + r;
         const float rn = (g < nfit) ? __ldg(nf + g) : 0.0f;
         rc = (g >= nfit) ? INF : corr ? 0.5f - guard * rn : rn * (1.0f - guard);
@@ -526,12 +547,15 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const int gg = rp * TV_ROWS + rr;
         if (gg >= nfit) break;
         const int c0 = S->cnt2[rr][0], c1 = S->cnt2[rr][1];
-        const bool over = c0 + c1 > Kp && (c0 > lcap - 64 || c1 > lcap - 64);
-        // (the row's first own threshold comes from its k1-th key as soon as
-        // those arrive: tighter than the seeded shared one, it cuts appends)
+        // a region near full: cut both back to the K' best
+        const bool cut = c0 + c1 > Kp && (c0 > lcap - 64 || c1 > lcap - 64);
+        // the row's first own threshold comes from its k1-th key as soon as
+        // those arrive (a rank search that moves no key): tighter than the
+        // shared one, it cuts appends. (Refreshing it after every k1 further
+        // appends was measured slower: the searches cost more than the
+        // appends they save.)
         const bool first = S->thr[rr] == INF && c0 + c1 >= k1;
-        if (!over && !first) continue;
-        const bool cut = c0 + c1 > Kp;
+        if (!cut && !first) continue;
         float tk1 = INF;
         float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, c0, lcap, c1, cut ? Kp : 0, hist, lane, k1,
                                     &tk1);
@@ -668,6 +692,12 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   MDS_TRY(err.alloc(ctx, 4 * sizeof(int)));
   MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, 4 * sizeof(int), s));
   MDS_CUDA(ctx, cudaMemsetAsync(rt, 0x7f, sizeof(float) * (size_t)nfit, s));
+  // in locality order each row's threshold starts from its k1-th distance to
+  // its start tile's members (the tile is screened first, without a storm of
+  // appends under no threshold)
+  if (order)
+    MDS_TRY(vec_seed_rows(ctx, Xr, pr, nref, Xf, pf, nfit, Dp, same ? nullptr : tdall.as<int>(), k + 1,
+                          nmax.as<float>(), rt));
   const int nst = (Dp <= 64) ? 4 : (Dp <= 96 ? 3 : 2);
   const size_t smem = tv_smem_bytes(Dp, nst);
   static bool attr_done = false;
@@ -679,14 +709,15 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   const float* pdlo = order ? dlo.as<float>() : nullptr;
   const int* ptdseg = (order && !same) ? tdseg.as<int>() : nullptr;
   const int* ptdall = (order && !same) ? tdall.as<int>() : nullptr;
-  // pilot pass: seed every row's threshold from TV_PILOT column tiles, so the
-  // main pass appends few pairs from its first tile on
-  if (ncoltiles >= 4 * TV_PILOT) {
+  // pilot pass (input order): seed every row's threshold from TV_PILOT
+  // column tiles, so the main pass appends few pairs from its first tile on.
+  // In locality order the near segments come first instead (tv_item).
+  if (!order && ncoltiles >= 4 * TV_PILOT) {
     ctx->stats.launches++;
     k_screen_tcv<<<std::min(nrp, ctx->num_sms), TV_THREADS, smem, s>>>(
         mA, mB, nfk, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC, idesc, Kp, 1, nrp,
         same ? 1 : 0, TV_PILOT, rt, work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
-        nmax.as<float>(), pdlo, ptdall, pr ? pf : nullptr, pr);
+        nmax.as<float>(), nullptr, nullptr, nullptr, 0, nullptr, nullptr);
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaMemsetAsync(err.as<int>() + 1, 0, sizeof(int), s));
   }
@@ -694,7 +725,8 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   k_screen_tcv<<<grid, TV_THREADS, smem, s>>>(mA, mB, nfk, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0,
                                               MDS_GUARD_TC, idesc, Kp, nseg, nitems, same ? 1 : 0, 0, rt,
                                               work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
-                                              nmax.as<float>(), pdlo, ptdseg, pr ? pf : nullptr, pr);
+                                              nmax.as<float>(), pdlo, ptdseg, ptdall, order ? 1 : 0,
+                                              pr ? pf : nullptr, pr);
   MDS_CUDA(ctx, cudaGetLastError());
   if (order) MDS_TRY(vec_unsort(ctx, rt, pf, nfit, rowthr));
   int herr[3] = {0, 0, 0};

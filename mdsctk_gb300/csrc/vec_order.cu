@@ -19,8 +19,8 @@
 //     rho = max |y - c| (accumulated in FP64 against the FP32 centre, rounded
 //     up).
 //  3. Per row pair tile I and column tile T, dlo = min over the rows x of I of
-//     |x - c_T| (FP32, shrunk by a relative 3e-5 for its rounding) minus rho_T
-//     minus an absolute margin for the rounding of the inputs to FP32. By the
+//     |x - c_T| (FP32, made a lower bound by a margin for its rounding) minus
+//     rho_T minus an absolute margin for the rounding of the inputs to FP32. By the
 //     triangle inequality every pair (x in I, y in T) has |x - y| >= dlo: when
 //     dlo > 0 and dlo^2 is at least every row's current threshold, none of
 //     the tile's pairs can enter any row's list, and the screen skips it.
@@ -42,12 +42,13 @@ __global__ void k_vo_seed(const float* __restrict__ X, int n, int Dp, float* __r
   for (int d = threadIdx.x; d < Dp; d += blockDim.x) cent[c * Dp + d] = X[v * Dp + d];
 }
 
-// Nearest centroid of each vector. sums/counts (zeroed by the caller): the
-// FP64 sums and counts of each centroid's vectors, for the next centroids.
+// Nearest centroid of every stride-th vector. sums/counts (zeroed by the
+// caller): the FP64 sums and counts of each centroid's vectors, for the next
+// centroids.
 // keys/vals: (centroid << 12 | distance quantised against *dmax) and the
 // vector's index, for the sort; dist/dmax: the distance to the nearest
 // centroid and (float bits) the largest one, for that quantisation.
-__global__ void __launch_bounds__(256) k_vo_assign(const float* __restrict__ X, int n, int Dp,
+__global__ void __launch_bounds__(256) k_vo_assign(const float* __restrict__ X, int n, int Dp, int stride,
                                                    const float* __restrict__ cent, double* __restrict__ sums,
                                                    int* __restrict__ counts, float* __restrict__ dist,
                                                    unsigned* __restrict__ dmax, int* __restrict__ label) {
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(256) k_vo_assign(const float* __restrict__ X, 
   }
   if (threadIdx.x < VO_CENT) sc[threadIdx.x] = 0;
   __syncthreads();
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t v = (int64_t)(blockIdx.x * blockDim.x + threadIdx.x) * stride;
   float best = __int_as_float(0x7f800000);
   int bl = 0;
   if (v < n) {
@@ -176,11 +177,16 @@ __global__ void k_vo_tile_geom(const float* __restrict__ X, const int* __restric
 // dlo[I][T] for the row pair tile I (blockDim.x = 256 sorted rows; rows past
 // n count as absent) and every column tile T. nmax: the reference set's
 // largest squared norm (float), for the absolute margin.
+//   |x - c|^2 = |x|^2 + |c|^2 - 2 x.c in FP32 (one FMA per dimension): each
+//   of the three terms errs by at most ~DP 2^-24 (|x|^2 + |c|^2), so
+//   4e-7 DP (|x|^2 + |c|^2) taken off before the square root keeps it a
+//   lower bound.
 template <int DP>
 __global__ void __launch_bounds__(256) k_vo_item_lb(const float* __restrict__ X, const int* __restrict__ perm, int n,
                                                     const float* __restrict__ center, const float* __restrict__ rad,
                                                     int nct, const float* __restrict__ nmax, float* __restrict__ dlo) {
   __shared__ __align__(16) float cen[32 * DP];
+  __shared__ float cnr[32];
   __shared__ float wmin[8][33];
   const int item = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int g = item * 256 + t;
@@ -200,39 +206,51 @@ __global__ void __launch_bounds__(256) k_vo_item_lb(const float* __restrict__ X,
 #pragma unroll
     for (int d = 0; d < DP; ++d) x[d] = 0.0f;
   }
+  float xn0 = 0.0f, xn1 = 0.0f;
+#pragma unroll
+  for (int d = 0; d < DP; d += 2) {
+    xn0 = fmaf(x[d], x[d], xn0);
+    xn1 = fmaf(x[d + 1], x[d + 1], xn1);
+  }
+  const float xn = xn0 + xn1;
   // |x32 - x| <= 2^-24 |x| for each input vector: 2e-6 (|x|max + |y|max)
   // covers the rounding of both sides with room (nmax: the reference set's
   // largest squared norm; the rows' own is found here)
-  float xn = 0.0f;
-#pragma unroll
-  for (int d = 0; d < DP; ++d) xn = fmaf(x[d], x[d], xn);
-  xn = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(xn)));
-  if (lane == 0) wmin[w][32] = xn;
+  float xm = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(xn)));
+  if (lane == 0) wmin[w][32] = xm;
   __syncthreads();
-  for (int k = 0; k < 8; ++k) xn = fmaxf(xn, wmin[k][32]);
-  const float nabs = 2e-6f * (sqrtf(__ldg(nmax)) + sqrtf(xn));
+  for (int k = 0; k < 8; ++k) xm = fmaxf(xm, wmin[k][32]);
+  const float nabs = 2e-6f * (sqrtf(__ldg(nmax)) + sqrtf(xm));
+  const float mrel = 4e-7f * DP;
   for (int T0 = 0; T0 < nct; T0 += 32) {
     const int nt = min(32, nct - T0);
     __syncthreads();
     for (int e = t; e < nt * DP; e += 256) cen[e] = center[(int64_t)T0 * DP + e];
     __syncthreads();
+    if (t < nt) {
+      float c0 = 0.0f, c1 = 0.0f;
+      for (int d = 0; d < DP; d += 2) {
+        c0 = fmaf(cen[t * DP + d], cen[t * DP + d], c0);
+        c1 = fmaf(cen[t * DP + d + 1], cen[t * DP + d + 1], c1);
+      }
+      cnr[t] = c0 + c1;
+    }
+    __syncthreads();
     for (int tt = 0; tt < nt; ++tt) {
       const float4* c4 = reinterpret_cast<const float4*>(cen + tt * DP);
-      float s0 = 0.0f, s1 = 0.0f;
+      float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
 #pragma unroll
       for (int q = 0; q < DP / 4; ++q) {
         const float4 c = c4[q];
-        float e = x[4 * q] - c.x;
-        s0 = fmaf(e, e, s0);
-        e = x[4 * q + 1] - c.y;
-        s1 = fmaf(e, e, s1);
-        e = x[4 * q + 2] - c.z;
-        s0 = fmaf(e, e, s0);
-        e = x[4 * q + 3] - c.w;
-        s1 = fmaf(e, e, s1);
+        s0 = fmaf(x[4 * q], c.x, s0);
+        s1 = fmaf(x[4 * q + 1], c.y, s1);
+        s2 = fmaf(x[4 * q + 2], c.z, s2);
+        s3 = fmaf(x[4 * q + 3], c.w, s3);
       }
+      const float cn = cnr[tt];
+      const float d2 = fmaxf((xn + cn) - 2.0f * ((s0 + s1) + (s2 + s3)) - mrel * (xn + cn), 0.0f);
       // squared distances are non-negative: their bits order as unsigned
-      unsigned u = valid ? __float_as_uint(s0 + s1) : 0x7f800000u;
+      unsigned u = valid ? __float_as_uint(d2) : 0x7f800000u;
       u = __reduce_min_sync(0xffffffffu, u);
       if (lane == 0) wmin[w][tt] = __uint_as_float(u);
     }
@@ -242,8 +260,95 @@ __global__ void __launch_bounds__(256) k_vo_item_lb(const float* __restrict__ X,
 #pragma unroll
       for (int k = 1; k < 8; ++k) m = fminf(m, wmin[k][lane]);
       const int T = T0 + lane;
-      dlo[(int64_t)item * nct + T] = sqrtf(m) * (1.0f - 3e-5f) - __ldg(rad + T) - nabs;
+      dlo[(int64_t)item * nct + T] = sqrtf(m) * (1.0f - 1e-6f) - __ldg(rad + T) - nabs;
     }
+  }
+}
+
+// Ascending bitonic sort of 128 values held 4 per lane (element 4 lane + i).
+__device__ __forceinline__ void warp_sort128(float (&v)[4], int lane) {
+#pragma unroll
+  for (int k = 2; k <= 128; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 4) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int e = lane * 4 + i;
+          const float o = __shfl_xor_sync(0xffffffffu, v[i], j >> 2);
+          v[i] = (((e & j) == 0) == ((e & k) == 0)) ? fminf(v[i], o) : fmaxf(v[i], o);
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int p = i ^ j;
+          if (p > i) {
+            const bool up = ((lane * 4 + i) & k) == 0;
+            const float a = v[i], b = v[p];
+            if ((a > b) == up) {
+              v[i] = b;
+              v[p] = a;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// Seeds the threshold of every sorted fit row: its k1-th smallest squared
+// distance to the members of its start tile (the diagonal tile for a set
+// against itself, else tdall[row pair tile]), raised by a margin for the
+// FP32 arithmetic -- an upper bound of the row's k1-th smallest over the
+// whole reference set, which holds those members. Block: one row pair tile,
+// 8 warps taking its rows in turn (lane j: members j, j + 32, j + 64, j + 96).
+// Rows whose start tile has fewer than k1 members keep +inf.
+__global__ void __launch_bounds__(256) k_vo_seed_rows(const float* __restrict__ Xr, const int* __restrict__ permr,
+                                                      int nref, const float* __restrict__ Xf,
+                                                      const int* __restrict__ permf, int nfit, int Dp,
+                                                      const int* __restrict__ tdall, int ncoltiles, int k1,
+                                                      const float* __restrict__ nmax, float* __restrict__ rowthr) {
+  extern __shared__ float sm[];  // members [128][Dp + 1], then rows [8][Dp]
+  const int item = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int T = tdall ? tdall[item] : min((item * 256 + 128) / 128, ncoltiles - 1);
+  const int j0 = T * 128, m = min(128, nref - j0);
+  const int ld = Dp + 1;
+  float* mem = sm;
+  float* rowv = sm + 128 * ld + w * Dp;
+  for (int e = threadIdx.x; e < 128 * Dp; e += blockDim.x) {
+    const int j = e / Dp, d = e % Dp;
+    mem[j * ld + d] = (j < m) ? Xr[(int64_t)permr[j0 + j] * Dp + d] : 0.0f;
+  }
+  __syncthreads();
+  const float nm = __ldg(nmax);
+  for (int r = w; r < 256; r += 8) {
+    const int g = item * 256 + r;
+    if (g >= nfit) break;
+    const float* x = Xf + (int64_t)permf[g] * Dp;
+    for (int d = lane; d < Dp; d += 32) rowv[d] = x[d];
+    __syncwarp();
+    float v[4];
+    float xn = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int j = lane + 32 * i;
+      const float* y = mem + j * ld;
+      float s0 = 0.0f, s1 = 0.0f;
+      for (int d = 0; d < Dp; d += 2) {
+        const float e0 = rowv[d] - y[d], e1 = rowv[d + 1] - y[d + 1];
+        s0 = fmaf(e0, e0, s0);
+        s1 = fmaf(e1, e1, s1);
+      }
+      v[i] = (j < m) ? s0 + s1 : __int_as_float(0x7f800000);
+    }
+    for (int d = 0; d < Dp; ++d) xn = fmaf(rowv[d], rowv[d], xn);
+    warp_sort128(v, lane);
+    const int q = k1 - 1;
+    const float vk = __shfl_sync(0xffffffffu, v[q & 3], q >> 2);
+    // the FP32 sum of Dp squares errs by < (Dp + 2) 2^-24 of itself; the
+    // inputs' rounding to FP32 moves d^2 by < 2.4e-7 (|x|^2 + |y|^2)
+    if (lane == 0 && k1 <= m) rowthr[g] = vk * (1.0f + 3e-5f) + 1e-6f * (xn + nm);
+    __syncwarp();
   }
 }
 
@@ -308,14 +413,17 @@ int vec_order(mds_ctx* ctx, const float* X, int n, int Dp, float* cent, bool fit
     MDS_CUDA(ctx, cudaMemsetAsync(counts.p, 0, sizeof(int) * VO_CENT, s));
     k_vo_seed<<<VO_CENT, 128, 0, s>>>(X, n, Dp, cent);
     ctx->stats.launches++;
+    // the iterations run on an evenly strided sample of about 16 k vectors
+    const int stride = std::max(1, n / 16384);
+    const int nbs = ((n + stride - 1) / stride + 255) / 256;
     for (int it = 0; it < VO_ITERS; ++it) {
-      k_vo_assign<<<nb, 256, 0, s>>>(X, n, Dp, cent, sums.as<double>(), counts.as<int>(), nullptr, nullptr,
-                                     nullptr);
+      k_vo_assign<<<nbs, 256, 0, s>>>(X, n, Dp, stride, cent, sums.as<double>(), counts.as<int>(), nullptr,
+                                      nullptr, nullptr);
       k_vo_update<<<VO_CENT, 128, 0, s>>>(cent, sums.as<double>(), counts.as<int>(), Dp);
       ctx->stats.launches += 2;
     }
   }
-  k_vo_assign<<<nb, 256, 0, s>>>(X, n, Dp, cent, nullptr, nullptr, dist.as<float>(), dmax.as<unsigned>(),
+  k_vo_assign<<<nb, 256, 0, s>>>(X, n, Dp, 1, cent, nullptr, nullptr, dist.as<float>(), dmax.as<unsigned>(),
                                  label.as<int>());
   MDS_TRY(k0.alloc(ctx, sizeof(unsigned long long) * (size_t)n));
   MDS_TRY(v0.alloc(ctx, sizeof(int64_t) * (size_t)n));
@@ -368,6 +476,25 @@ int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, c
     k_vo_start<<<dim3(nitems, nseg + 1), 32, 0, s>>>(dlo, nct, nseg, tdseg, tdall);
     ctx->stats.launches++;
   }
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+// Threshold seeds of the sorted fit rows (k_vo_seed_rows) into rowthr, whose
+// entries are +inf-like before (a row without a seed keeps its value). The
+// reference set is in tiles of 128.
+int vec_seed_rows(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
+                  int nfit, int Dp, const int* tdall, int k1, const float* nmax, float* rowthr) {
+  if (k1 > 128) return MDS_OK;
+  const int ncoltiles = (nref + 127) / 128, nitems = (nfit + 255) / 256;
+  const size_t smem = sizeof(float) * ((size_t)128 * (Dp + 1) + 8 * (size_t)Dp);
+  static bool attr_done = false;
+  static size_t attr_limit = 0;
+  MDS_TRY(mds_allow_dyn_smem(ctx, k_vo_seed_rows, &attr_done, &attr_limit));
+  if (smem > attr_limit) return MDS_OK;
+  k_vo_seed_rows<<<nitems, 256, smem, ctx->stream>>>(Xr, permr, nref, Xf, permf, nfit, Dp, tdall, ncoltiles, k1,
+                                                      nmax, rowthr);
+  ctx->stats.launches++;
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
 }

@@ -155,10 +155,10 @@ ORDER_LAUNCHES_FIT = 22 + 9 + 3 + 1
 @pytest.mark.parametrize("skip", [False, True])
 @pytest.mark.parametrize("fit_rows", [None, 700])
 def test_knn_data_tc_pilot_pass(ctx, oracle, fit_rows, skip):
-    """9,000 reference vectors (71 column tiles): the screen first seeds every
-    row's threshold from 16 tiles (around the diagonal for a set against
-    itself; spread over the set for separate fit vectors in input order, or
-    outward from the nearest tile in locality order)."""
+    """9,000 reference vectors (71 column tiles). In input order the screen
+    first seeds every row's threshold from 16 tiles (around the diagonal for a
+    set against itself, spread over the set for separate fit vectors); in
+    locality order each row pair's near segment is screened first instead."""
     rng = np.random.default_rng(21)
     ref = synth.dihedral_vectors(9000, 16, seed=12).astype(np.float64)
     fit = None if fit_rows is None else rng.normal(scale=0.7, size=(fit_rows, 16))
@@ -167,7 +167,8 @@ def test_knn_data_tc_pilot_pass(ctx, oracle, fit_rows, skip):
     od, oi = oracle.knn_data(ref, fit, 12)
     _check(d, i, od, oi)
     plain = 5 if fit is None else 7  # prep(s), split(s), pilot, screen, recheck
-    extra = (ORDER_LAUNCHES_SAME if fit is None else ORDER_LAUNCHES_FIT) if skip else 0
+    # in locality order: no pilot pass (each row pair's near segment goes first)
+    extra = (ORDER_LAUNCHES_SAME if fit is None else ORDER_LAUNCHES_FIT) - 1 if skip else 0
     assert st["launches"] == plain + extra
 
 
