@@ -394,7 +394,7 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
 // (value, index). Rows with more candidates than RW_MAXT, K' > RW_MAXC or
 // k + 1 > RW_MAXK1 are listed in big[] for k_data_recheck.
 #define RW_WARPS 8
-#define RW_MAXT 256
+#define RW_MAXT 512
 #define RW_MAXC 128
 #define RW_MAXK1 64
 
@@ -625,9 +625,12 @@ k_data_recheck_warp(const double* __restrict__ Xfit, const double* __restrict__ 
   else if (t <= 128)
     recheck_row<4>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
                    out_d, out_i, flagged, nflag, lane);
-  else
+  else if (t <= 256)
     recheck_row<8>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
                    out_d, out_i, flagged, nflag, lane);
+  else
+    recheck_row<16>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
+                    out_d, out_i, flagged, nflag, lane);
 }
 
 static size_t data_recheck_warp_smem(int dim) {
@@ -693,7 +696,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
     size_t smem = data_recheck_smem(dim, Kp, nseg, k, mode);
     if (smem > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "knn_data recheck: dim/k too large");
     const size_t wsmem = data_recheck_warp_smem(dim);
-    if (mode == 0 && !rowlist && nrows > 0 && wsmem <= 96 * 1024) {
+    if (mode == 0 && !rowlist && nrows > 0 && wsmem <= 96 * 1024 && k + 1 <= RW_MAXK1 && Kp <= RW_MAXC) {
       // a warp per row; the rows it cannot hold go to the block kernel
       MDS_TRY(big.alloc(ctx, sizeof(int) * (size_t)nrows));
       MDS_TRY(nbig.alloc(ctx, sizeof(int)));
