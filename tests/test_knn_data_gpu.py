@@ -146,9 +146,9 @@ def test_knn_data_fp32_large_k(ctx, oracle):
 # launches of the locality order (vec_order.cu): k-means (seed, 6 x assign +
 # update, final assign, keys), 2 radix passes of 3, the permutation; for a
 # second set assign, keys, sort, permutation; tile geometry, bounds, (start
-# tiles), rowthr back to the input order
-ORDER_LAUNCHES_SAME = 22 + 2 + 1
-ORDER_LAUNCHES_FIT = 22 + 9 + 3 + 1
+# tiles), threshold seeds, rowthr back to the input order
+ORDER_LAUNCHES_SAME = 22 + 2 + 1 + 1
+ORDER_LAUNCHES_FIT = 22 + 9 + 3 + 1 + 1
 
 
 @pytest.mark.gpu
