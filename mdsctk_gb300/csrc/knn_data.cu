@@ -385,18 +385,17 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
 }
 
 // ---------------------------------------------------------------------------
-// 3b. the candidate recheck (mode 0) with one warp per fit row
+// 3b. the candidate recheck (mode 0) in three stages
 // ---------------------------------------------------------------------------
-// The same result as k_data_recheck mode 0 with no block-wide barrier: the
-// merged candidate keys are sorted in registers (bitonic network over the
-// warp, element e = 32 i + lane), the exact values and indices of the
-// rechecked candidates are kept in shared memory and sorted the same way by
-// (value, index). Rows with more candidates than RW_MAXT, K' > RW_MAXC or
-// k + 1 > RW_MAXK1 are listed in big[] for k_data_recheck.
+// The same result as k_data_recheck mode 0, with no block-wide barrier and
+// the FP64 work packed densely: keys and (value, index) pairs are sorted in
+// registers by bitonic networks over a warp (element e = 32 i + lane). The
+// first k + 3 candidates of each row are rechecked; rows that need more, or
+// that hold more than RW_MAXT candidates, are listed in big[] for
+// k_data_recheck. Used for k + 1 <= RW_MAXK1.
 #define RW_WARPS 8
-#define RW_MAXT 512
-#define RW_MAXC 128
-#define RW_MAXK1 64
+#define RW_MAXT 512   // merged candidates a warp sorts in registers
+#define RW_MAXK1 64   // k + 1 (the first batch, k + 3, fits the finishing sort of 128)
 
 template <int PER>
 __device__ __forceinline__ void wsort_u64(uint64_t (&v)[PER], int lane) {
@@ -485,38 +484,16 @@ __device__ __forceinline__ uint64_t lane_elem(const uint64_t (&v)[PER], int e) {
   return r;
 }
 
-// Sorts the pairs (ev, ei)[0, n) (n <= 128) in place by (value, index).
-__device__ __forceinline__ void warp_sort_pairs_smem(double* ev, int* ei, int n, int lane) {
-  uint64_t v[4];
-  int x[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int e = i * 32 + lane;
-    v[i] = (e < n) ? (uint64_t)__double_as_longlong(ev[e]) : 0x7ff0000000000000ull;
-    x[i] = (e < n) ? ei[e] : 0x7fffffff;
-  }
-  wsort_pair<4>(v, x, lane);
-  __syncwarp();
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int e = i * 32 + lane;
-    if (e < n) {
-      ev[e] = __longlong_as_double((long long)v[i]);
-      ei[e] = x[i];
-    }
-  }
-  __syncwarp();
-}
-
+// Stage 1, one warp per fit row: merge the segments' lists, sort the keys
+// (element e < t comes from the segment s with off[s] <= e < off[s] + n[s]),
+// and write the first `first` candidate indices in order of their bound
+// (cidx [row][fw]), with the row's candidate count, tau (the bound of every
+// pair left out: the K'-th candidate's, or the screen's threshold, whichever
+// is smaller) and the next candidate's bound.
 template <int PER>
-__device__ void recheck_row(const double* __restrict__ Xref, const double* sa, double ma, double sda,
-                            const double* __restrict__ mr, const double* __restrict__ srv, int dim, int corr,
-                            const uint64_t* __restrict__ cand, int row, int nseg, int Kp, int k, int t, int segoff,
-                            int segn, float rthr, double* ev, int* ei, double* __restrict__ out_d,
-                            int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag, int lane) {
-  const int k1 = k + 1;
-  // merge the segments' lists: element e < t comes from the segment s with
-  // off[s] <= e < off[s] + n[s]
+__device__ void cands_row(const uint64_t* __restrict__ cand, int row, int nseg, int Kp, int k1, int fw, int t,
+                          int segoff, int segn, float rthr, int* __restrict__ cidx, int4* __restrict__ meta,
+                          int lane) {
   uint64_t v[PER];
 #pragma unroll
   for (int i = 0; i < PER; ++i) {
@@ -530,76 +507,25 @@ __device__ void recheck_row(const double* __restrict__ Xref, const double* sa, d
   }
   wsort_u64<PER>(v, lane);
   const int total = min(t, Kp);
-  // the bound of every pair left out: the K'-th candidate's, or the
-  // threshold the screen filtered them with, whichever is smaller
   float tau = rthr;
   if (t >= Kp) tau = fminf(tau, mds_key_value(lane_elem<PER>(v, Kp - 1)));
-  // candidates in order of their bound: the first k + 3 are rechecked, the
-  // rest only if the next bound is not above the (k+1)-th exact value so far
-  // or that value is not below tau
-  const int first = min(total, k1 + 2);
-  for (int base = 0; base < first; base += 32) {
+  const int first = min(total, fw);
+  const float nxt = (first < total) ? mds_key_value(lane_elem<PER>(v, first)) : __int_as_float(0x7f800000);
+  for (int base = 0; base < fw; base += 32) {
     const int e = base + lane;
     const uint64_t key = lane_elem<PER>(v, min(e, 32 * PER - 1));
-    if (e < first) {
-      const int j = mds_key_index(key);
-      const double* b = Xref + (int64_t)j * dim;
-      ev[e] = corr ? exact_corr(sa, ma, sda, b, mr[j], srv[j], dim) : exact_euclid(sa, b, dim);
-      ei[e] = j;
-    }
+    if (e < first) cidx[(int64_t)row * fw + e] = mds_key_index(key);
   }
-  __syncwarp();
-  int nd = first;
-  warp_sort_pairs_smem(ev, ei, nd, lane);
-  bool stopped = false;
-  if (nd < total) {
-    const double dk = (nd >= k1) ? ev[k1 - 1] : __longlong_as_double(0x7ff0000000000000ll);
-    const float nb = mds_key_value(lane_elem<PER>(v, nd));
-    if (dk < (double)nb && dk < (double)tau) {
-      stopped = true;
-    } else {
-      for (int base = nd; base < total; base += 32) {
-        const int e = base + lane;
-        const uint64_t key = lane_elem<PER>(v, min(e, 32 * PER - 1));
-        if (e < total) {
-          const int j = mds_key_index(key);
-          const double* b = Xref + (int64_t)j * dim;
-          ev[e] = corr ? exact_corr(sa, ma, sda, b, mr[j], srv[j], dim) : exact_euclid(sa, b, dim);
-          ei[e] = j;
-        }
-      }
-      __syncwarp();
-      nd = total;
-      warp_sort_pairs_smem(ev, ei, nd, lane);
-    }
-  }
-  // strict: a pair left out of the list has a lower bound >= tau, so only
-  // dk < tau proves that no left-out pair ties with or beats the k+1-th
-  if (lane == 0 && !stopped) {
-    const double dk = (nd >= k1) ? ev[k1 - 1] : __longlong_as_double(0x7ff0000000000000ll);
-    if (!(dk < (double)tau)) flagged[atomicAdd(nflag, 1)] = row;
-  }
-  for (int x = lane; x < k; x += 32) {
-    const bool have = x + 1 < nd;
-    out_d[(int64_t)row * k + x] = have ? sqrt(ev[x + 1]) : __longlong_as_double(0x7ff0000000000000ll);
-    out_i[(int64_t)row * k + x] = have ? ei[x + 1] : 0x7fffffff;
-  }
+  if (lane == 0) meta[row] = make_int4(first, total, __float_as_int(tau), __float_as_int(nxt));
 }
 
 __global__ void __launch_bounds__(RW_WARPS * 32)
-k_data_recheck_warp(const double* __restrict__ Xfit, const double* __restrict__ Xref, const double* __restrict__ mf,
-                    const double* __restrict__ sfv, const double* __restrict__ mr, const double* __restrict__ srv,
-                    int nrows, int dim, int corr, const uint64_t* __restrict__ cand, const int* __restrict__ cand_n,
-                    int nseg, int Kp, int k, const float* __restrict__ rowthr, double* __restrict__ out_d,
-                    int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag,
-                    int* __restrict__ big, int* __restrict__ nbig) {
-  extern __shared__ __align__(16) double rsm[];  // per warp: fit row [dim], values [RW_MAXC]; then indices
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row = blockIdx.x * RW_WARPS + w;
+k_recheck_cands(const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nrows, int nseg, int Kp,
+                int k1, int fw, const float* __restrict__ rowthr, int* __restrict__ cidx, int4* __restrict__ meta,
+                int* __restrict__ big, int* __restrict__ nbig) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * RW_WARPS + (threadIdx.x >> 5);
   if (row >= nrows) return;
-  double* sa = rsm + (size_t)w * (dim + RW_MAXC);
-  double* ev = sa + dim;
-  int* ei = reinterpret_cast<int*>(rsm + (size_t)RW_WARPS * (dim + RW_MAXC)) + w * RW_MAXC;
   const int segn = (lane < nseg) ? cand_n[(int64_t)row * nseg + lane] : 0;
   int inc = segn;
   for (int o = 1; o < 32; o <<= 1) {
@@ -607,34 +533,91 @@ k_data_recheck_warp(const double* __restrict__ Xfit, const double* __restrict__ 
     if (lane >= o) inc += y;
   }
   const int t = __shfl_sync(0xffffffffu, inc, 31);
-  if (t > RW_MAXT || Kp > RW_MAXC || k + 1 > RW_MAXK1) {
-    if (lane == 0) big[atomicAdd(nbig, 1)] = row;
+  if (t > RW_MAXT) {  // the block kernel takes the row
+    if (lane == 0) {
+      meta[row] = make_int4(-1, 0, 0, 0);
+      big[atomicAdd(nbig, 1)] = row;
+    }
     return;
   }
-  for (int d = lane; d < dim; d += 32) sa[d] = Xfit[(int64_t)row * dim + d];
-  __syncwarp();
-  const double ma = corr ? mf[row] : 0.0, sda = corr ? sfv[row] : 0.0;
   const float rthr = rowthr ? rowthr[row] : __int_as_float(0x7f800000);
   const int segoff = inc - segn;
   if (t <= 32)
-    recheck_row<1>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
-                   out_d, out_i, flagged, nflag, lane);
+    cands_row<1>(cand, row, nseg, Kp, k1, fw, t, segoff, segn, rthr, cidx, meta, lane);
   else if (t <= 64)
-    recheck_row<2>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
-                   out_d, out_i, flagged, nflag, lane);
+    cands_row<2>(cand, row, nseg, Kp, k1, fw, t, segoff, segn, rthr, cidx, meta, lane);
   else if (t <= 128)
-    recheck_row<4>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
-                   out_d, out_i, flagged, nflag, lane);
+    cands_row<4>(cand, row, nseg, Kp, k1, fw, t, segoff, segn, rthr, cidx, meta, lane);
   else if (t <= 256)
-    recheck_row<8>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
-                   out_d, out_i, flagged, nflag, lane);
+    cands_row<8>(cand, row, nseg, Kp, k1, fw, t, segoff, segn, rthr, cidx, meta, lane);
   else
-    recheck_row<16>(Xref, sa, ma, sda, mr, srv, dim, corr, cand, row, nseg, Kp, k, t, segoff, segn, rthr, ev, ei,
-                    out_d, out_i, flagged, nflag, lane);
+    cands_row<16>(cand, row, nseg, Kp, k1, fw, t, segoff, segn, rthr, cidx, meta, lane);
 }
 
-static size_t data_recheck_warp_smem(int dim) {
-  return (size_t)RW_WARPS * ((dim + RW_MAXC) * sizeof(double) + RW_MAXC * sizeof(int));
+// Stage 2, one thread per (row, candidate slot): the exact value of the
+// candidate in the reference's arithmetic. The slots of all rows are one
+// dense range, so every lane of the FP64 pipe has a pair to compute.
+__global__ void __launch_bounds__(256)
+k_recheck_exact(const double* __restrict__ Xfit, const double* __restrict__ Xref, const double* __restrict__ mf,
+                const double* __restrict__ sfv, const double* __restrict__ mr, const double* __restrict__ srv,
+                int nrows, int dim, int corr, int fw, const int* __restrict__ cidx, const int4* __restrict__ meta,
+                double* __restrict__ ev) {
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= (int64_t)nrows * fw) return;
+  const int row = (int)(slot / fw), c = (int)(slot % fw);
+  if (c >= meta[row].x) return;
+  const int j = cidx[slot];
+  const double* a = Xfit + (int64_t)row * dim;
+  const double* b = Xref + (int64_t)j * dim;
+  ev[slot] = corr ? exact_corr(a, mf[row], sfv[row], b, mr[j], srv[j], dim) : exact_euclid(a, b, dim);
+}
+
+// Stage 3, one warp per row: the k+1 best rechecked candidates by (value,
+// index). The row is done when the next candidate's bound lies above the
+// (k+1)-th exact value and that value lies below tau, or when every
+// candidate was rechecked (then dk < tau is required, else the row is
+// flagged); otherwise it goes to the block kernel, which rechecks all its
+// candidates.
+__global__ void __launch_bounds__(RW_WARPS * 32)
+k_recheck_finish(int nrows, int k, int fw, const int* __restrict__ cidx, const int4* __restrict__ meta,
+                 const double* __restrict__ ev, double* __restrict__ out_d, int* __restrict__ out_i,
+                 int* __restrict__ flagged, int* __restrict__ nflag, int* __restrict__ big, int* __restrict__ nbig) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * RW_WARPS + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  const int4 m = meta[row];
+  const int first = m.x, total = m.y;
+  if (first < 0) return;
+  const float tau = __int_as_float(m.z), nxt = __int_as_float(m.w);
+  const int k1 = k + 1;
+  uint64_t v[4];
+  int x[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int e = i * 32 + lane;
+    v[i] = (e < first) ? (uint64_t)__double_as_longlong(ev[(int64_t)row * fw + e]) : 0x7ff0000000000000ull;
+    x[i] = (e < first) ? cidx[(int64_t)row * fw + e] : 0x7fffffff;
+  }
+  wsort_pair<4>(v, x, lane);
+  const uint64_t dkb = lane_elem<4>(v, k1 - 1);
+  const double dk = __longlong_as_double((long long)dkb);
+  if (first < total && !(dk < (double)nxt && dk < (double)tau)) {
+    if (lane == 0) big[atomicAdd(nbig, 1)] = row;
+    return;
+  }
+  // strict: a pair left out of the list has a lower bound >= tau, so only
+  // dk < tau proves that no left-out pair ties with or beats the k+1-th
+  if (lane == 0 && first == total && !(dk < (double)tau)) flagged[atomicAdd(nflag, 1)] = row;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int e = i * 32 + lane;
+    if (e >= 1 && e <= k) {
+      const bool have = e < first;
+      out_d[(int64_t)row * k + e - 1] = have ? sqrt(__longlong_as_double((long long)v[i]))
+                                             : __longlong_as_double(0x7ff0000000000000ll);
+      out_i[(int64_t)row * k + e - 1] = have ? x[i] : 0x7fffffff;
+    }
+  }
 }
 
 static size_t data_recheck_smem(int dim, int Kp, int nseg, int k, int mode) {
@@ -690,27 +673,37 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   MDS_TRY(flagged.alloc(ctx, sizeof(int) * (size_t)std::max(nfit, 1)));
   MDS_TRY(nflag.alloc(ctx, sizeof(int)));
   MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
-  DevBuf big(ctx), nbig(ctx);
+  DevBuf big(ctx), nbig(ctx), cidx(ctx), meta(ctx), evals(ctx);
   auto recheck = [&](int nrows, const int* rowlist, int mode, const uint64_t* cand, const int* cand_n, int nseg,
                      int Kp, const float* rowthr) -> int {
     size_t smem = data_recheck_smem(dim, Kp, nseg, k, mode);
     if (smem > 227 * 1024) return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "knn_data recheck: dim/k too large");
-    const size_t wsmem = data_recheck_warp_smem(dim);
-    if (mode == 0 && !rowlist && nrows > 0 && wsmem <= 96 * 1024 && k + 1 <= RW_MAXK1 && Kp <= RW_MAXC) {
-      // a warp per row; the rows it cannot hold go to the block kernel
+    if (mode == 0 && !rowlist && nrows > 0 && k + 1 <= RW_MAXK1) {
+      // three stages (candidates, dense exact values, finish); the rows they
+      // cannot finish go to the block kernel
+      const int fw = k + 3;
       MDS_TRY(big.alloc(ctx, sizeof(int) * (size_t)nrows));
       MDS_TRY(nbig.alloc(ctx, sizeof(int)));
+      MDS_TRY(cidx.alloc(ctx, sizeof(int) * (size_t)nrows * fw));
+      MDS_TRY(meta.alloc(ctx, sizeof(int4) * (size_t)nrows));
+      MDS_TRY(evals.alloc(ctx, sizeof(double) * (size_t)nrows * fw));
       MDS_CUDA(ctx, cudaMemsetAsync(nbig.p, 0, sizeof(int), s));
-      MDS_CUDA(ctx, cudaFuncSetAttribute(k_data_recheck_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)wsmem));
-      st.launches++;
-      k_data_recheck_warp<<<(nrows + RW_WARPS - 1) / RW_WARPS, RW_WARPS * 32, wsmem, s>>>(
-          dfit, dref, mf, sf, Mr.as<double>(), Sr.as<double>(), nrows, dim, corr, cand, cand_n, nseg, Kp, k, rowthr,
-          dout_d, dout_i, flagged.as<int>(), nflag.as<int>(), big.as<int>(), nbig.as<int>());
+      const int wb = (nrows + RW_WARPS - 1) / RW_WARPS;
+      st.launches += 3;
+      k_recheck_cands<<<wb, RW_WARPS * 32, 0, s>>>(cand, cand_n, nrows, nseg, Kp, k + 1, fw, rowthr, cidx.as<int>(),
+                                                   meta.as<int4>(), big.as<int>(), nbig.as<int>());
+      const int64_t slots = (int64_t)nrows * fw;
+      k_recheck_exact<<<(int)((slots + 255) / 256), 256, 0, s>>>(dfit, dref, mf, sf, Mr.as<double>(), Sr.as<double>(),
+                                                                 nrows, dim, corr, fw, cidx.as<int>(),
+                                                                 meta.as<int4>(), evals.as<double>());
+      k_recheck_finish<<<wb, RW_WARPS * 32, 0, s>>>(nrows, k, fw, cidx.as<int>(), meta.as<int4>(),
+                                                    evals.as<double>(), dout_d, dout_i, flagged.as<int>(),
+                                                    nflag.as<int>(), big.as<int>(), nbig.as<int>());
       MDS_CUDA(ctx, cudaGetLastError());
       int hbig = 0;
       MDS_CUDA(ctx, cudaMemcpyAsync(&hbig, nbig.p, sizeof(int), cudaMemcpyDeviceToHost, s));
       MDS_CUDA(ctx, cudaStreamSynchronize(s));
+      st.recheck_pairs = slots;
       if (hbig == 0) return MDS_OK;
       rowlist = big.as<int>();
       nrows = hbig;

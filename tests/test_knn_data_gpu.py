@@ -10,6 +10,13 @@ from mdsctk_gb300 import synth
 REF = os.path.join(os.path.dirname(__file__), "golden")
 
 
+def _recheck_launches(k):
+    """Launches of the candidate recheck: three stages (candidates, exact
+    values, finish) for k + 1 <= 64, plus the block kernel when some rows
+    need all their candidates; one block kernel launch otherwise."""
+    return (3, 4) if k + 1 <= 64 else (1,)
+
+
 def _check(d, i, od, oi):
     assert d.shape == od.shape
     # distances are computed in the reference's own arithmetic: bit-identical
@@ -67,7 +74,7 @@ def test_knn_data_tc_vonmises(ctx, oracle, corr):
     od, oi = oracle.knn_data(x, None, 20, correlation=corr)
     _check(d, i, od, oi)
     assert st["rows_flagged"] == 0
-    assert st["launches"] == 4  # prep, BF16 split, tensor-core screen, recheck
+    assert st["launches"] - 3 in _recheck_launches(20)  # prep, BF16 split, tensor-core screen, recheck
 
 
 @pytest.mark.gpu
@@ -81,7 +88,7 @@ def test_knn_data_tc_fit_vs_ref(ctx, oracle, nref, nfit, dim, k):
     st = ctx.stats()
     od, oi = oracle.knn_data(ref, fit, k)
     _check(d, i, od, oi)
-    assert st["launches"] == 6  # two preps, two splits, screen, recheck
+    assert st["launches"] - 5 in _recheck_launches(k)  # two preps, two splits, screen, recheck
 
 
 @pytest.mark.gpu
@@ -119,7 +126,7 @@ def test_knn_data_tc_fallback_shapes(ctx, oracle):
     rng = np.random.default_rng(5)
     x = rng.normal(size=(400, 130))
     d, i = ctx.knn_data(x, None, 9, precision="bf16x3")
-    assert ctx.stats()["launches"] == 3  # prep, FP32 screen, recheck
+    assert ctx.stats()["launches"] - 2 in _recheck_launches(9)  # prep, FP32 screen, recheck
     od, oi = oracle.knn_data(x, None, 9)
     _check(d, i, od, oi)
     x = rng.normal(size=(600, 4))
@@ -166,10 +173,10 @@ def test_knn_data_tc_pilot_pass(ctx, oracle, fit_rows, skip):
     st = ctx.stats()
     od, oi = oracle.knn_data(ref, fit, 12)
     _check(d, i, od, oi)
-    plain = 5 if fit is None else 7  # prep(s), split(s), pilot, screen, recheck
+    plain = 4 if fit is None else 6  # prep(s), split(s), pilot, screen
     # in locality order: no pilot pass (each row pair's near segment goes first)
     extra = (ORDER_LAUNCHES_SAME if fit is None else ORDER_LAUNCHES_FIT) - 1 if skip else 0
-    assert st["launches"] == plain + extra
+    assert st["launches"] - plain - extra in _recheck_launches(12)
 
 
 def _sampled(ctx, oracle, ref, fit, k, rows):
