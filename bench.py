@@ -368,6 +368,15 @@ def run_pipeline(args):
                     Qg = np.linalg.qr(Vg[g].T)[0]
                     Qo = np.linalg.qr(Vo_[g].T)[0]
                     res_g.append(float(np.linalg.norm(Qg - Qo @ (Qo.T @ Qg), 2)))
+                # eigenvalue 1 of the normalised affinity has one copy per
+                # connected component of the neighbour graph: a Krylov solver
+                # (ARPACK as much as this one) need not return them all
+                from scipy.sparse import csc_matrix
+                from scipy.sparse.csgraph import connected_components
+                G = csc_matrix((np.ones(len(irow)), np.asarray(irow), np.asarray(pcol)), shape=(nn, nn))
+                st["graph_components"] = int(connected_components(G, directed=False)[0])
+                st["eigenvalue_1_copies_gpu"] = int(np.sum(np.abs(w - 1.0) < 1e-12))
+                st["eigenvalue_1_copies_eigsh"] = int(np.sum(np.abs(np.asarray(wo) - 1.0) < 1e-12))
                 st["parity_evec_groups"] = [len(g) for g in groups]
                 st["parity_evec_group_max_residual_vs_eigsh"] = max(res_g) if res_g else None
                 st["parity_evec_groups_checked"] = len(res_g)
