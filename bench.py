@@ -93,6 +93,7 @@ def parse():
                         "sparse = contact_profile of 20,000 x 304 frames (atoms 0-151 vs 152-303, 12 A) "
                         "-> knn_data_sparse, k=32")
     p.add_argument("--pipeline-cpu", action="store_true", help="also time the CPU oracle's sysparse and eigsh")
+    p.add_argument("--vectors", type=int, default=200_000, help="--pipeline euclid: vectors in the set")
     p.add_argument("--precision-report", action="store_true",
                    help="per-pair screen RMSD error vs FP64 and output agreement on sampled rows")
     return p.parse_args()
@@ -414,7 +415,7 @@ def run_pipeline(args):
             st["parity_rows_checked"] = len(rows)
             st["parity_bit_exact_distances"] = bool(np.array_equal(d[rows], od))
         else:
-            n, dim, k = 200_000, 64, 32
+            n, dim, k = args.vectors, 64, 32
             x = synth.dihedral_vectors(n, dim, seed=SEED + 13).astype(np.float64)
             out["config"] = {"workload": f"knn_data {n} x {dim} (f64), k={k}", "precision": args.precision}
             d, i = timed("knn_data", lambda: c.knn_data(x, None, k, precision=args.precision), c)
