@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "knn_common.cuh"
+#include "warp_sort.cuh"
 
 #define DT_TM 64
 #define DT_TN 64
@@ -397,37 +398,6 @@ k_data_recheck(const double* __restrict__ Xfit, const double* __restrict__ Xref,
 #define RW_MAXT 512   // merged candidates a warp sorts in registers
 #define RW_MAXK1 64   // k + 1 (the first batch, k + 3, fits the finishing sort of 128)
 
-template <int PER>
-__device__ __forceinline__ void wsort_u64(uint64_t (&v)[PER], int lane) {
-#pragma unroll
-  for (int k = 2; k <= 32 * PER; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      if (j >= 32) {
-#pragma unroll
-        for (int i = 0; i < PER; ++i) {
-          const int p = i ^ (j >> 5);
-          if (p > i) {
-            const bool up = ((i * 32 + lane) & k) == 0;
-            const uint64_t a = v[i], b = v[p];
-            if ((a > b) == up) {
-              v[i] = b;
-              v[p] = a;
-            }
-          }
-        }
-      } else {
-#pragma unroll
-        for (int i = 0; i < PER; ++i) {
-          const int e = i * 32 + lane;
-          const uint64_t o = __shfl_xor_sync(0xffffffffu, v[i], j);
-          v[i] = (((e & j) == 0) == ((e & k) == 0)) ? min(v[i], o) : max(v[i], o);
-        }
-      }
-    }
-  }
-}
-
 // (value bits, index) pairs in ascending (value, index) order; the values
 // are non-negative or +inf, so their bits order as unsigned integers
 __device__ __forceinline__ bool pair_less(uint64_t a, int ia, uint64_t b, int ib) {
@@ -470,18 +440,6 @@ __device__ __forceinline__ void wsort_pair(uint64_t (&v)[PER], int (&x)[PER], in
       }
     }
   }
-}
-
-// Element e (any e < 32 PER, per lane) of a warp-distributed array.
-template <int PER>
-__device__ __forceinline__ uint64_t lane_elem(const uint64_t (&v)[PER], int e) {
-  uint64_t r = 0;
-#pragma unroll
-  for (int i = 0; i < PER; ++i) {
-    const uint64_t y = __shfl_sync(0xffffffffu, v[i], e & 31);
-    if (i == (e >> 5)) r = y;
-  }
-  return r;
 }
 
 // Stage 1, one warp per fit row: merge the segments' lists, sort the keys
