@@ -155,10 +155,7 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const fl
                    const int* cand_n, int nseg, int segstride, int Kp, int k, double* out_d, int* out_i,
                    int* flagged, int* nflag, const float* rowthr = nullptr, const RecheckAudit* audit = nullptr,
                    int cand_by_row = 0);
-int launch_recheck_rows(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
-                        const float* Ur, int nrows, const uint64_t* cand, const int* cand_n, int nseg, int segstride,
-                        int Kp, int k, double* out_d, int* out_i, int* flagged, int* nflag, const float* rowthr,
-                        const RecheckAudit* audit, long long* pairs_out);
+
 int choose_nseg_fp32(int nfit, int num_sms, int nref);
 
 // Candidates wanted per row before rounding: k+33, 2(k+1), and with the

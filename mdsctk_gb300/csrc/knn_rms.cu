@@ -28,9 +28,7 @@
 #include <vector>
 
 #include "knn_common.cuh"
-#include "warp_sort.cuh"
 #include "qcp.cuh"
-#include "tc_ptx.cuh"
 
 // ---------------------------------------------------------------------------
 // 1. centring
@@ -665,6 +663,31 @@ __device__ __forceinline__ float pair_rmsd2(const float* w, const float* C6, con
                            P[3] - P[1]);
 }
 
+// The sums of one pair over four atoms: D += |d|^2 and Q[3r+s] += a_i,r d_s
+// (unless nofit), d = a_i - a_j; x* = a_i's and y* = a_j's x, y, z of the
+// four atoms, two atoms per packed instruction.
+__device__ __forceinline__ void pair_acc4(float2 (&w)[10], const float4& ia, const float4& ib, const float4& ic,
+                                          const float4& ja, const float4& jb, const float4& jc, bool nofit) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  const float2 x0[2] = {make_float2(ia.x, ia.y), make_float2(ia.z, ia.w)};
+  const float2 x1[2] = {make_float2(ib.x, ib.y), make_float2(ib.z, ib.w)};
+  const float2 x2[2] = {make_float2(ic.x, ic.y), make_float2(ic.z, ic.w)};
+  const float2 y0[2] = {make_float2(ja.x, ja.y), make_float2(ja.z, ja.w)};
+  const float2 y1[2] = {make_float2(jb.x, jb.y), make_float2(jb.z, jb.w)};
+  const float2 y2[2] = {make_float2(jc.x, jc.y), make_float2(jc.z, jc.w)};
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float2 d0 = __ffma2_rn(y0[e], m1, x0[e]), d1 = __ffma2_rn(y1[e], m1, x1[e]);
+    const float2 d2 = __ffma2_rn(y2[e], m1, x2[e]);
+    w[0] = __ffma2_rn(d0, d0, __ffma2_rn(d1, d1, __ffma2_rn(d2, d2, w[0])));
+    if (!nofit) {
+      w[1] = __ffma2_rn(x0[e], d0, w[1]); w[2] = __ffma2_rn(x0[e], d1, w[2]); w[3] = __ffma2_rn(x0[e], d2, w[3]);
+      w[4] = __ffma2_rn(x1[e], d0, w[4]); w[5] = __ffma2_rn(x1[e], d1, w[5]); w[6] = __ffma2_rn(x1[e], d2, w[6]);
+      w[7] = __ffma2_rn(x2[e], d0, w[7]); w[8] = __ffma2_rn(x2[e], d1, w[8]); w[9] = __ffma2_rn(x2[e], d2, w[9]);
+    }
+  }
+}
+
 __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restrict__ ui, const float* C6,
                               const float* __restrict__ Ar, const float* __restrict__ Ur, int Ap, const int* cj,
                               int nc, bool nofit, float* sd, float* ssum) {
@@ -680,49 +703,54 @@ __device__ void recheck_chunk(const float* __restrict__ sa, const float* __restr
   const int grp = lane / RC_GW, gl = lane % RC_GW;
   const int Ap4 = Ap >> 2;
   const float4* sa4 = reinterpret_cast<const float4*>(sa);
-  for (int c0 = CPW * warp; c0 < nc; c0 += CPW * nw) {
-    const int c = c0 + grp;
-    const bool valid = c < nc;
-    const float4* aj4 = reinterpret_cast<const float4*>(Ar + (int64_t)cj[valid ? c : c0] * 3 * Ap);
+  // Each group takes two candidates at once (c and c + CPW), so every shared
+  // load of the row serves two pairs: per four atoms of a pair 4.5 loads
+  // through the L1TEX pipe instead of 6.
+  for (int c0 = 2 * CPW * warp; c0 < nc; c0 += 2 * CPW * nw) {
+    const int ca = c0 + grp, cb = c0 + CPW + grp;
+    const bool va = ca < nc, vb = cb < nc;
+    const float4* aja = reinterpret_cast<const float4*>(Ar + (int64_t)cj[va ? ca : c0] * 3 * Ap);
+    const float4* ajb = reinterpret_cast<const float4*>(Ar + (int64_t)cj[vb ? cb : c0] * 3 * Ap);
     // Packed FP32 arithmetic (two atoms per instruction, each lane keeping
     // two partial sums per quantity): d = a_i - a_j as fma(a_j, -1, a_i),
     // exact in the product, one rounding like the subtraction.
-    float2 w[10];
+    float2 wa[10], wb[10];
 #pragma unroll
-    for (int i = 0; i < 10; ++i) w[i] = make_float2(0.0f, 0.0f);
-    const float2 m1 = make_float2(-1.0f, -1.0f);
+    for (int i = 0; i < 10; ++i) {
+      wa[i] = make_float2(0.0f, 0.0f);
+      wb[i] = make_float2(0.0f, 0.0f);
+    }
     for (int q = gl; q < Ap4; q += RC_GW) {
       const float4 ia = sa4[q], ib = sa4[Ap4 + q], ic = sa4[2 * Ap4 + q];
-      const float4 ja = __ldg(aj4 + q), jb = __ldg(aj4 + Ap4 + q), jc = __ldg(aj4 + 2 * Ap4 + q);
-      const float2 x0[2] = {make_float2(ia.x, ia.y), make_float2(ia.z, ia.w)};
-      const float2 x1[2] = {make_float2(ib.x, ib.y), make_float2(ib.z, ib.w)};
-      const float2 x2[2] = {make_float2(ic.x, ic.y), make_float2(ic.z, ic.w)};
-      const float2 y0[2] = {make_float2(ja.x, ja.y), make_float2(ja.z, ja.w)};
-      const float2 y1[2] = {make_float2(jb.x, jb.y), make_float2(jb.z, jb.w)};
-      const float2 y2[2] = {make_float2(jc.x, jc.y), make_float2(jc.z, jc.w)};
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        const float2 d0 = __ffma2_rn(y0[e], m1, x0[e]), d1 = __ffma2_rn(y1[e], m1, x1[e]);
-        const float2 d2 = __ffma2_rn(y2[e], m1, x2[e]);
-        w[0] = __ffma2_rn(d0, d0, __ffma2_rn(d1, d1, __ffma2_rn(d2, d2, w[0])));
-        if (!nofit) {
-          w[1] = __ffma2_rn(x0[e], d0, w[1]); w[2] = __ffma2_rn(x0[e], d1, w[2]); w[3] = __ffma2_rn(x0[e], d2, w[3]);
-          w[4] = __ffma2_rn(x1[e], d0, w[4]); w[5] = __ffma2_rn(x1[e], d1, w[5]); w[6] = __ffma2_rn(x1[e], d2, w[6]);
-          w[7] = __ffma2_rn(x2[e], d0, w[7]); w[8] = __ffma2_rn(x2[e], d1, w[8]); w[9] = __ffma2_rn(x2[e], d2, w[9]);
-        }
-      }
+      const float4 ja = __ldg(aja + q), jb = __ldg(aja + Ap4 + q), jc = __ldg(aja + 2 * Ap4 + q);
+      const float4 ka = __ldg(ajb + q), kb = __ldg(ajb + Ap4 + q), kc = __ldg(ajb + 2 * Ap4 + q);
+      pair_acc4(wa, ia, ib, ic, ja, jb, jc, nofit);
+      pair_acc4(wb, ia, ib, ic, ka, kb, kc, nofit);
     }
-    float v[10];
+    float v[10], u[10];
 #pragma unroll
-    for (int i = 0; i < 10; ++i) v[i] = w[i].x + w[i].y;
+    for (int i = 0; i < 10; ++i) {
+      v[i] = wa[i].x + wa[i].y;
+      u[i] = wb[i].x + wb[i].y;
+    }
     // sums over the lanes of each group (one shuffle serves every group)
 #pragma unroll
     for (int i = 0; i < 10; ++i)
-      for (int o = RC_GW / 2; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
-    if (valid && gl == 0) {
-      float2* w2 = reinterpret_cast<float2*>(ssum + c * 10);
+      for (int o = RC_GW / 2; o > 0; o >>= 1) {
+        v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+        u[i] += __shfl_xor_sync(0xffffffffu, u[i], o);
+      }
+    if (gl == 0) {
+      if (va) {
+        float2* w2 = reinterpret_cast<float2*>(ssum + ca * 10);
 #pragma unroll
-      for (int i = 0; i < 5; ++i) w2[i] = make_float2(v[2 * i], v[2 * i + 1]);
+        for (int i = 0; i < 5; ++i) w2[i] = make_float2(v[2 * i], v[2 * i + 1]);
+      }
+      if (vb) {
+        float2* w2 = reinterpret_cast<float2*>(ssum + cb * 10);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) w2[i] = make_float2(u[2 * i], u[2 * i + 1]);
+      }
     }
   }
   __syncthreads();
@@ -822,7 +850,7 @@ __device__ int merge_row_cands(const uint64_t* __restrict__ cand, const int* __r
 // K' keys, recheck, select k+1. mode 1: every reference is a candidate
 // (exact row). mode 2 (full matrix): write every exact distance in reference
 // order. Output: out_d/out_i rows of width `width` at row index grow.
-__global__ void __launch_bounds__(RC_THREADS, 4)
+__global__ void __launch_bounds__(RC_THREADS, 2)
 k_recheck(const float* __restrict__ Af, const float* __restrict__ Ar, const float* __restrict__ mu,
           const float* __restrict__ Ur, int nrows,
           const int* __restrict__ rowlist, int Nr, int Ap, int natoms, int nofit, int mode,
@@ -1086,393 +1114,6 @@ int launch_recheck(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const fl
                                                         audit ? audit->guard : 0.0f,
                                                         audit ? audit->counters : nullptr, cand_by_row);
   MDS_CUDA(ctx, cudaGetLastError());
-  return MDS_OK;
-}
-
-// ---------------------------------------------------------------------------
-// 4b. the candidate recheck (mode 0) over blocks of consecutive fit rows
-// ---------------------------------------------------------------------------
-// Consecutive frames of a trajectory share most of their candidates: the
-// lists of 4 consecutive rows hold about 1.035 times the candidates of one.
-// k_recheck reads every candidate's deviations (12 A bytes) once per row
-// through the L1TEX pipe, beside the row's from shared memory, and that pipe
-// bounds it. Here a block takes RR_ROWS consecutive rows and the union of
-// their candidate lists: each union frame is copied once into shared memory
-// by a bulk copy (no L1TEX load instructions), and each row's deviations
-// stay in registers, two warps per row (atom halves), so a pair costs the
-// shared-memory loads of the candidate only. Every union candidate is
-// computed for every row of the block: an exact value the row's own list
-// did not hold can only take a place it is entitled to. A row's sums over
-// its two halves are reduced by a transposing shuffle (31 shuffles for three
-// candidates' 30 sums) and their QCP roots solved 30 pairs at a time.
-#define RR_ROWS 4
-#define RR_THREADS 256  // 2 warps per row
-#define RR_UCAP 512     // union candidates a block holds
-#define RR_HASH 1024    // open-addressing slots for the union (power of two)
-#define RR_CB 3         // candidates per staged batch
-#define RR_NST 2        // staged batches in flight
-#define RR_MAXT 8       // float2 steps per lane over half the atoms: Ap <= 1024
-
-// Per fit row: the merged candidate keys within tau in bound order (cndk
-// [row][Kp]), their count and tau (meta), and C6 / U (rowc [row][24]).
-__global__ void __launch_bounds__(RC_THREADS, 4)
-k_recheck_prep(const float* __restrict__ Af, const float* __restrict__ mu, int nrows, int Ap, int natoms, int nofit,
-               const uint64_t* __restrict__ cand, const int* __restrict__ cand_n, int nseg, int segstride, int Kp,
-               int k, const float* __restrict__ rowthr, uint64_t* __restrict__ cndk, int2* __restrict__ meta,
-               float* __restrict__ rowc) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw);  // next_pow2(2 Kp)
-  __shared__ int s_total;
-  __shared__ double s_red[32 * 6];
-  __shared__ float C6[6];
-  __shared__ float ui[18];
-  __shared__ float redu[(RC_THREADS / 32) * 18];
-  const int row = blockIdx.x;
-  if (row >= nrows) return;
-  if (threadIdx.x < 18) ui[threadIdx.x] = 0.0f;
-  row_constants(Af + (int64_t)row * 3 * Ap, mu, Ap, natoms, nofit, C6, ui, s_red, redu);
-  float tau;
-  const int total = merge_row_cands(cand, cand_n, row, nseg, segstride, Kp, k + 1,
-                                    rowthr ? __ldcg(rowthr + row) : __int_as_float(0x7f800000), keys, &s_total,
-                                    &tau);
-  for (int x = threadIdx.x; x < total; x += blockDim.x) cndk[(int64_t)row * Kp + x] = keys[x];
-  if (threadIdx.x < 24) rowc[(int64_t)row * 24 + threadIdx.x] = (threadIdx.x < 6) ? C6[threadIdx.x] : ui[threadIdx.x - 6];
-  if (threadIdx.x == 0) meta[row] = make_int2(total, __float_as_int(tau));
-}
-
-__host__ __device__ constexpr size_t recheck_rows_smem(int Ap) {
-  return sizeof(float) * (size_t)RR_NST * RR_CB * 3 * Ap + sizeof(int) * (2 * RR_HASH + RR_UCAP) +
-         sizeof(float) * (2 * RR_ROWS * RR_UCAP + RR_ROWS * 32 + RR_ROWS * 32 * 10) + sizeof(int) * RR_ROWS * 32;
-}
-
-// The k+1 best of a row's union values (RMSD, frame), the guard check, the
-// audit of the row's own candidates and the output; one warp.
-template <int PER>
-__device__ void finish_row(const float* val, const int* uidx, const float* bnd, int U, int row, int k, float tau,
-                           const float* __restrict__ recf, const float* __restrict__ recr, float guard,
-                           unsigned long long* __restrict__ audit, double* __restrict__ out_d,
-                           int* __restrict__ out_i, int* __restrict__ flagged, int* __restrict__ nflag, int lane) {
-  uint64_t kk[PER];
-#pragma unroll
-  for (int i = 0; i < PER; ++i) {
-    const int e = i * 32 + lane;
-    kk[i] = (e < U) ? mds_pack_key(val[e], uidx[e]) : MDS_KEY_INF;
-  }
-  wsort_u64<PER>(kk, lane);
-  const int k1 = k + 1;
-  // audit: the row's own candidates carry their screen bound b
-  float a_coef = 0.0f;
-  int a_viol = 0;
-  if (audit) {
-    const float Ei = __ldg(recf + (int64_t)row * MDS_REC + 15);
-    for (int e = lane; e < U; e += 32) {
-      const float b = bnd[e];
-      if (b < __int_as_float(0x7f800000) && b > 0.0f) {  // (bounds clamped at zero carry no error information)
-        const float r2 = val[e] * val[e];
-        const float E = Ei + __ldg(recr + (int64_t)uidx[e] * MDS_REC + 15);
-        if (E > 0.0f) a_coef = fmaxf(a_coef, (b + guard * E - r2) / E);
-        a_viol += (b > r2 * (1.0f + 3e-5f)) ? 1 : 0;
-      }
-    }
-    const unsigned cb = __reduce_max_sync(0xffffffffu, __float_as_uint(fmaxf(a_coef, 0.0f)));
-    a_viol = (int)__reduce_add_sync(0xffffffffu, (unsigned)a_viol);
-    if (lane == 0) {
-      atomicAdd(audit + 0, (unsigned long long)U);
-      if (cb) atomicMax(audit + 2, (unsigned long long)cb);
-      if (a_viol) atomicAdd(audit + 1, (unsigned long long)a_viol);
-    }
-  }
-  // guard: the (k+1)-th exact RMSD^2 must not exceed tau, the smallest lower
-  // bound of every pair outside the union; no rechecked bound may exceed its
-  // exact value
-  const uint64_t kd = lane_elem<PER>(kk, min(k1 - 1, 32 * PER - 1));
-  const double dk = (k1 <= 32 * PER) ? (double)mds_key_value(kd) : (double)__int_as_float(0x7f800000);
-  if (lane == 0 && (a_viol > 0 || !(dk * dk * (1.0 + 1e-6) <= (double)tau))) {
-    flagged[atomicAdd(nflag, 1)] = row;
-    if (a_viol > 0) atomicAdd(audit + 3, 1ull);
-  }
-  for (int x0 = 0; x0 < k; x0 += 32) {
-    const int x = x0 + lane;
-    const uint64_t key = lane_elem<PER>(kk, min(x + 1, 32 * PER - 1));
-    if (x < k) {
-      const bool have = x + 1 < 32 * PER;
-      out_d[(int64_t)row * k + x] = have ? (double)mds_key_value(key) * 10.0 : (double)__int_as_float(0x7f800000);
-      out_i[(int64_t)row * k + x] = have ? mds_key_index(key) : -1;
-    }
-  }
-}
-
-__global__ void __launch_bounds__(RR_THREADS, 2)
-k_recheck_rows(const float* __restrict__ Af, const float* __restrict__ Ar, const float* __restrict__ Ur, int nrows,
-               int Ap, int nofit, const uint64_t* __restrict__ cndk, const int2* __restrict__ meta,
-               const float* __restrict__ rowc, int Kp, int k, double* __restrict__ out_d, int* __restrict__ out_i,
-               int* __restrict__ flagged, int* __restrict__ nflag, const float* __restrict__ recf,
-               const float* __restrict__ recr, float guard, unsigned long long* __restrict__ audit,
-               int* __restrict__ big, int* __restrict__ nbig, int* __restrict__ err) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  const int fsz = 3 * Ap;  // floats per frame
-  float* stage = reinterpret_cast<float*>(smem_raw);                  // [RR_NST][RR_CB][fsz]
-  int* hkey = reinterpret_cast<int*>(stage + (size_t)RR_NST * RR_CB * fsz);  // [RR_HASH] frame or -1
-  int* huid = hkey + RR_HASH;                                          // [RR_HASH] union index of a slot
-  int* uidx = huid + RR_HASH;                                          // [RR_UCAP] frame of a union entry
-  float* bnd = reinterpret_cast<float*>(uidx + RR_UCAP);              // [RR_ROWS][RR_UCAP] own bound or +inf
-  float* val = bnd + RR_ROWS * RR_UCAP;                                // [RR_ROWS][RR_UCAP] exact RMSD
-  float* hs = val + RR_ROWS * RR_UCAP;                                 // [RR_ROWS][32] second half's sums
-  float* fsum = hs + RR_ROWS * 32;                                     // [RR_ROWS][32][10] pending pairs
-  int* pu = reinterpret_cast<int*>(fsum + RR_ROWS * 32 * 10);         // [RR_ROWS][32] their union entries
-  __shared__ uint64_t full[RR_NST];
-  __shared__ int s_u, s_ovf, s_nw[RR_ROWS];
-  __shared__ volatile int s_abort;
-  __shared__ float s_tau[RR_ROWS], s_c[RR_ROWS][24];
-  __shared__ int s_scan[RR_THREADS / 32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int r = warp >> 1, h = warp & 1;
-  const int row0 = blockIdx.x * RR_ROWS;
-  const float INF = __int_as_float(0x7f800000);
-
-  for (int e = tid; e < RR_HASH; e += RR_THREADS) hkey[e] = -1;
-  if (tid < RR_ROWS) {
-    const int row = row0 + tid;
-    const int2 m = (row < nrows) ? meta[row] : make_int2(0, 0x7f800000);
-    s_nw[tid] = m.x;
-    s_tau[tid] = __int_as_float(m.y);
-  }
-  if (tid < RR_ROWS * 24) {
-    const int rr = tid / 24, row = row0 + rr;
-    s_c[rr][tid % 24] = (row < nrows) ? rowc[(int64_t)row * 24 + tid % 24] : 0.0f;
-  }
-  if (tid == 0) {
-    for (int s = 0; s < RR_NST; ++s) mbar_init(&full[s], 1);
-    mbar_fence_init();
-    s_ovf = 0;
-    s_abort = 0;
-  }
-  __syncthreads();
-  // union of the rows' candidates: open addressing with linear probing
-  for (int rr = 0; rr < RR_ROWS; ++rr) {
-    const int nw = s_nw[rr];
-    for (int p = tid; p < nw; p += RR_THREADS) {
-      const int j = mds_key_index(cndk[(int64_t)(row0 + rr) * Kp + p]);
-      uint32_t sl = ((uint32_t)j * 2654435761u) >> 22;
-      bool in = false;
-      for (int probe = 0; probe < RR_HASH && !in; ++probe) {
-        const int prev = atomicCAS(&hkey[sl], -1, j);
-        in = (prev == -1 || prev == j);
-        sl = (sl + 1) & (RR_HASH - 1);
-      }
-      if (!in) s_ovf = 1;
-    }
-  }
-  __syncthreads();
-  // union index of every occupied slot, in slot order (block scan, 4 slots a thread)
-  {
-    int c[4], n = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      c[q] = hkey[4 * tid + q] >= 0;
-      n += c[q];
-    }
-    int inc = n;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += y;
-    }
-    if (lane == 31) s_scan[warp] = inc;
-    __syncthreads();
-    int pos = inc - n;
-    for (int w = 0; w < warp; ++w) pos += s_scan[w];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      huid[4 * tid + q] = c[q] ? pos : -1;
-      if (c[q] && pos < RR_UCAP) uidx[pos] = hkey[4 * tid + q];
-      pos += c[q];
-    }
-    if (tid == RR_THREADS - 1) s_u = pos;
-  }
-  __syncthreads();
-  const int U = s_u;
-  if (U > RR_UCAP || s_ovf) {  // (uniform) the block kernel takes these rows
-    if (tid < RR_ROWS && row0 + tid < nrows) big[atomicAdd(nbig, 1)] = row0 + tid;
-    return;
-  }
-  for (int e = tid; e < RR_ROWS * RR_UCAP; e += RR_THREADS) bnd[e] = INF;
-  __syncthreads();
-  for (int rr = 0; rr < RR_ROWS; ++rr) {
-    const int nw = s_nw[rr];
-    for (int p = tid; p < nw; p += RR_THREADS) {
-      const uint64_t key = cndk[(int64_t)(row0 + rr) * Kp + p];
-      const int j = mds_key_index(key);
-      uint32_t sl = ((uint32_t)j * 2654435761u) >> 22;
-      for (int probe = 0; probe < RR_HASH && hkey[sl] != j; ++probe) sl = (sl + 1) & (RR_HASH - 1);
-      bnd[rr * RR_UCAP + huid[sl]] = mds_key_value(key);
-    }
-  }
-  // the union frames, RR_CB per batch, RR_NST batches in flight
-  const int nb = (U + RR_CB - 1) / RR_CB;
-  const uint32_t fbytes = (uint32_t)fsz * 4u;
-  auto issue = [&](int b) {
-    const int st = b % RR_NST, nc = min(RR_CB, U - b * RR_CB);
-    mbar_expect_tx(&full[st], (uint32_t)nc * fbytes);
-    for (int c = 0; c < nc; ++c)
-      bulk_load(stage + (size_t)(st * RR_CB + c) * fsz, Ar + (int64_t)uidx[b * RR_CB + c] * fsz, fbytes, &full[st]);
-  };
-  __syncthreads();
-  if (tid == 0)
-    for (int b = 0; b < min(RR_NST, nb); ++b) issue(b);
-  // this warp's half of its row's deviations, two atoms per float2
-  const int row = row0 + r;
-  const int nt = Ap / 128;
-  const int a0 = h * (Ap / 2) + 2 * lane;
-  const float* af = Af + (int64_t)min(row, nrows - 1) * fsz;
-  float2 xa[RR_MAXT], xb[RR_MAXT], xc[RR_MAXT];
-#pragma unroll
-  for (int t = 0; t < RR_MAXT; ++t) {
-    const int a = a0 + 64 * t;
-    const bool in = t < nt;
-    xa[t] = in ? *reinterpret_cast<const float2*>(af + a) : make_float2(0.f, 0.f);
-    xb[t] = in ? *reinterpret_cast<const float2*>(af + Ap + a) : make_float2(0.f, 0.f);
-    xc[t] = in ? *reinterpret_cast<const float2*>(af + 2 * Ap + a) : make_float2(0.f, 0.f);
-  }
-  const float2 m1 = make_float2(-1.0f, -1.0f);
-  int pend = 0;  // this row's pairs waiting for their QCP solve (kept by warp h = 0)
-  float* fr = fsum + r * 32 * 10;
-  int* pr = pu + r * 32;
-  auto solve = [&]() {  // warp h = 0: the pending pairs, one per lane
-    __syncwarp();
-    if (lane < pend)
-      val[r * RR_UCAP + pr[lane]] =
-          sqrtf(fmaxf(pair_rmsd2(fr + lane * 10, s_c[r], s_c[r] + 6, Ur + (int64_t)uidx[pr[lane]] * 18, nofit), 0.0f));
-    __syncwarp();
-    pend = 0;
-  };
-  bool ok = true;
-  int bfail = nb;
-  for (int b = 0; b < nb; ++b) {
-    const int st = b % RR_NST;
-    const bool got = mbar_wait(&full[st], (uint32_t)(b / RR_NST) & 1u, &s_abort, 200000000ull);
-    if (!__syncthreads_and(got)) {
-      ok = false;
-      bfail = b;
-      break;
-    }
-    const int nc = min(RR_CB, U - b * RR_CB);
-    float v[32];
-#pragma unroll
-    for (int c = 0; c < RR_CB; ++c) {
-      float2 w[10];
-#pragma unroll
-      for (int i = 0; i < 10; ++i) w[i] = make_float2(0.f, 0.f);
-      if (c < nc) {
-        const float* y = stage + (size_t)(st * RR_CB + c) * fsz;
-#pragma unroll
-        for (int t = 0; t < RR_MAXT; ++t) {
-          if (t < nt) {
-            const int a = a0 + 64 * t;
-            const float2 ya = *reinterpret_cast<const float2*>(y + a);
-            const float2 yb = *reinterpret_cast<const float2*>(y + Ap + a);
-            const float2 yc = *reinterpret_cast<const float2*>(y + 2 * Ap + a);
-            // d = a_i - a_j as fma(a_j, -1, a_i): exact in the product
-            const float2 d0 = __ffma2_rn(ya, m1, xa[t]), d1 = __ffma2_rn(yb, m1, xb[t]);
-            const float2 d2 = __ffma2_rn(yc, m1, xc[t]);
-            w[0] = __ffma2_rn(d0, d0, __ffma2_rn(d1, d1, __ffma2_rn(d2, d2, w[0])));
-            if (!nofit) {
-              w[1] = __ffma2_rn(xa[t], d0, w[1]); w[2] = __ffma2_rn(xa[t], d1, w[2]); w[3] = __ffma2_rn(xa[t], d2, w[3]);
-              w[4] = __ffma2_rn(xb[t], d0, w[4]); w[5] = __ffma2_rn(xb[t], d1, w[5]); w[6] = __ffma2_rn(xb[t], d2, w[6]);
-              w[7] = __ffma2_rn(xc[t], d0, w[7]); w[8] = __ffma2_rn(xc[t], d1, w[8]); w[9] = __ffma2_rn(xc[t], d2, w[9]);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < 10; ++i) v[c * 10 + i] = w[i].x + w[i].y;
-    }
-    v[30] = 0.0f;
-    v[31] = 0.0f;
-    float tot = warp_sum_transpose32(v, lane);  // lane l: sum l % 10 of candidate l / 10
-    if (h == 1) hs[r * 32 + lane] = tot;
-    bar_named(1 + r, 64);
-    if (h == 0) {
-      if (pend + RR_CB > 32) solve();
-      tot += hs[r * 32 + lane];
-      const int c = lane / 10;
-      if (lane < 10 * RR_CB && c < nc) {
-        fr[(pend + c) * 10 + lane % 10] = tot;
-        if (lane % 10 == 0) pr[pend + c] = b * RR_CB + c;
-      }
-      pend += nc;
-    }
-    __syncthreads();  // the batch's stage buffer and hs are free
-    if (tid == 0 && b + RR_NST < nb) issue(b + RR_NST);
-  }
-  if (!ok) {
-    if (tid == 0) {
-      atomicMax(err, 1);
-      // let the copies in flight (batches bfail .. bfail + RR_NST - 1) land,
-      // each wait bounded, before the block exits
-      volatile int dummy = 0;
-      for (int b = bfail; b < min(nb, bfail + RR_NST); ++b)
-        mbar_wait(&full[b % RR_NST], (uint32_t)(b / RR_NST) & 1u, &dummy, 50000000ull);
-    }
-    return;
-  }
-  if (h == 0) solve();
-  __syncthreads();
-  if (h != 0 || row >= nrows) return;
-  const float* vr = val + r * RR_UCAP;
-  const float* br = bnd + r * RR_UCAP;
-  const float tau = s_tau[r];
-  if (U <= 64)
-    finish_row<2>(vr, uidx, br, U, row, k, tau, recf, recr, guard, audit, out_d, out_i, flagged, nflag, lane);
-  else if (U <= 128)
-    finish_row<4>(vr, uidx, br, U, row, k, tau, recf, recr, guard, audit, out_d, out_i, flagged, nflag, lane);
-  else if (U <= 256)
-    finish_row<8>(vr, uidx, br, U, row, k, tau, recf, recr, guard, audit, out_d, out_i, flagged, nflag, lane);
-  else
-    finish_row<16>(vr, uidx, br, U, row, k, tau, recf, recr, guard, audit, out_d, out_i, flagged, nflag, lane);
-}
-
-// Mode 0 recheck of all nrows fit rows in order: k_recheck_prep, then
-// k_recheck_rows; the rows it cannot take (a union above RR_UCAP) go to
-// k_recheck. Returns MDS_ERR_UNSUPPORTED (nothing launched) when the shape
-// is outside the kernel's limits: Ap a multiple of 128 up to 128 RR_MAXT.
-int launch_recheck_rows(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Af, const float* Ar, const float* mu,
-                        const float* Ur, int nrows, const uint64_t* cand, const int* cand_n, int nseg, int segstride,
-                        int Kp, int k, double* out_d, int* out_i, int* flagged, int* nflag, const float* rowthr,
-                        const RecheckAudit* audit, long long* pairs_out) {
-  const int Ap = pl.Ap;
-  if (Ap % 128 || Ap > 128 * RR_MAXT || nrows <= 0 || !audit) return MDS_ERR_UNSUPPORTED;
-  const size_t smem_rows = recheck_rows_smem(Ap);
-  const size_t smem_prep = sizeof(uint64_t) * (size_t)next_pow2(2 * Kp);
-  static bool attr_r = false, attr_p = false;
-  static size_t lim_r = 0, lim_p = 0;
-  MDS_TRY(mds_allow_dyn_smem(ctx, k_recheck_rows, &attr_r, &lim_r));
-  MDS_TRY(mds_allow_dyn_smem(ctx, k_recheck_prep, &attr_p, &lim_p));
-  if (smem_rows > lim_r || smem_prep > lim_p) return MDS_ERR_UNSUPPORTED;
-  cudaStream_t s = ctx->stream;
-  DevBuf cndk(ctx), meta(ctx), rowc(ctx), big(ctx), nbig(ctx), err(ctx);
-  MDS_TRY(cndk.alloc(ctx, sizeof(uint64_t) * (size_t)nrows * Kp));
-  MDS_TRY(meta.alloc(ctx, sizeof(int2) * (size_t)nrows));
-  MDS_TRY(rowc.alloc(ctx, sizeof(float) * 24 * (size_t)nrows));
-  MDS_TRY(big.alloc(ctx, sizeof(int) * (size_t)nrows));
-  MDS_TRY(nbig.alloc(ctx, 2 * sizeof(int)));
-  MDS_CUDA(ctx, cudaMemsetAsync(nbig.p, 0, 2 * sizeof(int), s));
-  ctx->stats.launches += 2;
-  k_recheck_prep<<<nrows, RC_THREADS, smem_prep, s>>>(Af, mu, nrows, Ap, pl.natoms, pl.nofit, cand, cand_n, nseg,
-                                                      segstride, Kp, k, rowthr, cndk.as<uint64_t>(), meta.as<int2>(),
-                                                      rowc.as<float>());
-  k_recheck_rows<<<(nrows + RR_ROWS - 1) / RR_ROWS, RR_THREADS, smem_rows, s>>>(
-      Af, Ar, Ur, nrows, Ap, pl.nofit, cndk.as<uint64_t>(), meta.as<int2>(), rowc.as<float>(), Kp, k, out_d, out_i,
-      flagged, nflag, audit->recf, audit->recr, audit->guard, audit->counters, big.as<int>(), nbig.as<int>(),
-      nbig.as<int>() + 1);
-  MDS_CUDA(ctx, cudaGetLastError());
-  int h[2] = {0, 0};
-  MDS_CUDA(ctx, cudaMemcpyAsync(h, nbig.p, sizeof(h), cudaMemcpyDeviceToHost, s));
-  MDS_CUDA(ctx, cudaStreamSynchronize(s));
-  if (h[1]) return mds_fail(ctx, MDS_ERR_TIMEOUT, "recheck: a bounded wait for a staged frame timed out");
-  if (h[0] > 0)
-    MDS_TRY(launch_recheck(ctx, pl, Af, Ar, mu, Ur, h[0], big.as<int>(), 0, cand, cand_n, nseg, segstride, Kp, k,
-                           out_d, out_i, flagged, nflag, rowthr, audit, 1));
-  (void)pairs_out;
   return MDS_OK;
 }
 
@@ -1794,19 +1435,9 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   audit.recr = Rr.as<float>();
   audit.guard = (pl.prec == MDS_PREC_FP32) ? pl.guard_fp32 : pl.guard_tc;
   audit.counters = audit_c.as<unsigned long long>();
-  {
-    // consecutive rows share their candidates: recheck them in blocks of rows
-    // where the shape allows, else one block per row
-    int rc = launch_recheck_rows(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit,
-                                 cand.as<uint64_t>(), cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i,
-                                 flagged.as<int>(), nflag.as<int>(), rowthr.p ? rowthr.as<float>() : nullptr, &audit,
-                                 nullptr);
-    if (rc == MDS_ERR_UNSUPPORTED)
-      rc = launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 0,
-                          cand.as<uint64_t>(), cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i,
-                          flagged.as<int>(), nflag.as<int>(), rowthr.p ? rowthr.as<float>() : nullptr, &audit);
-    MDS_TRY(rc);
-  }
+  MDS_TRY(launch_recheck(ctx, pl, Afp, Ar.as<float>(), dmu.as<float>(), Ur.as<float>(), nfit, nullptr, 0,
+                         cand.as<uint64_t>(), cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i,
+                         flagged.as<int>(), nflag.as<int>(), rowthr.p ? rowthr.as<float>() : nullptr, &audit));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   int hflag = 0, hbad[2] = {0, 0}, herr[4] = {0, 0, 0, 0};
   unsigned long long hc[4] = {0, 0, 0, 0};
