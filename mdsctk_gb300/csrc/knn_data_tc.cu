@@ -51,6 +51,7 @@
 #define TV_LCAP 256         // keys per (row, column half) list region; a row's list is 2 regions
 #define TV_MAX_DP 128
 #define TV_PILOT 16         // column tiles each row pair visits in the threshold-seeding pass
+#define TV_KHMAX 64         // largest k + 1 with threshold heaps in the epilogue
 
 // FP32 vectors [n][Dp] -> BF16 split rows [rows][hi(Dp) | lo(Dp)], rows
 // beyond n zero. With terms != nullptr also the column term of each row as a
@@ -96,9 +97,43 @@ struct TvShared {
   float rslack[TV_ROWS][2];  // 2 g (|x|^2 + nmax): the (k+1)-th bound's slack of the row
 };
 
-static size_t tv_smem_bytes(int Dp, int nst) {
+static size_t tv_smem_bytes(int Dp, int nst, int KH) {
   return (size_t)TV_ROWS * 2 * Dp * 2 + (size_t)nst * TV_STAGE_BYTES + sizeof(TvShared) +
-         (size_t)TV_EPI * TV_SCR * 4 + 1024;
+         (size_t)TV_EPI * TV_SCR * 4 + (size_t)TV_ROWS * 2 * KH * 2 + 1024;
+}
+
+// The (row, column half) heaps of the epilogue: the k1 smallest bounds the
+// half has appended, as the upper 16 bits of the non-negative float rounded
+// up (so a heap value is never below the bound it stands for), in a max-heap
+// whose root is the half's k1-th smallest; 0x7F80 (+inf) marks a free slot.
+__device__ __forceinline__ uint16_t tv_u16_up(float b) {
+  const uint32_t u = __float_as_uint(b);
+  return (uint16_t)((u >> 16) + ((u & 0xFFFFu) ? 1u : 0u));
+}
+__device__ __forceinline__ float tv_u16_float(uint32_t h) { return __uint_as_float(h << 16); }
+// Replaces the root by v when v is smaller, restoring the heap; the root is
+// written once, with the new maximum, so a concurrent reader of the root sees
+// either the old or the new k1-th value.
+__device__ __forceinline__ void tv_heap_push(uint16_t* hp, int n, uint16_t v) {
+  if (v >= hp[0]) return;
+  int i = 0;
+  while (true) {
+    const int l = 2 * i + 1;
+    if (l >= n) break;
+    int c = l;
+    uint16_t cv = hp[l];
+    if (l + 1 < n) {
+      const uint16_t rv = hp[l + 1];
+      if (rv > cv) {
+        c = l + 1;
+        cv = rv;
+      }
+    }
+    if (cv <= v) break;
+    hp[i] = cv;
+    i = c;
+  }
+  hp[i] = v;
 }
 
 // Column tiles of a segment [t0, t1) in visiting order: outward from td.
@@ -169,7 +204,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
              float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
              int* __restrict__ cand_n, int* __restrict__ err, int lcap, int k1, const float* __restrict__ nmax,
              const float* __restrict__ dlo, const int* __restrict__ tdv, const int* __restrict__ tdall,
-             int near_first, const int* __restrict__ rperm, const int* __restrict__ cperm) {
+             int near_first, const int* __restrict__ rperm, const int* __restrict__ cperm, int KH) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host);
   // err[2]: column tiles computed (added to).
   // Locality order (vec_order.cu; all four null without it): rows and columns
@@ -181,6 +216,10 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   // [row pair tile][segment] otherwise) when the set is not screened against
   // itself, tdall [row pair tile] the start over all tiles; near_first: the
   // item order of tv_item.
+  // KH = k1 (or 0: off): the epilogue keeps, per (row, column half), a heap of
+  // the k1 smallest bounds it appended (tv_heap_push), so the row's threshold
+  // follows its running k1-th bound plus the slack below at every chunk,
+  // with no search of the list; the list is searched only to cut it back.
   // pilot > 0: a pass that only seeds rowthr: each item (one per row pair
   // tile, nseg = 1) visits `pilot` column tiles (outward from the diagonal
   // for a set against itself, else spread over the set) and lowers each
@@ -233,6 +272,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     S->cnt2[r][1] = 0;
     S->thr[r] = INF;
   }
+  uint16_t* heaps = reinterpret_cast<uint16_t*>(scratch_all + TV_EPI * TV_SCR);  // [TV_ROWS][2][KH]
+  for (int e = threadIdx.x; e < TV_ROWS * 2 * KH; e += blockDim.x) heaps[e] = 0x7F80;
   if (warp == 1) {
     tmem_alloc(&S->tmem_base, 512);
     tmem_relinquish();
@@ -422,6 +463,14 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     const int own0 = u * 128 + 32 * q + 16 * half;  // the 16 rows this warp compacts and publishes
     uint64_t* lists = work + (size_t)blockIdx.x * TV_ROWS * TC_CAPG;
     uint64_t* mylist = lists + (size_t)r * TC_CAPG + half * lcap;
+    uint16_t* hp = heaps + ((size_t)r * 2 + half) * KH;         // this lane's (row, half) heap
+    const uint16_t* hq = heaps + ((size_t)r * 2 + (half ^ 1)) * KH;  // the partner half's
+    // the heaps' bound of row rr: min of its halves' k1-th plus the slack
+    auto heap_thr = [&](int rr) -> float {
+      if (!KH) return INF;
+      const uint32_t h0 = heaps[(size_t)rr * 2 * KH], h1 = heaps[((size_t)rr * 2 + 1) * KH];
+      return tv_u16_float(min(h0, h1)) + S->rslack[rr][half];
+    };
     const float slack = 2.0f * guard * __ldg(nmax);  // + 2 g |x|^2 of the row, at each item's start
     const float mul = corr ? -0.5f : -2.0f;
     uint32_t acc = 0;
@@ -463,7 +512,10 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           const int rr = own0 + x;
           const int gg = rp * TV_ROWS + rr;
           if (gg < nfit && !pilot) {
-            const float tp = fminf(S->thr[rr], __ldcg(rowthr + gg));
+            // (the published threshold goes to rowthr: the recheck's tau may
+            // not exceed what any segment kept)
+            const float tp = fminf(fminf(S->thr[rr], __ldcg(rowthr + gg)), heap_thr(rr));
+            if (lane == 0 && KH) atomicMin(reinterpret_cast<int*>(rowthr + gg), __float_as_int(tp));
             const int64_t go = rperm ? (int64_t)__ldg(rperm + gg) : gg;
             tv_publish(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], S->cnt2[rr][1], lcap, Kp, tp, hist,
                        candout + (go * nseg + seg) * Kp, cand_n + go * nseg + seg, lane, cperm);
@@ -472,7 +524,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             float tk1 = INF;
             float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, S->cnt2[rr][0], lcap, S->cnt2[rr][1],
                                         c >= Kp ? Kp : 0, hist, lane, k1, &tk1);
-            t = fminf(t, tk1 + S->rslack[rr][half]);
+            t = fminf(fminf(t, tk1 + S->rslack[rr][half]), heap_thr(rr));
             if (lane == 0) atomicMin(reinterpret_cast<int*>(rowthr + gg), __float_as_int(t));
           }
           if (lane == 0) {
@@ -481,6 +533,11 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             S->thr[rr] = INF;
           }
         }
+        // both halves have read the owned rows' heaps: clear this lane's for
+        // the next item (the next task's barrier orders the clears before
+        // any read)
+        bar_named(pbar, 64);
+        for (int i = 0; i < KH; ++i) hp[i] = 0x7F80;
         __syncwarp();
         continue;
       }
@@ -488,7 +545,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       int cnt = S->cnt2[r][half];
       // screen value = rc + colterm + mul * x.y; a pair passes below the
       // row's threshold (its own list's or another segment's)
-      const float lim = fminf(S->thr[r], (g < nfit) ? __ldcg(rowthr + g) : INF) - rc;
+      const float lim0 = fminf(S->thr[r], (g < nfit) ? __ldcg(rowthr + g) : INF) - rc;
+      const float rsl = S->rslack[r][half];
       const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256 + u * TV_N + 64 * half;
       const int j0 = tile * TV_N + 64 * half;
       const float4* ct4 = reinterpret_cast<const float4*>(colterm + j0);
@@ -508,6 +566,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         float4 c4[4];
 #pragma unroll
         for (int t4 = 0; t4 < 4; ++t4) c4[t4] = __ldg(ct4 + cc * 4 + t4);
+        // the row's threshold now: the heaps' k1-th bound follows every append
+        const float lim = KH ? fminf(lim0, tv_u16_float(min((uint32_t)hp[0], (uint32_t)hq[0])) + rsl - rc) : lim0;
         // four independent mask chains; only passing values are parked
         uint32_t m4[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
@@ -527,8 +587,10 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           while (mask) {
             const int t = __ffs(mask) - 1;
             mask &= mask - 1;
-            if (cnt < lcap) mylist[cnt] = mds_pack_key(fmaxf(sv[t * 32 + lane] + rc, 0.0f), j0 + 16 * cc + t);
+            const float bv = fmaxf(sv[t * 32 + lane] + rc, 0.0f);
+            if (cnt < lcap) mylist[cnt] = mds_pack_key(bv, j0 + 16 * cc + t);
             ++cnt;
+            if (KH) tv_heap_push(hp, KH, tv_u16_up(bv));
           }
         }
         __syncwarp();
@@ -554,12 +616,13 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         // shared one, it cuts appends. (Refreshing it after every k1 further
         // appends was measured slower: the searches cost more than the
         // appends they save.)
-        const bool first = S->thr[rr] == INF && c0 + c1 >= k1;
+        // (with the heaps on, they give that threshold without a search)
+        const bool first = !KH && S->thr[rr] == INF && c0 + c1 >= k1;
         if (!cut && !first) continue;
         float tk1 = INF;
         float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, c0, lcap, c1, cut ? Kp : 0, hist, lane, k1,
                                     &tk1);
-        t = fminf(t, tk1 + S->rslack[rr][half]);
+        t = fminf(fminf(t, tk1 + S->rslack[rr][half]), heap_thr(rr));
         if (lane == 0) {
           if (cut) {
             S->cnt2[rr][0] = Kp;
@@ -699,10 +762,13 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
     MDS_TRY(vec_seed_rows(ctx, Xr, pr, nref, Xf, pf, nfit, Dp, same ? nullptr : tdall.as<int>(), k + 1,
                           nmax.as<float>(), rt));
   const int nst = (Dp <= 64) ? 4 : (Dp <= 96 ? 3 : 2);
-  const size_t smem = tv_smem_bytes(Dp, nst);
   static bool attr_done = false;
   static size_t attr_limit = 0;
   MDS_TRY(mds_allow_dyn_smem(ctx, k_screen_tcv, &attr_done, &attr_limit));
+  // threshold heaps of k1 entries per (row, column half) where they fit
+  int KH = (k + 1 <= TV_KHMAX) ? k + 1 : 0;
+  if (KH && tv_smem_bytes(Dp, nst, KH) > attr_limit) KH = 0;
+  const size_t smem = tv_smem_bytes(Dp, nst, KH);
   if (smem > attr_limit)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "vector screen needs %zu bytes of shared memory", smem);
   const uint32_t idesc = umma_idesc_f16(128, TV_N, 1);
@@ -717,7 +783,7 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
     k_screen_tcv<<<std::min(nrp, ctx->num_sms), TV_THREADS, smem, s>>>(
         mA, mB, nfk, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC, idesc, Kp, 1, nrp,
         same ? 1 : 0, TV_PILOT, rt, work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
-        nmax.as<float>(), nullptr, nullptr, nullptr, 0, nullptr, nullptr);
+        nmax.as<float>(), nullptr, nullptr, nullptr, 0, nullptr, nullptr, KH);
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaMemsetAsync(err.as<int>() + 1, 0, sizeof(int), s));
   }
@@ -726,7 +792,7 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
                                               MDS_GUARD_TC, idesc, Kp, nseg, nitems, same ? 1 : 0, 0, rt,
                                               work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
                                               nmax.as<float>(), pdlo, ptdseg, ptdall, order ? 1 : 0,
-                                              pr ? pf : nullptr, pr);
+                                              pr ? pf : nullptr, pr, KH);
   MDS_CUDA(ctx, cudaGetLastError());
   if (order) MDS_TRY(vec_unsort(ctx, rt, pf, nfit, rowthr));
   int herr[3] = {0, 0, 0};
