@@ -603,22 +603,32 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       if (cnt > lcap) atomicMax(err, 4);  // cannot happen: compaction keeps room for a tile
       S->cnt2[r][half] = min(cnt, lcap);
       bar_named(pbar, 64);  // both halves of these rows are appended
-      // compaction of the owned rows whose regions near full (or first fill)
-      for (int x = 0; x < 16; ++x) {
-        const int rr = own0 + x;
-        const int gg = rp * TV_ROWS + rr;
-        if (gg >= nfit) break;
+      // compaction of the owned rows whose regions near full (or first fill):
+      // lane x < 16 tests row own0 + x, and the warp visits only the rows
+      // that need it (testing the 16 rows one after another cost ~5,000
+      // cycles per tile in shared-memory round trips)
+      unsigned todo;
+      {
+        const int rr = own0 + (lane & 15);
         const int c0 = S->cnt2[rr][0], c1 = S->cnt2[rr][1];
         // a region near full: cut both back to the K' best
-        const bool cut = c0 + c1 > Kp && (c0 > lcap - 64 || c1 > lcap - 64);
+        const bool cutl = c0 + c1 > Kp && (c0 > lcap - 64 || c1 > lcap - 64);
         // the row's first own threshold comes from its k1-th key as soon as
         // those arrive (a rank search that moves no key): tighter than the
         // shared one, it cuts appends. (Refreshing it after every k1 further
         // appends was measured slower: the searches cost more than the
-        // appends they save.)
-        // (with the heaps on, they give that threshold without a search)
-        const bool first = !KH && S->thr[rr] == INF && c0 + c1 >= k1;
-        if (!cut && !first) continue;
+        // appends they save.) With the heaps on, they give that threshold
+        // without a search.
+        const bool firstl = !KH && S->thr[rr] == INF && c0 + c1 >= k1;
+        todo = __ballot_sync(0xffffffffu, lane < 16 && rp * TV_ROWS + rr < nfit && (cutl || firstl));
+      }
+      while (todo) {
+        const int x = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int rr = own0 + x;
+        const int gg = rp * TV_ROWS + rr;
+        const int c0 = S->cnt2[rr][0], c1 = S->cnt2[rr][1];
+        const bool cut = c0 + c1 > Kp && (c0 > lcap - 64 || c1 > lcap - 64);
         float tk1 = INF;
         float t = warp_select_keep2(lists + (size_t)rr * TC_CAPG, c0, lcap, c1, cut ? Kp : 0, hist, lane, k1,
                                     &tk1);
