@@ -51,7 +51,7 @@
 #define TV_LCAP 256         // keys per (row, column half) list region; a row's list is 2 regions
 #define TV_MAX_DP 128
 #define TV_PILOT 16         // column tiles each row pair visits in the threshold-seeding pass
-#define TV_KHMAX 64         // largest k + 1 with threshold heaps in the epilogue
+#define TV_KHMAX 96         // largest k + 1 with threshold heaps in the epilogue
 
 // FP32 vectors [n][Dp] -> BF16 split rows [rows][hi(Dp) | lo(Dp)], rows
 // beyond n zero. With terms != nullptr also the column term of each row as a
@@ -102,10 +102,10 @@ static size_t tv_smem_bytes(int Dp, int nst, int KH) {
          (size_t)TV_EPI * TV_SCR * 4 + (size_t)TV_ROWS * 2 * KH * 2 + 1024;
 }
 
-// The (row, column half) heaps of the epilogue: the k1 smallest bounds the
+// The (row, column half) heaps of the epilogue: the KH smallest bounds the
 // half has appended, as the upper 16 bits of the non-negative float rounded
 // up (so a heap value is never below the bound it stands for), in a max-heap
-// whose root is the half's k1-th smallest; 0x7F80 (+inf) marks a free slot.
+// whose root is the half's KH-th smallest; 0x7F80 (+inf) marks a free slot.
 __device__ __forceinline__ uint16_t tv_u16_up(float b) {
   const uint32_t u = __float_as_uint(b);
   return (uint16_t)((u >> 16) + ((u & 0xFFFFu) ? 1u : 0u));
@@ -216,10 +216,12 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   // [row pair tile][segment] otherwise) when the set is not screened against
   // itself, tdall [row pair tile] the start over all tiles; near_first: the
   // item order of tv_item.
-  // KH = k1 (or 0: off): the epilogue keeps, per (row, column half), a heap of
-  // the k1 smallest bounds it appended (tv_heap_push), so the row's threshold
-  // follows its running k1-th bound plus the slack below at every chunk,
-  // with no search of the list; the list is searched only to cut it back.
+  // KH = ceil(k1 / 2) (or 0: off): the epilogue keeps, per (row, column half),
+  // a heap of the KH smallest bounds it appended (tv_heap_push), so the row's
+  // threshold follows the larger of its halves' KH-th bounds (2 KH >= k1
+  // bounds lie at or below it) plus the slack, with no search of the list;
+  // the list is searched only to cut it back. (Heaps of k1 per half with the
+  // smaller root: one level deeper, and a half's k1-th is looser.)
   // pilot > 0: a pass that only seeds rowthr: each item (one per row pair
   // tile, nseg = 1) visits `pilot` column tiles (outward from the diagonal
   // for a set against itself, else spread over the set) and lowers each
@@ -465,11 +467,12 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     uint64_t* mylist = lists + (size_t)r * TC_CAPG + half * lcap;
     uint16_t* hp = heaps + ((size_t)r * 2 + half) * KH;         // this lane's (row, half) heap
     const uint16_t* hq = heaps + ((size_t)r * 2 + (half ^ 1)) * KH;  // the partner half's
-    // the heaps' bound of row rr: min of its halves' k1-th plus the slack
+    // the heaps' bound of row rr: each half holds its KH smallest, so the
+    // 2 KH >= k1 values of both lie at or below the larger root; plus the slack
     auto heap_thr = [&](int rr) -> float {
       if (!KH) return INF;
       const uint32_t h0 = heaps[(size_t)rr * 2 * KH], h1 = heaps[((size_t)rr * 2 + 1) * KH];
-      return tv_u16_float(min(h0, h1)) + S->rslack[rr][half];
+      return tv_u16_float(max(h0, h1)) + S->rslack[rr][half];
     };
     const float slack = 2.0f * guard * __ldg(nmax);  // + 2 g |x|^2 of the row, at each item's start
     const float mul = corr ? -0.5f : -2.0f;
@@ -547,6 +550,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       // row's threshold (its own list's or another segment's)
       const float lim0 = fminf(S->thr[r], (g < nfit) ? __ldcg(rowthr + g) : INF) - rc;
       const float rsl = S->rslack[r][half];
+      // the heaps' bound (read once per tile)
+      const float lim = KH ? fminf(lim0, tv_u16_float(max((uint32_t)hp[0], (uint32_t)hq[0])) + rsl - rc) : lim0;
       const uint32_t tq = tbase + ((uint32_t)(q * 32) << 16) + b * 256 + u * TV_N + 64 * half;
       const int j0 = tile * TV_N + 64 * half;
       const float4* ct4 = reinterpret_cast<const float4*>(colterm + j0);
@@ -566,8 +571,6 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         float4 c4[4];
 #pragma unroll
         for (int t4 = 0; t4 < 4; ++t4) c4[t4] = __ldg(ct4 + cc * 4 + t4);
-        // the row's threshold now: the heaps' k1-th bound follows every append
-        const float lim = KH ? fminf(lim0, tv_u16_float(min((uint32_t)hp[0], (uint32_t)hq[0])) + rsl - rc) : lim0;
         // four independent mask chains; only passing values are parked
         uint32_t m4[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
@@ -776,7 +779,7 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   static size_t attr_limit = 0;
   MDS_TRY(mds_allow_dyn_smem(ctx, k_screen_tcv, &attr_done, &attr_limit));
   // threshold heaps of k1 entries per (row, column half) where they fit
-  int KH = (k + 1 <= TV_KHMAX) ? k + 1 : 0;
+  int KH = (k + 1 <= TV_KHMAX) ? (k + 2) / 2 : 0;
   if (KH && tv_smem_bytes(Dp, nst, KH) > attr_limit) KH = 0;
   const size_t smem = tv_smem_bytes(Dp, nst, KH);
   if (smem > attr_limit)
