@@ -480,6 +480,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     bool ok = true;
     int cur = -1, rp = 0, seg = 0, g = 0;
     float rc = INF;
+    float rtn = INF;  // the row's shared threshold, loaded one tile ahead
     // The two warps of a pair meet at their named barrier twice per tile:
     // after the task read and the accumulator wait (whose outcomes are ANDed,
     // so both leave together), and after the appends (before compaction).
@@ -507,6 +508,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         g = rp * TV_ROWS + r;
         const float rn = (g < nfit) ? __ldg(nf + g) : 0.0f;
         rc = (g >= nfit) ? INF : corr ? 0.5f - guard * rn : rn * (1.0f - guard);
+        rtn = (g < nfit) ? __ldcg(rowthr + g) : INF;
         S->rslack[r][half] = slack + 2.0f * guard * rn;  // (each half's warp keeps its own copy)
       }
       if (task.y < 0) {
@@ -548,7 +550,10 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       int cnt = S->cnt2[r][half];
       // screen value = rc + colterm + mul * x.y; a pair passes below the
       // row's threshold (its own list's or another segment's)
-      const float lim0 = fminf(S->thr[r], (g < nfit) ? __ldcg(rowthr + g) : INF) - rc;
+      // (the shared threshold read for this tile was issued during the last
+      // one: a value a tile old is only looser, and its L2 latency is hidden)
+      const float lim0 = fminf(S->thr[r], rtn) - rc;
+      if (g < nfit) rtn = __ldcg(rowthr + g);
       const float rsl = S->rslack[r][half];
       // the heaps' bound (read once per tile)
       const float lim = KH ? fminf(lim0, tv_u16_float(max((uint32_t)hp[0], (uint32_t)hq[0])) + rsl - rc) : lim0;
