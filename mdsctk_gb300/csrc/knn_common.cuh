@@ -187,7 +187,8 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
 int vec_order_max_dp();
 int vec_order(mds_ctx* ctx, const float* X, int n, int Dp, float* cent, bool fit, int* perm);
 int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
-                    int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall);
+                    int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall,
+                    int k1, float* rowthr);
 int vec_seed_rows(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
                   int nfit, int Dp, const int* tdall, int k1, const float* nmax, float* rowthr);
 int vec_unsort(mds_ctx* ctx, const float* src, const int* perm, int n, float* dst);

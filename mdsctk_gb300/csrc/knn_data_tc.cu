@@ -759,10 +759,17 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
       MDS_TRY(tdseg.alloc(ctx, sizeof(int) * (size_t)nrp * nseg));
       MDS_TRY(tdall.alloc(ctx, sizeof(int) * (size_t)nrp));
     }
-    MDS_TRY(vec_tile_bounds(ctx, Xr, pr, nref, Xf, pf, nfit, Dp, TV_N, nmax.as<float>(), dlo.as<float>(), nseg,
-                            same ? nullptr : tdseg.as<int>(), same ? nullptr : tdall.as<int>()));
     MDS_TRY(rts.alloc(ctx, sizeof(float) * (size_t)nfit));
     rt = rts.as<float>();
+    MDS_CUDA(ctx, cudaMemsetAsync(rt, 0x7f, sizeof(float) * (size_t)nfit, s));
+    // the bounds, with each row's threshold seeded from its k1-th distance to
+    // its start tile's members (that tile is screened first, without a storm
+    // of appends under no threshold); the seeds also let the bounds skip the
+    // exact refinement of tiles the coarse bound already excludes
+    MDS_TRY(vec_tile_bounds(ctx, Xr, pr, nref, Xf, pf, nfit, Dp, TV_N, nmax.as<float>(), dlo.as<float>(), nseg,
+                            same ? nullptr : tdseg.as<int>(), same ? nullptr : tdall.as<int>(), k + 1, rt));
+  } else {
+    MDS_CUDA(ctx, cudaMemsetAsync(rt, 0x7f, sizeof(float) * (size_t)nfit, s));
   }
   CUtensorMap mA, mB;
   MDS_TRY(encode_map(ctx, &mA, pA, same ? rowsS : rowsA, Dp, 128, MDS_PREC_BF16X3));
@@ -772,13 +779,6 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   MDS_TRY(work.alloc(ctx, sizeof(uint64_t) * (size_t)grid * TV_ROWS * TC_CAPG));
   MDS_TRY(err.alloc(ctx, 4 * sizeof(int)));
   MDS_CUDA(ctx, cudaMemsetAsync(err.p, 0, 4 * sizeof(int), s));
-  MDS_CUDA(ctx, cudaMemsetAsync(rt, 0x7f, sizeof(float) * (size_t)nfit, s));
-  // in locality order each row's threshold starts from its k1-th distance to
-  // its start tile's members (the tile is screened first, without a storm of
-  // appends under no threshold)
-  if (order)
-    MDS_TRY(vec_seed_rows(ctx, Xr, pr, nref, Xf, pf, nfit, Dp, same ? nullptr : tdall.as<int>(), k + 1,
-                          nmax.as<float>(), rt));
   const int nst = (Dp <= 64) ? 4 : (Dp <= 96 ? 3 : 2);
   static bool attr_done = false;
   static size_t attr_limit = 0;

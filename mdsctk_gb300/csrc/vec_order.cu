@@ -18,14 +18,16 @@
 //  2. Per column tile, its centre c (FP32 mean of its vectors) and radius
 //     rho = max |y - c| (accumulated in FP64 against the FP32 centre, rounded
 //     up).
-//  3. Per row pair tile I and column tile T, dlo = min over the rows x of I of
-//     |x - c_T| (FP32, made a lower bound by a margin for its rounding) minus
-//     rho_T minus an absolute margin for the rounding of the inputs to FP32. By the
-//     triangle inequality every pair (x in I, y in T) has |x - y| >= dlo: when
+//  3. Per row pair tile I and column tile T, dlo, a lower bound of the
+//     distance of every pair (x in I, y in T) by the triangle inequality: when
 //     dlo > 0 and dlo^2 is at least every row's current threshold, none of
 //     the tile's pairs can enter any row's list, and the screen skips it.
-//     Also the start tile of each (row pair tile, column segment) visit: the
-//     one with the smallest dlo.
+//     First coarsely from I's own centre and radius, |c_I - c_T| - rho_I -
+//     rho_T; then, where that cannot prove a skip against the rows' threshold
+//     seeds, min over the rows x of I of |x - c_T| - rho_T (FP32, with margins
+//     for its rounding and the inputs' rounding to FP32). Also the start tile
+//     of each (row pair tile, column segment) visit: the one with the
+//     smallest dlo.
 #include <algorithm>
 
 #include "knn_common.cuh"
@@ -174,97 +176,6 @@ __global__ void k_vo_tile_geom(const float* __restrict__ X, const int* __restric
   }
 }
 
-// dlo[I][T] for the row pair tile I (blockDim.x = 256 sorted rows; rows past
-// n count as absent) and every column tile T. nmax: the reference set's
-// largest squared norm (float), for the absolute margin.
-//   |x - c|^2 = |x|^2 + |c|^2 - 2 x.c in FP32 (one FMA per dimension): each
-//   of the three terms errs by at most ~DP 2^-24 (|x|^2 + |c|^2), so
-//   4e-7 DP (|x|^2 + |c|^2) taken off before the square root keeps it a
-//   lower bound.
-template <int DP>
-__global__ void __launch_bounds__(256) k_vo_item_lb(const float* __restrict__ X, const int* __restrict__ perm, int n,
-                                                    const float* __restrict__ center, const float* __restrict__ rad,
-                                                    int nct, const float* __restrict__ nmax, float* __restrict__ dlo) {
-  __shared__ __align__(16) float cen[32 * DP];
-  __shared__ float cnr[32];
-  __shared__ float wmin[8][33];
-  const int item = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int g = item * 256 + t;
-  const bool valid = g < n;
-  float x[DP];
-  if (valid) {
-    const float4* x4 = reinterpret_cast<const float4*>(X + (int64_t)perm[g] * DP);
-#pragma unroll
-    for (int q = 0; q < DP / 4; ++q) {
-      const float4 v = x4[q];
-      x[4 * q] = v.x;
-      x[4 * q + 1] = v.y;
-      x[4 * q + 2] = v.z;
-      x[4 * q + 3] = v.w;
-    }
-  } else {
-#pragma unroll
-    for (int d = 0; d < DP; ++d) x[d] = 0.0f;
-  }
-  float xn0 = 0.0f, xn1 = 0.0f;
-#pragma unroll
-  for (int d = 0; d < DP; d += 2) {
-    xn0 = fmaf(x[d], x[d], xn0);
-    xn1 = fmaf(x[d + 1], x[d + 1], xn1);
-  }
-  const float xn = xn0 + xn1;
-  // |x32 - x| <= 2^-24 |x| for each input vector: 2e-6 (|x|max + |y|max)
-  // covers the rounding of both sides with room (nmax: the reference set's
-  // largest squared norm; the rows' own is found here)
-  float xm = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(xn)));
-  if (lane == 0) wmin[w][32] = xm;
-  __syncthreads();
-  for (int k = 0; k < 8; ++k) xm = fmaxf(xm, wmin[k][32]);
-  const float nabs = 2e-6f * (sqrtf(__ldg(nmax)) + sqrtf(xm));
-  const float mrel = 4e-7f * DP;
-  for (int T0 = 0; T0 < nct; T0 += 32) {
-    const int nt = min(32, nct - T0);
-    __syncthreads();
-    for (int e = t; e < nt * DP; e += 256) cen[e] = center[(int64_t)T0 * DP + e];
-    __syncthreads();
-    if (t < nt) {
-      float c0 = 0.0f, c1 = 0.0f;
-      for (int d = 0; d < DP; d += 2) {
-        c0 = fmaf(cen[t * DP + d], cen[t * DP + d], c0);
-        c1 = fmaf(cen[t * DP + d + 1], cen[t * DP + d + 1], c1);
-      }
-      cnr[t] = c0 + c1;
-    }
-    __syncthreads();
-    for (int tt = 0; tt < nt; ++tt) {
-      const float4* c4 = reinterpret_cast<const float4*>(cen + tt * DP);
-      float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-#pragma unroll
-      for (int q = 0; q < DP / 4; ++q) {
-        const float4 c = c4[q];
-        s0 = fmaf(x[4 * q], c.x, s0);
-        s1 = fmaf(x[4 * q + 1], c.y, s1);
-        s2 = fmaf(x[4 * q + 2], c.z, s2);
-        s3 = fmaf(x[4 * q + 3], c.w, s3);
-      }
-      const float cn = cnr[tt];
-      const float d2 = fmaxf((xn + cn) - 2.0f * ((s0 + s1) + (s2 + s3)) - mrel * (xn + cn), 0.0f);
-      // squared distances are non-negative: their bits order as unsigned
-      unsigned u = valid ? __float_as_uint(d2) : 0x7f800000u;
-      u = __reduce_min_sync(0xffffffffu, u);
-      if (lane == 0) wmin[w][tt] = __uint_as_float(u);
-    }
-    __syncthreads();
-    if (w == 0 && lane < nt) {
-      float m = wmin[0][lane];
-#pragma unroll
-      for (int k = 1; k < 8; ++k) m = fminf(m, wmin[k][lane]);
-      const int T = T0 + lane;
-      dlo[(int64_t)item * nct + T] = sqrtf(m) * (1.0f - 1e-6f) - __ldg(rad + T) - nabs;
-    }
-  }
-}
-
 // Ascending bitonic sort of 128 values held 4 per lane (element 4 lane + i).
 __device__ __forceinline__ void warp_sort128(float (&v)[4], int lane) {
 #pragma unroll
@@ -352,12 +263,163 @@ __global__ void __launch_bounds__(256) k_vo_seed_rows(const float* __restrict__ 
   }
 }
 
+// Coarse bound of every (row pair tile I, column tile T): with c_I, rho_I the
+// item's centre and radius (k_vo_tile_geom over 256-row tiles), every pair
+// has |x - y| >= |c_I - c_T| - rho_I - rho_T. |x| <= |c_I| + rho_I bounds the
+// rows' norms in the absolute margin. Grid (items, ceil(nct / 256)).
+__global__ void __launch_bounds__(256) k_vo_coarse(const float* __restrict__ cenI, const float* __restrict__ radI,
+                                                   const float* __restrict__ cenT, const float* __restrict__ radT,
+                                                   int nct, int Dp, const float* __restrict__ nmax,
+                                                   float* __restrict__ dlo) {
+  __shared__ float ci[VO_MAXDP];
+  const int item = blockIdx.x, T = blockIdx.y * blockDim.x + threadIdx.x;
+  for (int d = threadIdx.x; d < Dp; d += blockDim.x) ci[d] = cenI[(int64_t)item * Dp + d];
+  __syncthreads();
+  if (T >= nct) return;
+  float s0 = 0.0f, s1 = 0.0f, cn = 0.0f;
+  const float* ct = cenT + (int64_t)T * Dp;
+  for (int d = 0; d < Dp; d += 2) {
+    const float e0 = ci[d] - ct[d], e1 = ci[d + 1] - ct[d + 1];
+    s0 = fmaf(e0, e0, s0);
+    s1 = fmaf(e1, e1, s1);
+    cn = fmaf(ci[d], ci[d], fmaf(ci[d + 1], ci[d + 1], cn));
+  }
+  const float rI = __ldg(radI + item);
+  const float nabs = 2e-6f * (sqrtf(__ldg(nmax)) + sqrtf(cn) + rI);
+  dlo[(int64_t)item * nct + T] = sqrtf(s0 + s1) * (1.0f - 3e-5f) - rI - __ldg(radT + T) - nabs;
+}
+
+// Refines dlo[I][T] where the coarse bound cannot prove a skip: a tile is
+// skipped when dlo > 0 and dlo^2 is at least the largest threshold of the
+// item's rows, and those only fall from their seeds (rowthr on entry), so a
+// coarse dlo with dlo^2 >= the largest seed already skips and is kept. The
+// others (gathered 256 tiles at a time, computed 32 at a time; blockDim.x =
+// 256 sorted rows, rows past n absent) get min over the rows x of |x - c_T|
+// minus rho_T and the margins, the larger of the two bounds kept:
+//   |x - c|^2 = |x|^2 + |c|^2 - 2 x.c in FP32 (one FMA per dimension): each
+//   of the three terms errs by at most ~DP 2^-24 (|x|^2 + |c|^2), so
+//   4e-7 DP (|x|^2 + |c|^2) taken off before the square root keeps it a
+//   lower bound; |x32 - x| <= 2^-24 |x| for each input vector, which
+//   2e-6 (|x|max + |y|max) covers with room.
+template <int DP>
+__global__ void __launch_bounds__(256) k_vo_refine(const float* __restrict__ X, const int* __restrict__ perm, int n,
+                                                   const float* __restrict__ center, const float* __restrict__ rad,
+                                                   int nct, const float* __restrict__ nmax,
+                                                   const float* __restrict__ rowthr, float* __restrict__ dlo) {
+  __shared__ __align__(16) float cen[32 * DP];
+  __shared__ float cnr[32];
+  __shared__ float wmin[8][33];
+  __shared__ int list[256];
+  __shared__ int s_cnt;
+  const int item = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int g = item * 256 + t;
+  const bool valid = g < n;
+  float x[DP];
+  if (valid) {
+    const float4* x4 = reinterpret_cast<const float4*>(X + (int64_t)perm[g] * DP);
+#pragma unroll
+    for (int q = 0; q < DP / 4; ++q) {
+      const float4 v = x4[q];
+      x[4 * q] = v.x;
+      x[4 * q + 1] = v.y;
+      x[4 * q + 2] = v.z;
+      x[4 * q + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int d = 0; d < DP; ++d) x[d] = 0.0f;
+  }
+  float xn0 = 0.0f, xn1 = 0.0f;
+#pragma unroll
+  for (int d = 0; d < DP; d += 2) {
+    xn0 = fmaf(x[d], x[d], xn0);
+    xn1 = fmaf(x[d + 1], x[d + 1], xn1);
+  }
+  const float xn = xn0 + xn1;
+  // the rows' largest norm and largest seed (both non-negative: as unsigned bits)
+  unsigned xm = __reduce_max_sync(0xffffffffu, __float_as_uint(xn));
+  unsigned sm = __reduce_max_sync(0xffffffffu, valid ? __float_as_uint(fmaxf(__ldcg(rowthr + g), 0.0f)) : 0u);
+  if (lane == 0) {
+    wmin[w][31] = __uint_as_float(xm);
+    wmin[w][32] = __uint_as_float(sm);
+  }
+  __syncthreads();
+  float xmax = 0.0f, smax = 0.0f;
+  for (int k = 0; k < 8; ++k) {
+    xmax = fmaxf(xmax, wmin[k][31]);
+    smax = fmaxf(smax, wmin[k][32]);
+  }
+  __syncthreads();
+  const float nabs = 2e-6f * (sqrtf(__ldg(nmax)) + sqrtf(xmax));
+  const float mrel = 4e-7f * DP;
+  float* row = dlo + (int64_t)item * nct;
+  for (int W0 = 0; W0 < nct; W0 += 256) {
+    // the tiles of this window that the coarse bound cannot skip (the first
+    // barrier: every thread has read the last window's count and list)
+    __syncthreads();
+    if (t == 0) s_cnt = 0;
+    __syncthreads();
+    {
+      const int T = W0 + t;
+      const float c = (T < nct) ? row[T] : 1.0f;
+      const bool need = T < nct && !(c > 0.0f && c * c >= smax);
+      const unsigned b = __ballot_sync(0xffffffffu, need);
+      int base = 0;
+      if (lane == 0 && b) base = atomicAdd(&s_cnt, __popc(b));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (need) list[base + __popc(b & ((1u << lane) - 1u))] = T;
+    }
+    __syncthreads();
+    const int nl = s_cnt;
+    for (int L0 = 0; L0 < nl; L0 += 32) {
+      const int nt = min(32, nl - L0);
+      __syncthreads();
+      for (int e = t; e < nt * DP; e += 256) cen[e] = center[(int64_t)list[L0 + e / DP] * DP + e % DP];
+      __syncthreads();
+      if (t < nt) {
+        float c0 = 0.0f, c1 = 0.0f;
+        for (int d = 0; d < DP; d += 2) {
+          c0 = fmaf(cen[t * DP + d], cen[t * DP + d], c0);
+          c1 = fmaf(cen[t * DP + d + 1], cen[t * DP + d + 1], c1);
+        }
+        cnr[t] = c0 + c1;
+      }
+      __syncthreads();
+      for (int tt = 0; tt < nt; ++tt) {
+        const float4* c4 = reinterpret_cast<const float4*>(cen + tt * DP);
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+        for (int q = 0; q < DP / 4; ++q) {
+          const float4 c = c4[q];
+          s0 = fmaf(x[4 * q], c.x, s0);
+          s1 = fmaf(x[4 * q + 1], c.y, s1);
+          s2 = fmaf(x[4 * q + 2], c.z, s2);
+          s3 = fmaf(x[4 * q + 3], c.w, s3);
+        }
+        const float cn = cnr[tt];
+        const float d2 = fmaxf((xn + cn) - 2.0f * ((s0 + s1) + (s2 + s3)) - mrel * (xn + cn), 0.0f);
+        unsigned u = valid ? __float_as_uint(d2) : 0x7f800000u;
+        u = __reduce_min_sync(0xffffffffu, u);
+        if (lane == 0) wmin[w][tt] = __uint_as_float(u);
+      }
+      __syncthreads();
+      if (w == 0 && lane < nt) {
+        float m = wmin[0][lane];
+#pragma unroll
+        for (int k = 1; k < 8; ++k) m = fminf(m, wmin[k][lane]);
+        const int T = list[L0 + lane];
+        row[T] = fmaxf(row[T], sqrtf(m) * (1.0f - 1e-6f) - __ldg(rad + T) - nabs);
+      }
+    }
+  }
+}
+
 // Start tile of each (row pair tile, segment) visit: the smallest dlo in the
 // segment (lowest tile on ties). blockIdx.y == nseg: over all tiles (the
 // pilot's start). One warp per block.
 __global__ void k_vo_start(const float* __restrict__ dlo, int nct, int nseg, int* __restrict__ tdseg,
-                           int* __restrict__ tdall) {
-  const int item = blockIdx.x, sg = blockIdx.y, lane = threadIdx.x;
+                           int* __restrict__ tdall, int only_all) {
+  const int item = blockIdx.x, sg = only_all ? nseg : (int)blockIdx.y, lane = threadIdx.x;
   const int t0 = (sg == nseg) ? 0 : (int)((int64_t)nct * sg / nseg);
   const int t1 = (sg == nseg) ? nct : (int)((int64_t)nct * (sg + 1) / nseg);
   const float* row = dlo + (int64_t)item * nct;
@@ -379,10 +441,11 @@ __global__ void k_vo_start(const float* __restrict__ dlo, int nct, int nseg, int
     }
   }
   if (lane == 0) {
-    if (sg == nseg)
-      tdall[item] = bt;
-    else
+    if (sg == nseg) {
+      if (tdall) tdall[item] = bt;
+    } else {
       tdseg[(int64_t)item * nseg + sg] = bt;
+    }
   }
 }
 
@@ -442,38 +505,57 @@ int vec_order(mds_ctx* ctx, const float* X, int n, int Dp, float* cent, bool fit
   return MDS_OK;
 }
 
-// Column tile geometry of the sorted reference set (tiles of `tile` vectors)
-// and dlo [nitems][nct] of the sorted fit set's row pair tiles (256 rows),
-// with the start tiles tdseg [nitems][nseg] and tdall [nitems] (either may be
-// null). nmax: device float, the reference set's largest squared norm.
+// Column tile geometry of the sorted reference set (tiles of `tile` = 128
+// vectors), the row pair tiles' geometry (256 sorted fit rows), the coarse
+// bounds dlo [nitems][nct], tdall [nitems] (the start over all tiles; null
+// for a set against itself), the threshold seeds of the rows into rowthr
+// (sorted order, +inf-like before), then the refinement of the bounds the
+// coarse ones cannot skip by, and tdseg [nitems][nseg] (or null). nmax:
+// device float, the reference set's largest squared norm.
 int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
-                    int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall) {
+                    int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall,
+                    int k1, float* rowthr) {
   cudaStream_t s = ctx->stream;
   const int nct = (nref + tile - 1) / tile, nitems = (nfit + 255) / 256;
-  DevBuf center(ctx), rad(ctx);
+  DevBuf center(ctx), rad(ctx), cenI(ctx), radI(ctx);
   MDS_TRY(center.alloc(ctx, sizeof(float) * (size_t)nct * Dp));
   MDS_TRY(rad.alloc(ctx, sizeof(float) * (size_t)nct));
+  MDS_TRY(cenI.alloc(ctx, sizeof(float) * (size_t)nitems * Dp));
+  MDS_TRY(radI.alloc(ctx, sizeof(float) * (size_t)nitems));
   k_vo_tile_geom<<<nct, tile, 0, s>>>(Xr, permr, nref, Dp, tile, center.as<float>(), rad.as<float>());
-  ctx->stats.launches++;
+  k_vo_tile_geom<<<nitems, 256, 0, s>>>(Xf, permf, nfit, Dp, 256, cenI.as<float>(), radI.as<float>());
+  k_vo_coarse<<<dim3(nitems, (nct + 255) / 256), 256, 0, s>>>(cenI.as<float>(), radI.as<float>(), center.as<float>(),
+                                                               rad.as<float>(), nct, Dp, nmax, dlo);
+  ctx->stats.launches += 3;
+  if (tdall) {
+    k_vo_start<<<dim3(nitems, 1), 32, 0, s>>>(dlo, nct, nseg, nullptr, tdall, 1);
+    ctx->stats.launches++;
+  }
+  MDS_CUDA(ctx, cudaGetLastError());
+  MDS_TRY(vec_seed_rows(ctx, Xr, permr, nref, Xf, permf, nfit, Dp, tdall, k1, nmax, rowthr));
   switch (Dp) {
     case 32:
-      k_vo_item_lb<32><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      k_vo_refine<32><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
+                                             rowthr, dlo);
       break;
     case 64:
-      k_vo_item_lb<64><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      k_vo_refine<64><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
+                                             rowthr, dlo);
       break;
     case 96:
-      k_vo_item_lb<96><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      k_vo_refine<96><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
+                                             rowthr, dlo);
       break;
     case 128:
-      k_vo_item_lb<128><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax, dlo);
+      k_vo_refine<128><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
+                                              rowthr, dlo);
       break;
     default:
       return mds_fail(ctx, MDS_ERR_INTERNAL, "vec_tile_bounds: padded dimension %d", Dp);
   }
   ctx->stats.launches++;
-  if (tdseg || tdall) {
-    k_vo_start<<<dim3(nitems, nseg + 1), 32, 0, s>>>(dlo, nct, nseg, tdseg, tdall);
+  if (tdseg) {
+    k_vo_start<<<dim3(nitems, nseg), 32, 0, s>>>(dlo, nct, nseg, tdseg, nullptr, 0);
     ctx->stats.launches++;
   }
   MDS_CUDA(ctx, cudaGetLastError());

@@ -152,10 +152,11 @@ def test_knn_data_fp32_large_k(ctx, oracle):
 
 # launches of the locality order (vec_order.cu): k-means (seed, 6 x assign +
 # update, final assign, keys), 2 radix passes of 3, the permutation; for a
-# second set assign, keys, sort, permutation; tile geometry, bounds, (start
-# tiles), threshold seeds, rowthr back to the input order
-ORDER_LAUNCHES_SAME = 22 + 2 + 1 + 1
-ORDER_LAUNCHES_FIT = 22 + 9 + 3 + 1 + 1
+# second set assign, keys, sort, permutation; column and row tile geometry,
+# coarse bounds, (start tiles over all), threshold seeds, refined bounds,
+# (start tiles per segment), rowthr back to the input order
+ORDER_LAUNCHES_SAME = 22 + 5 + 1
+ORDER_LAUNCHES_FIT = 22 + 9 + 7 + 1
 
 
 @pytest.mark.gpu
