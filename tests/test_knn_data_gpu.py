@@ -233,3 +233,22 @@ def test_knn_data_tc_ordered_unstructured(ctx, oracle, dim):
     padded dimensions 32 and 128."""
     x = np.random.default_rng(35 + dim).normal(size=(6_000, dim))
     _sampled(ctx, oracle, x, None, 16, np.arange(0, 6_000, 3))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("k", [90, 100])
+def test_knn_data_tc_ordered_large_k(ctx, oracle, k):
+    """Locality order at k + 1 = 91 (threshold heaps of 46 per half) and
+    k + 1 = 101 (above the heaps' limit: thresholds from list searches)."""
+    x = synth.dihedral_vectors(8_000, 64, seed=36).astype(np.float64)
+    _sampled(ctx, oracle, x, None, k, np.arange(0, 8_000, 7))
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_ordered_dim96_and_one_fit_row(ctx, oracle):
+    """Padded dimension 96 (80 dimensions) in locality order, and a fit set of
+    a single vector against 5,000 references."""
+    rng = np.random.default_rng(37)
+    x = rng.normal(size=(5_000, 80)) + rng.integers(0, 4, size=(5_000, 1)) * 3.0
+    _sampled(ctx, oracle, x, None, 12, np.arange(0, 5_000, 5))
+    _sampled(ctx, oracle, x, x[1234:1235] + 0.01, 12, np.arange(1))
