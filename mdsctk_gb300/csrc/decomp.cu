@@ -322,24 +322,59 @@ static inline int spmv_blocks(int n) { return (int)(((int64_t)(n + 1) / 2 * 32 +
 // h[j] = sum_i V[i + j*ld] * w[i], j < ncols; partial sums per block then a
 // second kernel reduces them (deterministic order).
 #define GV_ROWS 256
+//
+// The second pass of the reorthogonalisation runs only where ARPACK's test
+// (dsaitr, after Daniel, Gragg, Kaufman and Stewart) asks for it: when the
+// first pass left ||w|| <= 0.717 of its norm before the projection. Its
+// kernels then get `gate`: the first pass's partial sums of the new w_i^2
+// (gnpart, gnparts of them) and ||w||^2 before it (gh[0]); every block of
+// this kernel decides the same way (one warp, fixed order) and block 0
+// stores the decision in *flag, which the pass's other kernels read. A
+// skipped pass writes no partial sums.
+// With with_wnorm also column ncols of part: the block's sum of w_i^2.
 __global__ void k_gemv_t_part(const double* __restrict__ V, int64_t ld, int n, int ncols,
-                              const double* __restrict__ w, double* __restrict__ part) {
-  extern __shared__ double sh[];  // [blockDim/32][ncols]
+                              const double* __restrict__ w, double* __restrict__ part, int with_wnorm,
+                              const double* __restrict__ gnpart, int gnparts, const double* __restrict__ gh,
+                              int* __restrict__ flag) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int r0 = blockIdx.x * GV_ROWS, r1 = min(n, r0 + GV_ROWS);
-  for (int j = warp; j < ncols; j += nw) {
-    double s = 0.0;
-    for (int i = r0 + lane; i < r1; i += 32) s += V[i + j * ld] * w[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = s;
+  if (gnpart) {
+    __shared__ int s_need;
+    if (warp == 0) {
+      double q = 0.0;
+      for (int b = lane; b < gnparts; b += 32) q += gnpart[b];
+      for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+      if (lane == 0) {
+        const int need = !(q > 0.514089 * gh[0]);  // 0.717^2
+        s_need = need;
+        if (blockIdx.x == 0) *flag = need;
+      }
+    }
+    __syncthreads();
+    if (!s_need) return;
   }
-  (void)sh;
+  const int r0 = blockIdx.x * GV_ROWS, r1 = min(n, r0 + GV_ROWS);
+  const int nout = ncols + (with_wnorm ? 1 : 0);
+  for (int j = warp; j < nout; j += nw) {
+    double s = 0.0;
+    if (j < ncols)
+      for (int i = r0 + lane; i < r1; i += 32) s += V[i + j * ld] * w[i];
+    else
+      for (int i = r0 + lane; i < r1; i += 32) s += w[i] * w[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) part[(int64_t)blockIdx.x * nout + j] = s;
+  }
 }
 // h[j] = sum over blocks of part[b][j]: one warp per column (lanes take
-// blocks b = lane, lane + 32, ...; fixed shuffle tree, deterministic)
-__global__ void k_reduce_part(const double* __restrict__ part, int nparts, int ncols, double* __restrict__ h) {
+// blocks b = lane, lane + 32, ...; fixed shuffle tree, deterministic). A
+// skipped pass (flag 0) gives h = 0.
+__global__ void k_reduce_part(const double* __restrict__ part, int nparts, int ncols, double* __restrict__ h,
+                              const int* __restrict__ flag) {
   const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (j >= ncols) return;
+  if (flag && !*flag) {
+    if (lane == 0) h[j] = 0.0;
+    return;
+  }
   double s = 0.0;
   for (int b = lane; b < nparts; b += 32) s += part[(int64_t)b * ncols + j];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -347,11 +382,17 @@ __global__ void k_reduce_part(const double* __restrict__ part, int nparts, int n
 }
 // w -= V[:, 0:ncols] h. With npart (blockDim.x = 256) also each block's sum
 // of the new w_i^2, in a fixed order, into npart[blockIdx.x] (the norm of w
-// without another pass over it).
+// without another pass over it). A skipped pass (flag 0) leaves w and takes
+// the partial sums of the pass before (npart_in).
 __global__ void k_gemv_sub(const double* __restrict__ V, int64_t ld, int n, int ncols,
-                           const double* __restrict__ h, double* __restrict__ w, double* __restrict__ npart) {
+                           const double* __restrict__ h, double* __restrict__ w, double* __restrict__ npart,
+                           const int* __restrict__ flag, const double* __restrict__ npart_in) {
   extern __shared__ double hs[];
   __shared__ double red[8];
+  if (flag && !*flag) {
+    if (npart && threadIdx.x == 0) npart[blockIdx.x] = npart_in[blockIdx.x];
+    return;
+  }
   for (int j = threadIdx.x; j < ncols; j += blockDim.x) hs[j] = h[j];
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -373,29 +414,40 @@ __global__ void k_gemv_sub(const double* __restrict__ V, int64_t ld, int n, int 
     npart[blockIdx.x] = t;
   }
 }
-// alpha_j = both projections onto v_j; beta_j = ||w|| from the per-block
-// partial sums of w_i^2 (one warp, fixed order); breakdown when beta_j <=
-// tol * max(|alpha_j|, 1)
-__global__ void k_lz_finish(const double* __restrict__ h1, const double* __restrict__ h2,
-                            const double* __restrict__ npart, int nparts, int idx, int j, double tol,
-                            double* __restrict__ alpha, double* __restrict__ beta, int* __restrict__ brk) {
-  const int lane = threadIdx.x & 31;
-  double q = 0.0;
-  for (int b = lane; b < nparts; b += 32) q += npart[b];
-  for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-  if (threadIdx.x != 0) return;
-  double a = h1[idx] + h2[idx];
-  double b = sqrt(fmax(q, 0.0));
-  alpha[j] = a;
-  beta[j] = b;
-  brk[j] = (b <= tol * fmax(fabs(a), 1.0)) ? 1 : 0;
-}
-// v_{j+1} = w / beta_j (zeros after a breakdown; those steps are redone)
-__global__ void k_lz_scale(const double* __restrict__ w, const double* __restrict__ beta, const int* __restrict__ brk,
-                           int j, int n, double* __restrict__ out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  out[i] = brk[j] ? 0.0 : w[i] * (1.0 / beta[j]);
+// The end of a Lanczos step in one launch: alpha_j = both projections onto
+// v_j; beta_j = ||w|| from the per-block partial sums of w_i^2, which every
+// block reduces itself in the same fixed order (one warp), so all blocks use
+// the same beta_j; breakdown when beta_j <= tol * max(|alpha_j|, 1); then
+// v_{j+1} = w / beta_j (zeros after a breakdown; those steps are redone).
+// Block 0 records alpha_j, beta_j and the flag. (A separate one-warp kernel
+// for alpha/beta cost one launch more per step.)
+__global__ void k_lz_finish_scale(const double* __restrict__ h1, const double* __restrict__ h2,
+                                  const double* __restrict__ npart, int nparts, int idx, int j, double tol,
+                                  double* __restrict__ alpha, double* __restrict__ beta, int* __restrict__ brk,
+                                  const double* __restrict__ w, int n, double* __restrict__ out) {
+  __shared__ double s_scale;
+  __shared__ int s_brk;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double q = 0.0;
+    for (int b = lane; b < nparts; b += 32) q += npart[b];
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if (lane == 0) {
+      const double a = h1[idx] + h2[idx];
+      const double bt = sqrt(fmax(q, 0.0));
+      const int bk = (bt <= tol * fmax(fabs(a), 1.0)) ? 1 : 0;
+      s_scale = 1.0 / bt;
+      s_brk = bk;
+      if (blockIdx.x == 0) {
+        alpha[j] = a;
+        beta[j] = bt;
+        brk[j] = bk;
+      }
+    }
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = s_brk ? 0.0 : w[i] * s_scale;
 }
 __global__ void k_scale_copy(const double* __restrict__ w, double a, int n, double* __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -591,8 +643,10 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   MDS_TRY(part.alloc(ctx, sizeof(double) * (size_t)nparts * (nlock + m + 1)));
   MDS_TRY(Yd.alloc(ctx, sizeof(double) * (size_t)m * m));
   MDS_TRY(tmp.alloc(ctx, sizeof(double) * (size_t)n * m));
-  DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx), npart(ctx);
+  DevBuf h1(ctx), h2(ctx), ab(ctx), brk(ctx), npart(ctx), npart1(ctx), flag2(ctx);
   MDS_TRY(npart.alloc(ctx, sizeof(double) * (size_t)((n + 255) / 256)));
+  MDS_TRY(npart1.alloc(ctx, sizeof(double) * (size_t)((n + 255) / 256)));
+  MDS_TRY(flag2.alloc(ctx, sizeof(int)));
   // step graphs by first step of the cycle; destroyed on every return path
   struct Graphs : std::map<int, cudaGraphExec_t> {
     ~Graphs() {
@@ -615,8 +669,8 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   // dots/subtract act on the first ncols columns of [locked | basis]
   auto dots = [&](int ncols, std::vector<double>& hh) -> int {
     ctx->stats.launches += 2;
-    k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, ncols, w, part.as<double>());
-    k_reduce_part<<<(ncols + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, ncols, h.as<double>());
+    k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, ncols, w, part.as<double>(), 0, nullptr, 0, nullptr, nullptr);
+    k_reduce_part<<<(ncols + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, ncols, h.as<double>(), nullptr);
     MDS_CUDA(ctx, cudaGetLastError());
     hh.resize(ncols);
     MDS_CUDA(ctx, cudaMemcpyAsync(hh.data(), h.p, sizeof(double) * ncols, cudaMemcpyDeviceToHost, s));
@@ -627,7 +681,7 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
     MDS_CUDA(ctx, cudaMemcpyAsync(h.p, hh.data(), sizeof(double) * ncols, cudaMemcpyHostToDevice, s));
     ctx->stats.launches++;
     k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * ncols, s>>>(Vl, ld, n, ncols, h.as<double>(), w,
-                                                                      nullptr);
+                                                                      nullptr, nullptr, nullptr);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
@@ -635,8 +689,8 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
   auto norm_w = [&](double* nr) -> int {
     // ||w|| through the same partial-sum kernels (V column = w itself)
     ctx->stats.launches += 2;
-    k_gemv_t_part<<<nparts, 256, 0, s>>>(w, ld, n, 1, w, part.as<double>());
-    k_reduce_part<<<1, 128, 0, s>>>(part.as<double>(), nparts, 1, h.as<double>());
+    k_gemv_t_part<<<nparts, 256, 0, s>>>(w, ld, n, 1, w, part.as<double>(), 0, nullptr, 0, nullptr, nullptr);
+    k_reduce_part<<<1, 128, 0, s>>>(part.as<double>(), nparts, 1, h.as<double>(), nullptr);
     double v = 0;
     MDS_CUDA(ctx, cudaMemcpyAsync(&v, h.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     MDS_CUDA(ctx, cudaStreamSynchronize(s));
@@ -683,18 +737,23 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
           const int nc = nlock + j + 1;  // full reorthogonalisation (twice)
           k_spmv<<<spmv_blocks(op.n), 256, 0, s>>>(op.rp.as<int64_t>(), op.col.as<int>(), op.w.as<double>(),
                                                    Vp + (int64_t)j * ld, op.n, w);
-          k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
-          k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h1.as<double>());
-          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h1.as<double>(), w, nullptr);
-          k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>());
-          k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h2.as<double>());
+          // first pass, with ||w||^2 before it (h1[nc]) and the new w's
+          // partial sums (npart1); the second pass only where ARPACK's test
+          // asks for it (k_gemv_t_part)
+          k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>(), 1, nullptr, 0, nullptr, nullptr);
+          k_reduce_part<<<(nc + 4) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc + 1, h1.as<double>(), nullptr);
+          k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h1.as<double>(), w,
+                                                                        npart1.as<double>(), nullptr, nullptr);
+          k_gemv_t_part<<<nparts, 256, 0, s>>>(Vl, ld, n, nc, w, part.as<double>(), 0, npart1.as<double>(),
+                                               (n + 255) / 256, h1.as<double>() + nc, flag2.as<int>());
+          k_reduce_part<<<(nc + 3) / 4, 128, 0, s>>>(part.as<double>(), nparts, nc, h2.as<double>(), flag2.as<int>());
           k_gemv_sub<<<(n + 255) / 256, 256, sizeof(double) * nc, s>>>(Vl, ld, n, nc, h2.as<double>(), w,
-                                                                       npart.as<double>());
-          k_lz_finish<<<1, 32, 0, s>>>(h1.as<double>(), h2.as<double>(), npart.as<double>(), (n + 255) / 256,
-                                       nlock + j, j, eps * 10.0, ab.as<double>(), ab.as<double>() + m,
-                                       brk.as<int>());
-          k_lz_scale<<<(n + 255) / 256, 256, 0, s>>>(w, ab.as<double>() + m, brk.as<int>(), j, n,
-                                                     Vp + (int64_t)(j + 1) * ld);
+                                                                       npart.as<double>(), flag2.as<int>(),
+                                                                       npart1.as<double>());
+          k_lz_finish_scale<<<(n + 255) / 256, 256, 0, s>>>(h1.as<double>(), h2.as<double>(), npart.as<double>(),
+                                                             (n + 255) / 256, nlock + j, j, eps * 10.0,
+                                                             ab.as<double>(), ab.as<double>() + m, brk.as<int>(), w,
+                                                             n, Vp + (int64_t)(j + 1) * ld);
         }
         cudaGraph_t g = nullptr;
         cudaError_t ce = cudaStreamEndCapture(s, &g);
@@ -707,7 +766,7 @@ static int lanczos(mds_ctx* ctx, const SymOp& op, int nev, int ncv, double tol, 
       }
       MDS_CUDA(ctx, cudaGraphLaunch(git->second, s));
       out.matvecs += m - j0;
-      ctx->stats.launches += 9 * (m - j0);
+      ctx->stats.launches += 8 * (m - j0);
       MDS_CUDA(ctx, cudaGetLastError());
       std::vector<double> hab(2 * m);
       std::vector<int> hbrk(m);
