@@ -173,9 +173,10 @@ int mds_knn_data(mds_ctx* ctx, const double* ref, int n_ref, const double* fit, 
  * n * dim * 4 bytes of vectors) are rejected with MDS_ERR_UNSUPPORTED. When
  * K' < k + 17 every row is rechecked exactly, as mds_knn_data does.
  *   flags: 0 or MDS_CORRELATION (sorted output only).
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress, once per device); make that first call before any
- * stream capture. The call synchronises ctx's stream before it returns.
+ * The call synchronises ctx's stream before it returns and reads a device
+ * count on the host to decide on a second pass, so it cannot be recorded
+ * into a CUDA graph. The first call on a device also looks up the array's
+ * device address (cudaGetSymbolAddress, once per device).
  * Calls share the array and it keeps the last call's contents: calls that
  * may overlap on the GPU (other contexts or threads) race and must be
  * serialised by the caller. The caller's current device is restored on
