@@ -89,7 +89,7 @@ def parse():
     p.add_argument("--pipeline", choices=["small", "scale", "euclid", "sparse"],
                    help="per-stage wall time of a whole pipeline: small = 2,000 x 304 frames (parity vs the oracle), "
                         "scale = 100,000 x 304 (kNN k=64, sysparse, Lanczos nev=20 ncv=60 tol=1e-8), "
-                        "euclid = knn_data 200,000 x 64, k=32, "
+                        "euclid = knn_data 200,000 x 64, k=32 (Euclidean, then correlation), "
                         "sparse = contact_profile of 20,000 x 304 frames (atoms 0-151 vs 152-303, 12 A) "
                         "-> knn_data_sparse, k=32")
     p.add_argument("--pipeline-cpu", action="store_true", help="also time the CPU oracle's sysparse and eigsh")
@@ -424,6 +424,12 @@ def run_pipeline(args):
             od, oi = O.knn_data(x, x[rows], k)
             st["parity_rows_checked"] = len(rows)
             st["parity_bit_exact_distances"] = bool(np.array_equal(d[rows], od))
+            # the same set under the correlation metric (knn_data -c)
+            d, i = timed("knn_data_correlation",
+                         lambda: c.knn_data(x, None, k, correlation=True, precision=args.precision), c)
+            st["correlation_pairs_per_s"] = n * n / st["knn_data_correlation"]
+            od, oi = O.knn_data(x, x[rows], k, correlation=True)
+            st["correlation_parity_bit_exact_distances"] = bool(np.array_equal(d[rows], od))
     out["stages"] = st
     print(json.dumps(out))
     return 0

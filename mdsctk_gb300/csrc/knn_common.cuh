@@ -89,6 +89,15 @@ __device__ __forceinline__ void block_bitonic_sort(uint64_t* a, int P2) {
     }
 }
 
+// The correlation metric's squared distance (1 - r) / 2 of two standardised
+// vectors is |z_x - z_y|^2 / 4 of their FP32 operands within this margin:
+// half the largest | |z|^2 - 1 | of the FP32 norms (devn, the float's bits),
+// the norms' summation error (< Dp 2^-24), and the operands' rounding to
+// FP32 (< 2^-24 |z| per vector).
+__device__ __forceinline__ float corr_margin(const unsigned* devn, int Dp) {
+  return 0.5f * __uint_as_float(__ldg(devn)) + 1e-7f * (float)Dp + 1e-6f;
+}
+
 __host__ __device__ static inline int next_pow2(int x) {
   int p = 1;
   while (p < x) p <<= 1;
@@ -188,9 +197,10 @@ int vec_order_max_dp();
 int vec_order(mds_ctx* ctx, const float* X, int n, int Dp, float* cent, bool fit, int* perm);
 int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
                     int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall,
-                    int k1, float* rowthr);
+                    int k1, float* rowthr, const unsigned* devn);
 int vec_seed_rows(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
-                  int nfit, int Dp, const int* tdall, int k1, const float* nmax, float* rowthr);
+                  int nfit, int Dp, const int* tdall, int k1, const float* nmax, float* rowthr,
+                  const unsigned* devn);
 int vec_unsort(mds_ctx* ctx, const float* src, const int* perm, int n, float* dst);
 
 // Tile skipping data of the tensor-core screen (knn_rms_tc.cu): lower

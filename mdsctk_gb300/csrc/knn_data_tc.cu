@@ -60,18 +60,21 @@
 // With nmax != nullptr (zeroed by the caller) also the largest norm of the n
 // vectors, as the float's bits (norms are non-negative). perm (or null): row
 // r is vector perm[r] (the locality order of vec_order.cu); nsorted (or
-// null) receives the norms in that order.
+// null) receives the norms in that order. devn (or null; correlation): the
+// largest | |z|^2 - 1 | of the standardised vectors, as the float's bits.
 __global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows, __nv_bfloat16* __restrict__ out,
                             const float* __restrict__ nrm, float guard, int corr, float* __restrict__ terms,
-                            float* __restrict__ nmax, const int* __restrict__ perm, float* __restrict__ nsorted) {
+                            float* __restrict__ nmax, const int* __restrict__ perm, float* __restrict__ nsorted,
+                            unsigned* __restrict__ devn) {
   const int64_t total = (int64_t)rows * Dp;
-  float mx = 0.0f;
+  float mx = 0.0f, dv = 0.0f;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = e / Dp;
     const int d = (int)(e % Dp);
     const int64_t src = (r < n && perm) ? (int64_t)perm[r] : r;
     if (nmax && d == 0 && r < n) mx = fmaxf(mx, nrm[src]);
     if (nsorted && d == 0 && r < n) nsorted[r] = nrm[src];
+    if (devn && d == 0 && r < n) dv = fmaxf(dv, fabsf(nrm[src] - 1.0f));
     if (terms && d == 0)
       terms[r] = (r < n) ? (corr ? -guard * nrm[src] : nrm[src] * (1.0f - guard)) : __int_as_float(0x7f800000);
     const float x = (r < n) ? X[src * Dp + d] : 0.0f;
@@ -83,6 +86,10 @@ __global__ void k_vec_split(const float* __restrict__ X, int n, int Dp, int rows
   if (nmax) {
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(reinterpret_cast<int*>(nmax), __float_as_int(mx));
+  }
+  if (devn) {
+    for (int o = 16; o > 0; o >>= 1) dv = fmaxf(dv, __shfl_xor_sync(0xffffffffu, dv, o));
+    if ((threadIdx.x & 31) == 0 && dv > 0.0f) atomicMax(devn, __float_as_uint(dv));
   }
 }
 
@@ -204,7 +211,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
              float* __restrict__ rowthr, uint64_t* __restrict__ work, uint64_t* __restrict__ candout,
              int* __restrict__ cand_n, int* __restrict__ err, int lcap, int k1, const float* __restrict__ nmax,
              const float* __restrict__ dlo, const int* __restrict__ tdv, const int* __restrict__ tdall,
-             int near_first, const int* __restrict__ rperm, const int* __restrict__ cperm, int KH) {
+             int near_first, const int* __restrict__ rperm, const int* __restrict__ cperm, int KH,
+             const unsigned* __restrict__ devn) {
   // err[0]: error code; err[1]: next unclaimed work item (zeroed by the host);
   // err[2]: column tiles computed (added to).
   // Locality order (vec_order.cu; all four null without it): rows and columns
@@ -215,7 +223,9 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   // the item's rows. tdv: the visit's start tile ([item] for the pilot,
   // [row pair tile][segment] otherwise) when the set is not screened against
   // itself, tdall [row pair tile] the start over all tiles; near_first: the
-  // item order of tv_item.
+  // item order of tv_item. For the correlation metric (devn != null) dlo
+  // bounds |z_x - z_y| of the standardised vectors, and the distance is
+  // |z_x - z_y|^2 / 4 within corr_margin.
   // KH = ceil(k1 / 2) (or 0: off): the epilogue keeps, per (row, column half),
   // a heap of the KH smallest bounds it appended (tv_heap_push), so the row's
   // threshold follows the larger of its halves' KH-th bounds (2 KH >= k1
@@ -338,6 +348,8 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       if (!ok) break;
       ++na;
       const float* dl = (dlo && !pilot) ? dlo + (int64_t)rp * ncoltiles : nullptr;
+      const float dsc = devn ? 0.25f : 1.0f;
+      const float dmarg = devn ? corr_margin(devn, Dp) : 0.0f;
       for (int base = 0; base < nvisit && ok; base += 32) {
         unsigned skip = 0u;
         if (dl) {
@@ -352,7 +364,7 @@ k_screen_tcv(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
           bool sk = false;
           if (base + lane < nvisit) {
             const float b = __ldg(dl + tv_tile_order(base + lane, t0, t1, td));
-            sk = b > 0.0f && b * b >= mx;
+            sk = b > 0.0f && b * b * dsc - dmarg >= mx;
           }
           skip = __ballot_sync(0xffffffffu, sk);
         }
@@ -684,7 +696,7 @@ int tcv_choose_nseg(mds_ctx* ctx, int nfit, int nref) {
 // multiple of 32, at most TV_MAX_DP), nf/nr their squared norms. same: Xf is
 // Xr (a set screened against itself; the visit starts at the diagonal).
 // order: screen in locality order with tile skipping (vec_order.cu; the
-// Euclidean metric only). Writes the candidate lists candout [nfit][nseg][Kp]
+// Euclidean and correlation metrics). Writes the candidate lists candout [nfit][nseg][Kp]
 // (each unsorted), their sizes cand_n [nfit][nseg], and rowthr [nfit]: the
 // threshold below which a row's pairs were kept (the bound of every pair left
 // out when a row's lists hold fewer than K' in all). *tiles: the column tiles
@@ -698,16 +710,18 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
   const int ncoltiles = (nref + TV_N - 1) / TV_N;
   if (nseg < 1 || nseg > ncoltiles) return mds_fail(ctx, MDS_ERR_INTERNAL, "bad segment count %d", nseg);
   // (below 16 column tiles the order is not worth its launches)
-  if (order && (corr || Dp > vec_order_max_dp() || nref < 16 * TV_N)) order = false;
+  if (order && (Dp > vec_order_max_dp() || nref < 16 * TV_N)) order = false;
   cudaStream_t s = ctx->stream;
   const int rowsA = (nfit + TV_ROWS - 1) / TV_ROWS * TV_ROWS, rowsB = ncoltiles * TV_N;
   const int rowsS = std::max(rowsA, rowsB);
   const int nrp = rowsA / TV_ROWS;
-  DevBuf A(ctx), B(ctx), work(ctx), err(ctx), terms(ctx), nmax(ctx);
+  DevBuf A(ctx), B(ctx), work(ctx), err(ctx), terms(ctx), nmax(ctx), devn(ctx);
   DevBuf cent(ctx), permr(ctx), permf(ctx), nrs(ctx), nfs(ctx), dlo(ctx), tdseg(ctx), tdall(ctx), rts(ctx);
   MDS_TRY(terms.alloc(ctx, sizeof(float) * (size_t)rowsS));
   MDS_TRY(nmax.alloc(ctx, sizeof(float)));
   MDS_CUDA(ctx, cudaMemsetAsync(nmax.p, 0, sizeof(float), s));
+  MDS_TRY(devn.alloc(ctx, sizeof(unsigned)));
+  MDS_CUDA(ctx, cudaMemsetAsync(devn.p, 0, sizeof(unsigned), s));
   const int* pr = nullptr;
   const int* pf = nullptr;
   if (order) {
@@ -736,7 +750,8 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
     const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 16);
     ctx->stats.launches++;
     k_vec_split<<<grid, 256, 0, s>>>(X, n, Dp, rows, out.as<__nv_bfloat16>(), nrm, MDS_GUARD_TC, corr ? 1 : 0, t,
-                                     t ? nmax.as<float>() : nullptr, perm, nsorted);
+                                     t ? nmax.as<float>() : nullptr, perm, nsorted,
+                                     (order && corr) ? devn.as<unsigned>() : nullptr);
     MDS_CUDA(ctx, cudaGetLastError());
     return MDS_OK;
   };
@@ -767,7 +782,8 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
     // of appends under no threshold); the seeds also let the bounds skip the
     // exact refinement of tiles the coarse bound already excludes
     MDS_TRY(vec_tile_bounds(ctx, Xr, pr, nref, Xf, pf, nfit, Dp, TV_N, nmax.as<float>(), dlo.as<float>(), nseg,
-                            same ? nullptr : tdseg.as<int>(), same ? nullptr : tdall.as<int>(), k + 1, rt));
+                            same ? nullptr : tdseg.as<int>(), same ? nullptr : tdall.as<int>(), k + 1, rt,
+                            corr ? devn.as<unsigned>() : nullptr));
   } else {
     MDS_CUDA(ctx, cudaMemsetAsync(rt, 0x7f, sizeof(float) * (size_t)nfit, s));
   }
@@ -801,7 +817,7 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
     k_screen_tcv<<<std::min(nrp, ctx->num_sms), TV_THREADS, smem, s>>>(
         mA, mB, nfk, terms.as<float>(), nfit, nref, Dp, nst, corr ? 1 : 0, MDS_GUARD_TC, idesc, Kp, 1, nrp,
         same ? 1 : 0, TV_PILOT, rt, work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
-        nmax.as<float>(), nullptr, nullptr, nullptr, 0, nullptr, nullptr, KH);
+        nmax.as<float>(), nullptr, nullptr, nullptr, 0, nullptr, nullptr, KH, nullptr);
     MDS_CUDA(ctx, cudaGetLastError());
     MDS_CUDA(ctx, cudaMemsetAsync(err.as<int>() + 1, 0, sizeof(int), s));
   }
@@ -810,7 +826,8 @@ int launch_screen_tcv(mds_ctx* ctx, const float* Xf, const float* nf, int nfit, 
                                               MDS_GUARD_TC, idesc, Kp, nseg, nitems, same ? 1 : 0, 0, rt,
                                               work.as<uint64_t>(), candout, cand_n, err.as<int>(), lcap, k + 1,
                                               nmax.as<float>(), pdlo, ptdseg, ptdall, order ? 1 : 0,
-                                              pr ? pf : nullptr, pr, KH);
+                                              pr ? pf : nullptr, pr, KH,
+                                              (order && corr) ? devn.as<unsigned>() : nullptr);
   MDS_CUDA(ctx, cudaGetLastError());
   if (order) MDS_TRY(vec_unsort(ctx, rt, pf, nfit, rowthr));
   int herr[3] = {0, 0, 0};

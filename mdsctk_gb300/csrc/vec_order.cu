@@ -218,7 +218,8 @@ __global__ void __launch_bounds__(256) k_vo_seed_rows(const float* __restrict__ 
                                                       int nref, const float* __restrict__ Xf,
                                                       const int* __restrict__ permf, int nfit, int Dp,
                                                       const int* __restrict__ tdall, int ncoltiles, int k1,
-                                                      const float* __restrict__ nmax, float* __restrict__ rowthr) {
+                                                      const float* __restrict__ nmax, float* __restrict__ rowthr,
+                                                      const unsigned* __restrict__ devn) {
   extern __shared__ float sm[];  // members [128][Dp + 1], then rows [8][Dp]
   const int item = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int T = tdall ? tdall[item] : min((item * 256 + 128) / 128, ncoltiles - 1);
@@ -258,7 +259,9 @@ __global__ void __launch_bounds__(256) k_vo_seed_rows(const float* __restrict__ 
     const float vk = __shfl_sync(0xffffffffu, v[q & 3], q >> 2);
     // the FP32 sum of Dp squares errs by < (Dp + 2) 2^-24 of itself; the
     // inputs' rounding to FP32 moves d^2 by < 2.4e-7 (|x|^2 + |y|^2)
-    if (lane == 0 && k1 <= m) rowthr[g] = vk * (1.0f + 3e-5f) + 1e-6f * (xn + nm);
+    // (correlation: the distance is a quarter of that within corr_margin)
+    const float up = vk * (1.0f + 3e-5f) + 1e-6f * (xn + nm);
+    if (lane == 0 && k1 <= m) rowthr[g] = devn ? 0.25f * up + corr_margin(devn, Dp) : up;
     __syncwarp();
   }
 }
@@ -305,7 +308,8 @@ template <int DP>
 __global__ void __launch_bounds__(256) k_vo_refine(const float* __restrict__ X, const int* __restrict__ perm, int n,
                                                    const float* __restrict__ center, const float* __restrict__ rad,
                                                    int nct, const float* __restrict__ nmax,
-                                                   const float* __restrict__ rowthr, float* __restrict__ dlo) {
+                                                   const float* __restrict__ rowthr, float* __restrict__ dlo,
+                                                   const unsigned* __restrict__ devn) {
   __shared__ __align__(16) float cen[32 * DP];
   __shared__ float cnr[32];
   __shared__ float wmin[8][33];
@@ -352,6 +356,9 @@ __global__ void __launch_bounds__(256) k_vo_refine(const float* __restrict__ X, 
   __syncthreads();
   const float nabs = 2e-6f * (sqrtf(__ldg(nmax)) + sqrtf(xmax));
   const float mrel = 4e-7f * DP;
+  // the distance as a function of |x - y| (correlation: see k_vo_seed_rows)
+  const float dsc = devn ? 0.25f : 1.0f;
+  const float dmarg = devn ? corr_margin(devn, DP) : 0.0f;
   float* row = dlo + (int64_t)item * nct;
   for (int W0 = 0; W0 < nct; W0 += 256) {
     // the tiles of this window that the coarse bound cannot skip (the first
@@ -362,7 +369,7 @@ __global__ void __launch_bounds__(256) k_vo_refine(const float* __restrict__ X, 
     {
       const int T = W0 + t;
       const float c = (T < nct) ? row[T] : 1.0f;
-      const bool need = T < nct && !(c > 0.0f && c * c >= smax);
+      const bool need = T < nct && !(c > 0.0f && c * c * dsc - dmarg >= smax);
       const unsigned b = __ballot_sync(0xffffffffu, need);
       int base = 0;
       if (lane == 0 && b) base = atomicAdd(&s_cnt, __popc(b));
@@ -511,10 +518,11 @@ int vec_order(mds_ctx* ctx, const float* X, int n, int Dp, float* cent, bool fit
 // for a set against itself), the threshold seeds of the rows into rowthr
 // (sorted order, +inf-like before), then the refinement of the bounds the
 // coarse ones cannot skip by, and tdseg [nitems][nseg] (or null). nmax:
-// device float, the reference set's largest squared norm.
+// device float, the reference set's largest squared norm. devn (or null):
+// the correlation metric's largest | |z|^2 - 1 | (float bits).
 int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
                     int nfit, int Dp, int tile, const float* nmax, float* dlo, int nseg, int* tdseg, int* tdall,
-                    int k1, float* rowthr) {
+                    int k1, float* rowthr, const unsigned* devn) {
   cudaStream_t s = ctx->stream;
   const int nct = (nref + tile - 1) / tile, nitems = (nfit + 255) / 256;
   DevBuf center(ctx), rad(ctx), cenI(ctx), radI(ctx);
@@ -532,23 +540,23 @@ int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, c
     ctx->stats.launches++;
   }
   MDS_CUDA(ctx, cudaGetLastError());
-  MDS_TRY(vec_seed_rows(ctx, Xr, permr, nref, Xf, permf, nfit, Dp, tdall, k1, nmax, rowthr));
+  MDS_TRY(vec_seed_rows(ctx, Xr, permr, nref, Xf, permf, nfit, Dp, tdall, k1, nmax, rowthr, devn));
   switch (Dp) {
     case 32:
       k_vo_refine<32><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
-                                             rowthr, dlo);
+                                             rowthr, dlo, devn);
       break;
     case 64:
       k_vo_refine<64><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
-                                             rowthr, dlo);
+                                             rowthr, dlo, devn);
       break;
     case 96:
       k_vo_refine<96><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
-                                             rowthr, dlo);
+                                             rowthr, dlo, devn);
       break;
     case 128:
       k_vo_refine<128><<<nitems, 256, 0, s>>>(Xf, permf, nfit, center.as<float>(), rad.as<float>(), nct, nmax,
-                                              rowthr, dlo);
+                                              rowthr, dlo, devn);
       break;
     default:
       return mds_fail(ctx, MDS_ERR_INTERNAL, "vec_tile_bounds: padded dimension %d", Dp);
@@ -566,7 +574,8 @@ int vec_tile_bounds(mds_ctx* ctx, const float* Xr, const int* permr, int nref, c
 // entries are +inf-like before (a row without a seed keeps its value). The
 // reference set is in tiles of 128.
 int vec_seed_rows(mds_ctx* ctx, const float* Xr, const int* permr, int nref, const float* Xf, const int* permf,
-                  int nfit, int Dp, const int* tdall, int k1, const float* nmax, float* rowthr) {
+                  int nfit, int Dp, const int* tdall, int k1, const float* nmax, float* rowthr,
+                  const unsigned* devn) {
   if (k1 > 128) return MDS_OK;
   const int ncoltiles = (nref + 127) / 128, nitems = (nfit + 255) / 256;
   const size_t smem = sizeof(float) * ((size_t)128 * (Dp + 1) + 8 * (size_t)Dp);
@@ -575,7 +584,7 @@ int vec_seed_rows(mds_ctx* ctx, const float* Xr, const int* permr, int nref, con
   MDS_TRY(mds_allow_dyn_smem(ctx, k_vo_seed_rows, &attr_done, &attr_limit));
   if (smem > attr_limit) return MDS_OK;
   k_vo_seed_rows<<<nitems, 256, smem, ctx->stream>>>(Xr, permr, nref, Xf, permf, nfit, Dp, tdall, ncoltiles, k1,
-                                                      nmax, rowthr);
+                                                      nmax, rowthr, devn);
   ctx->stats.launches++;
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;

@@ -180,19 +180,19 @@ def test_knn_data_tc_pilot_pass(ctx, oracle, fit_rows, skip):
     assert st["launches"] - plain - extra in _recheck_launches(12)
 
 
-def _sampled(ctx, oracle, ref, fit, k, rows):
+def _sampled(ctx, oracle, ref, fit, k, rows, corr=False):
     """Both tensor-core screens (locality order with tile skipping, and every
     tile in input order) give the same output, and sampled rows match the
     oracle bit for bit."""
-    d, i = ctx.knn_data(ref, fit, k, precision="bf16x3")
+    d, i = ctx.knn_data(ref, fit, k, correlation=corr, precision="bf16x3")
     st = ctx.stats()
-    d0, i0 = ctx.knn_data(ref, fit, k, precision="bf16x3", skip=False)
+    d0, i0 = ctx.knn_data(ref, fit, k, correlation=corr, precision="bf16x3", skip=False)
     st0 = ctx.stats()
     assert np.array_equal(d, d0)
     for r, c in np.argwhere(i != i0):
         assert np.sum(d0[r] == d0[r, c]) >= 2
     q = ref if fit is None else fit
-    od, oi = oracle.knn_data(ref, q[rows], k)
+    od, oi = oracle.knn_data(ref, q[rows], k, correlation=corr)
     _check(d[rows], i[rows], od, oi)
     return st, st0
 
@@ -252,3 +252,27 @@ def test_knn_data_tc_ordered_dim96_and_one_fit_row(ctx, oracle):
     x = rng.normal(size=(5_000, 80)) + rng.integers(0, 4, size=(5_000, 1)) * 3.0
     _sampled(ctx, oracle, x, None, 12, np.arange(0, 5_000, 5))
     _sampled(ctx, oracle, x, x[1234:1235] + 0.01, 12, np.arange(1))
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_ordered_correlation(ctx, oracle):
+    """Correlation metric in locality order (the standardised vectors' tiles
+    and bounds): 20,000 x 64 mixture vectors against themselves, k = 32, and
+    3,001 separate fit vectors against 12,345 references, k = 20."""
+    x = synth.dihedral_vectors(20_000, 64, seed=41).astype(np.float64)
+    st, st0 = _sampled(ctx, oracle, x, None, 32, np.linspace(0, 19_999, 200).astype(int), corr=True)
+    assert st["screen_pairs"] < st0["screen_pairs"], (st["screen_pairs"], st0["screen_pairs"])
+    fit = synth.dihedral_vectors(3_001, 64, seed=42).astype(np.float64)
+    _sampled(ctx, oracle, x[:12_345], fit, 20, np.arange(0, 3_001, 3), corr=True)
+
+
+@pytest.mark.gpu
+def test_knn_data_tc_ordered_correlation_offset(ctx, oracle):
+    """Correlation of vectors on a large common offset (1e4 + N(0, 0.01^2)):
+    the single-pass standard deviation loses digits, so the standardised
+    vectors' norms stray from 1 and the bounds' margin grows with them; each
+    vector present twice (ties at distance 0)."""
+    rng = np.random.default_rng(43)
+    base = 1e4 + 0.01 * rng.normal(size=(2_500, 24)) + 0.02 * rng.integers(0, 3, size=(2_500, 1)) * np.arange(24)
+    x = np.concatenate([base, base])[rng.permutation(5_000)]
+    _sampled(ctx, oracle, x, None, 10, np.arange(0, 5_000, 2), corr=True)
