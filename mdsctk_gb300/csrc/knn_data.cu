@@ -243,6 +243,26 @@ __device__ __forceinline__ double exact_corr(const double* a, double ma, double 
   return value;  // squared distance; sqrt taken by the caller
 }
 
+// the same on vectors already centred (x - mean, in the reference's own
+// subtraction, by k_vec_center): the products and sums are unchanged
+__device__ __forceinline__ double exact_corr_centred(const double* ac, double sa, const double* bc, double sb,
+                                                     int dim) {
+  double dsize = (double)dim, value = 0.0;
+  for (int x = 0; x < dim; ++x) value = __dadd_rn(value, __dmul_rn(ac[x], bc[x]));
+  value = __ddiv_rn(__dsub_rn(1.0, __ddiv_rn(value, __dmul_rn(__dmul_rn(__dsub_rn(dsize, 1.0), sa), sb))), 2.0);
+  if (value < 0.0) value = 0.0;
+  return value;
+}
+
+// Xc [n][dim] = X - mean of its vector, for the correlation recheck: each
+// (x - mean) of correlation_distance (mdsctk.cpp:349) is a per-vector
+// value, computed once here instead of once per pair.
+__global__ void k_vec_center(const double* __restrict__ X, int64_t total, int dim, const double* __restrict__ mean,
+                             double* __restrict__ Xc) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    Xc[e] = __dsub_rn(X[e], mean[e / dim]);
+}
+
 #define DR_THREADS 256
 
 // One block per fit row. mode 0: candidates from the screen; mode 1: every
@@ -514,12 +534,12 @@ k_recheck_cands(const uint64_t* __restrict__ cand, const int* __restrict__ cand_
 
 // Stage 2, one thread per (row, candidate slot): the exact value of the
 // candidate in the reference's arithmetic. The slots of all rows are one
-// dense range, so every lane of the FP64 pipe has a pair to compute.
+// dense range, so every lane of the FP64 pipe has a pair to compute. For
+// the correlation metric Xfit / Xref are the centred vectors (k_vec_center).
 __global__ void __launch_bounds__(256)
-k_recheck_exact(const double* __restrict__ Xfit, const double* __restrict__ Xref, const double* __restrict__ mf,
-                const double* __restrict__ sfv, const double* __restrict__ mr, const double* __restrict__ srv,
-                int nrows, int dim, int corr, int fw, const int* __restrict__ cidx, const int4* __restrict__ meta,
-                double* __restrict__ ev) {
+k_recheck_exact(const double* __restrict__ Xfit, const double* __restrict__ Xref, const double* __restrict__ sfv,
+                const double* __restrict__ srv, int nrows, int dim, int corr, int fw, const int* __restrict__ cidx,
+                const int4* __restrict__ meta, double* __restrict__ ev) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= (int64_t)nrows * fw) return;
   const int row = (int)(slot / fw), c = (int)(slot % fw);
@@ -527,7 +547,7 @@ k_recheck_exact(const double* __restrict__ Xfit, const double* __restrict__ Xref
   const int j = cidx[slot];
   const double* a = Xfit + (int64_t)row * dim;
   const double* b = Xref + (int64_t)j * dim;
-  ev[slot] = corr ? exact_corr(a, mf[row], sfv[row], b, mr[j], srv[j], dim) : exact_euclid(a, b, dim);
+  ev[slot] = corr ? exact_corr_centred(a, sfv[row], b, srv[j], dim) : exact_euclid(a, b, dim);
 }
 
 // Stage 3, one warp per row: the k+1 best rechecked candidates by (value,
@@ -631,7 +651,7 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
   MDS_TRY(flagged.alloc(ctx, sizeof(int) * (size_t)std::max(nfit, 1)));
   MDS_TRY(nflag.alloc(ctx, sizeof(int)));
   MDS_CUDA(ctx, cudaMemsetAsync(nflag.p, 0, sizeof(int), s));
-  DevBuf big(ctx), nbig(ctx), cidx(ctx), meta(ctx), evals(ctx);
+  DevBuf big(ctx), nbig(ctx), cidx(ctx), meta(ctx), evals(ctx), Cr(ctx), Cf(ctx);
   auto recheck = [&](int nrows, const int* rowlist, int mode, const uint64_t* cand, const int* cand_n, int nseg,
                      int Kp, const float* rowthr) -> int {
     size_t smem = data_recheck_smem(dim, Kp, nseg, k, mode);
@@ -646,14 +666,33 @@ int knn_data_run(mds_ctx* ctx, const double* dref, int nref, const double* dfit,
       MDS_TRY(meta.alloc(ctx, sizeof(int4) * (size_t)nrows));
       MDS_TRY(evals.alloc(ctx, sizeof(double) * (size_t)nrows * fw));
       MDS_CUDA(ctx, cudaMemsetAsync(nbig.p, 0, sizeof(int), s));
+      const double* ea = dfit;
+      const double* eb = dref;
+      if (corr) {
+        // centred copies of both sets (one for a set against itself)
+        auto center = [&](const double* X, int n, const double* mean, DevBuf& out) -> int {
+          const int64_t total = (int64_t)n * dim;
+          MDS_TRY(out.alloc(ctx, sizeof(double) * (size_t)total));
+          const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 8);
+          st.launches++;
+          k_vec_center<<<grid, 256, 0, s>>>(X, total, dim, mean, out.as<double>());
+          MDS_CUDA(ctx, cudaGetLastError());
+          return MDS_OK;
+        };
+        MDS_TRY(center(dref, nref, Mr.as<double>(), Cr));
+        eb = ea = Cr.as<double>();
+        if (!same) {
+          MDS_TRY(center(dfit, nfit, mf, Cf));
+          ea = Cf.as<double>();
+        }
+      }
       const int wb = (nrows + RW_WARPS - 1) / RW_WARPS;
       st.launches += 3;
       k_recheck_cands<<<wb, RW_WARPS * 32, 0, s>>>(cand, cand_n, nrows, nseg, Kp, k + 1, fw, rowthr, cidx.as<int>(),
                                                    meta.as<int4>(), big.as<int>(), nbig.as<int>());
       const int64_t slots = (int64_t)nrows * fw;
-      k_recheck_exact<<<(int)((slots + 255) / 256), 256, 0, s>>>(dfit, dref, mf, sf, Mr.as<double>(), Sr.as<double>(),
-                                                                 nrows, dim, corr, fw, cidx.as<int>(),
-                                                                 meta.as<int4>(), evals.as<double>());
+      k_recheck_exact<<<(int)((slots + 255) / 256), 256, 0, s>>>(ea, eb, sf, Sr.as<double>(), nrows, dim, corr, fw,
+                                                                 cidx.as<int>(), meta.as<int4>(), evals.as<double>());
       k_recheck_finish<<<wb, RW_WARPS * 32, 0, s>>>(nrows, k, fw, cidx.as<int>(), meta.as<int4>(),
                                                     evals.as<double>(), dout_d, dout_i, flagged.as<int>(),
                                                     nflag.as<int>(), big.as<int>(), nbig.as<int>());

@@ -10,11 +10,12 @@ from mdsctk_gb300 import synth
 REF = os.path.join(os.path.dirname(__file__), "golden")
 
 
-def _recheck_launches(k):
+def _recheck_launches(k, centred=0):
     """Launches of the candidate recheck: three stages (candidates, exact
     values, finish) for k + 1 <= 64, plus the block kernel when some rows
-    need all their candidates; one block kernel launch otherwise."""
-    return (3, 4) if k + 1 <= 64 else (1,)
+    need all their candidates, plus (correlation) the centring of each
+    distinct set; one block kernel launch otherwise."""
+    return (3 + centred, 4 + centred) if k + 1 <= 64 else (1,)
 
 
 def _check(d, i, od, oi):
@@ -74,7 +75,8 @@ def test_knn_data_tc_vonmises(ctx, oracle, corr):
     od, oi = oracle.knn_data(x, None, 20, correlation=corr)
     _check(d, i, od, oi)
     assert st["rows_flagged"] == 0
-    assert st["launches"] - 3 in _recheck_launches(20)  # prep, BF16 split, tensor-core screen, recheck
+    # prep, BF16 split, tensor-core screen, recheck
+    assert st["launches"] - 3 in _recheck_launches(20, centred=1 if corr else 0)
 
 
 @pytest.mark.gpu
