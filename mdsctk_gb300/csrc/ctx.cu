@@ -26,7 +26,7 @@ void mds_trim_cache(mds_ctx* ctx, size_t keep) {
 }
 
 int mds_upload_chunked(mds_ctx* ctx, void* dst, const void* src, int n, size_t frame_bytes, int ev0,
-                       std::vector<int>& bounds, int* nchunks) {
+                       std::vector<int>& bounds, int* nchunks, int align) {
   if (!ctx->order_ev) {
     for (auto& cs : ctx->copy_stream) MDS_CUDA(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     for (auto& e : ctx->chunk_ev) MDS_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -35,14 +35,23 @@ int mds_upload_chunked(mds_ctx* ctx, void* dst, const void* src, int n, size_t f
   // chunks of at least 4 MiB, at most MDS_MAX_CHUNKS
   const size_t total = frame_bytes * (size_t)n;
   int c = (int)std::min<size_t>(MDS_MAX_CHUNKS, std::max<size_t>(1, total >> 22));
-  c = std::max(1, std::min(c, n));
+  align = std::max(align, 1);
+  c = std::max(1, std::min(c, n / align));
   bounds.resize(c + 1);
-  for (int i = 0; i <= c; ++i) bounds[i] = (int)((int64_t)n * i / c);
+  for (int i = 0; i <= c; ++i) bounds[i] = (i == c) ? n : (int)((int64_t)n * i / c / align * align);
+  // (bounds stay strictly increasing: consecutive ones are at least
+  // n / c >= align frames apart before rounding down to the alignment)
   // the destination may be a cached block last used by work on ctx->stream
   MDS_CUDA(ctx, cudaEventRecord(ctx->order_ev, ctx->stream));
   for (auto cs : ctx->copy_stream) MDS_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->order_ev, 0));
+  // All chunks on one copy stream, so they land in order. The host link
+  // carries ~205 GB/s whichever way the copies are issued (one or several
+  // streams, or a kernel reading the mapped host memory); with the chunks
+  // alternating between two streams, one copy engine served every chunk of
+  // one stream before any of the other's, and the first chunk landed last
+  // but one.
   for (int i = 0; i < c; ++i) {
-    cudaStream_t cs = ctx->copy_stream[i & 1];
+    cudaStream_t cs = ctx->copy_stream[0];
     const size_t off = frame_bytes * (size_t)bounds[i], bytes = frame_bytes * (size_t)(bounds[i + 1] - bounds[i]);
     MDS_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, bytes,
                                   cudaMemcpyHostToDevice, cs));

@@ -4,6 +4,8 @@
 
 #include <cuda.h>
 
+#include <vector>
+
 #include "mds_common.cuh"
 
 // Screen guards: the lower bound of RMSD^2 is the screen value minus
@@ -218,13 +220,21 @@ struct TcSkip {
 // or, for a set screened against itself (rowpiv), of every row tile
 // (nP = row tiles, rad = two radii per column tile, rrad = the row tiles').
 struct TcPivots {
-  DevBuf A, R, rad, rrad;
+  DevBuf A, R, rad, rrad, idx;
   TcOperands tc;
+  std::vector<int> hidx;  // the pivots' frame indices
   int nC = 0, nP = 0;
   bool rowpiv = false;
 };
 int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv,
                    bool rowpiv = false);
+// The same in steps, for frames prepared chunk by chunk: indices and buffers
+// (radii zeroed); the split pivot operand once pv.A / pv.R hold the pivots'
+// deviations and records; the radii of the row tiles of frames [f0, f1)
+// (row-tile pivots; f0 a multiple of a column tile).
+int tc_pivots_begin(mds_ctx* ctx, const KnnRmsPlan& pl, TcPivots& pv, bool rowpiv);
+int tc_pivots_operand(mds_ctx* ctx, const KnnRmsPlan& pl, TcPivots& pv);
+int tc_pivots_radii(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, TcPivots& pv, int f0, int f1);
 int tc_skip_rowlo(mds_ctx* ctx, const TcPivots& pv, const float* lb, int n, float* rowlo);
 // Order of the non-diagonal work items of a self screen with nseg segments,
 // estimated heaviest first (work: 3 * 1024 + row tiles * (nseg - 1) ints;
@@ -232,11 +242,18 @@ int tc_skip_rowlo(mds_ctx* ctx, const TcPivots& pv, const float* lb, int n, floa
 int tc_far_order(mds_ctx* ctx, const TcPivots& pv, const float* lb, const float* rowlo, int n, int nseg,
                  int* work, int* perm);
 int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
-                   const TcPivots& pv, float* lb, int* derr = nullptr);
+                   const TcPivots& pv, float* lb, int* derr = nullptr, int f0 = 0, int f1 = 0);
+// rt0 / nrt_items: the row tiles [rt0, rt0 + nrt_items) only (dense mode;
+// nrt_items < 0: every row tile)
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
                      int* cand_n, int* derr = nullptr, const TcSkip* skip = nullptr,
                      float* dense = nullptr, float* rowthr = nullptr, const float* nmax = nullptr,
-                     unsigned long long* ntiles = nullptr);
+                     unsigned long long* ntiles = nullptr, int rt0 = 0, int nrt_items = -1);
+// Split operands in steps: the buffer for n frames, then the rows of frames
+// [f0, f1) (f0 a multiple of a column tile; f1 too unless it is n).
+int tc_alloc(mds_ctx* ctx, const KnnRmsPlan& pl, int n, TcOperands& op, int layout);
+int tc_prepare_range(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout,
+                     int f0, int f1);
 // *out = the largest |a|^2 over the records rec[n] (a device float).
 int tc_rec_nmax(mds_ctx* ctx, const float* rec, int n, float* out);

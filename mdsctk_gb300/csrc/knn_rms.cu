@@ -1106,6 +1106,17 @@ int launch_center(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, co
   return MDS_OK;
 }
 
+// dst[t] = frame idx[t] of src (fl floats per frame); src may be page-locked
+// host memory read through its device mapping.
+__global__ void k_gather_raw(const float* __restrict__ src, const int* __restrict__ idx, int n, int fl,
+                             float* __restrict__ dst) {
+  const int t = blockIdx.x;
+  if (t >= n) return;
+  const float* a = src + (int64_t)idx[t] * fl;
+  float* b = dst + (int64_t)t * fl;
+  for (int e = threadIdx.x; e < fl; e += blockDim.x) b[e] = a[e];
+}
+
 int launch_prep(mds_ctx* ctx, const float* draw, int n, int natoms, int Ap, const float* dmass, const float* dswn,
                 float tm, const float* dmu, const double* dM0, int nofit, float* A, float* R, float* Uhl, int* bad,
                 int fbase) {
@@ -1177,8 +1188,41 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   // consumes chunk by chunk
   std::vector<int> cb_ref{0, nref}, cb_fit{0, nfit};
   int nc_ref = 1, nc_fit = 1;
+  // Staged preparation (a set screened against itself from host frames, on
+  // the tensor-core screen with tile skipping): the row-tile pivots' frames
+  // are copied first and prepared on their own, so that as each upload chunk
+  // lands its frames are superposed, split into the screen's operands, and
+  // bounded against every pivot (the pivot pass over its row tiles) while
+  // later chunks are still in flight. The kernels and results are those of
+  // the unstaged order; only the order of the work changes.
+  // (page-locked host frames only: the pivots' frames are read through the
+  // device mapping of that memory, and only such uploads overlap anyway)
+  const float* hmap = nullptr;
+  if (pl.href) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, pl.href) == cudaSuccess && pa.type == cudaMemoryTypeHost)
+      hmap = static_cast<const float*>(pa.devicePointer);
+    cudaGetLastError();
+  }
+  const bool staged = hmap && same && pl.prec != MDS_PREC_FP32 && !pl.screen_keys && !pl.noskip && !pl.full &&
+                      !pl.prep_dev && (nref + TC_FR_N - 1) / TC_FR_N >= 4;
+  TcPivots spv;
+  DevBuf praw(ctx), gidx(ctx);
+  if (staged) MDS_TRY(tc_pivots_begin(ctx, pl, spv, true));
   if (pl.href)
-    MDS_TRY(mds_upload_chunked(ctx, const_cast<float*>(draw_ref), pl.href, nref, frame_bytes, 0, cb_ref, &nc_ref));
+    MDS_TRY(mds_upload_chunked(ctx, const_cast<float*>(draw_ref), pl.href, nref, frame_bytes, 0, cb_ref, &nc_ref,
+                               staged ? TC_FR_N : 1));
+  if (staged) {
+    // the pivots' frames, and frame 0 (the template's) after them, gathered
+    // from the host frames while the chunks are in flight
+    std::vector<int> gi(spv.hidx);
+    gi.push_back(0);
+    MDS_TRY(gidx.alloc(ctx, sizeof(int) * gi.size()));
+    MDS_CUDA(ctx, cudaMemcpyAsync(gidx.p, gi.data(), sizeof(int) * gi.size(), cudaMemcpyHostToDevice, s));
+    MDS_TRY(praw.alloc(ctx, frame_bytes * gi.size()));
+    k_gather_raw<<<(int)gi.size(), 128, 0, s>>>(hmap, gidx.as<int>(), (int)gi.size(), 3 * natoms, praw.as<float>());
+    MDS_CUDA(ctx, cudaGetLastError());
+  }
   if (pl.hfit && !same)
     MDS_TRY(mds_upload_chunked(ctx, const_cast<float*>(draw_fit), pl.hfit, nfit, frame_bytes, MDS_MAX_CHUNKS,
                                cb_fit, &nc_fit));
@@ -1186,11 +1230,11 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   DevBuf Y0(ctx), E0(ctx);
   MDS_TRY(Y0.alloc(ctx, sizeof(float) * 3 * Ap));
   MDS_TRY(E0.alloc(ctx, sizeof(double)));
-  st.launches = 0;
+  st.launches = staged ? 1 : 0;  // (the pivots' gather)
   st.launches++;
-  if (pl.href) MDS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->chunk_ev[0], 0));
-  k_center<<<1, 128, 0, s>>>(draw_ref, 1, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm, Y0.as<float>(),
-                             E0.as<double>());
+  if (pl.href && !staged) MDS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->chunk_ev[0], 0));
+  k_center<<<1, 128, 0, s>>>(staged ? praw.as<float>() + (size_t)spv.nP * 3 * natoms : draw_ref, 1, natoms, Ap,
+                             dmass.as<float>(), dswn.as<float>(), tm, Y0.as<float>(), E0.as<double>());
   MDS_CUDA(ctx, cudaGetLastError());
 
   const int k = pl.k;
@@ -1230,8 +1274,40 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     }
     return MDS_OK;
   };
-  MDS_TRY(prep_chunks(draw_ref, pl.href != nullptr, cb_ref, nc_ref, 0, Ar.as<float>(), Rr.as<float>(),
-                      pl.nofit ? nullptr : Ur.as<float>(), badf.as<int>()));
+  // error words of the tensor-core launches, read at the call's
+  // synchronisation after the recheck: [0..1] the pivot pass, [2..3] the
+  // screen, then two per staged chunk's pivot pass
+  DevBuf tcerr(ctx);
+  const int nerr = 4 + 2 * MDS_MAX_CHUNKS;
+  MDS_TRY(tcerr.alloc(ctx, nerr * sizeof(int)));
+  MDS_CUDA(ctx, cudaMemsetAsync(tcerr.p, 0, nerr * sizeof(int), s));
+  TcOperands tcr, tcf;
+  DevBuf slb(ctx);  // staged: lower bounds from every frame to every pivot [nP][n]
+  if (staged) {
+    MDS_TRY(launch_prep(ctx, praw.as<float>(), spv.nP, natoms, Ap, dmass.as<float>(), dswn.as<float>(), tm,
+                        dmu.as<float>(), dM0.as<double>(), pl.nofit, spv.A.as<float>(), spv.R.as<float>(), nullptr,
+                        nullptr, 0));
+    MDS_TRY(tc_pivots_operand(ctx, pl, spv));
+    MDS_TRY(tc_alloc(ctx, pl, nref, tcr, 1));
+    MDS_TRY(tc_alloc(ctx, pl, nref, tcr, 0));
+    MDS_TRY(slb.alloc(ctx, sizeof(float) * (size_t)spv.nP * nref));
+    for (int c = 0; c < nc_ref; ++c) {
+      MDS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->chunk_ev[c], 0));
+      const int f0 = cb_ref[c], f1 = cb_ref[c + 1];
+      MDS_TRY(launch_prep(ctx, draw_ref + (size_t)f0 * 3 * natoms, f1 - f0, natoms, Ap, dmass.as<float>(),
+                          dswn.as<float>(), tm, dmu.as<float>(), dM0.as<double>(), pl.nofit,
+                          Ar.as<float>() + (size_t)f0 * 3 * Ap, Rr.as<float>() + (size_t)f0 * MDS_REC,
+                          pl.nofit ? nullptr : Ur.as<float>() + (size_t)f0 * 18, badf.as<int>(), f0));
+      MDS_TRY(tc_prepare_range(ctx, pl, Ar.as<float>(), nref, tcr, 1, f0, f1));
+      MDS_TRY(tc_prepare_range(ctx, pl, Ar.as<float>(), nref, tcr, 0, f0, f1));
+      MDS_TRY(tc_pivots_radii(ctx, pl, Ar.as<float>(), spv, f0, f1));
+      MDS_TRY(tc_skip_bounds(ctx, pl, tcr, Rr.as<float>(), nref, spv, slb.as<float>(), tcerr.as<int>() + 4 + 2 * c,
+                             f0, f1));
+    }
+  } else {
+    MDS_TRY(prep_chunks(draw_ref, pl.href != nullptr, cb_ref, nc_ref, 0, Ar.as<float>(), Rr.as<float>(),
+                        pl.nofit ? nullptr : Ur.as<float>(), badf.as<int>()));
+  }
   const float* Afp = Ar.as<float>();
   const float* Rfp = Rr.as<float>();
   if (!same) {
@@ -1270,8 +1346,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     return MDS_OK;
   }
   // tensor-core operands (split hi/lo), when that screen is selected
-  TcOperands tcr, tcf;
-  if (pl.prec != MDS_PREC_FP32) {
+  if (pl.prec != MDS_PREC_FP32 && !staged) {
     MDS_TRY(tc_prepare(ctx, pl, Ar.as<float>(), nref, tcr, 1));
     MDS_TRY(tc_prepare(ctx, pl, Afp, nfit, same ? tcr : tcf, 0));
   }
@@ -1301,11 +1376,6 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   DevBuf ntiles(ctx);             // tiles the tensor-core screen computed
   unsigned long long ht = 0;      // (read back after the recheck)
   long long dense_pairs = 0;
-  // error words of the tensor-core launches (pivot pass, screen), read at the
-  // call's synchronisation after the recheck instead of after each launch
-  DevBuf tcerr(ctx);
-  MDS_TRY(tcerr.alloc(ctx, 4 * sizeof(int)));
-  MDS_CUDA(ctx, cudaMemsetAsync(tcerr.p, 0, 4 * sizeof(int), s));
   DevBuf f_lb(ctx), f_rowlo(ctx);
   TcPivots f_pv;
   if (pl.prec == MDS_PREC_FP32) {
@@ -1355,13 +1425,17 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
     // tile skipping by the triangle inequality once there are tiles to skip
     // (a set screened against itself uses row-tile pivots)
     TcSkip sk;
-    TcPivots pv;
-    DevBuf lb(ctx), rowlo(ctx), farw(ctx), farp(ctx);
+    TcPivots upv;
+    DevBuf ulb(ctx), rowlo(ctx), farw(ctx), farp(ctx);
+    TcPivots& pv = staged ? spv : upv;  // (staged: pivots, radii and bounds made with the chunks)
+    DevBuf& lb = staged ? slb : ulb;
     const bool skipping = !pl.screen_keys && !pl.noskip && (nref + 79) / 80 >= 4;
     if (skipping) {
-      MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv, same));
-      MDS_TRY(lb.alloc(ctx, sizeof(float) * (size_t)pv.nP * nfit));
-      MDS_TRY(tc_skip_bounds(ctx, pl, same ? tcr : tcf, Rfp, nfit, pv, lb.as<float>(), tcerr.as<int>()));
+      if (!staged) {
+        MDS_TRY(tc_skip_pivots(ctx, pl, Ar.as<float>(), Rr.as<float>(), pv, same));
+        MDS_TRY(lb.alloc(ctx, sizeof(float) * (size_t)pv.nP * nfit));
+        MDS_TRY(tc_skip_bounds(ctx, pl, same ? tcr : tcf, Rfp, nfit, pv, lb.as<float>(), tcerr.as<int>()));
+      }
       sk.pivlb = lb.as<float>();
       sk.prad = pv.rad.as<float>();
       if (same) {
@@ -1391,6 +1465,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
                              rowthr.as<float>(), pl.screen_keys ? nullptr : nmax.as<float>(),
                              ntiles.as<unsigned long long>()));
     st.screen_launches = skipping ? 2 : 1;
+    // (staged: the pivot pass ran with the chunks, its time in the prep stage)
     dense_pairs = skipping ? (long long)pv.nP * nfit : 0;
   }
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
@@ -1418,7 +1493,7 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
                          cand.as<uint64_t>(), cand_n.as<int>(), nseg, segstride, Kp, k, dout_d, dout_i,
                          flagged.as<int>(), nflag.as<int>(), rowthr.p ? rowthr.as<float>() : nullptr, &audit));
   MDS_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
-  int hflag = 0, hbad[2] = {0, 0}, herr[4] = {0, 0, 0, 0};
+  int hflag = 0, hbad[2] = {0, 0}, herr[4 + 2 * MDS_MAX_CHUNKS] = {};
   unsigned long long hc[4] = {0, 0, 0, 0};
   MDS_CUDA(ctx, cudaMemcpyAsync(herr, tcerr.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
   if (ntiles.p) MDS_CUDA(ctx, cudaMemcpyAsync(&ht, ntiles.p, sizeof(ht), cudaMemcpyDeviceToHost, s));
@@ -1426,6 +1501,8 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   MDS_CUDA(ctx, cudaMemcpyAsync(hc, audit_c.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaMemcpyAsync(hbad, badf.p, sizeof(hbad), cudaMemcpyDeviceToHost, s));
   MDS_CUDA(ctx, cudaStreamSynchronize(s));
+  for (int c = 0; c < MDS_MAX_CHUNKS; ++c)
+    if (herr[4 + 2 * c] && !herr[0]) herr[0] = herr[4 + 2 * c];
   if (herr[0] || herr[2])
     return mds_fail(ctx, MDS_ERR_TIMEOUT, "tensor-core screen: a bounded wait timed out (pass %s, role %d)",
                     herr[0] ? "pivots" : "screen", herr[0] ? herr[0] : herr[2]);

@@ -83,10 +83,11 @@ template <>
 __device__ __forceinline__ unsigned short lp_bits<__half>(__half x) { return __half_as_ushort(x); }
 
 template <class T>
-__global__ void k_tc_split(const float* __restrict__ dev, int n, int Ap, int layout, int rows, float scale,
+__global__ void k_tc_split(const float* __restrict__ dev, int n, int Ap, int layout, int r0, int rows, float scale,
                            T* __restrict__ out) {
+  // operand rows [r0, rows)
   const int A8 = Ap >> 3;
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t idx = (int64_t)r0 * A8 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (int64_t)rows * A8) return;
   const int r = (int)(idx / A8), k = (int)(idx % A8) * 8;
   int frame, c;
@@ -127,24 +128,46 @@ __global__ void k_tc_split(const float* __restrict__ dev, int n, int Ap, int lay
 
 static float tc_scale(unsigned prec) { return prec == MDS_PREC_FP16X3 ? 64.0f : 1.0f; }
 
-int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout) {
-  int rows = (layout == 0) ? (n + TC_FR_M - 1) / TC_FR_M * TC_M : (n + TC_FR_N - 1) / TC_FR_N * TC_N;
+static int tc_layout_rows(int n, int layout) {
+  return (layout == 0) ? (n + TC_FR_M - 1) / TC_FR_M * TC_M : (n + TC_FR_N - 1) / TC_FR_N * TC_N;
+}
+
+int tc_alloc(mds_ctx* ctx, const KnnRmsPlan& pl, int n, TcOperands& op, int layout) {
+  const int rows = tc_layout_rows(n, layout);
   DevBuf& buf = (layout == 0) ? op.A : op.B;
   MDS_TRY(buf.alloc(ctx, (size_t)rows * 2 * pl.Ap * 2));
   if (layout == 0) op.rowsA = rows; else op.rowsB = rows;
   op.n = n;
   op.K = pl.Ap;
-  int64_t total = (int64_t)rows * (pl.Ap / 8);
-  int blocks = (int)((total + 255) / 256);
+  return MDS_OK;
+}
+
+int tc_prepare_range(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout,
+                     int f0, int f1) {
+  if (f0 % TC_FR_N || (f1 < n && f1 % TC_FR_N))
+    return mds_fail(ctx, MDS_ERR_INTERNAL, "operand range [%d, %d) not aligned to %d frames", f0, f1, TC_FR_N);
+  // a row tile of layout 0 holds TC_FR_M frames in TC_M rows, a column tile
+  // of layout 1 TC_FR_N frames in TC_N rows
+  const int r0 = (layout == 0) ? f0 / TC_FR_M * TC_M : f0 / TC_FR_N * TC_N;
+  const int r1 = tc_layout_rows(f1, layout);
+  if (r1 <= r0) return MDS_OK;
+  DevBuf& buf = (layout == 0) ? op.A : op.B;
+  const int64_t total = (int64_t)(r1 - r0) * (pl.Ap / 8);
+  const int blocks = (int)((total + 255) / 256);
   ctx->stats.launches++;
   if (pl.prec == MDS_PREC_FP16X3)
-    k_tc_split<__half><<<blocks, 256, 0, ctx->stream>>>(dev, n, pl.Ap, layout, rows, tc_scale(pl.prec),
+    k_tc_split<__half><<<blocks, 256, 0, ctx->stream>>>(dev, n, pl.Ap, layout, r0, r1, tc_scale(pl.prec),
                                                         buf.as<__half>());
   else
-    k_tc_split<__nv_bfloat16><<<blocks, 256, 0, ctx->stream>>>(dev, n, pl.Ap, layout, rows, tc_scale(pl.prec),
+    k_tc_split<__nv_bfloat16><<<blocks, 256, 0, ctx->stream>>>(dev, n, pl.Ap, layout, r0, r1, tc_scale(pl.prec),
                                                                buf.as<__nv_bfloat16>());
   MDS_CUDA(ctx, cudaGetLastError());
   return MDS_OK;
+}
+
+int tc_prepare(mds_ctx* ctx, const KnnRmsPlan& pl, const float* dev, int n, TcOperands& op, int layout) {
+  MDS_TRY(tc_alloc(ctx, pl, n, op, layout));
+  return tc_prepare_range(ctx, pl, dev, n, op, layout, 0, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -224,7 +247,7 @@ __device__ __forceinline__ void item_split(int item, int nrt, int nseg, int nct,
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             const float* __restrict__ recf, const float* __restrict__ recr, int nfit, int Nr, int Ap,
-            int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int diag,
+            int nofit, float guard, float ginv, uint32_t idesc, int Kp, int nseg, int nitems, int rt0, int diag,
             const float* __restrict__ pivlb, const float* __restrict__ prad, const float* __restrict__ rowlo,
             int piv2, const int* __restrict__ far_perm,
             float* __restrict__ dense, float* __restrict__ rowthr, const float* __restrict__ nmax, int k1,
@@ -348,6 +371,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       }
       int rt, seg;
       item_split(item, nitems / nseg, nseg, ncoltiles, diag, far_perm, rt, seg);
+      rt += rt0;
       const int t0 = (int)((int64_t)ncoltiles * seg / nseg), t1 = (int)((int64_t)ncoltiles * (seg + 1) / nseg);
       const int td = diag ? min(max((rt * TC_FR_M + TC_FR_M / 2) / TC_FR_N, t0), t1 - 1) : t0;
       uint32_t skipbits = 0;  // bit b: tile tbase + b of the current batch of 8 is skipped
@@ -517,6 +541,7 @@ k_screen_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         // start of an item: row records and this warp's rows' lists
         cur = task.x;
         item_split(cur, nitems / nseg, nseg, ncoltiles, diag, far_perm, rt, seg);
+        rt += rt0;
         grow = rt * TC_FR_M + rloc;
         rowok = (f < 10) && grow < nfit;
         ntile = 0;
@@ -764,7 +789,7 @@ int tc_seg_stride() { return TC_CAPG; }
 int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const TcOperands& ref,
                      const float* recf, const float* recr, int nfit, int Kp, int nseg, uint64_t* cand,
                      int* cand_n, int* derr, const TcSkip* skip, float* dense, float* rowthr, const float* nmax,
-                     unsigned long long* ntiles) {
+                     unsigned long long* ntiles, int rt0, int nrt_items) {
   if (Kp + 2 * TC_FR_N > TC_CAPG)
     return mds_fail(ctx, MDS_ERR_UNSUPPORTED, "tensor-core screen supports K' <= %d (k too large)",
                     TC_CAPG - 2 * TC_FR_N);
@@ -772,8 +797,11 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
   CUtensorMap mA, mB;
   MDS_TRY(encode_map(ctx, &mA, fit.A.p, fit.rowsA, pl.Ap, TC_M, pl.prec));
   MDS_TRY(encode_map(ctx, &mB, ref.B.p, ref.rowsB, pl.Ap, TC_N, pl.prec));
-  const int nrt = (nfit + TC_FR_M - 1) / TC_FR_M;
+  // row tiles [rt0, rt0 + nrt) (dense mode may take a range; else all)
+  const int nrt = (nrt_items >= 0) ? nrt_items : (nfit + TC_FR_M - 1) / TC_FR_M;
+  if (rt0 && (&fit == &ref || !dense)) return mds_fail(ctx, MDS_ERR_INTERNAL, "row-tile range outside the pivot pass");
   const int nitems = nrt * nseg;
+  if (nitems <= 0) return MDS_OK;
   const int grid = std::min(nitems, ctx->num_sms);
   const size_t smem = TC_SMEM_BYTES;
   static bool attr_set = false;  // set once: the call is also made while a stream is being captured
@@ -798,7 +826,7 @@ int launch_screen_tc(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, 
   ctx->inject &= ~MDS_INJECT_SCREEN_STALL;
   ctx->stats.launches++;
   k_screen_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(mA, mB, recf, recr, nfit, pl.nref, pl.Ap, pl.nofit,
-                                                       pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems,
+                                                       pl.guard_tc, 1.0f / (s * s), idesc, Kp, nseg, nitems, rt0,
                                                        &fit == &ref ? 1 : 0, skip ? skip->pivlb : nullptr,
                                                        skip ? skip->prad : nullptr, skip ? skip->rowlo : nullptr,
                                                        skip ? skip->piv2 : 0, skip ? skip->far_perm : nullptr,
@@ -857,54 +885,40 @@ __global__ void k_tile_radius(const float* __restrict__ A, int Nr, int Ap, const
   }
 }
 
-// Radii of a set screened against itself with row-tile pivots, in one pass
-// over its frames: block R takes row tile R (TC_FR_M frames), which lies in
-// column tile T = R / 2 with the pivots p_2T and p_2T+1 (idx). rrad[R] bounds
-// RMSD(i, p_R) over the row tile; prad[2T] and prad[2T+1] (zeroed beforehand;
-// non-negative floats order as their bits) bound the distances of the column
-// tile's frames to p_2T and p_2T+1. All rounded up as above.
+// Radii of a set screened against itself with row-tile pivots, one warp per
+// frame j of [F0, F1): j lies in row tile R = j / TC_FR_M and column tile
+// T = R / 2, with the pivots p_2T and p_2T+1 (idx). rrad[R] bounds
+// RMSD(i, p_R) over the row tile; prad[2T] and prad[2T+1] bound the
+// distances of the column tile's frames to p_2T and p_2T+1. All zeroed
+// beforehand and raised by atomicMax (non-negative floats order as their
+// bits); the rounding up as above is monotonic, so the maximum of the
+// rounded values is the rounded maximum.
 __global__ void k_tile_radius_rc(const float* __restrict__ A, int N, int Ap, const int* __restrict__ idx, int nR,
-                                 float* __restrict__ prad, float* __restrict__ rrad) {
+                                 int F0, int F1, float* __restrict__ prad, float* __restrict__ rrad) {
   static_assert(TC_FR_N == 2 * TC_FR_M, "a column tile is two row tiles");
-  __shared__ float wmax[2][8];
-  const int R = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int T = R / 2;
+  const int lane = threadIdx.x & 31;
+  const int j = F0 + (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (j >= F1 || j >= N) return;
+  const int R = j / TC_FR_M, T = R / 2;
   const bool hasb = 2 * T + 1 < nR;
   const float4* pa = reinterpret_cast<const float4*>(A + (int64_t)idx[2 * T] * 3 * Ap);
   const float4* pb = reinterpret_cast<const float4*>(A + (int64_t)idx[hasb ? 2 * T + 1 : 2 * T] * 3 * Ap);
-  float ba = 0.0f, bb = 0.0f;
-  for (int g = warp; g < TC_FR_M; g += blockDim.x >> 5) {
-    const int j = R * TC_FR_M + g;
-    if (j >= N) break;
-    const float4* aj = reinterpret_cast<const float4*>(A + (int64_t)j * 3 * Ap);
-    float ac = 0.0f, ar = 0.0f;
-    for (int q = lane; q < 3 * Ap / 4; q += 32) {
-      const float4 u = __ldg(aj + q), v = __ldg(pa + q), w = __ldg(pb + q);
-      float d0 = u.x - v.x, d1 = u.y - v.y, d2 = u.z - v.z, d3 = u.w - v.w;
-      ac = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, ac))));
-      d0 = u.x - w.x, d1 = u.y - w.y, d2 = u.z - w.z, d3 = u.w - w.w;
-      ar = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, ar))));
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      ac += __shfl_xor_sync(0xffffffffu, ac, o);
-      ar += __shfl_xor_sync(0xffffffffu, ar, o);
-    }
-    ba = fmaxf(ba, ac);
-    bb = fmaxf(bb, ar);
+  const float4* aj = reinterpret_cast<const float4*>(A + (int64_t)j * 3 * Ap);
+  float ac = 0.0f, ar = 0.0f;
+  for (int q = lane; q < 3 * Ap / 4; q += 32) {
+    const float4 u = __ldg(aj + q), v = __ldg(pa + q), w = __ldg(pb + q);
+    float d0 = u.x - v.x, d1 = u.y - v.y, d2 = u.z - v.z, d3 = u.w - v.w;
+    ac = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, ac))));
+    d0 = u.x - w.x, d1 = u.y - w.y, d2 = u.z - w.z, d3 = u.w - w.w;
+    ar = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, ar))));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ac += __shfl_xor_sync(0xffffffffu, ac, o);
+    ar += __shfl_xor_sync(0xffffffffu, ar, o);
   }
   if (lane == 0) {
-    wmax[0][warp] = ba;
-    wmax[1][warp] = bb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float ma = 0.0f, mb = 0.0f;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      ma = fmaxf(ma, wmax[0][w]);
-      mb = fmaxf(mb, wmax[1][w]);
-    }
-    const float ra = sqrtf(ma) * (1.0f + 1e-5f) + 1e-7f, rb = sqrtf(mb) * (1.0f + 1e-5f) + 1e-7f;
-    rrad[R] = (R == 2 * T) ? ra : rb;
+    const float ra = sqrtf(ac) * (1.0f + 1e-5f) + 1e-7f, rb = sqrtf(ar) * (1.0f + 1e-5f) + 1e-7f;
+    atomicMax(reinterpret_cast<int*>(rrad + R), __float_as_int(R == 2 * T ? ra : rb));
     atomicMax(reinterpret_cast<int*>(prad + 2 * T), __float_as_int(ra));
     if (hasb) atomicMax(reinterpret_cast<int*>(prad + 2 * T + 1), __float_as_int(rb));
   }
@@ -948,57 +962,91 @@ int tc_rec_nmax(mds_ctx* ctx, const float* rec, int n, float* out) {
 // against itself) the middle frame of every row tile of TC_FR_M frames
 // instead (nP = row tiles): prad[2T], prad[2T+1] bound column tile T's
 // distances to its two row pivots and rrad[R] row tile R's radius.
-int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv, bool rowpiv) {
+int tc_pivots_begin(mds_ctx* ctx, const KnnRmsPlan& pl, TcPivots& pv, bool rowpiv) {
   const int Nr = pl.nref, Ap = pl.Ap;
   const int nC = (Nr + TC_FR_N - 1) / TC_FR_N;
   const int nR = (Nr + TC_FR_M - 1) / TC_FR_M;
   const int nP = rowpiv ? nR : nC;
   cudaStream_t s = ctx->stream;
-  std::vector<int> piv(nP);
+  pv.hidx.resize(nP);
   if (rowpiv)
-    for (int R = 0; R < nR; ++R) piv[R] = R * TC_FR_M + std::min(TC_FR_M, Nr - R * TC_FR_M) / 2;
+    for (int R = 0; R < nR; ++R) pv.hidx[R] = R * TC_FR_M + std::min(TC_FR_M, Nr - R * TC_FR_M) / 2;
   else
-    for (int T = 0; T < nC; ++T) piv[T] = std::min(T * TC_FR_N + TC_FR_N / 2, Nr - 1);
-  DevBuf dpiv(ctx);
-  MDS_TRY(dpiv.alloc(ctx, sizeof(int) * nP));
+    for (int T = 0; T < nC; ++T) pv.hidx[T] = std::min(T * TC_FR_N + TC_FR_N / 2, Nr - 1);
+  MDS_TRY(pv.idx.alloc(ctx, sizeof(int) * nP));
   MDS_TRY(pv.A.alloc(ctx, sizeof(float) * 3 * Ap * (size_t)nP));
   MDS_TRY(pv.R.alloc(ctx, sizeof(float) * MDS_REC * (size_t)nP));
   MDS_TRY(pv.rad.alloc(ctx, sizeof(float) * (rowpiv ? 2 * nC : nC)));
   if (rowpiv) MDS_TRY(pv.rrad.alloc(ctx, sizeof(float) * nR));
-  MDS_CUDA(ctx, cudaMemcpyAsync(dpiv.p, piv.data(), sizeof(int) * nP, cudaMemcpyHostToDevice, s));
-  ctx->stats.launches += 2;
-  k_gather_frames<<<nP, 128, 0, s>>>(Ar, Rr, dpiv.as<int>(), nP, Ap, pv.A.as<float>(), pv.R.as<float>());
+  // (pv.hidx lives until pv is destroyed, after the stream has used it)
+  MDS_CUDA(ctx, cudaMemcpyAsync(pv.idx.p, pv.hidx.data(), sizeof(int) * nP, cudaMemcpyHostToDevice, s));
   if (rowpiv) {
     MDS_CUDA(ctx, cudaMemsetAsync(pv.rad.p, 0, sizeof(float) * 2 * nC, s));
-    k_tile_radius_rc<<<nR, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), nR, pv.rad.as<float>(), pv.rrad.as<float>());
-  } else {
-    k_tile_radius<<<nC, 256, 0, s>>>(Ar, Nr, Ap, dpiv.as<int>(), pv.rad.as<float>());
+    MDS_CUDA(ctx, cudaMemsetAsync(pv.rrad.p, 0, sizeof(float) * nR, s));
   }
-  MDS_CUDA(ctx, cudaGetLastError());
   pv.nC = nC;
   pv.nP = nP;
   pv.rowpiv = rowpiv;
-  KnnRmsPlan pp = pl;
-  pp.nref = nP;
-  MDS_TRY(tc_prepare(ctx, pp, pv.A.as<float>(), nP, pv.tc, 1));
-  // (dpiv goes back to the context's cache on return; its later users are
-  // ordered after these kernels on the same stream, and the host copy above
-  // was staged before cudaMemcpyAsync returned, so no synchronisation)
   return MDS_OK;
 }
 
-// Lower bounds of RMSD from every fit frame to every pivot (the screen in
-// dense mode over the pivots) into lb [nP][nfit]. With derr (2 ints) the call
-// does not synchronise and can be captured in a CUDA graph.
-int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
-                   const TcPivots& pv, float* lb, int* derr) {
+int tc_pivots_operand(mds_ctx* ctx, const KnnRmsPlan& pl, TcPivots& pv) {
   KnnRmsPlan pp = pl;
   pp.nref = pv.nP;
+  return tc_prepare(ctx, pp, pv.A.as<float>(), pv.nP, pv.tc, 1);
+}
+
+int tc_pivots_radii(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, TcPivots& pv, int f0, int f1) {
+  if (!pv.rowpiv) return mds_fail(ctx, MDS_ERR_INTERNAL, "radii by row-tile range need row-tile pivots");
+  // row tiles [R0, R1) hold frames [f0, f1); f0 starts a column tile, so the
+  // frames of each column tile T and its pivots 2T, 2T+1 are all in range
+  if (f0 % TC_FR_N) return mds_fail(ctx, MDS_ERR_INTERNAL, "radii range starts inside a column tile");
+  f1 = std::min(f1, pl.nref);
+  if (f1 <= f0) return MDS_OK;
+  ctx->stats.launches++;
+  k_tile_radius_rc<<<(f1 - f0 + 7) / 8, 256, 0, ctx->stream>>>(Ar, pl.nref, pl.Ap, pv.idx.as<int>(), pv.nP, f0, f1,
+                                                               pv.rad.as<float>(), pv.rrad.as<float>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  return MDS_OK;
+}
+
+int tc_skip_pivots(mds_ctx* ctx, const KnnRmsPlan& pl, const float* Ar, const float* Rr, TcPivots& pv, bool rowpiv) {
+  MDS_TRY(tc_pivots_begin(ctx, pl, pv, rowpiv));
+  cudaStream_t s = ctx->stream;
+  ctx->stats.launches++;
+  k_gather_frames<<<pv.nP, 128, 0, s>>>(Ar, Rr, pv.idx.as<int>(), pv.nP, pl.Ap, pv.A.as<float>(), pv.R.as<float>());
+  MDS_CUDA(ctx, cudaGetLastError());
+  if (rowpiv) {
+    MDS_TRY(tc_pivots_radii(ctx, pl, Ar, pv, 0, pl.nref));
+  } else {
+    ctx->stats.launches++;
+    k_tile_radius<<<pv.nC, 256, 0, s>>>(Ar, pl.nref, pl.Ap, pv.idx.as<int>(), pv.rad.as<float>());
+    MDS_CUDA(ctx, cudaGetLastError());
+  }
+  return tc_pivots_operand(ctx, pl, pv);
+}
+
+// Lower bounds of RMSD from every fit frame to every pivot (the screen in
+// dense mode over the pivots) into lb [nP][nfit]; with f1 > 0 only for the
+// fit frames [f0, f1) (f0 a multiple of the row tile). With derr (2 ints)
+// the call does not synchronise and can be captured in a CUDA graph.
+int tc_skip_bounds(mds_ctx* ctx, const KnnRmsPlan& pl, const TcOperands& fit, const float* recf, int nfit,
+                   const TcPivots& pv, float* lb, int* derr, int f0, int f1) {
+  KnnRmsPlan pp = pl;
+  pp.nref = pv.nP;
+  if (f1 <= 0) {
+    f0 = 0;
+    f1 = nfit;
+  }
+  if (f0 % TC_FR_M) return mds_fail(ctx, MDS_ERR_INTERNAL, "pivot pass range starts inside a row tile");
+  const int rt0 = f0 / TC_FR_M;
+  const int nrt = (std::min(f1, nfit) + TC_FR_M - 1) / TC_FR_M - rt0;
+  if (nrt <= 0) return MDS_OK;
   // column segments (no lists in dense mode) so that there are >= 4 items per SM
-  const int nrt = (nfit + TC_FR_M - 1) / TC_FR_M, nct = (pv.nP + TC_FR_N - 1) / TC_FR_N;
+  const int nct = (pv.nP + TC_FR_N - 1) / TC_FR_N;
   const int nseg = std::max(1, std::min(nct, (4 * ctx->num_sms + nrt - 1) / nrt));
   return launch_screen_tc(ctx, pp, fit, pv.tc, recf, pv.R.as<float>(), nfit, 32, nseg, nullptr, nullptr, derr,
-                          nullptr, lb);
+                          nullptr, lb, nullptr, nullptr, nullptr, rt0, nrt);
 }
 
 // The row-tile bounds of a set screened against itself (pivots with rowpiv,

@@ -46,14 +46,15 @@ struct mds_ctx {
 int mds_fail(mds_ctx* ctx, int code, const char* fmt, ...);
 
 // Upload n frames of `frame_bytes` each from host memory to dst in up to
-// MDS_MAX_CHUNKS chunks, alternating between the context's two copy streams
-// and ordered after the work already queued on ctx->stream. Chunk c covers
+// MDS_MAX_CHUNKS chunks, in order on the context's first copy stream and
+// ordered after the work already queued on ctx->stream. Chunk c covers
 // frames [bounds[c], bounds[c+1]) and completes event ctx->chunk_ev[ev0 + c];
 // the consumer waits on that event before reading the chunk. From pageable
 // host memory the copies are correct but do not overlap. Returns the number
-// of chunks through *nchunks.
+// of chunks through *nchunks. Inner chunk bounds are multiples of `align`
+// frames.
 int mds_upload_chunked(mds_ctx* ctx, void* dst, const void* src, int n, size_t frame_bytes, int ev0,
-                       std::vector<int>& bounds, int* nchunks);
+                       std::vector<int>& bounds, int* nchunks, int align = 1);
 
 // Free cached device blocks until at most `keep` bytes remain cached
 // (synchronises the context's stream first).

@@ -134,3 +134,22 @@ def test_knn_rms_pinned_host_frames(ctx):
     d2, i2 = ctx.knn_rms(xp, torch.from_numpy(f).pin_memory(), m, 20, precision="bf16x3")
     d3, i3 = ctx.knn_rms(x, f, m, 20, precision="bf16x3")
     assert np.array_equal(d2, d3) and np.array_equal(i2, i3)
+
+
+@pytest.mark.gpu
+def test_knn_rms_pinned_staged_chunks(ctx):
+    """Page-locked frames of a set against itself take the staged path (the
+    pivots' frames gathered first; each upload chunk superposed, split and
+    bounded against the pivots as it lands): several chunks and a partial
+    last row tile give the unstaged path's results bit for bit."""
+    import torch
+
+    x = synth.trajectory(20_017, 64, seed=15, basins=4, dwell=300.0, drift_sigma=0.05)
+    m = np.ones(64, np.float32)
+    d0, i0 = ctx.knn_rms(x, None, m, 16, precision="bf16x3")
+    assert ctx.stats()["screen_launches"] == 2
+    xp = torch.from_numpy(x).pin_memory()
+    d1, i1 = ctx.knn_rms(xp, None, m, 16, precision="bf16x3")
+    st = ctx.stats()
+    assert st["screen_launches"] == 2 and st["rows_flagged"] == 0
+    assert np.array_equal(d0, d1) and np.array_equal(i0, i1)
