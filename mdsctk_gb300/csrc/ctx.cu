@@ -50,8 +50,8 @@ int mds_upload_chunked(mds_ctx* ctx, void* dst, const void* src, int n, size_t f
   // alternating between two streams, one copy engine served every chunk of
   // one stream before any of the other's, and the first chunk landed last
   // but one.
+  cudaStream_t cs = ctx->copy_stream[0];
   for (int i = 0; i < c; ++i) {
-    cudaStream_t cs = ctx->copy_stream[0];
     const size_t off = frame_bytes * (size_t)bounds[i], bytes = frame_bytes * (size_t)(bounds[i + 1] - bounds[i]);
     MDS_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, bytes,
                                   cudaMemcpyHostToDevice, cs));

@@ -32,10 +32,10 @@ struct mds_ctx {
   mds_knn_stats stats{};
   // timing of the last call's dominant kernel (CUDA events on ctx->stream)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  // host-to-device uploads in chunks (created on first use): two copy
-  // streams, one event per chunk, one event ordering the copies after the
+  // host-to-device uploads in chunks (created on first use): a copy
+  // stream, one event per chunk, one event ordering the copies after the
   // work already queued on `stream`
-  cudaStream_t copy_stream[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream[1] = {nullptr};
   cudaEvent_t chunk_ev[MDS_MAX_CHUNKS * 2] = {};
   cudaEvent_t order_ev = nullptr;
   // mds_test_inject: faults armed for the next call that reaches them
