@@ -120,6 +120,10 @@ int mds_test_inject(mds_ctx* ctx, unsigned what);
  *            [n_fit][n_ref] = 0..n_ref-1
  *   k_used   optional: receives the clamped k
  * Entries [1..k] of the k+1 nearest are written, as the reference does.
+ * Host frames are uploaded in chunks that overlap the superposition; from
+ * page-locked (cudaHostAlloc / registered) memory the uploads run
+ * asynchronously and, for a set against itself, the screen's operands and
+ * pivot bounds are built chunk by chunk during the upload as well.
  */
 int mds_knn_rms(mds_ctx* ctx, const float* ref_xyz, int n_ref, const float* fit_xyz, int n_fit,
                 int natoms, const float* mass, int k, unsigned flags, double* out_d,
