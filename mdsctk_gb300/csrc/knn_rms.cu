@@ -1197,10 +1197,16 @@ int knn_rms_run(mds_ctx* ctx, KnnRmsPlan& pl, const float* draw_ref, const float
   // the unstaged order; only the order of the work changes.
   // (page-locked host frames only: the pivots' frames are read through the
   // device mapping of that memory, and only such uploads overlap anyway)
+  // Both ends of the frames must be page-locked host memory, mapped for the
+  // device as one range, so that the gather kernel can read any frame.
   const float* hmap = nullptr;
-  if (pl.href) {
-    cudaPointerAttributes pa;
-    if (cudaPointerGetAttributes(&pa, pl.href) == cudaSuccess && pa.type == cudaMemoryTypeHost)
+  if (pl.href && nref > 0) {
+    const size_t span = frame_bytes * (size_t)nref - 1;
+    const char* first = reinterpret_cast<const char*>(pl.href);
+    cudaPointerAttributes pa, pb;
+    if (cudaPointerGetAttributes(&pa, first) == cudaSuccess && cudaPointerGetAttributes(&pb, first + span) == cudaSuccess &&
+        pa.type == cudaMemoryTypeHost && pb.type == cudaMemoryTypeHost && pa.devicePointer &&
+        static_cast<const char*>(pb.devicePointer) == static_cast<const char*>(pa.devicePointer) + span)
       hmap = static_cast<const float*>(pa.devicePointer);
     cudaGetLastError();
   }
